@@ -1,0 +1,281 @@
+"""ctypes driver for the CPU oracle (liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, by ``__graft_entry__.smoke()`` as
+the checker and by ``bench.py``'s CPU-baseline leg.  The product library never
+imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+
+_lib = None
+
+I32P = C.POINTER(C.c_int32)
+F64P = C.POINTER(C.c_double)
+
+
+class OrcMT(C.Structure):
+    _fields_ = [("mti", C.c_int32), ("mt", C.c_uint64 * 624)]
+
+
+class OrcZig(C.Structure):
+    _fields_ = [("z", OrcMT), ("kn", C.c_int32 * 128), ("fn", C.c_double * 128), ("wn", C.c_double * 128)]
+
+
+class OrcHam(C.Structure):
+    _fields_ = [
+        ("natom", C.c_int), ("mensemble", C.c_int), ("max_no_neigh", C.c_int), ("nham", C.c_int),
+        ("nlist", I32P), ("nlistsize", I32P), ("ncoup", F64P), ("aham", I32P),
+        ("do_dm", C.c_int), ("max_no_dmneigh", C.c_int), ("dmlist", I32P), ("dmlistsize", I32P),
+        ("dm_vect", F64P), ("do_aniso", C.c_int), ("taniso", I32P), ("eaniso", F64P),
+        ("kaniso", F64P), ("sb", F64P), ("extfield", F64P),
+    ]
+
+
+class OrcLLG(C.Structure):
+    _fields_ = [
+        ("sdealgh", C.c_int), ("delta_t", C.c_double), ("bn", C.c_double), ("temprescale", C.c_double),
+        ("lambda1", F64P), ("temp", F64P), ("landeg", F64P), ("noise_mode", C.c_int),
+        ("zig", C.POINTER(OrcZig)), ("noise", F64P), ("seed", C.c_uint64), ("step", C.c_int64),
+    ]
+
+
+class OrcState(C.Structure):
+    _fields_ = [("emom", F64P), ("emom2", F64P), ("emomM", F64P), ("mmom", F64P),
+                ("b2eff", F64P), ("beff", F64P), ("ranv", F64P)]
+
+
+class OrcCumulant(C.Structure):
+    _fields_ = [("cumuw", C.c_double), ("cumutotw", C.c_double), ("avrgmcum", C.c_double),
+                ("avrgm2cum", C.c_double), ("avrgm4cum", C.c_double), ("avrgecum", C.c_double),
+                ("avrge2cum", C.c_double), ("navrgcum", C.c_int)]
+
+
+NOISE_NONE, NOISE_ZIGGURAT, NOISE_ARRAY, NOISE_PHILOX = 0, 1, 2, 3
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB):
+        build()
+    lib = C.CDLL(LIB)
+    lib.orc_mt_init.argtypes = [C.POINTER(OrcMT), C.c_int32]
+    lib.orc_mt_rand64.argtypes = [C.POINTER(OrcMT)]
+    lib.orc_mt_rand64.restype = C.c_uint64
+    lib.orc_mt_real2.argtypes = [C.POINTER(OrcMT)]
+    lib.orc_mt_real2.restype = C.c_double
+    lib.orc_mt_real1.argtypes = [C.POINTER(OrcMT)]
+    lib.orc_mt_real1.restype = C.c_double
+    lib.orc_zig_setup.argtypes = [C.POINTER(OrcZig), C.c_int32]
+    lib.orc_zig_nor.argtypes = [C.POINTER(OrcZig)]
+    lib.orc_zig_nor.restype = C.c_double
+    lib.orc_zig_fill.argtypes = [C.POINTER(OrcZig), F64P, C.c_int64]
+    lib.orc_philox4x32_10.argtypes = [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]
+    lib.orc_philox_normal3.argtypes = [C.c_uint64, C.c_int64, C.c_int32, C.c_int64, C.c_uint32, F64P]
+    lib.orc_philox_uniform4.argtypes = [C.c_uint64, C.c_int64, C.c_int32, C.c_int64, C.c_uint32, F64P]
+    lib.orc_effective_field.argtypes = [C.POINTER(OrcHam), F64P, F64P]
+    lib.orc_effective_field.restype = C.c_double
+    lib.orc_sd_step.argtypes = [C.POINTER(OrcHam), C.POINTER(OrcLLG), C.POINTER(OrcState)]
+    lib.orc_sd_step.restype = C.c_int
+    lib.orc_llg_draw_normals.argtypes = [C.POINTER(OrcLLG), C.c_int, C.c_int, F64P]
+    lib.orc_initmag_random.argtypes = [C.POINTER(OrcMT), C.c_int, C.c_int, F64P, F64P, F64P]
+    lib.orc_choose_random_atom_x.argtypes = [C.POINTER(OrcMT), C.c_int, I32P]
+    lib.orc_mc_evolve_ref.argtypes = [C.POINTER(OrcHam), C.c_char, C.c_double, C.c_double, I32P,
+                                      C.POINTER(OrcMT), C.POINTER(OrcZig), F64P, F64P, F64P, F64P]
+    lib.orc_mc_sweep_checkerboard.argtypes = [C.POINTER(OrcHam), C.c_char, C.c_double, I32P, I32P, C.c_int,
+                                              C.c_uint64, C.c_int64, F64P, F64P, F64P]
+    lib.orc_mavg.argtypes = [C.c_int, C.c_int, F64P, F64P, F64P]
+    lib.orc_energy.argtypes = [C.POINTER(OrcHam), F64P, F64P, F64P, F64P, F64P, F64P]
+    lib.orc_cumulant_update.argtypes = [C.POINTER(OrcCumulant), C.c_int, C.c_int, F64P, C.c_double, F64P, F64P]
+    lib.orc_set_threads.argtypes = [C.c_int]
+    lib.orc_get_threads.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a, t=F64P):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class Oracle:
+    """Holds one Hamiltonian and one spin state in the reference's layout."""
+
+    def __init__(self, lat, threads: int = 0):
+        self.lib = load()
+        self.lib.orc_set_threads(threads)
+        self.lat = lat
+        N, M = lat.natom, lat.mensemble
+        self._keep = []
+
+        def keep(a, dtype):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            self._keep.append(a)
+            return a
+
+        h = OrcHam()
+        h.natom, h.mensemble = N, M
+        h.max_no_neigh, h.nham = lat.max_no_neigh, lat.nham
+        h.nlist = _p(keep(lat.nlist, np.int32), I32P)
+        h.nlistsize = _p(keep(lat.nlistsize, np.int32), I32P)
+        h.ncoup = _p(keep(lat.ncoup, np.float64))
+        h.aham = _p(keep(lat.aham, np.int32), I32P)
+        h.do_dm = lat.do_dm
+        if lat.do_dm:
+            h.max_no_dmneigh = lat.dmlist.shape[1]
+            h.dmlist = _p(keep(lat.dmlist, np.int32), I32P)
+            h.dmlistsize = _p(keep(lat.dmlistsize, np.int32), I32P)
+            h.dm_vect = _p(keep(lat.dm_vect, np.float64))
+        h.do_aniso = lat.do_aniso
+        if lat.do_aniso:
+            h.taniso = _p(keep(lat.taniso, np.int32), I32P)
+            h.eaniso = _p(keep(lat.eaniso, np.float64))
+            h.kaniso = _p(keep(lat.kaniso, np.float64))
+            h.sb = _p(keep(lat.sb if lat.sb is not None else np.zeros(N), np.float64))
+        self.extfield = keep(np.broadcast_to(lat.extfield, (M, N, 3)), np.float64)
+        h.extfield = _p(self.extfield)
+        self.ham = h
+        self.mmom = keep(np.broadcast_to(lat.mmom, (M, N)), np.float64)
+        shape3 = (M, N, 3)
+        self.emom = np.zeros(shape3)
+        self.emom2 = np.zeros(shape3)
+        self.emomM = np.zeros(shape3)
+        self.beff = np.zeros(shape3)
+        self.b2eff = np.zeros(shape3)
+        self.ranv = np.zeros(shape3)
+        st = OrcState()
+        st.emom, st.emom2, st.emomM = _p(self.emom), _p(self.emom2), _p(self.emomM)
+        st.mmom, st.b2eff, st.beff, st.ranv = _p(self.mmom), _p(self.b2eff), _p(self.beff), _p(self.ranv)
+        self.state = st
+        self.zig = None
+        self.mt = None
+
+    # ---- state ----
+    def set_moments(self, emom):
+        emom = np.asarray(emom, dtype=np.float64).reshape(self.emom.shape)
+        self.emom[...] = emom
+        self.emom2[...] = emom
+        self.emomM[...] = emom * self.mmom[..., None]
+
+    def init_random(self, seed: int):
+        """initmag 1 from a fresh mtprng stream seeded with `seed` (rng_init)."""
+        self.mt = OrcMT()
+        self.lib.orc_mt_init(C.byref(self.mt), seed)
+        self.lib.orc_initmag_random(C.byref(self.mt), self.lat.natom, self.lat.mensemble, _p(self.mmom),
+                                    _p(self.emom), _p(self.emomM))
+        self.emom2[...] = self.emom
+
+    def setup_ziggurat(self, seed: int):
+        self.zig = OrcZig()
+        self.lib.orc_zig_setup(C.byref(self.zig), seed)
+
+    # ---- field / energy ----
+    def field(self):
+        e = self.lib.orc_effective_field(C.byref(self.ham), _p(self.emomM), _p(self.beff))
+        return self.beff.copy(), e
+
+    def energy(self):
+        M = self.lat.mensemble
+        out = [np.zeros(M) for _ in range(5)]
+        self.lib.orc_energy(C.byref(self.ham), _p(self.emomM), *[_p(o) for o in out])
+        return {"total": out[0], "xc": out[1], "dm": out[2], "ani": out[3], "ext": out[4]}
+
+    def mavg(self):
+        M = self.lat.mensemble
+        mv = np.zeros((M, 3))
+        ma = np.zeros(M)
+        self.lib.orc_mavg(self.lat.natom, M, _p(self.emomM), _p(mv), _p(ma))
+        return mv, ma
+
+    # ---- LLG ----
+    def make_llg(self, sdealgh, delta_t, lambda1, temp, landeg=1.0, noise_mode=NOISE_PHILOX, seed=0, bn=1.0):
+        N = self.lat.natom
+        self._lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lambda1, dtype=np.float64), (N,)))
+        self._temp = np.ascontiguousarray(np.broadcast_to(np.asarray(temp, dtype=np.float64), (N,)))
+        self._g = np.ascontiguousarray(np.broadcast_to(np.asarray(landeg, dtype=np.float64), (N,)))
+        p = OrcLLG()
+        p.sdealgh, p.delta_t, p.bn, p.temprescale = sdealgh, delta_t, bn, 1.0
+        p.lambda1, p.temp, p.landeg = _p(self._lam), _p(self._temp), _p(self._g)
+        p.noise_mode = noise_mode
+        p.seed = seed
+        p.step = 0
+        if noise_mode == NOISE_ZIGGURAT:
+            if self.zig is None:
+                raise ValueError("setup_ziggurat() first")
+            p.zig = C.pointer(self.zig)
+        self.llg = p
+        return p
+
+    def sd_step(self, noise=None):
+        if noise is not None:
+            self._noise = np.ascontiguousarray(noise, dtype=np.float64)
+            self.llg.noise = _p(self._noise)
+        rc = self.lib.orc_sd_step(C.byref(self.ham), C.byref(self.llg), C.byref(self.state))
+        if rc != 0:
+            raise RuntimeError(f"orc_sd_step failed ({rc})")
+        self.llg.step += 1
+
+    def draw_normals(self):
+        out = np.zeros(self.emom.shape)
+        self.lib.orc_llg_draw_normals(C.byref(self.llg), self.lat.natom, self.lat.mensemble, _p(out))
+        return out
+
+    # ---- MC ----
+    def mc_sweep_ref(self, mode: str, temperature: float, iflip_a):
+        if self.mt is None or self.zig is None:
+            raise ValueError("seed the uniform and ziggurat streams first")
+        return self.lib.orc_mc_evolve_ref(C.byref(self.ham), mode.encode(), temperature, 1.0,
+                                          _p(np.ascontiguousarray(iflip_a, dtype=np.int32), I32P),
+                                          C.byref(self.mt), C.byref(self.zig), _p(self.emom), _p(self.emomM),
+                                          _p(self.mmom), _p(self.beff))
+
+    def choose_random_atom_x(self):
+        out = np.zeros(self.lat.natom, dtype=np.int32)
+        self.lib.orc_choose_random_atom_x(C.byref(self.mt), self.lat.natom, _p(out, I32P))
+        return out
+
+    def mc_sweep_checkerboard(self, mode: str, temperature: float, colour_sites, colour_start, seed: int, sweep: int):
+        cs = np.ascontiguousarray(colour_sites, dtype=np.int32)
+        st = np.ascontiguousarray(colour_start, dtype=np.int32)
+        return self.lib.orc_mc_sweep_checkerboard(C.byref(self.ham), mode.encode(), temperature, _p(cs, I32P),
+                                                  _p(st, I32P), len(st) - 1, seed, sweep, _p(self.emom),
+                                                  _p(self.emomM), _p(self.mmom))
+
+
+def philox(ctr, key):
+    lib = load()
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib.orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def mt_stream(seed: int, n: int, kind: str = "real2"):
+    lib = load()
+    s = OrcMT()
+    lib.orc_mt_init(C.byref(s), seed)
+    f = {"real2": lib.orc_mt_real2, "real1": lib.orc_mt_real1, "u32": lib.orc_mt_rand64}[kind]
+    return np.array([f(C.byref(s)) for _ in range(n)])
+
+
+def ziggurat_stream(seed: int, n: int):
+    lib = load()
+    z = OrcZig()
+    lib.orc_zig_setup(C.byref(z), seed)
+    out = np.zeros(n)
+    lib.orc_zig_fill(C.byref(z), _p(out), n)
+    return out

@@ -1,0 +1,307 @@
+"""Synthetic lattices in the reference's Hamiltonian layout.
+
+The arrays built here are what UppASD's setup leaves in ``ham_t``
+(Hamiltonian/hamiltoniandatatype.f90:14-100) and the moment module:
+
+* ``nlist``      (natom, mnn)      -- Fortran ``nlist(mnn, natom)``, 1-based
+* ``nlistsize``  (nham,)
+* ``ncoup``      (nham, mnn)       -- J * 2 mRy/muB / (m_i m_j)
+  (Hamiltonian/hamiltonianinit.f90:1041-1068, lexp = 1)
+* ``dmlist``, ``dmlistsize``, ``dm_vect`` (nham, mnn_dm, 3) -- same scaling
+* ``taniso``, ``eaniso`` (natom, 3), ``kaniso`` (natom, 2) = mRy/muB * K / m^2
+  (hamiltonianinit.f90:895-909)
+* ``extfield``  (mensemble, natom, 3)
+* ``mmom``      (mensemble, natom)
+
+Every array is C-ordered with the Fortran axes reversed, so the memory image is
+exactly the Fortran column-major array and can be handed to the C ABI as is.
+Atoms are numbered like the reference: i = I0 + NA*(I1 + N1*(I2 + N2*I3))
+(System/geometry.f90:445-453), 0-based here.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Optional
+
+import numpy as np
+
+MRY = 2.179872325e-21
+MUB = 9.274009994e-24
+FC = MRY / MUB
+FC2 = 2.0 * MRY / MUB
+
+
+@dataclass
+class Lattice:
+    natom: int
+    mensemble: int
+    nlist: np.ndarray
+    nlistsize: np.ndarray
+    ncoup: np.ndarray
+    aham: np.ndarray
+    mmom: np.ndarray
+    extfield: np.ndarray
+    dmlist: Optional[np.ndarray] = None
+    dmlistsize: Optional[np.ndarray] = None
+    dm_vect: Optional[np.ndarray] = None
+    taniso: Optional[np.ndarray] = None
+    eaniso: Optional[np.ndarray] = None
+    kaniso: Optional[np.ndarray] = None
+    sb: Optional[np.ndarray] = None
+    # geometry hints for structured kernels (cells along x, y, z and basis size)
+    cells: tuple = (0, 0, 0)
+    nbasis: int = 1
+    periodic: tuple = (True, True, True)
+    # neighbour offsets per basis atom: (nbasis, mnn, 4) = (dx, dy, dz, basis_j)
+    stencil: Optional[np.ndarray] = None
+    species: Optional[np.ndarray] = None   # (natom,) chemical type, 0-based
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def max_no_neigh(self) -> int:
+        return self.nlist.shape[1]
+
+    @property
+    def nham(self) -> int:
+        return self.ncoup.shape[0]
+
+    @property
+    def do_dm(self) -> int:
+        return 1 if self.dmlist is not None else 0
+
+    @property
+    def do_aniso(self) -> int:
+        return 1 if self.taniso is not None else 0
+
+    def with_ensembles(self, mensemble: int) -> "Lattice":
+        """Same Hamiltonian, `mensemble` copies of the moment arrays."""
+        lat = Lattice(**{k: getattr(self, k) for k in self.__dataclass_fields__})
+        lat.mensemble = mensemble
+        lat.mmom = np.ascontiguousarray(np.broadcast_to(self.mmom[:1], (mensemble, self.natom)))
+        lat.extfield = np.ascontiguousarray(np.broadcast_to(self.extfield[:1], (mensemble, self.natom, 3)))
+        return lat
+
+
+def _site_index(b, x, y, z, nb, n1, n2):
+    return b + nb * (x + n1 * (y + n2 * z))
+
+
+def _build_from_stencil(cells, nbasis, periodic, stencil, coup_fn, natom):
+    """Neighbour lists from a translation-invariant stencil.
+
+    stencil: list over basis atoms of lists of (dx, dy, dz, bj, shell) tuples.
+    coup_fn(i_idx, j_idx, shell) -> coupling array (vectorised over sites).
+    Sites whose neighbour falls outside a non-periodic boundary drop it, like
+    the reference's neighbour map with vacuum boundaries.
+    """
+    n1, n2, n3 = cells
+    mnn = max(len(s) for s in stencil)
+    nlist = np.zeros((natom, mnn), dtype=np.int32)
+    nsize = np.zeros(natom, dtype=np.int32)
+    ncoup = np.zeros((natom, mnn), dtype=np.float64)
+    idx = np.arange(natom, dtype=np.int64)
+    b = idx % nbasis
+    cell = idx // nbasis
+    x = cell % n1
+    y = (cell // n1) % n2
+    z = cell // (n1 * n2)
+    for bi in range(nbasis):
+        sel = np.nonzero(b == bi)[0]
+        xs, ys, zs = x[sel], y[sel], z[sel]
+        for s, (dx, dy, dz, bj, shell) in enumerate(stencil[bi]):
+            xx, yy, zz = xs + dx, ys + dy, zs + dz
+            ok = np.ones(sel.size, dtype=bool)
+            for ax, (vv, nn, per) in enumerate(((xx, n1, periodic[0]), (yy, n2, periodic[1]), (zz, n3, periodic[2]))):
+                if per:
+                    vv %= nn
+                else:
+                    ok &= (vv >= 0) & (vv < nn)
+            j = _site_index(bj, xx, yy, zz, nbasis, n1, n2)
+            rows = sel[ok]
+            slot = nsize[rows]
+            nlist[rows, slot] = (j[ok] + 1).astype(np.int32)
+            ncoup[rows, slot] = coup_fn(rows, j[ok], shell)
+            nsize[rows] += 1
+    return nlist, nsize, ncoup
+
+
+def chain(n: int, j_mry: float, mom: float = 1.0, periodic: bool = True) -> Lattice:
+    """1D chain along z, one atom per cell (tests/Solvers and tests/HeisChain setup)."""
+    stencil = [[(0, 0, 1, 0, 1), (0, 0, -1, 0, 1)]]
+    coup = lambda i, j, sh: np.full(i.shape, j_mry * FC2 / mom / mom)
+    nlist, nsize, ncoup = _build_from_stencil((1, 1, n), 1, (False, False, periodic), stencil, coup, n)
+    return Lattice(natom=n, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=ncoup,
+                   aham=np.arange(1, n + 1, dtype=np.int32), mmom=np.full((1, n), mom),
+                   extfield=np.zeros((1, n, 3)), cells=(1, 1, n), nbasis=1,
+                   periodic=(False, False, periodic),
+                   stencil=np.array([[s[:4] for s in stencil[0]]], dtype=np.int32))
+
+
+# bcc shells in units of the conventional cell, expressed as (cell offset, basis)
+# for basis 0 at (0,0,0) and basis 1 at (1/2,1/2,1/2).
+def _bcc_shells(nshell: int):
+    out = [[], []]
+    vecs = []
+    # shell 1: (+-1/2, +-1/2, +-1/2); shell 2: (+-1,0,0); shell 3: (+-1,+-1,0); shell 4: (+-3/2,+-1/2,+-1/2)
+    half = [(sx * 0.5, sy * 0.5, sz * 0.5) for sx in (1, -1) for sy in (1, -1) for sz in (1, -1)]
+    vecs.append(half)
+    s2 = []
+    for ax in range(3):
+        for sg in (1, -1):
+            v = [0, 0, 0]
+            v[ax] = sg
+            s2.append(tuple(float(t) for t in v))
+    vecs.append(s2)
+    s3 = []
+    for a, bb in ((0, 1), (0, 2), (1, 2)):
+        for sa in (1, -1):
+            for sb_ in (1, -1):
+                v = [0, 0, 0]
+                v[a] = sa
+                v[bb] = sb_
+                s3.append(tuple(float(t) for t in v))
+    vecs.append(s3)
+    s4 = []
+    for ax in range(3):
+        for sa in (1.5, -1.5):
+            for s1 in (0.5, -0.5):
+                for s2_ in (0.5, -0.5):
+                    v = [0.0, 0.0, 0.0]
+                    v[ax] = sa
+                    others = [t for t in range(3) if t != ax]
+                    v[others[0]] = s1
+                    v[others[1]] = s2_
+                    s4.append(tuple(v))
+    vecs.append(s4)
+    for bi, off in ((0, 0.0), (1, 0.5)):
+        for sh in range(nshell):
+            for v in vecs[sh]:
+                p = (off + v[0], off + v[1], off + v[2])
+                # target basis: integer -> 0, half-integer -> 1
+                bj = 0 if abs(p[0] - round(p[0])) < 1e-9 else 1
+                o = 0.0 if bj == 0 else 0.5
+                d = tuple(int(round(p[t] - o)) for t in range(3))
+                out[bi].append((d[0], d[1], d[2], bj, sh + 1))
+    return out
+
+
+def bcc(L: int, j_shells_mry, mom: float = 2.2) -> Lattice:
+    """bcc ferromagnet, L^3 conventional cells, 2-atom basis, periodic."""
+    nsh = len(j_shells_mry)
+    st = _bcc_shells(nsh)
+    natom = 2 * L ** 3
+    coup = lambda i, j, sh: np.full(i.shape, j_shells_mry[sh - 1] * FC2 / mom / mom)
+    nlist, nsize, ncoup = _build_from_stencil((L, L, L), 2, (True, True, True), st, coup, natom)
+    return Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=ncoup,
+                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=np.full((1, natom), mom),
+                   extfield=np.zeros((1, natom, 3)), cells=(L, L, L), nbasis=2,
+                   stencil=np.array([[s[:4] for s in b] for b in st], dtype=np.int32),
+                   meta={"shells": [[s[4] for s in b] for b in st]})
+
+
+def bcc_alloy(L: int, seed: int, j_pair_mry=((1.3, 1.8), (1.8, 0.9)), decay: float = 0.5,
+              nshell: int = 4, moms=(2.2, 1.6), conc: float = 0.5) -> Lattice:
+    """Random binary alloy on bcc: species drawn from `seed`, J(shell) = J_ab * decay^(shell-1)."""
+    st = _bcc_shells(nshell)
+    natom = 2 * L ** 3
+    rng = np.random.default_rng(seed)
+    species = (rng.random(natom) >= conc).astype(np.int8)   # 0 = A, 1 = B
+    mom_of = np.asarray(moms, dtype=np.float64)[species]
+    jp = np.asarray(j_pair_mry, dtype=np.float64)
+
+    def coup(i, j, sh):
+        jv = jp[species[i], species[j]] * decay ** (sh - 1)
+        return jv * FC2 / mom_of[i] / mom_of[j]
+
+    nlist, nsize, ncoup = _build_from_stencil((L, L, L), 2, (True, True, True), st, coup, natom)
+    return Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=ncoup,
+                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=mom_of[None, :].copy(),
+                   extfield=np.zeros((1, natom, 3)), cells=(L, L, L), nbasis=2,
+                   stencil=np.array([[s[:4] for s in b] for b in st], dtype=np.int32),
+                   species=species,
+                   meta={"shells": [[s[4] for s in b] for b in st], "j_pair_mry": jp.tolist(),
+                         "decay": decay, "moms": list(moms)})
+
+
+def square_dmi(L: int, j_mry: float = 1.0, d_mry: float = 0.3, k_mry: float = -0.05,
+               bz: float = 0.5, mom: float = 1.0) -> Lattice:
+    """Square monolayer, 4 nn exchange, interfacial DMI D_ij = D (z x r_ij),
+    uniaxial anisotropy along z (energy +K (m.e)^2, so K < 0 is an easy axis),
+    Zeeman field along z.  Periodic in-plane."""
+    stencil = [[(1, 0, 0, 0, 1), (-1, 0, 0, 0, 1), (0, 1, 0, 0, 1), (0, -1, 0, 0, 1)]]
+    natom = L * L
+    coup = lambda i, j, sh: np.full(i.shape, j_mry * FC2 / mom / mom)
+    nlist, nsize, ncoup = _build_from_stencil((L, L, 1), 1, (True, True, False), stencil, coup, natom)
+    # DMI: same neighbour order; D vector = D * (z x r)
+    dm = np.zeros((natom, 4, 3))
+    for s, (dx, dy, dz, bj, sh) in enumerate(stencil[0]):
+        r = np.array([dx, dy, dz], dtype=np.float64)
+        dv = np.cross(np.array([0.0, 0.0, 1.0]), r)
+        dm[:, s, :] = dv * d_mry * FC2 / mom / mom
+    taniso = np.ones(natom, dtype=np.int32)
+    e = np.array([0.0, 0.0, 1.0])
+    eaniso = np.tile(e / np.sqrt(e @ e + 1.0e-15), (natom, 1))
+    kaniso = np.zeros((natom, 2))
+    kaniso[:, 0] = FC * k_mry / (mom * mom)
+    ext = np.zeros((1, natom, 3))
+    ext[..., 2] = bz
+    return Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=ncoup,
+                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=np.full((1, natom), mom),
+                   extfield=ext, dmlist=nlist.copy(), dmlistsize=nsize.copy(), dm_vect=dm,
+                   taniso=taniso, eaniso=eaniso, kaniso=kaniso, sb=np.zeros(natom),
+                   cells=(L, L, 1), nbasis=1, periodic=(True, True, False),
+                   stencil=np.array([[s[:4] for s in stencil[0]]], dtype=np.int32))
+
+
+def greedy_colouring(lat: Lattice):
+    """Colour sites so that no two coupled sites (exchange or DMI) share a colour.
+
+    Returns (colour_of_site, colour_sites, colour_start).  Uses the sublattice /
+    cell-parity structure first (exact for the shipped lattices) and verifies
+    it; falls back to a greedy colouring of the coupling graph.
+    """
+    n = lat.natom
+    nl = lat.nlist.astype(np.int64) - 1
+    mask = np.arange(nl.shape[1])[None, :] < lat.nlistsize[lat.aham - 1][:, None]
+    col = None
+    if lat.cells[0] > 0:
+        n1, n2, n3 = lat.cells
+        idx = np.arange(n)
+        b = idx % lat.nbasis
+        c = idx // lat.nbasis
+        x, y, z = c % n1, (c // n1) % n2, c // (n1 * n2)
+        cand = (b * 2 + ((x + y + z) % 2)).astype(np.int32)
+        if _colouring_ok(cand, nl, mask, lat):
+            col = cand
+    if col is None:
+        col = np.full(n, -1, dtype=np.int32)
+        for i in range(n):
+            used = set(col[nl[i][mask[i]]].tolist())
+            if lat.dmlist is not None:
+                dm = lat.dmlist[i][: lat.dmlistsize[lat.aham[i] - 1]] - 1
+                used |= set(col[dm].tolist())
+            cc = 0
+            while cc in used:
+                cc += 1
+            col[i] = cc
+        assert _colouring_ok(col, nl, mask, lat)
+    # compact colour ids
+    uniq = np.unique(col)
+    remap = {u: k for k, u in enumerate(uniq)}
+    col = np.array([remap[u] for u in col], dtype=np.int32) if len(uniq) < col.max() + 1 else col
+    order = np.argsort(col, kind="stable").astype(np.int32)
+    start = np.zeros(len(uniq) + 1, dtype=np.int32)
+    start[1:] = np.cumsum(np.bincount(col, minlength=len(uniq)))
+    return col, order, start
+
+
+def _colouring_ok(col, nl, mask, lat) -> bool:
+    same = (col[nl] == col[:, None]) & mask
+    if same.any():
+        return False
+    if lat.dmlist is not None:
+        dl = lat.dmlist.astype(np.int64) - 1
+        dmask = np.arange(dl.shape[1])[None, :] < lat.dmlistsize[lat.aham - 1][:, None]
+        if ((col[dl] == col[:, None]) & dmask).any():
+            return False
+    return True
