@@ -1,0 +1,355 @@
+"""Benchmark of the GB300 LLG hot path (one JSON line on stdout).
+
+Workload (default): the large plain + batched LLG configuration -- random
+binary alloy on bcc 100x100x100 conventional cells (2,000,000 atoms), A/B
+50/50 from a seed, four exchange shells J_AA/AB/BB = 1.3/1.8/0.9 mRy decaying
+0.5x per shell, moments 2.2/1.6 muB, Depondt solver, T = 300 K, 8 ensembles
+advanced together (16 M spins).  Inputs are synthetic (generated from seeds);
+the spin state (>= 384 MB) is larger than the 129 MB L2, so no L2 flush is
+needed between timed steps.
+
+A "step" is one full LLG step (field, predictor, field, corrector, moment
+update) of all 16 M spins.  `value` is atom-steps/s with the state resident in
+HBM; `e2e` is the same metric through the C ABI with the spin state copied
+from pinned host memory before, and back after, each block of `--e2e-inner`
+steps (the drop-in's measurement interval).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    "alloy2m": dict(kind="alloy", L=100, ens=8, solver=5, dt=1e-16, damping=0.1, temp=300.0,
+                    desc="bcc random binary alloy 100^3 cells (2,000,000 atoms) x 8 ensembles, 4 shells (50 nbrs), "
+                         "Depondt, T=300 K"),
+    "bcc16k": dict(kind="bcc", L=20, ens=1, solver=5, dt=1e-16, damping=0.1, temp=300.0,
+                   desc="bcc ferromagnet 20^3 cells (16,000 atoms), J1=1.3 J2=0.7 mRy, Depondt, T=300 K"),
+    "square256": dict(kind="square", L=256, ens=1, solver=1, dt=1e-16, damping=0.05, temp=50.0,
+                      desc="square monolayer 256^2, J=1.0, interfacial D=0.3, Kz=-0.05 mRy, Bz=0.5 T, midpoint, "
+                           "T=50 K"),
+}
+
+
+def build_lattice(w):
+    from uppasd_gb300 import lattice
+
+    if w["kind"] == "alloy":
+        lat = lattice.bcc_alloy(w["L"], seed=2024)
+    elif w["kind"] == "bcc":
+        lat = lattice.bcc(w["L"], [1.3, 0.7], 2.2)
+    else:
+        lat = lattice.square_dmi(w["L"], 1.0, 0.3, -0.05, 0.5, 1.0)
+    return lat.with_ensembles(w["ens"])
+
+
+def random_state(n_ens, natom, seed=7):
+    rng = np.random.default_rng(seed)
+    e = rng.normal(size=(n_ens, natom, 3))
+    e /= np.linalg.norm(e, axis=-1, keepdims=True)
+    return e
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(name):
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get(name)
+    return None
+
+
+def cpu_baseline(w, lat, e0, threads, target_s=12.0):
+    """The oracle (C restatement of the reference's Fortran) on a bounded sample:
+    one ensemble of the same lattice, steps until ~target_s of CPU work."""
+    from oracle import pyoracle as po
+
+    lat1 = lat.with_ensembles(1)
+    o = po.Oracle(lat1, threads=threads)
+    o.set_moments(e0[:1])
+    o.make_llg(w["solver"], w["dt"], w["damping"], w["temp"], 1.0, noise_mode=po.NOISE_PHILOX, seed=5)
+    t0 = time.perf_counter()
+    o.sd_step()
+    one = time.perf_counter() - t0
+    n = max(1, min(50, int(target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    for _ in range(n):
+        o.sd_step()
+    dt = time.perf_counter() - t0
+    return {"value": lat1.natom * n / dt, "unit": "atom-steps/s", "cores": o.lib.orc_get_threads(),
+            "kind": "port",
+            "sample": f"{n} steps of 1 of {lat.mensemble} ensembles ({lat1.natom} atoms), same Hamiltonian"}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return world, rank
+
+
+def dist_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def run_reference(args, w):
+    world, rank = dist_setup()
+    if rank != 0:
+        return
+    lat = build_lattice(w)
+    e0 = random_state(lat.mensemble, lat.natom)
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as po
+
+    po.build()
+    lat1 = lat.with_ensembles(1)
+    o = po.Oracle(lat1, threads=threads)
+    o.set_moments(e0[:1])
+    o.make_llg(w["solver"], w["dt"], w["damping"], w["temp"], 1.0, noise_mode=po.NOISE_PHILOX, seed=5)
+    for _ in range(args.warmup):
+        o.sd_step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.sd_step()
+    dt = time.perf_counter() - t0
+    v = lat1.natom * args.steps / dt
+    line = {"impl": "reference", "metric": "LLG atom-steps/s", "value": v, "unit": "atom-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"],
+                                            "sample_ensembles": 1, "ensembles": lat.mensemble},
+            "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} steps of 1 ensemble ({lat1.natom} atoms) per run"},
+            "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, w):
+    import torch
+
+    world, rank = dist_setup()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from uppasd_gb300 import build as b
+
+    b.build()
+    from uppasd_gb300.simulation import GpuSimulation
+
+    lat = build_lattice(w)
+    e0 = random_state(lat.mensemble, lat.natom, seed=7 + rank)
+    prec = args.precision
+    sim = None
+    if prec in ("auto", "1"):
+        try:
+            sim = GpuSimulation(lat, sdealgh=w["solver"], delta_t=w["dt"], damping=w["damping"],
+                                temperature=w["temp"], seed=1000 + rank, emom=e0, precision=1)
+            prec = "1"
+        except Exception as exc:  # structured path not applicable -> FP64 generic path
+            if args.precision == "1":
+                raise
+            print(f"# structured path unavailable ({exc}); using FP64 generic path", file=sys.stderr)
+            sim = None
+    if sim is None:
+        sim = GpuSimulation(lat, sdealgh=w["solver"], delta_t=w["dt"], damping=w["damping"],
+                            temperature=w["temp"], seed=1000 + rank, emom=e0, precision=0)
+        prec = "0"
+    stream = torch.cuda.current_stream()
+    sim.set_stream(stream.cuda_stream)
+    nspin = lat.natom * lat.mensemble
+    # warm-up (also builds and instantiates the step graph)
+    sim.evolve(max(args.warmup, 1))
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        dist_barrier(world)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        sim.evolve(args.steps)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        dist_barrier(world)
+    ms = ev0.elapsed_time(ev1)
+    ms = dist_max(ms, world)
+    value = nspin * args.steps * world / (ms * 1e-3)
+    graphs, rem = divmod(args.steps, 16)
+    per_step_launches = 2
+    launches = graphs * (16 * per_step_launches + 1) + rem * per_step_launches + (1 if rem else 0)
+    # per-kernel device time (events on the launching stream)
+    kt = sim.time_kernels(3)
+    s = 8 if prec == "0" else 8  # stored master state bytes per component
+    bytes_pred = 6 * s * nspin
+    bytes_corr = 9 * s * nspin
+    if kt["correct_ms"] >= kt["predict_ms"]:
+        dom, dom_ms, dom_bytes = "llg_correct", kt["correct_ms"], bytes_corr
+    else:
+        dom, dom_ms, dom_bytes = "llg_predict", kt["predict_ms"], bytes_pred
+    peak, peak_kind = measured_peaks()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = profiled_traffic(f"{dom}:{args.workload}:p{prec}")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": dom_bytes,
+            "step": {"achieved_GBs": (bytes_pred + bytes_corr) / (ms * 1e-3 / args.steps) / 1e9,
+                     "bytes_per_spin_step": 15 * s}}
+    # e2e through the C ABI with pinned host buffers
+    inner = args.e2e_inner
+    host = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
+    host[...] = e0
+    hout = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
+    sim.put_moments(host)
+    sim.evolve(inner)
+    sim.get_moments_into(hout) if hasattr(sim, "get_moments_into") else sim.get_moments()
+    e2e_rounds = max(1, args.e2e_rounds)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_rounds):
+        sim.put_moments(host)
+        sim.evolve(inner)
+        out = sim.get_moments()
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_val = nspin * inner * e2e_rounds * world / e2e_s
+    nbytes = host.nbytes
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(w, lat, e0, os.cpu_count() or 1)
+    sim.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "LLG atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == "0" else "f32-gather/f64-state", "data": "synthetic (seeded lattice and spins)",
+        "config": {"workload": args.workload, "description": w["desc"], "natom": lat.natom,
+                   "ensembles": lat.mensemble, "spins": nspin, "solver": "Depondt" if w["solver"] == 5 else "midpoint",
+                   "precision_path": "fp64-generic" if prec == "0" else "structured-mixed",
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
+        "roofline": roof,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "inner_steps_per_call": inner,
+                "note": "put_moments(pinned host) + sd_run(inner) + get_moments per e2e step"},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+        "kernel_ms": kt,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="alloy2m", choices=sorted(WORKLOADS))
+    ap.add_argument("--precision", default="auto", choices=["auto", "0", "1"])
+    ap.add_argument("--e2e-inner", type=int, default=10)
+    ap.add_argument("--e2e-rounds", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    w = WORKLOADS[args.workload]
+    if args.impl == "reference":
+        run_reference(args, w)
+    else:
+        run_gb300(args, w)
+
+
+if __name__ == "__main__":
+    main()

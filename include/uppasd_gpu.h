@@ -1,0 +1,131 @@
+/*
+ * uppasd_gpu.h -- C ABI of the GB300 spin-update hot path for UppASD.
+ *
+ * The Fortran drivers call these through iso_c_binding (bind(c)); every
+ * argument is a plain pointer or scalar, arrays are passed in the reference's
+ * own layout: Fortran column-major (3, Natom, Mensemble) spins, 1-based
+ * neighbour indices, couplings already scaled by the reference's setup.
+ * Every entry point returns an int status (0 = success, < 0 = error) and
+ * never exits the process; uppasd_gpu_last_error() gives the message.
+ *
+ * Reference interfaces replaced (paths relative to the UppASD source tree):
+ *   uppasd_gpu_init            <- FortranData_Initiate + fortrandata_setconstants_/
+ *                                 setmatrices_/setinputdata_ (chelper.f90:166-188,
+ *                                 gpu_files/fortranData.cpp:141-185) and
+ *                                 cudamdsim_initiateconstants_/initiatematrices_
+ *                                 (gpu_files/fort_helper.cpp:52-60)
+ *   uppasd_gpu_sd_run          <- cudamdsim_measurementphase_ step loop
+ *                                 (gpu_files/fort_helper.cpp:62-64,
+ *                                 cudaMdSimulation.cu:461-499), i.e. the
+ *                                 effective_field / evolve_first / evolve_second /
+ *                                 moment_update sequence of sd_mphase
+ *                                 (sd_driver.f90:657-767)
+ *   uppasd_gpu_get_moments     <- the measurement copy-back (cudaMeasurement.cu:108-179)
+ *   uppasd_gpu_mc_run          <- mc_evolve sweeps of mc_mphase (mc_driver.f90:309-366,
+ *                                 MonteCarlo/montecarlo.f90:44-273)
+ *   uppasd_gpu_observables     <- calc_mavrg (Measurement/measurements.f90:211-235) and
+ *                                 calc_energy (Hamiltonian/energy.f90:60-405)
+ *   uppasd_gpu_finalize        <- CudaMdSimulation teardown (cudaMdSimulation.cu:210-243)
+ */
+#ifndef UPPASD_GPU_H
+#define UPPASD_GPU_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UPPASD_GPU_OK 0
+#define UPPASD_GPU_EINVAL -1   /* bad argument or size */
+#define UPPASD_GPU_ENOMEM -2   /* device allocation failed */
+#define UPPASD_GPU_ECUDA -3    /* CUDA runtime error */
+#define UPPASD_GPU_ESTATE -4   /* call not valid in the current state */
+#define UPPASD_GPU_ENODEV -6   /* no usable sm_103 device */
+#define UPPASD_GPU_EUNSUPPORTED -7
+
+typedef struct uppasd_gpu_sim uppasd_gpu_sim;
+
+/* Scalars of fortrandata_setconstants_ (gpu_files/fortranData.cpp:67-98) that the
+ * hot path uses, plus explicit sizes and the solver / RNG selection. */
+typedef struct {
+    int32_t natom, mensemble;
+    int32_t max_no_neigh, nham;        /* ncoup is (max_no_neigh, nham) */
+    int32_t do_dm, max_no_dmneigh;
+    int32_t do_aniso;
+    int32_t sdealgh;                   /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point */
+    double delta_t, bn, temprescale;
+    uint64_t gpu_rng_seed;             /* Philox key (gpu_rng_seed keyword) */
+    int32_t gpu_rng;                   /* 0 Philox in-kernel, 1 caller-injected normals */
+    int32_t precision;                 /* 0 FP64 everywhere; 1 FP32 gather, FP64 master
+                                          (structured periodic lattices only) */
+    /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
+       0 when unknown (the structured path then stays off) */
+    int32_t n1, n2, n3, na;
+} uppasd_gpu_consts;
+
+/* Arrays of fortrandata_setmatrices_ (gpu_files/fortranData.cpp:101-130) on the hot path. */
+typedef struct {
+    const int32_t *nlist;        /* (max_no_neigh, natom), 1-based */
+    const int32_t *nlistsize;    /* (nham) */
+    const double *ncoup;         /* (max_no_neigh, nham) */
+    const int32_t *aham;         /* (natom), 1-based */
+    const int32_t *dmlist;       /* (max_no_dmneigh, natom) or NULL */
+    const int32_t *dmlistsize;   /* (nham) */
+    const double *dm_vect;       /* (3, max_no_dmneigh, nham) */
+    const int32_t *taniso;       /* (natom) or NULL */
+    const double *eaniso;        /* (3, natom) */
+    const double *kaniso;        /* (2, natom) */
+    const double *sb;            /* (natom) */
+    const double *external_field;/* (3, natom, mensemble) */
+    const double *mmom;          /* (natom, mensemble) */
+    const double *lambda1_array; /* (natom) */
+    const double *temp_array;    /* (natom) */
+    const double *landeg;        /* (natom); NULL means 1.0 (g = 2) */
+    const double *emom;          /* (3, natom, mensemble) initial unit moments */
+    const int32_t *species;      /* (natom) chemical type, 0-based, or NULL (structured path) */
+} uppasd_gpu_arrays;
+
+const char *uppasd_gpu_last_error(void);
+int uppasd_gpu_device_info(int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor, int64_t *hbm_bytes);
+
+int uppasd_gpu_init(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a, uppasd_gpu_sim **out);
+int uppasd_gpu_finalize(uppasd_gpu_sim *s);
+
+/* Spin state transfer in the reference layout (3, natom, mensemble). */
+int uppasd_gpu_put_moments(uppasd_gpu_sim *s, const double *emom);
+int uppasd_gpu_get_moments(uppasd_gpu_sim *s, double *emom, double *emomM);
+int uppasd_gpu_set_temperature(uppasd_gpu_sim *s, const double *temp_array);
+int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
+
+/* Caller-provided N(0,1) numbers for the next `nsteps` steps, laid out as
+ * nsteps consecutive (3, natom, mensemble) blocks (the order the reference's
+ * fill_rngarray draws them).  Selects gpu_rng = 1 until exhausted. */
+int uppasd_gpu_set_noise(uppasd_gpu_sim *s, const double *normals, int64_t nsteps);
+
+/* nsteps full LLG steps (field, predictor, field, corrector, moment update). */
+int uppasd_gpu_sd_run(uppasd_gpu_sim *s, int64_t nsteps);
+/* Effective field of the current state, (3, natom, mensemble). */
+int uppasd_gpu_get_field(uppasd_gpu_sim *s, double *beff);
+
+/* Monte Carlo sweeps on a colouring of the coupling graph ('M' Metropolis with
+ * Hinzke-Nowak trials, 'H' heat bath). */
+int uppasd_gpu_mc_run(uppasd_gpu_sim *s, char mode, double temperature, int64_t nsweeps);
+
+/* Per-ensemble total moment (3, mensemble), |M|/natom (mensemble) and energy per
+ * atom in mRy (mensemble); any output may be NULL. */
+int uppasd_gpu_observables(uppasd_gpu_sim *s, double *mvec, double *mabs, double *energy);
+
+/* Run the library's work on the caller's CUDA stream (a cudaStream_t passed as
+ * void*); NULL returns to the library's own stream.  Replaces the reference's
+ * two internal streams (cudaParallelizationHelper.hpp:88-175). */
+int uppasd_gpu_set_stream(uppasd_gpu_sim *s, void *cuda_stream);
+/* Profiling hook (the reference's StopwatchDeviceSync, gpu_files/stopwatchDeviceSync.hpp):
+ * advances `nrep` steps launching kernel by kernel and returns the mean device
+ * time per launch in ms, measured with CUDA events on the launching stream:
+ * ms[0] predictor kernel, ms[1] corrector kernel, ms[2] whole step. */
+int uppasd_gpu_time_kernels(uppasd_gpu_sim *s, int32_t nrep, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,649 @@
+// abi.cu -- the C ABI (include/uppasd_gpu.h): set-up, layout conversion at the
+// boundary, the step loop under a CUDA graph, and teardown.
+//
+// Ownership follows the reference's CUDA path (cudaMdSimulation.cu:133-243):
+// the caller owns every host array; init copies what the hot path needs into
+// device memory in the layout described in sim.h; get_moments copies the
+// state back in the caller's Fortran layout.  Unlike the reference, nothing
+// here exits the process: every failure returns a status code.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "sim.h"
+
+struct uppasd_gpu_sim {
+    uppasd::Sim s;
+};
+
+namespace uppasd {
+
+static thread_local std::string g_err;
+void set_error(const std::string &msg) { g_err = msg; }
+
+int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a);  // llg_stencil.cu
+int structured_step(Sim &s, int64_t step_offset, int phase);
+int structured_sync_state(Sim &s);  // master state -> s.e / s.eM
+int structured_load_state(Sim &s);  // s.e -> master state
+void structured_free(Sim &s);
+
+namespace {
+
+template <typename T>
+int dalloc(Sim &s, T **p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+        *p = nullptr;
+        return UPPASD_GPU_ENOMEM;
+    }
+    s.bytes_allocated += n * sizeof(T);
+    return UPPASD_GPU_OK;
+}
+
+template <typename T>
+int upload(Sim &s, T **p, const std::vector<T> &h) {
+    int rc = dalloc(s, p, h.size());
+    if (rc) return rc;
+    UPPASD_CUDA_TRY(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return UPPASD_GPU_OK;
+}
+
+int alloc_vec3(Sim &s, Vec3D &v, size_t n) {
+    int rc;
+    if ((rc = dalloc(s, &v.x, n)) || (rc = dalloc(s, &v.y, n)) || (rc = dalloc(s, &v.z, n))) return rc;
+    return UPPASD_GPU_OK;
+}
+
+void free_vec3(Vec3D &v) {
+    cudaFree(v.x);
+    cudaFree(v.y);
+    cudaFree(v.z);
+    v = Vec3D{};
+}
+
+__global__ void aos_to_soa(const double *aos, Vec3D e, Vec3D eM, const double *mmom, int64_t n) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    double x = aos[3 * t], y = aos[3 * t + 1], z = aos[3 * t + 2];
+    double m = mmom[t];
+    e.x[t] = x;
+    e.y[t] = y;
+    e.z[t] = z;
+    eM.x[t] = x * m;
+    eM.y[t] = y * m;
+    eM.z[t] = z * m;
+}
+
+__global__ void soa_to_aos(Vec3D v, double *aos, int64_t n) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    aos[3 * t] = v.x[t];
+    aos[3 * t + 1] = v.y[t];
+    aos[3 * t + 2] = v.z[t];
+}
+
+__global__ void advance_step(int64_t *d_step, int64_t n) { *d_step += n; }
+
+int check_device(Sim &s) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ENODEV;
+    }
+    cudaDeviceProp p;
+    e = cudaGetDeviceProperties(&p, dev);
+    if (e != cudaSuccess) {
+        set_error(std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ENODEV;
+    }
+    if (!(p.major == 10 && p.minor == 3)) {
+        char buf[160];
+        snprintf(buf, sizeof(buf), "device %d is sm_%d%d; this library is built for sm_103a (GB300) only", dev,
+                 p.major, p.minor);
+        set_error(buf);
+        return UPPASD_GPU_ENODEV;
+    }
+    s.device = dev;
+    return UPPASD_GPU_OK;
+}
+
+// Colouring of the coupling graph so that same-colour sites share no bond.
+// Tries the cell-parity x sublattice colouring first (exact for the simple
+// and bcc lattices with nearest and next-nearest shells), verifies it, and
+// falls back to greedy colouring.
+int build_colouring(Sim &s, const uppasd_gpu_consts *c, const std::vector<int32_t> &nlT,
+                    const std::vector<int32_t> &nsize, const std::vector<int32_t> &dmT,
+                    const std::vector<int32_t> &dmsize) {
+    const int N = c->natom, mnn = c->max_no_neigh, mdm = c->do_dm ? c->max_no_dmneigh : 0;
+    std::vector<int32_t> col(N, -1);
+    auto ok = [&](const std::vector<int32_t> &cc) {
+        for (int i = 0; i < N; ++i) {
+            for (int q = 0; q < nsize[i]; ++q)
+                if (cc[nlT[(size_t)q * N + i]] == cc[i]) return false;
+            for (int q = 0; mdm && q < dmsize[i]; ++q)
+                if (cc[dmT[(size_t)q * N + i]] == cc[i]) return false;
+        }
+        return true;
+    };
+    bool done = false;
+    if (c->n1 > 0 && c->n2 > 0 && c->n3 > 0 && c->na > 0 && (int64_t)c->n1 * c->n2 * c->n3 * c->na == N) {
+        std::vector<int32_t> cand(N);
+        for (int i = 0; i < N; ++i) {
+            int b = i % c->na, cell = i / c->na;
+            int x = cell % c->n1, y = (cell / c->n1) % c->n2, z = cell / (c->n1 * c->n2);
+            cand[i] = b * 2 + ((x + y + z) & 1);
+        }
+        if (ok(cand)) {
+            col = cand;
+            done = true;
+        }
+    }
+    if (!done) {
+        std::vector<char> used;
+        for (int i = 0; i < N; ++i) {
+            used.assign(used.size(), 0);
+            auto mark = [&](int j) {
+                int cj = col[j];
+                if (cj < 0) return;
+                if ((size_t)cj >= used.size()) used.resize(cj + 1, 0);
+                used[cj] = 1;
+            };
+            for (int q = 0; q < nsize[i]; ++q) mark(nlT[(size_t)q * N + i]);
+            for (int q = 0; mdm && q < dmsize[i]; ++q) mark(dmT[(size_t)q * N + i]);
+            int cc = 0;
+            while ((size_t)cc < used.size() && used[cc]) ++cc;
+            col[i] = cc;
+        }
+        if (!ok(col)) {
+            set_error("colouring failed verification");
+            return UPPASD_GPU_EINVAL;
+        }
+        (void)mnn;
+    }
+    int ncol = *std::max_element(col.begin(), col.end()) + 1;
+    std::vector<int32_t> start(ncol + 1, 0), order;
+    for (int i = 0; i < N; ++i) start[col[i] + 1]++;
+    for (int q = 0; q < ncol; ++q) start[q + 1] += start[q];
+    order.resize(N);
+    std::vector<int32_t> fill(start.begin(), start.end() - 1);
+    for (int i = 0; i < N; ++i) order[fill[col[i]]++] = i;
+    // drop empty colours
+    std::vector<int32_t> st2{0};
+    for (int q = 0; q < ncol; ++q)
+        if (start[q + 1] > start[q]) st2.push_back(start[q + 1]);
+    s.ncolour = (int)st2.size() - 1;
+    s.colour_start_h = new (std::nothrow) int32_t[st2.size()];
+    if (!s.colour_start_h) return UPPASD_GPU_ENOMEM;
+    std::copy(st2.begin(), st2.end(), s.colour_start_h);
+    return upload(s, &s.colour_sites, order);
+}
+
+int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
+    auto bad = [](const char *m) {
+        set_error(m);
+        return UPPASD_GPU_EINVAL;
+    };
+    if (!c || !a) return bad("null consts or arrays");
+    if (c->natom <= 0 || c->mensemble <= 0) return bad("natom and mensemble must be positive");
+    if ((int64_t)c->natom * c->mensemble > (int64_t)1 << 31) return bad("natom*mensemble exceeds 2^31");
+    if (c->max_no_neigh < 0 || c->nham <= 0 || c->nham > c->natom) return bad("bad max_no_neigh or nham");
+    if (!a->nlist || !a->nlistsize || !a->ncoup || !a->aham || !a->mmom || !a->lambda1_array || !a->temp_array ||
+        !a->emom || !a->external_field)
+        return bad("required array missing");
+    if (c->do_dm && (!a->dmlist || !a->dmlistsize || !a->dm_vect || c->max_no_dmneigh <= 0))
+        return bad("do_dm set but DM arrays missing");
+    if (c->do_aniso && (!a->taniso || !a->eaniso || !a->kaniso)) return bad("do_aniso set but anisotropy arrays missing");
+    if (!(c->sdealgh == 1 || c->sdealgh == 4 || c->sdealgh == 5 || c->sdealgh == 6))
+        return bad("SDEalgh must be 1, 4, 5 or 6");
+    if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
+    if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
+    if (c->precision != 0 && c->precision != 1) return bad("precision must be 0 or 1");
+    for (int i = 0; i < c->natom; ++i)
+        if (a->aham[i] < 1 || a->aham[i] > c->nham) return bad("aham out of range");
+    for (int h = 0; h < c->nham; ++h) {
+        if (a->nlistsize[h] < 0 || a->nlistsize[h] > c->max_no_neigh) return bad("nlistsize out of range");
+        if (c->do_dm && (a->dmlistsize[h] < 0 || a->dmlistsize[h] > c->max_no_dmneigh))
+            return bad("dmlistsize out of range");
+    }
+    for (int i = 0; i < c->natom; ++i) {
+        int ih = a->aham[i] - 1;
+        for (int q = 0; q < a->nlistsize[ih]; ++q) {
+            int j = a->nlist[q + (size_t)c->max_no_neigh * i];
+            if (j < 1 || j > c->natom) return bad("nlist entry out of range");
+        }
+        if (c->do_dm)
+            for (int q = 0; q < a->dmlistsize[ih]; ++q) {
+                int j = a->dmlist[q + (size_t)c->max_no_dmneigh * i];
+                if (j < 1 || j > c->natom) return bad("dmlist entry out of range");
+            }
+        if (c->do_aniso) {
+            int t = a->taniso[i];
+            if (t != 0 && t != 1 && t != 2 && t != 7) return bad("taniso must be 0, 1, 2 or 7");
+        }
+    }
+    for (int64_t t = 0; t < (int64_t)c->natom * c->mensemble; ++t)
+        if (!(a->mmom[t] > 0.0)) return bad("mmom must be positive");
+    return UPPASD_GPU_OK;
+}
+
+int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
+    int rc = validate(c, a);
+    if (rc) return rc;
+    if ((rc = check_device(s))) return rc;
+    UPPASD_CUDA_TRY(cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking));
+    const int N = c->natom, M = c->mensemble, mnn = c->max_no_neigh, nham = c->nham;
+    const size_t NM = (size_t)N * M;
+    HamDev &h = s.ham;
+    h.natom = N;
+    h.mensemble = M;
+    h.mnn = mnn;
+    h.nham = nham;
+    // neighbour lists, slot-major, 0-based, padded with the site itself
+    std::vector<int32_t> nlT((size_t)std::max(mnn, 1) * N), nsize(N), aham0(N);
+    std::vector<double> ncT((size_t)std::max(mnn, 1) * nham);
+    for (int i = 0; i < N; ++i) {
+        aham0[i] = a->aham[i] - 1;
+        nsize[i] = a->nlistsize[aham0[i]];
+        for (int q = 0; q < mnn; ++q)
+            nlT[(size_t)q * N + i] = q < nsize[i] ? a->nlist[q + (size_t)mnn * i] - 1 : i;
+    }
+    for (int ih = 0; ih < nham; ++ih)
+        for (int q = 0; q < mnn; ++q) ncT[(size_t)q * nham + ih] = a->ncoup[q + (size_t)mnn * ih];
+    if ((rc = upload(s, &h.nlist, nlT)) || (rc = upload(s, &h.nsize, nsize)) || (rc = upload(s, &h.aham, aham0)) ||
+        (rc = upload(s, &h.ncoup, ncT)))
+        return rc;
+    std::vector<int32_t> dmT, dmsize;
+    if (c->do_dm) {
+        const int mdm = c->max_no_dmneigh;
+        h.do_dm = 1;
+        h.mnn_dm = mdm;
+        dmT.resize((size_t)mdm * N);
+        dmsize.resize(N);
+        std::vector<double> dx((size_t)mdm * nham), dy(dx.size()), dz(dx.size());
+        for (int i = 0; i < N; ++i) {
+            dmsize[i] = a->dmlistsize[aham0[i]];
+            for (int q = 0; q < mdm; ++q)
+                dmT[(size_t)q * N + i] = q < dmsize[i] ? a->dmlist[q + (size_t)mdm * i] - 1 : i;
+        }
+        for (int ih = 0; ih < nham; ++ih)
+            for (int q = 0; q < mdm; ++q) {
+                const double *d = &a->dm_vect[3 * (q + (size_t)mdm * ih)];
+                dx[(size_t)q * nham + ih] = d[0];
+                dy[(size_t)q * nham + ih] = d[1];
+                dz[(size_t)q * nham + ih] = d[2];
+            }
+        if ((rc = upload(s, &h.dmlist, dmT)) || (rc = upload(s, &h.dmsize, dmsize)) || (rc = upload(s, &h.dmx, dx)) ||
+            (rc = upload(s, &h.dmy, dy)) || (rc = upload(s, &h.dmz, dz)))
+            return rc;
+    }
+    if (c->do_aniso) {
+        h.do_aniso = 1;
+        std::vector<int32_t> ta(a->taniso, a->taniso + N);
+        std::vector<double> ex(N), ey(N), ez(N), k1(N), k2(N), sb(N, 0.0);
+        for (int i = 0; i < N; ++i) {
+            ex[i] = a->eaniso[3 * (size_t)i];
+            ey[i] = a->eaniso[3 * (size_t)i + 1];
+            ez[i] = a->eaniso[3 * (size_t)i + 2];
+            k1[i] = a->kaniso[2 * (size_t)i];
+            k2[i] = a->kaniso[2 * (size_t)i + 1];
+            if (a->sb) sb[i] = a->sb[i];
+        }
+        if ((rc = upload(s, &h.taniso, ta)) || (rc = upload(s, &h.eax, ex)) || (rc = upload(s, &h.eay, ey)) ||
+            (rc = upload(s, &h.eaz, ez)) || (rc = upload(s, &h.k1, k1)) || (rc = upload(s, &h.k2, k2)) ||
+            (rc = upload(s, &h.sb, sb)))
+            return rc;
+    }
+    {
+        std::vector<double> ex(NM), ey(NM), ez(NM);
+        for (size_t t = 0; t < NM; ++t) {
+            ex[t] = a->external_field[3 * t];
+            ey[t] = a->external_field[3 * t + 1];
+            ez[t] = a->external_field[3 * t + 2];
+        }
+        if ((rc = upload(s, &h.ext.x, ex)) || (rc = upload(s, &h.ext.y, ey)) || (rc = upload(s, &h.ext.z, ez)))
+            return rc;
+    }
+    // integrator parameters
+    LlgDev &p = s.llg;
+    p.sdealgh = c->sdealgh;
+    p.delta_t = c->delta_t;
+    p.bn = c->bn;
+    p.temprescale = c->temprescale;
+    p.seed = c->gpu_rng_seed;
+    p.noise_mode = 0;
+    {
+        std::vector<double> lam(a->lambda1_array, a->lambda1_array + N), tmp(a->temp_array, a->temp_array + N);
+        std::vector<double> g(N, 1.0);
+        if (a->landeg) g.assign(a->landeg, a->landeg + N);
+        std::vector<double> mm(a->mmom, a->mmom + NM);
+        double lmin = *std::min_element(lam.begin(), lam.end());
+        p.noise_on = lmin > 1e-12 ? 1 : 0;  // evolution.f90:143 (lambdatol)
+        if ((rc = upload(s, &p.lambda, lam)) || (rc = upload(s, &p.temp, tmp)) || (rc = upload(s, &p.landeg, g)) ||
+            (rc = upload(s, &p.mmom, mm)))
+            return rc;
+        std::vector<int64_t> st(1, 0);
+        if ((rc = upload(s, &p.d_step, st))) return rc;
+    }
+    if ((rc = alloc_vec3(s, s.e, NM)) || (rc = alloc_vec3(s, s.eM, NM)) || (rc = alloc_vec3(s, s.p, NM)) ||
+        (rc = alloc_vec3(s, s.pM, NM)) || (rc = alloc_vec3(s, s.b2, NM)) || (rc = dalloc(s, &s.red, (size_t)8 * M)))
+        return rc;
+    if ((rc = build_colouring(s, c, nlT, nsize, dmT, dmsize))) return rc;
+    s.precision = c->precision;
+    if (c->precision == 1) {
+        if ((rc = structured_init(s, c, a))) return rc;
+    }
+    if ((rc = uppasd_gpu_put_moments(reinterpret_cast<uppasd_gpu_sim *>(&s), a->emom))) return rc;
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return UPPASD_GPU_OK;
+}
+
+void destroy(Sim &s) {
+    if (s.stream) cudaStreamSynchronize(s.stream);
+    if (s.graph) cudaGraphExecDestroy(s.graph);
+    structured_free(s);
+    HamDev &h = s.ham;
+    void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
+                    h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
+                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites};
+    for (void *q : ptrs) cudaFree(q);
+    free_vec3(h.ext);
+    free_vec3(s.e);
+    free_vec3(s.eM);
+    free_vec3(s.p);
+    free_vec3(s.pM);
+    free_vec3(s.b2);
+    delete[] s.colour_start_h;
+    if (s.own_stream) s.stream = s.own_stream;
+    if (s.stream) cudaStreamDestroy(s.stream);
+}
+
+int one_step(Sim &s, int64_t off, int phase = 3) {
+    return s.precision == 1 ? structured_step(s, off, phase) : llg_generic_step(s, off, phase);
+}
+
+int run_steps(Sim &s, int64_t n) {
+    const int G = 16;
+    int rc;
+    if (!s.graph && n >= G) {
+        cudaGraph_t g;
+        UPPASD_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
+        for (int j = 0; j < G; ++j)
+            if ((rc = one_step(s, j))) {
+                cudaStreamEndCapture(s.stream, &g);
+                return rc;
+            }
+        advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, G);
+        UPPASD_CUDA_TRY(cudaStreamEndCapture(s.stream, &g));
+        cudaError_t e = cudaGraphInstantiate(&s.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            s.graph = nullptr;
+            set_error(std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e));
+            return UPPASD_GPU_ECUDA;
+        }
+        s.graph_steps = G;
+    }
+    int64_t done = 0;
+    if (s.graph)
+        for (; done + s.graph_steps <= n; done += s.graph_steps) UPPASD_CUDA_TRY(cudaGraphLaunch(s.graph, s.stream));
+    int64_t rem = n - done;
+    for (int64_t j = 0; j < rem; ++j)
+        if ((rc = one_step(s, j))) return rc;
+    if (rem > 0) advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, rem);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    s.step += n;
+    return UPPASD_GPU_OK;
+}
+
+void drop_graph(Sim &s) {
+    if (s.graph) {
+        cudaStreamSynchronize(s.stream);
+        cudaGraphExecDestroy(s.graph);
+        s.graph = nullptr;
+    }
+}
+
+}  // namespace
+}  // namespace uppasd
+
+using uppasd::Sim;
+
+extern "C" {
+
+const char *uppasd_gpu_last_error(void) { return uppasd::g_err.c_str(); }
+
+int uppasd_gpu_device_info(int32_t *sm_count, int32_t *cc_major, int32_t *cc_minor, int64_t *hbm_bytes) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    cudaDeviceProp p;
+    if (e == cudaSuccess) e = cudaGetDeviceProperties(&p, dev);
+    if (e != cudaSuccess) {
+        uppasd::set_error(std::string("no CUDA device: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ENODEV;
+    }
+    if (sm_count) *sm_count = p.multiProcessorCount;
+    if (cc_major) *cc_major = p.major;
+    if (cc_minor) *cc_minor = p.minor;
+    if (hbm_bytes) *hbm_bytes = (int64_t)p.totalGlobalMem;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_init(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a, uppasd_gpu_sim **out) {
+    if (!out) {
+        uppasd::set_error("out is NULL");
+        return UPPASD_GPU_EINVAL;
+    }
+    *out = nullptr;
+    uppasd_gpu_sim *w = new (std::nothrow) uppasd_gpu_sim();
+    if (!w) {
+        uppasd::set_error("host allocation failed");
+        return UPPASD_GPU_ENOMEM;
+    }
+    int rc = uppasd::do_init(w->s, c, a);
+    if (rc) {
+        uppasd::destroy(w->s);
+        delete w;
+        return rc;
+    }
+    *out = w;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_finalize(uppasd_gpu_sim *w) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    uppasd::destroy(w->s);
+    delete w;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
+    if (!w || !emom) {
+        uppasd::set_error("null argument");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
+    double *d = nullptr;
+    UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
+    cudaError_t e = cudaMemcpyAsync(d, emom, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.stream);
+    if (e == cudaSuccess) {
+        uppasd::aos_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(d, s.e, s.eM, s.llg.mmom, n);
+        e = cudaGetLastError();
+    }
+    cudaFreeAsync(d, s.stream);
+    if (e != cudaSuccess) {
+        uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ECUDA;
+    }
+    if (s.precision == 1) return uppasd::structured_load_state(s);
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
+    if (!w) {
+        uppasd::set_error("null sim");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    int rc;
+    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
+    double *d = nullptr;
+    UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
+    cudaError_t e = cudaSuccess;
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    if (emom) {
+        uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.e, d, n);
+        e = cudaMemcpyAsync(emom, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+    }
+    if (e == cudaSuccess && emomM) {
+        uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.eM, d, n);
+        e = cudaMemcpyAsync(emomM, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+    }
+    cudaFreeAsync(d, s.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
+    if (e != cudaSuccess) {
+        uppasd::set_error(std::string("get_moments: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ECUDA;
+    }
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
+    if (!w || !temp_array) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.temp, temp_array, sizeof(double) * s.ham.natom, cudaMemcpyHostToDevice,
+                                    s.stream));
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_step(uppasd_gpu_sim *w, int64_t step) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.d_step, &step, sizeof(int64_t), cudaMemcpyHostToDevice, s.stream));
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    s.step = step;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_noise(uppasd_gpu_sim *w, const double *normals, int64_t nsteps) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    uppasd::drop_graph(s);
+    cudaFree(s.llg.inj);
+    s.llg.inj = nullptr;
+    s.llg.inj_steps = 0;
+    if (!normals || nsteps <= 0) {
+        s.llg.noise_mode = 0;
+        return UPPASD_GPU_OK;
+    }
+    const size_t n = (size_t)nsteps * 3 * s.ham.natom * s.ham.mensemble;
+    UPPASD_CUDA_TRY(cudaMalloc(&s.llg.inj, n * sizeof(double)));
+    UPPASD_CUDA_TRY(cudaMemcpy(s.llg.inj, normals, n * sizeof(double), cudaMemcpyHostToDevice));
+    s.llg.inj_steps = nsteps;
+    s.llg.inj_first = s.step;
+    s.llg.noise_mode = 1;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_sd_run(uppasd_gpu_sim *w, int64_t nsteps) {
+    if (!w || nsteps < 0) {
+        uppasd::set_error("bad arguments");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    if (s.llg.noise_mode == 1 && (s.step < s.llg.inj_first || s.step + nsteps > s.llg.inj_first + s.llg.inj_steps)) {
+        uppasd::set_error("injected noise does not cover the requested steps");
+        return UPPASD_GPU_ESTATE;
+    }
+    return uppasd::run_steps(s, nsteps);
+}
+
+int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {
+    if (!w || !beff) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    int rc;
+    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    return uppasd::field_to_host(s, beff);
+}
+
+int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t nsweeps) {
+    if (!w || nsweeps < 0 || !(temperature > 0.0) || (mode != 'M' && mode != 'H')) {
+        uppasd::set_error("mc_run: mode must be 'M' or 'H', temperature > 0, nsweeps >= 0");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    int rc;
+    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    rc = uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
+    if (rc) return rc;
+    if (s.precision == 1) return uppasd::structured_load_state(s);
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_stream(uppasd_gpu_sim *w, void *cuda_stream) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    uppasd::drop_graph(s);
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    if (!s.own_stream) s.own_stream = s.stream;
+    s.stream = cuda_stream ? (cudaStream_t)cuda_stream : s.own_stream;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_time_kernels(uppasd_gpu_sim *w, int32_t nrep, double *ms) {
+    if (!w || nrep <= 0 || !ms) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    if (s.llg.noise_mode == 1 && (s.step < s.llg.inj_first || s.step + nrep > s.llg.inj_first + s.llg.inj_steps)) {
+        uppasd::set_error("injected noise does not cover the requested steps");
+        return UPPASD_GPU_ESTATE;
+    }
+    cudaEvent_t ev[3];
+    for (auto &e : ev) UPPASD_CUDA_TRY(cudaEventCreate(&e));
+    double acc[3] = {0.0, 0.0, 0.0};
+    int rc = UPPASD_GPU_OK;
+    for (int r = 0; r < nrep && rc == UPPASD_GPU_OK; ++r) {
+        cudaEventRecord(ev[0], s.stream);
+        rc = uppasd::one_step(s, 0, 1);
+        cudaEventRecord(ev[1], s.stream);
+        if (rc == UPPASD_GPU_OK) rc = uppasd::one_step(s, 0, 2);
+        cudaEventRecord(ev[2], s.stream);
+        uppasd::advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, 1);
+        s.step += 1;
+        cudaError_t e = cudaEventSynchronize(ev[2]);
+        if (e != cudaSuccess) {
+            uppasd::set_error(std::string("time_kernels: ") + cudaGetErrorString(e));
+            rc = UPPASD_GPU_ECUDA;
+            break;
+        }
+        float a = 0.f, b = 0.f;
+        cudaEventElapsedTime(&a, ev[0], ev[1]);
+        cudaEventElapsedTime(&b, ev[1], ev[2]);
+        acc[0] += a;
+        acc[1] += b;
+        acc[2] += a + b;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int q = 0; q < 3; ++q) ms[q] = acc[q] / nrep;
+    return rc;
+}
+
+int uppasd_gpu_observables(uppasd_gpu_sim *w, double *mvec, double *mabs, double *energy) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    int rc;
+    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    return uppasd::observables(s, mvec, mabs, energy, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,90 @@
+// common.cuh -- device helpers shared by the sm_103a kernels.
+//
+// Physical constants follow Parameters/constants.f90:14-19 of the reference.
+// The counter-based RNG is Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11),
+// written here from the published round function and constants.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace uppasd {
+
+constexpr double kGama = 1.760859644e11;   // s^-1 T^-1
+constexpr double kKbolt = 1.38064852e-23;  // J/K
+constexpr double kMub = 9.274009994e-24;   // J/T
+constexpr double kMry = 2.179872325e-21;   // J
+constexpr double kPi = 3.141592653589793238462643383279502884197;
+
+// Philox streams: one per consumer so draws never collide.
+enum : uint32_t { kStreamLLG = 0u, kStreamMC = 1u, kStreamMCGauss = 2u, kStreamLearned = 3u };
+
+struct Philox4 {
+    uint32_t x, y, z, w;
+};
+
+__host__ __device__ inline Philox4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                                 uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0;
+        uint32_t n2 = hi0 ^ c3 ^ k1;
+        c0 = n0;
+        c1 = lo1;
+        c2 = n2;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return Philox4{c0, c1, c2, c3};
+}
+
+// Counter layout: (site, ensemble, step low word, step high 16 bits | stream << 16).
+__host__ __device__ inline Philox4 philox_draw(uint64_t seed, int64_t site, int32_t ens, int64_t step,
+                                               uint32_t stream) {
+    return philox4x32_10((uint32_t)site, (uint32_t)ens, (uint32_t)step,
+                         ((uint32_t)((uint64_t)step >> 32) & 0xFFFFu) | (stream << 16), (uint32_t)seed,
+                         (uint32_t)(seed >> 32));
+}
+
+__host__ __device__ inline double u01_open(uint32_t x) { return ((double)x + 0.5) * 2.3283064365386963e-10; }
+__host__ __device__ inline float u01_openf(uint32_t x) {
+    return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f;  // 24-bit grid in (0,1)
+}
+
+// Three N(0,1) draws in FP64 (Box-Muller on the four Philox words).
+__device__ inline void normal3_f64(uint64_t seed, int64_t site, int32_t ens, int64_t step, uint32_t stream,
+                                   double z[3]) {
+    Philox4 w = philox_draw(seed, site, ens, step, stream);
+    const double twopi = 2.0 * kPi;
+    double r0 = sqrt(-2.0 * log(u01_open(w.x)));
+    double t0 = twopi * u01_open(w.y);
+    double r1 = sqrt(-2.0 * log(u01_open(w.z)));
+    double t1 = twopi * u01_open(w.w);
+    z[0] = r0 * cos(t0);
+    z[1] = r0 * sin(t0);
+    z[2] = r1 * cos(t1);
+}
+
+// Three N(0,1) draws in FP32.
+__device__ inline void normal3_f32(uint64_t seed, int64_t site, int32_t ens, int64_t step, uint32_t stream,
+                                   float z[3]) {
+    Philox4 w = philox_draw(seed, site, ens, step, stream);
+    float r0 = sqrtf(-2.0f * __logf(u01_openf(w.x)));
+    float r1 = sqrtf(-2.0f * __logf(u01_openf(w.z)));
+    float s0, c0, s1, c1;
+    sincospif(2.0f * u01_openf(w.y), &s0, &c0);
+    sincospif(2.0f * u01_openf(w.w), &s1, &c1);
+    z[0] = r0 * c0;
+    z[1] = r0 * s0;
+    z[2] = r1 * c1;
+}
+
+}  // namespace uppasd

@@ -1,0 +1,100 @@
+// sim.h -- internal state of one simulation (one Hamiltonian, Mensemble spin
+// replicas) on one GB300.  Not part of the public C ABI (include/uppasd_gpu.h).
+//
+// HBM layout (all device arrays, ensemble-major structure of arrays):
+//   spin component c of site i in ensemble k lives at  c_array[k * natom + i];
+//   x, y, z are separate arrays so a warp's loads of one component coalesce.
+//   The reference's Fortran (3, natom, mensemble) AoS arrays are converted at
+//   the boundary by the transpose kernels in abi.cu.
+//   Neighbour lists are stored slot-major ("transposed ELL"): slot s of site i
+//   at nlist[s * natom + i], 0-based, so consecutive sites read consecutive words.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <string>
+
+#include "../../include/uppasd_gpu.h"
+
+namespace uppasd {
+
+struct Vec3D {
+    double *x = nullptr, *y = nullptr, *z = nullptr;
+};
+
+struct HamDev {
+    int natom = 0, mensemble = 0, mnn = 0, nham = 0;
+    int32_t *nlist = nullptr;   // [mnn][natom] 0-based
+    int32_t *nsize = nullptr;   // [natom] = nlistsize(aham(i))
+    int32_t *aham = nullptr;    // [natom] 0-based
+    double *ncoup = nullptr;    // [mnn][nham]
+    int do_dm = 0, mnn_dm = 0;
+    int32_t *dmlist = nullptr;  // [mnn_dm][natom]
+    int32_t *dmsize = nullptr;  // [natom]
+    double *dmx = nullptr, *dmy = nullptr, *dmz = nullptr;  // [mnn_dm][nham]
+    int do_aniso = 0;
+    int32_t *taniso = nullptr;  // [natom]
+    double *eax = nullptr, *eay = nullptr, *eaz = nullptr;  // [natom]
+    double *k1 = nullptr, *k2 = nullptr, *sb = nullptr;     // [natom]
+    Vec3D ext;                  // [mensemble][natom]
+};
+
+struct LlgDev {
+    int sdealgh = 5;
+    double delta_t = 1e-16, bn = 1.0, temprescale = 1.0;
+    double *lambda = nullptr, *temp = nullptr, *landeg = nullptr;  // [natom]
+    double *mmom = nullptr;  // [mensemble][natom]
+    uint64_t seed = 0;
+    int noise_mode = 0;            // 0 Philox, 1 injected normals, 2 none
+    int noise_on = 1;              // midpoint/SIB draw noise only when min(lambda) > 1e-12
+    double *inj = nullptr;         // injected N(0,1): [nsteps][3][mensemble][natom]
+    int64_t inj_steps = 0, inj_first = 0;
+    int64_t *d_step = nullptr;     // device step counter (read by kernels, advanced in-stream)
+};
+
+struct StructuredFast;  // mixed-precision structured-lattice path (llg_stencil.cu)
+
+struct Sim {
+    HamDev ham;
+    LlgDev llg;
+    Vec3D e, eM;        // state at t: unit vectors and full moments
+    Vec3D p, pM;        // predictor / midpoint estimate
+    Vec3D b2;           // Depondt b2eff / Heun field at t
+    int64_t step = 0;   // host mirror of the step counter
+    cudaStream_t stream = nullptr;      // stream all work is issued on
+    cudaStream_t own_stream = nullptr;  // the library's stream while a caller's stream is set
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    int device = 0;
+    int precision = 0;  // 0 FP64 generic, 1 structured mixed precision
+    StructuredFast *fast = nullptr;
+    // MC
+    int ncolour = 0;
+    int32_t *colour_sites = nullptr;   // sites listed colour by colour
+    int32_t *colour_start_h = nullptr; // host copy, ncolour+1
+    int64_t mc_sweep = 0;
+    // scratch for observables
+    double *red = nullptr;             // [mensemble][8]
+    size_t bytes_allocated = 0;
+};
+
+// llg_generic.cu
+// phase: 1 predictor only, 2 corrector only, 3 both
+int llg_generic_step(Sim &s, int64_t step_offset, int phase = 3);
+// observables.cu
+int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src);
+int field_to_host(Sim &s, double *beff_h);
+// mc.cu
+int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps);
+
+void set_error(const std::string &msg);
+
+#define UPPASD_CUDA_TRY(expr)                                                              \
+    do {                                                                                   \
+        cudaError_t _e = (expr);                                                           \
+        if (_e != cudaSuccess) {                                                           \
+            ::uppasd::set_error(std::string(#expr) + ": " + cudaGetErrorString(_e));       \
+            return UPPASD_GPU_ECUDA;                                                       \
+        }                                                                                  \
+    } while (0)
+
+}  // namespace uppasd

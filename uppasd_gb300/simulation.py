@@ -1,0 +1,173 @@
+"""Host-side mirror of the reference's interface to the spin-update hot path.
+
+``GpuSimulation`` plays the role of the reference's ``CudaMdSimulation``
+(gpu_files/cudaMdSimulation.cu) behind the Fortran driver, and exposes the
+calls the reference's Python layer makes (uppasd/simulator.py:
+``get_moments``, ``put_moments``, ``get_fields``, ``relax``, ``evolve``) on top
+of the C ABI in include/uppasd_gpu.h.  Arrays cross the boundary in the
+reference's layout: (mensemble, natom, 3) C-ordered, i.e. Fortran
+(3, natom, mensemble).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _lib
+from .lattice import Lattice
+
+SOLVERS = {"midpoint": 1, "heun": 4, "depondt": 5, "sib": 6}
+
+
+def _ptr(a, t=_lib.F64P):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+class GpuSimulation:
+    """One Hamiltonian and `mensemble` spin replicas resident on the GPU."""
+
+    def __init__(self, lat: Lattice, sdealgh: int = 5, delta_t: float = 1e-16, damping=0.1,
+                 temperature=0.0, landeg=1.0, seed: int = 1, emom: Optional[np.ndarray] = None,
+                 precision: int = 0, gpu_rng: int = 0, bn: float = 1.0):
+        if isinstance(sdealgh, str):
+            sdealgh = SOLVERS[sdealgh]
+        self.lat = lat
+        N, M = lat.natom, lat.mensemble
+        self._keep = []
+
+        def keep(a, dtype):
+            a = np.ascontiguousarray(a, dtype=dtype)
+            self._keep.append(a)
+            return a
+
+        c = _lib.Consts()
+        c.natom, c.mensemble = N, M
+        c.max_no_neigh, c.nham = lat.max_no_neigh, lat.nham
+        c.do_dm = lat.do_dm
+        c.max_no_dmneigh = lat.dmlist.shape[1] if lat.do_dm else 0
+        c.do_aniso = lat.do_aniso
+        c.sdealgh = int(sdealgh)
+        c.delta_t, c.bn, c.temprescale = float(delta_t), float(bn), 1.0
+        c.gpu_rng_seed = int(seed)
+        c.gpu_rng = int(gpu_rng)
+        c.precision = int(precision)
+        if lat.cells[0] > 0:
+            c.n1, c.n2, c.n3 = lat.cells
+            c.na = lat.nbasis
+        a = _lib.Arrays()
+        a.nlist = _ptr(keep(lat.nlist, np.int32), _lib.I32P)
+        a.nlistsize = _ptr(keep(lat.nlistsize, np.int32), _lib.I32P)
+        a.ncoup = _ptr(keep(lat.ncoup, np.float64))
+        a.aham = _ptr(keep(lat.aham, np.int32), _lib.I32P)
+        if lat.do_dm:
+            a.dmlist = _ptr(keep(lat.dmlist, np.int32), _lib.I32P)
+            a.dmlistsize = _ptr(keep(lat.dmlistsize, np.int32), _lib.I32P)
+            a.dm_vect = _ptr(keep(lat.dm_vect, np.float64))
+        if lat.do_aniso:
+            a.taniso = _ptr(keep(lat.taniso, np.int32), _lib.I32P)
+            a.eaniso = _ptr(keep(lat.eaniso, np.float64))
+            a.kaniso = _ptr(keep(lat.kaniso, np.float64))
+            a.sb = _ptr(keep(lat.sb if lat.sb is not None else np.zeros(N), np.float64))
+        a.external_field = _ptr(keep(np.broadcast_to(lat.extfield, (M, N, 3)), np.float64))
+        self.mmom = keep(np.broadcast_to(lat.mmom, (M, N)), np.float64)
+        a.mmom = _ptr(self.mmom)
+        a.lambda1_array = _ptr(keep(np.broadcast_to(np.asarray(damping, float), (N,)), np.float64))
+        a.temp_array = _ptr(keep(np.broadcast_to(np.asarray(temperature, float), (N,)), np.float64))
+        a.landeg = _ptr(keep(np.broadcast_to(np.asarray(landeg, float), (N,)), np.float64))
+        if emom is None:
+            emom = np.zeros((M, N, 3))
+            emom[..., 2] = 1.0
+        a.emom = _ptr(keep(np.broadcast_to(emom, (M, N, 3)), np.float64))
+        if lat.species is not None:
+            a.species = _ptr(keep(lat.species, np.int32), _lib.I32P)
+        h = C.c_void_p()
+        _lib.call("uppasd_gpu_init", C.byref(c), C.byref(a), C.byref(h))
+        self._h = h
+        self._keep = []  # init copied everything it needs
+
+    # -- lifecycle --
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.call("uppasd_gpu_finalize", self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- state (uppasd/simulator.py get_moments / put_moments / get_fields) --
+    def put_moments(self, emom):
+        e = np.ascontiguousarray(np.broadcast_to(emom, (self.lat.mensemble, self.lat.natom, 3)), dtype=np.float64)
+        _lib.call("uppasd_gpu_put_moments", self._h, _ptr(e))
+
+    def get_moments(self, full: bool = False):
+        shape = (self.lat.mensemble, self.lat.natom, 3)
+        e = np.empty(shape)
+        em = np.empty(shape) if full else None
+        _lib.call("uppasd_gpu_get_moments", self._h, _ptr(e), _ptr(em))
+        return (e, em) if full else e
+
+    def get_fields(self):
+        b = np.empty((self.lat.mensemble, self.lat.natom, 3))
+        _lib.call("uppasd_gpu_get_field", self._h, _ptr(b))
+        return b
+
+    def set_temperature(self, temperature):
+        t = np.ascontiguousarray(np.broadcast_to(np.asarray(temperature, float), (self.lat.natom,)))
+        _lib.call("uppasd_gpu_set_temperature", self._h, _ptr(t))
+
+    def set_step(self, step: int):
+        _lib.call("uppasd_gpu_set_step", self._h, int(step))
+
+    def set_noise(self, normals: Optional[np.ndarray]):
+        """Inject N(0,1) numbers, shape (nsteps, mensemble, natom, 3) (reference draw order)."""
+        if normals is None:
+            _lib.call("uppasd_gpu_set_noise", self._h, None, 0)
+            return
+        n = np.ascontiguousarray(normals, dtype=np.float64)
+        _lib.call("uppasd_gpu_set_noise", self._h, _ptr(n), n.shape[0])
+
+    # -- dynamics (sd_mphase) and Monte Carlo (mc_mphase) --
+    def evolve(self, nsteps: int):
+        _lib.call("uppasd_gpu_sd_run", self._h, int(nsteps))
+
+    def relax(self, mode: str = "H", temperature: float = 1.0, nsweeps: int = 1):
+        """Monte Carlo sweeps: mode 'M' (Metropolis) or 'H' (heat bath)."""
+        _lib.call("uppasd_gpu_mc_run", self._h, mode.encode()[:1], float(temperature), int(nsweeps))
+
+    def set_stream(self, cuda_stream_handle: int):
+        """Issue all work on the caller's CUDA stream (0 = the library's own)."""
+        _lib.call("uppasd_gpu_set_stream", self._h, C.c_void_p(cuda_stream_handle or None))
+
+    def time_kernels(self, nrep: int = 5):
+        """Mean device ms per launch: predictor, corrector, whole step (advances nrep steps)."""
+        ms = np.zeros(3)
+        _lib.call("uppasd_gpu_time_kernels", self._h, int(nrep), _ptr(ms))
+        return {"predict_ms": ms[0], "correct_ms": ms[1], "step_ms": ms[2]}
+
+    def observables(self):
+        M = self.lat.mensemble
+        mv = np.empty((M, 3))
+        ma = np.empty(M)
+        en = np.empty(M)
+        _lib.call("uppasd_gpu_observables", self._h, _ptr(mv), _ptr(ma), _ptr(en))
+        return {"mvec": mv, "mabs": ma, "energy": en}
+
+
+def device_info():
+    sm = C.c_int32()
+    ma = C.c_int32()
+    mi = C.c_int32()
+    mem = C.c_int64()
+    _lib.call("uppasd_gpu_device_info", C.byref(sm), C.byref(ma), C.byref(mi), C.byref(mem))
+    return {"sm_count": sm.value, "cc": (ma.value, mi.value), "hbm_bytes": mem.value}
