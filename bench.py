@@ -218,6 +218,49 @@ def run_reference(args, w):
     print(json.dumps(line), flush=True)
 
 
+def _make_sim(lat, w, prec, seed, e0):
+    from uppasd_gb300.simulation import GpuSimulation
+
+    return GpuSimulation(lat, sdealgh=w["solver"], delta_t=w["dt"], damping=w["damping"], temperature=w["temp"],
+                         seed=seed, emom=e0, precision=prec)
+
+
+def _time_steps(sim, stream, steps, warmup, world):
+    import torch
+
+    sim.evolve(max(warmup, 1))  # warm-up; also captures and instantiates the step graph
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    sim.evolve(steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    return dist_max(ev0.elapsed_time(ev1), world)
+
+
+def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic):
+    bytes_pred = 6 * s_bytes * nspin
+    bytes_corr = 9 * s_bytes * nspin
+    if kt["correct_ms"] >= kt["predict_ms"]:
+        dom, dom_ms, dom_bytes = "correct", kt["correct_ms"], bytes_corr
+    else:
+        dom, dom_ms, dom_bytes = "predict", kt["predict_ms"], bytes_pred
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "kernel": dom, "peak_source": peak_kind, "algorithmic_bytes_per_launch": dom_bytes,
+            "step": {"achieved_GBs": (bytes_pred + bytes_corr) / (ms_step * 1e-3) / 1e9,
+                     "frac": (bytes_pred + bytes_corr) / (ms_step * 1e-3) / 1e9 / peak,
+                     "bytes_per_spin_step": 15 * s_bytes}}
+
+
+PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master"}
+KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_predict", "stencil_correct"),
+                2: ("stencil_predict", "stencil_correct")}
+
+
 def run_gb300(args, w):
     import torch
 
@@ -226,106 +269,90 @@ def run_gb300(args, w):
     from uppasd_gb300 import build as b
 
     b.build()
-    from uppasd_gb300.simulation import GpuSimulation
-
     lat = build_lattice(w)
     e0 = random_state(lat.mensemble, lat.natom, seed=7 + rank)
-    prec = args.precision
-    sim = None
-    if prec in ("auto", "1"):
-        try:
-            sim = GpuSimulation(lat, sdealgh=w["solver"], delta_t=w["dt"], damping=w["damping"],
-                                temperature=w["temp"], seed=1000 + rank, emom=e0, precision=1)
-            prec = "1"
-        except Exception as exc:  # structured path not applicable -> FP64 generic path
-            if args.precision == "1":
-                raise
-            print(f"# structured path unavailable ({exc}); using FP64 generic path", file=sys.stderr)
-            sim = None
-    if sim is None:
-        sim = GpuSimulation(lat, sdealgh=w["solver"], delta_t=w["dt"], damping=w["damping"],
-                            temperature=w["temp"], seed=1000 + rank, emom=e0, precision=0)
-        prec = "0"
-    stream = torch.cuda.current_stream()
-    sim.set_stream(stream.cuda_stream)
     nspin = lat.natom * lat.mensemble
-    # warm-up (also builds and instantiates the step graph)
-    sim.evolve(max(args.warmup, 1))
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    order = [int(args.precision)] if args.precision != "auto" else [1, 0]
+    sim, prec = None, None
+    for p in order:
+        try:
+            sim = _make_sim(lat, w, p, 1000 + rank, e0)
+            prec = p
+            break
+        except Exception as exc:
+            print(f"# precision {p} unavailable ({exc})", file=sys.stderr)
+    if sim is None:
+        raise SystemExit("no GPU path could be set up")
+    # a dedicated (non-default) stream: the library issues all work on it and the
+    # CUDA events are recorded on the same stream
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    sim.set_stream(stream.cuda_stream)
     with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
-        dist_barrier(world)
-        torch.cuda.synchronize()
-        ev0.record(stream)
-        sim.evolve(args.steps)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        dist_barrier(world)
-    ms = ev0.elapsed_time(ev1)
-    ms = dist_max(ms, world)
+        ms = _time_steps(sim, stream, args.steps, args.warmup, world)
     value = nspin * args.steps * world / (ms * 1e-3)
     graphs, rem = divmod(args.steps, 16)
-    per_step_launches = 2
-    launches = graphs * (16 * per_step_launches + 1) + rem * per_step_launches + (1 if rem else 0)
-    # per-kernel device time (events on the launching stream)
+    launches = graphs * (16 * 2 + 1) + rem * 2 + (1 if rem else 0)
     kt = sim.time_kernels(3)
-    s = 8 if prec == "0" else 8  # stored master state bytes per component
-    bytes_pred = 6 * s * nspin
-    bytes_corr = 9 * s * nspin
-    if kt["correct_ms"] >= kt["predict_ms"]:
-        dom, dom_ms, dom_bytes = "llg_correct", kt["correct_ms"], bytes_corr
-    else:
-        dom, dom_ms, dom_bytes = "llg_predict", kt["predict_ms"], bytes_pred
     peak, peak_kind = measured_peaks()
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
-    traffic = profiled_traffic(f"{dom}:{args.workload}:p{prec}")
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": dom, "peak_source": peak_kind,
-            "algorithmic_bytes_per_launch": dom_bytes,
-            "step": {"achieved_GBs": (bytes_pred + bytes_corr) / (ms * 1e-3 / args.steps) / 1e9,
-                     "bytes_per_spin_step": 15 * s}}
+    kname = KERNEL_NAMES[prec][1 if kt["correct_ms"] >= kt["predict_ms"] else 0]
+    roof = _roofline(kt, nspin, 8, ms / args.steps, peak, peak_kind,
+                     profiled_traffic(f"{kname}:{args.workload}:p{prec}"))
+    roof["kernel"] = kname
     # e2e through the C ABI with pinned host buffers
     inner = args.e2e_inner
     host = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
     host[...] = e0
-    hout = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
     sim.put_moments(host)
     sim.evolve(inner)
-    sim.get_moments_into(hout) if hasattr(sim, "get_moments_into") else sim.get_moments()
-    e2e_rounds = max(1, args.e2e_rounds)
+    sim.get_moments()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(e2e_rounds):
+    for _ in range(max(1, args.e2e_rounds)):
         sim.put_moments(host)
         sim.evolve(inner)
-        out = sim.get_moments()
+        sim.get_moments()
     torch.cuda.synchronize()
     e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e_val = nspin * inner * e2e_rounds * world / e2e_s
-    nbytes = host.nbytes
+    e2e_val = nspin * inner * max(1, args.e2e_rounds) * world / e2e_s
+    sim.close()
+    variants = {}
+    if args.variants and prec == 1:
+        try:
+            alt = _make_sim(lat, w, 2, 1000 + rank, e0)
+            alt.set_stream(stream.cuda_stream)
+            ms2 = _time_steps(alt, stream, args.steps, args.warmup, world)
+            kt2 = alt.time_kernels(3)
+            alt.close()
+            variants["double_single_master"] = {
+                "value": nspin * args.steps * world / (ms2 * 1e-3), "ms_per_step": ms2 / args.steps,
+                "kernel_ms": kt2, "roofline": _roofline(kt2, nspin, 8, ms2 / args.steps, peak, peak_kind, None)}
+        except Exception as exc:
+            variants["double_single_master"] = {"error": str(exc)}
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, lat, e0, os.cpu_count() or 1)
-    sim.close()
     if rank != 0:
         return
     line = {
         "metric": "LLG atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == "0" else "f32-gather/f64-state", "data": "synthetic (seeded lattice and spins)",
+        "dtype": "f64" if prec == 0 else "f32-gather/f64-state",
+        "data": "synthetic (seeded lattice, species and spins)",
         "config": {"workload": args.workload, "description": w["desc"], "natom": lat.natom,
-                   "ensembles": lat.mensemble, "spins": nspin, "solver": "Depondt" if w["solver"] == 5 else "midpoint",
-                   "precision_path": "fp64-generic" if prec == "0" else "structured-mixed",
+                   "ensembles": lat.mensemble, "spins": nspin,
+                   "solver": "Depondt" if w["solver"] == 5 else "midpoint", "precision_path": PREC_NAMES[prec],
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "inner_steps_per_call": inner,
-                "note": "put_moments(pinned host) + sd_run(inner) + get_moments per e2e step"},
+        "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": host.nbytes,
+                "d2h_bytes_per_step": host.nbytes, "inner_steps_per_call": inner,
+                "note": "put_moments(pinned host) + sd_run(inner steps) + get_moments per e2e step"},
         "clocks": clk.summary(),
         "gpu_launches": launches,
         "kernel_ms": kt,
+        "variants": variants,
     }
     print(json.dumps(line), flush=True)
 
@@ -337,10 +364,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="alloy2m", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="auto", choices=["auto", "0", "1"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "0", "1", "2"])
     ap.add_argument("--e2e-inner", type=int, default=10)
     ap.add_argument("--e2e-rounds", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variants", action="store_true", help="also time the double-single master variant")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -56,8 +56,11 @@ typedef struct {
     double delta_t, bn, temprescale;
     uint64_t gpu_rng_seed;             /* Philox key (gpu_rng_seed keyword) */
     int32_t gpu_rng;                   /* 0 Philox in-kernel, 1 caller-injected normals */
-    int32_t precision;                 /* 0 FP64 everywhere; 1 FP32 gather, FP64 master
-                                          (structured periodic lattices only) */
+    int32_t precision;                 /* 0 FP64 everywhere (any neighbour list);
+                                          1 FP32 field gather + FP64 spin master and
+                                            renormalisation (structured lattices, Depondt);
+                                          2 FP32 field gather + double-single (float-float)
+                                            spin master and renormalisation (same scope) */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;

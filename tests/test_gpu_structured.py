@@ -1,0 +1,93 @@
+"""Structured mixed-precision LLG path (precision 1: FP64 master, 2: double-single
+master) against the FP64 CPU oracle.
+
+The field gather, thermal field and rotation run in FP32, so trajectories are
+compared with an FP32-scale tolerance; the spin norm, which the higher-precision
+master renormalises every step, is held to 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from uppasd_gb300 import lattice
+from uppasd_gb300._lib import UppasdGpuError
+from uppasd_gb300.simulation import GpuSimulation
+
+pytestmark = pytest.mark.gpu
+
+# Max per-component deviation from the FP64 oracle after the steps below
+# (FP32 gather: ~1e-7 relative per step, accumulated over the run).
+TRAJ_TOL = {200: 2e-5, 1000: 2e-4}
+
+
+def _rand_unit(rng, shape):
+    e = rng.normal(size=shape)
+    return e / np.linalg.norm(e, axis=-1, keepdims=True)
+
+
+def _run(lat, prec, temp, nsteps, e0, seed=21):
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=temp, seed=seed, emom=e0,
+                        precision=prec)
+    sim.evolve(nsteps)
+    e = sim.get_moments()
+    sim.close()
+    return e
+
+
+def _oracle(lat, temp, nsteps, e0, seed=21):
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(5, 1e-16, 0.1, temp, 1.0, noise_mode=po.NOISE_PHILOX, seed=seed)
+    for _ in range(nsteps):
+        o.sd_step()
+    return o.emom.copy()
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("kind", ["bcc2", "alloy4"])
+def test_structured_vs_oracle(prec, kind):
+    if kind == "bcc2":
+        lat = lattice.bcc(6, [1.3, 0.7], 2.2).with_ensembles(2)
+    else:
+        lat = lattice.bcc_alloy(6, seed=4).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(8), (2, lat.natom, 3))
+    for temp, nsteps in ((0.0, 1000), (300.0, 200)):
+        g = _run(lat, prec, temp, nsteps, e0)
+        ref = _oracle(lat, temp, nsteps, e0)
+        err = np.max(np.abs(g - ref))
+        print(f"prec={prec} {kind} T={temp} steps={nsteps}: max|GPU-oracle| = {err:.3e}")
+        assert err <= TRAJ_TOL[nsteps]
+        assert np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)) <= 1e-12
+
+
+def test_master_variants_agree():
+    lat = lattice.bcc_alloy(6, seed=9).with_ensembles(1)
+    e0 = _rand_unit(np.random.default_rng(10), (1, lat.natom, 3))
+    a = _run(lat, 1, 300.0, 500, e0)
+    b = _run(lat, 2, 300.0, 500, e0)
+    assert np.max(np.abs(a - b)) <= 1e-5
+
+
+def test_structured_refuses_unsupported_hamiltonian():
+    lat = lattice.square_dmi(16)
+    with pytest.raises(UppasdGpuError) as ei:
+        GpuSimulation(lat, sdealgh=5, precision=1)
+    assert ei.value.rc == -7
+
+
+def test_structured_observables_and_mc_roundtrip():
+    """Observables and MC sweeps read the structured master state."""
+    lat = lattice.bcc(6, [1.3, 0.7], 2.2).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(11), (2, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=0.0, emom=e0, precision=2)
+    sim.evolve(10)
+    e = sim.get_moments()
+    o = po.Oracle(lat)
+    o.set_moments(e)
+    obs = sim.observables()
+    assert np.allclose(obs["energy"], o.energy()["total"], rtol=1e-10, atol=1e-12)
+    sim.relax("H", 500.0, 2)
+    sim.evolve(10)
+    e2 = sim.get_moments()
+    assert np.max(np.abs(np.linalg.norm(e2, axis=-1) - 1.0)) <= 1e-12
+    sim.close()

@@ -206,7 +206,7 @@ int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
         return bad("SDEalgh must be 1, 4, 5 or 6");
     if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
     if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
-    if (c->precision != 0 && c->precision != 1) return bad("precision must be 0 or 1");
+    if (c->precision < 0 || c->precision > 2) return bad("precision must be 0, 1 or 2");
     for (int i = 0; i < c->natom; ++i)
         if (a->aham[i] < 1 || a->aham[i] > c->nham) return bad("aham out of range");
     for (int h = 0; h < c->nham; ++h) {
@@ -338,7 +338,7 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
         return rc;
     if ((rc = build_colouring(s, c, nlT, nsize, dmT, dmsize))) return rc;
     s.precision = c->precision;
-    if (c->precision == 1) {
+    if (c->precision >= 1) {
         if ((rc = structured_init(s, c, a))) return rc;
     }
     if ((rc = uppasd_gpu_put_moments(reinterpret_cast<uppasd_gpu_sim *>(&s), a->emom))) return rc;
@@ -367,7 +367,7 @@ void destroy(Sim &s) {
 }
 
 int one_step(Sim &s, int64_t off, int phase = 3) {
-    return s.precision == 1 ? structured_step(s, off, phase) : llg_generic_step(s, off, phase);
+    return s.precision >= 1 ? structured_step(s, off, phase) : llg_generic_step(s, off, phase);
 }
 
 int run_steps(Sim &s, int64_t n) {
@@ -484,7 +484,7 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
         uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
         return UPPASD_GPU_ECUDA;
     }
-    if (s.precision == 1) return uppasd::structured_load_state(s);
+    if (s.precision >= 1) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;
 }
 
@@ -495,7 +495,7 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
     }
     Sim &s = w->s;
     int rc;
-    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     double *d = nullptr;
     UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
@@ -573,7 +573,7 @@ int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {
     if (!w || !beff) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
     return uppasd::field_to_host(s, beff);
 }
 
@@ -584,10 +584,10 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t 
     }
     Sim &s = w->s;
     int rc;
-    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
     rc = uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
     if (rc) return rc;
-    if (s.precision == 1) return uppasd::structured_load_state(s);
+    if (s.precision >= 1) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;
 }
 
@@ -642,7 +642,7 @@ int uppasd_gpu_observables(uppasd_gpu_sim *w, double *mvec, double *mabs, double
     if (!w) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (s.precision == 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
     return uppasd::observables(s, mvec, mabs, energy, nullptr);
 }
 

@@ -1,17 +1,550 @@
-// llg_stencil.cu -- structured-lattice mixed-precision LLG path (precision = 1).
-// Placeholder until the structured kernels land: every entry reports that the
-// path is unavailable so callers fall back to precision = 0.
+// llg_stencil.cu -- structured-lattice mixed-precision LLG (precision 1 and 2).
+//
+// Scope: periodic bcc lattices (2-atom conventional cell) with up to four
+// exchange shells and up to two chemical species, uniform damping and
+// temperature, Depondt solver (Evolution/depondt.f90:50-333), exchange plus a
+// uniform Zeeman field.  init verifies that the caller's nlist/ncoup are
+// exactly this structure (every neighbour and every FP64 coupling) and refuses
+// otherwise, so the generic FP64 path stays the fallback.
+//
+// What changes against the FP64 path:
+//  * neighbour indices are not stored: they follow from the cell coordinates
+//    and a compile-time stencil; couplings come from a (shell, species_i,
+//    species_j) table, so the only per-neighbour data is the neighbour's spin;
+//  * the field gather, thermal field, damping term and Rodrigues rotation run in
+//    FP32 on a float4 mirror (unit spin xyz + species in w);
+//  * the spin state itself is kept in higher precision and renormalised every
+//    step: FP64 (precision 1) or double-single hi+lo float pairs (precision 2,
+//    hi = the FP32 mirror itself, lo = a residual array).  GB300's FP64 pipe
+//    runs at ~1/70 of FP32, which is why the double-single master exists.
+//
+// HBM layout: site (basis b, cell x,y,z) of ensemble k at
+//   ((k*2 + b)*L3 + z)*L2*L1 + y*L1 + x       (basis-major sublattices)
+// Threads: 3D tiles of cells (TX x TY x TZ) per block, one basis and one
+// ensemble per block, so a warp reads consecutive x of the same sublattice.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
 #include "sim.h"
 
 namespace uppasd {
 
-int structured_init(Sim &, const uppasd_gpu_consts *, const uppasd_gpu_arrays *) {
-    set_error("precision = 1 (structured mixed-precision path) is not available in this build");
-    return UPPASD_GPU_EUNSUPPORTED;
+namespace {
+
+constexpr int TX = 8, TY = 4, TZ = 8;
+constexpr int kMaxNb = 50;
+
+// bcc neighbour stencil: (dx, dy, dz, target basis, shell) in cell units, for
+// basis 0 (corner) and basis 1 (body centre); shells 1..4 = 8, 6, 12, 24 sites.
+struct St {
+    int8_t dx, dy, dz, bj, sh;
+};
+
+__host__ __device__ constexpr St stencil_entry(int b, int s) {
+    // shell 1 : s in [0,8)   other basis, offsets {-1,0}^3 (b=0) or {0,1}^3 (b=1)
+    // shell 2 : s in [8,14)  same basis, +-unit axis
+    // shell 3 : s in [14,26) same basis, (+-1,+-1,0) permutations
+    // shell 4 : s in [26,50) other basis, one axis {-2,+1} (b=0) / {-1,+2} (b=1), others as shell 1
+    if (s < 8) {
+        int o0 = b == 0 ? -1 : 0;
+        return St{(int8_t)(o0 + ((s >> 0) & 1)), (int8_t)(o0 + ((s >> 1) & 1)), (int8_t)(o0 + ((s >> 2) & 1)),
+                  (int8_t)(1 - b), 1};
+    }
+    if (s < 14) {
+        int q = s - 8, ax = q >> 1, sg = (q & 1) ? -1 : 1;
+        return St{(int8_t)(ax == 0 ? sg : 0), (int8_t)(ax == 1 ? sg : 0), (int8_t)(ax == 2 ? sg : 0), (int8_t)b, 2};
+    }
+    if (s < 26) {
+        int q = s - 14, pr = q >> 2, sa = (q & 1) ? -1 : 1, sb = (q & 2) ? -1 : 1;
+        int a0 = pr == 2 ? 1 : 0, a1 = pr == 0 ? 1 : 2;
+        int d[3] = {0, 0, 0};
+        d[a0] = sa;
+        d[a1] = sb;
+        return St{(int8_t)d[0], (int8_t)d[1], (int8_t)d[2], (int8_t)b, 3};
+    }
+    int q = s - 26, ax = q >> 3, far = (q >> 2) & 1, p1 = q & 1, p2 = (q >> 1) & 1;
+    int o0 = b == 0 ? -1 : 0;
+    int fa = b == 0 ? (far ? -2 : 1) : (far ? -1 : 2);
+    int d[3] = {0, 0, 0};
+    d[ax] = fa;
+    int oa = ax == 0 ? 1 : 0, ob = ax == 2 ? 1 : 2;
+    d[oa] = o0 + p1;
+    d[ob] = o0 + p2;
+    return St{(int8_t)d[0], (int8_t)d[1], (int8_t)d[2], (int8_t)(1 - b), 4};
 }
-int structured_step(Sim &, int64_t, int) { return UPPASD_GPU_EUNSUPPORTED; }
-int structured_sync_state(Sim &) { return UPPASD_GPU_EUNSUPPORTED; }
-int structured_load_state(Sim &) { return UPPASD_GPU_EUNSUPPORTED; }
-void structured_free(Sim &) {}
+
+constexpr int nb_of_shells(int nsh) { return nsh >= 4 ? 50 : nsh == 3 ? 26 : nsh == 2 ? 14 : 8; }
+
+struct SParams {
+    int L1, L2, L3, nens;
+    long long nsite;   // sites per ensemble
+    float4 *mt, *mp;   // mirrors at t and at the predictor
+    float *b2x, *b2y, *b2z;
+    float *lox, *loy, *loz;        // double-single residuals (precision 2)
+    double *mx, *my, *mz;          // FP64 master (precision 1)
+    float cu[4][2][2];             // coupling on unit vectors: ncoup * m_j, per shell / species_i / species_j
+    float sigma[2];                // thermal-field amplitude per species (Depondt, depondt.f90:143-144)
+    float lam, dtg;                // damping, delta_t*gama/(1+lambda^2)
+    float ext[3];
+    uint64_t seed;
+    const int64_t *d_step;
+    long long step_off;
+};
+
+__device__ __forceinline__ long long sidx(const SParams &p, int k, int b, int x, int y, int z) {
+    return (((long long)(k * 2 + b) * p.L3 + z) * p.L2 + y) * (long long)p.L1 + x;
+}
+
+// Reference numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3)) (0-based) for the Philox counter,
+// so the structured and the generic path draw the same thermal-field stream.
+__device__ __forceinline__ long long ref_site(const SParams &p, int b, int x, int y, int z) {
+    return b + 2LL * (x + (long long)p.L1 * (y + (long long)p.L2 * z));
+}
+
+template <int NSH, int b>
+__device__ __forceinline__ void gather_b(const SParams &p, const float4 *__restrict__ m, int k, int x, int y, int z,
+                                         int ti, float B[3]) {
+    constexpr int NB = nb_of_shells(NSH);
+    int xw[5], yo[5], zo[5];
+#pragma unroll
+    for (int d = -2; d <= 2; ++d) {
+        int xx = x + d, yy = y + d, zz = z + d;
+        xx += xx < 0 ? p.L1 : (xx >= p.L1 ? -p.L1 : 0);
+        yy += yy < 0 ? p.L2 : (yy >= p.L2 ? -p.L2 : 0);
+        zz += zz < 0 ? p.L3 : (zz >= p.L3 ? -p.L3 : 0);
+        xw[d + 2] = xx;
+        yo[d + 2] = yy * p.L1;
+        zo[d + 2] = zz * p.L2 * p.L1;
+    }
+    const long long plane = (long long)p.L1 * p.L2 * p.L3;
+    const float4 *base[2] = {m + (long long)(k * 2 + 0) * plane, m + (long long)(k * 2 + 1) * plane};
+    float cA[4], cB[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        cA[s] = p.cu[s][ti][0];
+        cB[s] = p.cu[s][ti][1];
+    }
+    float bx = 0.f, by = 0.f, bz = 0.f;
+#pragma unroll
+    for (int s = 0; s < NB; ++s) {
+        const St e = stencil_entry(b, s);
+        const float4 v = __ldg(base[e.bj] + (zo[e.dz + 2] + yo[e.dy + 2] + xw[e.dx + 2]));
+        const float c = v.w != 0.f ? cB[e.sh - 1] : cA[e.sh - 1];
+        bx = fmaf(c, v.x, bx);
+        by = fmaf(c, v.y, by);
+        bz = fmaf(c, v.z, bz);
+    }
+    B[0] = bx + p.ext[0];
+    B[1] = by + p.ext[1];
+    B[2] = bz + p.ext[2];
+}
+
+// The basis index is block-uniform; dispatching on it makes every stencil offset
+// a compile-time constant, so the wrapped-coordinate tables stay in registers.
+template <int NSH>
+__device__ __forceinline__ void gather(const SParams &p, const float4 *__restrict__ m, int k, int b, int x, int y,
+                                       int z, int ti, float B[3]) {
+    if (b == 0)
+        gather_b<NSH, 0>(p, m, k, x, y, z, ti, B);
+    else
+        gather_b<NSH, 1>(p, m, k, x, y, z, ti, B);
+}
+
+// Depondt's effective field including damping: bdup = bloc + lambda * e x bloc
+__device__ __forceinline__ void depondt_bdup(float lam, const float e[3], const float bl[3], float o[3]) {
+    o[0] = bl[0] + lam * (e[1] * bl[2] - e[2] * bl[1]);
+    o[1] = bl[1] + lam * (e[2] * bl[0] - e[0] * bl[2]);
+    o[2] = bl[2] + lam * (e[0] * bl[1] - e[1] * bl[0]);
+}
+
+// Rodrigues rotation increment: R e - e = (1-cos v)[(h.e)h - e] + sin v (h x e),
+// with h = bdup/|bdup| and v = |bdup| dt gama/(1+lambda^2)  (depondt.f90:156-179).
+__device__ __forceinline__ void rotation_delta(const float bd[3], const float e[3], float dtg, float d[3]) {
+    float bn = sqrtf(bd[0] * bd[0] + bd[1] * bd[1] + bd[2] * bd[2]) + 1e-15f;
+    float inv = 1.0f / bn;
+    float hx = bd[0] * inv, hy = bd[1] * inv, hz = bd[2] * inv;
+    float v = bn * dtg;
+    float sv, cv;
+    __sincosf(v, &sv, &cv);
+    // 1 - cos v computed as 2 sin^2(v/2) to keep it accurate for small v
+    float sh = __sinf(0.5f * v);
+    float u = 2.0f * sh * sh;
+    float he = hx * e[0] + hy * e[1] + hz * e[2];
+    d[0] = u * (he * hx - e[0]) + sv * (hy * e[2] - hz * e[1]);
+    d[1] = u * (he * hy - e[1]) + sv * (hz * e[0] - hx * e[2]);
+    d[2] = u * (he * hz - e[2]) + sv * (hx * e[1] - hy * e[0]);
+}
+
+template <int NSH>
+__global__ void __launch_bounds__(TX *TY *TZ) stencil_predict(SParams p, int ntx, int nty) {
+    const int tile = blockIdx.x;
+    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
+    const int x = tx * TX + threadIdx.x, y = ty * TY + threadIdx.y, z = tz * TZ + threadIdx.z;
+    if (x >= p.L1 || y >= p.L2 || z >= p.L3) return;
+    const int b = blockIdx.y, k = blockIdx.z;
+    const long long o = sidx(p, k, b, x, y, z);
+    const float4 me = p.mt[o];
+    const int ti = me.w != 0.f ? 1 : 0;
+    float B[3];
+    gather<NSH>(p, p.mt, k, b, x, y, z, ti, B);
+    const long long step = *p.d_step + p.step_off;
+    float zr[3];
+    normal3_f32(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
+    const float sg = p.sigma[ti];
+    const float e[3] = {me.x, me.y, me.z};
+    float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
+    float bd[3], d[3];
+    depondt_bdup(p.lam, e, bl, bd);
+    rotation_delta(bd, e, p.dtg, d);
+    p.mp[o] = make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w);
+    p.b2x[o] = bd[0];
+    p.b2y[o] = bd[1];
+    p.b2z[o] = bd[2];
+}
+
+// Double-single helpers (Dekker / Knuth error-free transformations).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    e = b - (s - a);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+
+template <int NSH, int MASTER>  // MASTER 1: FP64, 2: double-single
+__global__ void __launch_bounds__(TX *TY *TZ) stencil_correct(SParams p, int ntx, int nty) {
+    const int tile = blockIdx.x;
+    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
+    const int x = tx * TX + threadIdx.x, y = ty * TY + threadIdx.y, z = tz * TZ + threadIdx.z;
+    if (x >= p.L1 || y >= p.L2 || z >= p.L3) return;
+    const int b = blockIdx.y, k = blockIdx.z;
+    const long long o = sidx(p, k, b, x, y, z);
+    const float4 mp = p.mp[o];
+    const int ti = mp.w != 0.f ? 1 : 0;
+    float B[3];
+    gather<NSH>(p, p.mp, k, b, x, y, z, ti, B);
+    const long long step = *p.d_step + p.step_off;
+    float zr[3];
+    normal3_f32(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
+    const float sg = p.sigma[ti];
+    const float ep[3] = {mp.x, mp.y, mp.z};
+    float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
+    float bd[3];
+    depondt_bdup(p.lam, ep, bl, bd);
+    bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[o];
+    bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[o];
+    bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[o];
+    const float4 mt = p.mt[o];
+    const float eh[3] = {mt.x, mt.y, mt.z};
+    float d[3];
+    rotation_delta(bd, eh, p.dtg, d);
+    if (MASTER == 1) {
+        double e0 = p.mx[o] + (double)d[0], e1 = p.my[o] + (double)d[1], e2 = p.mz[o] + (double)d[2];
+        double n2 = fma(e2, e2, fma(e1, e1, e0 * e0));
+        double xx = n2 - 1.0;
+        double s = fma(xx, fma(0.375, xx, -0.5), 1.0);  // 1/sqrt(1+x) to second order, |x| ~ 1e-7
+        e0 *= s;
+        e1 *= s;
+        e2 *= s;
+        p.mx[o] = e0;
+        p.my[o] = e1;
+        p.mz[o] = e2;
+        p.mt[o] = make_float4((float)e0, (float)e1, (float)e2, mt.w);
+    } else {
+        float lo[3] = {p.lox[o], p.loy[o], p.loz[o]};
+        float hi[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float s, e;
+            two_sum(eh[c], d[c], s, e);
+            quick_two_sum(s, e + lo[c], hi[c], lo[c]);
+        }
+        // |e|^2 - 1 in double-single: sum of hi^2 (exact products) plus 2 hi lo
+        float n2h = 0.f, n2l = 0.f;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float pp, pe, s, e;
+            two_prod(hi[c], hi[c], pp, pe);
+            two_sum(n2h, pp, s, e);
+            n2h = s;
+            n2l += e + pe + 2.0f * hi[c] * lo[c];
+        }
+        float xs, xe;
+        two_sum(n2h, -1.0f, xs, xe);
+        float xx = xs + (xe + n2l);                    // |e|^2 - 1, ~1e-7
+        float sm1 = xx * fmaf(0.375f, xx, -0.5f);      // 1/sqrt(1+x) - 1
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            float corr = hi[c] * sm1 + lo[c] * sm1;
+            float s, e;
+            two_sum(hi[c], corr, s, e);
+            quick_two_sum(s, e + lo[c], hi[c], lo[c]);
+        }
+        p.lox[o] = lo[0];
+        p.loy[o] = lo[1];
+        p.loz[o] = lo[2];
+        p.mt[o] = make_float4(hi[0], hi[1], hi[2], mt.w);
+    }
+}
+
+// Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
+// and the structured state.
+__global__ void to_structured(SParams p, const double *ex, const double *ey, const double *ez,
+                              const int8_t *species, int master) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = p.nsite * p.nens;
+    if (t >= total) return;
+    int k = (int)(t / p.nsite);
+    long long i = t - (long long)k * p.nsite;  // reference site index
+    int b = (int)(i & 1);
+    long long cell = i >> 1;
+    int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
+    long long o = sidx(p, k, b, x, y, z);
+    double e0 = ex[t], e1 = ey[t], e2 = ez[t];
+    float w = species ? (float)species[i] : 0.f;
+    float h0 = (float)e0, h1 = (float)e1, h2 = (float)e2;
+    p.mt[o] = make_float4(h0, h1, h2, w);
+    if (master == 1) {
+        p.mx[o] = e0;
+        p.my[o] = e1;
+        p.mz[o] = e2;
+    } else {
+        p.lox[o] = (float)(e0 - (double)h0);
+        p.loy[o] = (float)(e1 - (double)h1);
+        p.loz[o] = (float)(e2 - (double)h2);
+    }
+}
+
+__global__ void from_structured(SParams p, double *ex, double *ey, double *ez, double *mx, double *my, double *mz,
+                                const double *mmom, int master) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = p.nsite * p.nens;
+    if (t >= total) return;
+    int k = (int)(t / p.nsite);
+    long long i = t - (long long)k * p.nsite;
+    int b = (int)(i & 1);
+    long long cell = i >> 1;
+    int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
+    long long o = sidx(p, k, b, x, y, z);
+    double e0, e1, e2;
+    if (master == 1) {
+        e0 = p.mx[o];
+        e1 = p.my[o];
+        e2 = p.mz[o];
+    } else {
+        float4 h = p.mt[o];
+        e0 = (double)h.x + (double)p.lox[o];
+        e1 = (double)h.y + (double)p.loy[o];
+        e2 = (double)h.z + (double)p.loz[o];
+    }
+    double m = mmom[t];
+    ex[t] = e0;
+    ey[t] = e1;
+    ez[t] = e2;
+    mx[t] = e0 * m;
+    my[t] = e1 * m;
+    mz[t] = e2 * m;
+}
+
+}  // namespace
+
+struct StructuredFast {
+    SParams p{};
+    int nshell = 0, master = 1, ntx = 0, nty = 0, ntz = 0;
+    int8_t *species = nullptr;
+};
+
+static void fast_free(StructuredFast *f) {
+    if (!f) return;
+    void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.lox, f->p.loy, f->p.loz,
+                    f->p.mx, f->p.my, f->p.mz, f->species};
+    for (void *q : ptrs) cudaFree(q);
+    delete f;
+}
+
+void structured_free(Sim &s) {
+    fast_free(s.fast);
+    s.fast = nullptr;
+}
+
+int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
+    auto no = [](const std::string &m) {
+        set_error("structured path not applicable: " + m);
+        return UPPASD_GPU_EUNSUPPORTED;
+    };
+    if (c->sdealgh != 5) return no("only the Depondt solver (SDEalgh 5) is implemented");
+    if (c->do_dm || c->do_aniso) return no("DM and anisotropy terms use the generic path");
+    if (c->na != 2 || c->n1 < 4 || c->n2 < 4 || c->n3 < 4) return no("needs a bcc cell grid (na = 2, n >= 4)");
+    const int N = c->natom, M = c->mensemble, L1 = c->n1, L2 = c->n2, L3 = c->n3;
+    if ((long long)2 * L1 * L2 * L3 != N) return no("natom != 2*n1*n2*n3");
+    for (int i = 1; i < N; ++i)
+        if (a->lambda1_array[i] != a->lambda1_array[0] || a->temp_array[i] != a->temp_array[0])
+            return no("damping and temperature must be uniform");
+    for (long long t = 1; t < (long long)N * M; ++t)
+        if (a->external_field[3 * t] != a->external_field[0] || a->external_field[3 * t + 1] != a->external_field[1] ||
+            a->external_field[3 * t + 2] != a->external_field[2])
+            return no("external field must be uniform");
+    std::vector<int8_t> sp(N, 0);
+    if (a->species)
+        for (int i = 0; i < N; ++i) {
+            if (a->species[i] < 0 || a->species[i] > 1) return no("at most two species");
+            sp[i] = (int8_t)a->species[i];
+        }
+    // moment per species (must be uniform within a species and across ensembles)
+    double mom[2] = {-1.0, -1.0};
+    for (long long t = 0; t < (long long)N * M; ++t) {
+        int sI = sp[t % N];
+        if (mom[sI] < 0) mom[sI] = a->mmom[t];
+        else if (mom[sI] != a->mmom[t]) return no("moment must be uniform per species");
+    }
+    // identify shells and the coupling table, verifying every neighbour and coupling
+    const int mnn = c->max_no_neigh;
+    int nshell = 0;
+    for (int sh : {1, 2, 3, 4})
+        if (mnn == nb_of_shells(sh)) nshell = sh;
+    if (!nshell) return no("neighbour count must be 8, 14, 26 or 50 (bcc shells 1..4)");
+    const int NB = nb_of_shells(nshell);
+    double tab[4][2][2];
+    bool have[4][2][2] = {};
+    std::vector<std::pair<int, int>> expect(NB), got(NB);
+    for (int i = 0; i < N; ++i) {
+        int ih = a->aham[i] - 1;
+        if (a->nlistsize[ih] != NB) return no("every site must have the full shell set");
+        int b = i & 1, cell = i >> 1;
+        int x = cell % L1, y = (cell / L1) % L2, z = cell / (L1 * L2);
+        for (int q = 0; q < NB; ++q) {
+            St e = stencil_entry(b, q);
+            int xx = ((x + e.dx) % L1 + L1) % L1, yy = ((y + e.dy) % L2 + L2) % L2, zz = ((z + e.dz) % L3 + L3) % L3;
+            int j = e.bj + 2 * (xx + L1 * (yy + L2 * zz));
+            expect[q] = {j, e.sh};
+            got[q] = {a->nlist[q + (size_t)mnn * i] - 1, q};
+        }
+        std::vector<std::pair<int, int>> es = expect, gs = got;
+        std::sort(es.begin(), es.end());
+        std::sort(gs.begin(), gs.end());
+        for (int q = 0; q < NB; ++q) {
+            if (es[q].first != gs[q].first) return no("neighbour list does not match the bcc shell stencil");
+            if (q + 1 < NB && es[q].first == es[q + 1].first) return no("periodic images coincide (lattice too small)");
+            int sh = es[q].second - 1;
+            double cval = a->ncoup[gs[q].second + (size_t)mnn * ih];
+            int tj = sp[es[q].first];
+            if (!have[sh][sp[i]][tj]) {
+                tab[sh][sp[i]][tj] = cval;
+                have[sh][sp[i]][tj] = true;
+            } else if (tab[sh][sp[i]][tj] != cval) {
+                return no("couplings are not a function of (shell, species_i, species_j)");
+            }
+        }
+    }
+    StructuredFast *f = new (std::nothrow) StructuredFast();
+    if (!f) return UPPASD_GPU_ENOMEM;
+    f->nshell = nshell;
+    f->master = c->precision;
+    SParams &p = f->p;
+    p.L1 = L1;
+    p.L2 = L2;
+    p.L3 = L3;
+    p.nens = M;
+    p.nsite = N;
+    for (int sh = 0; sh < 4; ++sh)
+        for (int ti = 0; ti < 2; ++ti)
+            for (int tj = 0; tj < 2; ++tj) {
+                double v = (sh < nshell && have[sh][ti][tj]) ? tab[sh][ti][tj] * (mom[tj] > 0 ? mom[tj] : 0.0) : 0.0;
+                p.cu[sh][ti][tj] = (float)v;
+            }
+    const double lam = a->lambda1_array[0], T = a->temp_array[0];
+    for (int ti = 0; ti < 2; ++ti) {
+        double Dp = (2.0 * lam * kKbolt) / (c->delta_t * kGama * kMub);
+        double m = mom[ti] > 0 ? mom[ti] : 1.0;
+        p.sigma[ti] = (float)sqrt(Dp * c->temprescale * T / m);
+    }
+    p.lam = (float)lam;
+    p.dtg = (float)(c->delta_t * kGama / (1.0 + lam * lam));
+    for (int q = 0; q < 3; ++q) p.ext[q] = (float)a->external_field[q];
+    p.seed = c->gpu_rng_seed;
+    p.d_step = s.llg.d_step;
+    const size_t n = (size_t)N * M;
+    cudaError_t e = cudaSuccess;
+    auto al = [&](void **q, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(q, bytes);
+        if (e == cudaSuccess) s.bytes_allocated += bytes;
+    };
+    al((void **)&p.mt, n * sizeof(float4));
+    al((void **)&p.mp, n * sizeof(float4));
+    al((void **)&p.b2x, n * sizeof(float));
+    al((void **)&p.b2y, n * sizeof(float));
+    al((void **)&p.b2z, n * sizeof(float));
+    if (f->master == 1) {
+        al((void **)&p.mx, n * sizeof(double));
+        al((void **)&p.my, n * sizeof(double));
+        al((void **)&p.mz, n * sizeof(double));
+    } else {
+        al((void **)&p.lox, n * sizeof(float));
+        al((void **)&p.loy, n * sizeof(float));
+        al((void **)&p.loz, n * sizeof(float));
+    }
+    al((void **)&f->species, N);
+    if (e == cudaSuccess) e = cudaMemcpy(f->species, sp.data(), N, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        fast_free(f);
+        set_error(std::string("structured_init: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? UPPASD_GPU_ENOMEM : UPPASD_GPU_ECUDA;
+    }
+    f->ntx = (L1 + TX - 1) / TX;
+    f->nty = (L2 + TY - 1) / TY;
+    f->ntz = (L3 + TZ - 1) / TZ;
+    s.fast = f;
+    return UPPASD_GPU_OK;
+}
+
+int structured_load_state(Sim &s) {
+    StructuredFast *f = s.fast;
+    long long total = f->p.nsite * f->p.nens;
+    to_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, f->species,
+                                                                         f->master);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
+int structured_sync_state(Sim &s) {
+    StructuredFast *f = s.fast;
+    long long total = f->p.nsite * f->p.nens;
+    from_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y,
+                                                                           s.eM.z, s.llg.mmom, f->master);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
+template <int NSH>
+static void launch(StructuredFast *f, cudaStream_t st, int phase) {
+    dim3 grid((unsigned)(f->ntx * f->nty * f->ntz), 2, (unsigned)f->p.nens), block(TX, TY, TZ);
+    if (phase & 1) stencil_predict<NSH><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
+    if (phase & 2) {
+        if (f->master == 1) stencil_correct<NSH, 1><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
+        else stencil_correct<NSH, 2><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
+    }
+}
+
+int structured_step(Sim &s, int64_t step_offset, int phase) {
+    StructuredFast *f = s.fast;
+    f->p.step_off = step_offset;
+    f->p.d_step = s.llg.d_step;
+    switch (f->nshell) {
+    case 1: launch<1>(f, s.stream, phase); break;
+    case 2: launch<2>(f, s.stream, phase); break;
+    case 3: launch<3>(f, s.stream, phase); break;
+    default: launch<4>(f, s.stream, phase); break;
+    }
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
 
 }  // namespace uppasd
