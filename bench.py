@@ -36,6 +36,11 @@ WORKLOADS = {
     "alloy2m": dict(kind="alloy", L=100, ens=8, solver=5, dt=1e-16, damping=0.1, temp=300.0,
                     desc="bcc random binary alloy 100^3 cells (2,000,000 atoms) x 8 ensembles, 4 shells (50 nbrs), "
                          "Depondt, T=300 K"),
+    # same Hamiltonian on 64^3 cells (524,288 atoms x 8 = 4.2 M spins, ~0.3 GB of state):
+    # the profiling case (still larger than L2, a few hundred MB on the device)
+    "alloy64": dict(kind="alloy", L=64, ens=8, solver=5, dt=1e-16, damping=0.1, temp=300.0,
+                    desc="bcc random binary alloy 64^3 cells (524,288 atoms) x 8 ensembles, 4 shells, Depondt, "
+                         "T=300 K"),
     "bcc16k": dict(kind="bcc", L=20, ens=1, solver=5, dt=1e-16, damping=0.1, temp=300.0,
                    desc="bcc ferromagnet 20^3 cells (16,000 atoms), J1=1.3 J2=0.7 mRy, Depondt, T=300 K"),
     "square256": dict(kind="square", L=256, ens=1, solver=1, dt=1e-16, damping=0.05, temp=50.0,
