@@ -77,8 +77,11 @@ __device__ inline void normal3_f64(uint64_t seed, int64_t site, int32_t ens, int
 __device__ inline void normal3_f32(uint64_t seed, int64_t site, int32_t ens, int64_t step, uint32_t stream,
                                    float z[3]) {
     Philox4 w = philox_draw(seed, site, ens, step, stream);
-    float r0 = sqrtf(-2.0f * __logf(u01_openf(w.x)));
-    float r1 = sqrtf(-2.0f * __logf(u01_openf(w.z)));
+    // radii from the full 32-bit words (relative precision of u, not absolute,
+    // is what the tail of -2 ln u needs), angles from the 24-bit grid
+    const float k32 = 2.3283064365386963e-10f;
+    float r0 = sqrtf(-2.0f * logf(fmaf((float)w.x, k32, 0.5f * k32)));
+    float r1 = sqrtf(-2.0f * logf(fmaf((float)w.z, k32, 0.5f * k32)));
     float s0, c0, s1, c1;
     sincospif(2.0f * u01_openf(w.y), &s0, &c0);
     sincospif(2.0f * u01_openf(w.w), &s1, &c1);

@@ -8,9 +8,12 @@
 // otherwise, so the generic FP64 path stays the fallback.
 //
 // What changes against the FP64 path:
-//  * neighbour indices are not stored: they follow from the cell coordinates
-//    and a compile-time stencil; couplings come from a (shell, species_i,
-//    species_j) table, so the only per-neighbour data is the neighbour's spin;
+//  * neighbour indices are not stored: each sublattice is kept in a
+//    ghost-padded array, so a neighbour is the site's own address plus a
+//    block-uniform offset (no wrap logic, no per-neighbour index loads);
+//  * couplings come from a (shell, species_i, species_j) table: with the
+//    neighbour's species s_j in {0,1} carried in the float4's w, the coupling
+//    is c_A + s_j (c_B - c_A), one FMA;
 //  * the field gather, thermal field, damping term and Rodrigues rotation run in
 //    FP32 on a float4 mirror (unit spin xyz + species in w);
 //  * the spin state itself is kept in higher precision and renormalised every
@@ -18,10 +21,13 @@
 //    hi = the FP32 mirror itself, lo = a residual array).  GB300's FP64 pipe
 //    runs at ~1/70 of FP32, which is why the double-single master exists.
 //
-// HBM layout: site (basis b, cell x,y,z) of ensemble k at
-//   ((k*2 + b)*L3 + z)*L2*L1 + y*L1 + x       (basis-major sublattices)
-// Threads: 3D tiles of cells (TX x TY x TZ) per block, one basis and one
-// ensemble per block, so a warp reads consecutive x of the same sublattice.
+// HBM layout.  Mirrors (float4): per (ensemble k, basis b) a padded box of
+// P3 x P2 x P1 cells, interior cell (x,y,z) at ((z+2)*P2 + (y+2))*P1 + (x+XOFF);
+// the 2-cell ghost shell holds periodic copies written by the producing kernel.
+// Other per-site arrays (b2eff, residual / FP64 master) are unpadded:
+// ((k*2 + b)*L3 + z)*L2*L1 + y*L1 + x.
+// Threads: block (TXB, TYB) covers TXB consecutive x of TYB rows at one z, one
+// basis and one ensemble per block.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -33,8 +39,7 @@ namespace uppasd {
 
 namespace {
 
-constexpr int TX = 8, TY = 4, TZ = 8;
-constexpr int kMaxNb = 50;
+constexpr int XOFF = 8;  // left x padding: keeps interior rows 128-byte aligned
 
 // bcc neighbour stencil: (dx, dy, dz, target basis, shell) in cell units, for
 // basis 0 (corner) and basis 1 (body centre); shells 1..4 = 8, 6, 12, 24 sites.
@@ -79,59 +84,82 @@ constexpr int nb_of_shells(int nsh) { return nsh >= 4 ? 50 : nsh == 3 ? 26 : nsh
 
 struct SParams {
     int L1, L2, L3, nens;
-    long long nsite;   // sites per ensemble
-    float4 *mt, *mp;   // mirrors at t and at the predictor
+    int P1, P2;                 // padded row and plane pitch (cells)
+    long long pbox;             // cells per padded sublattice box = P2 * (L3 + 4)
+    long long nsite;            // sites per ensemble (2 L1 L2 L3)
+    float4 *mt, *mp;            // padded mirrors at t and at the predictor
     float *b2x, *b2y, *b2z;
-    float *lox, *loy, *loz;        // double-single residuals (precision 2)
-    double *mx, *my, *mz;          // FP64 master (precision 1)
-    float cu[4][2][2];             // coupling on unit vectors: ncoup * m_j, per shell / species_i / species_j
-    float sigma[2];                // thermal-field amplitude per species (Depondt, depondt.f90:143-144)
-    float lam, dtg;                // damping, delta_t*gama/(1+lambda^2)
+    float *lox, *loy, *loz;     // double-single residuals (precision 2)
+    double *mx, *my, *mz;       // FP64 master (precision 1)
+    float cA[4][2], cD[4][2];   // coupling on unit vectors: cA[sh][s_i] + s_j * cD[sh][s_i]
+    float sigma[2];             // thermal-field amplitude per species (Depondt, depondt.f90:143-144)
+    float lam, dtg;             // damping, delta_t*gama/(1+lambda^2)
     float ext[3];
     uint64_t seed;
     const int64_t *d_step;
     long long step_off;
 };
 
-__device__ __forceinline__ long long sidx(const SParams &p, int k, int b, int x, int y, int z) {
+__device__ __forceinline__ long long pidx(const SParams &p, int k, int b, int x, int y, int z) {
+    return (long long)(k * 2 + b) * p.pbox + ((long long)(z + 2) * p.P2 + (long long)(y + 2) * p.P1 + (x + XOFF));
+}
+__device__ __forceinline__ long long uidx(const SParams &p, int k, int b, int x, int y, int z) {
     return (((long long)(k * 2 + b) * p.L3 + z) * p.L2 + y) * (long long)p.L1 + x;
 }
-
-// Reference numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3)) (0-based) for the Philox counter,
-// so the structured and the generic path draw the same thermal-field stream.
+// Reference numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3)) (0-based) for the Philox
+// counter, so the structured and the generic path draw the same thermal-field stream.
 __device__ __forceinline__ long long ref_site(const SParams &p, int b, int x, int y, int z) {
     return b + 2LL * (x + (long long)p.L1 * (y + (long long)p.L2 * z));
 }
 
+// Store a site's mirror value and its periodic ghost copies.
+__device__ __forceinline__ void store_mirror(const SParams &p, float4 *m, int k, int b, int x, int y, int z,
+                                             float4 v) {
+    float4 *bx = m + (long long)(k * 2 + b) * p.pbox;
+    const int gx0 = x + XOFF, gy0 = y + 2, gz0 = z + 2;
+    // second (ghost) coordinate per axis, -1 when the site is not within 2 cells of that face
+    const int gx1 = x < 2 ? gx0 + p.L1 : (x >= p.L1 - 2 ? gx0 - p.L1 : -1);
+    const int gy1 = y < 2 ? gy0 + p.L2 : (y >= p.L2 - 2 ? gy0 - p.L2 : -1);
+    const int gz1 = z < 2 ? gz0 + p.L3 : (z >= p.L3 - 2 ? gz0 - p.L3 : -1);
+    const long long py0 = (long long)gy0 * p.P1, pz0 = (long long)gz0 * p.P2;
+    bx[pz0 + py0 + gx0] = v;
+    if (gx1 < 0 && gy1 < 0 && gz1 < 0) return;
+    const long long py1 = (long long)gy1 * p.P1, pz1 = (long long)gz1 * p.P2;
+    if (gx1 >= 0) bx[pz0 + py0 + gx1] = v;
+    if (gy1 >= 0) {
+        bx[pz0 + py1 + gx0] = v;
+        if (gx1 >= 0) bx[pz0 + py1 + gx1] = v;
+    }
+    if (gz1 >= 0) {
+        bx[pz1 + py0 + gx0] = v;
+        if (gx1 >= 0) bx[pz1 + py0 + gx1] = v;
+        if (gy1 >= 0) {
+            bx[pz1 + py1 + gx0] = v;
+            if (gx1 >= 0) bx[pz1 + py1 + gx1] = v;
+        }
+    }
+}
+
 template <int NSH, int b>
 __device__ __forceinline__ void gather_b(const SParams &p, const float4 *__restrict__ m, int k, int x, int y, int z,
-                                         int ti, float B[3]) {
+                                         int si, float B[3]) {
     constexpr int NB = nb_of_shells(NSH);
-    int xw[5], yo[5], zo[5];
-#pragma unroll
-    for (int d = -2; d <= 2; ++d) {
-        int xx = x + d, yy = y + d, zz = z + d;
-        xx += xx < 0 ? p.L1 : (xx >= p.L1 ? -p.L1 : 0);
-        yy += yy < 0 ? p.L2 : (yy >= p.L2 ? -p.L2 : 0);
-        zz += zz < 0 ? p.L3 : (zz >= p.L3 ? -p.L3 : 0);
-        xw[d + 2] = xx;
-        yo[d + 2] = yy * p.L1;
-        zo[d + 2] = zz * p.L2 * p.L1;
-    }
-    const long long plane = (long long)p.L1 * p.L2 * p.L3;
-    const float4 *base[2] = {m + (long long)(k * 2 + 0) * plane, m + (long long)(k * 2 + 1) * plane};
-    float cA[4], cB[4];
+    const long long own = (long long)(z + 2) * p.P2 + (long long)(y + 2) * p.P1 + (x + XOFF);
+    const float4 *base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
+    const float4 *base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
+    float cA[4], cD[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        cA[s] = p.cu[s][ti][0];
-        cB[s] = p.cu[s][ti][1];
+        cA[s] = p.cA[s][si];
+        cD[s] = p.cD[s][si];
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
 #pragma unroll
     for (int s = 0; s < NB; ++s) {
         const St e = stencil_entry(b, s);
-        const float4 v = __ldg(base[e.bj] + (zo[e.dz + 2] + yo[e.dy + 2] + xw[e.dx + 2]));
-        const float c = v.w != 0.f ? cB[e.sh - 1] : cA[e.sh - 1];
+        const int off = e.dz * p.P2 + e.dy * p.P1 + e.dx;  // block-uniform
+        const float4 v = __ldg((e.bj ? base1 : base0) + off);
+        const float c = fmaf(v.w, cD[e.sh - 1], cA[e.sh - 1]);
         bx = fmaf(c, v.x, bx);
         by = fmaf(c, v.y, by);
         bz = fmaf(c, v.z, bz);
@@ -139,17 +167,6 @@ __device__ __forceinline__ void gather_b(const SParams &p, const float4 *__restr
     B[0] = bx + p.ext[0];
     B[1] = by + p.ext[1];
     B[2] = bz + p.ext[2];
-}
-
-// The basis index is block-uniform; dispatching on it makes every stencil offset
-// a compile-time constant, so the wrapped-coordinate tables stay in registers.
-template <int NSH>
-__device__ __forceinline__ void gather(const SParams &p, const float4 *__restrict__ m, int k, int b, int x, int y,
-                                       int z, int ti, float B[3]) {
-    if (b == 0)
-        gather_b<NSH, 0>(p, m, k, x, y, z, ti, B);
-    else
-        gather_b<NSH, 1>(p, m, k, x, y, z, ti, B);
 }
 
 // Depondt's effective field including damping: bdup = bloc + lambda * e x bloc
@@ -185,31 +202,49 @@ __device__ __forceinline__ void rotation_delta(const float bd[3], const float e[
     d[2] = u * (he * hz - e[2]) + sv * (hx * e[1] - hy * e[0]);
 }
 
-template <int NSH>
-__global__ void __launch_bounds__(TX *TY *TZ) stencil_predict(SParams p, int ntx, int nty) {
-    const int tile = blockIdx.x;
-    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
-    const int x = tx * TX + threadIdx.x, y = ty * TY + threadIdx.y, z = tz * TZ + threadIdx.z;
-    if (x >= p.L1 || y >= p.L2 || z >= p.L3) return;
-    const int b = blockIdx.y, k = blockIdx.z;
-    const long long o = sidx(p, k, b, x, y, z);
+struct Site {
+    int x, y, z, b, k;
+};
+
+__device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
+    const int nyt = (p.L2 + blockDim.y - 1) / blockDim.y;
+    s.x = threadIdx.x;
+    s.y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
+    s.z = blockIdx.x / nyt;
+    s.b = blockIdx.y;
+    s.k = blockIdx.z;
+    return s.x < p.L1 && s.y < p.L2;
+}
+
+template <int NSH, int b>
+__device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
+    const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
     const float4 me = p.mt[o];
-    const int ti = me.w != 0.f ? 1 : 0;
+    const int si = me.w != 0.f ? 1 : 0;
     float B[3];
-    gather<NSH>(p, p.mt, k, b, x, y, z, ti, B);
+    gather_b<NSH, b>(p, p.mt, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
-    normal3_f32(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
-    const float sg = p.sigma[ti];
+    normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
+    const float sg = p.sigma[si];
     const float e[3] = {me.x, me.y, me.z};
     float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
     float bd[3], d[3];
     depondt_bdup(p.lam, e, bl, bd);
     rotation_delta(bd, e, p.dtg, d);
-    p.mp[o] = make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w);
-    p.b2x[o] = bd[0];
-    p.b2y[o] = bd[1];
-    p.b2z[o] = bd[2];
+    store_mirror(p, p.mp, s.k, b, s.x, s.y, s.z, make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w));
+    const long long u = uidx(p, s.k, b, s.x, s.y, s.z);
+    p.b2x[u] = bd[0];
+    p.b2y[u] = bd[1];
+    p.b2z[u] = bd[2];
+}
+
+template <int NSH>
+__global__ void __launch_bounds__(256) stencil_predict(SParams p) {
+    Site s;
+    if (!site_of_thread(p, s)) return;
+    if (s.b == 0) predict_site<NSH, 0>(p, s);
+    else predict_site<NSH, 1>(p, s);
 }
 
 // Double-single helpers (Dekker / Knuth error-free transformations).
@@ -227,80 +262,86 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
     e = fmaf(a, b, -p);
 }
 
-template <int NSH, int MASTER>  // MASTER 1: FP64, 2: double-single
-__global__ void __launch_bounds__(TX *TY *TZ) stencil_correct(SParams p, int ntx, int nty) {
-    const int tile = blockIdx.x;
-    const int tx = tile % ntx, ty = (tile / ntx) % nty, tz = tile / (ntx * nty);
-    const int x = tx * TX + threadIdx.x, y = ty * TY + threadIdx.y, z = tz * TZ + threadIdx.z;
-    if (x >= p.L1 || y >= p.L2 || z >= p.L3) return;
-    const int b = blockIdx.y, k = blockIdx.z;
-    const long long o = sidx(p, k, b, x, y, z);
+template <int NSH, int MASTER, int b>  // MASTER 1: FP64, 2: double-single
+__device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
+    const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
+    const long long u = uidx(p, s.k, b, s.x, s.y, s.z);
     const float4 mp = p.mp[o];
-    const int ti = mp.w != 0.f ? 1 : 0;
+    const int si = mp.w != 0.f ? 1 : 0;
     float B[3];
-    gather<NSH>(p, p.mp, k, b, x, y, z, ti, B);
+    gather_b<NSH, b>(p, p.mp, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
-    normal3_f32(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
-    const float sg = p.sigma[ti];
+    normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
+    const float sg = p.sigma[si];
     const float ep[3] = {mp.x, mp.y, mp.z};
     float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
     float bd[3];
     depondt_bdup(p.lam, ep, bl, bd);
-    bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[o];
-    bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[o];
-    bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[o];
+    bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[u];
+    bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[u];
+    bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[u];
     const float4 mt = p.mt[o];
     const float eh[3] = {mt.x, mt.y, mt.z};
     float d[3];
     rotation_delta(bd, eh, p.dtg, d);
+    float4 out;
     if (MASTER == 1) {
-        double e0 = p.mx[o] + (double)d[0], e1 = p.my[o] + (double)d[1], e2 = p.mz[o] + (double)d[2];
+        double e0 = p.mx[u] + (double)d[0], e1 = p.my[u] + (double)d[1], e2 = p.mz[u] + (double)d[2];
         double n2 = fma(e2, e2, fma(e1, e1, e0 * e0));
         double xx = n2 - 1.0;
-        double s = fma(xx, fma(0.375, xx, -0.5), 1.0);  // 1/sqrt(1+x) to second order, |x| ~ 1e-7
-        e0 *= s;
-        e1 *= s;
-        e2 *= s;
-        p.mx[o] = e0;
-        p.my[o] = e1;
-        p.mz[o] = e2;
-        p.mt[o] = make_float4((float)e0, (float)e1, (float)e2, mt.w);
+        double sc = fma(xx, fma(0.375, xx, -0.5), 1.0);  // 1/sqrt(1+x) to second order, |x| ~ 1e-7
+        e0 *= sc;
+        e1 *= sc;
+        e2 *= sc;
+        p.mx[u] = e0;
+        p.my[u] = e1;
+        p.mz[u] = e2;
+        out = make_float4((float)e0, (float)e1, (float)e2, mt.w);
     } else {
-        float lo[3] = {p.lox[o], p.loy[o], p.loz[o]};
+        float lo[3] = {p.lox[u], p.loy[u], p.loz[u]};
         float hi[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            float s, e;
-            two_sum(eh[c], d[c], s, e);
-            quick_two_sum(s, e + lo[c], hi[c], lo[c]);
+            float sm, er;
+            two_sum(eh[c], d[c], sm, er);
+            quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
         }
         // |e|^2 - 1 in double-single: sum of hi^2 (exact products) plus 2 hi lo
         float n2h = 0.f, n2l = 0.f;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            float pp, pe, s, e;
+            float pp, pe, sm, er;
             two_prod(hi[c], hi[c], pp, pe);
-            two_sum(n2h, pp, s, e);
-            n2h = s;
-            n2l += e + pe + 2.0f * hi[c] * lo[c];
+            two_sum(n2h, pp, sm, er);
+            n2h = sm;
+            n2l += er + pe + 2.0f * hi[c] * lo[c];
         }
         float xs, xe;
         two_sum(n2h, -1.0f, xs, xe);
-        float xx = xs + (xe + n2l);                    // |e|^2 - 1, ~1e-7
-        float sm1 = xx * fmaf(0.375f, xx, -0.5f);      // 1/sqrt(1+x) - 1
+        float xx = xs + (xe + n2l);                // |e|^2 - 1, ~1e-7
+        float sm1 = xx * fmaf(0.375f, xx, -0.5f);  // 1/sqrt(1+x) - 1
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             float corr = hi[c] * sm1 + lo[c] * sm1;
-            float s, e;
-            two_sum(hi[c], corr, s, e);
-            quick_two_sum(s, e + lo[c], hi[c], lo[c]);
+            float sm, er;
+            two_sum(hi[c], corr, sm, er);
+            quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
         }
-        p.lox[o] = lo[0];
-        p.loy[o] = lo[1];
-        p.loz[o] = lo[2];
-        p.mt[o] = make_float4(hi[0], hi[1], hi[2], mt.w);
+        p.lox[u] = lo[0];
+        p.loy[u] = lo[1];
+        p.loz[u] = lo[2];
+        out = make_float4(hi[0], hi[1], hi[2], mt.w);
     }
+    store_mirror(p, p.mt, s.k, b, s.x, s.y, s.z, out);
+}
+
+template <int NSH, int MASTER>
+__global__ void __launch_bounds__(256) stencil_correct(SParams p) {
+    Site s;
+    if (!site_of_thread(p, s)) return;
+    if (s.b == 0) correct_site<NSH, MASTER, 0>(p, s);
+    else correct_site<NSH, MASTER, 1>(p, s);
 }
 
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
@@ -315,19 +356,19 @@ __global__ void to_structured(SParams p, const double *ex, const double *ey, con
     int b = (int)(i & 1);
     long long cell = i >> 1;
     int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
-    long long o = sidx(p, k, b, x, y, z);
+    long long u = uidx(p, k, b, x, y, z);
     double e0 = ex[t], e1 = ey[t], e2 = ez[t];
     float w = species ? (float)species[i] : 0.f;
     float h0 = (float)e0, h1 = (float)e1, h2 = (float)e2;
-    p.mt[o] = make_float4(h0, h1, h2, w);
+    store_mirror(p, p.mt, k, b, x, y, z, make_float4(h0, h1, h2, w));
     if (master == 1) {
-        p.mx[o] = e0;
-        p.my[o] = e1;
-        p.mz[o] = e2;
+        p.mx[u] = e0;
+        p.my[u] = e1;
+        p.mz[u] = e2;
     } else {
-        p.lox[o] = (float)(e0 - (double)h0);
-        p.loy[o] = (float)(e1 - (double)h1);
-        p.loz[o] = (float)(e2 - (double)h2);
+        p.lox[u] = (float)(e0 - (double)h0);
+        p.loy[u] = (float)(e1 - (double)h1);
+        p.loz[u] = (float)(e2 - (double)h2);
     }
 }
 
@@ -341,17 +382,17 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
     int b = (int)(i & 1);
     long long cell = i >> 1;
     int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
-    long long o = sidx(p, k, b, x, y, z);
+    long long u = uidx(p, k, b, x, y, z);
     double e0, e1, e2;
     if (master == 1) {
-        e0 = p.mx[o];
-        e1 = p.my[o];
-        e2 = p.mz[o];
+        e0 = p.mx[u];
+        e1 = p.my[u];
+        e2 = p.mz[u];
     } else {
-        float4 h = p.mt[o];
-        e0 = (double)h.x + (double)p.lox[o];
-        e1 = (double)h.y + (double)p.loy[o];
-        e2 = (double)h.z + (double)p.loz[o];
+        float4 h = p.mt[pidx(p, k, b, x, y, z)];
+        e0 = (double)h.x + (double)p.lox[u];
+        e1 = (double)h.y + (double)p.loy[u];
+        e2 = (double)h.z + (double)p.loz[u];
     }
     double m = mmom[t];
     ex[t] = e0;
@@ -366,7 +407,8 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
 
 struct StructuredFast {
     SParams p{};
-    int nshell = 0, master = 1, ntx = 0, nty = 0, ntz = 0;
+    int nshell = 0, master = 1;
+    dim3 grid, block;
     int8_t *species = nullptr;
 };
 
@@ -393,6 +435,7 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     if (c->na != 2 || c->n1 < 4 || c->n2 < 4 || c->n3 < 4) return no("needs a bcc cell grid (na = 2, n >= 4)");
     const int N = c->natom, M = c->mensemble, L1 = c->n1, L2 = c->n2, L3 = c->n3;
     if ((long long)2 * L1 * L2 * L3 != N) return no("natom != 2*n1*n2*n3");
+    if (L1 > 1024) return no("n1 must be <= 1024");
     for (int i = 1; i < N; ++i)
         if (a->lambda1_array[i] != a->lambda1_array[0] || a->temp_array[i] != a->temp_array[0])
             return no("damping and temperature must be uniform");
@@ -422,7 +465,7 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     const int NB = nb_of_shells(nshell);
     double tab[4][2][2];
     bool have[4][2][2] = {};
-    std::vector<std::pair<int, int>> expect(NB), got(NB);
+    std::vector<std::pair<int, int>> es(NB), gs(NB);
     for (int i = 0; i < N; ++i) {
         int ih = a->aham[i] - 1;
         if (a->nlistsize[ih] != NB) return no("every site must have the full shell set");
@@ -431,11 +474,9 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
         for (int q = 0; q < NB; ++q) {
             St e = stencil_entry(b, q);
             int xx = ((x + e.dx) % L1 + L1) % L1, yy = ((y + e.dy) % L2 + L2) % L2, zz = ((z + e.dz) % L3 + L3) % L3;
-            int j = e.bj + 2 * (xx + L1 * (yy + L2 * zz));
-            expect[q] = {j, e.sh};
-            got[q] = {a->nlist[q + (size_t)mnn * i] - 1, q};
+            es[q] = {e.bj + 2 * (xx + L1 * (yy + L2 * zz)), e.sh};
+            gs[q] = {a->nlist[q + (size_t)mnn * i] - 1, q};
         }
-        std::vector<std::pair<int, int>> es = expect, gs = got;
         std::sort(es.begin(), es.end());
         std::sort(gs.begin(), gs.end());
         for (int q = 0; q < NB; ++q) {
@@ -462,12 +503,18 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     p.L3 = L3;
     p.nens = M;
     p.nsite = N;
+    p.P1 = ((L1 + XOFF + 2) + 7) / 8 * 8;
+    p.P2 = p.P1 * (L2 + 4);
+    p.pbox = (long long)p.P2 * (L3 + 4);
     for (int sh = 0; sh < 4; ++sh)
-        for (int ti = 0; ti < 2; ++ti)
-            for (int tj = 0; tj < 2; ++tj) {
-                double v = (sh < nshell && have[sh][ti][tj]) ? tab[sh][ti][tj] * (mom[tj] > 0 ? mom[tj] : 0.0) : 0.0;
-                p.cu[sh][ti][tj] = (float)v;
-            }
+        for (int ti = 0; ti < 2; ++ti) {
+            double v[2];
+            for (int tj = 0; tj < 2; ++tj)
+                v[tj] = (sh < nshell && have[sh][ti][tj]) ? tab[sh][ti][tj] * (mom[tj] > 0 ? mom[tj] : 0.0) : 0.0;
+            if (!(sh < nshell && have[sh][ti][1])) v[1] = v[0];
+            p.cA[sh][ti] = (float)v[0];
+            p.cD[sh][ti] = (float)(v[1] - v[0]);
+        }
     const double lam = a->lambda1_array[0], T = a->temp_array[0];
     for (int ti = 0; ti < 2; ++ti) {
         double Dp = (2.0 * lam * kKbolt) / (c->delta_t * kGama * kMub);
@@ -480,13 +527,16 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     p.seed = c->gpu_rng_seed;
     p.d_step = s.llg.d_step;
     const size_t n = (size_t)N * M;
+    const size_t nbox = (size_t)p.pbox * 2 * M;
     cudaError_t e = cudaSuccess;
     auto al = [&](void **q, size_t bytes) {
         if (e == cudaSuccess) e = cudaMalloc(q, bytes);
         if (e == cudaSuccess) s.bytes_allocated += bytes;
     };
-    al((void **)&p.mt, n * sizeof(float4));
-    al((void **)&p.mp, n * sizeof(float4));
+    al((void **)&p.mt, nbox * sizeof(float4));
+    al((void **)&p.mp, nbox * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemset(p.mt, 0, nbox * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemset(p.mp, 0, nbox * sizeof(float4));
     al((void **)&p.b2x, n * sizeof(float));
     al((void **)&p.b2y, n * sizeof(float));
     al((void **)&p.b2z, n * sizeof(float));
@@ -506,9 +556,14 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
         set_error(std::string("structured_init: ") + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? UPPASD_GPU_ENOMEM : UPPASD_GPU_ECUDA;
     }
-    f->ntx = (L1 + TX - 1) / TX;
-    f->nty = (L2 + TY - 1) / TY;
-    f->ntz = (L3 + TZ - 1) / TZ;
+    const int bx = L1 <= 256 ? L1 : 256;
+    if (L1 > 256) {
+        fast_free(f);
+        return no("n1 must be <= 256 for the structured kernels");
+    }
+    const int by = std::max(1, 256 / bx);
+    f->block = dim3(bx, by, 1);
+    f->grid = dim3((unsigned)(((L2 + by - 1) / by) * L3), 2, (unsigned)M);
     s.fast = f;
     return UPPASD_GPU_OK;
 }
@@ -533,11 +588,10 @@ int structured_sync_state(Sim &s) {
 
 template <int NSH>
 static void launch(StructuredFast *f, cudaStream_t st, int phase) {
-    dim3 grid((unsigned)(f->ntx * f->nty * f->ntz), 2, (unsigned)f->p.nens), block(TX, TY, TZ);
-    if (phase & 1) stencil_predict<NSH><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
+    if (phase & 1) stencil_predict<NSH><<<f->grid, f->block, 0, st>>>(f->p);
     if (phase & 2) {
-        if (f->master == 1) stencil_correct<NSH, 1><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
-        else stencil_correct<NSH, 2><<<grid, block, 0, st>>>(f->p, f->ntx, f->nty);
+        if (f->master == 1) stencil_correct<NSH, 1><<<f->grid, f->block, 0, st>>>(f->p);
+        else stencil_correct<NSH, 2><<<f->grid, f->block, 0, st>>>(f->p);
     }
 }
 
