@@ -140,24 +140,31 @@ __device__ __forceinline__ void store_mirror(const SParams &p, float4 *m, int k,
     }
 }
 
-template <int NSH, int b>
+// Padded pitches of a cubic L^3 lattice; LC = 0 selects the runtime pitches.
+__host__ __device__ constexpr int pitch1(int L) { return ((L + XOFF + 2) + 7) / 8 * 8; }
+__host__ __device__ constexpr int pitch2(int L) { return pitch1(L) * (L + 4); }
+
+template <int NSH, int b, int LC>
 __device__ __forceinline__ void gather_b(const SParams &p, const float4 *__restrict__ m, int k, int x, int y, int z,
                                          int si, float B[3]) {
     constexpr int NB = nb_of_shells(NSH);
-    const long long own = (long long)(z + 2) * p.P2 + (long long)(y + 2) * p.P1 + (x + XOFF);
+    // with LC fixed at compile time every neighbour offset is an immediate in the load
+    const int P1 = LC ? pitch1(LC) : p.P1;
+    const int P2 = LC ? pitch2(LC) : p.P2;
+    const long long own = (long long)(z + 2) * P2 + (long long)(y + 2) * P1 + (x + XOFF);
     const float4 *base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
     const float4 *base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
     float cA[4], cD[4];
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
-        cA[s] = p.cA[s][si];
-        cD[s] = p.cD[s][si];
+        cA[s] = si ? p.cA[s][1] : p.cA[s][0];
+        cD[s] = si ? p.cD[s][1] : p.cD[s][0];
     }
     float bx = 0.f, by = 0.f, bz = 0.f;
 #pragma unroll
     for (int s = 0; s < NB; ++s) {
         const St e = stencil_entry(b, s);
-        const int off = e.dz * p.P2 + e.dy * p.P1 + e.dx;  // block-uniform
+        const int off = e.dz * P2 + e.dy * P1 + e.dx;  // block-uniform (immediate when LC > 0)
         const float4 v = __ldg((e.bj ? base1 : base0) + off);
         const float c = fmaf(v.w, cD[e.sh - 1], cA[e.sh - 1]);
         bx = fmaf(c, v.x, bx);
@@ -216,13 +223,13 @@ __device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
     return s.x < p.L1 && s.y < p.L2;
 }
 
-template <int NSH, int b>
+template <int NSH, int b, int LC>
 __device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
     const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
     const float4 me = p.mt[o];
     const int si = me.w != 0.f ? 1 : 0;
     float B[3];
-    gather_b<NSH, b>(p, p.mt, s.k, s.x, s.y, s.z, si, B);
+    gather_b<NSH, b, LC>(p, p.mt, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
     normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
@@ -239,12 +246,12 @@ __device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
     p.b2z[u] = bd[2];
 }
 
-template <int NSH>
+template <int NSH, int LC>
 __global__ void __launch_bounds__(256) stencil_predict(SParams p) {
     Site s;
     if (!site_of_thread(p, s)) return;
-    if (s.b == 0) predict_site<NSH, 0>(p, s);
-    else predict_site<NSH, 1>(p, s);
+    if (s.b == 0) predict_site<NSH, 0, LC>(p, s);
+    else predict_site<NSH, 1, LC>(p, s);
 }
 
 // Double-single helpers (Dekker / Knuth error-free transformations).
@@ -262,14 +269,14 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
     e = fmaf(a, b, -p);
 }
 
-template <int NSH, int MASTER, int b>  // MASTER 1: FP64, 2: double-single
+template <int NSH, int MASTER, int b, int LC>  // MASTER 1: FP64, 2: double-single
 __device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
     const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
     const long long u = uidx(p, s.k, b, s.x, s.y, s.z);
     const float4 mp = p.mp[o];
     const int si = mp.w != 0.f ? 1 : 0;
     float B[3];
-    gather_b<NSH, b>(p, p.mp, s.k, s.x, s.y, s.z, si, B);
+    gather_b<NSH, b, LC>(p, p.mp, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
     normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
@@ -336,12 +343,12 @@ __device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
     store_mirror(p, p.mt, s.k, b, s.x, s.y, s.z, out);
 }
 
-template <int NSH, int MASTER>
+template <int NSH, int MASTER, int LC>
 __global__ void __launch_bounds__(256) stencil_correct(SParams p) {
     Site s;
     if (!site_of_thread(p, s)) return;
-    if (s.b == 0) correct_site<NSH, MASTER, 0>(p, s);
-    else correct_site<NSH, MASTER, 1>(p, s);
+    if (s.b == 0) correct_site<NSH, MASTER, 0, LC>(p, s);
+    else correct_site<NSH, MASTER, 1, LC>(p, s);
 }
 
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
@@ -407,7 +414,7 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
 
 struct StructuredFast {
     SParams p{};
-    int nshell = 0, master = 1;
+    int nshell = 0, master = 1, lc = 0;
     dim3 grid, block;
     int8_t *species = nullptr;
 };
@@ -503,8 +510,13 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     p.L3 = L3;
     p.nens = M;
     p.nsite = N;
-    p.P1 = ((L1 + XOFF + 2) + 7) / 8 * 8;
+    p.P1 = pitch1(L1);
     p.P2 = p.P1 * (L2 + 4);
+    // cubic lattices of the sizes below get kernels with compile-time pitches
+    f->lc = 0;
+    if (L1 == L2 && L2 == L3)
+        for (int lc : {6, 64, 100})
+            if (L1 == lc && (nshell == 2 || nshell == 4)) f->lc = lc;
     p.pbox = (long long)p.P2 * (L3 + 4);
     for (int sh = 0; sh < 4; ++sh)
         for (int ti = 0; ti < 2; ++ti) {
@@ -586,13 +598,26 @@ int structured_sync_state(Sim &s) {
     return UPPASD_GPU_OK;
 }
 
+template <int NSH, int LC>
+static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
+    if (phase & 1) stencil_predict<NSH, LC><<<f->grid, f->block, 0, st>>>(f->p);
+    if (phase & 2) {
+        if (f->master == 1) stencil_correct<NSH, 1, LC><<<f->grid, f->block, 0, st>>>(f->p);
+        else stencil_correct<NSH, 2, LC><<<f->grid, f->block, 0, st>>>(f->p);
+    }
+}
+
 template <int NSH>
 static void launch(StructuredFast *f, cudaStream_t st, int phase) {
-    if (phase & 1) stencil_predict<NSH><<<f->grid, f->block, 0, st>>>(f->p);
-    if (phase & 2) {
-        if (f->master == 1) stencil_correct<NSH, 1><<<f->grid, f->block, 0, st>>>(f->p);
-        else stencil_correct<NSH, 2><<<f->grid, f->block, 0, st>>>(f->p);
+    if (NSH == 2 || NSH == 4) {
+        switch (f->lc) {
+        case 6: launch_lc<NSH, 6>(f, st, phase); return;
+        case 64: launch_lc<NSH, 64>(f, st, phase); return;
+        case 100: launch_lc<NSH, 100>(f, st, phase); return;
+        default: break;
+        }
     }
+    launch_lc<NSH, 0>(f, st, phase);
 }
 
 int structured_step(Sim &s, int64_t step_offset, int phase) {
