@@ -49,12 +49,16 @@ def _run(lat, prec, temp, nsteps, e0, seed=21):
 
 
 @pytest.mark.parametrize("prec", [1, 2])
-@pytest.mark.parametrize("kind", ["bcc2", "alloy4"])
+@pytest.mark.parametrize("kind", ["bcc2", "alloy4", "alloy4_L5"])
 def test_structured_vs_oracle(prec, kind):
+    """L = 6 runs the z-marching kernels (compile-time pitches, factorised
+    couplings); L = 5 runs the general gather kernels with runtime pitches."""
     if kind == "bcc2":
         lat = lattice.bcc(6, [1.3, 0.7], 2.2).with_ensembles(2)
-    else:
+    elif kind == "alloy4":
         lat = lattice.bcc_alloy(6, seed=4).with_ensembles(2)
+    else:
+        lat = lattice.bcc_alloy(5, seed=4).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(8), (2, lat.natom, 3))
     sim, o = _sim(lat, prec, 0.0, e0), _oracle(lat, 0.0, e0)
     done = 0
