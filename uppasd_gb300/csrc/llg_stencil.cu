@@ -89,15 +89,12 @@ struct SParams {
     long long pbox;             // cells per padded sublattice box = P2 * (L3 + 4)
     long long nsite;            // sites per ensemble (2 L1 L2 L3)
     float4 *mt, *mp;            // padded mirrors at t and at the predictor
-    float *b2x, *b2y, *b2z;
+    float *b2x, *b2y, *b2z;     // predictor's damped field (Depondt b2eff)
+    float *thx, *thy, *thz;     // thermal field drawn by the predictor, reused by the corrector
     float *lox, *loy, *loz;     // double-single residuals (precision 2)
     double *mx, *my, *mz;       // FP64 master (precision 1)
     float cA[4][2], cD[4][2];   // coupling on unit vectors: cA[sh][s_i] + s_j * cD[sh][s_i]
     float sigma[2];             // thermal-field amplitude per species (Depondt, depondt.f90:143-144)
-    // factorised couplings for the z-marching kernels: c(sh, s_i, s_j) = dsh[sh] * K[s_i][s_j],
-    // K[s_i][s_j] = kA[s_i] + s_j * kD[s_i]
-    float dsh[4], kA[2], kD[2];
-    int zc;                     // z planes per thread column (z-marching kernels)
     float lam, dtg;             // damping, delta_t*gama/(1+lambda^2)
     float ext[3];
     uint64_t seed;
@@ -237,10 +234,11 @@ __device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
     gather_b<NSH, b, LC>(p, p.mt, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
-    normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
+    normal3_f32_fast(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
     const float sg = p.sigma[si];
     const float e[3] = {me.x, me.y, me.z};
-    float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
+    const float th[3] = {zr[0] * sg, zr[1] * sg, zr[2] * sg};
+    float bl[3] = {B[0] + th[0], B[1] + th[1], B[2] + th[2]};
     float bd[3], d[3];
     depondt_bdup(p.lam, e, bl, bd);
     rotation_delta(bd, e, p.dtg, d);
@@ -249,6 +247,9 @@ __device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
     p.b2x[u] = bd[0];
     p.b2y[u] = bd[1];
     p.b2z[u] = bd[2];
+    p.thx[u] = th[0];
+    p.thy[u] = th[1];
+    p.thz[u] = th[2];
 }
 
 template <int NSH, int LC>
@@ -282,12 +283,8 @@ __device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
     const int si = mp.w != 0.f ? 1 : 0;
     float B[3];
     gather_b<NSH, b, LC>(p, p.mp, s.k, s.x, s.y, s.z, si, B);
-    const long long step = *p.d_step + p.step_off;
-    float zr[3];
-    normal3_f32(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
-    const float sg = p.sigma[si];
     const float ep[3] = {mp.x, mp.y, mp.z};
-    float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
+    float bl[3] = {B[0] + p.thx[u], B[1] + p.thy[u], B[2] + p.thz[u]};
     float bd[3];
     depondt_bdup(p.lam, ep, bl, bd);
     bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[u];
@@ -356,269 +353,6 @@ __global__ void __launch_bounds__(256) stencil_correct(SParams p) {
     else correct_site<NSH, MASTER, 1, LC>(p, s);
 }
 
-// ---------------------------------------------------------------------------
-// z-marching, register-blocked variant (couplings of the factorised form
-// c = dsh[shell] * K[s_i][s_j]).  A thread owns one (x, y) column of a z chunk
-// of one ensemble and produces both sublattice sites of every cell in it.  It
-// walks input planes z_in = z0-2 .. z0+zc+1; each plane point it needs is loaded
-// once and scattered into the field accumulators of the (up to five) output
-// planes z_in-2 .. z_in+2 that use it.  Two accumulator channels per output,
-//   T1 = sum_j dsh e_j   and   T2 = sum_j dsh s_j e_j,
-// give the field without knowing the output's species until it is finalised:
-//   B = kA[s_o] T1 + kD[s_o] T2 + B_ext.
-// Per cell this reads 26 plane points per input plane instead of 100 gathers.
-
-// Flat table of (plane point, output) pairs, built once by the constexpr
-// evaluator: for every sublattice point (bj, dx, dy) some entry uses, the
-// entries of either output basis it feeds (output basis, dz, shell).
-struct ZPt {
-    int8_t bj, dx, dy, first, count;
-};
-struct ZPair {
-    int8_t bo, dz, sh;
-};
-struct ZTables {
-    ZPt pts[50];
-    ZPair pairs[100];
-    int npts, npairs;
-};
-
-__host__ __device__ constexpr ZTables make_ztables(int nsh) {
-    ZTables t{};
-    int np = 0, nq = 0;
-    for (int bj = 0; bj < 2; ++bj)
-        for (int dy = -2; dy <= 2; ++dy)
-            for (int dx = -2; dx <= 2; ++dx) {
-                int first = nq;
-                for (int bo = 0; bo < 2; ++bo)
-                    for (int s = 0; s < nb_of_shells(nsh); ++s) {
-                        St e = stencil_entry(bo, s);
-                        if (e.bj == bj && e.dx == dx && e.dy == dy)
-                            t.pairs[nq++] = ZPair{(int8_t)bo, e.dz, e.sh};
-                    }
-                if (nq > first)
-                    t.pts[np++] = ZPt{(int8_t)bj, (int8_t)dx, (int8_t)dy, (int8_t)first, (int8_t)(nq - first)};
-            }
-    t.npts = np;
-    t.npairs = nq;
-    return t;
-}
-
-template <int NSH>
-struct ZT {
-    static constexpr ZTables t = make_ztables(NSH);
-};
-
-struct ZAcc {
-    float t1[5][2][3];
-    float t2[5][2][3];
-};
-
-// The point and pair loops are expanded with integer sequences so that every
-// table entry, slot and accumulator index is a constant expression: the
-// accumulators then live in registers.
-template <int NSH, int PH, int I>
-__device__ __forceinline__ void zm_pair(ZAcc &a, const float4 &v, float w0, float w1, float w2, const float d[4]) {
-    constexpr ZPair pr = ZT<NSH>::t.pairs[I];
-    constexpr int slot = (PH - pr.dz + 10) % 5;
-    constexpr int bo = pr.bo;
-    constexpr int sh = pr.sh - 1;
-    a.t1[slot][bo][0] = fmaf(d[sh], v.x, a.t1[slot][bo][0]);
-    a.t1[slot][bo][1] = fmaf(d[sh], v.y, a.t1[slot][bo][1]);
-    a.t1[slot][bo][2] = fmaf(d[sh], v.z, a.t1[slot][bo][2]);
-    a.t2[slot][bo][0] = fmaf(d[sh], w0, a.t2[slot][bo][0]);
-    a.t2[slot][bo][1] = fmaf(d[sh], w1, a.t2[slot][bo][1]);
-    a.t2[slot][bo][2] = fmaf(d[sh], w2, a.t2[slot][bo][2]);
-}
-
-template <int NSH, int PH, int FIRST, int... R>
-__device__ __forceinline__ void zm_pairs(ZAcc &a, const float4 &v, float w0, float w1, float w2, const float d[4],
-                                         std::integer_sequence<int, R...>) {
-    (zm_pair<NSH, PH, FIRST + R>(a, v, w0, w1, w2, d), ...);
-}
-
-template <int NSH, int LC, int PH, int Q>
-__device__ __forceinline__ void zm_point(const float4 *base0, const float4 *base1, ZAcc &a, const float d[4]) {
-    constexpr ZPt pt = ZT<NSH>::t.pts[Q];
-    constexpr int off = pt.dy * pitch1(LC) + pt.dx;
-    const float4 v = __ldg((pt.bj ? base1 : base0) + off);
-    zm_pairs<NSH, PH, pt.first>(a, v, v.w * v.x, v.w * v.y, v.w * v.z, d,
-                                std::make_integer_sequence<int, pt.count>{});
-}
-
-template <int NSH, int LC, int PH, int... Q>
-__device__ __forceinline__ void zm_points(const float4 *base0, const float4 *base1, ZAcc &a, const float d[4],
-                                          std::integer_sequence<int, Q...>) {
-    (zm_point<NSH, LC, PH, Q>(base0, base1, a, d), ...);
-}
-
-template <int NSH, int LC, int PH>
-__device__ __forceinline__ void zm_accumulate(const SParams &p, const float4 *__restrict__ m, int k, int x, int y,
-                                              int zin, ZAcc &a, const float d[4]) {
-    constexpr int P1 = pitch1(LC), P2 = pitch2(LC);
-    const long long own = (long long)(zin + 2) * P2 + (long long)(y + 2) * P1 + (x + XOFF);
-    const float4 *base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
-    const float4 *base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
-    zm_points<NSH, LC, PH>(base0, base1, a, d, std::make_integer_sequence<int, ZT<NSH>::t.npts>{});
-}
-
-// Emitted once (not inlined into the five plane phases): the per-site update of
-// a finished output site from its two accumulator channels.
-template <int KIND, int MASTER>  // KIND 0: predictor, 1: corrector
-__device__ __noinline__ void zm_finalize(const SParams &p, int k, int b, int x, int y, int z, float t10, float t11,
-                                         float t12, float t20, float t21, float t22) {
-    const float t1[3] = {t10, t11, t12}, t2[3] = {t20, t21, t22};
-    const long long o = pidx(p, k, b, x, y, z);
-    const long long u = uidx(p, k, b, x, y, z);
-    const float4 src = KIND == 0 ? p.mt[o] : p.mp[o];
-    const int si = src.w != 0.f ? 1 : 0;
-    const float ka = si ? p.kA[1] : p.kA[0], kd = si ? p.kD[1] : p.kD[0];
-    float B[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) B[c] = fmaf(ka, t1[c], fmaf(kd, t2[c], p.ext[c]));
-    const long long step = *p.d_step + p.step_off;
-    float zr[3];
-    normal3_f32(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
-    const float sg = p.sigma[si];
-    const float es[3] = {src.x, src.y, src.z};
-    float bl[3] = {B[0] + zr[0] * sg, B[1] + zr[1] * sg, B[2] + zr[2] * sg};
-    float bd[3], d[3];
-    depondt_bdup(p.lam, es, bl, bd);
-    if (KIND == 0) {
-        rotation_delta(bd, es, p.dtg, d);
-        store_mirror(p, p.mp, k, b, x, y, z, make_float4(es[0] + d[0], es[1] + d[1], es[2] + d[2], src.w));
-        p.b2x[u] = bd[0];
-        p.b2y[u] = bd[1];
-        p.b2z[u] = bd[2];
-        return;
-    }
-    bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[u];
-    bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[u];
-    bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[u];
-    const float4 mt = p.mt[o];
-    const float eh[3] = {mt.x, mt.y, mt.z};
-    rotation_delta(bd, eh, p.dtg, d);
-    float4 out;
-    if (MASTER == 1) {
-        double e0 = p.mx[u] + (double)d[0], e1 = p.my[u] + (double)d[1], e2 = p.mz[u] + (double)d[2];
-        double n2 = fma(e2, e2, fma(e1, e1, e0 * e0));
-        double xx = n2 - 1.0;
-        double sc = fma(xx, fma(0.375, xx, -0.5), 1.0);
-        e0 *= sc;
-        e1 *= sc;
-        e2 *= sc;
-        p.mx[u] = e0;
-        p.my[u] = e1;
-        p.mz[u] = e2;
-        out = make_float4((float)e0, (float)e1, (float)e2, mt.w);
-    } else {
-        float lo[3] = {p.lox[u], p.loy[u], p.loz[u]};
-        float hi[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float sm, er;
-            two_sum(eh[c], d[c], sm, er);
-            quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
-        }
-        float n2h = 0.f, n2l = 0.f;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float pp, pe, sm, er;
-            two_prod(hi[c], hi[c], pp, pe);
-            two_sum(n2h, pp, sm, er);
-            n2h = sm;
-            n2l += er + pe + 2.0f * hi[c] * lo[c];
-        }
-        float xs, xe;
-        two_sum(n2h, -1.0f, xs, xe);
-        float xx = xs + (xe + n2l);
-        float sm1 = xx * fmaf(0.375f, xx, -0.5f);
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float corr = hi[c] * sm1 + lo[c] * sm1;
-            float sm, er;
-            two_sum(hi[c], corr, sm, er);
-            quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
-        }
-        p.lox[u] = lo[0];
-        p.loy[u] = lo[1];
-        p.loz[u] = lo[2];
-        out = make_float4(hi[0], hi[1], hi[2], mt.w);
-    }
-    store_mirror(p, p.mt, k, b, x, y, z, out);
-}
-
-// One input plane: zero the slot entering the window, accumulate, and hand the
-// slot leaving it (compile-time index PH) to the caller through `out`.
-template <int NSH, int LC, int PH>
-__device__ __forceinline__ void zm_plane(const SParams &p, const float4 *__restrict__ m, int k, int x, int y, int zin,
-                                         ZAcc &a, const float d[4], float out[2][2][3]) {
-    constexpr int enter = (PH + 2) % 5, leave = (PH + 3) % 5;
-#pragma unroll
-    for (int bo = 0; bo < 2; ++bo)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            a.t1[enter][bo][c] = 0.f;
-            a.t2[enter][bo][c] = 0.f;
-        }
-    zm_accumulate<NSH, LC, PH>(p, m, k, x, y, zin, a, d);
-#pragma unroll
-    for (int bo = 0; bo < 2; ++bo)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            out[0][bo][c] = a.t1[leave][bo][c];
-            out[1][bo][c] = a.t2[leave][bo][c];
-        }
-}
-
-template <int NSH, int LC, int KIND, int MASTER>
-__global__ void __launch_bounds__(256) zmarch(const __grid_constant__ SParams p) {
-    const int nyt = (p.L2 + blockDim.y - 1) / blockDim.y;
-    const int x = threadIdx.x;
-    const int y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
-    const int z0 = (blockIdx.x / nyt) * p.zc;
-    const int k = blockIdx.y;
-    if (x >= p.L1 || y >= p.L2) return;
-    const int z1 = min(z0 + p.zc, p.L3);
-    const float4 *m = KIND == 0 ? p.mt : p.mp;
-    const float d[4] = {p.dsh[0], p.dsh[1], p.dsh[2], p.dsh[3]};
-    ZAcc a;
-#pragma unroll
-    for (int s = 0; s < 5; ++s)
-#pragma unroll
-        for (int bo = 0; bo < 2; ++bo)
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                a.t1[s][bo][c] = 0.f;
-                a.t2[s][bo][c] = 0.f;
-            }
-    // input planes z0-2 .. z1+1 (ghost planes make z_in in [-2, L3+1] valid
-    // addresses), five per round so every slot index is a compile-time constant
-    int zin = z0 - 2;
-    const int zend = z1 + 2;
-#define UPPASD_ZM_PHASE(PH)                                                                                 \
-    {                                                                                                        \
-        if (zin >= zend) break;                                                                              \
-        float out[2][2][3];                                                                                  \
-        zm_plane<NSH, LC, PH>(p, m, k, x, y, zin, a, d, out);                                                \
-        if (zin - 2 >= z0) {                                                                                 \
-            zm_finalize<KIND, MASTER>(p, k, 0, x, y, zin - 2, out[0][0][0], out[0][0][1], out[0][0][2],      \
-                                      out[1][0][0], out[1][0][1], out[1][0][2]);                             \
-            zm_finalize<KIND, MASTER>(p, k, 1, x, y, zin - 2, out[0][1][0], out[0][1][1], out[0][1][2],      \
-                                      out[1][1][0], out[1][1][1], out[1][1][2]);                             \
-        }                                                                                                    \
-        ++zin;                                                                                               \
-    }
-    for (;;) {
-        UPPASD_ZM_PHASE(0)
-        UPPASD_ZM_PHASE(1)
-        UPPASD_ZM_PHASE(2)
-        UPPASD_ZM_PHASE(3)
-        UPPASD_ZM_PHASE(4)
-    }
-#undef UPPASD_ZM_PHASE
-}
-
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
 // and the structured state.
 __global__ void to_structured(SParams p, const double *ex, const double *ey, const double *ez,
@@ -683,15 +417,13 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
 struct StructuredFast {
     SParams p{};
     int nshell = 0, master = 1, lc = 0;
-    bool zmarch = false;  // factorised couplings and a compile-time size: z-marching kernels
-    dim3 zgrid, zblock;
     dim3 grid, block;
     int8_t *species = nullptr;
 };
 
 static void fast_free(StructuredFast *f) {
     if (!f) return;
-    void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.lox, f->p.loy, f->p.loz,
+    void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.thx, f->p.thy, f->p.thz, f->p.lox, f->p.loy, f->p.loz,
                     f->p.mx, f->p.my, f->p.mz, f->species};
     for (void *q : ptrs) cudaFree(q);
     delete f;
@@ -803,33 +535,6 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
         double m = mom[ti] > 0 ? mom[ti] : 1.0;
         p.sigma[ti] = (float)sqrt(Dp * c->temprescale * T / m);
     }
-    // factorisation c(sh, s_i, s_j) = dsh[sh] * K[s_i][s_j] with K = the shell-1 table
-    {
-        double cu[4][2][2];
-        for (int sh = 0; sh < 4; ++sh)
-            for (int ti = 0; ti < 2; ++ti)
-                for (int tj = 0; tj < 2; ++tj)
-                    cu[sh][ti][tj] = (sh < nshell && have[sh][ti][tj]) ? tab[sh][ti][tj] * mom[tj] : 0.0;
-        bool ok = have[0][0][0] && cu[0][0][0] != 0.0;
-        double dsh[4] = {1.0, 0.0, 0.0, 0.0};
-        for (int sh = 1; sh < nshell && ok; ++sh) dsh[sh] = cu[sh][0][0] / cu[0][0][0];
-        for (int sh = 0; sh < nshell && ok; ++sh)
-            for (int ti = 0; ti < 2; ++ti)
-                for (int tj = 0; tj < 2; ++tj) {
-                    if (!have[sh][ti][tj]) continue;
-                    double want = dsh[sh] * cu[0][ti][tj];
-                    if (!have[0][ti][tj] || fabs(cu[sh][ti][tj] - want) > 1e-12 * fabs(want) + 1e-300) ok = false;
-                }
-        if (ok) {
-            for (int sh = 0; sh < 4; ++sh) p.dsh[sh] = (float)dsh[sh];
-            for (int ti = 0; ti < 2; ++ti) {
-                double k0 = cu[0][ti][0], k1 = have[0][ti][1] ? cu[0][ti][1] : k0;
-                p.kA[ti] = (float)k0;
-                p.kD[ti] = (float)(k1 - k0);
-            }
-        }
-        f->zmarch = ok && f->lc != 0;
-    }
     p.lam = (float)lam;
     p.dtg = (float)(c->delta_t * kGama / (1.0 + lam * lam));
     for (int q = 0; q < 3; ++q) p.ext[q] = (float)a->external_field[q];
@@ -849,6 +554,9 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     al((void **)&p.b2x, n * sizeof(float));
     al((void **)&p.b2y, n * sizeof(float));
     al((void **)&p.b2z, n * sizeof(float));
+    al((void **)&p.thx, n * sizeof(float));
+    al((void **)&p.thy, n * sizeof(float));
+    al((void **)&p.thz, n * sizeof(float));
     if (f->master == 1) {
         al((void **)&p.mx, n * sizeof(double));
         al((void **)&p.my, n * sizeof(double));
@@ -873,12 +581,6 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     const int by = std::max(1, 256 / bx);
     f->block = dim3(bx, by, 1);
     f->grid = dim3((unsigned)(((L2 + by - 1) / by) * L3), 2, (unsigned)M);
-    {
-        const int zby = std::min(L2, std::max(1, 256 / bx));
-        p.zc = std::min(L3, std::max(8, (L3 + 3) / 4));
-        f->zblock = dim3(bx, zby, 1);
-        f->zgrid = dim3((unsigned)(((L2 + zby - 1) / zby) * ((L3 + p.zc - 1) / p.zc)), (unsigned)M, 1);
-    }
     s.fast = f;
     return UPPASD_GPU_OK;
 }
@@ -903,16 +605,6 @@ int structured_sync_state(Sim &s) {
 
 template <int NSH, int LC>
 static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
-    if constexpr (LC != 0) {
-        if (f->zmarch) {
-            if (phase & 1) zmarch<NSH, LC, 0, 2><<<f->zgrid, f->zblock, 0, st>>>(f->p);
-            if (phase & 2) {
-                if (f->master == 1) zmarch<NSH, LC, 1, 1><<<f->zgrid, f->zblock, 0, st>>>(f->p);
-                else zmarch<NSH, LC, 1, 2><<<f->zgrid, f->zblock, 0, st>>>(f->p);
-            }
-            return;
-        }
-    }
     if (phase & 1) stencil_predict<NSH, LC><<<f->grid, f->block, 0, st>>>(f->p);
     if (phase & 2) {
         if (f->master == 1) stencil_correct<NSH, 1, LC><<<f->grid, f->block, 0, st>>>(f->p);
