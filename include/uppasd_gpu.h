@@ -128,6 +128,28 @@ int uppasd_gpu_set_stream(uppasd_gpu_sim *s, void *cuda_stream);
  * ms[0] predictor kernel, ms[1] corrector kernel, ms[2] whole step. */
 int uppasd_gpu_time_kernels(uppasd_gpu_sim *s, int32_t nrep, double *ms);
 
+/* Allocation-free magnetisation sums.  This entry point has no counterpart in
+ * the reference; it is for callers that cannot call cudaMalloc: a host code
+ * that manages device memory through its own pool or arena and forbids
+ * allocations behind it, code that runs while a CUDA graph is being captured
+ * elsewhere in the process, or an embedding runtime that reserves the whole
+ * device up front.
+ *   d_emomM : device array of full moments in the reference layout
+ *             (3, natom, mensemble), FP64, owned by the caller;
+ *   d_out   : device array (4, mensemble), owned by the caller: total moment
+ *             x, y, z and |M| / natom per ensemble;
+ *   cuda_stream : cudaStream_t as void* (NULL = legacy default stream).
+ * It allocates nothing: its scratch is a fixed 192 KiB device array inside this
+ * library, which every GPU that loads the library keeps until the process
+ * exits.  Limit: mensemble <= 64 (larger values return UPPASD_GPU_EINVAL);
+ * natom is not limited.  The first call on each device looks up that array's
+ * device address (cudaGetSymbolAddress) with the device current, so make the
+ * first call on a device before any stream capture.  All calls share the
+ * array: calls that overlap on the GPU (different streams) race and must be
+ * serialised by the caller.  The result is asynchronous on `cuda_stream`. */
+int uppasd_gpu_moment_sums_noalloc(const double *d_emomM, int32_t natom, int32_t mensemble, double *d_out,
+                                   void *cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

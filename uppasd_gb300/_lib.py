@@ -59,6 +59,7 @@ SIGNATURES = {
     "uppasd_gpu_observables": [C.c_void_p, F64P, F64P, F64P],
     "uppasd_gpu_set_stream": [C.c_void_p, C.c_void_p],
     "uppasd_gpu_time_kernels": [C.c_void_p, C.c_int32, F64P],
+    "uppasd_gpu_moment_sums_noalloc": [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p],
 }
 
 _lib = None

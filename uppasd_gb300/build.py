@@ -29,6 +29,7 @@ UNITS = [
     ("observables.cu", ["--fmad=false"]),
     ("mc.cu", ["--fmad=false"]),
     ("llg_stencil.cu", []),
+    ("noalloc.cu", []),
 ]
 
 
