@@ -225,16 +225,14 @@ __device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
     return s.x < p.L1 && s.y < p.L2;
 }
 
-template <int NSH, int b, int LC>
-__device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
-    const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
-    const float4 me = p.mt[o];
+// Predictor update of one site from its field B: thermal field, Depondt damped
+// field, Rodrigues rotation; writes m_pred (with ghosts), b2eff and the thermal field.
+__device__ __forceinline__ void predict_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &me,
+                                               const float B[3]) {
     const int si = me.w != 0.f ? 1 : 0;
-    float B[3];
-    gather_b<NSH, b, LC>(p, p.mt, s.k, s.x, s.y, s.z, si, B);
     const long long step = *p.d_step + p.step_off;
     float zr[3];
-    normal3_f32_fast(p.seed, ref_site(p, b, s.x, s.y, s.z), s.k, step, kStreamLLG, zr);
+    normal3_f32_fast(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
     const float sg = p.sigma[si];
     const float e[3] = {me.x, me.y, me.z};
     const float th[3] = {zr[0] * sg, zr[1] * sg, zr[2] * sg};
@@ -242,14 +240,22 @@ __device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
     float bd[3], d[3];
     depondt_bdup(p.lam, e, bl, bd);
     rotation_delta(bd, e, p.dtg, d);
-    store_mirror(p, p.mp, s.k, b, s.x, s.y, s.z, make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w));
-    const long long u = uidx(p, s.k, b, s.x, s.y, s.z);
+    store_mirror(p, p.mp, k, b, x, y, z, make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w));
+    const long long u = uidx(p, k, b, x, y, z);
     p.b2x[u] = bd[0];
     p.b2y[u] = bd[1];
     p.b2z[u] = bd[2];
     p.thx[u] = th[0];
     p.thy[u] = th[1];
     p.thz[u] = th[2];
+}
+
+template <int NSH, int b, int LC>
+__device__ __forceinline__ void predict_site(const SParams &p, const Site &s) {
+    const float4 me = p.mt[pidx(p, s.k, b, s.x, s.y, s.z)];
+    float B[3];
+    gather_b<NSH, b, LC>(p, p.mt, s.k, s.x, s.y, s.z, me.w != 0.f ? 1 : 0, B);
+    predict_update(p, s.k, b, s.x, s.y, s.z, me, B);
 }
 
 template <int NSH, int LC>
@@ -275,14 +281,13 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
     e = fmaf(a, b, -p);
 }
 
-template <int NSH, int MASTER, int b, int LC>  // MASTER 1: FP64, 2: double-single
-__device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
-    const long long o = pidx(p, s.k, b, s.x, s.y, s.z);
-    const long long u = uidx(p, s.k, b, s.x, s.y, s.z);
-    const float4 mp = p.mp[o];
-    const int si = mp.w != 0.f ? 1 : 0;
-    float B[3];
-    gather_b<NSH, b, LC>(p, p.mp, s.k, s.x, s.y, s.z, si, B);
+// Corrector update of one site from the field B at the predictor: Depondt
+// average with b2eff, rotation of m(t), master update and renormalisation.
+template <int MASTER>  // MASTER 1: FP64, 2: double-single
+__device__ __forceinline__ void correct_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &mp,
+                                               const float B[3]) {
+    const long long o = pidx(p, k, b, x, y, z);
+    const long long u = uidx(p, k, b, x, y, z);
     const float ep[3] = {mp.x, mp.y, mp.z};
     float bl[3] = {B[0] + p.thx[u], B[1] + p.thy[u], B[2] + p.thz[u]};
     float bd[3];
@@ -342,7 +347,15 @@ __device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
         p.loz[u] = lo[2];
         out = make_float4(hi[0], hi[1], hi[2], mt.w);
     }
-    store_mirror(p, p.mt, s.k, b, s.x, s.y, s.z, out);
+    store_mirror(p, p.mt, k, b, x, y, z, out);
+}
+
+template <int NSH, int MASTER, int b, int LC>
+__device__ __forceinline__ void correct_site(const SParams &p, const Site &s) {
+    const float4 mp = p.mp[pidx(p, s.k, b, s.x, s.y, s.z)];
+    float B[3];
+    gather_b<NSH, b, LC>(p, p.mp, s.k, s.x, s.y, s.z, mp.w != 0.f ? 1 : 0, B);
+    correct_update<MASTER>(p, s.k, b, s.x, s.y, s.z, mp, B);
 }
 
 template <int NSH, int MASTER, int LC>
@@ -351,6 +364,127 @@ __global__ void __launch_bounds__(256) stencil_correct(SParams p) {
     if (!site_of_thread(p, s)) return;
     if (s.b == 0) correct_site<NSH, MASTER, 0, LC>(p, s);
     else correct_site<NSH, MASTER, 1, LC>(p, s);
+}
+
+// ---------------------------------------------------------------------------
+// z-blocked gather: a thread produces NZ sites of one sublattice stacked in z.
+// Neighbour points shared by several of its sites are loaded once (about 28
+// loads per site instead of 50 for the four-shell stencil, NZ = 4).  The point
+// list and the (site, shell) pairs each point feeds are built by the constexpr
+// evaluator and expanded with integer sequences, so every offset, coupling
+// register and accumulator index is a compile-time constant.
+struct ZbPt {
+    int8_t bj, dx, dy, dz;
+    uint8_t first, count;
+};
+struct ZbPair {
+    int8_t q, sh;
+};
+struct ZbTables {
+    ZbPt pts[256];
+    ZbPair pairs[256];
+    int npts, npairs;
+};
+
+__host__ __device__ constexpr ZbTables make_zb(int nsh, int b, int nz) {
+    ZbTables t{};
+    int np = 0, nq = 0;
+    for (int bj = 0; bj < 2; ++bj)
+        for (int zz = -2; zz <= nz + 1; ++zz)
+            for (int dy = -2; dy <= 2; ++dy)
+                for (int dx = -2; dx <= 2; ++dx) {
+                    const int first = nq;
+                    for (int q = 0; q < nz; ++q)
+                        for (int s = 0; s < nb_of_shells(nsh); ++s) {
+                            const St e = stencil_entry(b, s);
+                            if (e.bj == bj && e.dx == dx && e.dy == dy && q + e.dz == zz)
+                                t.pairs[nq++] = ZbPair{(int8_t)q, e.sh};
+                        }
+                    if (nq > first)
+                        t.pts[np++] = ZbPt{(int8_t)bj, (int8_t)dx, (int8_t)dy, (int8_t)zz, (uint8_t)first,
+                                           (uint8_t)(nq - first)};
+                }
+    t.npts = np;
+    t.npairs = nq;
+    return t;
+}
+
+template <int NSH, int B, int NZ>
+struct ZB {
+    static constexpr ZbTables t = make_zb(NSH, B, NZ);
+};
+
+template <int NSH, int B, int NZ, int I>
+__device__ __forceinline__ void zb_pair(const float4 &v, const float (&cA)[NZ][4], const float (&cD)[NZ][4],
+                                        float (&acc)[NZ][3]) {
+    constexpr ZbPair pr = ZB<NSH, B, NZ>::t.pairs[I];
+    const float c = fmaf(v.w, cD[pr.q][pr.sh - 1], cA[pr.q][pr.sh - 1]);
+    acc[pr.q][0] = fmaf(c, v.x, acc[pr.q][0]);
+    acc[pr.q][1] = fmaf(c, v.y, acc[pr.q][1]);
+    acc[pr.q][2] = fmaf(c, v.z, acc[pr.q][2]);
+}
+
+template <int NSH, int B, int NZ, int FIRST, int... R>
+__device__ __forceinline__ void zb_pairs(const float4 &v, const float (&cA)[NZ][4], const float (&cD)[NZ][4],
+                                         float (&acc)[NZ][3], std::integer_sequence<int, R...>) {
+    (zb_pair<NSH, B, NZ, FIRST + R>(v, cA, cD, acc), ...);
+}
+
+template <int NSH, int B, int NZ, int LC, int Q>
+__device__ __forceinline__ void zb_point(const float4 *base0, const float4 *base1, const float (&cA)[NZ][4],
+                                         const float (&cD)[NZ][4], float (&acc)[NZ][3]) {
+    constexpr ZbPt pt = ZB<NSH, B, NZ>::t.pts[Q];
+    constexpr int off = pt.dz * pitch2(LC) + pt.dy * pitch1(LC) + pt.dx;
+    const float4 v = __ldg((pt.bj ? base1 : base0) + off);
+    zb_pairs<NSH, B, NZ, pt.first>(v, cA, cD, acc, std::make_integer_sequence<int, pt.count>{});
+}
+
+template <int NSH, int B, int NZ, int LC, int... Q>
+__device__ __forceinline__ void zb_points(const float4 *base0, const float4 *base1, const float (&cA)[NZ][4],
+                                          const float (&cD)[NZ][4], float (&acc)[NZ][3],
+                                          std::integer_sequence<int, Q...>) {
+    (zb_point<NSH, B, NZ, LC, Q>(base0, base1, cA, cD, acc), ...);
+}
+
+template <int NSH, int B, int NZ, int LC, int KIND, int MASTER>
+__device__ __forceinline__ void zb_sites(const SParams &p, int k, int x, int y, int z0) {
+    constexpr int P1 = pitch1(LC), P2 = pitch2(LC);
+    const float4 *m = KIND == 0 ? p.mt : p.mp;
+    const long long own = (long long)(z0 + 2) * P2 + (long long)(y + 2) * P1 + (x + XOFF);
+    const float4 *base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
+    const float4 *base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
+    float4 me[NZ];
+    float cA[NZ][4], cD[NZ][4], acc[NZ][3];
+#pragma unroll
+    for (int q = 0; q < NZ; ++q) {
+        me[q] = (B ? base1 : base0)[q * P2];
+        const int si = me[q].w != 0.f ? 1 : 0;
+#pragma unroll
+        for (int s = 0; s < 4; ++s) {
+            cA[q][s] = si ? p.cA[s][1] : p.cA[s][0];
+            cD[q][s] = si ? p.cD[s][1] : p.cD[s][0];
+        }
+        acc[q][0] = acc[q][1] = acc[q][2] = 0.f;
+    }
+    zb_points<NSH, B, NZ, LC>(base0, base1, cA, cD, acc, std::make_integer_sequence<int, ZB<NSH, B, NZ>::t.npts>{});
+#pragma unroll
+    for (int q = 0; q < NZ; ++q) {
+        const float Bf[3] = {acc[q][0] + p.ext[0], acc[q][1] + p.ext[1], acc[q][2] + p.ext[2]};
+        if (KIND == 0) predict_update(p, k, B, x, y, z0 + q, me[q], Bf);
+        else correct_update<MASTER>(p, k, B, x, y, z0 + q, me[q], Bf);
+    }
+}
+
+template <int NSH, int NZ, int LC, int KIND, int MASTER>
+__global__ void __launch_bounds__(256) stencil_zblock(SParams p) {
+    const int nyt = (p.L2 + blockDim.y - 1) / blockDim.y;
+    const int x = threadIdx.x;
+    const int y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
+    const int z0 = (blockIdx.x / nyt) * NZ;
+    const int k = blockIdx.z;
+    if (x >= p.L1 || y >= p.L2) return;
+    if (blockIdx.y == 0) zb_sites<NSH, 0, NZ, LC, KIND, MASTER>(p, k, x, y, z0);
+    else zb_sites<NSH, 1, NZ, LC, KIND, MASTER>(p, k, x, y, z0);
 }
 
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
@@ -605,6 +739,17 @@ int structured_sync_state(Sim &s) {
 
 template <int NSH, int LC>
 static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
+    if constexpr (LC != 0) {
+        // compiled cubic sizes: NZ sites per thread stacked in z (NZ divides LC)
+        constexpr int NZ = LC % 4 == 0 ? 4 : 2;
+        dim3 grid((unsigned)(((f->p.L2 + f->block.y - 1) / f->block.y) * (LC / NZ)), 2, (unsigned)f->p.nens);
+        if (phase & 1) stencil_zblock<NSH, NZ, LC, 0, 2><<<grid, f->block, 0, st>>>(f->p);
+        if (phase & 2) {
+            if (f->master == 1) stencil_zblock<NSH, NZ, LC, 1, 1><<<grid, f->block, 0, st>>>(f->p);
+            else stencil_zblock<NSH, NZ, LC, 1, 2><<<grid, f->block, 0, st>>>(f->p);
+        }
+        return;
+    }
     if (phase & 1) stencil_predict<NSH, LC><<<f->grid, f->block, 0, st>>>(f->p);
     if (phase & 2) {
         if (f->master == 1) stencil_correct<NSH, 1, LC><<<f->grid, f->block, 0, st>>>(f->p);
