@@ -740,13 +740,19 @@ int structured_sync_state(Sim &s) {
 template <int NSH, int LC>
 static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
     if constexpr (LC != 0) {
-        // compiled cubic sizes: NZ sites per thread stacked in z (NZ divides LC)
-        constexpr int NZ = LC % 4 == 0 ? 4 : 2;
-        dim3 grid((unsigned)(((f->p.L2 + f->block.y - 1) / f->block.y) * (LC / NZ)), 2, (unsigned)f->p.nens);
-        if (phase & 1) stencil_zblock<NSH, NZ, LC, 0, 2><<<grid, f->block, 0, st>>>(f->p);
+        // compiled cubic sizes: NZ sites per thread stacked in z (NZ divides LC).
+        // The corrector's per-site update (master renormalisation) is heavier, so it
+        // takes fewer sites per thread to keep occupancy.
+        constexpr int NZP = LC % 4 == 0 ? 4 : 2;
+        constexpr int NZC = 2;
+        const unsigned nyt = (unsigned)((f->p.L2 + f->block.y - 1) / f->block.y);
+        if (phase & 1)
+            stencil_zblock<NSH, NZP, LC, 0, 2>
+                <<<dim3(nyt * (LC / NZP), 2, (unsigned)f->p.nens), f->block, 0, st>>>(f->p);
         if (phase & 2) {
-            if (f->master == 1) stencil_zblock<NSH, NZ, LC, 1, 1><<<grid, f->block, 0, st>>>(f->p);
-            else stencil_zblock<NSH, NZ, LC, 1, 2><<<grid, f->block, 0, st>>>(f->p);
+            const dim3 g(nyt * (LC / NZC), 2, (unsigned)f->p.nens);
+            if (f->master == 1) stencil_zblock<NSH, NZC, LC, 1, 1><<<g, f->block, 0, st>>>(f->p);
+            else stencil_zblock<NSH, NZC, LC, 1, 2><<<g, f->block, 0, st>>>(f->p);
         }
         return;
     }
