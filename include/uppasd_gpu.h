@@ -150,6 +150,62 @@ int uppasd_gpu_time_kernels(uppasd_gpu_sim *s, int32_t nrep, double *ms);
 int uppasd_gpu_moment_sums_noalloc(const double *d_emomM, int32_t natom, int32_t mensemble, double *d_out,
                                    void *cuda_stream);
 
+/* ---- Batched replica Monte Carlo ------------------------------------------
+ * Many bcc J1/J2 Heisenberg replicas (temperatures x sizes, uneven atom counts)
+ * swept together by one persistent cooperative launch, replayed from a captured
+ * CUDA graph.  This is the replica table the reference's temperature loops feed
+ * one system at a time: mc_mphase (MonteCarlo/mc_driver.f90:234-420) per
+ * temperature, and the replica list of parallel tempering
+ * (MonteCarlo/pt_driver.f90:58-367).  The single-spin updates are flip_h and
+ * flip_a (MonteCarlo/montecarlo_common.f90:139-200, 371-422) over checkerboard
+ * colours (sublattice x cell parity); observables are E (mRy/atom, as
+ * calc_energy, Hamiltonian/energy.f90:60-405) and M (muB/atom, as calc_mavrg,
+ * Measurement/measurements.f90:211-235) after every sweep, accumulated in FP64. */
+typedef struct uppasd_gpu_mcbatch uppasd_gpu_mcbatch;
+
+/* nrep replicas; replica r: L[r]^3 bcc cells (2 L^3 atoms, L even, 4..1024),
+ * temperature[r] (K), heatbath[r] (1 heat bath, 0 Metropolis; NULL = all heat
+ * bath).  j_shells_mry[2] = J1, J2 (mRy), mom = moment (muB), bfield[3] (T or
+ * NULL).  Initial spins are uniform on the sphere from `seed`.  series_len > 0
+ * keeps a ring buffer of (E, |M|) per replica and measured sweep;
+ * max_sweeps_per_launch bounds the sweeps of one persistent launch. */
+int uppasd_gpu_mcbatch_create(int32_t nrep, const int32_t *L, const double *temperature, const int32_t *heatbath,
+                              const double *j_shells_mry, double mom, const double *bfield, uint64_t seed,
+                              int32_t series_len, int32_t max_sweeps_per_launch, uppasd_gpu_mcbatch **out);
+int uppasd_gpu_mcbatch_destroy(uppasd_gpu_mcbatch *b);
+int uppasd_gpu_mcbatch_set_stream(uppasd_gpu_mcbatch *b, void *cuda_stream);
+/* Schedule: register build of the sweep kernel (0: unconstrained, 1: sized for 3
+ * CTAs per SM, 2: for 4), threads per CTA (multiple of 32, <= 256) and CTAs per
+ * replica (>= 1 each, total within the co-resident limit). */
+int uppasd_gpu_mcbatch_set_schedule(uppasd_gpu_mcbatch *b, int32_t reg_build, int32_t threads,
+                                    const int32_t *ctas_per_rep);
+int uppasd_gpu_mcbatch_get_schedule(uppasd_gpu_mcbatch *b, int32_t *reg_build, int32_t *threads,
+                                    int32_t *ctas_per_rep);
+/* Autotuner: times register builds, block sizes and CTAs per SM, rebalances the CTAs per replica
+ * from per-group times, installs the fastest; cached per device and replica
+ * table in cache_path (NULL = no cache).  Its sweeps are real sweeps (the chain
+ * advances; use it during thermalisation). */
+int uppasd_gpu_mcbatch_autotune(uppasd_gpu_mcbatch *b, int32_t sweeps_per_trial, const char *cache_path,
+                                float *best_ms_per_sweep);
+/* nsweeps sweeps in graph replays of sweeps_per_launch; measure != 0 adds every
+ * sweep to the moments and the series.  Synchronises and checks the barrier
+ * error flag. */
+int uppasd_gpu_mcbatch_run(uppasd_gpu_mcbatch *b, int64_t nsweeps, int32_t sweeps_per_launch, int32_t measure);
+/* Same, asynchronous on the batch's stream; uppasd_gpu_mcbatch_check synchronises. */
+int uppasd_gpu_mcbatch_enqueue(uppasd_gpu_mcbatch *b, int64_t nsweeps, int32_t sweeps_per_launch, int32_t measure);
+int uppasd_gpu_mcbatch_check(uppasd_gpu_mcbatch *b);
+/* acc (nrep, 10): n, sum E, E^2, |M|, M^2, M^4, Mx, My, Mz, |M|^3 over measured sweeps;
+ * nsample (nrep); last (nrep, 4): E, Mx, My, Mz after the latest sweep.  Any may be NULL. */
+int uppasd_gpu_mcbatch_stats(uppasd_gpu_mcbatch *b, double *acc, int64_t *nsample, double *last);
+/* (nrep, series_len, 2) ring buffer of (E, |M|); sample k of replica r at k % series_len. */
+int uppasd_gpu_mcbatch_series(uppasd_gpu_mcbatch *b, double *series);
+int uppasd_gpu_mcbatch_reset_stats(uppasd_gpu_mcbatch *b);
+/* Unit spins, replica-major, each in the reference layout (3, 2 L^3), site b + 2 (x + L (y + L z)). */
+int uppasd_gpu_mcbatch_get_spins(uppasd_gpu_mcbatch *b, double *emom);
+int uppasd_gpu_mcbatch_put_spins(uppasd_gpu_mcbatch *b, const double *emom);
+/* Sweep counter (the Philox step of the next sweep). */
+int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
+
 #ifdef __cplusplus
 }
 #endif

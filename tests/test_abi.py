@@ -97,3 +97,29 @@ def test_null_arguments(lib):
     assert lib.uppasd_gpu_finalize(None) == -1
     assert lib.uppasd_gpu_sd_run(None, 1) == -1
     assert lib.uppasd_gpu_mc_run(None, b"H", 1.0, 1) == -1
+
+
+def test_mcbatch_rejects_bad_tables(lib):
+    from uppasd_gb300 import _lib
+    js = np.array([1.3, 0.7])
+    h = C.c_void_p()
+
+    def create(L, T, nrep=None, spl=64, mom=2.2):
+        L = np.ascontiguousarray(L, dtype=np.int32)
+        T = np.ascontiguousarray(T, dtype=np.float64)
+        n = len(L) if nrep is None else nrep
+        return lib.uppasd_gpu_mcbatch_create(n, L.ctypes.data_as(_lib.I32P), T.ctypes.data_as(_lib.F64P), None,
+                                             js.ctypes.data_as(_lib.F64P), mom, None, 1, 0, spl, C.byref(h))
+
+    assert create([5], [500.0]) == -1          # odd L
+    assert create([2], [500.0]) == -1          # too small
+    assert create([8], [-1.0]) == -1           # negative temperature
+    assert create([8], [500.0], nrep=0) == -1  # empty table
+    assert create([8], [500.0], spl=0) == -1   # no sweeps per launch
+    assert create([8], [500.0], mom=0.0) == -1
+    assert h.value is None
+    assert lib.uppasd_gpu_last_error()
+    for fn, args in [("uppasd_gpu_mcbatch_run", (None, 1, 1, 0)), ("uppasd_gpu_mcbatch_destroy", (None,)),
+                     ("uppasd_gpu_mcbatch_stats", (None, None, None, None)), ("uppasd_gpu_mcbatch_check", (None,)),
+                     ("uppasd_gpu_mcbatch_get_spins", (None, None)), ("uppasd_gpu_mcbatch_set_sweep", (None, 0))]:
+        assert getattr(lib, fn)(*args) == -1, fn

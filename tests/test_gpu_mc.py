@@ -57,8 +57,10 @@ def test_statistics_match_reference_chain(mode):
     ntherm, nmeas = 500, 3000
     # reference chain on the CPU (oracle), its own RNG streams
     o = po.Oracle(lat)
-    e0 = np.zeros((1, lat.natom, 3))
-    e0[..., 2] = 1.0
+    # random start: from an exactly collinear state flip_h's field frame degenerates
+    # (zcp = zsp = 0 when the field lies on z) and the heat bath never leaves the z axis
+    e0 = np.random.default_rng(17).normal(size=(1, lat.natom, 3))
+    e0 /= np.linalg.norm(e0, axis=-1, keepdims=True)
     o.set_moments(e0)
     o.mt = po.OrcMT()
     o.lib.orc_mt_init(C.byref(o.mt), 17)

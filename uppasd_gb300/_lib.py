@@ -60,6 +60,23 @@ SIGNATURES = {
     "uppasd_gpu_set_stream": [C.c_void_p, C.c_void_p],
     "uppasd_gpu_time_kernels": [C.c_void_p, C.c_int32, F64P],
     "uppasd_gpu_moment_sums_noalloc": [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p],
+    # batched replica Monte Carlo
+    "uppasd_gpu_mcbatch_create": [C.c_int32, I32P, F64P, I32P, F64P, C.c_double, F64P, C.c_uint64, C.c_int32,
+                                  C.c_int32, C.POINTER(C.c_void_p)],
+    "uppasd_gpu_mcbatch_destroy": [C.c_void_p],
+    "uppasd_gpu_mcbatch_set_stream": [C.c_void_p, C.c_void_p],
+    "uppasd_gpu_mcbatch_set_schedule": [C.c_void_p, C.c_int32, C.c_int32, I32P],
+    "uppasd_gpu_mcbatch_get_schedule": [C.c_void_p, I32P, I32P, I32P],
+    "uppasd_gpu_mcbatch_autotune": [C.c_void_p, C.c_int32, C.c_char_p, C.POINTER(C.c_float)],
+    "uppasd_gpu_mcbatch_run": [C.c_void_p, C.c_int64, C.c_int32, C.c_int32],
+    "uppasd_gpu_mcbatch_enqueue": [C.c_void_p, C.c_int64, C.c_int32, C.c_int32],
+    "uppasd_gpu_mcbatch_check": [C.c_void_p],
+    "uppasd_gpu_mcbatch_stats": [C.c_void_p, F64P, C.POINTER(C.c_int64), F64P],
+    "uppasd_gpu_mcbatch_series": [C.c_void_p, F64P],
+    "uppasd_gpu_mcbatch_reset_stats": [C.c_void_p],
+    "uppasd_gpu_mcbatch_get_spins": [C.c_void_p, F64P],
+    "uppasd_gpu_mcbatch_put_spins": [C.c_void_p, F64P],
+    "uppasd_gpu_mcbatch_set_sweep": [C.c_void_p, C.c_int64],
 }
 
 _lib = None

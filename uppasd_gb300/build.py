@@ -30,6 +30,7 @@ UNITS = [
     ("mc.cu", ["--fmad=false"]),
     ("llg_stencil.cu", []),
     ("noalloc.cu", []),
+    ("mc_batch.cu", []),
 ]
 
 
