@@ -14,6 +14,16 @@ HBM; `e2e` is the same metric through the C ABI with the spin state copied
 from pinned host memory before, and back after, each block of `--e2e-inner`
 steps (the drop-in's measurement interval).
 
+The same JSON line carries an "mc" object for the batched Monte Carlo
+temperature sweep: 64 bcc J1/J2 replicas (16 temperatures 600-1400 K x L = 16,
+24, 32, 48 cells; 8,192 to 221,184 atoms each, 5,160,960 spins), checkerboard
+heat bath, 10^4 thermalisation + 10^5 measured sweeps in one persistent launch
+per 250 sweeps replayed from a CUDA graph, autotuned schedule.  Its headline is
+independent samples/s = sum_r (sweeps/s) / (2 tau_int,r), tau_int the larger of
+the Sokal-windowed times of E and |M| per replica, against the plain GPU heat
+bath (one launch per colour per replica, the same Markov chain and so the same
+tau_int) timed on the same sizes.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 """
 from __future__ import annotations
@@ -220,7 +230,170 @@ def run_reference(args, w):
             "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
                              "sample": f"{args.steps} steps of 1 ensemble ({lat1.natom} atoms) per run"},
             "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if not args.no_mc:
+        line["mc"] = {"cpu_baseline": mc_cpu_baseline()}
     print(json.dumps(line), flush=True)
+
+
+MC_LS = (16, 24, 32, 48)
+MC_T = (600.0, 1400.0, 16)
+MC_J = (1.3, 0.7)
+
+
+def mc_table():
+    Ts = np.linspace(*MC_T)
+    return [l for l in MC_LS for _ in Ts], [float(t) for _ in MC_LS for t in Ts]
+
+
+def _mc_cpu_worker(job):
+    """One replica of the reference chain (random-permutation heat bath, mtprng +
+    ziggurat) on one core for about `seconds`: spin updates per second."""
+    L, T, seconds, seed = job
+    from oracle import pyoracle as po
+    from uppasd_gb300 import lattice
+
+    lat = lattice.bcc(L, list(MC_J), 2.2)
+    o = po.Oracle(lat, threads=1)
+    rng = np.random.default_rng(seed)
+    e0 = rng.normal(size=(1, lat.natom, 3))
+    e0 /= np.linalg.norm(e0, axis=-1, keepdims=True)
+    o.set_moments(e0)
+    import ctypes as C
+
+    o.mt = po.OrcMT()
+    o.lib.orc_mt_init(C.byref(o.mt), seed)
+    o.setup_ziggurat(seed)
+    iflip = o.choose_random_atom_x()
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.mc_sweep_ref("H", T, iflip)
+        n += 1
+        dt = time.perf_counter() - t0
+        if dt >= seconds:
+            break
+    return lat.natom * n / dt, n
+
+
+def mc_cpu_baseline(seconds=10.0):
+    """The reference's MC path restated (oracle) on the host cores: one process per
+    core, each sweeping one replica of the table (the reference runs one
+    replica per thread; its OpenMP site loop is racy)."""
+    import multiprocessing as mp
+
+    L, T = mc_table()
+    ncores = os.cpu_count() or 1
+    jobs = [(L[i * len(L) // ncores], T[i * len(L) // ncores], seconds, 11 + i) for i in range(ncores)]
+    with mp.get_context("spawn").Pool(ncores) as pool:
+        res = pool.map(_mc_cpu_worker, jobs)
+    return {"value": float(sum(r[0] for r in res)), "unit": "spin-updates/s", "cores": ncores, "kind": "port",
+            "sample": f"{ncores} replicas of the table (one per core), {seconds:.0f} s of heat-bath sweeps each"}
+
+
+def run_mc(args, world, rank, peak, peak_kind):
+    """Batched replica MC against the plain GPU heat bath (see the module docstring)."""
+    import torch
+
+    from uppasd_gb300 import analysis, lattice
+    from uppasd_gb300.batch import DEFAULT_CACHE, ReplicaBatch
+    from uppasd_gb300.simulation import GpuSimulation
+
+    L, T = mc_table()
+    spl = 250
+    b = ReplicaBatch(L, T, heatbath=1, j_shells_mry=MC_J, seed=31 + rank, series_len=args.mc_meas,
+                     max_sweeps_per_launch=spl)
+    tuned = b.autotune(20, cache=DEFAULT_CACHE)
+    bld, thr, ctas = b.schedule()
+    b.run(args.mc_therm, spl)
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    b.run(0, spl, measure=True)  # sets the measuring flag before the timed region
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    dist_barrier(world)
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    b.enqueue(args.mc_meas, spl, measure=True)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    b.check()
+    dist_barrier(world)
+    ms = dist_max(ev0.elapsed_time(ev1), world)
+    sweeps_s = args.mc_meas / (ms * 1e-3)
+    tau = b.tau_int()
+    st = b.stats()
+    natoms = np.asarray(b.natoms, dtype=np.float64)
+    indep = float(np.sum(sweeps_s / (2.0 * tau))) * world
+    updates = float(natoms.sum()) * sweeps_s * world
+    nlaunch = -(-args.mc_meas // spl)
+    b.close()
+    # plain GPU heat bath: the same chain, one launch per colour, one replica at a time
+    plain_sweeps_s = {}
+    for Lv in MC_LS:
+        lat = lattice.bcc(Lv, list(MC_J), 2.2)
+        e0 = random_state(1, lat.natom, seed=3)
+        sim = GpuSimulation(lat, emom=e0, seed=5)
+        sim.set_stream(stream.cuda_stream)
+        sim.relax("H", 1000.0, 20)
+        n = 200
+        torch.cuda.synchronize()
+        e0v, e1v = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0v.record(stream)
+        sim.relax("H", 1000.0, n)
+        e1v.record(stream)
+        torch.cuda.synchronize()
+        plain_sweeps_s[Lv] = n / (e0v.elapsed_time(e1v) * 1e-3)
+        sim.close()
+    # the plain path shares the GPU between replicas one at a time: a sweep of the
+    # whole table costs sum_r 1/rate_r, and each replica advances one sweep per table sweep
+    table_sweep_s = float(np.sum([1.0 / plain_sweeps_s[l] for l in L]))
+    plain_indep = float(np.sum((1.0 / table_sweep_s) / (2.0 * tau))) * world
+    # algorithmic bytes: 6 s per spin update (read and write 3 FP32 components)
+    per_launch_bytes = 24.0 * natoms.sum() * spl
+    ms_launch = ms / nlaunch
+    achieved = per_launch_bytes / (ms_launch * 1e-3) / 1e9
+    out = {
+        "metric": "MC independent samples/s (batched heat bath)", "value": indep, "unit": "samples/s",
+        "plain_gpu_heat_bath": plain_indep, "speedup_vs_plain": indep / plain_indep,
+        "spin_updates_per_s": updates, "sweeps_per_s_per_replica": sweeps_s, "ms_per_sweep": ms / args.mc_meas,
+        "tau_int": {"min": float(tau.min()), "max": float(tau.max()), "median": float(np.median(tau))},
+        "plain_sweeps_per_s": {str(k): v for k, v in plain_sweeps_s.items()},
+        "plain_table_sweep_ms": table_sweep_s * 1e3,
+        "workload": "bcc J1=1.3 J2=0.7 mRy, 64 replicas: 16 T in 600-1400 K x L=16,24,32,48 (5,160,960 spins), "
+                    "checkerboard heat bath",
+        "thermalisation_sweeps": args.mc_therm, "measured_sweeps": args.mc_meas, "sweeps_per_launch": spl,
+        "schedule": {"register_build": bld, "threads": thr, "ctas": int(ctas.sum()),
+                     "ctas_per_L": {str(l): int(ctas[i * 16]) for i, l in enumerate(MC_LS)},
+                     "tuned_ms_per_sweep": tuned},
+        "gpu_launches": 3 * nlaunch,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": profiled_traffic("mb_sweeps:mc64"), "kernel": "mb_sweeps",
+                     "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
+                     "note": "24 B per spin update; the 83 MB spin pool is L2-resident"},
+        "observables": {f"L{l}": {"T": [round(t, 1) for t in T[i * 16:(i + 1) * 16]],
+                                  "binder": [round(float(u), 5) for u in st["binder"][i * 16:(i + 1) * 16]],
+                                  "M": [round(float(m), 5) for m in st["M"][i * 16:(i + 1) * 16]],
+                                  "E": [round(float(e), 5) for e in st["E"][i * 16:(i + 1) * 16]]}
+                        for i, l in enumerate(MC_LS)},
+    }
+    return out
+
+
+def run_mc_only(args):
+    """The Monte Carlo section alone (profiling and quick checks)."""
+    import torch
+
+    world, rank = dist_setup()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from uppasd_gb300 import build as b
+
+    b.build()
+    peak, peak_kind = measured_peaks()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        mc = run_mc(args, world, rank, peak, peak_kind)
+    if rank == 0:
+        if not args.no_cpu_baseline:
+            mc["cpu_baseline"] = mc_cpu_baseline()
+        mc["clocks"] = clk.summary()
+        print(json.dumps(mc), flush=True)
 
 
 def _make_sim(lat, w, prec, seed, e0):
@@ -334,9 +507,14 @@ def run_gb300(args, w):
                 "kernel_ms": kt2, "roofline": _roofline(kt2, nspin, 8, ms2 / args.steps, peak, peak_kind, None)}
         except Exception as exc:
             variants["double_single_master"] = {"error": str(exc)}
+    mc = None
+    if not args.no_mc:
+        mc = run_mc(args, world, rank, peak, peak_kind)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, lat, e0, os.cpu_count() or 1)
+        if mc is not None:
+            mc["cpu_baseline"] = mc_cpu_baseline()
     if rank != 0:
         return
     line = {
@@ -355,9 +533,10 @@ def run_gb300(args, w):
                 "d2h_bytes_per_step": host.nbytes, "inner_steps_per_call": inner,
                 "note": "put_moments(pinned host) + sd_run(inner steps) + get_moments per e2e step"},
         "clocks": clk.summary(),
-        "gpu_launches": launches,
+        "gpu_launches": launches + (mc["gpu_launches"] if mc else 0),
         "kernel_ms": kt,
         "variants": variants,
+        "mc": mc,
     }
     print(json.dumps(line), flush=True)
 
@@ -374,12 +553,18 @@ def main():
     ap.add_argument("--e2e-rounds", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--variants", action="store_true", help="also time the double-single master variant")
+    ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
+    ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
+    ap.add_argument("--mc-therm", type=int, default=10000)
+    ap.add_argument("--mc-meas", type=int, default=100000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     w = WORKLOADS[args.workload]
     if args.impl == "reference":
         run_reference(args, w)
+    elif args.mc_only:
+        run_mc_only(args)
     else:
         run_gb300(args, w)
 
