@@ -206,6 +206,15 @@ int uppasd_gpu_mcbatch_put_spins(uppasd_gpu_mcbatch *b, const double *emom);
 /* Sweep counter (the Philox step of the next sweep). */
 int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
 
+/* ---- BF16 tensor-core GEMM (tcgen05, TMEM accumulator, TMA operands) -------
+ * No counterpart in the reference: the dense contraction of the learned patch
+ * proposal.  C (M x N) = A (M x K) B (N x K)^T on host buffers (bf16 as raw
+ * uint16 bit patterns, row-major), FP32 accumulation; M % 128 == 0, K % 64 == 0,
+ * N % bn == 0, bn in {64, 128, 256}.  epilogue: 0 Cf = AB^T; 1 Cf = AB^T + bias;
+ * 2 Cb = tanh(AB^T + bias) in bf16; 3 Cb = AB^T * (1 - Y^2) in bf16 (Y: M x N bf16). */
+int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_t *A, const uint16_t *B, const float *bias,
+                       const uint16_t *Y, int32_t epilogue, int32_t bn, float *Cf, uint16_t *Cb);
+
 #ifdef __cplusplus
 }
 #endif

@@ -31,6 +31,7 @@ UNITS = [
     ("llg_stencil.cu", []),
     ("noalloc.cu", []),
     ("mc_batch.cu", []),
+    ("tc_host.cu", []),
 ]
 
 
