@@ -215,6 +215,41 @@ int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
 int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_t *A, const uint16_t *B, const float *bias,
                        const uint16_t *Y, int32_t epilogue, int32_t bn, float *Cf, uint16_t *Cb);
 
+/* ---- Learned 4x4-patch proposal with exact Metropolis-Hastings -------------
+ * No counterpart in the reference; it acts beside the heat bath of mc_mphase
+ * (uppasd_gpu_mc_run) on the same simulation's spins.  The simulation must be
+ * an L x L square lattice, one atom per cell, site i = x + L y, L % 8 == 0 and
+ * Mensemble * (L/8)^2 a multiple of 128.  Network: MADE over the patch's four
+ * sub-lattice groups; input the 8 x 8 window (192 features), 3 tanh layers of
+ * 256, output eta = kappa mu per patch spin (48 of 64 used), eta = eta_scale *
+ * output; BF16 tensor-core GEMMs with FP32 accumulation.  data_capacity = rows
+ * of the training-window buffer (0 = none).  Parameter vector layout: W1
+ * (256 x 192), W2, W3 (256 x 256), W4 (64 x 256), b1, b2, b3 (256), b4 (64). */
+typedef struct uppasd_gpu_proposal uppasd_gpu_proposal;
+int uppasd_gpu_proposal_create(uppasd_gpu_sim *s, int32_t L, float eta_scale, int32_t data_capacity, uint64_t seed,
+                               uppasd_gpu_proposal **out);
+int uppasd_gpu_proposal_destroy(uppasd_gpu_proposal *p);
+int uppasd_gpu_proposal_nparams(uppasd_gpu_proposal *p, int64_t *n);
+int uppasd_gpu_proposal_get_params(uppasd_gpu_proposal *p, float *params);
+/* Rejects parameter vectors whose masked (non-autoregressive) weights are non-zero. */
+int uppasd_gpu_proposal_set_params(uppasd_gpu_proposal *p, const float *params);
+/* The 0/1 autoregressive masks of W1..W4 (weights part of the parameter layout). */
+int uppasd_gpu_proposal_get_masks(uppasd_gpu_proposal *p, float *masks);
+/* Network outputs (rows x 64) for explicit windows (rows x 192, fp32, rounded to bf16). */
+int uppasd_gpu_proposal_forward(uppasd_gpu_proposal *p, const float *x, int32_t rows, float *out);
+/* Mean negative log-likelihood of the windows' patches and its gradient (parameter layout). */
+int uppasd_gpu_proposal_loss_grad(uppasd_gpu_proposal *p, const float *x, int32_t rows, double *loss,
+                                  float *grad);
+/* Append the windows of every patch of every chain of the simulation's current spins. */
+int uppasd_gpu_proposal_collect(uppasd_gpu_proposal *p);
+/* nsteps Adam steps on random minibatches of `rows` collected windows; losses[nsteps] or NULL. */
+int uppasd_gpu_proposal_train(uppasd_gpu_proposal *p, int32_t nsteps, int32_t rows, float lr, double *losses);
+/* nsweeps learned sweeps (each: the four patch colours) at `temperature` (K) on the
+ * simulation's spins; counts of accepted and proposed patch moves and the summed
+ * energy change of accepted moves (J). */
+int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_t nsweeps, int64_t *accepted,
+                              int64_t *proposed, double *dE_accepted);
+
 #ifdef __cplusplus
 }
 #endif

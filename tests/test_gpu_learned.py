@@ -1,0 +1,131 @@
+"""Learned 4x4-patch proposal on the GPU (tcgen05 BF16 network, exact MH):
+
+* forward outputs and the loss gradient of the hand-written backward pass
+  against the CPU oracle (oracle/made_oracle.py) with the same bf16 rounding
+  points (tolerances stated per check);
+* training on heat-bath windows lowers the loss and keeps masked weights zero;
+* the summed energy change of accepted moves equals the measured change of
+  the total energy (the MH kernel's dE is exact);
+* heat bath + learned moves sample the same distribution as the plain heat
+  bath: E and |M| within 3 sigma over independent chains.
+"""
+import numpy as np
+import pytest
+
+from oracle import made_oracle as mo
+from uppasd_gb300 import lattice
+from uppasd_gb300.learned import LearnedProposal
+from uppasd_gb300.simulation import GpuSimulation
+
+pytestmark = pytest.mark.gpu
+
+MRY = 2.179872325e-21
+
+
+def make(L=16, chains=32, bz=20.0, seed=3, emom=None):
+    lat = lattice.square_dmi(L, 1.0, 0.3, 0.0, bz, 1.0).with_ensembles(chains)
+    if emom is None:
+        rng = np.random.default_rng(seed)
+        emom = rng.normal(size=(chains, lat.natom, 3))
+        emom /= np.linalg.norm(emom, axis=-1, keepdims=True)
+    return lat, GpuSimulation(lat, emom=emom, seed=seed)
+
+
+def test_forward_and_gradient_match_oracle():
+    lat, sim = make()
+    prop = LearnedProposal(sim, 16, eta_scale=3.0, seed=1)
+    vec = mo.random_params(7, scale_out=1.0)
+    prop.set_params(vec)
+    assert np.array_equal(prop.get_params(), vec)
+    X = mo.random_windows(256, 8)
+    O_gpu = prop.forward(X)
+    O_ref = mo.forward(vec, X, bf16=True)[0]
+    # bf16 activations: tanh.approx can round a hidden unit to the neighbouring bf16 value
+    assert np.max(np.abs(O_gpu - O_ref)) <= 2e-2 * np.max(np.abs(O_ref))
+    loss_g, g_gpu = prop.loss_grad(X)
+    loss_r, g_ref = mo.loss_grad(vec, X, 3.0, bf16=True)
+    assert abs(loss_g - loss_r) <= 2e-3 * abs(loss_r)
+    o = 0
+    for n in [256 * 192, 256 * 256, 256 * 256, 64 * 256, 256, 256, 256, 64]:
+        a, b = g_gpu[o:o + n].astype(np.float64), g_ref[o:o + n]
+        rel = np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30)
+        cos = a @ b / max(np.linalg.norm(a) * np.linalg.norm(b), 1e-30)
+        assert rel < 3e-2 and cos > 0.999, (o, n, rel, cos)
+        o += n
+    prop.close()
+    sim.close()
+
+
+def test_training_lowers_loss_and_keeps_masks():
+    lat, sim = make()
+    T = 60.0
+    sim.relax("H", T, 200)
+    prop = LearnedProposal(sim, 16, eta_scale=8.0, data_capacity=32 * 16 * 20, seed=2)
+    for _ in range(20):
+        sim.relax("H", T, 5)
+        prop.collect()
+    losses = prop.train(150, rows=1024, lr=2e-3)
+    assert losses[-10:].mean() < losses[:10].mean() - 1.0, (losses[:10].mean(), losses[-10:].mean())
+    vec = prop.get_params()
+    o = 0
+    for m in prop.masks():
+        w = vec[o:o + m.size].reshape(m.shape)
+        assert np.all(w[m == 0] == 0.0)
+        o += m.size
+    prop.close()
+    sim.close()
+
+
+def test_accepted_energy_change_is_exact():
+    lat, sim = make(seed=11)
+    T = 60.0
+    sim.relax("H", T, 100)
+    prop = LearnedProposal(sim, 16, eta_scale=8.0, data_capacity=32 * 16 * 10, seed=5)
+    for _ in range(10):
+        sim.relax("H", T, 3)
+        prop.collect()
+    prop.train(100, rows=1024, lr=2e-3)
+    e0 = sim.observables()["energy"].copy()
+    acc, prop_n, dE = prop.sweep(T, 1)
+    e1 = sim.observables()["energy"]
+    assert acc > 0
+    measured = np.sum(e1 - e0) * lat.natom * MRY
+    scale = np.sum(np.abs(e0)) * lat.natom * MRY
+    assert abs(measured - dE) <= 1e-10 * scale + 1e-12 * abs(dE), (measured, dE)
+    prop.close()
+    sim.close()
+
+
+def _chain_stats(sim, n, learned=None, T=None):
+    es, ms = [], []
+    for _ in range(n):
+        sim.relax("H", T, 1)
+        if learned is not None:
+            learned.sweep(T, 1)
+        ob = sim.observables()
+        es.append(ob["energy"].copy())
+        ms.append(ob["mabs"].copy())
+    return np.array(es), np.array(ms)
+
+
+def test_learned_chain_samples_the_same_distribution():
+    T, nth, nme = 60.0, 300, 600
+    latA, simA = make(seed=21)
+    latB, simB = make(seed=22)
+    simA.relax("H", T, nth)
+    simB.relax("H", T, nth)
+    prop = LearnedProposal(simB, 16, eta_scale=8.0, data_capacity=32 * 16 * 20, seed=9)
+    for _ in range(20):
+        simB.relax("H", T, 5)
+        prop.collect()
+    prop.train(200, rows=1024, lr=2e-3)
+    eA, mA = _chain_stats(simA, nme, None, T)
+    eB, mB = _chain_stats(simB, nme, prop, T)
+    for a, b in ((eA, eB), (mA, mB)):
+        ma, mb = a.mean(axis=0), b.mean(axis=0)        # per chain
+        sa = ma.std(ddof=1) / np.sqrt(ma.size)
+        sb = mb.std(ddof=1) / np.sqrt(mb.size)
+        assert abs(ma.mean() - mb.mean()) <= 3.0 * np.hypot(sa, sb), (ma.mean(), mb.mean(), sa, sb)
+    prop.close()
+    simA.close()
+    simB.close()

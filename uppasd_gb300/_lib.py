@@ -80,6 +80,19 @@ SIGNATURES = {
     # tcgen05 BF16 GEMM on host buffers (validation entry point)
     "uppasd_gpu_tc_gemm": [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_int32, C.c_int32, C.c_void_p, C.c_void_p],
+    # learned patch proposal
+    "uppasd_gpu_proposal_create": [C.c_void_p, C.c_int32, C.c_float, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)],
+    "uppasd_gpu_proposal_destroy": [C.c_void_p],
+    "uppasd_gpu_proposal_nparams": [C.c_void_p, C.POINTER(C.c_int64)],
+    "uppasd_gpu_proposal_get_params": [C.c_void_p, C.c_void_p],
+    "uppasd_gpu_proposal_set_params": [C.c_void_p, C.c_void_p],
+    "uppasd_gpu_proposal_get_masks": [C.c_void_p, C.c_void_p],
+    "uppasd_gpu_proposal_forward": [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p],
+    "uppasd_gpu_proposal_loss_grad": [C.c_void_p, C.c_void_p, C.c_int32, F64P, C.c_void_p],
+    "uppasd_gpu_proposal_collect": [C.c_void_p],
+    "uppasd_gpu_proposal_train": [C.c_void_p, C.c_int32, C.c_int32, C.c_float, C.c_void_p],
+    "uppasd_gpu_proposal_sweep": [C.c_void_p, C.c_double, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                  F64P],
 }
 
 _lib = None

@@ -32,6 +32,7 @@ UNITS = [
     ("noalloc.cu", []),
     ("mc_batch.cu", []),
     ("tc_host.cu", []),
+    ("learned.cu", []),
 ]
 
 

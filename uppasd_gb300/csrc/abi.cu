@@ -17,9 +17,6 @@
 #include "common.cuh"
 #include "sim.h"
 
-struct uppasd_gpu_sim {
-    uppasd::Sim s;
-};
 
 namespace uppasd {
 

@@ -77,6 +77,15 @@ struct Sim {
     size_t bytes_allocated = 0;
 };
 
+}  // namespace uppasd
+
+// the public handle of include/uppasd_gpu.h
+struct uppasd_gpu_sim {
+    uppasd::Sim s;
+};
+
+namespace uppasd {
+
 // llg_generic.cu
 // phase: 1 predictor only, 2 corrector only, 3 both
 int llg_generic_step(Sim &s, int64_t step_offset, int phase = 3);
