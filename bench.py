@@ -134,6 +134,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def bf16_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        return float(json.load(open(p)).get("bf16_tflops", 1900.0))
+    return 1900.0
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -377,6 +384,119 @@ def run_mc(args, world, rank, peak, peak_kind):
     return out
 
 
+C3 = dict(L=128, chains=64, T=10.0, bz=20.0, J=1.0, D=0.3, eta_scale=16.0, therm=30000, snapshots=16,
+          snap_every=50, train_steps=3000, train_rows=16384, lr=1e-3)
+
+
+def _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms):
+    """Run each (name, hb, learned, cycles) mode from the same snapshot: tau_int of E and
+    |M| per chain (median over chains), cost per cycle, independent samples/s."""
+    from uppasd_gb300 import analysis
+
+    out = {}
+    chains = snap.shape[0]
+    for name, k_hb, k_l, n, plain in modes:
+        sim.put_moments(snap)
+        es, ms = [], []
+        acc = prop_n = 0
+        for _ in range(n):
+            if plain:
+                sim.relax("H", T, 1)
+            elif k_l:
+                a, p_, _ = prop.mix(T, 1, k_hb)
+                acc += a
+                prop_n += p_
+            else:
+                sim.relax("H", T, k_hb, structured=True)
+            ob = sim.observables()
+            es.append(ob["energy"].copy())
+            ms.append(ob["mabs"].copy())
+        es, ms = np.array(es), np.array(ms)
+        te = float(np.median([analysis.tau_int(es[:, k])[0] for k in range(chains)]))
+        tm = float(np.median([analysis.tau_int(ms[:, k])[0] for k in range(chains)]))
+        cost = plain_ms if plain else k_hb * structured_ms + k_l * learned_ms
+        e_chain, m_chain = es.mean(axis=0), ms.mean(axis=0)
+        out[name] = {"heat_bath_sweeps_per_cycle": k_hb, "learned_sweeps_per_cycle": k_l, "cycles": n,
+                     "tau_E": te, "tau_M": tm, "ms_per_cycle": cost,
+                     "indep_samples_per_s": chains / (2.0 * max(te, tm) * cost * 1e-3),
+                     "acceptance": acc / prop_n if prop_n else None,
+                     "E": [float(e_chain.mean()), float(e_chain.std(ddof=1) / np.sqrt(chains))],
+                     "M": [float(m_chain.mean()), float(m_chain.std(ddof=1) / np.sqrt(chains))]}
+    return out
+
+
+def run_c3(args, peak_tf):
+    """Learned-proposal MC on the square DMI lattice against the plain heat bath."""
+    import torch
+
+    from uppasd_gb300 import lattice
+    from uppasd_gb300.learned import LearnedProposal
+    from uppasd_gb300.simulation import GpuSimulation
+
+    c = C3
+    lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, c["bz"], 1.0).with_ensembles(c["chains"])
+    e0 = random_state(c["chains"], lat.natom, seed=1)
+    sim = GpuSimulation(lat, emom=e0, seed=2)
+    T = c["T"]
+    sim.relax("H", T, c["therm"], structured=True)
+    prop = LearnedProposal(sim, c["L"], eta_scale=c["eta_scale"], data_capacity=c["chains"] * 1024 * c["snapshots"],
+                           seed=3)
+    untrained = prop.mix(T, 2, 0)
+    for _ in range(c["snapshots"]):
+        sim.relax("H", T, c["snap_every"], structured=True)
+        prop.collect()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    losses = prop.train(c["train_steps"], rows=c["train_rows"], lr=c["lr"])
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    snap = sim.get_moments()
+
+    def timed(fn, n):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        fn(n)
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / n * 1e3
+
+    learned_ms = timed(lambda n: prop.mix(T, n, 0), 100)
+    structured_ms = timed(lambda n: sim.relax("H", T, n, structured=True), 2000)
+    plain_ms = timed(lambda n: sim.relax("H", T, n), 200)
+    modes = [("plain_fp64_heat_bath", 1, 0, 1500, True), ("batched_heat_bath", 1, 0, 6000, False),
+             ("learned", 0, 1, 3000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
+    res = _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms)
+    rows = c["chains"] * (c["L"] // 8) ** 2
+    flop_pass = 2.0 * rows * (192 * 256 + 2 * 256 * 256 + 256 * 64)
+    flops_sweep = 4 * 4 * flop_pass  # 4 colours x 4 passes
+    achieved_tf = flops_sweep / (learned_ms * 1e-3) / 1e12
+    plain = res["plain_fp64_heat_bath"]["indep_samples_per_s"]
+    prop.close()
+    sim.close()
+    return {
+        "metric": "MC independent samples/s, learned + batched vs plain heat bath",
+        "workload": f"square {c['L']}x{c['L']} J={c['J']} mRy, D/J={c['D']/c['J']}, Bz={c['bz']} T, T={T} K, "
+                    f"{c['chains']} chains; MADE 4x4-patch proposal (3x8x8 input, 3x256 tanh, vMF per spin)",
+        "value": res["batched_heat_bath_x8+learned"]["indep_samples_per_s"], "unit": "samples/s",
+        "speedup_vs_plain": res["batched_heat_bath_x8+learned"]["indep_samples_per_s"] / plain,
+        "learned_only_vs_plain": res["learned"]["indep_samples_per_s"] / plain,
+        "batched_heat_bath_vs_plain": res["batched_heat_bath"]["indep_samples_per_s"] / plain,
+        "learned_tau_M_gain_per_sweep": res["batched_heat_bath"]["tau_M"] / res["learned"]["tau_M"],
+        "acceptance_untrained": untrained[0] / max(untrained[1], 1),
+        "modes": res,
+        "ms_per_sweep": {"plain_fp64_heat_bath": plain_ms, "batched_heat_bath": structured_ms,
+                         "learned": learned_ms},
+        "training": {"windows": int(c["chains"] * 1024 * c["snapshots"]), "steps": c["train_steps"],
+                     "rows_per_step": c["train_rows"], "samples": c["train_steps"] * c["train_rows"],
+                     "seconds": t_train, "loss_first": float(losses[0]),
+                     "loss_last100": float(np.mean(losses[-100:]))},
+        "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
+                     "frac": achieved_tf / peak_tf, "traffic": None, "kernel": "learned sweep (all kernels)",
+                     "flop_per_sweep": flops_sweep,
+                     "note": "network FLOPs of a learned sweep over its whole duration (GEMMs plus sampling "
+                             "and acceptance kernels)"},
+    }
+
+
 def run_mc_only(args):
     """The Monte Carlo section alone (profiling and quick checks)."""
     import torch
@@ -510,6 +630,9 @@ def run_gb300(args, w):
     mc = None
     if not args.no_mc:
         mc = run_mc(args, world, rank, peak, peak_kind)
+    c3 = None
+    if not args.no_mc:
+        c3 = run_c3(args, bf16_peak())
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(w, lat, e0, os.cpu_count() or 1)
@@ -537,6 +660,7 @@ def run_gb300(args, w):
         "kernel_ms": kt,
         "variants": variants,
         "mc": mc,
+        "mc_learned": c3,
     }
     print(json.dumps(line), flush=True)
 
@@ -555,6 +679,7 @@ def main():
     ap.add_argument("--variants", action="store_true", help="also time the double-single master variant")
     ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
+    ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
     ap.add_argument("--mc-therm", type=int, default=10000)
     ap.add_argument("--mc-meas", type=int, default=100000)
     args = ap.parse_args()
@@ -565,6 +690,14 @@ def main():
         run_reference(args, w)
     elif args.mc_only:
         run_mc_only(args)
+    elif args.c3_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        from uppasd_gb300 import build as b
+
+        b.build()
+        print(json.dumps(run_c3(args, bf16_peak())), flush=True)
     else:
         run_gb300(args, w)
 

@@ -114,6 +114,13 @@ int uppasd_gpu_get_field(uppasd_gpu_sim *s, double *beff);
  * Hinzke-Nowak trials, 'H' heat bath). */
 int uppasd_gpu_mc_run(uppasd_gpu_sim *s, char mode, double temperature, int64_t nsweeps);
 
+/* Structured heat bath for a uniform square lattice of edge L (site i = x + L y;
+ * exchange and DMI on x +- 1, y +- 1, uniform moment and Zeeman field, no
+ * anisotropy; recognised from the arrays given at init, -7 otherwise): the
+ * checkerboard chain of uppasd_gpu_mc_run 'H' with FP32 draws on the FP64 state,
+ * all ensembles per launch. */
+int uppasd_gpu_mc_run_square(uppasd_gpu_sim *s, int32_t L, double temperature, int64_t nsweeps);
+
 /* Per-ensemble total moment (3, mensemble), |M|/natom (mensemble) and energy per
  * atom in mRy (mensemble); any output may be NULL. */
 int uppasd_gpu_observables(uppasd_gpu_sim *s, double *mvec, double *mabs, double *energy);
@@ -249,6 +256,11 @@ int uppasd_gpu_proposal_train(uppasd_gpu_proposal *p, int32_t nsteps, int32_t ro
  * energy change of accepted moves (J). */
 int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_t nsweeps, int64_t *accepted,
                               int64_t *proposed, double *dE_accepted);
+/* ncycles of (hb_per_cycle sweeps of uppasd_gpu_mc_run_square, then one learned
+ * sweep), enqueued back to back (the learned sweep replayed from a captured CUDA
+ * graph) with one synchronisation at the end; counts as for proposal_sweep. */
+int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t ncycles, int32_t hb_per_cycle,
+                            int64_t *accepted, int64_t *proposed, double *dE_accepted);
 
 #ifdef __cplusplus
 }

@@ -89,3 +89,53 @@ def test_statistics_match_reference_chain(mode):
         mr, sr = _binned(ref)
         mg, sg = _binned(gpu)
         assert abs(mr - mg) <= 3.0 * np.hypot(sr, sg), (mr, sr, mg, sg)
+
+
+def test_square_structured_heat_bath_matches_oracle_chain():
+    """The structured square-lattice heat bath is the checkerboard chain (x + y even,
+    then odd) of the FP64 path with FP32 draws: per spin within 2e-4 after 3 sweeps."""
+    lat = lattice.square_dmi(16, 1.0, 0.3, 0.0, 5.0, 1.0).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(8), (2, lat.natom, 3))
+    T = 40.0
+    sim = GpuSimulation(lat, emom=e0, seed=77)
+    sim.relax("H", T, 3, structured=True)
+    g = sim.get_moments()
+    sim.close()
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    idx = np.arange(lat.natom)
+    par = (idx % 16 + idx // 16) % 2
+    order = np.concatenate([idx[par == 0], idx[par == 1]]).astype(np.int32)
+    start = np.array([0, (par == 0).sum(), lat.natom], dtype=np.int32)
+    for sw in range(3):
+        o.mc_sweep_checkerboard("H", T, order, start, 77, sw)
+    assert np.max(np.abs(g - o.emom)) < 2e-4
+
+
+def test_square_structured_statistics_match_fp64_path():
+    lat = lattice.square_dmi(16, 1.0, 0.3, 0.0, 5.0, 1.0).with_ensembles(32)
+    T = 40.0
+    out = []
+    for structured in (False, True):
+        sim = GpuSimulation(lat, emom=_rand_unit(np.random.default_rng(9 + structured), (32, lat.natom, 3)),
+                            seed=5 + structured)
+        sim.relax("H", T, 300, structured=structured)
+        es = []
+        for _ in range(300):
+            sim.relax("H", T, 2, structured=structured)
+            es.append(sim.observables()["energy"].copy())
+        sim.close()
+        per_chain = np.array(es).mean(axis=0)
+        out.append((per_chain.mean(), per_chain.std(ddof=1) / np.sqrt(per_chain.size)))
+    (a, sa), (b, sb) = out
+    assert abs(a - b) <= 3 * np.hypot(sa, sb), out
+
+
+def test_square_structured_refuses_other_lattices():
+    from uppasd_gb300 import _lib
+    lat = lattice.bcc(4, [1.3, 0.7], 2.2)
+    sim = GpuSimulation(lat)
+    with pytest.raises(_lib.UppasdGpuError) as ei:
+        _lib.call("uppasd_gpu_mc_run_square", sim._h, 8, 100.0, 1)
+    assert ei.value.rc == -7
+    sim.close()

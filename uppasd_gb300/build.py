@@ -33,6 +33,7 @@ UNITS = [
     ("mc_batch.cu", []),
     ("tc_host.cu", []),
     ("learned.cu", []),
+    ("mc_square.cu", []),
 ]
 
 

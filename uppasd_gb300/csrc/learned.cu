@@ -178,30 +178,35 @@ __device__ __forceinline__ double log_vmf(const double eta[3], const double x[3]
     return dot + log(kap) - log(2.0 * kPi) - log(-expm1(-2.0 * kap)) - kap;
 }
 
-// Group g of every row: when g == 0, log q(old) of all 16 old spins first; then draw
-// the group's 4 spins from their vMF, add their log density to log q(new), write
-// them to the new-patch buffer and into the window (for the next group's pass).
-__global__ void k_vmf_group(int rows, int g, float eta_scale, const float *O, __nv_bfloat16 *X,
-                            const double *old_patch, double *new_patch, double *logq_old, double *logq_new,
-                            uint64_t seed, long long ctr) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    if (r >= rows) return;
+// log vMF in FP32 (summed in FP64 by the callers): the same function scores the
+// sampled and the current patch, and the sampler itself is FP32.
+__device__ __forceinline__ float log_vmf_f(float ex, float ey, float ez, float x, float y, float z) {
+    const float kap = sqrtf(ex * ex + ey * ey + ez * ez);
+    const float dot = ex * x + ey * y + ez * z;
+    if (kap < 1e-6f) return dot - 2.5310242469692907f;  // log(4 pi)
+    return dot + logf(kap) - 1.8378770664093453f - logf(-expm1f(-2.0f * kap)) - kap;  // log(2 pi)
+}
+
+// Group g of every row, two rows per warp and one lane per patch spin: when g == 0
+// the 16 lanes of a row score the current patch (log q(old)); then the lanes of
+// group g draw their spins from vMF(eta), add their log density to log q(new),
+// and write them to the new-patch buffer and into the window for the next pass.
+__global__ void __launch_bounds__(128) k_vmf_group(int rows, int g, float eta_scale, const float *O,
+                                                   __nv_bfloat16 *X, const double *old_patch, double *new_patch,
+                                                   double *logq_old, double *logq_new, uint64_t seed,
+                                                   const long long *dctr, int sub) {
+    const int lane = threadIdx.x & 31;
+    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;  // rows % 8 == 0: whole warps stay in range
+    const int s = lane & 15, py = s >> 2, px = s & 3;
+    const long long ctr = *dctr * 16 + sub;  // device sweep counter: graph replays draw fresh numbers
     const float *o = O + (size_t)r * kOut;
+    const float ex = eta_scale * o[3 * s], ey = eta_scale * o[3 * s + 1], ez = eta_scale * o[3 * s + 2];
+    double t_old = 0.0, t_new = 0.0;
     if (g == 0) {
-        double lq = 0.0;
-        for (int s = 0; s < kSpins; ++s) {
-            const double eta[3] = {(double)eta_scale * o[3 * s], (double)eta_scale * o[3 * s + 1],
-                                   (double)eta_scale * o[3 * s + 2]};
-            lq += log_vmf(eta, old_patch + (size_t)r * 48 + 3 * s);
-        }
-        logq_old[r] = lq;
-        logq_new[r] = 0.0;
+        const double *op = old_patch + (size_t)r * 48 + 3 * s;
+        t_old = (double)log_vmf_f(ex, ey, ez, (float)op[0], (float)op[1], (float)op[2]);
     }
-    double lq = logq_new[r];
-    const int py0 = g >> 1, px0 = g & 1;
-    for (int q = 0; q < 4; ++q) {
-        const int py = py0 + 2 * (q >> 1), px = px0 + 2 * (q & 1), s = py * 4 + px;
-        const float ex = eta_scale * o[3 * s], ey = eta_scale * o[3 * s + 1], ez = eta_scale * o[3 * s + 2];
+    if (patch_group(py, px) == g) {
         const float kap = sqrtf(ex * ex + ey * ey + ez * ez);
         const Philox4 w = philox_draw(seed, r, s, ctr, kStreamLearned);
         const float u1 = fmaf((float)w.x, 2.3283064365386963e-10f, 1.1641532182693481e-10f);
@@ -247,20 +252,106 @@ __global__ void k_vmf_group(int rows, int g, float eta_scale, const float *O, __
         nx *= il;
         ny *= il;
         nz *= il;
-        const double x[3] = {(double)nx, (double)ny, (double)nz};
-        const double eta[3] = {(double)ex, (double)ey, (double)ez};
-        lq += log_vmf(eta, x);
+        t_new = (double)log_vmf_f(ex, ey, ez, nx, ny, nz);
         double *np_ = new_patch + (size_t)r * 48 + 3 * s;
-        np_[0] = x[0];
-        np_[1] = x[1];
-        np_[2] = x[2];
-        const int pos = (py + 2) * 8 + (px + 2);
-        __nv_bfloat16 *xr = X + (size_t)r * kFeat + pos * 3;
+        np_[0] = nx;
+        np_[1] = ny;
+        np_[2] = nz;
+        __nv_bfloat16 *xr = X + (size_t)r * kFeat + ((py + 2) * 8 + (px + 2)) * 3;
         xr[0] = __float2bfloat16_rn(nx);
         xr[1] = __float2bfloat16_rn(ny);
         xr[2] = __float2bfloat16_rn(nz);
     }
-    logq_new[r] = lq;
+    // sums over the 16 lanes of the row
+#pragma unroll
+    for (int off = 8; off > 0; off >>= 1) {
+        t_old += __shfl_xor_sync(0xffffffffu, t_old, off);
+        t_new += __shfl_xor_sync(0xffffffffu, t_new, off);
+    }
+    if (s == 0) {
+        if (g == 0) {
+            logq_old[r] = t_old;
+            logq_new[r] = t_new;
+        } else {
+            logq_new[r] += t_new;
+        }
+    }
+}
+
+// Uniform square-lattice couplings (SquareMC) for the patch energy.
+struct SqCoup {
+    float c[4], d[4][3], ext[3], mom;
+};
+
+// One warp per patch on a uniform square lattice: lanes 0-15 score the new patch,
+// lanes 16-31 the old one (bonds leaving the patch in full, bonds inside it at one
+// half, Zeeman on site), FP64; then the Metropolis-Hastings decision and write-back.
+__global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D e, Vec3D eM, int natom, int rows,
+                                                   const double *old_patch, const double *new_patch,
+                                                   const double *logq_old, const double *logq_new, double beta_mub,
+                                                   uint64_t seed, const long long *dctr, int sub,
+                                                   unsigned long long *accepted, double *dE_sum) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (warp >= rows) return;
+    const int r = warp;
+    const long long ctr = *dctr * 16 + sub;
+    int k, x0, y0;
+    patch_of_row(g, r, k, x0, y0);
+    const int s = lane & 15, py = s >> 2, px = s & 3;
+    const double *patch = (lane < 16 ? new_patch : old_patch) + (size_t)r * 48;
+    const double ei[3] = {patch[3 * s], patch[3 * s + 1], patch[3 * s + 2]};
+    const size_t off = (size_t)k * natom;
+    double E = -(q.ext[0] * ei[0] + q.ext[1] * ei[1] + q.ext[2] * ei[2]);
+    const int ddx[4] = {1, -1, 0, 0}, ddy[4] = {0, 0, 1, -1};
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const int nx = px + ddx[d], ny = py + ddy[d];
+        double ej[3], w;
+        if (nx >= 0 && nx < 4 && ny >= 0 && ny < 4) {
+            const int sj = ny * 4 + nx;
+            ej[0] = patch[3 * sj];
+            ej[1] = patch[3 * sj + 1];
+            ej[2] = patch[3 * sj + 2];
+            w = 0.5;
+        } else {
+            const size_t o = off + wrap_site(x0 + nx, y0 + ny, g.L);
+            ej[0] = e.x[o];
+            ej[1] = e.y[o];
+            ej[2] = e.z[o];
+            w = 1.0;
+        }
+        const double cx = ei[1] * ej[2] - ei[2] * ej[1], cy = ei[2] * ej[0] - ei[0] * ej[2],
+                     cz = ei[0] * ej[1] - ei[1] * ej[0];
+        E -= w * ((double)q.c[d] * (ei[0] * ej[0] + ei[1] * ej[1] + ei[2] * ej[2]) +
+                  ((double)q.d[d][0] * cx + (double)q.d[d][1] * cy + (double)q.d[d][2] * cz));
+    }
+    E *= (double)q.mom;
+    double dE = lane < 16 ? E : -E;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
+    const double loga = -beta_mub * dE + logq_old[r] - logq_new[r];
+    int acc = 0;
+    if (lane == 0) {
+        const Philox4 w = philox_draw(seed, r, 16, ctr, kStreamLearned);
+        const double u = u01_open(w.z);
+        acc = (loga >= 0.0 || log(u) < loga) ? 1 : 0;
+    }
+    acc = __shfl_sync(0xffffffffu, acc, 0);
+    if (!acc) return;
+    if (lane == 0) {
+        atomicAdd(accepted, 1ull);
+        atomicAdd(dE_sum, dE);
+    }
+    if (lane < kSpins) {
+        const size_t o = off + wrap_site(x0 + px, y0 + py, g.L);
+        const double mm = (double)q.mom;
+        e.x[o] = ei[0];
+        e.y[o] = ei[1];
+        e.z[o] = ei[2];
+        eM.x[o] = mm * ei[0];
+        eM.y[o] = mm * ei[1];
+        eM.z[o] = mm * ei[2];
+    }
 }
 
 // Energy of patch spin `s` (site i) in one configuration: bonds to sites outside the
@@ -329,11 +420,12 @@ __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const doub
 // One warp per patch: exact energy change, Metropolis-Hastings decision, write-back.
 __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double *mmom, int rows,
                          const double *old_patch, const double *new_patch, const double *logq_old,
-                         const double *logq_new, double beta_mub, uint64_t seed, long long ctr,
+                         const double *logq_new, double beta_mub, uint64_t seed, const long long *dctr, int sub,
                          unsigned long long *accepted, double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (warp >= rows) return;
     const int r = warp;
+    const long long ctr = *dctr * 16 + sub;
     int k, x0, y0;
     patch_of_row(g, r, k, x0, y0);
     double dE = 0.0;
@@ -429,6 +521,8 @@ __global__ void k_adam(float *p, const float *gr, const float *mask, float *m, f
     p[i] = pi;
 }
 
+__global__ void k_advance(long long *dctr) { *dctr += 1; }
+
 // Random minibatch of dataset rows into X.
 __global__ void k_sample_rows(const __nv_bfloat16 *D, long long count, int rows, uint64_t seed, long long ctr,
                               __nv_bfloat16 *X) {
@@ -465,11 +559,17 @@ struct uppasd_gpu_proposal {
     // dataset
     __nv_bfloat16 *data = nullptr;
     long long data_cap = 0, data_count = 0, data_next = 0;
-    long long ctr = 0;         // Philox counter of proposals and minibatches
+    long long ctr = 0;             // Philox counter of minibatches (host)
+    long long *dctr = nullptr;     // Philox counter of learned sweeps (device, advanced in-stream)
     int adam_t = 0;
     // prepared GEMMs: forward (rows R) for the current row count
     int prepared_rows = -1;
     uppasd::tc::Gemm fwd[4], bwd[3], wgr[4];
+    // one learned sweep captured as a CUDA graph (rebuilt when T or the rows change)
+    cudaGraphExec_t sweep_graph = nullptr;
+    double graph_T = -1.0;
+    int graph_rows = -1;
+    bool warmed = false;
 };
 
 namespace {
@@ -485,7 +585,9 @@ void free_all(uppasd_gpu_proposal *p) {
     if (!p) return;
     cudaDeviceSynchronize();
     void *ptrs[] = {p->params, p->B.X, p->B.dO, p->B.Xt, p->B.dOt, p->B.O, p->B.gW4t, p->old_patch,
-                    p->new_patch, p->logq_old, p->logq_new, p->accepted, p->dE_sum, p->loss, p->err, p->data};
+                    p->new_patch, p->logq_old, p->logq_new, p->accepted, p->dE_sum, p->loss, p->err, p->data,
+                    p->dctr};
+    if (p->sweep_graph) cudaGraphExecDestroy(p->sweep_graph);
     for (void *q : ptrs) cudaFree(q);
     for (int l = 0; l < 3; ++l) {
         cudaFree(p->B.H[l]);
@@ -536,14 +638,14 @@ int prepare(uppasd_gpu_proposal *p, int rows) {
     if (p->prepared_rows == rows) return UPPASD_GPU_OK;
     auto &B = p->B;
     int rc = 0;
-    rc = rc ? rc : tc::gemm_prepare(p->fwd[0], B.X, B.wb[0], rows, kHid, kFeat, tc::kEpiBiasTanhBF16, 128);
-    rc = rc ? rc : tc::gemm_prepare(p->fwd[1], B.H[0], B.wb[1], rows, kHid, kHid, tc::kEpiBiasTanhBF16, 128);
-    rc = rc ? rc : tc::gemm_prepare(p->fwd[2], B.H[1], B.wb[2], rows, kHid, kHid, tc::kEpiBiasTanhBF16, 128);
-    rc = rc ? rc : tc::gemm_prepare(p->fwd[3], B.H[2], B.wb[3], rows, kOut, kHid, tc::kEpiBiasF32, 64);
+    rc = rc ? rc : tc::gemm_prepare(p->fwd[0], B.X, B.wb[0], rows, kHid, kFeat, tc::kEpiBiasTanhBF16, 128, 2);
+    rc = rc ? rc : tc::gemm_prepare(p->fwd[1], B.H[0], B.wb[1], rows, kHid, kHid, tc::kEpiBiasTanhBF16, 128, 2);
+    rc = rc ? rc : tc::gemm_prepare(p->fwd[2], B.H[1], B.wb[2], rows, kHid, kHid, tc::kEpiBiasTanhBF16, 128, 2);
+    rc = rc ? rc : tc::gemm_prepare(p->fwd[3], B.H[2], B.wb[3], rows, kOut, kHid, tc::kEpiBiasF32, 64, 2);
     // backward data: dH3 = (dO W4) (1 - H3^2), dH2 = (dH3 W3) (1 - H2^2), dH1 = (dH2 W2) (1 - H1^2)
-    rc = rc ? rc : tc::gemm_prepare(p->bwd[2], B.dO, B.wt[3], rows, kHid, kOut, tc::kEpiDTanhBF16, 128);
-    rc = rc ? rc : tc::gemm_prepare(p->bwd[1], B.dH[2], B.wt[2], rows, kHid, kHid, tc::kEpiDTanhBF16, 128);
-    rc = rc ? rc : tc::gemm_prepare(p->bwd[0], B.dH[1], B.wt[1], rows, kHid, kHid, tc::kEpiDTanhBF16, 128);
+    rc = rc ? rc : tc::gemm_prepare(p->bwd[2], B.dO, B.wt[3], rows, kHid, kOut, tc::kEpiDTanhBF16, 128, 2);
+    rc = rc ? rc : tc::gemm_prepare(p->bwd[1], B.dH[2], B.wt[2], rows, kHid, kHid, tc::kEpiDTanhBF16, 128, 2);
+    rc = rc ? rc : tc::gemm_prepare(p->bwd[0], B.dH[1], B.wt[1], rows, kHid, kHid, tc::kEpiDTanhBF16, 128, 2);
     // weight gradients (K = rows): gW1 = dH1^T X, gW2 = dH2^T H1, gW3 = dH3^T H2, gW4^T = H3^T dO
     rc = rc ? rc : tc::gemm_prepare(p->wgr[0], B.dHt[0], B.Xt, kHid, kFeat, rows, tc::kEpiStoreF32, 64);
     rc = rc ? rc : tc::gemm_prepare(p->wgr[1], B.dHt[1], B.Ht[0], kHid, kHid, rows, tc::kEpiStoreF32, 128);
@@ -619,6 +721,41 @@ PatchGeom geom(const uppasd_gpu_proposal *p, int colour) {
     g.np = g.half * g.half;
     g.colour = colour;
     return g;
+}
+
+// One learned sweep (the four patch colours) enqueued on `st`; capturable.
+int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_t st) {
+    Sim &s = p->sim->s;
+    const long long nt = (long long)rows * 64;
+    int rc;
+    for (int c = 0; c < 4; ++c) {
+        PatchGeom g = geom(p, c);
+        k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch);
+        for (int grp = 0; grp < 4; ++grp) {
+            if ((rc = forward(p, st))) return rc;
+            k_vmf_group<<<rows / 8, 128, 0, st>>>(rows, grp, p->eta_scale, p->B.O, p->B.X, p->old_patch,
+                                                   p->new_patch, p->logq_old, p->logq_new, p->seed, p->dctr, c * 4 + grp);
+        }
+        if (s.sq.L == p->L) {
+            SqCoup q;
+            for (int d = 0; d < 4; ++d) {
+                q.c[d] = s.sq.c[d];
+                for (int cc = 0; cc < 3; ++cc) q.d[d][cc] = s.sq.d[d][cc];
+            }
+            for (int cc = 0; cc < 3; ++cc) q.ext[cc] = s.sq.ext[cc];
+            q.mom = s.sq.mom;
+            k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.e, s.eM, s.ham.natom, rows, p->old_patch,
+                                                                  p->new_patch, p->logq_old, p->logq_new, beta_mub,
+                                                                  p->seed, p->dctr, c, p->accepted, p->dE_sum);
+        } else {
+            k_accept<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, s.ham, s.e, s.eM, s.llg.mmom, rows, p->old_patch,
+                                                               p->new_patch, p->logq_old, p->logq_new, beta_mub,
+                                                               p->seed, p->dctr, c, p->accepted, p->dE_sum);
+        }
+    }
+    k_advance<<<1, 1, 0, st>>>(p->dctr);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? UPPASD_GPU_OK : cuda_fail("proposal sweep", e);
 }
 
 }  // namespace
@@ -702,6 +839,7 @@ int uppasd_gpu_proposal_create(uppasd_gpu_sim *sim, int32_t L, float eta_scale, 
     al((void **)&p->dE_sum, sizeof(double));
     al((void **)&p->loss, sizeof(double));
     al((void **)&p->err, sizeof(int));
+    al((void **)&p->dctr, sizeof(long long));
     p->data_cap = data_capacity;
     if (data_capacity > 0) al((void **)&p->data, (size_t)data_capacity * kFeat * 2);
     if (e != cudaSuccess) {
@@ -726,6 +864,9 @@ int uppasd_gpu_proposal_create(uppasd_gpu_sim *sim, int32_t L, float eta_scale, 
         if (e == cudaSuccess) e = cudaMemcpy(p->P.mask[l], mask[l].data(), kNW[l] * 4, cudaMemcpyHostToDevice);
     }
     int rc = e == cudaSuccess ? sync_weights(p, sim->s.stream) : cuda_fail("proposal_create", e);
+    // uniform square couplings select the structured energy kernel; anything else
+    // (anisotropy, site-dependent couplings) uses the neighbour-list kernel
+    if (!rc && sim->s.sq.L != L && square_recognise(sim->s, L) != UPPASD_GPU_OK) sim->s.sq.L = 0;
     if (!rc) rc = check_err(p, sim->s.stream);
     if (rc) {
         free_all(p);
@@ -949,8 +1090,15 @@ int uppasd_gpu_proposal_train(uppasd_gpu_proposal *p, int32_t nsteps, int32_t ro
 // nsweeps learned sweeps (4 patch colours each) at `temperature` on the simulation's spins.
 int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_t nsweeps, int64_t *accepted,
                               int64_t *proposed, double *dE_accepted) {
-    if (!p || !(temperature > 0.0) || nsweeps < 0) {
-        set_error("proposal_sweep: bad arguments");
+    return uppasd_gpu_proposal_mix(p, temperature, nsweeps, 0, accepted, proposed, dE_accepted);
+}
+
+// ncycles of (hb_per_cycle structured heat-bath sweeps, then one learned sweep), all
+// enqueued on the simulation's stream; one synchronisation at the end.
+int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t ncycles, int32_t hb_per_cycle,
+                            int64_t *accepted, int64_t *proposed, double *dE_accepted) {
+    if (!p || !(temperature > 0.0) || ncycles < 0 || hb_per_cycle < 0) {
+        set_error("proposal_mix: bad arguments");
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = p->sim->s;
@@ -960,36 +1108,50 @@ int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_
     if (rc) return rc;
     cudaError_t e = cudaMemsetAsync(p->accepted, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->dE_sum, 0, sizeof(double), st);
-    if (e != cudaSuccess) return cuda_fail("proposal_sweep", e);
+    if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
     const double beta_mub = kMub / (kKbolt * temperature);
-    const long long nt = (long long)rows * 64;
-    for (int64_t sw = 0; sw < nsweeps; ++sw) {
-        for (int c = 0; c < 4; ++c) {
-            PatchGeom g = geom(p, c);
-            const long long ctr = p->ctr++;
-            k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch);
-            for (int grp = 0; grp < 4; ++grp) {
-                if ((rc = forward(p, st))) return rc;
-                k_vmf_group<<<(rows + 127) / 128, 128, 0, st>>>(rows, grp, p->eta_scale, p->B.O, p->B.X, p->old_patch,
-                                                                 p->new_patch, p->logq_old, p->logq_new, p->seed,
-                                                                 ctr * 4 + grp);
-            }
-            k_accept<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, s.ham, s.e, s.eM, s.llg.mmom, rows, p->old_patch,
-                                                               p->new_patch, p->logq_old, p->logq_new, beta_mub,
-                                                               p->seed, ctr, p->accepted, p->dE_sum);
-        }
+    int64_t done = 0;
+    auto heat_bath = [&]() -> int {
+        return hb_per_cycle > 0 ? uppasd_gpu_mc_run_square(p->sim, p->L, temperature, hb_per_cycle) : 0;
+    };
+    if (ncycles > 0 && !p->warmed) {
+        // first sweep eagerly: sets the GEMM kernels' shared-memory attributes before any capture
+        if ((rc = heat_bath()) || (rc = enqueue_sweep(p, rows, beta_mub, st))) return rc;
+        p->warmed = true;
+        done = 1;
     }
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return cuda_fail("proposal_sweep", e);
+    if (done < ncycles && (!p->sweep_graph || p->graph_T != temperature || p->graph_rows != rows)) {
+        if (p->sweep_graph) cudaGraphExecDestroy(p->sweep_graph);
+        p->sweep_graph = nullptr;
+        cudaGraph_t g = nullptr;
+        e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_fail("proposal_mix capture", e);
+        rc = enqueue_sweep(p, rows, beta_mub, st);
+        e = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->sweep_graph, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail("proposal_mix graph", e);
+        p->graph_T = temperature;
+        p->graph_rows = rows;
+    }
+    for (; done < ncycles; ++done) {
+        if ((rc = heat_bath())) return rc;
+        e = cudaGraphLaunch(p->sweep_graph, st);
+        if (e != cudaSuccess) return cuda_fail("proposal_mix graph launch", e);
+    }
     rc = check_err(p, st);
     if (rc) return rc;
     unsigned long long a = 0;
     double de = 0.0;
     e = cudaMemcpy(&a, p->accepted, sizeof(a), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(&de, p->dE_sum, sizeof(de), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail("proposal_sweep", e);
+    if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
     if (accepted) *accepted = (int64_t)a;
-    if (proposed) *proposed = (int64_t)rows * 4 * nsweeps;
+    if (proposed) *proposed = (int64_t)rows * 4 * ncycles;
     if (dE_accepted) *dE_accepted = de * kMub;
     return UPPASD_GPU_OK;
 }

@@ -1,0 +1,221 @@
+// mc_square.cu -- structured heat bath for uniform square-lattice Hamiltonians
+// (exchange and interfacial DMI on the four nearest neighbours, uniform moment
+// and Zeeman field), all ensembles of a simulation in one launch per colour.
+//
+// The reference's general path (mc.cu) gathers through the neighbour list in
+// FP64; here the neighbours are x +- 1, y +- 1 of site i = x + L y, the
+// couplings are per-direction constants recognised once from the caller's
+// nlist/ncoup/dmlist/dm_vect, and the heat-bath draw (flip_h,
+// MonteCarlo/montecarlo_common.f90:371-422) runs in FP32 on the FP64 spin state.
+// The chain is the checkerboard chain of mc.cu (colours x + y even, then odd)
+// with the same Philox counters (site, ensemble, sweep), so it agrees with the
+// FP64 path to FP32 rounding.
+#include <cmath>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "sim.h"
+
+namespace uppasd {
+namespace {
+
+struct SqArgs {
+    int L, N, mensemble, colour;
+    float c[4], d[4][3], ext[3], beta_mu, mom;
+    uint64_t seed;
+    long long sweep;
+};
+
+__device__ __forceinline__ float3 heat_bath_f32(float3 h, float beta_mu, float q, float fp) {
+    const float zx = beta_mu * h.x, zy = beta_mu * h.y, zz = beta_mu * h.z;
+    const float rxy = sqrtf(zx * zx + zy * zy);
+    const float zarg = sqrtf(fmaf(rxy, rxy, zz * zz));
+    const float izarg = 1.0f / zarg;
+    const float zct = zz * izarg, zst = rxy * izarg;
+    const float zcp = rxy > 0.0f ? zx / rxy : 1.0f, zsp = rxy > 0.0f ? zy / rxy : 0.0f;
+    const float e2 = __expf(-2.0f * zarg);
+    const float omc = fminf(2.0f, fmaxf(0.0f, -__logf(fmaf(1.0f - e2, q, e2) + 1e-14f) * izarg));
+    const float ct = 1.0f - omc, st = sqrtf(omc * (2.0f - omc));
+    float sp, cp;
+    __sincosf(3.14159265358979f * (2.0f * fp - 1.0f), &sp, &cp);
+    const float s0 = st * cp, s1 = st * sp;
+    const float nx = zcp * zct * s0 - zsp * s1 + zcp * zst * ct;
+    const float ny = zsp * zct * s0 + zcp * s1 + zsp * zst * ct;
+    const float nz = -zst * s0 + zct * ct;
+    const float il = rsqrtf(nx * nx + ny * ny + nz * nz);
+    return make_float3(nx * il, ny * il, nz * il);
+}
+
+__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, Vec3D e, Vec3D eM) {
+    const int half = a.L >> 1;
+    const long long per = (long long)a.L * half;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= per * a.mensemble) return;
+    const int k = (int)(t / per);
+    const int idx = (int)(t - (long long)k * per);
+    const int y = idx / half;
+    const int x = 2 * (idx - y * half) + ((y + a.colour) & 1);
+    const int L = a.L;
+    const int xp = x + 1 == L ? 0 : x + 1, xm = x == 0 ? L - 1 : x - 1;
+    const int yp = y + 1 == L ? 0 : y + 1, ym = y == 0 ? L - 1 : y - 1;
+    const size_t off = (size_t)k * a.N;
+    const int nb[4] = {xp + L * y, xm + L * y, x + L * yp, x + L * ym};
+    float hx = a.ext[0], hy = a.ext[1], hz = a.ext[2];
+#pragma unroll
+    for (int d = 0; d < 4; ++d) {
+        const size_t o = off + nb[d];
+        const float ex = (float)e.x[o], ey = (float)e.y[o], ez = (float)e.z[o];
+        // exchange c e_j plus DMI e_j x d
+        hx += a.c[d] * ex + (ey * a.d[d][2] - ez * a.d[d][1]);
+        hy += a.c[d] * ey + (ez * a.d[d][0] - ex * a.d[d][2]);
+        hz += a.c[d] * ez + (ex * a.d[d][1] - ey * a.d[d][0]);
+    }
+    const int i = x + L * y;
+    const Philox4 w = philox_draw(a.seed, i, k, a.sweep, kStreamMC);
+    const float k32 = 2.3283064365386963e-10f;
+    const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
+    const float3 n = heat_bath_f32(make_float3(hx, hy, hz), a.beta_mu, q, fp);
+    const size_t o = off + i;
+    e.x[o] = n.x;
+    e.y[o] = n.y;
+    e.z[o] = n.z;
+    eM.x[o] = (double)a.mom * n.x;
+    eM.y[o] = (double)a.mom * n.y;
+    eM.z[o] = (double)a.mom * n.z;
+}
+
+template <typename T>
+int to_host(std::vector<T> &h, const T *d, size_t n) {
+    h.resize(n);
+    return cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost) == cudaSuccess ? 0 : 1;
+}
+
+}  // namespace
+
+// Recognise a uniform square-lattice Hamiltonian of edge L; fills s.sq or returns an error.
+int square_recognise(Sim &s, int L) {
+    const HamDev &h = s.ham;
+    const int N = h.natom;
+    auto fail = [&](const std::string &why) {
+        set_error("structured heat bath: " + why);
+        return UPPASD_GPU_EUNSUPPORTED;
+    };
+    if (L < 2 || (L & 1) || N != L * L) return fail("natom must equal L^2 with L even");
+    std::vector<int32_t> nlist, nsize, aham, dml, dms, ta;
+    std::vector<double> nc, dx, dy, dz, mm, ex, ey, ez, k1, k2;
+    int bad = to_host(nlist, h.nlist, (size_t)h.mnn * N) | to_host(nsize, h.nsize, N) | to_host(aham, h.aham, N) |
+              to_host(nc, h.ncoup, (size_t)h.mnn * h.nham) | to_host(mm, s.llg.mmom, (size_t)N * h.mensemble) |
+              to_host(ex, h.ext.x, (size_t)N * h.mensemble) | to_host(ey, h.ext.y, (size_t)N * h.mensemble) |
+              to_host(ez, h.ext.z, (size_t)N * h.mensemble);
+    if (h.do_dm)
+        bad |= to_host(dml, h.dmlist, (size_t)h.mnn_dm * N) | to_host(dms, h.dmsize, N) |
+               to_host(dx, h.dmx, (size_t)h.mnn_dm * h.nham) | to_host(dy, h.dmy, (size_t)h.mnn_dm * h.nham) |
+               to_host(dz, h.dmz, (size_t)h.mnn_dm * h.nham);
+    if (h.do_aniso) bad |= to_host(k1, h.k1, N) | to_host(k2, h.k2, N) | to_host(ta, h.taniso, N);
+    if (bad) {
+        set_error("structured heat bath: device copy failed");
+        return UPPASD_GPU_ECUDA;
+    }
+    auto dir_of = [&](int i, int j) {
+        const int x = i % L, y = i / L, jx = j % L, jy = j / L;
+        const int dx_ = (jx - x + L) % L, dy_ = (jy - y + L) % L;
+        if (dx_ == 1 && dy_ == 0) return 0;
+        if (dx_ == L - 1 && dy_ == 0) return 1;
+        if (dx_ == 0 && dy_ == 1) return 2;
+        if (dx_ == 0 && dy_ == L - 1) return 3;
+        return -1;
+    };
+    double cdir[4];
+    double ddir[4][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    bool seen[4] = {false, false, false, false}, dseen[4] = {false, false, false, false};
+    for (int i = 0; i < N; ++i) {
+        if (nsize[i] != 4) return fail("every site needs exactly 4 exchange neighbours");
+        for (int q = 0; q < 4; ++q) {
+            const int d = dir_of(i, nlist[(size_t)q * N + i]);
+            if (d < 0) return fail("neighbours must be x +- 1, y +- 1 (periodic)");
+            const double c = nc[(size_t)q * h.nham + aham[i]];
+            if (!seen[d]) {
+                cdir[d] = c;
+                seen[d] = true;
+            } else if (c != cdir[d]) {
+                return fail("exchange must be uniform per direction");
+            }
+        }
+        if (h.do_dm) {
+            if (dms[i] != 4 && dms[i] != 0) return fail("DMI must act on the 4 nearest neighbours");
+            for (int q = 0; q < dms[i]; ++q) {
+                const int d = dir_of(i, dml[(size_t)q * N + i]);
+                if (d < 0) return fail("DMI neighbours must be x +- 1, y +- 1");
+                const size_t o = (size_t)q * h.nham + aham[i];
+                const double v[3] = {dx[o], dy[o], dz[o]};
+                if (!dseen[d]) {
+                    for (int c = 0; c < 3; ++c) ddir[d][c] = v[c];
+                    dseen[d] = true;
+                } else if (v[0] != ddir[d][0] || v[1] != ddir[d][1] || v[2] != ddir[d][2]) {
+                    return fail("DMI vectors must be uniform per direction");
+                }
+            }
+        }
+        if (h.do_aniso && ta[i] != 0 && (k1[i] != 0.0 || k2[i] != 0.0))
+            return fail("anisotropy is not supported (the heat bath of a quadratic term is not exact)");
+    }
+    for (size_t q = 1; q < mm.size(); ++q)
+        if (mm[q] != mm[0]) return fail("moments must be uniform");
+    for (size_t q = 1; q < ex.size(); ++q)
+        if (ex[q] != ex[0] || ey[q] != ey[0] || ez[q] != ez[0]) return fail("the Zeeman field must be uniform");
+    SquareMC &sq = s.sq;
+    sq.mom = (float)mm[0];
+    for (int d = 0; d < 4; ++d) {
+        sq.c[d] = (float)(cdir[d] * mm[0]);
+        for (int c = 0; c < 3; ++c) sq.d[d][c] = (float)(ddir[d][c] * mm[0]);
+    }
+    sq.ext[0] = (float)ex[0];
+    sq.ext[1] = (float)ey[0];
+    sq.ext[2] = (float)ez[0];
+    sq.L = L;
+    return UPPASD_GPU_OK;
+}
+
+}  // namespace uppasd
+
+extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double temperature, int64_t nsweeps) {
+    using namespace uppasd;
+    if (!w || nsweeps < 0 || !(temperature > 0.0) || L < 2) {
+        set_error("mc_run_square: temperature > 0, nsweeps >= 0, L >= 2");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    if (s.precision >= 1) {
+        set_error("mc_run_square: needs the FP64 state path (precision 0)");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
+    if (s.sq.L != L) {
+        const int rc = square_recognise(s, L);
+        if (rc) return rc;
+    }
+    SqArgs a{};
+    a.L = L;
+    a.N = s.ham.natom;
+    a.mensemble = s.ham.mensemble;
+    for (int d = 0; d < 4; ++d) {
+        a.c[d] = s.sq.c[d];
+        for (int c = 0; c < 3; ++c) a.d[d][c] = s.sq.d[d][c];
+    }
+    for (int c = 0; c < 3; ++c) a.ext[c] = s.sq.ext[c];
+    a.mom = s.sq.mom;
+    a.beta_mu = (float)(kMub * s.sq.mom / (kKbolt * temperature));
+    a.seed = s.llg.seed;
+    const long long per = (long long)L * (L / 2) * a.mensemble;
+    const unsigned blocks = (unsigned)((per + 255) / 256);
+    for (int64_t sw = 0; sw < nsweeps; ++sw) {
+        a.sweep = s.mc_sweep;
+        for (int c = 0; c < 2; ++c) {
+            a.colour = c;
+            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.e, s.eM);
+        }
+        s.mc_sweep += 1;
+    }
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}

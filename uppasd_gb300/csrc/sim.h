@@ -53,6 +53,17 @@ struct LlgDev {
 
 struct StructuredFast;  // mixed-precision structured-lattice path (llg_stencil.cu)
 
+// Uniform square-lattice Hamiltonian recognised for the structured heat bath
+// (mc_square.cu): per neighbour direction (+x, -x, +y, -y) the exchange field per
+// unit neighbour and the DMI vector, uniform moment and Zeeman field.
+struct SquareMC {
+    int L = 0;          // 0: not recognised yet; -1: recognised as not square-uniform
+    float c[4];         // ncoup * m (T per unit neighbour vector)
+    float d[4][3];      // D * m (field e_j x d)
+    float ext[3];       // Zeeman field (T)
+    float mom;          // moment (muB)
+};
+
 struct Sim {
     HamDev ham;
     LlgDev llg;
@@ -72,6 +83,7 @@ struct Sim {
     int32_t *colour_sites = nullptr;   // sites listed colour by colour
     int32_t *colour_start_h = nullptr; // host copy, ncolour+1
     int64_t mc_sweep = 0;
+    SquareMC sq;
     // scratch for observables
     double *red = nullptr;             // [mensemble][8]
     size_t bytes_allocated = 0;
@@ -94,6 +106,8 @@ int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const 
 int field_to_host(Sim &s, double *beff_h);
 // mc.cu
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps);
+// mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
+int square_recognise(Sim &s, int L);
 
 void set_error(const std::string &msg);
 

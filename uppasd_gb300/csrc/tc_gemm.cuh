@@ -26,7 +26,7 @@ namespace tc {
 
 constexpr int kBM = 128;
 constexpr int kBK = 64;       // bf16 elements per K slice = one 128-byte swizzle row
-constexpr int kStages = 4;
+constexpr int kMaxStages = 4;
 constexpr int kThreads = 128;
 constexpr long long kWaitLimit = 1LL << 22;
 
@@ -140,9 +140,10 @@ __device__ __forceinline__ float tanh_fast(float x) {
     return y;
 }
 
-template <int BN, int EPI>
+template <int BN, int EPI, int kStages>
 __global__ void __launch_bounds__(kThreads, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, GemmArgs g) {
+    static_assert(kStages >= 1 && kStages <= kMaxStages, "stages");
     static_assert(BN == 64 || BN == 128 || BN == 256, "BN");
     constexpr uint32_t kABytes = kBM * kBK * 2, kBBytes = BN * kBK * 2;
     constexpr uint32_t kStageBytes = kABytes + kBBytes;
@@ -269,9 +270,9 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-template <int BN>
+template <int BN, int STAGES>
 constexpr size_t gemm_smem_bytes() {
-    return (size_t)kStages * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
+    return (size_t)STAGES * (kBM * kBK * 2 + BN * kBK * 2) + 1024;
 }
 
 }  // namespace tc

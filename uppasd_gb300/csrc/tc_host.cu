@@ -55,10 +55,10 @@ int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows) 
     return UPPASD_GPU_OK;
 }
 
-template <int BN, int EPI>
+template <int BN, int EPI, int ST>
 int launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t st) {
-    auto kern = tc_gemm_kernel<BN, EPI>;
-    const size_t smem = gemm_smem_bytes<BN>();
+    auto kern = tc_gemm_kernel<BN, EPI, ST>;
+    const size_t smem = gemm_smem_bytes<BN, ST>();
     static bool attr_set = false;  // per instantiation
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -77,20 +77,25 @@ int launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, c
     return UPPASD_GPU_OK;
 }
 
-template <int BN>
+template <int BN, int ST>
 int launch_epi(int epi, const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t st) {
     switch (epi) {
-    case kEpiStoreF32: return launch_bn<BN, kEpiStoreF32>(ma, mb, g, st);
-    case kEpiBiasF32: return launch_bn<BN, kEpiBiasF32>(ma, mb, g, st);
-    case kEpiBiasTanhBF16: return launch_bn<BN, kEpiBiasTanhBF16>(ma, mb, g, st);
-    case kEpiDTanhBF16: return launch_bn<BN, kEpiDTanhBF16>(ma, mb, g, st);
+    case kEpiStoreF32: return launch_bn<BN, kEpiStoreF32, ST>(ma, mb, g, st);
+    case kEpiBiasF32: return launch_bn<BN, kEpiBiasF32, ST>(ma, mb, g, st);
+    case kEpiBiasTanhBF16: return launch_bn<BN, kEpiBiasTanhBF16, ST>(ma, mb, g, st);
+    case kEpiDTanhBF16: return launch_bn<BN, kEpiDTanhBF16, ST>(ma, mb, g, st);
     }
     set_error("tc_gemm: unknown epilogue");
     return UPPASD_GPU_EINVAL;
 }
 }  // namespace
 
-int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int epi, int bn) {
+int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int epi, int bn,
+                 int stages) {
+    if (stages != 2 && stages != 4) {
+        set_error("tc_gemm: stages must be 2 or 4");
+        return UPPASD_GPU_EINVAL;
+    }
     if (M <= 0 || N <= 0 || K <= 0 || M % kBM || K % kBK || !(bn == 64 || bn == 128 || bn == 256) || N % bn) {
         set_error("tc_gemm: need M % 128 == 0, K % 64 == 0, N % BN == 0 with BN in {64, 128, 256}");
         return UPPASD_GPU_EINVAL;
@@ -107,6 +112,7 @@ int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M
     op.K = K;
     op.epi = epi;
     op.bn = bn;
+    op.stages = stages;
     return UPPASD_GPU_OK;
 }
 
@@ -124,10 +130,18 @@ int gemm_run(const Gemm &op, const float *bias, const __nv_bfloat16 *Y, float *C
         return UPPASD_GPU_EINVAL;
     }
     GemmArgs g{op.M, op.N, op.K, bias, Y, Cf, Cb, err};
+    // a short K loop (<= 2 slices per stage ring) fits 2 stages and more resident CTAs
+    if (op.stages == 2) {
+        switch (op.bn) {
+        case 64: return launch_epi<64, 2>(op.epi, op.ma, op.mb, g, st);
+        case 128: return launch_epi<128, 2>(op.epi, op.ma, op.mb, g, st);
+        default: return launch_epi<256, 2>(op.epi, op.ma, op.mb, g, st);
+        }
+    }
     switch (op.bn) {
-    case 64: return launch_epi<64>(op.epi, op.ma, op.mb, g, st);
-    case 128: return launch_epi<128>(op.epi, op.ma, op.mb, g, st);
-    default: return launch_epi<256>(op.epi, op.ma, op.mb, g, st);
+    case 64: return launch_epi<64, 4>(op.epi, op.ma, op.mb, g, st);
+    case 128: return launch_epi<128, 4>(op.epi, op.ma, op.mb, g, st);
+    default: return launch_epi<256, 4>(op.epi, op.ma, op.mb, g, st);
     }
 }
 
@@ -181,7 +195,7 @@ extern "C" int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_
         rc = UPPASD_GPU_ECUDA;
     }
     tc::Gemm op;
-    if (!rc) rc = tc::gemm_prepare(op, dA, dB, M, N, K, epilogue, bn);
+    if (!rc) rc = tc::gemm_prepare(op, dA, dB, M, N, K, epilogue, bn, K > 128 ? 4 : 2);
     if (!rc) rc = tc::gemm_run(op, dbias, dY, dCf, dCb, derr, 0);
     int herr = 0;
     if (!rc) {

@@ -10,11 +10,13 @@ namespace tc {
 // A prepared GEMM: shapes, epilogue, tile width and the two TMA tensor maps.
 struct Gemm {
     CUtensorMap ma, mb;
-    int M = 0, N = 0, K = 0, epi = 0, bn = 0;
+    int M = 0, N = 0, K = 0, epi = 0, bn = 0, stages = 4;
 };
 
 // C(M x N) = A(M x K) B(N x K)^T; A, B device bf16 row-major.  Checks shapes and alignment.
-int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int epi, int bn);
+// stages: depth of the TMA ring (2 or 4; 2 lets more CTAs share an SM when K is short).
+int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int epi, int bn,
+                 int stages = 4);
 // Launch on `st` (capturable).  Outputs/extra operands by epilogue (see tc_gemm.cuh).
 int gemm_run(const Gemm &op, const float *bias, const __nv_bfloat16 *Y, float *Cf, __nv_bfloat16 *Cb, int *err,
              cudaStream_t st);

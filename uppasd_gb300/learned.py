@@ -102,6 +102,13 @@ class LearnedProposal:
                   C.byref(de))
         return int(a.value), int(p.value), float(de.value)
 
+    def mix(self, temperature: float, ncycles: int, hb_per_cycle: int = 1):
+        """ncycles of (hb_per_cycle structured heat-bath sweeps + one learned sweep), one sync."""
+        a, p, de = C.c_int64(), C.c_int64(), C.c_double()
+        _lib.call("uppasd_gpu_proposal_mix", self.h, float(temperature), int(ncycles), int(hb_per_cycle),
+                  C.byref(a), C.byref(p), C.byref(de))
+        return int(a.value), int(p.value), float(de.value)
+
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             _lib.call("uppasd_gpu_proposal_destroy", self.h)

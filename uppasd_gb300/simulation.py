@@ -141,8 +141,16 @@ class GpuSimulation:
     def evolve(self, nsteps: int):
         _lib.call("uppasd_gpu_sd_run", self._h, int(nsteps))
 
-    def relax(self, mode: str = "H", temperature: float = 1.0, nsweeps: int = 1):
-        """Monte Carlo sweeps: mode 'M' (Metropolis) or 'H' (heat bath)."""
+    def relax(self, mode: str = "H", temperature: float = 1.0, nsweeps: int = 1, structured: bool = False):
+        """Monte Carlo sweeps: mode 'M' (Metropolis) or 'H' (heat bath).  structured=True
+        runs the square-lattice heat bath (FP32 draws, uniform couplings recognised at
+        the first call)."""
+        if structured:
+            if mode != "H":
+                raise ValueError("the structured path is a heat bath")
+            L = int(round(np.sqrt(self.lat.natom)))
+            _lib.call("uppasd_gpu_mc_run_square", self._h, L, float(temperature), int(nsweeps))
+            return
         _lib.call("uppasd_gpu_mc_run", self._h, mode.encode()[:1], float(temperature), int(nsweeps))
 
     def set_stream(self, cuda_stream_handle: int):
