@@ -462,7 +462,7 @@ def run_c3(args, peak_tf):
     learned_ms = timed(lambda n: prop.mix(T, n, 0), 100)
     structured_ms = timed(lambda n: sim.relax("H", T, n, structured=True), 2000)
     plain_ms = timed(lambda n: sim.relax("H", T, n), 200)
-    modes = [("plain_fp64_heat_bath", 1, 0, 1500, True), ("batched_heat_bath", 1, 0, 6000, False),
+    modes = [("plain_fp64_heat_bath", 1, 0, 6000, True), ("batched_heat_bath", 1, 0, 6000, False),
              ("learned", 0, 1, 3000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
     res = _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms)
     rows = c["chains"] * (c["L"] // 8) ** 2
@@ -680,6 +680,8 @@ def main():
     ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
     ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
+    ap.add_argument("--c3-profile", action="store_true",
+                    help="two learned sweeps of the learned-proposal workload (kernel profiling)")
     ap.add_argument("--mc-therm", type=int, default=10000)
     ap.add_argument("--mc-meas", type=int, default=100000)
     args = ap.parse_args()
@@ -690,6 +692,18 @@ def main():
         run_reference(args, w)
     elif args.mc_only:
         run_mc_only(args)
+    elif args.c3_profile:
+        from uppasd_gb300 import build as b
+        from uppasd_gb300 import lattice
+        from uppasd_gb300.learned import LearnedProposal
+        from uppasd_gb300.simulation import GpuSimulation
+
+        b.build()
+        c = C3
+        lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, c["bz"], 1.0).with_ensembles(c["chains"])
+        sim = GpuSimulation(lat, emom=random_state(c["chains"], lat.natom, seed=1), seed=2)
+        prop = LearnedProposal(sim, c["L"], eta_scale=c["eta_scale"], seed=3)
+        print(json.dumps({"learned_sweeps": 2, "accepted_proposed": prop.mix(c["T"], 2, 0)[:2]}), flush=True)
     elif args.c3_only:
         import torch
 

@@ -740,10 +740,11 @@ int structured_sync_state(Sim &s) {
 template <int NSH, int LC>
 static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
     if constexpr (LC != 0) {
-        // compiled cubic sizes: NZ sites per thread stacked in z (NZ divides LC).
-        // The corrector's per-site update (master renormalisation) is heavier, so it
-        // takes fewer sites per thread to keep occupancy.
-        constexpr int NZP = LC % 4 == 0 ? 4 : 2;
+        // compiled cubic sizes: NZ sites per thread stacked in z (NZ divides LC).  Two
+        // sites per thread in both kernels: on the 100^3 alloy NZ = 4 in the predictor
+        // was 5-10 % slower (a larger unrolled body stalls on instruction fetch) and
+        // NZ = 1 in either kernel 5-10 % slower (fewer shared neighbour loads).
+        constexpr int NZP = 2;
         constexpr int NZC = 2;
         const unsigned nyt = (unsigned)((f->p.L2 + f->block.y - 1) / f->block.y);
         if (phase & 1)
