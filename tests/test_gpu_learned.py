@@ -92,7 +92,9 @@ def test_accepted_energy_change_is_exact(k_mry):
     assert acc > 0
     measured = np.sum(e1 - e0) * lat.natom * MRY
     scale = np.sum(np.abs(e0)) * lat.natom * MRY
-    assert abs(measured - dE) <= 1e-10 * scale + 1e-12 * abs(dE), (measured, dE)
+    # neighbour-list kernel: FP64 throughout; uniform-lattice kernel: FP32 bond sums
+    tol = 1e-10 if k_mry != 0.0 else 1e-8
+    assert abs(measured - dE) <= tol * scale + 1e-12 * abs(dE), (measured, dE)
     prop.close()
     sim.close()
 

@@ -285,7 +285,10 @@ struct SqCoup {
 
 // One warp per patch on a uniform square lattice: lanes 0-15 score the new patch,
 // lanes 16-31 the old one (bonds leaving the patch in full, bonds inside it at one
-// half, Zeeman on site), FP64; then the Metropolis-Hastings decision and write-back.
+// half, Zeeman on site); then the Metropolis-Hastings decision and write-back.
+// Each lane's bond sum is FP32 (a bond term is at most |J| m ~ 500 T muB, rounded to
+// ~3e-5), the patch sums and the decision FP64: the log acceptance carries an error
+// of ~1e-5 / T[K], far below any statistical resolution.
 __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D e, Vec3D eM, int natom, int rows,
                                                    const double *old_patch, const double *new_patch,
                                                    const double *logq_old, const double *logq_new, double beta_mub,
@@ -300,33 +303,34 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
     const int s = lane & 15, py = s >> 2, px = s & 3;
     const double *patch = (lane < 16 ? new_patch : old_patch) + (size_t)r * 48;
     const double ei[3] = {patch[3 * s], patch[3 * s + 1], patch[3 * s + 2]};
+    const float fi[3] = {(float)ei[0], (float)ei[1], (float)ei[2]};
     const size_t off = (size_t)k * natom;
-    double E = -(q.ext[0] * ei[0] + q.ext[1] * ei[1] + q.ext[2] * ei[2]);
+    float E = -(q.ext[0] * fi[0] + q.ext[1] * fi[1] + q.ext[2] * fi[2]);
     const int ddx[4] = {1, -1, 0, 0}, ddy[4] = {0, 0, 1, -1};
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
         const int nx = px + ddx[d], ny = py + ddy[d];
-        double ej[3], w;
+        float ej[3], w;
         if (nx >= 0 && nx < 4 && ny >= 0 && ny < 4) {
             const int sj = ny * 4 + nx;
-            ej[0] = patch[3 * sj];
-            ej[1] = patch[3 * sj + 1];
-            ej[2] = patch[3 * sj + 2];
-            w = 0.5;
+            ej[0] = (float)patch[3 * sj];
+            ej[1] = (float)patch[3 * sj + 1];
+            ej[2] = (float)patch[3 * sj + 2];
+            w = 0.5f;
         } else {
             const size_t o = off + wrap_site(x0 + nx, y0 + ny, g.L);
-            ej[0] = e.x[o];
-            ej[1] = e.y[o];
-            ej[2] = e.z[o];
-            w = 1.0;
+            ej[0] = (float)e.x[o];
+            ej[1] = (float)e.y[o];
+            ej[2] = (float)e.z[o];
+            w = 1.0f;
         }
-        const double cx = ei[1] * ej[2] - ei[2] * ej[1], cy = ei[2] * ej[0] - ei[0] * ej[2],
-                     cz = ei[0] * ej[1] - ei[1] * ej[0];
-        E -= w * ((double)q.c[d] * (ei[0] * ej[0] + ei[1] * ej[1] + ei[2] * ej[2]) +
-                  ((double)q.d[d][0] * cx + (double)q.d[d][1] * cy + (double)q.d[d][2] * cz));
+        const float cx = fi[1] * ej[2] - fi[2] * ej[1], cy = fi[2] * ej[0] - fi[0] * ej[2],
+                    cz = fi[0] * ej[1] - fi[1] * ej[0];
+        E -= w * (q.c[d] * (fi[0] * ej[0] + fi[1] * ej[1] + fi[2] * ej[2]) +
+                  (q.d[d][0] * cx + q.d[d][1] * cy + q.d[d][2] * cz));
     }
-    E *= (double)q.mom;
-    double dE = lane < 16 ? E : -E;
+    E *= q.mom;
+    double dE = lane < 16 ? (double)E : -(double)E;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
     const double loga = -beta_mub * dE + logq_old[r] - logq_new[r];
