@@ -149,13 +149,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+# DRAM read + write bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum),
+# scaled to the bench sizes by the units processed: profiles/stencil_zblock_alloy64.md
+# (alloy 64^3 capture x 3.815 sites) and profiles/mb_sweeps_mc64.md (40 sweeps x 250/40).
+PROFILED_TRAFFIC = {
+    "stencil_zblock_correct:alloy2m:p1": 1.928e9,
+    "stencil_zblock_predict:alloy2m:p1": 0.858e9,
+    "mb_sweeps:mc64": 12.8e9,
+}
+
+
 def profiled_traffic(name):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(p):
-        d = json.load(open(p))
-        return d.get(name)
-    return None
+    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summaries."""
+    return PROFILED_TRAFFIC.get(name)
 
 
 def cpu_baseline(w, lat, e0, threads, target_s=12.0):
@@ -555,8 +561,8 @@ def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic):
 
 
 PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master"}
-KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_predict", "stencil_correct"),
-                2: ("stencil_predict", "stencil_correct")}
+KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_zblock_predict", "stencil_zblock_correct"),
+                2: ("stencil_zblock_predict", "stencil_zblock_correct")}
 
 
 def run_gb300(args, w):
