@@ -212,6 +212,17 @@ int uppasd_gpu_mcbatch_get_spins(uppasd_gpu_mcbatch *b, double *emom);
 int uppasd_gpu_mcbatch_put_spins(uppasd_gpu_mcbatch *b, const double *emom);
 /* Sweep counter (the Philox step of the next sweep). */
 int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
+/* Replica exchange (the swap step of MonteCarlo/pt_driver.f90:58-367 on the batch):
+ * after every launch, replicas holding adjacent temperatures of one size swap
+ * their temperatures with probability min(1, exp((beta_a - beta_b)(E_a - E_b))),
+ * even and odd ladder pairs alternately.  Statistics and series then belong to
+ * the temperature slots (the original replica order of temperature[]); spins
+ * stay with their replica. */
+int uppasd_gpu_mcbatch_set_exchange(uppasd_gpu_mcbatch *b, int32_t enable);
+/* slot_of_rep (nrep), ladder pairs of slots (npairs x 2), attempts and accepts per
+ * pair; any output may be NULL, *npairs is always written. */
+int uppasd_gpu_mcbatch_exchange_state(uppasd_gpu_mcbatch *b, int32_t *slot_of_rep, int32_t *npairs,
+                                      int32_t *pairs, int64_t *attempts, int64_t *accepts);
 
 /* ---- BF16 tensor-core GEMM (tcgen05, TMEM accumulator, TMA operands) -------
  * No counterpart in the reference: the dense contraction of the learned patch

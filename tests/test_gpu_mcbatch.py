@@ -202,3 +202,41 @@ def test_full_replica_table_invariants():
         E = o.energy()["total"][0]
         assert abs(st["last"][r, 0] - E) <= 2e-5 * abs(E), (r, st["last"][r, 0], E)
     b.close()
+
+
+def test_replica_exchange_keeps_the_distribution():
+    """Temperature swaps between ladder neighbours: the slots stay a permutation
+    within each size, swaps are accepted, and per-temperature E and |M| agree with
+    the same table run without exchange within 3 sigma (independent replicas per
+    temperature on each side)."""
+    Ts = list(np.linspace(900.0, 1500.0, 8))
+    copies = 6
+    L = [6] * (8 * copies)
+    T = Ts * copies
+    res = {}
+    for ex in (False, True):
+        b = ReplicaBatch(L, T, seed=41 + ex, series_len=2000, max_sweeps_per_launch=16)
+        if ex:
+            # exchange within each copy of the ladder only: build one batch per copy
+            b.close()
+            stats = []
+            for c in range(copies):
+                bb = ReplicaBatch([6] * 8, Ts, seed=100 + c, series_len=2000, max_sweeps_per_launch=16)
+                bb.set_exchange(True)
+                bb.run(400, 4)
+                bb.run(2000, 4, measure=True)
+                slot, pairs, att, acc = bb.exchange_state()
+                assert sorted(slot.tolist()) == list(range(8))
+                assert att.sum() > 0 and acc.sum() > 0
+                stats.append(bb.series())
+                bb.close()
+            s = np.concatenate(stats, axis=0)  # (copies*8, n, 2), slot order per copy
+        else:
+            b.run(400, 4)
+            b.run(2000, 4, measure=True)
+            s = b.series()
+            b.close()
+        per_t = s.reshape(copies, 8, -1, 2).mean(axis=2)  # (copies, T, 2)
+        res[ex] = (per_t.mean(axis=0), per_t.std(axis=0, ddof=1) / np.sqrt(copies))
+    (m0, s0), (m1, s1) = res[False], res[True]
+    assert np.all(np.abs(m0 - m1) <= 3.5 * np.hypot(s0, s1) + 1e-12), (m0, m1, s0, s1)

@@ -92,6 +92,25 @@ class ReplicaBatch:
     def set_sweep(self, sweep: int):
         _lib.call("uppasd_gpu_mcbatch_set_sweep", self.h, int(sweep))
 
+    # ---- replica exchange ----
+    def set_exchange(self, enable: bool = True):
+        """Swap temperatures between ladder neighbours (same L) after every launch."""
+        _lib.call("uppasd_gpu_mcbatch_set_exchange", self.h, 1 if enable else 0)
+
+    def exchange_state(self):
+        """(slot_of_replica, pairs (n, 2) of slots, attempts, accepts)."""
+        n = C.c_int32()
+        _lib.call("uppasd_gpu_mcbatch_exchange_state", self.h, None, C.byref(n), None, None, None)
+        slot = np.zeros(self.nrep, dtype=np.int32)
+        pairs = np.zeros((max(n.value, 1), 2), dtype=np.int32)
+        att = np.zeros(max(n.value, 1), dtype=np.int64)
+        acc = np.zeros(max(n.value, 1), dtype=np.int64)
+        _lib.call("uppasd_gpu_mcbatch_exchange_state", self.h, self._p(slot, _lib.I32P), C.byref(n),
+                  self._p(pairs, _lib.I32P), att.ctypes.data_as(C.POINTER(C.c_int64)),
+                  acc.ctypes.data_as(C.POINTER(C.c_int64)))
+        k = n.value
+        return slot, pairs[:k], att[:k], acc[:k]
+
     # ---- results ----
     def raw_stats(self):
         acc = np.zeros((self.nrep, 10))

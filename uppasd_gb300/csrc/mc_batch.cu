@@ -70,6 +70,7 @@ struct MBRep {
     int cta_first, cta_count;
     double e_scale;         // unit-vector energy sum -> mRy per atom: m muB / mRy / N
     double m_scale;         // unit-vector moment sum -> muB per atom: m / N
+    int slot;               // temperature slot held (replica exchange moves slots between replicas)
 };
 
 struct MBParams {
@@ -92,6 +93,13 @@ struct MBParams {
     long long *rep_ns;        // per replica: ns the group spent in the last launch
     uint64_t seed;
     long long spin_limit;
+    // replica exchange (parallel tempering) between adjacent temperatures of one size
+    int *rep_of_slot;             // replica currently at each temperature slot
+    const double *slot_beta;      // 1 / (kB T) of each slot (1/J)
+    const int2 *pairs;            // (slot a, slot b) ladder neighbours: even pairs then odd pairs
+    int npair[2];                 // number of even / odd pairs
+    long long *pt_ctr;            // exchange counter (parity of the next attempt)
+    unsigned long long *pt_att, *pt_acc;  // attempts / accepts per pair (pairs array order)
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long *a) {
@@ -133,7 +141,6 @@ __device__ __forceinline__ bool group_barrier(const MBParams &p, int r, int n) {
     return failed == 0;
 }
 
-__device__ __forceinline__ int wrapi(int v, int L) { return v < 0 ? v + L : (v >= L ? v - L : v); }
 
 // Exchange field on site (b, x, y, z) of parity p and colour-array index t, in Tesla,
 // from the unit-vector neighbours; `rep` points at the replica's four colour arrays.
@@ -358,12 +365,13 @@ __global__ void __launch_bounds__(kMBMaxThreads) mb_recount(MBParams p) {
 __global__ void mb_scan(MBParams p, int nsweeps) {
     const int r = blockIdx.x, lane = threadIdx.x;
     const MBRep R = p.reps[r];
+    const int sl = R.slot;  // statistics and series belong to the temperature, not the replica
     const bool meas = *p.measuring != 0;
     double run[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) run[q] = p.base[4 * r + q];
     double s[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    const long long n0 = p.nsample[r];
+    const long long n0 = p.nsample[sl];
     for (int c0 = 0; c0 < nsweeps; c0 += 32) {
         const int sw = c0 + lane;
         double d[4] = {0.0, 0.0, 0.0, 0.0};
@@ -400,7 +408,7 @@ __global__ void mb_scan(MBParams p, int nsweeps) {
                 s[8] += Mz;
                 s[9] += M2 * Ma;
                 if (p.series_len > 0) {
-                    double *o = p.series + 2 * ((size_t)r * p.series_len + (size_t)((n0 + sw) % p.series_len));
+                    double *o = p.series + 2 * ((size_t)sl * p.series_len + (size_t)((n0 + sw) % p.series_len));
                     o[0] = E;
                     o[1] = Ma;
                 }
@@ -422,13 +430,48 @@ __global__ void mb_scan(MBParams p, int nsweeps) {
     }
     if (lane == 0) {
         if (meas) {
-            for (int q = 0; q < 10; ++q) p.acc[10 * r + q] += s[q];
-            p.nsample[r] = n0 + nsweeps;
+            for (int q = 0; q < 10; ++q) p.acc[10 * sl + q] += s[q];
+            p.nsample[sl] = n0 + nsweeps;
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) p.base[4 * r + q] = 0.0;
         if (r == 0) *p.sweep_ctr += nsweeps;
     }
+}
+
+// Replica exchange between adjacent temperatures of one ladder (one system size),
+// even pairs and odd pairs on alternate calls: swap with probability
+// min(1, exp((beta_a - beta_b)(E_a - E_b))), E the total energy of the replica
+// holding each slot after its last sweep (pt_driver.f90:58-367 restated on the
+// batch).  A swap exchanges the temperature parameters of the two replicas; the
+// spins stay where they are.  One thread per pair; pairs of one parity are disjoint.
+__global__ void mb_swap(MBParams p, MBRep *reps) {
+    const long long c = *p.pt_ctr;
+    const int par = (int)(c & 1);
+    const int n = p.npair[par], first = par ? p.npair[0] : 0;
+    for (int q = threadIdx.x; q < n; q += blockDim.x) {
+        const int2 pr = p.pairs[first + q];
+        const int ra = p.rep_of_slot[pr.x], rb = p.rep_of_slot[pr.y];
+        const MBRep A = reps[ra], B = reps[rb];
+        const double ea = p.last[4 * ra] * (double)(4 * A.nhalf) * kMry;
+        const double eb = p.last[4 * rb] * (double)(4 * B.nhalf) * kMry;
+        const double x = (p.slot_beta[pr.x] - p.slot_beta[pr.y]) * (ea - eb);
+        const Philox4 w = philox_draw(p.seed, first + q, 0, c, kStreamLearned + 3u);
+        atomicAdd(p.pt_att + first + q, 1ull);
+        if (x >= 0.0 || log(u01_open(w.x)) < x) {
+            atomicAdd(p.pt_acc + first + q, 1ull);
+            reps[ra].beta_mu = B.beta_mu;
+            reps[ra].delta = B.delta;
+            reps[ra].slot = B.slot;
+            reps[rb].beta_mu = A.beta_mu;
+            reps[rb].delta = A.delta;
+            reps[rb].slot = A.slot;
+            p.rep_of_slot[pr.x] = rb;
+            p.rep_of_slot[pr.y] = ra;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) *p.pt_ctr = c + 1;
 }
 
 }  // namespace
@@ -450,6 +493,15 @@ struct uppasd_gpu_mcbatch {
     cudaGraphExec_t graph = nullptr;
     int graph_sweeps = 0;
     int measuring_h = 0;
+    // replica exchange
+    bool exchange = false;
+    std::vector<double> temperature;   // per slot
+    int *rep_of_slot_d = nullptr;
+    double *slot_beta_d = nullptr;
+    int2 *pairs_d = nullptr;
+    long long *pt_ctr_d = nullptr;
+    unsigned long long *pt_att_d = nullptr, *pt_acc_d = nullptr;
+    std::vector<int2> pairs_h;
 };
 
 namespace {
@@ -460,9 +512,10 @@ void mb_free(uppasd_gpu_mcbatch *b) {
     if (!b) return;
     if (b->stream) cudaStreamSynchronize(b->stream);
     if (b->graph) cudaGraphExecDestroy(b->graph);
-    void *ptrs[] = {b->reps_d,  b->cta_rep_d, b->measuring_d, b->p.pool,    b->p.bar,       b->p.err,    b->p.delta,
-                    b->p.base,  b->p.acc,     b->p.last,      b->p.series,  b->p.nsample,   b->p.sweep_ctr,
-                    b->p.rep_ns};
+    void *ptrs[] = {b->reps_d,  b->cta_rep_d, b->measuring_d, b->p.pool,      b->p.bar,       b->p.err,
+                    b->p.delta, b->p.base,    b->p.acc,       b->p.last,      b->p.series,    b->p.nsample,
+                    b->p.sweep_ctr, b->p.rep_ns, b->rep_of_slot_d, b->slot_beta_d, b->pairs_d, b->pt_ctr_d,
+                    b->pt_att_d, b->pt_acc_d};
     for (void *q : ptrs) cudaFree(q);
     if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -545,6 +598,11 @@ int install(uppasd_gpu_mcbatch *b, int build, int threads, const std::vector<int
                   ")");
         return UPPASD_GPU_EINVAL;
     }
+    cudaError_t es = cudaStreamSynchronize(b->stream);
+    // the device copy holds the current temperature of each replica (exchange moves them)
+    if (es == cudaSuccess)
+        es = cudaMemcpy(b->reps.data(), b->reps_d, b->reps.size() * sizeof(MBRep), cudaMemcpyDeviceToHost);
+    if (es != cudaSuccess) return cuda_fail("mcbatch schedule", es);
     std::vector<int> map;
     map.reserve((size_t)tot);
     for (size_t i = 0; i < b->reps.size(); ++i) {
@@ -593,6 +651,7 @@ int enqueue_chunk(uppasd_gpu_mcbatch *b, int n) {
     cudaError_t e = cudaLaunchKernelEx(&cfg, sweep_kernel(b->kind, b->build), p, n);
     if (e != cudaSuccess) return cuda_fail("mcbatch sweep launch", e);
     uppasd::mb_scan<<<p.nrep, 32, 0, b->stream>>>(p, n);
+    if (b->exchange) uppasd::mb_swap<<<1, 256, 0, b->stream>>>(p, b->reps_d);
     e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("mcbatch launch", e);
     return UPPASD_GPU_OK;
@@ -788,6 +847,8 @@ int uppasd_gpu_mcbatch_create(int32_t nrep, const int32_t *L, const double *temp
         R.beta_mu = (float)(uppasd::kMub * mom / (uppasd::kKbolt * temperature[i]));
         R.delta = (float)((double)(2.0f / 25.0f) * pow(uppasd::kKbolt * temperature[i] / uppasd::kMub, 0.20));
         R.heatbath = heatbath ? (heatbath[i] ? 1 : 0) : 1;
+        R.slot = i;
+        b->temperature.push_back(temperature[i]);
         const double natom = 4.0 * (double)R.nhalf;  // 2 L^3
         R.e_scale = mom * uppasd::kMub / uppasd::kMry / natom;
         R.m_scale = mom / natom;
@@ -812,6 +873,27 @@ int uppasd_gpu_mcbatch_create(int32_t nrep, const int32_t *L, const double *temp
     al((void **)&b->p.sweep_ctr, sizeof(long long));
     al((void **)&b->p.rep_ns, (size_t)nrep * sizeof(long long));
     if (series_len > 0) al((void **)&b->p.series, (size_t)nrep * series_len * 2 * sizeof(double));
+    al((void **)&b->rep_of_slot_d, (size_t)nrep * sizeof(int));
+    al((void **)&b->slot_beta_d, (size_t)nrep * sizeof(double));
+    al((void **)&b->pt_ctr_d, sizeof(long long));
+    if (e == cudaSuccess) {
+        std::vector<int> id(nrep);
+        std::vector<double> beta(nrep);
+        for (int i = 0; i < nrep; ++i) {
+            id[i] = i;
+            beta[i] = 1.0 / (uppasd::kKbolt * temperature[i]);
+        }
+        e = cudaMemcpy(b->rep_of_slot_d, id.data(), nrep * sizeof(int), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(b->slot_beta_d, beta.data(), nrep * sizeof(double), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) {
+        int rc = cuda_fail("mcbatch_create", e);
+        mb_free(b);
+        return rc;
+    }
+    // the device copy of the replica table is authoritative from here on (replica
+    // exchange edits temperatures in place; install() reads it back)
+    if (e == cudaSuccess) e = cudaMemcpy(b->reps_d, b->reps.data(), nrep * sizeof(MBRep), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         int rc = cuda_fail("mcbatch_create", e);
         mb_free(b);
@@ -823,6 +905,9 @@ int uppasd_gpu_mcbatch_create(int32_t nrep, const int32_t *L, const double *temp
     b->p.series_len = series_len;
     b->p.measuring = b->measuring_d;
     b->p.seed = seed;
+    b->p.rep_of_slot = b->rep_of_slot_d;
+    b->p.slot_beta = b->slot_beta_d;
+    b->p.pt_ctr = b->pt_ctr_d;
     b->p.spin_limit = 1LL << 25;  // x ~32-100 ns naps: a stalled group gives up within seconds
     // initial state: uniform on the sphere, Philox (site, replica, 0, stream kStreamLearned + 1)
     {
@@ -1121,6 +1206,87 @@ int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep) {
     cudaError_t e = cudaStreamSynchronize(b->stream);
     if (e == cudaSuccess) e = cudaMemcpy(b->p.sweep_ctr, &v, sizeof(long long), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail("mcbatch_set_sweep", e);
+    return UPPASD_GPU_OK;
+}
+
+// Replica exchange after every launch (every sweeps_per_launch sweeps) between
+// temperatures adjacent in T among the replicas of one size L.
+int uppasd_gpu_mcbatch_set_exchange(uppasd_gpu_mcbatch *b, int32_t enable) {
+    if (!b) {
+        set_error("mcbatch_set_exchange: null handle");
+        return UPPASD_GPU_EINVAL;
+    }
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_fail("mcbatch_set_exchange", e);
+    if (enable && !b->pairs_d) {
+        // ladders: per size, slots sorted by temperature; even pairs first, then odd pairs
+        std::vector<int> order(b->reps.size());
+        for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+        std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+            return b->reps[a].L != b->reps[c].L ? b->reps[a].L < b->reps[c].L
+                                                 : b->temperature[a] < b->temperature[c];
+        });
+        std::vector<int2> even, odd;
+        for (size_t i = 0; i + 1 < order.size(); ++i) {
+            if (b->reps[order[i]].L != b->reps[order[i + 1]].L) continue;
+            // position within the ladder decides the parity
+            size_t start = i;
+            while (start > 0 && b->reps[order[start - 1]].L == b->reps[order[i]].L) --start;
+            ((i - start) % 2 == 0 ? even : odd).push_back(make_int2(order[i], order[i + 1]));
+        }
+        b->pairs_h = even;
+        b->pairs_h.insert(b->pairs_h.end(), odd.begin(), odd.end());
+        if (b->pairs_h.empty()) {
+            set_error("mcbatch_set_exchange: no two replicas share a size");
+            return UPPASD_GPU_EINVAL;
+        }
+        const size_t np = b->pairs_h.size();
+        e = cudaMalloc(&b->pairs_d, np * sizeof(int2));
+        if (e == cudaSuccess) e = cudaMemcpy(b->pairs_d, b->pairs_h.data(), np * sizeof(int2), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc(&b->pt_att_d, np * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemset(b->pt_att_d, 0, np * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&b->pt_acc_d, np * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemset(b->pt_acc_d, 0, np * sizeof(unsigned long long));
+        if (e != cudaSuccess) return cuda_fail("mcbatch_set_exchange", e);
+        b->p.pairs = b->pairs_d;
+        b->p.npair[0] = (int)even.size();
+        b->p.npair[1] = (int)odd.size();
+        b->p.pt_att = b->pt_att_d;
+        b->p.pt_acc = b->pt_acc_d;
+    }
+    b->exchange = enable != 0;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return UPPASD_GPU_OK;
+}
+
+// slot_of_rep (nrep): the temperature slot each replica holds; pairs (npairs x 2)
+// of slots, attempts and accepts (npairs), any may be NULL; *npairs always set.
+int uppasd_gpu_mcbatch_exchange_state(uppasd_gpu_mcbatch *b, int32_t *slot_of_rep, int32_t *npairs,
+                                      int32_t *pairs, int64_t *attempts, int64_t *accepts) {
+    if (!b || !npairs) {
+        set_error("mcbatch_exchange_state: null argument");
+        return UPPASD_GPU_EINVAL;
+    }
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    std::vector<MBRep> reps(b->reps.size());
+    if (e == cudaSuccess) e = cudaMemcpy(reps.data(), b->reps_d, reps.size() * sizeof(MBRep), cudaMemcpyDeviceToHost);
+    const size_t np = b->pairs_h.size();
+    if (e == cudaSuccess && np && attempts)
+        e = cudaMemcpy(attempts, b->pt_att_d, np * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && np && accepts)
+        e = cudaMemcpy(accepts, b->pt_acc_d, np * sizeof(int64_t), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail("mcbatch_exchange_state", e);
+    *npairs = (int32_t)np;
+    if (slot_of_rep)
+        for (size_t i = 0; i < reps.size(); ++i) slot_of_rep[i] = reps[i].slot;
+    if (pairs)
+        for (size_t q = 0; q < np; ++q) {
+            pairs[2 * q] = b->pairs_h[q].x;
+            pairs[2 * q + 1] = b->pairs_h[q].y;
+        }
     return UPPASD_GPU_OK;
 }
 
