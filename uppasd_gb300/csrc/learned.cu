@@ -41,6 +41,7 @@
 #include "sim.h"
 #include "tc_gemm.cuh"
 #include "tc_host.h"
+#include "tc_mlp.cuh"
 
 namespace uppasd {
 namespace lp {
@@ -569,6 +570,9 @@ struct uppasd_gpu_proposal {
     // prepared GEMMs: forward (rows R) for the current row count
     int prepared_rows = -1;
     uppasd::tc::Gemm fwd[4], bwd[3], wgr[4];
+    // fused forward (tc_mlp.cuh): maps of the input rows and of the four bf16 weights
+    int mlp_rows = -1;
+    CUtensorMap mlp_x, mlp_w[4];
     // one learned sweep captured as a CUDA graph (rebuilt when T or the rows change)
     cudaGraphExec_t sweep_graph = nullptr;
     double graph_T = -1.0;
@@ -668,6 +672,38 @@ int forward(uppasd_gpu_proposal *p, cudaStream_t st) {
     return rc;
 }
 
+// The whole forward pass of the rows in B.X (fused kernel) into B.O.
+int forward_fused(uppasd_gpu_proposal *p, int rows, cudaStream_t st) {
+    auto &B = p->B;
+    if (rows <= 0 || rows % 128 || rows > p->max_rows) {
+        set_error("proposal forward: rows must be a positive multiple of 128 within the buffers");
+        return UPPASD_GPU_EINVAL;
+    }
+    if (p->mlp_rows != rows) {
+        const int nrow[4] = {kHid, kHid, kHid, kOut}, ncol[4] = {kFeat, kHid, kHid, kHid};
+        int rc = tc::make_map(&p->mlp_x, B.X, rows, kFeat, 128);
+        for (int l = 0; l < 4 && !rc; ++l) rc = tc::make_map(&p->mlp_w[l], B.wb[l], nrow[l], ncol[l], nrow[l]);
+        if (rc) return rc;
+        p->mlp_rows = rows;
+    }
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(tc::tc_mlp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tc::mlp_smem_bytes());
+        if (e != cudaSuccess) return cuda_fail("proposal forward attribute", e);
+        attr_set = true;
+    }
+    tc::MlpArgs a{};
+    for (int l = 0; l < 4; ++l) a.bias[l] = p->P.b[l];
+    a.out = B.O;
+    a.rows = rows;
+    a.err = p->err;
+    tc::tc_mlp_kernel<<<rows / 128, tc::kMlpThreads, tc::mlp_smem_bytes(), st>>>(p->mlp_x, p->mlp_w[0], p->mlp_w[1],
+                                                                                  p->mlp_w[2], p->mlp_w[3], a);
+    cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? UPPASD_GPU_OK : cuda_fail("proposal forward", e);
+}
+
 void transpose(const __nv_bfloat16 *src, __nv_bfloat16 *dst, int rows, int cols, cudaStream_t st) {
     dim3 grid((cols + 31) / 32, (rows + 31) / 32);
     k_transpose_bf16<<<grid, dim3(32, 8), 0, st>>>(src, dst, rows, cols);
@@ -736,7 +772,7 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
         PatchGeom g = geom(p, c);
         k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch);
         for (int grp = 0; grp < 4; ++grp) {
-            if ((rc = forward(p, st))) return rc;
+            if ((rc = forward_fused(p, rows, st))) return rc;
             k_vmf_group<<<rows / 8, 128, 0, st>>>(rows, grp, p->eta_scale, p->B.O, p->B.X, p->old_patch,
                                                    p->new_patch, p->logq_old, p->logq_new, p->seed, p->dctr, c * 4 + grp);
         }
@@ -964,8 +1000,7 @@ int uppasd_gpu_proposal_forward(uppasd_gpu_proposal *p, const float *x, int32_t 
         return cuda_fail("proposal_forward", e);
     }
     k_cast_bf16<<<(rows * kFeat + 255) / 256, 256, 0, st>>>(dx, p->B.X, rows * kFeat);
-    int rc = prepare(p, rows);
-    if (!rc) rc = forward(p, st);
+    int rc = forward_fused(p, rows, st);
     if (!rc) rc = check_err(p, st);
     if (!rc) {
         e = cudaMemcpy(out, p->B.O, (size_t)rows * kOut * 4, cudaMemcpyDeviceToHost);

@@ -33,6 +33,8 @@ int encode_fn() {
     return UPPASD_GPU_OK;
 }
 
+}  // namespace
+
 // 2-D bf16 map over a rows x cols row-major matrix, box = 64 columns x box_rows, 128-byte swizzle
 int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows) {
     int rc = encode_fn();
@@ -54,6 +56,8 @@ int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows) 
     }
     return UPPASD_GPU_OK;
 }
+
+namespace {
 
 template <int BN, int EPI, int ST>
 int launch_bn(const CUtensorMap &ma, const CUtensorMap &mb, const GemmArgs &g, cudaStream_t st) {

@@ -17,6 +17,9 @@ struct Gemm {
 // stages: depth of the TMA ring (2 or 4; 2 lets more CTAs share an SM when K is short).
 int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M, int N, int K, int epi, int bn,
                  int stages = 4);
+// 2-D bf16 TMA map over a rows x cols row-major matrix (box 64 columns x box_rows,
+// 128-byte swizzle); checks base alignment and row pitch.
+int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows);
 // Launch on `st` (capturable).  Outputs/extra operands by epilogue (see tc_gemm.cuh).
 int gemm_run(const Gemm &op, const float *bias, const __nv_bfloat16 *Y, float *Cf, __nv_bfloat16 *Cb, int *err,
              cudaStream_t st);
