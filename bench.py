@@ -468,9 +468,17 @@ def run_c3(args, peak_tf):
     learned_ms = timed(lambda n: prop.mix(T, n, 0), 100)
     structured_ms = timed(lambda n: sim.relax("H", T, n, structured=True), 2000)
     plain_ms = timed(lambda n: sim.relax("H", T, n), 200)
-    modes = [("plain_fp64_heat_bath", 1, 0, 6000, True), ("batched_heat_bath", 1, 0, 6000, False),
-             ("learned", 0, 1, 3000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
+    # run lengths in sweeps: 24000 (batched heat bath), 6000 (plain), 6000 (learned), 27000 (8+1):
+    # the slow |M| mode needs long runs for its tau_int estimate to settle
+    modes = [("plain_fp64_heat_bath", 1, 0, 6000, True), ("batched_heat_bath", 1, 0, 24000, False),
+             ("learned", 0, 1, 6000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
     res = _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms)
+    # the plain and the batched heat bath run the same Markov chain (same colours, same
+    # Philox draws): the plain path's samples/s use the longer run's tau_int
+    pb = res["plain_fp64_heat_bath"]
+    pb["tau_M_own_run"], pb["tau_E_own_run"] = pb["tau_M"], pb["tau_E"]
+    pb["tau_M"], pb["tau_E"] = res["batched_heat_bath"]["tau_M"], res["batched_heat_bath"]["tau_E"]
+    pb["indep_samples_per_s"] = c["chains"] / (2.0 * max(pb["tau_M"], pb["tau_E"]) * plain_ms * 1e-3)
     rows = c["chains"] * (c["L"] // 8) ** 2
     flop_pass = 2.0 * rows * (192 * 256 + 2 * 256 * 256 + 256 * 64)
     flops_sweep = 4 * 4 * flop_pass  # 4 colours x 4 passes

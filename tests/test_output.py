@@ -1,0 +1,64 @@
+"""Reference-format output files (uppasd_gb300/output.py): Fortran ES/A editing,
+the cumulant bookkeeping against the oracle's restatement of
+calc_and_print_cumulant (itself pinned to the reference's cumulant rows), and
+round trips through the reference harness's column reading."""
+import ctypes as C
+
+import numpy as np
+
+from oracle import pyoracle as po
+from uppasd_gb300 import output
+
+
+def test_fortran_edit_descriptors():
+    assert output.fortran_es(1.5) == "  1.50000000E+00"
+    assert output.fortran_es(-1.23e-4) == " -1.23000000E-04"
+    assert output.fortran_es(0.0) == "  0.00000000E+00"
+    assert output.fortran_es(1e-120) == "  1.00000000-120"
+    assert output.fortran_es(2.5e3, 12, 4) == "  2.5000E+03"
+    assert output.fortran_a("#Iter", 8) == "   #Iter"
+
+
+def test_cumulants_match_oracle(tmp_path):
+    rng = np.random.default_rng(4)
+    natom, M, T = 128, 2, 640.0
+    cu = po.OrcCumulant()
+    lib = po.load()
+    f = output.CumulantsFile(str(tmp_path / "cumulants.test.out"), natom, T)
+    out = (C.c_double * 6)()
+    for _ in range(30):
+        e = rng.normal(size=(M, natom, 3)) + np.array([0.0, 0.0, 1.0])
+        e /= np.linalg.norm(e, axis=-1, keepdims=True)
+        emomM = np.ascontiguousarray(2.2 * e)
+        en = rng.normal(size=M) - 7.0
+        lib.orc_cumulant_update(C.byref(cu), natom, M, emomM.ctypes.data_as(po.F64P), T,
+                                np.ascontiguousarray(en).ctypes.data_as(po.F64P), out)
+        mabs = np.linalg.norm(emomM.sum(axis=1), axis=1) / natom
+        row = f.add(mabs, en)
+        assert np.allclose(row[:6], list(out), rtol=1e-12, atol=0)
+    cols = output.read_columns(str(tmp_path / "cumulants.test.out"))
+    assert cols.shape == (30, 10) and cols[-1, 0] == 30
+    assert np.allclose(cols[-1, 1:7], list(out), rtol=1e-8)
+
+
+def test_averages_and_restart_round_trip(tmp_path):
+    rng = np.random.default_rng(2)
+    p = str(tmp_path / "averages.test.out")
+    f = output.AveragesFile(p)
+    mv = rng.normal(size=(3, 3))
+    f.write(0, mv)
+    f.write(100, mv * 0.5)
+    cols = output.read_columns(p)
+    m = np.linalg.norm(mv, axis=1)
+    assert cols.shape == (2, 6) and cols[1, 0] == 100
+    assert np.allclose(cols[0, 1:4], mv.mean(axis=0), rtol=1e-8)
+    assert np.isclose(cols[0, 4], m.mean(), rtol=1e-8)
+    assert np.isclose(cols[0, 5], np.sqrt(np.mean(m * m) - m.mean() ** 2), rtol=1e-7)
+    e = rng.normal(size=(2, 5, 3))
+    e /= np.linalg.norm(e, axis=-1, keepdims=True)
+    r = str(tmp_path / "restart.test.out")
+    output.write_restart(r, 1234, e, np.full((2, 5), 2.2))
+    lines = open(r).read().splitlines()
+    assert lines[0].strip() == "1234" and len(lines) == 11
+    vals = np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
+    assert np.allclose(vals[:, 3:], e.reshape(-1, 3), atol=1e-8) and np.all(vals[:, 2] == 2.2)

@@ -1,0 +1,160 @@
+"""Reference-compatible output files, so runs through this library can be checked
+by the reference's own regression harness (its tests read these files by column).
+
+* ``AveragesFile``  -- ``averages.<simid>.out`` of prn_avrg
+  (Measurement/prn_averages.f90:566-651): per measurement, the ensemble means of
+  the average moment vector and of its norm, and the ensemble standard deviation
+  of the norm; header ``(a8,6a16)``, rows ``(i8,6es16.8)`` (``(es12.4,6es16.8)``
+  with real time).
+* ``CumulantsFile`` -- ``cumulants.<simid>.out`` of calc_and_print_cumulant
+  (prn_averages.f90:919-1095): running averages whose weights grow by one per
+  sample, Binder cumulant, susceptibility and specific heat in the reference's
+  units, written every ``cumu_buff`` samples; rows ``(i8,10es16.8)``.
+* ``write_restart`` -- the legacy ``restart.<simid>.out`` of prnrestart
+  (System/restart.f90): ``(i8)`` step, then ``(i8,i8,2x,4es16.8)`` per atom.
+* ``sd_run_with_averages`` -- the measurement cadence of sd_mphase: a row every
+  ``avrg_step`` steps starting at iteration 0.
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+KBOLT = 1.38064852e-23
+MUB = 9.274009994e-24
+MRY = 2.179872325e-21
+DBL_TOLERANCE = float(np.float32(1e-14))
+
+
+def fortran_es(x: float, width: int = 16, digits: int = 8) -> str:
+    """Fortran ``ESw.d``: one digit before the point; exponents beyond two digits drop the E."""
+    s = f"{float(x):.{digits}E}"
+    mant, exp = s.split("E")
+    e = int(exp)
+    tail = f"E{e:+03d}" if abs(e) < 100 else f"{e:+04d}"
+    return (mant + tail).rjust(width)
+
+
+def fortran_a(s: str, width: int) -> str:
+    """Fortran ``Aw`` output: right-justified in the field, truncated on the right."""
+    return s[:width].rjust(width)
+
+
+class AveragesFile:
+    HEADER = ("#Iter", "<M>_x", "<M>_y", "<M>_z", "<M>", "M_{stdv}")
+
+    def __init__(self, path: str, real_time: bool = False):
+        self.path = path
+        self.real_time = real_time
+        self._first = not os.path.exists(path)
+
+    def write(self, index, mvec_per_atom):
+        """mvec_per_atom: (Mensemble, 3) = sum of emomM over atoms / Natom per ensemble."""
+        mv = np.asarray(mvec_per_atom, dtype=np.float64).reshape(-1, 3)
+        m = np.sqrt(np.sum(mv * mv, axis=1))
+        mvm = mv.mean(axis=0)
+        mm = m.mean()
+        ms = np.mean(m * m) - mm * mm  # the reference divides by Mensemble, not Mensemble - 1
+        ms = 0.0 if ms < DBL_TOLERANCE else math.sqrt(ms)
+        with open(self.path, "a") as f:
+            if self._first:
+                head = ("Time[s]",) + self.HEADER[1:] if self.real_time else self.HEADER
+                f.write(fortran_a(head[0], 12 if self.real_time else 8) +
+                        "".join(fortran_a(h, 16) for h in head[1:]) + "\n")
+                self._first = False
+            lead = fortran_es(index, 12, 4) if self.real_time else f"{int(index):8d}"
+            f.write(lead + "".join(fortran_es(v) for v in (*mvm, mm, ms)) + "\n")
+
+
+class CumulantsFile:
+    HEADER = ("#Iter", "<M>", "<M^2>", "<M^4>", "U_{Binder}", "\\chi", "C_v(tot)", "<E>", "<E_{exc}>",
+              "<E_{lsf}>")
+
+    def __init__(self, path: str, natom: int, temperature: float, cumu_buff: int = 1):
+        self.path, self.natom, self.temp, self.cumu_buff = path, int(natom), float(temperature), int(cumu_buff)
+        self.cumuw = self.cumutotw = 0.0
+        self.m = self.m2 = self.m4 = self.e = self.e2 = self.exc = 0.0
+        self.navrgcum = 0
+        self.mensemble = None
+        self._first = not os.path.exists(path)
+
+    def add(self, mabs, energy=None, energy_xc=None):
+        """One measurement: |M| per ensemble (muB/atom), total (and exchange) energy per
+        ensemble in mRy/atom or None.  Returns the row (<M>, <M^2>, <M^4>, U, chi, Cv, <E>,
+        <E_exc>, <E_lsf>) after the update."""
+        mabs = np.atleast_1d(np.asarray(mabs, dtype=np.float64))
+        self.mensemble = mabs.size
+        cumulant = chi = cv = 0.0
+        for k in range(mabs.size):
+            me = mabs[k]
+            self.cumuw += 1.0
+            w0, w = self.cumutotw, self.cumuw
+            self.m = (self.m * w0 + me * w) / (w0 + w)
+            self.m2 = (self.m2 * w0 + me * me * w) / (w0 + w)
+            self.m4 = (self.m4 * w0 + me ** 4 * w) / (w0 + w)
+            cumulant = 1.0 - self.m4 / 3.0 / (self.m2 * self.m2)
+            if self.temp > 0.0:
+                chi = (self.m2 - self.m * self.m) * MUB * MUB * self.natom / (KBOLT * KBOLT) / self.temp
+            else:
+                chi = (self.m2 - self.m * self.m) * self.natom * MUB * MUB / KBOLT
+            if energy is not None and self.temp > 0.0:
+                en = float(np.atleast_1d(energy)[k])
+                self.e = (self.e * w0 + en * w) / (w0 + w)
+                self.e2 = (self.e2 * w0 + en * en * w) / (w0 + w)
+                if energy_xc is not None:
+                    ex = float(np.atleast_1d(energy_xc)[k])
+                    self.exc = (self.exc * w0 + ex * w) / (w0 + w)
+                cv = (self.e2 - self.e * self.e) * MRY * MRY * self.natom / (KBOLT * KBOLT) / (self.temp ** 2)
+            self.navrgcum += 1
+            self.cumutotw += self.cumuw
+        row = (self.m, self.m2, self.m4, cumulant, chi, cv, self.e, self.exc, 0.0)
+        n = self.navrgcum // self.mensemble
+        if (n - 1) % self.cumu_buff == 0:
+            with open(self.path, "a") as f:
+                if self._first:
+                    f.write(fortran_a(self.HEADER[0], 8) + "".join(fortran_a(h, 16) for h in self.HEADER[1:]) + "\n")
+                    self._first = False
+                f.write(f"{n:8d}" + "".join(fortran_es(v) for v in row) + "\n")
+        return row
+
+
+def write_restart(path: str, mstep: int, emom, mmom):
+    """emom (Mensemble, Natom, 3) unit vectors, mmom (Mensemble, Natom)."""
+    emom = np.asarray(emom, dtype=np.float64)
+    mmom = np.broadcast_to(np.asarray(mmom, dtype=np.float64), emom.shape[:2])
+    with open(path, "w") as f:
+        f.write(f"{int(mstep):8d}\n")
+        for k in range(emom.shape[0]):
+            for i in range(emom.shape[1]):
+                f.write(f"{k + 1:8d}{i + 1:8d}  " + fortran_es(mmom[k, i]) +
+                        "".join(fortran_es(v) for v in emom[k, i]) + "\n")
+
+
+def read_columns(path: str):
+    """The reference harness's reading: whitespace-split rows, '#' lines skipped."""
+    rows = []
+    with open(path) as f:
+        for line in f:
+            if line.strip() and not line.lstrip().startswith("#"):
+                rows.append([float(v) for v in line.split()])
+    return np.array(rows)
+
+
+def sd_run_with_averages(sim, nsteps: int, avrg_step: int, path: str):
+    """sd_mphase's measurement cadence: a row at iteration 0 and every avrg_step steps
+    (mstep - 1 divisible by avrg_step), then the steps up to the next measurement."""
+    f = AveragesFile(path)
+    natom = sim.lat.natom
+    it = 0
+    while it <= nsteps:
+        full = sim.get_moments(full=True)
+        emomM = full[1] if isinstance(full, tuple) else full
+        f.write(it, emomM.sum(axis=1) / natom)
+        if it == nsteps:
+            break
+        n = min(avrg_step, nsteps - it)
+        sim.evolve(n)
+        it += n
+    return f
