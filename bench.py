@@ -468,10 +468,11 @@ def run_c3(args, peak_tf):
     learned_ms = timed(lambda n: prop.mix(T, n, 0), 100)
     structured_ms = timed(lambda n: sim.relax("H", T, n, structured=True), 2000)
     plain_ms = timed(lambda n: sim.relax("H", T, n), 200)
-    # run lengths in sweeps: 24000 (batched heat bath), 6000 (plain), 6000 (learned), 27000 (8+1):
-    # the slow |M| mode needs long runs for its tau_int estimate to settle
+    # run lengths in sweeps: 24000 (batched heat bath), 6000 (plain), 24000 (learned), 27000 (8+1):
+    # the slow |M| mode needs long runs for its tau_int estimate to settle, and the modes
+    # are compared at (nearly) equal numbers of sweeps
     modes = [("plain_fp64_heat_bath", 1, 0, 6000, True), ("batched_heat_bath", 1, 0, 24000, False),
-             ("learned", 0, 1, 6000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
+             ("learned", 0, 1, 24000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
     res = _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms)
     # the plain and the batched heat bath run the same Markov chain (same colours, same
     # Philox draws): the plain path's samples/s use the longer run's tau_int
