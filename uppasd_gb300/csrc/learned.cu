@@ -148,7 +148,8 @@ __device__ __forceinline__ int wrap_site(int x, int y, int L) {
 
 // Windows of `rows` patches into X (rows x 192, bf16); optionally the old patch
 // spins (rows x 48, FP64).  One thread per (row, window position).
-__global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat16 *X, double *old_patch) {
+__global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat16 *X, double *old_patch,
+                         float *win) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)rows * 64) return;
     const int r = (int)(t >> 6), pos = (int)(t & 63);
@@ -162,6 +163,13 @@ __global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat1
     xr[0] = __float2bfloat16_rn((float)v[0]);
     xr[1] = __float2bfloat16_rn((float)v[1]);
     xr[2] = __float2bfloat16_rn((float)v[2]);
+    if (win) {
+        // FP32 copy of the window for the acceptance kernel's bonds to the boundary
+        float *wr = win + (size_t)r * kFeat + pos * 3;
+        wr[0] = (float)v[0];
+        wr[1] = (float)v[1];
+        wr[2] = (float)v[2];
+    }
     if (old_patch && wy >= 2 && wy < 6 && wx >= 2 && wx < 6) {
         const int s = (wy - 2) * 4 + (wx - 2);
         double *op = old_patch + (size_t)r * 48 + 3 * s;
@@ -279,6 +287,32 @@ __global__ void __launch_bounds__(128) k_vmf_group(int rows, int g, float eta_sc
     }
 }
 
+// Accepted moves and their energy change summed per block (one warp per patch,
+// lane 0 holds the warp's values): one atomic per block rather than one per patch,
+// which serialised on the counters.  Every warp of the block must reach this.
+__device__ __forceinline__ void block_count(int acc, double dE, unsigned long long *accepted, double *dE_sum) {
+    __shared__ unsigned bacc[32];
+    __shared__ double bde[32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        bacc[w] = acc ? 1u : 0u;
+        bde[w] = acc ? dE : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned a = 0;
+        double d = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) {
+            a += bacc[q];
+            d += bde[q];
+        }
+        if (a) {
+            atomicAdd(accepted, (unsigned long long)a);
+            atomicAdd(dE_sum, d);
+        }
+    }
+}
+
 // Uniform square-lattice couplings (SquareMC) for the patch energy.
 struct SqCoup {
     float c[4], d[4][3], ext[3], mom;
@@ -291,12 +325,12 @@ struct SqCoup {
 // ~3e-5), the patch sums and the decision FP64: the log acceptance carries an error
 // of ~1e-5 / T[K], far below any statistical resolution.
 __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D e, Vec3D eM, int natom, int rows,
-                                                   const double *old_patch, const double *new_patch,
+                                                   const float *win, const double *old_patch, const double *new_patch,
                                                    const double *logq_old, const double *logq_new, double beta_mub,
                                                    uint64_t seed, const long long *dctr, int sub,
                                                    unsigned long long *accepted, double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= rows) return;
+    // rows is a multiple of 128 and blocks hold 8 warps: every warp of the grid is a patch
     const int r = warp;
     const long long ctr = *dctr * 16 + sub;
     int k, x0, y0;
@@ -319,10 +353,11 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
             ej[2] = (float)patch[3 * sj + 2];
             w = 0.5f;
         } else {
-            const size_t o = off + wrap_site(x0 + nx, y0 + ny, g.L);
-            ej[0] = (float)e.x[o];
-            ej[1] = (float)e.y[o];
-            ej[2] = (float)e.z[o];
+            // the boundary site from the window copy (no other patch of this colour touches it)
+            const float *wv = win + (size_t)r * kFeat + ((ny + 2) * 8 + (nx + 2)) * 3;
+            ej[0] = wv[0];
+            ej[1] = wv[1];
+            ej[2] = wv[2];
             w = 1.0f;
         }
         const float cx = fi[1] * ej[2] - fi[2] * ej[1], cy = fi[2] * ej[0] - fi[0] * ej[2],
@@ -342,12 +377,7 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
         acc = (loga >= 0.0 || log(u) < loga) ? 1 : 0;
     }
     acc = __shfl_sync(0xffffffffu, acc, 0);
-    if (!acc) return;
-    if (lane == 0) {
-        atomicAdd(accepted, 1ull);
-        atomicAdd(dE_sum, dE);
-    }
-    if (lane < kSpins) {
+    if (acc && lane < kSpins) {
         const size_t o = off + wrap_site(x0 + px, y0 + py, g.L);
         const double mm = (double)q.mom;
         e.x[o] = ei[0];
@@ -357,6 +387,7 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
         eM.y[o] = mm * ei[1];
         eM.z[o] = mm * ei[2];
     }
+    block_count(acc, dE, accepted, dE_sum);
 }
 
 // Energy of patch spin `s` (site i) in one configuration: bonds to sites outside the
@@ -428,7 +459,7 @@ __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double 
                          const double *logq_new, double beta_mub, uint64_t seed, const long long *dctr, int sub,
                          unsigned long long *accepted, double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (warp >= rows) return;
+    // rows is a multiple of 128 and blocks hold 8 warps: every warp of the grid is a patch
     const int r = warp;
     const long long ctr = *dctr * 16 + sub;
     int k, x0, y0;
@@ -450,12 +481,7 @@ __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double 
         acc = (loga >= 0.0 || log(u) < loga) ? 1 : 0;
     }
     acc = __shfl_sync(0xffffffffu, acc, 0);
-    if (!acc) return;
-    if (lane == 0) {
-        atomicAdd(accepted, 1ull);
-        atomicAdd(dE_sum, dE);
-    }
-    if (lane < kSpins) {
+    if (acc && lane < kSpins) {
         const int py = lane >> 2, px = lane & 3;
         const int i = wrap_site(x0 + px, y0 + py, g.L);
         const size_t o = (size_t)k * h.natom + i;
@@ -468,6 +494,7 @@ __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double 
         eM.y[o] = mm * np_[1];
         eM.z[o] = mm * np_[2];
     }
+    block_count(acc, dE, accepted, dE_sum);
 }
 
 // Loss and output gradient: L = -(1/R) sum_rows sum_s log vMF(x_s; eta_s), eta = scale * O;
@@ -558,6 +585,7 @@ struct uppasd_gpu_proposal {
     long long nparams = 0;
     // sampling
     double *old_patch = nullptr, *new_patch = nullptr, *logq_old = nullptr, *logq_new = nullptr;
+    float *win = nullptr;  // FP32 copy of each row's window (rows x 192)
     unsigned long long *accepted = nullptr;
     double *dE_sum = nullptr, *loss = nullptr;
     int *err = nullptr;
@@ -594,7 +622,7 @@ void free_all(uppasd_gpu_proposal *p) {
     cudaDeviceSynchronize();
     void *ptrs[] = {p->params, p->B.X, p->B.dO, p->B.Xt, p->B.dOt, p->B.O, p->B.gW4t, p->old_patch,
                     p->new_patch, p->logq_old, p->logq_new, p->accepted, p->dE_sum, p->loss, p->err, p->data,
-                    p->dctr};
+                    p->dctr, p->win};
     if (p->sweep_graph) cudaGraphExecDestroy(p->sweep_graph);
     for (void *q : ptrs) cudaFree(q);
     for (int l = 0; l < 3; ++l) {
@@ -770,7 +798,7 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
     int rc;
     for (int c = 0; c < 4; ++c) {
         PatchGeom g = geom(p, c);
-        k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch);
+        k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch, p->win);
         for (int grp = 0; grp < 4; ++grp) {
             if ((rc = forward_fused(p, rows, st))) return rc;
             k_vmf_group<<<rows / 8, 128, 0, st>>>(rows, grp, p->eta_scale, p->B.O, p->B.X, p->old_patch,
@@ -784,7 +812,7 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
             }
             for (int cc = 0; cc < 3; ++cc) q.ext[cc] = s.sq.ext[cc];
             q.mom = s.sq.mom;
-            k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.e, s.eM, s.ham.natom, rows, p->old_patch,
+            k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.e, s.eM, s.ham.natom, rows, p->win, p->old_patch,
                                                                   p->new_patch, p->logq_old, p->logq_new, beta_mub,
                                                                   p->seed, p->dctr, c, p->accepted, p->dE_sum);
         } else {
@@ -874,6 +902,7 @@ int uppasd_gpu_proposal_create(uppasd_gpu_sim *sim, int32_t L, float eta_scale, 
     al((void **)&p->old_patch, (size_t)R * 48 * 8);
     al((void **)&p->new_patch, (size_t)R * 48 * 8);
     al((void **)&p->logq_old, (size_t)R * 8);
+    al((void **)&p->win, (size_t)R * kFeat * 4);
     al((void **)&p->logq_new, (size_t)R * 8);
     al((void **)&p->accepted, sizeof(unsigned long long));
     al((void **)&p->dE_sum, sizeof(double));
@@ -1079,7 +1108,7 @@ int uppasd_gpu_proposal_collect(uppasd_gpu_proposal *p) {
     PatchGeom g = geom(p, -1);
     const long long nt = (long long)rows * 64;
     k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, s.stream>>>(g, s.e, s.ham.natom, rows,
-                                                                 p->data + (size_t)at * kFeat, nullptr);
+                                                                 p->data + (size_t)at * kFeat, nullptr, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("proposal_collect", e);
     p->data_next = at + rows;
