@@ -100,6 +100,16 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *s, double *emom, double *emomM);
 int uppasd_gpu_set_temperature(uppasd_gpu_sim *s, const double *temp_array);
 int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
 
+/* SKKR-style exchange tensor (do_jtensor = 1): j_tens(3,3,max_no_neigh,nHam) in the
+ * reference layout and scaling (Hamiltonian/hamiltoniandata.f90:138), on the exchange
+ * list given at init.  It replaces ncoup in the effective field (tensor_field,
+ * Hamiltonian/hamiltonianactions.f90:499-542, selected at :191-200), in the Monte
+ * Carlo energy change (MonteCarlo/montecarlo_common.f90:502-510) and in the exchange
+ * slot of the energy (the pair energy, Hamiltonian/energy.f90:244-247; as there, no
+ * separate DM energy is evaluated while the tensor is on, the DM field stays).
+ * NULL switches back to ncoup.  -7 on the structured path (precision >= 1). */
+int uppasd_gpu_set_jtensor(uppasd_gpu_sim *s, const double *j_tens);
+
 /* Caller-provided N(0,1) numbers for the next `nsteps` steps, laid out as
  * nsteps consecutive (3, natom, mensemble) blocks (the order the reference's
  * fill_rngarray draws them).  Selects gpu_rng = 1 until exhausted. */

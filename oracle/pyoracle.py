@@ -36,6 +36,7 @@ class OrcHam(C.Structure):
         ("do_dm", C.c_int), ("max_no_dmneigh", C.c_int), ("dmlist", I32P), ("dmlistsize", I32P),
         ("dm_vect", F64P), ("do_aniso", C.c_int), ("taniso", I32P), ("eaniso", F64P),
         ("kaniso", F64P), ("sb", F64P), ("extfield", F64P),
+        ("do_jtensor", C.c_int), ("j_tens", F64P),
     ]
 
 
@@ -145,6 +146,9 @@ class Oracle:
             h.eaniso = _p(keep(lat.eaniso, np.float64))
             h.kaniso = _p(keep(lat.kaniso, np.float64))
             h.sb = _p(keep(lat.sb if lat.sb is not None else np.zeros(N), np.float64))
+        if getattr(lat, "j_tens", None) is not None:
+            h.do_jtensor = 1
+            h.j_tens = _p(keep(lat.j_tens, np.float64))
         self.extfield = keep(np.broadcast_to(lat.extfield, (M, N, 3)), np.float64)
         h.extfield = _p(self.extfield)
         self.ham = h

@@ -259,15 +259,32 @@ static void site_field_aniso(const orc_ham *h, const double *emomM, int i, int k
     }
 }
 
-/* heisenberg_field (:431-466), dzyaloshinskii_moriya_field (:546-580),
- * uniaxial_anisotropy_field (:842-879), cubic_anisotropy_field (:883-919);
+/* tensor_field (:499-542): field(a) = field(a) + J(a,1) m1 + J(a,2) m2 + J(a,3) m3 over
+ * the exchange list.  The reference indexes j_tens by the atom i there although the
+ * array is allocated per Hamiltonian index (hamiltoniandata.f90:138) and the Monte
+ * Carlo energy (montecarlo_common.f90:502-510) indexes it by aham(i); the two agree
+ * whenever the Hamiltonian is not reduced, and aham(i) is used here. */
+static void tensor_exchange(const orc_ham *h, const double *emomM, int i, int ih, int k, double b[3]) {
+    const int N = h->natom;
+    int nn = h->nlistsize[ih];
+    for (int j = 0; j < nn; ++j) {
+        int jn = h->nlist[j + (int64_t)h->max_no_neigh * i] - 1;
+        const double *J = &h->j_tens[9 * (j + (int64_t)h->max_no_neigh * ih)];  /* J(a,b) = J[a + 3b] */
+        double m1 = V3(emomM, 0, jn, k, N), m2 = V3(emomM, 1, jn, k, N), m3 = V3(emomM, 2, jn, k, N);
+        for (int a = 0; a < 3; ++a) b[a] = b[a] + J[a] * m1 + J[a + 3] * m2 + J[a + 6] * m3;
+    }
+}
+
+/* heisenberg_field (:431-466) or tensor_field (:499-542), dzyaloshinskii_moriya_field
+ * (:546-580), uniaxial_anisotropy_field (:842-879), cubic_anisotropy_field (:883-919);
  * accumulation order of effective_field_full (:187-246). */
 static void site_field(const orc_ham *h, const double *emomM, int i, int k, double bs[3], double bq[3]) {
     const int N = h->natom;
     bs[0] = bs[1] = bs[2] = 0.0;
     bq[0] = bq[1] = bq[2] = 0.0;
     int ih = h->aham[i] - 1;
-    int nn = h->nlistsize[ih];
+    int nn = h->do_jtensor == 1 ? 0 : h->nlistsize[ih];
+    if (h->do_jtensor == 1) tensor_exchange(h, emomM, i, ih, k, bs);
     for (int j = 0; j < nn; ++j) {
         int jn = h->nlist[j + (int64_t)h->max_no_neigh * i] - 1;
         double c = h->ncoup[j + (int64_t)h->max_no_neigh * ih];
@@ -796,7 +813,13 @@ static double calculate_energy(const orc_ham *h, const double *emomM, const doub
     int ih = h->aham[iflip] - 1;
     const double *mi = &V3(emomM, 0, iflip, k, N);
     const double *ei = &V3(emom, 0, iflip, k, N);
-    int nn = h->nlistsize[ih];
+    if (h->do_jtensor == 1) {  /* montecarlo_common.f90:502-510 */
+        double bt[3] = {0.0, 0.0, 0.0};
+        tensor_exchange(h, emomM, iflip, ih, k, bt);
+        e_c = e_c - (mi[0] * bt[0] + mi[1] * bt[1] + mi[2] * bt[2]);
+        e_t = e_t - (tm[0] * bt[0] + tm[1] * bt[1] + tm[2] * bt[2]);
+    }
+    int nn = h->do_jtensor == 1 ? 0 : h->nlistsize[ih];
     for (int j = 0; j < nn; ++j) {
         int jn = h->nlist[j + (int64_t)h->max_no_neigh * iflip] - 1;
         double c = h->ncoup[j + (int64_t)h->max_no_neigh * ih];
@@ -1000,13 +1023,18 @@ void orc_energy(const orc_ham *h, const double *emomM, double *e_tot, double *e_
             const double *mi = &V3(emomM, 0, i, k, N);
             int ih = h->aham[i] - 1;
             double bx[3] = {0.0, 0.0, 0.0};
-            for (int j = 0; j < h->nlistsize[ih]; ++j) {
-                int jn = h->nlist[j + (int64_t)h->max_no_neigh * i] - 1;
-                double c = h->ncoup[j + (int64_t)h->max_no_neigh * ih];
-                for (int cc = 0; cc < 3; ++cc) bx[cc] = bx[cc] + c * V3(emomM, cc, jn, k, N);
+            if (h->do_jtensor == 1) {
+                tensor_exchange(h, emomM, i, ih, k, bx);  /* energy.f90:244-247: the pair energy */
+            } else {
+                for (int j = 0; j < h->nlistsize[ih]; ++j) {
+                    int jn = h->nlist[j + (int64_t)h->max_no_neigh * i] - 1;
+                    double c = h->ncoup[j + (int64_t)h->max_no_neigh * ih];
+                    for (int cc = 0; cc < 3; ++cc) bx[cc] = bx[cc] + c * V3(emomM, cc, jn, k, N);
+                }
             }
             exc = exc + (-0.5 * (mi[0] * bx[0] + mi[1] * bx[1] + mi[2] * bx[2]));
-            if (h->do_dm == 1) {
+            /* with the tensor the DM energy is not evaluated (energy.f90:219-247, :371-379) */
+            if (h->do_dm == 1 && h->do_jtensor != 1) {
                 double bd[3] = {0.0, 0.0, 0.0};
                 for (int j = 0; j < h->dmlistsize[ih]; ++j) {
                     int jn = h->dmlist[j + (int64_t)h->max_no_dmneigh * i] - 1;

@@ -80,6 +80,10 @@ typedef struct {
     const double  *kaniso;     /* (2, natom) */
     const double  *sb;         /* (natom) */
     const double  *extfield;   /* (3, natom, mensemble) */
+    /* SKKR-style exchange tensor (hamiltoniandata.f90:138, j_tens(3,3,max_no_neigh,nHam));
+     * with do_jtensor == 1 it replaces ncoup in the field and energies. */
+    int do_jtensor;
+    const double  *j_tens;     /* (3, 3, max_no_neigh, nham) */
 } orc_ham;
 
 /* effective_field_full (hamiltonianactions.f90:108-252).  Returns energy in mRy

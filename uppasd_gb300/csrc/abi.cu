@@ -348,7 +348,7 @@ void destroy(Sim &s) {
     if (s.graph) cudaGraphExecDestroy(s.graph);
     structured_free(s);
     HamDev &h = s.ham;
-    void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
+    void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
                     s.llg.inj, s.llg.d_step, s.red, s.colour_sites};
     for (void *q : ptrs) cudaFree(q);
@@ -521,6 +521,45 @@ int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
     UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.temp, temp_array, sizeof(double) * s.ham.natom, cudaMemcpyHostToDevice,
                                     s.stream));
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_jtensor(uppasd_gpu_sim *w, const double *j_tens) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    uppasd::HamDev &h = s.ham;
+    if (s.precision >= 1) {
+        uppasd::set_error("set_jtensor: the structured path (precision >= 1) covers scalar exchange; use precision 0");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
+    std::vector<double> jt;
+    if (j_tens) {
+        // Fortran j_tens(3,3,max_no_neigh,nHam): J_ab of slot q at a + 3 b + 9 (q + mnn ih)
+        const int mnn = h.mnn, nham = h.nham;
+        jt.resize((size_t)std::max(mnn, 1) * nham * 9, 0.0);
+        for (int ih = 0; ih < nham; ++ih)
+            for (int q = 0; q < mnn; ++q)
+                for (int a = 0; a < 3; ++a)
+                    for (int b = 0; b < 3; ++b) {
+                        const double v = j_tens[a + 3 * b + 9 * (q + (size_t)mnn * ih)];
+                        if (!std::isfinite(v)) {
+                            uppasd::set_error("set_jtensor: non-finite tensor element");
+                            return UPPASD_GPU_EINVAL;
+                        }
+                        jt[((size_t)q * nham + ih) * 9 + 3 * a + b] = v;
+                    }
+    }
+    uppasd::drop_graph(s);
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    cudaFree(h.jt);
+    h.jt = nullptr;
+    h.do_jtensor = 0;
+    s.sq.L = 0;  // the structured square recognition no longer holds
+    if (!j_tens) return UPPASD_GPU_OK;
+    int rc = uppasd::upload(s, &h.jt, jt);
+    if (rc) return rc;
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    h.do_jtensor = 1;
     return UPPASD_GPU_OK;
 }
 

@@ -3,6 +3,7 @@
 // include it are compiled with --fmad=false so every product and sum rounds
 // separately, in the order of the reference's Fortran expressions:
 //   heisenberg_field      Hamiltonian/hamiltonianactions.f90:431-466
+//   tensor_field          Hamiltonian/hamiltonianactions.f90:499-542 (do_jtensor)
 //   dzyaloshinskii_moriya Hamiltonian/hamiltonianactions.f90:546-580
 //   uniaxial / cubic      Hamiltonian/hamiltonianactions.f90:842-919
 //   assembly              Hamiltonian/hamiltonianactions.f90:187-243
@@ -63,6 +64,24 @@ __device__ __forceinline__ void aniso_field(const HamDev &h, int i, double m1, d
     }
 }
 
+// Tensor exchange field of site i: b_a += J_a1 m1 + J_a2 m2 + J_a3 m3 per neighbour,
+// summed left to right as the reference's array expression is.  The tensor is read
+// per Hamiltonian index aham(i), as the Monte Carlo energy (montecarlo_common.f90:502-510)
+// does; tensor_field indexes it by the atom, which is the same for a full Hamiltonian.
+__device__ __forceinline__ void tensor_exchange(const HamDev &h, const Vec3D &m, int i, int ih, size_t off,
+                                                double b[3]) {
+    const int N = h.natom;
+    const int nn = h.nsize[i];
+    for (int s = 0; s < nn; ++s) {
+        int j = __ldg(&h.nlist[(size_t)s * N + i]);
+        const double *J = h.jt + ((size_t)s * h.nham + ih) * 9;
+        double m1 = __ldg(&m.x[off + j]), m2 = __ldg(&m.y[off + j]), m3 = __ldg(&m.z[off + j]);
+        b[0] = b[0] + __ldg(&J[0]) * m1 + __ldg(&J[1]) * m2 + __ldg(&J[2]) * m3;
+        b[1] = b[1] + __ldg(&J[3]) * m1 + __ldg(&J[4]) * m2 + __ldg(&J[5]) * m3;
+        b[2] = b[2] + __ldg(&J[6]) * m1 + __ldg(&J[7]) * m2 + __ldg(&J[8]) * m3;
+    }
+}
+
 // Total effective field of site i in ensemble k from the full moments m.
 __device__ __forceinline__ void site_field(const HamDev &h, const Vec3D &m, int i, int k, double B[3]) {
     const int N = h.natom;
@@ -70,12 +89,16 @@ __device__ __forceinline__ void site_field(const HamDev &h, const Vec3D &m, int 
     double bs[3] = {0.0, 0.0, 0.0}, bq[3] = {0.0, 0.0, 0.0};
     const int ih = h.aham[i];
     const int nn = h.nsize[i];
-    for (int s = 0; s < nn; ++s) {
-        int j = __ldg(&h.nlist[(size_t)s * N + i]);
-        double c = __ldg(&h.ncoup[(size_t)s * h.nham + ih]);
-        bs[0] = bs[0] + c * __ldg(&m.x[off + j]);
-        bs[1] = bs[1] + c * __ldg(&m.y[off + j]);
-        bs[2] = bs[2] + c * __ldg(&m.z[off + j]);
+    if (h.do_jtensor) {
+        tensor_exchange(h, m, i, ih, off, bs);
+    } else {
+        for (int s = 0; s < nn; ++s) {
+            int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            double c = __ldg(&h.ncoup[(size_t)s * h.nham + ih]);
+            bs[0] = bs[0] + c * __ldg(&m.x[off + j]);
+            bs[1] = bs[1] + c * __ldg(&m.y[off + j]);
+            bs[2] = bs[2] + c * __ldg(&m.z[off + j]);
+        }
     }
     if (h.do_dm) {
         const int nd = h.dmsize[i];

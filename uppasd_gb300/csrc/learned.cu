@@ -838,6 +838,10 @@ int uppasd_gpu_proposal_create(uppasd_gpu_sim *sim, int32_t L, float eta_scale, 
     }
     *out = nullptr;
     const Sim &s = sim->s;
+    if (s.ham.do_jtensor) {
+        set_error("proposal_create: the exchange is a tensor; learned patch moves cover scalar exchange");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     if (s.ham.natom != L * L) {
         set_error("proposal_create: the simulation is not an L x L square lattice with one atom per cell");
         return UPPASD_GPU_EINVAL;
@@ -1170,6 +1174,10 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = p->sim->s;
+    if (s.ham.do_jtensor) {
+        set_error("proposal_mix: the exchange became a tensor after the proposal was created");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     cudaStream_t st = s.stream;
     const int rows = s.ham.mensemble * (p->L / 8) * (p->L / 8);
     int rc = prepare(p, rows);

@@ -54,12 +54,20 @@ __device__ double delta_energy(const HamDev &h, const Vec3D &eM, const Vec3D &e,
     double mi[3] = {eM.x[off + i], eM.y[off + i], eM.z[off + i]};
     double ei[3] = {e.x[off + i], e.y[off + i], e.z[off + i]};
     const int ih = h.aham[i];
-    for (int s = 0; s < h.nsize[i]; ++s) {
-        int j = h.nlist[(size_t)s * N + i];
-        double c = h.ncoup[(size_t)s * h.nham + ih];
-        double mj0 = eM.x[off + j], mj1 = eM.y[off + j], mj2 = eM.z[off + j];
-        e_c = e_c - c * (mi[0] * mj0 + mi[1] * mj1 + mi[2] * mj2);
-        e_t = e_t - c * (tm[0] * mj0 + tm[1] * mj1 + tm[2] * mj2);
+    if (h.do_jtensor) {
+        // montecarlo_common.f90:502-510: the tensor field of the neighbours, then the dot products
+        double bt[3] = {0.0, 0.0, 0.0};
+        tensor_exchange(h, eM, i, ih, off, bt);
+        e_c = e_c - (mi[0] * bt[0] + mi[1] * bt[1] + mi[2] * bt[2]);
+        e_t = e_t - (tm[0] * bt[0] + tm[1] * bt[1] + tm[2] * bt[2]);
+    } else {
+        for (int s = 0; s < h.nsize[i]; ++s) {
+            int j = h.nlist[(size_t)s * N + i];
+            double c = h.ncoup[(size_t)s * h.nham + ih];
+            double mj0 = eM.x[off + j], mj1 = eM.y[off + j], mj2 = eM.z[off + j];
+            e_c = e_c - c * (mi[0] * mj0 + mi[1] * mj1 + mi[2] * mj2);
+            e_t = e_t - c * (tm[0] * mj0 + tm[1] * mj1 + tm[2] * mj2);
+        }
     }
     if (h.do_aniso) {
         int ta = h.taniso[i];

@@ -102,6 +102,7 @@ int square_recognise(Sim &s, int L) {
         return UPPASD_GPU_EUNSUPPORTED;
     };
     if (L < 2 || (L & 1) || N != L * L) return fail("natom must equal L^2 with L even");
+    if (h.do_jtensor) return fail("the exchange is a tensor; the structured path covers scalar exchange");
     std::vector<int32_t> nlist, nsize, aham, dml, dms, ta;
     std::vector<double> nc, dx, dy, dz, mm, ex, ey, ez, k1, k2;
     int bad = to_host(nlist, h.nlist, (size_t)h.mnn * N) | to_host(nsize, h.nsize, N) | to_host(aham, h.aham, N) |

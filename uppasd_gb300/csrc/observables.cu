@@ -33,15 +33,20 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
         v[2] = mi[2];
         const int ih = h.aham[i];
         double bx[3] = {0.0, 0.0, 0.0};
-        for (int s = 0; s < h.nsize[i]; ++s) {
-            int j = h.nlist[(size_t)s * N + i];
-            double c = h.ncoup[(size_t)s * h.nham + ih];
-            bx[0] = bx[0] + c * m.x[off + j];
-            bx[1] = bx[1] + c * m.y[off + j];
-            bx[2] = bx[2] + c * m.z[off + j];
+        if (h.do_jtensor) {
+            tensor_exchange(h, m, i, ih, off, bx);  // the pair energy, energy.f90:244-247
+        } else {
+            for (int s = 0; s < h.nsize[i]; ++s) {
+                int j = h.nlist[(size_t)s * N + i];
+                double c = h.ncoup[(size_t)s * h.nham + ih];
+                bx[0] = bx[0] + c * m.x[off + j];
+                bx[1] = bx[1] + c * m.y[off + j];
+                bx[2] = bx[2] + c * m.z[off + j];
+            }
         }
         v[3] = -0.5 * (mi[0] * bx[0] + mi[1] * bx[1] + mi[2] * bx[2]);
-        if (h.do_dm) {
+        // with the tensor the reference evaluates no separate DM energy (energy.f90:219-247, :371-379)
+        if (h.do_dm && !h.do_jtensor) {
             double bd[3] = {0.0, 0.0, 0.0};
             for (int s = 0; s < h.dmsize[i]; ++s) {
                 int j = h.dmlist[(size_t)s * N + i];

@@ -36,6 +36,10 @@ struct HamDev {
     double *eax = nullptr, *eay = nullptr, *eaz = nullptr;  // [natom]
     double *k1 = nullptr, *k2 = nullptr, *sb = nullptr;     // [natom]
     Vec3D ext;                  // [mensemble][natom]
+    // exchange tensor (do_jtensor = 1): J_ab of slot s, Hamiltonian index ih at
+    // jt[(s * nham + ih) * 9 + 3 a + b]; replaces ncoup in fields and energies
+    int do_jtensor = 0;
+    double *jt = nullptr;
 };
 
 struct LlgDev {

@@ -12,6 +12,9 @@ The arrays built here are what UppASD's setup leaves in ``ham_t``
   (hamiltonianinit.f90:895-909)
 * ``extfield``  (mensemble, natom, 3)
 * ``mmom``      (mensemble, natom)
+* ``j_tens``    (nham, mnn, 3, 3)  -- Fortran ``j_tens(3,3,mnn,nham)``: element
+  ``[ih, j, b, a]`` is J_ab of neighbour slot j, same scaling as ncoup; when set it
+  replaces ncoup (do_jtensor = 1, Hamiltonian/hamiltoniandata.f90:138)
 
 Every array is C-ordered with the Fortran axes reversed, so the memory image is
 exactly the Fortran column-major array and can be handed to the C ABI as is.
@@ -48,6 +51,7 @@ class Lattice:
     eaniso: Optional[np.ndarray] = None
     kaniso: Optional[np.ndarray] = None
     sb: Optional[np.ndarray] = None
+    j_tens: Optional[np.ndarray] = None
     # geometry hints for structured kernels (cells along x, y, z and basis size)
     cells: tuple = (0, 0, 0)
     nbasis: int = 1
@@ -251,6 +255,63 @@ def square_dmi(L: int, j_mry: float = 1.0, d_mry: float = 0.3, k_mry: float = -0
                    taniso=taniso, eaniso=eaniso, kaniso=kaniso, sb=np.zeros(natom),
                    cells=(L, L, 1), nbasis=1, periodic=(True, True, False),
                    stencil=np.array([[s[:4] for s in stencil[0]]], dtype=np.int32))
+
+
+def tensor_from_matrices(mats) -> np.ndarray:
+    """(nham, mnn, 3, 3) matrices J[ih, j, a, b] -> the Fortran memory image of j_tens."""
+    return np.ascontiguousarray(np.swapaxes(np.asarray(mats, dtype=np.float64), -1, -2))
+
+
+def with_isotropic_tensor(lat: Lattice) -> Lattice:
+    """The tensor form of a scalar exchange, J_ab = ncoup * delta_ab per neighbour slot, as
+    read_exchange_build_tensor (Input/inputhandler_ext.f90) builds it for calc_jtensor;
+    the DMI list stays a separate term, as the reference's field keeps it."""
+    out = Lattice(**{k: getattr(lat, k) for k in lat.__dataclass_fields__})
+    eye = np.eye(3)
+    out.j_tens = tensor_from_matrices(lat.ncoup[:, :, None, None] * eye)
+    return out
+
+
+_KAGOME_BASIS = np.array([[0.0, 0.0], [0.5, 0.0], [0.0, 0.5]])
+_KAGOME_STENCIL = [
+    [(0, 0, 0, 1, 1), (-1, 0, 0, 1, 1), (0, 0, 0, 2, 1), (0, -1, 0, 2, 1)],
+    [(0, 0, 0, 0, 1), (1, 0, 0, 0, 1), (0, 0, 0, 2, 1), (1, -1, 0, 2, 1)],
+    [(0, 0, 0, 0, 1), (0, 1, 0, 0, 1), (0, 0, 0, 1, 1), (-1, 1, 0, 1, 1)],
+]
+
+
+def kagome(L: int, j_mry: float = -1.0, d_mry: float = 0.1, g_mry: float = 0.05, mom: float = 1.0,
+           bz: float = 0.0) -> Lattice:
+    """Kagome monolayer (triangular cell a1 = (1, 0), a2 = (1/2, sqrt(3)/2), three sites at
+    (0, 0), (1/2, 0), (0, 1/2) in cell units), L x L cells, periodic, nearest neighbours
+    only, with a full exchange tensor per bond (do_jtensor = 1):
+
+        J_ij = j I + g e e^T + [D]_x,   D = d (z x e),   e = unit bond vector i -> j,
+
+    [D]_x the antisymmetric matrix with m_i . [D]_x m_j = D . (m_i x m_j).  J_ji = J_ij^T,
+    so the energy -1/2 sum m_i J_ij m_j is a proper pair sum.  Scaled like ncoup."""
+    natom = 3 * L * L
+    nlist, nsize, _ = _build_from_stencil((L, L, 1), 3, (True, True, False), _KAGOME_STENCIL,
+                                          lambda i, j, sh: np.zeros(i.shape), natom)
+    a1, a2 = np.array([1.0, 0.0, 0.0]), np.array([0.5, np.sqrt(3.0) / 2.0, 0.0])
+    z = np.array([0.0, 0.0, 1.0])
+    mats = np.zeros((3, 4, 3, 3))
+    for bi in range(3):
+        for s, (dx, dy, dz, bj, sh) in enumerate(_KAGOME_STENCIL[bi]):
+            dr = _KAGOME_BASIS[bj] + (dx, dy) - _KAGOME_BASIS[bi]
+            e = dr[0] * a1 + dr[1] * a2
+            e = e / np.linalg.norm(e)
+            D = d_mry * np.cross(z, e)
+            A = np.array([[0.0, D[2], -D[1]], [-D[2], 0.0, D[0]], [D[1], -D[0], 0.0]])
+            mats[bi, s] = (j_mry * np.eye(3) + g_mry * np.outer(e, e) + A) * FC2 / mom / mom
+    jt = tensor_from_matrices(mats[np.arange(natom) % 3])
+    ext = np.zeros((1, natom, 3))
+    ext[..., 2] = bz
+    return Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize,
+                   ncoup=np.zeros((natom, 4)), aham=np.arange(1, natom + 1, dtype=np.int32),
+                   mmom=np.full((1, natom), mom), extfield=ext, j_tens=jt,
+                   cells=(L, L, 1), nbasis=3, periodic=(True, True, False),
+                   stencil=np.array([[s[:4] for s in b] for b in _KAGOME_STENCIL], dtype=np.int32))
 
 
 def greedy_colouring(lat: Lattice):

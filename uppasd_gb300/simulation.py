@@ -86,6 +86,19 @@ class GpuSimulation:
         _lib.call("uppasd_gpu_init", C.byref(c), C.byref(a), C.byref(h))
         self._h = h
         self._keep = []  # init copied everything it needs
+        if lat.j_tens is not None:
+            self.set_jtensor(lat.j_tens)
+
+    def set_jtensor(self, j_tens: Optional[np.ndarray]):
+        """Exchange tensor in the Fortran image (nham, mnn, 3, 3) = j_tens(3,3,mnn,nham);
+        None returns to the scalar couplings."""
+        if j_tens is None:
+            _lib.call("uppasd_gpu_set_jtensor", self._h, None)
+            return
+        jt = np.ascontiguousarray(j_tens, dtype=np.float64)
+        if jt.shape != (self.lat.nham, self.lat.max_no_neigh, 3, 3):
+            raise ValueError(f"j_tens must be (nham, mnn, 3, 3), got {jt.shape}")
+        _lib.call("uppasd_gpu_set_jtensor", self._h, _ptr(jt))
 
     # -- lifecycle --
     def close(self):
