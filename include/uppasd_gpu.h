@@ -135,6 +135,12 @@ int uppasd_gpu_mc_run_square(uppasd_gpu_sim *s, int32_t L, double temperature, i
  * atom in mRy (mensemble); any output may be NULL. */
 int uppasd_gpu_observables(uppasd_gpu_sim *s, double *mvec, double *mabs, double *energy);
 
+/* Per-ensemble energy terms of calc_energy (Hamiltonian/energy.f90:60-405) in mRy per
+ * atom, terms(5, mensemble) = {total, exchange (the pair energy with the tensor),
+ * anisotropy, DM, Zeeman}: the ene%energy / ene_xc / ene_ani / ene_dm / ene_ext values
+ * that totenergy.<simid>.out averages over the ensembles (:407-500). */
+int uppasd_gpu_energy_terms(uppasd_gpu_sim *s, double *terms);
+
 /* Run the library's work on the caller's CUDA stream (a cudaStream_t passed as
  * void*); NULL returns to the library's own stream.  Replaces the reference's
  * two internal streams (cudaParallelizationHelper.hpp:88-175). */

@@ -30,3 +30,25 @@ def test_solvers_averages_file_passes_reference_check(pins, solver, name, tmp_pa
     exp = np.array(pins[name]["expected"])
     got = row[1:5]
     assert np.all(np.abs(got - exp) <= 1e-8 + 0.5 * 10.0 ** (np.floor(np.log10(np.abs(exp))) - 8)), (got, exp)
+
+
+@pytest.mark.parametrize("kind", ["square_dmi", "kagome_tensor"])
+def test_energy_terms_match_oracle_and_write_totenergy(tmp_path, kind):
+    from uppasd_gb300 import lattice as lt
+    lat = (lt.square_dmi(16, 1.0, 0.3, -0.05, 0.5, 1.0) if kind == "square_dmi"
+           else lt.kagome(8, -1.0, 0.1, 0.05, 1.0, 0.2)).with_ensembles(3)
+    rng = np.random.default_rng(51)
+    e0 = rng.normal(size=(3, lat.natom, 3))
+    e0 /= np.linalg.norm(e0, axis=-1, keepdims=True)
+    sim = GpuSimulation(lat, emom=e0)
+    t = sim.energy_terms()
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    ref = o.energy()
+    for k in ("total", "xc", "dm", "ani", "ext"):
+        assert np.allclose(t[k], ref[k], rtol=1e-12, atol=1e-13), k
+    f = output.TotEnergyFile(str(tmp_path / "totenergy.x.out"), tensor=lat.j_tens is not None)
+    f.write(0, t)
+    row = output.read_columns(str(tmp_path / "totenergy.x.out"))[0]
+    assert np.isclose(row[1], ref["total"].mean(), rtol=1e-8)
+    sim.close()

@@ -62,3 +62,27 @@ def test_averages_and_restart_round_trip(tmp_path):
     assert lines[0].strip() == "1234" and len(lines) == 11
     vals = np.array([[float(v) for v in ln.split()] for ln in lines[1:]])
     assert np.allclose(vals[:, 3:], e.reshape(-1, 3), atol=1e-8) and np.all(vals[:, 2] == 2.2)
+
+
+def test_totenergy_layout_and_deviation(tmp_path):
+    rng = np.random.default_rng(5)
+    terms = {k: rng.normal(size=4) for k in ("xc", "ani", "dm", "ext")}
+    terms["total"] = terms["xc"] + terms["ani"] + terms["dm"] + terms["ext"]
+    f = output.TotEnergyFile(str(tmp_path / "totenergy.t.out"), std_path=str(tmp_path / "stdenergy.t.out"))
+    f.write(0, terms)
+    f.write(10, terms)
+    lines = open(tmp_path / "totenergy.t.out").read().splitlines()
+    assert len(lines[0]) == 8 + 13 * 20 and lines[0].split()[:3] == ["#Iter", "Tot", "Exc"]
+    assert all(len(l) == 8 + 13 * 16 for l in lines[1:])
+    cols = output.read_columns(str(tmp_path / "totenergy.t.out"))
+    assert cols[:, 0].tolist() == [0, 10]
+    want = [terms[k].mean() for k in ("total", "xc", "ani", "dm")] + [0.0] * 4 + [terms["ext"].mean()]
+    assert np.allclose(cols[0, 1:10], want, rtol=1e-8, atol=1e-12)
+    fc = output.MUB / output.MRY
+    std = output.read_columns(str(tmp_path / "stdenergy.t.out"))
+    assert np.isclose(std[0, 1], np.var(terms["total"] / fc, ddof=1) * fc, rtol=1e-8)
+    t = output.TotEnergyFile(str(tmp_path / "totenergy.j.out"), tensor=True)
+    t.write(0, terms)
+    lines = open(tmp_path / "totenergy.j.out").read().splitlines()
+    assert lines[0].split()[2] == "Heis-Tens" and len(lines[0]) == 8 + 11 * 16
+    assert len(lines[1]) == 8 + 11 * 16

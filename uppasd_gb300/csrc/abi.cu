@@ -682,4 +682,12 @@ int uppasd_gpu_observables(uppasd_gpu_sim *w, double *mvec, double *mabs, double
     return uppasd::observables(s, mvec, mabs, energy, nullptr);
 }
 
+int uppasd_gpu_energy_terms(uppasd_gpu_sim *w, double *terms) {
+    if (!w || !terms) return UPPASD_GPU_EINVAL;
+    Sim &s = w->s;
+    int rc;
+    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    return uppasd::observables(s, nullptr, nullptr, nullptr, nullptr, terms);
+}
+
 }  // extern "C"

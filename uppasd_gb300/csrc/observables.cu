@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
     }
 }
 
-int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src) {
+int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src, double *terms_h) {
     const int N = s.ham.natom, M = s.ham.mensemble;
     const Vec3D &m = src ? *src : s.eM;
     UPPASD_CUDA_TRY(cudaMemsetAsync(s.red, 0, sizeof(double) * kRedCount * M, s.stream));
@@ -110,9 +110,15 @@ int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const 
             mvec_h[3 * k + 2] = r[kRedMz];
         }
         if (mabs_h) mabs_h[k] = sqrt(r[kRedMx] * r[kRedMx] + r[kRedMy] * r[kRedMy] + r[kRedMz] * r[kRedMz]) / N;
-        if (energy_h) {
-            double xc = r[kRedXc] / N, dm = r[kRedDm] / N, an = r[kRedAni] / N, ex = r[kRedExt] / N;
-            energy_h[k] = (xc + dm + ex + an) * fcinv;
+        double xc = r[kRedXc] / N, dm = r[kRedDm] / N, an = r[kRedAni] / N, ex = r[kRedExt] / N;
+        if (energy_h) energy_h[k] = (xc + dm + ex + an) * fcinv;
+        if (terms_h) {
+            double *t = terms_h + 5 * (size_t)k;
+            t[0] = (xc + dm + ex + an) * fcinv;
+            t[1] = xc * fcinv;
+            t[2] = an * fcinv;
+            t[3] = dm * fcinv;
+            t[4] = ex * fcinv;
         }
     }
     delete[] h;

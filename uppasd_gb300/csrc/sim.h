@@ -106,7 +106,10 @@ namespace uppasd {
 // phase: 1 predictor only, 2 corrector only, 3 both
 int llg_generic_step(Sim &s, int64_t step_offset, int phase = 3);
 // observables.cu
-int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src);
+// terms_h (optional): per ensemble {total, exchange (pair energy with the tensor),
+// anisotropy, DM, Zeeman} in mRy per atom, the per-ensemble values of calc_energy.
+int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src,
+                double *terms_h = nullptr);
 int field_to_host(Sim &s, double *beff_h);
 // mc.cu
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps);

@@ -272,6 +272,27 @@ def with_isotropic_tensor(lat: Lattice) -> Lattice:
     return out
 
 
+def reduced(lat: Lattice) -> Lattice:
+    """The reduced Hamiltonian (do_reduced = 'Y'): one coupling row per basis atom,
+    aHam(i) = anumb(i) (Hamiltonian/hamiltonianinit.f90:818-838, nHam = NA at :185).
+    Valid for translation-invariant lattices, whose rows of one basis atom coincide;
+    raises otherwise.  Neighbour lists, anisotropy and fields stay per atom."""
+    nb = lat.nbasis
+    if lat.cells[0] <= 0 or lat.nham != lat.natom:
+        raise ValueError("reduced() needs a full (nham == natom) lattice with a cell structure")
+    b = np.arange(lat.natom) % nb
+    out = Lattice(**{k: getattr(lat, k) for k in lat.__dataclass_fields__})
+    for name in ("ncoup", "nlistsize", "dmlistsize", "dm_vect", "j_tens"):
+        a = getattr(lat, name)
+        if a is None:
+            continue
+        if not np.array_equal(a, a[:nb][b]):
+            raise ValueError(f"{name} is not translation invariant; the Hamiltonian does not reduce")
+        setattr(out, name, np.ascontiguousarray(a[:nb]))
+    out.aham = (b + 1).astype(np.int32)
+    return out
+
+
 _KAGOME_BASIS = np.array([[0.0, 0.0], [0.5, 0.0], [0.0, 0.5]])
 _KAGOME_STENCIL = [
     [(0, 0, 0, 1, 1), (-1, 0, 0, 1, 1), (0, 0, 0, 2, 1), (0, -1, 0, 2, 1)],

@@ -10,6 +10,12 @@ by the reference's own regression harness (its tests read these files by column)
   (prn_averages.f90:919-1095): running averages whose weights grow by one per
   sample, Binder cumulant, susceptibility and specific heat in the reference's
   units, written every ``cumu_buff`` samples; rows ``(i8,10es16.8)``.
+* ``TotEnergyFile`` -- ``totenergy.<simid>.out`` (and ``stdenergy.<simid>.out`` for
+  several ensembles) of calc_energy (Hamiltonian/energy.f90:407-500): the ensemble mean
+  of each energy term in mRy/atom, header ``(a8,16a20)`` and rows ``(i8,14es16.8)``;
+  with an exchange tensor the pair-energy layout, header ``(a8,11a16)``, rows
+  ``(i8,11es16.8)``.  The deviation file holds calculate_mean_and_deviation's value
+  (:577-602): the ensemble variance over M - 1, times mub/mry.
 * ``write_restart`` -- the legacy ``restart.<simid>.out`` of prnrestart
   (System/restart.f90): ``(i8)`` step, then ``(i8,i8,2x,4es16.8)`` per atom.
 * ``sd_run_with_averages`` -- the measurement cadence of sd_mphase: a row every
@@ -19,6 +25,7 @@ from __future__ import annotations
 
 import math
 import os
+from typing import Optional
 
 import numpy as np
 
@@ -118,6 +125,45 @@ class CumulantsFile:
                     self._first = False
                 f.write(f"{n:8d}" + "".join(fortran_es(v) for v in row) + "\n")
         return row
+
+
+class TotEnergyFile:
+    HEADER = ("#Iter", "Tot", "Exc", "Ani", "DM", "PD", "BiqDM", "BQ", "Dip", "Zeeman", "LSF", "Chir", "Ring", "SA")
+    HEADER_TENSOR = ("#Iter", "Tot", "Heis-Tens", "Ani", "PD", "BiqDM", "BQ", "Dip", "Zeeman", "LSF", "Chir",
+                     "Ring")
+
+    def __init__(self, path: str, tensor: bool = False, std_path: Optional[str] = None):
+        self.path, self.std_path, self.tensor = path, std_path, bool(tensor)
+        self._first = {p: not os.path.exists(p) for p in (path, std_path) if p}
+
+    def _columns(self, t):
+        """Term values in the file's column order; terms absent from this library are 0."""
+        z = np.zeros_like(t["total"])
+        if self.tensor:
+            return [t["total"], t["xc"], t["ani"], z, z, z, z, t["ext"], z, z, z]
+        return [t["total"], t["xc"], t["ani"], t["dm"], z, z, z, z, t["ext"], z, z, z, z]
+
+    def _write(self, path, index, vals):
+        with open(path, "a") as f:
+            if self._first[path]:
+                head = self.HEADER_TENSOR if self.tensor else self.HEADER
+                w = 16 if self.tensor else 20
+                f.write(fortran_a(head[0], 8) + "".join(fortran_a(h, w) for h in head[1:]) + "\n")
+                self._first[path] = False
+            f.write(f"{int(index):8d}" + "".join(fortran_es(v) for v in vals) + "\n")
+
+    def write(self, index, terms):
+        """terms: dict of per-ensemble arrays in mRy/atom (GpuSimulation.energy_terms())."""
+        cols = [np.atleast_1d(np.asarray(c, dtype=np.float64)) for c in self._columns(terms)]
+        m = cols[0].size
+        fcinv = MUB / MRY
+        means = [c.mean() if m > 1 else c[0] for c in cols]
+        self._write(self.path, index, means)
+        if self.std_path and m > 1:
+            # calculate_mean_and_deviation works on the unscaled values and scales once
+            devs = [np.sum((c / fcinv - mu / fcinv) ** 2) / (m - 1.0) * fcinv for c, mu in zip(cols, means)]
+            self._write(self.std_path, index, devs)
+        return means
 
 
 def write_restart(path: str, mstep: int, emom, mmom):

@@ -184,6 +184,13 @@ class GpuSimulation:
         _lib.call("uppasd_gpu_observables", self._h, _ptr(mv), _ptr(ma), _ptr(en))
         return {"mvec": mv, "mabs": ma, "energy": en}
 
+    def energy_terms(self):
+        """Per-ensemble energy terms in mRy/atom: dict of (mensemble,) arrays
+        total, xc (the pair energy with an exchange tensor), ani, dm, ext."""
+        t = np.empty((self.lat.mensemble, 5))
+        _lib.call("uppasd_gpu_energy_terms", self._h, _ptr(t))
+        return dict(zip(("total", "xc", "ani", "dm", "ext"), t.T.copy()))
+
 
 def device_info():
     sm = C.c_int32()
