@@ -52,7 +52,7 @@ typedef struct {
     int32_t max_no_neigh, nham;        /* ncoup is (max_no_neigh, nham) */
     int32_t do_dm, max_no_dmneigh;
     int32_t do_aniso;
-    int32_t sdealgh;                   /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point */
+    int32_t sdealgh;                   /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point, 11 LLGI */
     double delta_t, bn, temprescale;
     uint64_t gpu_rng_seed;             /* Philox key (gpu_rng_seed keyword) */
     int32_t gpu_rng;                   /* 0 Philox in-kernel, 1 caller-injected normals */
@@ -99,6 +99,10 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *s, const double *emom);
 int uppasd_gpu_get_moments(uppasd_gpu_sim *s, double *emom, double *emomM);
 int uppasd_gpu_set_temperature(uppasd_gpu_sim *s, const double *temp_array);
 int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
+
+/* Relaxation time of the inertial regime for SDEalgh 11 (LLGI, Evolution/llgi.f90;
+ * input keyword relaxtime, Input/inputhandler.f90:768, default 0).  Seconds, >= 0. */
+int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *s, double relaxtime);
 
 /* SKKR-style exchange tensor (do_jtensor = 1): j_tens(3,3,max_no_neigh,nHam) in the
  * reference layout and scaling (Hamiltonian/hamiltoniandata.f90:138), on the exchange

@@ -45,12 +45,13 @@ class OrcLLG(C.Structure):
         ("sdealgh", C.c_int), ("delta_t", C.c_double), ("bn", C.c_double), ("temprescale", C.c_double),
         ("lambda1", F64P), ("temp", F64P), ("landeg", F64P), ("noise_mode", C.c_int),
         ("zig", C.POINTER(OrcZig)), ("noise", F64P), ("seed", C.c_uint64), ("step", C.c_int64),
+        ("relaxtime", C.c_double),
     ]
 
 
 class OrcState(C.Structure):
     _fields_ = [("emom", F64P), ("emom2", F64P), ("emomM", F64P), ("mmom", F64P),
-                ("b2eff", F64P), ("beff", F64P), ("ranv", F64P)]
+                ("b2eff", F64P), ("beff", F64P), ("ranv", F64P), ("mpast", F64P)]
 
 
 class OrcCumulant(C.Structure):
@@ -160,9 +161,11 @@ class Oracle:
         self.beff = np.zeros(shape3)
         self.b2eff = np.zeros(shape3)
         self.ranv = np.zeros(shape3)
+        self.mpast = np.zeros(shape3)
         st = OrcState()
         st.emom, st.emom2, st.emomM = _p(self.emom), _p(self.emom2), _p(self.emomM)
         st.mmom, st.b2eff, st.beff, st.ranv = _p(self.mmom), _p(self.b2eff), _p(self.beff), _p(self.ranv)
+        st.mpast = _p(self.mpast)
         self.state = st
         self.zig = None
         self.mt = None
@@ -173,6 +176,7 @@ class Oracle:
         self.emom[...] = emom
         self.emom2[...] = emom
         self.emomM[...] = emom * self.mmom[..., None]
+        self.mpast[...] = 0.0   # LLGI starts without a previous step (llgi.f90:295)
 
     def init_random(self, seed: int):
         """initmag 1 from a fresh mtprng stream seeded with `seed` (rng_init)."""
@@ -181,6 +185,7 @@ class Oracle:
         self.lib.orc_initmag_random(C.byref(self.mt), self.lat.natom, self.lat.mensemble, _p(self.mmom),
                                     _p(self.emom), _p(self.emomM))
         self.emom2[...] = self.emom
+        self.mpast[...] = 0.0
 
     def setup_ziggurat(self, seed: int):
         self.zig = OrcZig()
@@ -205,7 +210,8 @@ class Oracle:
         return mv, ma
 
     # ---- LLG ----
-    def make_llg(self, sdealgh, delta_t, lambda1, temp, landeg=1.0, noise_mode=NOISE_PHILOX, seed=0, bn=1.0):
+    def make_llg(self, sdealgh, delta_t, lambda1, temp, landeg=1.0, noise_mode=NOISE_PHILOX, seed=0, bn=1.0,
+                 relaxtime=0.0):
         N = self.lat.natom
         self._lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lambda1, dtype=np.float64), (N,)))
         self._temp = np.ascontiguousarray(np.broadcast_to(np.asarray(temp, dtype=np.float64), (N,)))
@@ -216,6 +222,7 @@ class Oracle:
         p.noise_mode = noise_mode
         p.seed = seed
         p.step = 0
+        p.relaxtime = relaxtime
         if noise_mode == NOISE_ZIGGURAT:
             if self.zig is None:
                 raise ValueError("setup_ziggurat() first")

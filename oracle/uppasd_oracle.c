@@ -692,6 +692,84 @@ static void sib_second(const orc_llg *p, int N, int M, orc_state *s) {
     }
 }
 
+/* llgiheun (Evolution/llgi.f90:178-278): one implicit step of the inertial LLG,
+ * m_new = A^-1 B with A = I + beta [e1]x, from m(t) = e1, m(t - dt) = et and the
+ * field h; no Lande factor and no 1/(1 + lambda^2), as there. */
+static void llgiheun(double lam, double delta_t, double relaxtime, const double et[3], const double e1[3],
+                     const double h[3], double out[3]) {
+    double alfa = lam;
+    double beta = -alfa * (1.0 + relaxtime / delta_t);
+    double zeta = -alfa * (relaxtime / delta_t);
+    double dtg = -delta_t * ORC_GAMA;
+    double A12 = -beta * e1[2], A13 = beta * e1[1];
+    double A21 = beta * e1[2], A23 = -beta * e1[0];
+    double A31 = -beta * e1[1], A32 = beta * e1[0];
+    double det = 1.0 - A23 * A32 - A12 * A21 - A13 * A31;
+    det = 1.0 / det;
+    double I11 = (1.0 - A32 * A23) * det, I12 = (A13 * A32 - A12) * det, I13 = (A12 * A23 - A13) * det;
+    double I21 = (A23 * A31 - A21) * det, I22 = (1.0 - A31 * A13) * det, I23 = (A13 * A21 - A23) * det;
+    double I31 = (A21 * A32 - A31) * det, I32 = (A12 * A31 - A32) * det, I33 = (1.0 - A21 * A12) * det;
+    double B1 = e1[0] + dtg * (e1[1] * h[2] - e1[2] * h[1]) + zeta * (e1[2] * et[1] - e1[1] * et[2]);
+    double B2 = e1[1] + dtg * (e1[2] * h[0] - e1[0] * h[2]) + zeta * (e1[0] * et[2] - e1[2] * et[0]);
+    double B3 = e1[2] + dtg * (e1[0] * h[1] - e1[1] * h[0]) + zeta * (e1[1] * et[0] - e1[0] * et[1]);
+    out[0] = I11 * B1 + I12 * B2 + I13 * B3;
+    out[1] = I21 * B1 + I22 * B2 + I23 * B3;
+    out[2] = I31 * B1 + I32 * B2 + I33 * B3;
+}
+
+/* llgi_evolve_first (Evolution/llgi.f90:18-66): thermfield (:120-159, the Depondt
+ * noise amplitude), bdup = beff + btherm, predictor from (m(t - dt), m(t)). */
+static void llgi_first(const orc_llg *p, int N, int M, orc_state *s) {
+    orc_llg_draw_normals(p, N, M, s->ranv); /* btherm */
+#pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
+    for (int k = 0; k < M; ++k)
+        for (int i = 0; i < N; ++i) {
+            double lam = p->lambda1[i];
+            double Dp = (2.0 * lam * ORC_KBOLT) / (p->delta_t * ORC_GAMA * ORC_MUB);
+            double sigma = sqrt(Dp * p->temprescale * p->temp[i] / M2(s->mmom, i, k, N));
+            double bdup[3], et[3], e1[3], mt[3];
+            for (int c = 0; c < 3; ++c) {
+                double bth = V3(s->ranv, c, i, k, N) * sigma;
+                V3(s->ranv, c, i, k, N) = bth;
+                bdup[c] = V3(s->beff, c, i, k, N) + bth;
+                et[c] = V3(s->mpast, c, i, k, N);
+                e1[c] = V3(s->emom2, c, i, k, N);
+            }
+            llgiheun(lam, p->delta_t, p->relaxtime, et, e1, bdup, mt);
+            double mm = M2(s->mmom, i, k, N);
+            for (int c = 0; c < 3; ++c) {
+                V3(s->emom, c, i, k, N) = mt[c];
+                V3(s->emomM, c, i, k, N) = mt[c] * mm;
+                V3(s->b2eff, c, i, k, N) = bdup[c];
+            }
+        }
+}
+
+/* llgi_evolve_second (Evolution/llgi.f90:68-118): bdup = (beff + btherm)/2 + b2eff/2,
+ * corrector from (m(t - dt), m(t)), then m(t) becomes the new m(t - dt) and the
+ * normalised corrector the new m(t).  norm2 is evaluated as sqrt(x^2 + y^2 + z^2);
+ * compilers differ in how they evaluate it, by the last bit. */
+static void llgi_second(const orc_llg *p, int N, int M, orc_state *s) {
+#pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
+    for (int k = 0; k < M; ++k)
+        for (int i = 0; i < N; ++i) {
+            double bdup[3], et[3], e1[3], mt[3];
+            for (int c = 0; c < 3; ++c) {
+                bdup[c] = 0.5 * (V3(s->beff, c, i, k, N) + V3(s->ranv, c, i, k, N)) +
+                          0.5 * V3(s->b2eff, c, i, k, N);
+                et[c] = V3(s->mpast, c, i, k, N);
+                e1[c] = V3(s->emom2, c, i, k, N);
+                V3(s->mpast, c, i, k, N) = e1[c];
+            }
+            llgiheun(p->lambda1[i], p->delta_t, p->relaxtime, et, e1, bdup, mt);
+            double etot = 1.0 / sqrt(mt[0] * mt[0] + mt[1] * mt[1] + mt[2] * mt[2]);
+            for (int c = 0; c < 3; ++c) {
+                V3(s->emom, c, i, k, N) = e1[c];
+                V3(s->emom2, c, i, k, N) = mt[c] * etot;
+            }
+        }
+}
+
 /* copym (Evolution/updatemoments.f90:48-99), initexc /= 'I', mompar = 0 */
 static void copym(int N, int M, orc_state *s) {
 #pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
@@ -727,6 +805,10 @@ int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
         break;
     case 4: heun_first(p, N, M, s); break;
     case 5: depondt_first(p, N, M, s); break;
+    case 11:
+        if (!s->mpast) return -1;
+        llgi_first(p, N, M, s);
+        break;
     default: return -1;
     }
     orc_effective_field(h, s->emomM, s->beff);
@@ -735,6 +817,7 @@ int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
     case 6: sib_second(p, N, M, s); break;
     case 4: heun_second(p, N, M, s); break;
     case 5: depondt_second(p, N, M, s); break;
+    case 11: llgi_second(p, N, M, s); break;
     }
     copym(N, M, s);
     return 0;

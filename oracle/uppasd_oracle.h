@@ -97,7 +97,7 @@ void orc_effective_field_single(const orc_ham *h, const double *emomM, int i, in
 enum { ORC_NOISE_NONE = 0, ORC_NOISE_ZIGGURAT = 1, ORC_NOISE_ARRAY = 2, ORC_NOISE_PHILOX = 3 };
 
 typedef struct {
-    int sdealgh;            /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point */
+    int sdealgh;            /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point, 11 LLGI */
     double delta_t, bn, temprescale;
     const double *lambda1;  /* (natom) */
     const double *temp;     /* (natom) */
@@ -107,6 +107,7 @@ typedef struct {
     const double *noise;    /* ORC_NOISE_ARRAY: N(0,1) values (3,natom,mensemble) for this step */
     uint64_t seed;          /* ORC_NOISE_PHILOX */
     int64_t step;           /* ORC_NOISE_PHILOX counter */
+    double relaxtime;       /* SDEalgh 11: relaxation time of the inertial regime (s) */
 } orc_llg;
 
 typedef struct {
@@ -114,6 +115,7 @@ typedef struct {
     double *mmom;                  /* (natom,mensemble) */
     double *b2eff, *beff;          /* (3,natom,mensemble) work */
     double *ranv;                  /* (3,natom,mensemble) work */
+    double *mpast;                 /* SDEalgh 11: m(t - dt), zero before the first step */
 } orc_state;
 
 /* One full step: field -> evolve_first -> field -> evolve_second -> moment_update. */

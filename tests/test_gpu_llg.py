@@ -166,3 +166,30 @@ def test_noise_statistics_philox():
     ma = sim.observables()["mabs"]
     assert np.all(ma < 2.2) and np.all(ma > 1.5)
     sim.close()
+
+
+@pytest.mark.parametrize("kind,temp,tau", [("bcc", 0.0, 0.0), ("bcc", 0.0, 2e-15), ("bcc", 300.0, 2e-15),
+                                           ("kagome_tensor", 100.0, 1e-15)])
+def test_llgi_1000_steps(kind, temp, tau):
+    """SDEalgh 11 (inertial LLG) through the C ABI against the oracle."""
+    lat = (lattice.bcc(4, [1.3, 0.7], 2.2) if kind == "bcc" else lattice.kagome(8)).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(8), (2, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=11, delta_t=1e-16, damping=0.05, temperature=temp, seed=13, emom=e0,
+                        relaxtime=tau)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(11, 1e-16, 0.05, temp, 1.0, noise_mode=po.NOISE_PHILOX, seed=13, relaxtime=tau)
+    sim.evolve(1000)
+    for _ in range(1000):
+        o.sd_step()
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= TOL
+    # a new state starts without a previous step, as a fresh run does
+    sim.put_moments(e0)
+    sim.set_step(0)
+    sim.evolve(10)
+    o.set_moments(e0)
+    o.llg.step = 0
+    for _ in range(10):
+        o.sd_step()
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= TOL
+    sim.close()

@@ -199,8 +199,8 @@ int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     if (c->do_dm && (!a->dmlist || !a->dmlistsize || !a->dm_vect || c->max_no_dmneigh <= 0))
         return bad("do_dm set but DM arrays missing");
     if (c->do_aniso && (!a->taniso || !a->eaniso || !a->kaniso)) return bad("do_aniso set but anisotropy arrays missing");
-    if (!(c->sdealgh == 1 || c->sdealgh == 4 || c->sdealgh == 5 || c->sdealgh == 6))
-        return bad("SDEalgh must be 1, 4, 5 or 6");
+    if (!(c->sdealgh == 1 || c->sdealgh == 4 || c->sdealgh == 5 || c->sdealgh == 6 || c->sdealgh == 11))
+        return bad("SDEalgh must be 1, 4, 5, 6 or 11");
     if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
     if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
     if (c->precision < 0 || c->precision > 2) return bad("precision must be 0, 1 or 2");
@@ -333,6 +333,7 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     if ((rc = alloc_vec3(s, s.e, NM)) || (rc = alloc_vec3(s, s.eM, NM)) || (rc = alloc_vec3(s, s.p, NM)) ||
         (rc = alloc_vec3(s, s.pM, NM)) || (rc = alloc_vec3(s, s.b2, NM)) || (rc = dalloc(s, &s.red, (size_t)8 * M)))
         return rc;
+    if (c->sdealgh == 11 && (rc = alloc_vec3(s, s.mpast, NM))) return rc;  // zeroed by put_moments
     if ((rc = build_colouring(s, c, nlT, nsize, dmT, dmsize))) return rc;
     s.precision = c->precision;
     if (c->precision >= 1) {
@@ -358,6 +359,7 @@ void destroy(Sim &s) {
     free_vec3(s.p);
     free_vec3(s.pM);
     free_vec3(s.b2);
+    free_vec3(s.mpast);
     delete[] s.colour_start_h;
     if (s.own_stream) s.stream = s.own_stream;
     if (s.stream) cudaStreamDestroy(s.stream);
@@ -476,6 +478,9 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
         uppasd::aos_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(d, s.e, s.eM, s.llg.mmom, n);
         e = cudaGetLastError();
     }
+    // SDEalgh 11: a new state has no previous step (the reference's mpast starts at zero, llgi.f90:295)
+    for (double *q : {s.mpast.x, s.mpast.y, s.mpast.z})
+        if (e == cudaSuccess && q) e = cudaMemsetAsync(q, 0, n * sizeof(double), s.stream);
     cudaFreeAsync(d, s.stream);
     if (e != cudaSuccess) {
         uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
@@ -521,6 +526,17 @@ int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
     UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.temp, temp_array, sizeof(double) * s.ham.natom, cudaMemcpyHostToDevice,
                                     s.stream));
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *w, double relaxtime) {
+    if (!w || !std::isfinite(relaxtime) || relaxtime < 0.0) {
+        uppasd::set_error("set_relaxtime: relaxtime must be finite and >= 0");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    uppasd::drop_graph(s);  // the step arguments are captured by value
+    s.llg.relaxtime = relaxtime;
     return UPPASD_GPU_OK;
 }
 

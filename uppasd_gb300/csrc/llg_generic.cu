@@ -14,6 +14,7 @@
 //              RNG/randomnumbers.f90:660-745
 //   Heun       Evolution/heun_proper.f90:28-161, 261-530
 //   SIB        Evolution/sphmidpoint.f90:36-477
+//   LLGI       Evolution/llgi.f90:18-278 (SDEalgh 11, inertial LLG)
 //   moments    Evolution/updatemoments.f90:48-77
 #include "common.cuh"
 #include "field_fp64.cuh"
@@ -97,15 +98,39 @@ __device__ __forceinline__ void sib_fixed_point(const double e1[3], const double
     }
 }
 
+// llgiheun (Evolution/llgi.f90:178-278): m_new = A^-1 B, A = I + beta [e1]x, from
+// m(t) = e1, m(t - dt) = et and the field h.
+__device__ __forceinline__ void llgi_heun(double lam, double delta_t, double relaxtime, const double et[3],
+                                          const double e1[3], const double h[3], double out[3]) {
+    const double alfa = lam;
+    const double beta = -alfa * (1.0 + relaxtime / delta_t);
+    const double zeta = -alfa * (relaxtime / delta_t);
+    const double dtg = -delta_t * kGama;
+    const double A12 = -beta * e1[2], A13 = beta * e1[1];
+    const double A21 = beta * e1[2], A23 = -beta * e1[0];
+    const double A31 = -beta * e1[1], A32 = beta * e1[0];
+    double det = 1.0 - A23 * A32 - A12 * A21 - A13 * A31;
+    det = 1.0 / det;
+    const double I11 = (1.0 - A32 * A23) * det, I12 = (A13 * A32 - A12) * det, I13 = (A12 * A23 - A13) * det;
+    const double I21 = (A23 * A31 - A21) * det, I22 = (1.0 - A31 * A13) * det, I23 = (A13 * A21 - A23) * det;
+    const double I31 = (A21 * A32 - A31) * det, I32 = (A12 * A31 - A32) * det, I33 = (1.0 - A21 * A12) * det;
+    const double B1 = e1[0] + dtg * (e1[1] * h[2] - e1[2] * h[1]) + zeta * (e1[2] * et[1] - e1[1] * et[2]);
+    const double B2 = e1[1] + dtg * (e1[2] * h[0] - e1[0] * h[2]) + zeta * (e1[0] * et[2] - e1[2] * et[0]);
+    const double B3 = e1[2] + dtg * (e1[0] * h[1] - e1[1] * h[0]) + zeta * (e1[1] * et[0] - e1[0] * et[1]);
+    out[0] = I11 * B1 + I12 * B2 + I13 * B3;
+    out[1] = I21 * B1 + I22 * B2 + I23 * B3;
+    out[2] = I31 * B1 + I32 * B2 + I33 * B3;
+}
+
 struct StepArgs {
     HamDev h;
     NoiseArgs nz;
     const double *lambda, *temp, *landeg, *mmom;
-    double delta_t, bn, temprescale;
+    double delta_t, bn, temprescale, relaxtime;
     int noise_on;  // midpoint/SIB: rannum only when min(lambda) > 1e-12
     const int64_t *d_step;
     int64_t step_off;
-    Vec3D e, eM, p, pM, b2;
+    Vec3D e, eM, p, pM, b2, mpast;
 };
 
 template <int ALG>
@@ -206,6 +231,24 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
         a.pM.x[o] = etx * mm;
         a.pM.y[o] = ety * mm;
         a.pM.z[o] = etz * mm;
+    } else if (ALG == 11) {
+        // llgi_evolve_first: thermfield (Depondt amplitude), bdup = beff + btherm
+        noise3(a.nz, i, k, N, M, step, z);
+        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
+        double bdup[3], et[3] = {a.mpast.x[o], a.mpast.y[o], a.mpast.z[o]}, mt[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bdup[c] = B[c] + z[c] * sigma;
+        llgi_heun(lam, a.delta_t, a.relaxtime, et, e, bdup, mt);
+        a.p.x[o] = mt[0];
+        a.p.y[o] = mt[1];
+        a.p.z[o] = mt[2];
+        a.pM.x[o] = mt[0] * mm;
+        a.pM.y[o] = mt[1] * mm;
+        a.pM.z[o] = mt[2] * mm;
+        a.b2.x[o] = bdup[0];
+        a.b2.y[o] = bdup[1];
+        a.b2.z[o] = bdup[2];
     }
 }
 
@@ -263,6 +306,24 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
             sib_a1s1(lam, pr, B, r, a1, s1);
             sib_fixed_point(e, a1, s1, dtg, sqrtdtg, out);
         }
+    } else if (ALG == 11) {
+        // llgi_evolve_second: the same btherm as the predictor (same counter), averaged
+        // field, corrector from (m(t - dt), m(t)); m(t) becomes the new m(t - dt)
+        noise3(a.nz, i, k, N, M, step, z);
+        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
+        double b2v[3] = {a.b2.x[o], a.b2.y[o], a.b2.z[o]};
+        double bdup[3], et[3] = {a.mpast.x[o], a.mpast.y[o], a.mpast.z[o]}, mt[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) bdup[c] = 0.5 * (B[c] + z[c] * sigma) + 0.5 * b2v[c];
+        llgi_heun(lam, a.delta_t, a.relaxtime, et, e, bdup, mt);
+        a.mpast.x[o] = e[0];
+        a.mpast.y[o] = e[1];
+        a.mpast.z[o] = e[2];
+        double etot = 1.0 / sqrt(mt[0] * mt[0] + mt[1] * mt[1] + mt[2] * mt[2]);
+        out[0] = mt[0] * etot;
+        out[1] = mt[1] * etot;
+        out[2] = mt[2] * etot;
     } else {  // ALG == 4
         noise3(a.nz, i, k, N, M, step, z);
         double dt = a.delta_t * kGama;
@@ -334,6 +395,7 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     a.delta_t = s.llg.delta_t;
     a.bn = s.llg.bn;
     a.temprescale = s.llg.temprescale;
+    a.relaxtime = s.llg.relaxtime;
     a.noise_on = s.llg.noise_on;
     a.d_step = s.llg.d_step;
     a.step_off = step_offset;
@@ -342,6 +404,7 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     a.p = s.p;
     a.pM = s.pM;
     a.b2 = s.b2;
+    a.mpast = s.mpast;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const int grid = (int)((n + 255) / 256);
     switch (s.llg.sdealgh) {
@@ -349,6 +412,7 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     case 4: launch_pair<4>(s, a, grid, phase); break;
     case 5: launch_pair<5>(s, a, grid, phase); break;
     case 6: launch_pair<6>(s, a, grid, phase); break;
+    case 11: launch_pair<11>(s, a, grid, phase); break;
     default: set_error("unsupported SDEalgh"); return UPPASD_GPU_EUNSUPPORTED;
     }
     UPPASD_CUDA_TRY(cudaGetLastError());

@@ -45,6 +45,7 @@ struct HamDev {
 struct LlgDev {
     int sdealgh = 5;
     double delta_t = 1e-16, bn = 1.0, temprescale = 1.0;
+    double relaxtime = 0.0;  // SDEalgh 11: relaxation time of the inertial regime (s)
     double *lambda = nullptr, *temp = nullptr, *landeg = nullptr;  // [natom]
     double *mmom = nullptr;  // [mensemble][natom]
     uint64_t seed = 0;
@@ -74,6 +75,7 @@ struct Sim {
     Vec3D e, eM;        // state at t: unit vectors and full moments
     Vec3D p, pM;        // predictor / midpoint estimate
     Vec3D b2;           // Depondt b2eff / Heun field at t
+    Vec3D mpast;        // SDEalgh 11: m(t - dt), zero before the first step
     int64_t step = 0;   // host mirror of the step counter
     cudaStream_t stream = nullptr;      // stream all work is issued on
     cudaStream_t own_stream = nullptr;  // the library's stream while a caller's stream is set

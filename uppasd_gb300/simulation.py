@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from .lattice import Lattice
 
-SOLVERS = {"midpoint": 1, "heun": 4, "depondt": 5, "sib": 6}
+SOLVERS = {"midpoint": 1, "heun": 4, "depondt": 5, "sib": 6, "llgi": 11}
 
 
 def _ptr(a, t=_lib.F64P):
@@ -30,7 +30,7 @@ class GpuSimulation:
 
     def __init__(self, lat: Lattice, sdealgh: int = 5, delta_t: float = 1e-16, damping=0.1,
                  temperature=0.0, landeg=1.0, seed: int = 1, emom: Optional[np.ndarray] = None,
-                 precision: int = 0, gpu_rng: int = 0, bn: float = 1.0):
+                 precision: int = 0, gpu_rng: int = 0, bn: float = 1.0, relaxtime: float = 0.0):
         if isinstance(sdealgh, str):
             sdealgh = SOLVERS[sdealgh]
         self.lat = lat
@@ -88,6 +88,8 @@ class GpuSimulation:
         self._keep = []  # init copied everything it needs
         if lat.j_tens is not None:
             self.set_jtensor(lat.j_tens)
+        if relaxtime:
+            _lib.call("uppasd_gpu_set_relaxtime", self._h, float(relaxtime))
 
     def set_jtensor(self, j_tens: Optional[np.ndarray]):
         """Exchange tensor in the Fortran image (nham, mnn, 3, 3) = j_tens(3,3,mnn,nham);
