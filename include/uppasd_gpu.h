@@ -100,6 +100,11 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *s, double *emom, double *emomM);
 int uppasd_gpu_set_temperature(uppasd_gpu_sim *s, const double *temp_array);
 int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
 
+/* Input keyword perp = 'Y' (Input/inputhandler.f90:784): before each half-step the
+ * effective field loses its component along emom (Evolution/evolution.f90:104-112,
+ * :327-335).  0 or 1; -7 on the structured path. */
+int uppasd_gpu_set_perp(uppasd_gpu_sim *s, int32_t perp);
+
 /* Relaxation time of the inertial regime for SDEalgh 11 (LLGI, Evolution/llgi.f90;
  * input keyword relaxtime, Input/inputhandler.f90:768, default 0).  Seconds, >= 0. */
 int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *s, double relaxtime);

@@ -45,7 +45,7 @@ class OrcLLG(C.Structure):
         ("sdealgh", C.c_int), ("delta_t", C.c_double), ("bn", C.c_double), ("temprescale", C.c_double),
         ("lambda1", F64P), ("temp", F64P), ("landeg", F64P), ("noise_mode", C.c_int),
         ("zig", C.POINTER(OrcZig)), ("noise", F64P), ("seed", C.c_uint64), ("step", C.c_int64),
-        ("relaxtime", C.c_double),
+        ("relaxtime", C.c_double), ("perp", C.c_int),
     ]
 
 
@@ -211,7 +211,7 @@ class Oracle:
 
     # ---- LLG ----
     def make_llg(self, sdealgh, delta_t, lambda1, temp, landeg=1.0, noise_mode=NOISE_PHILOX, seed=0, bn=1.0,
-                 relaxtime=0.0):
+                 relaxtime=0.0, perp=False):
         N = self.lat.natom
         self._lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lambda1, dtype=np.float64), (N,)))
         self._temp = np.ascontiguousarray(np.broadcast_to(np.asarray(temp, dtype=np.float64), (N,)))
@@ -223,6 +223,7 @@ class Oracle:
         p.seed = seed
         p.step = 0
         p.relaxtime = relaxtime
+        p.perp = 1 if perp else 0
         if noise_mode == NOISE_ZIGGURAT:
             if self.zig is None:
                 raise ValueError("setup_ziggurat() first")

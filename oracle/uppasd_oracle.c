@@ -790,11 +790,28 @@ static int min_lambda_gt(const orc_llg *p, int N, double tol) {
     return 1;
 }
 
+/* perp = 'Y' (Evolution/evolution.f90:104-112 and :327-335): the field loses its
+ * component along emom, whatever emom holds at that point of the step. */
+static void perp_project(int N, int M, orc_state *s) {
+#pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
+    for (int k = 0; k < M; ++k)
+        for (int i = 0; i < N; ++i) {
+            double b[3], e[3];
+            for (int c = 0; c < 3; ++c) {
+                b[c] = V3(s->beff, c, i, k, N);
+                e[c] = V3(s->emom, c, i, k, N);
+            }
+            double d = b[0] * e[0] + b[1] * e[1] + b[2] * e[2];
+            for (int c = 0; c < 3; ++c) V3(s->beff, c, i, k, N) = b[c] - e[c] * d;
+        }
+}
+
 /* sd_mphase step body (sd_driver.f90:657-767) with evolve_first / evolve_second
  * dispatch (Evolution/evolution.f90:38-406). */
 int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
     const int N = h->natom, M = h->mensemble;
     orc_effective_field(h, s->emomM, s->beff);
+    if (p->perp) perp_project(N, M, s);
     switch (p->sdealgh) {
     case 1:
     case 6:
@@ -812,6 +829,7 @@ int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
     default: return -1;
     }
     orc_effective_field(h, s->emomM, s->beff);
+    if (p->perp) perp_project(N, M, s);
     switch (p->sdealgh) {
     case 1: midpoint_second(p, N, M, s); break;
     case 6: sib_second(p, N, M, s); break;

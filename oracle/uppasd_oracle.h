@@ -108,6 +108,7 @@ typedef struct {
     uint64_t seed;          /* ORC_NOISE_PHILOX */
     int64_t step;           /* ORC_NOISE_PHILOX counter */
     double relaxtime;       /* SDEalgh 11: relaxation time of the inertial regime (s) */
+    int perp;               /* input perp = 'Y': field projected perpendicular to emom */
 } orc_llg;
 
 typedef struct {

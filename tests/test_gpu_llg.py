@@ -193,3 +193,30 @@ def test_llgi_1000_steps(kind, temp, tau):
         o.sd_step()
     assert np.max(np.abs(sim.get_moments() - o.emom)) <= TOL
     sim.close()
+
+
+@pytest.mark.parametrize("solver", [1, 4, 5, 6, 11])
+def test_perp_projection(solver):
+    """Input perp = 'Y': the field loses its component along emom before each half-step."""
+    lat = lattice.square_dmi(16, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(9), (2, lat.natom, 3))
+    nsteps = 300 if solver != 6 else 100
+    sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.1, temperature=50.0, seed=21, emom=e0,
+                        relaxtime=1e-15 if solver == 11 else 0.0, perp=True)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, 1e-16, 0.1, 50.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=21,
+               relaxtime=1e-15 if solver == 11 else 0.0, perp=True)
+    sim.evolve(nsteps)
+    for _ in range(nsteps):
+        o.sd_step()
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= TOL
+    # the projection changes the trajectory of a finite step
+    ref = po.Oracle(lat)
+    ref.set_moments(e0)
+    ref.make_llg(solver, 1e-16, 0.1, 50.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=21,
+                 relaxtime=1e-15 if solver == 11 else 0.0)
+    for _ in range(nsteps):
+        ref.sd_step()
+    assert np.max(np.abs(ref.emom - o.emom)) > 1e-12
+    sim.close()

@@ -69,3 +69,21 @@ def test_zero_relaxtime_converges_to_depondt():
     d1 = np.abs(out[(11, 2e-18)] - out[(5, 1e-18)]).max()
     d2 = np.abs(out[(11, 1e-18)] - out[(5, 1e-18)]).max()
     assert d2 < 0.6 * d1 and d2 < 1e-3
+
+
+def test_perp_projection_is_a_small_change_per_step():
+    """perp = 'Y' removes the field along emom: each solver's step changes by far less
+    than the step itself (the parallel part does not drive the LLG equation)."""
+    lat = lattice.bcc(2, [1.3, 0.7], 2.2)
+    e0 = _rand_unit(np.random.default_rng(63), (1, lat.natom, 3))
+    for alg in (1, 4, 5, 6, 11):
+        out = []
+        for perp in (False, True):
+            o = po.Oracle(lat, threads=1)
+            o.set_moments(e0)
+            o.make_llg(alg, 1e-17, 0.1, 0.0, perp=perp)
+            o.sd_step()
+            out.append(o.emom.copy())
+        step = np.abs(out[0] - e0).max()
+        diff = np.abs(out[0] - out[1]).max()
+        assert 0.0 < diff < 0.2 * step, (alg, diff, step)

@@ -529,6 +529,21 @@ int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
     return UPPASD_GPU_OK;
 }
 
+int uppasd_gpu_set_perp(uppasd_gpu_sim *w, int32_t perp) {
+    if (!w || (perp != 0 && perp != 1)) {
+        uppasd::set_error("set_perp: perp must be 0 or 1");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    if (perp && s.precision >= 1) {
+        uppasd::set_error("set_perp: the structured path (precision >= 1) has no field projection; use precision 0");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
+    uppasd::drop_graph(s);  // the step arguments are captured by value
+    s.llg.perp = perp;
+    return UPPASD_GPU_OK;
+}
+
 int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *w, double relaxtime) {
     if (!w || !std::isfinite(relaxtime) || relaxtime < 0.0) {
         uppasd::set_error("set_relaxtime: relaxtime must be finite and >= 0");

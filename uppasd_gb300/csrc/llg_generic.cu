@@ -122,12 +122,21 @@ __device__ __forceinline__ void llgi_heun(double lam, double delta_t, double rel
     out[2] = I31 * B1 + I32 * B2 + I33 * B3;
 }
 
+// perp = 'Y' (Evolution/evolution.f90:104-112, :327-335): B <- B - e (B . e)
+__device__ __forceinline__ void perp_project(double B[3], const double e[3]) {
+    const double d = B[0] * e[0] + B[1] * e[1] + B[2] * e[2];
+    B[0] = B[0] - e[0] * d;
+    B[1] = B[1] - e[1] * d;
+    B[2] = B[2] - e[2] * d;
+}
+
 struct StepArgs {
     HamDev h;
     NoiseArgs nz;
     const double *lambda, *temp, *landeg, *mmom;
     double delta_t, bn, temprescale, relaxtime;
-    int noise_on;  // midpoint/SIB: rannum only when min(lambda) > 1e-12
+    int noise_on;
+    int perp;  // midpoint/SIB: rannum only when min(lambda) > 1e-12
     const int64_t *d_step;
     int64_t step_off;
     Vec3D e, eM, p, pM, b2, mpast;
@@ -146,6 +155,7 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
     const double lam = a.lambda[i];
     const double mm = a.mmom[o];
     double e[3] = {a.e.x[o], a.e.y[o], a.e.z[o]};
+    if (a.perp) perp_project(B, e);  // emom is m(t) before every solver's first half-step
     double z[3];
     if (ALG == 5) {
         noise3(a.nz, i, k, N, M, step, z);
@@ -266,6 +276,9 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
     const double mm = a.mmom[o];
     double e[3] = {a.e.x[o], a.e.y[o], a.e.z[o]};
     double pr[3] = {a.p.x[o], a.p.y[o], a.p.z[o]};
+    // after the first half-step emom is m(t) for midpoint and SIB, the predictor for
+    // Heun, Depondt and LLGI
+    if (a.perp) perp_project(B, (ALG == 1 || ALG == 6) ? e : pr);
     double out[3];
     double z[3];
     if (ALG == 5) {
@@ -396,6 +409,7 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     a.bn = s.llg.bn;
     a.temprescale = s.llg.temprescale;
     a.relaxtime = s.llg.relaxtime;
+    a.perp = s.llg.perp;
     a.noise_on = s.llg.noise_on;
     a.d_step = s.llg.d_step;
     a.step_off = step_offset;

@@ -46,6 +46,7 @@ struct LlgDev {
     int sdealgh = 5;
     double delta_t = 1e-16, bn = 1.0, temprescale = 1.0;
     double relaxtime = 0.0;  // SDEalgh 11: relaxation time of the inertial regime (s)
+    int perp = 0;            // input perp = 'Y': field projected perpendicular to emom
     double *lambda = nullptr, *temp = nullptr, *landeg = nullptr;  // [natom]
     double *mmom = nullptr;  // [mensemble][natom]
     uint64_t seed = 0;

@@ -30,7 +30,8 @@ class GpuSimulation:
 
     def __init__(self, lat: Lattice, sdealgh: int = 5, delta_t: float = 1e-16, damping=0.1,
                  temperature=0.0, landeg=1.0, seed: int = 1, emom: Optional[np.ndarray] = None,
-                 precision: int = 0, gpu_rng: int = 0, bn: float = 1.0, relaxtime: float = 0.0):
+                 precision: int = 0, gpu_rng: int = 0, bn: float = 1.0, relaxtime: float = 0.0,
+                 perp: bool = False):
         if isinstance(sdealgh, str):
             sdealgh = SOLVERS[sdealgh]
         self.lat = lat
@@ -90,6 +91,8 @@ class GpuSimulation:
             self.set_jtensor(lat.j_tens)
         if relaxtime:
             _lib.call("uppasd_gpu_set_relaxtime", self._h, float(relaxtime))
+        if perp:
+            _lib.call("uppasd_gpu_set_perp", self._h, 1)
 
     def set_jtensor(self, j_tens: Optional[np.ndarray]):
         """Exchange tensor in the Fortran image (nham, mnn, 3, 3) = j_tens(3,3,mnn,nham);
