@@ -147,8 +147,8 @@ __device__ __forceinline__ int wrap_site(int x, int y, int L) {
 }
 
 // Windows of `rows` patches into X (rows x 192, bf16); optionally the old patch
-// spins (rows x 48, FP64).  One thread per (row, window position).
-__global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat16 *X, double *old_patch,
+// spins (rows x 48, FP32).  One thread per (row, window position).
+__global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat16 *X, float *old_patch,
                          float *win) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)rows * 64) return;
@@ -172,10 +172,10 @@ __global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat1
     }
     if (old_patch && wy >= 2 && wy < 6 && wx >= 2 && wx < 6) {
         const int s = (wy - 2) * 4 + (wx - 2);
-        double *op = old_patch + (size_t)r * 48 + 3 * s;
-        op[0] = v[0];
-        op[1] = v[1];
-        op[2] = v[2];
+        float *op = old_patch + (size_t)r * 48 + 3 * s;
+        op[0] = (float)v[0];
+        op[1] = (float)v[1];
+        op[2] = (float)v[2];
     }
 }
 
@@ -187,8 +187,9 @@ __device__ __forceinline__ double log_vmf(const double eta[3], const double x[3]
     return dot + log(kap) - log(2.0 * kPi) - log(-expm1(-2.0 * kap)) - kap;
 }
 
-// log vMF in FP32 (summed in FP64 by the callers): the same function scores the
-// sampled and the current patch, and the sampler itself is FP32.
+// log vMF in FP32: the same function scores the sampled and the current patch, and
+// the sampler itself is FP32.  A row's 16 terms are summed in FP32 (rounding ~1e-5,
+// far below what the acceptance test resolves).
 __device__ __forceinline__ float log_vmf_f(float ex, float ey, float ez, float x, float y, float z) {
     const float kap = sqrtf(ex * ex + ey * ey + ez * ez);
     const float dot = ex * x + ey * y + ez * z;
@@ -201,8 +202,8 @@ __device__ __forceinline__ float log_vmf_f(float ex, float ey, float ez, float x
 // group g draw their spins from vMF(eta), add their log density to log q(new),
 // and write them to the new-patch buffer and into the window for the next pass.
 __global__ void __launch_bounds__(128) k_vmf_group(int rows, int g, float eta_scale, const float *O,
-                                                   __nv_bfloat16 *X, const double *old_patch, double *new_patch,
-                                                   double *logq_old, double *logq_new, uint64_t seed,
+                                                   __nv_bfloat16 *X, const float *old_patch, float *new_patch,
+                                                   float *logq_old, float *logq_new, uint64_t seed,
                                                    const long long *dctr, int sub) {
     const int lane = threadIdx.x & 31;
     const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;  // rows % 8 == 0: whole warps stay in range
@@ -210,10 +211,10 @@ __global__ void __launch_bounds__(128) k_vmf_group(int rows, int g, float eta_sc
     const long long ctr = *dctr * 16 + sub;  // device sweep counter: graph replays draw fresh numbers
     const float *o = O + (size_t)r * kOut;
     const float ex = eta_scale * o[3 * s], ey = eta_scale * o[3 * s + 1], ez = eta_scale * o[3 * s + 2];
-    double t_old = 0.0, t_new = 0.0;
+    float t_old = 0.f, t_new = 0.f;
     if (g == 0) {
-        const double *op = old_patch + (size_t)r * 48 + 3 * s;
-        t_old = (double)log_vmf_f(ex, ey, ez, (float)op[0], (float)op[1], (float)op[2]);
+        const float *op = old_patch + (size_t)r * 48 + 3 * s;
+        t_old = log_vmf_f(ex, ey, ez, op[0], op[1], op[2]);
     }
     if (patch_group(py, px) == g) {
         const float kap = sqrtf(ex * ex + ey * ey + ez * ez);
@@ -261,8 +262,8 @@ __global__ void __launch_bounds__(128) k_vmf_group(int rows, int g, float eta_sc
         nx *= il;
         ny *= il;
         nz *= il;
-        t_new = (double)log_vmf_f(ex, ey, ez, nx, ny, nz);
-        double *np_ = new_patch + (size_t)r * 48 + 3 * s;
+        t_new = log_vmf_f(ex, ey, ez, nx, ny, nz);
+        float *np_ = new_patch + (size_t)r * 48 + 3 * s;
         np_[0] = nx;
         np_[1] = ny;
         np_[2] = nz;
@@ -325,8 +326,8 @@ struct SqCoup {
 // ~3e-5), the patch sums and the decision FP64: the log acceptance carries an error
 // of ~1e-5 / T[K], far below any statistical resolution.
 __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D e, Vec3D eM, int natom, int rows,
-                                                   const float *win, const double *old_patch, const double *new_patch,
-                                                   const double *logq_old, const double *logq_new, double beta_mub,
+                                                   const float *win, const float *old_patch, const float *new_patch,
+                                                   const float *logq_old, const float *logq_new, float beta_mub,
                                                    uint64_t seed, const long long *dctr, int sub,
                                                    unsigned long long *accepted, double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
@@ -336,9 +337,8 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
     int k, x0, y0;
     patch_of_row(g, r, k, x0, y0);
     const int s = lane & 15, py = s >> 2, px = s & 3;
-    const double *patch = (lane < 16 ? new_patch : old_patch) + (size_t)r * 48;
-    const double ei[3] = {patch[3 * s], patch[3 * s + 1], patch[3 * s + 2]};
-    const float fi[3] = {(float)ei[0], (float)ei[1], (float)ei[2]};
+    const float *patch = (lane < 16 ? new_patch : old_patch) + (size_t)r * 48;
+    const float fi[3] = {patch[3 * s], patch[3 * s + 1], patch[3 * s + 2]};
     const size_t off = (size_t)k * natom;
     float E = -(q.ext[0] * fi[0] + q.ext[1] * fi[1] + q.ext[2] * fi[2]);
     const int ddx[4] = {1, -1, 0, 0}, ddy[4] = {0, 0, 1, -1};
@@ -348,9 +348,9 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
         float ej[3], w;
         if (nx >= 0 && nx < 4 && ny >= 0 && ny < 4) {
             const int sj = ny * 4 + nx;
-            ej[0] = (float)patch[3 * sj];
-            ej[1] = (float)patch[3 * sj + 1];
-            ej[2] = (float)patch[3 * sj + 2];
+            ej[0] = patch[3 * sj];
+            ej[1] = patch[3 * sj + 1];
+            ej[2] = patch[3 * sj + 2];
             w = 0.5f;
         } else {
             // the boundary site from the window copy (no other patch of this colour touches it)
@@ -366,20 +366,24 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
                   (q.d[d][0] * cx + q.d[d][1] * cy + q.d[d][2] * cz));
     }
     E *= q.mom;
-    double dE = lane < 16 ? (double)E : -(double)E;
+    // per spin new - old (lanes s and s + 16), then the sum over the patch; FP32
+    // throughout, as GB300's FP64 pipe would set this kernel's time
+    float dE = lane < 16 ? E : -E;
+    dE += __shfl_xor_sync(0xffffffffu, dE, 16);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
-    const double loga = -beta_mub * dE + logq_old[r] - logq_new[r];
+    for (int o = 8; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
     int acc = 0;
     if (lane == 0) {
+        const float loga = -beta_mub * dE + (logq_old[r] - logq_new[r]);
         const Philox4 w = philox_draw(seed, r, 16, ctr, kStreamLearned);
-        const double u = u01_open(w.z);
-        acc = (loga >= 0.0 || log(u) < loga) ? 1 : 0;
+        const float u = u01_openf(w.z);
+        acc = (loga >= 0.f || logf(u) < loga) ? 1 : 0;
     }
     acc = __shfl_sync(0xffffffffu, acc, 0);
     if (acc && lane < kSpins) {
         const size_t o = off + wrap_site(x0 + px, y0 + py, g.L);
         const double mm = (double)q.mom;
+        const double ei[3] = {(double)fi[0], (double)fi[1], (double)fi[2]};
         e.x[o] = ei[0];
         e.y[o] = ei[1];
         e.z[o] = ei[2];
@@ -387,17 +391,29 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
         eM.y[o] = mm * ei[1];
         eM.z[o] = mm * ei[2];
     }
-    block_count(acc, dE, accepted, dE_sum);
+    block_count(acc, (double)dE, accepted, dE_sum);
 }
 
 // Energy of patch spin `s` (site i) in one configuration: bonds to sites outside the
 // patch in full, bonds inside the patch at one half, plus on-site terms.  Units: T muB.
+// OLD: the configuration in the state (FP64, read from eM); otherwise the sampled
+// patch (FP32 values, exact in FP64) with the state outside it.
+template <bool OLD>
 __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const double *mmom, int k, int i, int x0,
-                                    int y0, int L, const double *patch /*48*/, int s) {
+                                    int y0, int L, const float *patch /*48*/, int s) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
     const double mm = mmom[off + i];
-    const double mi[3] = {patch[3 * s] * mm, patch[3 * s + 1] * mm, patch[3 * s + 2] * mm};
+    double mi[3];
+    if (OLD) {
+        mi[0] = eM.x[off + i];
+        mi[1] = eM.y[off + i];
+        mi[2] = eM.z[off + i];
+    } else {
+        mi[0] = (double)patch[3 * s] * mm;
+        mi[1] = (double)patch[3 * s + 1] * mm;
+        mi[2] = (double)patch[3 * s + 2] * mm;
+    }
     const int ih = h.aham[i];
     double E = 0.0;
     for (int q = 0; q < h.nsize[i]; ++q) {
@@ -406,12 +422,18 @@ __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const doub
         const int dx = (jx - x0 + L) % L, dy = (jy - y0 + L) % L;
         double mj[3], w = 1.0;
         if (dx < 4 && dy < 4) {
-            const int sj = dy * 4 + dx;
-            const double mmj = mmom[off + j];
-            mj[0] = patch[3 * sj] * mmj;
-            mj[1] = patch[3 * sj + 1] * mmj;
-            mj[2] = patch[3 * sj + 2] * mmj;
             w = 0.5;
+            if (OLD) {
+                mj[0] = eM.x[off + j];
+                mj[1] = eM.y[off + j];
+                mj[2] = eM.z[off + j];
+            } else {
+                const int sj = dy * 4 + dx;
+                const double mmj = mmom[off + j];
+                mj[0] = (double)patch[3 * sj] * mmj;
+                mj[1] = (double)patch[3 * sj + 1] * mmj;
+                mj[2] = (double)patch[3 * sj + 2] * mmj;
+            }
         } else {
             mj[0] = eM.x[off + j];
             mj[1] = eM.y[off + j];
@@ -427,12 +449,18 @@ __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const doub
             const int dx = (jx - x0 + L) % L, dy = (jy - y0 + L) % L;
             double mj[3], w = 1.0;
             if (dx < 4 && dy < 4) {
-                const int sj = dy * 4 + dx;
-                const double mmj = mmom[off + j];
-                mj[0] = patch[3 * sj] * mmj;
-                mj[1] = patch[3 * sj + 1] * mmj;
-                mj[2] = patch[3 * sj + 2] * mmj;
                 w = 0.5;
+                if (OLD) {
+                    mj[0] = eM.x[off + j];
+                    mj[1] = eM.y[off + j];
+                    mj[2] = eM.z[off + j];
+                } else {
+                    const int sj = dy * 4 + dx;
+                    const double mmj = mmom[off + j];
+                    mj[0] = (double)patch[3 * sj] * mmj;
+                    mj[1] = (double)patch[3 * sj + 1] * mmj;
+                    mj[2] = (double)patch[3 * sj + 2] * mmj;
+                }
             } else {
                 mj[0] = eM.x[off + j];
                 mj[1] = eM.y[off + j];
@@ -455,9 +483,9 @@ __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const doub
 
 // One warp per patch: exact energy change, Metropolis-Hastings decision, write-back.
 __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double *mmom, int rows,
-                         const double *old_patch, const double *new_patch, const double *logq_old,
-                         const double *logq_new, double beta_mub, uint64_t seed, const long long *dctr, int sub,
-                         unsigned long long *accepted, double *dE_sum) {
+                         const float *new_patch, const float *logq_old, const float *logq_new, double beta_mub,
+                         uint64_t seed, const long long *dctr, int sub, unsigned long long *accepted,
+                         double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     // rows is a multiple of 128 and blocks hold 8 warps: every warp of the grid is a patch
     const int r = warp;
@@ -468,31 +496,31 @@ __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double 
     if (lane < kSpins) {
         const int py = lane >> 2, px = lane & 3;
         const int i = wrap_site(x0 + px, y0 + py, g.L);
-        dE = patch_spin_energy(h, eM, mmom, k, i, x0, y0, g.L, new_patch + (size_t)r * 48, lane) -
-             patch_spin_energy(h, eM, mmom, k, i, x0, y0, g.L, old_patch + (size_t)r * 48, lane);
+        dE = patch_spin_energy<false>(h, eM, mmom, k, i, x0, y0, g.L, new_patch + (size_t)r * 48, lane) -
+             patch_spin_energy<true>(h, eM, mmom, k, i, x0, y0, g.L, nullptr, lane);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
-    const double loga = -beta_mub * dE + logq_old[r] - logq_new[r];
     int acc = 0;
     if (lane == 0) {
+        const double loga = -beta_mub * dE + (double)(logq_old[r] - logq_new[r]);
         const Philox4 w = philox_draw(seed, r, 16, ctr, kStreamLearned);
-        const double u = u01_open(w.z);
-        acc = (loga >= 0.0 || log(u) < loga) ? 1 : 0;
+        const float u = u01_openf(w.z);
+        acc = (loga >= 0.0 || (double)logf(u) < loga) ? 1 : 0;
     }
     acc = __shfl_sync(0xffffffffu, acc, 0);
     if (acc && lane < kSpins) {
         const int py = lane >> 2, px = lane & 3;
         const int i = wrap_site(x0 + px, y0 + py, g.L);
         const size_t o = (size_t)k * h.natom + i;
-        const double *np_ = new_patch + (size_t)r * 48 + 3 * lane;
+        const float *np_ = new_patch + (size_t)r * 48 + 3 * lane;
         const double mm = mmom[o];
-        e.x[o] = np_[0];
-        e.y[o] = np_[1];
-        e.z[o] = np_[2];
-        eM.x[o] = mm * np_[0];
-        eM.y[o] = mm * np_[1];
-        eM.z[o] = mm * np_[2];
+        e.x[o] = (double)np_[0];
+        e.y[o] = (double)np_[1];
+        e.z[o] = (double)np_[2];
+        eM.x[o] = mm * (double)np_[0];
+        eM.y[o] = mm * (double)np_[1];
+        eM.z[o] = mm * (double)np_[2];
     }
     block_count(acc, dE, accepted, dE_sum);
 }
@@ -584,7 +612,7 @@ struct uppasd_gpu_proposal {
     float *params = nullptr;   // one allocation for all fp32 parameter-sized arrays
     long long nparams = 0;
     // sampling
-    double *old_patch = nullptr, *new_patch = nullptr, *logq_old = nullptr, *logq_new = nullptr;
+    float *old_patch = nullptr, *new_patch = nullptr, *logq_old = nullptr, *logq_new = nullptr;
     float *win = nullptr;  // FP32 copy of each row's window (rows x 192)
     unsigned long long *accepted = nullptr;
     double *dE_sum = nullptr, *loss = nullptr;
@@ -816,7 +844,7 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
                                                                   p->new_patch, p->logq_old, p->logq_new, beta_mub,
                                                                   p->seed, p->dctr, c, p->accepted, p->dE_sum);
         } else {
-            k_accept<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, s.ham, s.e, s.eM, s.llg.mmom, rows, p->old_patch,
+            k_accept<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, s.ham, s.e, s.eM, s.llg.mmom, rows,
                                                                p->new_patch, p->logq_old, p->logq_new, beta_mub,
                                                                p->seed, p->dctr, c, p->accepted, p->dE_sum);
         }
@@ -903,11 +931,11 @@ int uppasd_gpu_proposal_create(uppasd_gpu_sim *sim, int32_t L, float eta_scale, 
         al((void **)&B.wb[l], (size_t)kNW[l] * 2);
         al((void **)&B.wt[l], (size_t)kNW[l] * 2);
     }
-    al((void **)&p->old_patch, (size_t)R * 48 * 8);
-    al((void **)&p->new_patch, (size_t)R * 48 * 8);
-    al((void **)&p->logq_old, (size_t)R * 8);
+    al((void **)&p->old_patch, (size_t)R * 48 * 4);
+    al((void **)&p->new_patch, (size_t)R * 48 * 4);
+    al((void **)&p->logq_old, (size_t)R * 4);
     al((void **)&p->win, (size_t)R * kFeat * 4);
-    al((void **)&p->logq_new, (size_t)R * 8);
+    al((void **)&p->logq_new, (size_t)R * 4);
     al((void **)&p->accepted, sizeof(unsigned long long));
     al((void **)&p->dE_sum, sizeof(double));
     al((void **)&p->loss, sizeof(double));
