@@ -7,9 +7,11 @@
 // (M = 128, N = 256 or 64, K = 16) into TMEM columns [0, N), and the four compute
 // warps read the accumulator back (tcgen05.ld, warp w = rows 32w..32w+31), apply
 // bias + tanh, round to bf16 and write the result into A in the same swizzled
-// K-major layout the next layer's MMAs read.  The last layer writes fp32 outputs
-// (bias, no activation) to global memory.  A fifth warp is the TMA producer, so
-// the compute warps' named barrier never waits on it.
+// K-major layout the next layer's MMAs read.  Eight compute warps share the
+// epilogue: warps w and w + 4 read the same TMEM lane quadrant (w % 4, the rows
+// 32 (w % 4) .. + 31) and take one half of the columns each.  The last layer writes
+// fp32 outputs (bias, no activation) to global memory.  A ninth warp is the TMA
+// producer, so the compute warps' named barrier never waits on it.
 //
 // Shared memory: A 64 KB (the input tile uses 48 KB of it, then each hidden
 // layer's activations) + ring 4 x 32 KB.  TMEM: 256 columns.  Every wait is
@@ -22,7 +24,8 @@ namespace uppasd {
 namespace tc {
 
 constexpr int kMlpIn = 192, kMlpHid = 256, kMlpOut = 64;
-constexpr int kMlpThreads = 160;                  // 4 compute warps + 1 producer warp
+constexpr int kMlpCompute = 8;                    // compute warps (two per TMEM lane quadrant)
+constexpr int kMlpThreads = 32 * (kMlpCompute + 1); // + 1 producer warp
 constexpr uint32_t kMlpABytes = 128 * 256 * 2;    // activation tile: 4 K-slices of 16 KB
 constexpr uint32_t kMlpStageBytes = 256 * 64 * 2; // one weight K-slice (N <= 256)
 constexpr int kMlpStages = 4;
@@ -40,7 +43,7 @@ __host__ __device__ constexpr int mlp_k_of_chunk(int g) { return g < 3 ? g : (g 
 __host__ __device__ constexpr int mlp_n(int l) { return l == 3 ? kMlpOut : kMlpHid; }
 __host__ __device__ constexpr int mlp_kslices(int l) { return l == 0 ? 3 : 4; }
 
-__device__ __forceinline__ void named_bar_compute() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+__device__ __forceinline__ void named_bar_compute() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
 __global__ void __launch_bounds__(kMlpThreads, 1)
     tc_mlp_kernel(const __grid_constant__ CUtensorMap mapX, const __grid_constant__ CUtensorMap mapW0,
@@ -77,7 +80,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base_s;
 
-    if (warp == 4) {
+    if (warp == kMlpCompute) {
         // producer: the input tile, then every weight K-slice of every layer through the ring
         if (lane == 0) {
             mbar_expect_tx(&xfull, 128 * kMlpIn * 2);
@@ -115,11 +118,12 @@ __global__ void __launch_bounds__(kMlpThreads, 1)
             if (lane == 0 && !mbar_wait(&done, l & 1)) atomicExch(a.err, 14);
             __syncwarp();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            // epilogue: row r = 32 warp + lane, columns in slices of 16
-            const int r = warp * 32 + lane;
-            const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+            // epilogue: row r = 32 (warp % 4) + lane, column half warp / 4, slices of 16
+            const int quad = warp & 3, half = warp >> 2;
+            const int r = quad * 32 + lane;
+            const uint32_t tl = tmem + ((uint32_t)(quad * 32) << 16);
             const float *bias = a.bias[l];
-            for (int c = 0; c < N; c += 16) {
+            for (int c = half * (N / 2); c < (half + 1) * (N / 2); c += 16) {
                 float v[16];
                 tmem_ld16(tl + c, v);
                 if (l < 3) {
