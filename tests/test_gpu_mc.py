@@ -139,3 +139,36 @@ def test_square_structured_refuses_other_lattices():
         _lib.call("uppasd_gpu_mc_run_square", sim._h, 8, 100.0, 1)
     assert ei.value.rc == -7
     sim.close()
+
+
+def test_square_mirror_follows_every_state_change():
+    """The structured square path reads an FP32 mirror of the spins: FP64 sweeps, LLG
+    steps and put_moments in between must all be seen by the next structured sweep."""
+    lat = lattice.square_dmi(16, 1.0, 0.3, 0.0, 5.0, 1.0).with_ensembles(2)
+    rng = np.random.default_rng(18)
+    e0, e1 = _rand_unit(rng, (2, lat.natom, 3)), _rand_unit(rng, (2, lat.natom, 3))
+    T = 40.0
+    sim = GpuSimulation(lat, emom=e0, seed=77, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=0.0)
+    sim.relax("H", T, 2, structured=True)
+    sim.relax("H", T, 1)
+    sim.evolve(5)
+    sim.relax("H", T, 2, structured=True)
+    g1 = sim.get_moments()
+    sim.put_moments(e1)
+    sim.relax("H", T, 1, structured=True)
+    g2 = sim.get_moments()
+    sim.close()
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(5, 1e-16, 0.1, 0.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=77)
+    _, order, start = lattice.greedy_colouring(lat)
+    for sw in range(3):
+        o.mc_sweep_checkerboard("H", T, order, start, 77, sw)
+    for _ in range(5):
+        o.sd_step()
+    for sw in (3, 4):
+        o.mc_sweep_checkerboard("H", T, order, start, 77, sw)
+    assert np.max(np.abs(g1 - o.emom)) < 2e-4
+    o.set_moments(e1)
+    o.mc_sweep_checkerboard("H", T, order, start, 77, 5)
+    assert np.max(np.abs(g2 - o.emom)) < 2e-4

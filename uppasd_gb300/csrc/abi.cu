@@ -351,7 +351,7 @@ void destroy(Sim &s) {
     HamDev &h = s.ham;
     void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
-                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites};
+                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm};
     for (void *q : ptrs) cudaFree(q);
     free_vec3(h.ext);
     free_vec3(s.e);
@@ -372,6 +372,7 @@ int one_step(Sim &s, int64_t off, int phase = 3) {
 int run_steps(Sim &s, int64_t n) {
     const int G = 16;
     int rc;
+    square_mirror_stale(s);
     if (!s.graph && n >= G) {
         cudaGraph_t g;
         UPPASD_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
@@ -470,6 +471,7 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = w->s;
+    uppasd::square_mirror_stale(s);
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     double *d = nullptr;
     UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
@@ -679,6 +681,7 @@ int uppasd_gpu_time_kernels(uppasd_gpu_sim *w, int32_t nrep, double *ms) {
     for (auto &e : ev) UPPASD_CUDA_TRY(cudaEventCreate(&e));
     double acc[3] = {0.0, 0.0, 0.0};
     int rc = UPPASD_GPU_OK;
+    uppasd::square_mirror_stale(s);
     for (int r = 0; r < nrep && rc == UPPASD_GPU_OK; ++r) {
         cudaEventRecord(ev[0], s.stream);
         rc = uppasd::one_step(s, 0, 1);

@@ -147,9 +147,10 @@ __device__ __forceinline__ int wrap_site(int x, int y, int L) {
 }
 
 // Windows of `rows` patches into X (rows x 192, bf16); optionally the old patch
-// spins (rows x 48, FP32).  One thread per (row, window position).
-__global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat16 *X, float *old_patch,
-                         float *win) {
+// spins (rows x 48, FP32).  One thread per (row, window position).  The spins come
+// from the FP32 mirror when `m` is given (the square-lattice path), else from e.
+__global__ void k_gather(PatchGeom g, Vec3D e, const float4 *m, int natom, int rows, __nv_bfloat16 *X,
+                         float *old_patch, float *win) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)rows * 64) return;
     const int r = (int)(t >> 6), pos = (int)(t & 63);
@@ -158,24 +159,34 @@ __global__ void k_gather(PatchGeom g, Vec3D e, int natom, int rows, __nv_bfloat1
     const int wy = pos >> 3, wx = pos & 7;
     const int i = wrap_site(x0 - 2 + wx, y0 - 2 + wy, g.L);
     const size_t o = (size_t)k * natom + i;
-    const double v[3] = {e.x[o], e.y[o], e.z[o]};
+    float v[3];
+    if (m) {
+        const float4 q = m[o];
+        v[0] = q.x;
+        v[1] = q.y;
+        v[2] = q.z;
+    } else {
+        v[0] = (float)e.x[o];
+        v[1] = (float)e.y[o];
+        v[2] = (float)e.z[o];
+    }
     __nv_bfloat16 *xr = X + (size_t)r * kFeat + pos * 3;
-    xr[0] = __float2bfloat16_rn((float)v[0]);
-    xr[1] = __float2bfloat16_rn((float)v[1]);
-    xr[2] = __float2bfloat16_rn((float)v[2]);
+    xr[0] = __float2bfloat16_rn(v[0]);
+    xr[1] = __float2bfloat16_rn(v[1]);
+    xr[2] = __float2bfloat16_rn(v[2]);
     if (win) {
         // FP32 copy of the window for the acceptance kernel's bonds to the boundary
         float *wr = win + (size_t)r * kFeat + pos * 3;
-        wr[0] = (float)v[0];
-        wr[1] = (float)v[1];
-        wr[2] = (float)v[2];
+        wr[0] = v[0];
+        wr[1] = v[1];
+        wr[2] = v[2];
     }
     if (old_patch && wy >= 2 && wy < 6 && wx >= 2 && wx < 6) {
         const int s = (wy - 2) * 4 + (wx - 2);
         float *op = old_patch + (size_t)r * 48 + 3 * s;
-        op[0] = (float)v[0];
-        op[1] = (float)v[1];
-        op[2] = (float)v[2];
+        op[0] = v[0];
+        op[1] = v[1];
+        op[2] = v[2];
     }
 }
 
@@ -325,7 +336,8 @@ struct SqCoup {
 // Each lane's bond sum is FP32 (a bond term is at most |J| m ~ 500 T muB, rounded to
 // ~3e-5), the patch sums and the decision FP64: the log acceptance carries an error
 // of ~1e-5 / T[K], far below any statistical resolution.
-__global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D e, Vec3D eM, int natom, int rows,
+__global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, float4 *m, Vec3D e, Vec3D eM, int natom,
+                                                   int rows,
                                                    const float *win, const float *old_patch, const float *new_patch,
                                                    const float *logq_old, const float *logq_new, float beta_mub,
                                                    uint64_t seed, const long long *dctr, int sub,
@@ -384,6 +396,7 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, Vec3D 
         const size_t o = off + wrap_site(x0 + px, y0 + py, g.L);
         const double mm = (double)q.mom;
         const double ei[3] = {(double)fi[0], (double)fi[1], (double)fi[2]};
+        m[o] = make_float4(fi[0], fi[1], fi[2], 0.f);
         e.x[o] = ei[0];
         e.y[o] = ei[1];
         e.z[o] = ei[2];
@@ -826,7 +839,10 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
     int rc;
     for (int c = 0; c < 4; ++c) {
         PatchGeom g = geom(p, c);
-        k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, s.ham.natom, rows, p->B.X, p->old_patch, p->win);
+        // the square-lattice path reads the FP32 mirror (made ready by the caller)
+        const float4 *mirror = s.sq.L == p->L ? s.sqm : nullptr;
+        k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(g, s.e, mirror, s.ham.natom, rows, p->B.X,
+                                                                p->old_patch, p->win);
         for (int grp = 0; grp < 4; ++grp) {
             if ((rc = forward_fused(p, rows, st))) return rc;
             k_vmf_group<<<rows / 8, 128, 0, st>>>(rows, grp, p->eta_scale, p->B.O, p->B.X, p->old_patch,
@@ -840,7 +856,8 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
             }
             for (int cc = 0; cc < 3; ++cc) q.ext[cc] = s.sq.ext[cc];
             q.mom = s.sq.mom;
-            k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.e, s.eM, s.ham.natom, rows, p->win, p->old_patch,
+            k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.sqm, s.e, s.eM, s.ham.natom, rows, p->win,
+                                                                  p->old_patch,
                                                                   p->new_patch, p->logq_old, p->logq_new, beta_mub,
                                                                   p->seed, p->dctr, c, p->accepted, p->dE_sum);
         } else {
@@ -1139,7 +1156,11 @@ int uppasd_gpu_proposal_collect(uppasd_gpu_proposal *p) {
     if (at + rows > p->data_cap) at = 0;
     PatchGeom g = geom(p, -1);
     const long long nt = (long long)rows * 64;
-    k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, s.stream>>>(g, s.e, s.ham.natom, rows,
+    const bool sq = s.sq.L == p->L;
+    if (sq) {
+        if (const int rc = square_mirror_ready(s)) return rc;
+    }
+    k_gather<<<(unsigned)((nt + 255) / 256), 256, 0, s.stream>>>(g, s.e, sq ? s.sqm : nullptr, s.ham.natom, rows,
                                                                  p->data + (size_t)at * kFeat, nullptr, nullptr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail("proposal_collect", e);
@@ -1214,6 +1235,12 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     if (e == cudaSuccess) e = cudaMemsetAsync(p->dE_sum, 0, sizeof(double), st);
     if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
     const double beta_mub = kMub / (kKbolt * temperature);
+    if (s.sq.L == p->L) {
+        // learned moves on the square lattice read and write the FP32 mirror as well
+        if ((rc = square_mirror_ready(s))) return rc;
+    } else {
+        square_mirror_stale(s);  // the neighbour-list path writes e / eM only
+    }
     int64_t done = 0;
     auto heat_bath = [&]() -> int {
         return hb_per_cycle > 0 ? uppasd_gpu_mc_run_square(p->sim, p->L, temperature, hb_per_cycle) : 0;

@@ -729,6 +729,7 @@ int structured_load_state(Sim &s) {
 }
 
 int structured_sync_state(Sim &s) {
+    square_mirror_stale(s);
     StructuredFast *f = s.fast;
     long long total = f->p.nsite * f->p.nens;
     from_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y,

@@ -173,6 +173,7 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
 }
 
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps) {
+    square_mirror_stale(s);
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");
         return UPPASD_GPU_ESTATE;

@@ -7,6 +7,10 @@
 // couplings are per-direction constants recognised once from the caller's
 // nlist/ncoup/dmlist/dm_vect, and the heat-bath draw (flip_h,
 // MonteCarlo/montecarlo_common.f90:371-422) runs in FP32 on the FP64 spin state.
+// Neighbours are read from an FP32 mirror of the state (the values the draw uses
+// anyway), and every new spin is written to the mirror and to e / eM: on GB300
+// the double-to-float conversions of the neighbours, which run on the FP64 pipe,
+// would otherwise set the sweep's time.
 // The chain is the checkerboard chain of mc.cu (colours x + y even, then odd)
 // with the same Philox counters (site, ensemble, sweep), so it agrees with the
 // FP64 path to FP32 rounding.
@@ -47,7 +51,7 @@ __device__ __forceinline__ float3 heat_bath_f32(float3 h, float beta_mu, float q
     return make_float3(nx * il, ny * il, nz * il);
 }
 
-__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, Vec3D e, Vec3D eM) {
+__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e, Vec3D eM) {
     const int half = a.L >> 1;
     const long long per = (long long)a.L * half;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -64,8 +68,8 @@ __global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, Vec3D e, Vec3D eM)
     float hx = a.ext[0], hy = a.ext[1], hz = a.ext[2];
 #pragma unroll
     for (int d = 0; d < 4; ++d) {
-        const size_t o = off + nb[d];
-        const float ex = (float)e.x[o], ey = (float)e.y[o], ez = (float)e.z[o];
+        const float4 v = m[off + nb[d]];
+        const float ex = v.x, ey = v.y, ez = v.z;
         // exchange c e_j plus DMI e_j x d
         hx += a.c[d] * ex + (ey * a.d[d][2] - ez * a.d[d][1]);
         hy += a.c[d] * ey + (ez * a.d[d][0] - ex * a.d[d][2]);
@@ -77,12 +81,18 @@ __global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, Vec3D e, Vec3D eM)
     const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
     const float3 n = heat_bath_f32(make_float3(hx, hy, hz), a.beta_mu, q, fp);
     const size_t o = off + i;
+    m[o] = make_float4(n.x, n.y, n.z, 0.f);
     e.x[o] = n.x;
     e.y[o] = n.y;
     e.z[o] = n.z;
     eM.x[o] = (double)a.mom * n.x;
     eM.y[o] = (double)a.mom * n.y;
     eM.z[o] = (double)a.mom * n.z;
+}
+
+__global__ void to_mirror(Vec3D e, float4 *m, long long n) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) m[t] = make_float4((float)e.x[t], (float)e.y[t], (float)e.z[t], 0.f);
 }
 
 template <typename T>
@@ -178,6 +188,19 @@ int square_recognise(Sim &s, int L) {
     return UPPASD_GPU_OK;
 }
 
+int square_mirror_ready(Sim &s) {
+    if (s.sqm_valid) return UPPASD_GPU_OK;
+    const long long n = (long long)s.ham.natom * s.ham.mensemble;
+    if (!s.sqm) {
+        UPPASD_CUDA_TRY(cudaMalloc(&s.sqm, (size_t)n * sizeof(float4)));
+        s.bytes_allocated += (size_t)n * sizeof(float4);
+    }
+    to_mirror<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.e, s.sqm, n);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    s.sqm_valid = 1;
+    return UPPASD_GPU_OK;
+}
+
 }  // namespace uppasd
 
 extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double temperature, int64_t nsweeps) {
@@ -195,6 +218,7 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
         const int rc = square_recognise(s, L);
         if (rc) return rc;
     }
+    if (const int rc = square_mirror_ready(s)) return rc;
     SqArgs a{};
     a.L = L;
     a.N = s.ham.natom;
@@ -213,7 +237,7 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
         a.sweep = s.mc_sweep;
         for (int c = 0; c < 2; ++c) {
             a.colour = c;
-            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.e, s.eM);
+            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.sqm, s.e, s.eM);
         }
         s.mc_sweep += 1;
     }

@@ -91,6 +91,11 @@ struct Sim {
     int32_t *colour_start_h = nullptr; // host copy, ncolour+1
     int64_t mc_sweep = 0;
     SquareMC sq;
+    // FP32 read mirror of the unit spins (x, y, z, 0), [mensemble][natom], for the
+    // structured square heat bath and the learned patch moves: they read it and write
+    // every update to both it and e / eM; any other writer of e marks it stale.
+    float4 *sqm = nullptr;
+    int sqm_valid = 0;
     // scratch for observables
     double *red = nullptr;             // [mensemble][8]
     size_t bytes_allocated = 0;
@@ -118,6 +123,8 @@ int field_to_host(Sim &s, double *beff_h);
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps);
 // mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
 int square_recognise(Sim &s, int L);
+int square_mirror_ready(Sim &s);  // builds the FP32 mirror from e when it is stale
+inline void square_mirror_stale(Sim &s) { s.sqm_valid = 0; }
 
 void set_error(const std::string &msg);
 
