@@ -60,7 +60,10 @@ typedef struct {
                                           1 FP32 field gather + FP64 spin master and
                                             renormalisation (structured lattices, Depondt);
                                           2 FP32 field gather + double-single (float-float)
-                                            spin master and renormalisation (same scope) */
+                                            spin master and renormalisation (same scope);
+                                          3 FP32 field gather over any neighbour list (scalar
+                                            or tensor exchange, DMI, anisotropy, Zeeman) + FP64
+                                            spin master and renormalisation (Depondt, midpoint) */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;

@@ -1,0 +1,128 @@
+"""Precision 3: FP32 gather over the caller's neighbour lists with the FP64 state as
+master (renormalised in FP64 every step), on Hamiltonians outside the structured bcc
+path: exchange (scalar or tensor), DMI, anisotropy and Zeeman, midpoint and Depondt.
+
+The field, thermal field and rotation run in FP32, so trajectories are compared with
+the FP64 oracle at FP32-scale tolerances that grow with the step count (a random
+start at T = 0 amplifies a 1e-7 perturbation to ~1e-5 in 100 steps); spin norms are
+held to 1e-12.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from uppasd_gb300 import _lib, lattice
+from uppasd_gb300.simulation import GpuSimulation
+
+pytestmark = pytest.mark.gpu
+CHECKPOINTS = {10: 2e-6, 100: 2e-5}
+THERMAL_TOL = 2e-4
+
+
+def _rand_unit(rng, shape):
+    e = rng.normal(size=shape)
+    return e / np.linalg.norm(e, axis=-1, keepdims=True)
+
+
+def _pair(lat, solver, temp, e0, seed=31, damping=0.05):
+    sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=damping, temperature=temp, seed=seed,
+                        emom=e0, precision=3)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, 1e-16, damping, temp, 1.0, noise_mode=po.NOISE_PHILOX, seed=seed)
+    return sim, o
+
+
+@pytest.mark.parametrize("kind,solver", [("square_dmi_aniso", 1), ("square_dmi_aniso", 5), ("kagome_tensor", 5),
+                                         ("kagome_tensor", 1)])
+def test_T0_against_oracle(kind, solver):
+    lat = (lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0) if kind == "square_dmi_aniso"
+           else lattice.kagome(12, -1.0, 0.1, 0.05, 1.0, 0.2)).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(41), (2, lat.natom, 3))
+    sim, o = _pair(lat, solver, 0.0, e0)
+    done = 0
+    for n, tol in CHECKPOINTS.items():
+        sim.evolve(n - done)
+        for _ in range(n - done):
+            o.sd_step()
+        done = n
+        g = sim.get_moments()
+        assert np.max(np.abs(g - o.emom)) <= tol, (n, np.max(np.abs(g - o.emom)))
+        assert np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)) <= 1e-12
+    sim.close()
+
+
+@pytest.mark.parametrize("solver", [1, 5])
+def test_thermal_philox_against_oracle(solver):
+    lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(42), (2, lat.natom, 3))
+    sim, o = _pair(lat, solver, 50.0, e0)
+    sim.evolve(200)
+    for _ in range(200):
+        o.sd_step()
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= THERMAL_TOL
+    sim.close()
+
+
+def test_injected_noise_against_oracle():
+    lat = lattice.kagome(12).with_ensembles(1)
+    e0 = _rand_unit(np.random.default_rng(43), (1, lat.natom, 3))
+    nsteps = 100
+    normals = po.ziggurat_stream(3, nsteps * 3 * lat.natom).reshape(nsteps, 1, lat.natom, 3)
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.05, temperature=100.0, emom=e0, precision=3)
+    sim.set_noise(normals)
+    sim.evolve(nsteps)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(5, 1e-16, 0.05, 100.0, 1.0, noise_mode=po.NOISE_ARRAY)
+    for s in range(nsteps):
+        o.sd_step(noise=normals[s])
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= THERMAL_TOL
+    sim.close()
+
+
+def test_agrees_with_structured_path_on_the_alloy():
+    lat = lattice.bcc_alloy(6, seed=9).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(44), (2, lat.natom, 3))
+    out = []
+    for prec in (1, 3):
+        sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=300.0, seed=21, emom=e0,
+                            precision=prec)
+        sim.evolve(100)
+        out.append(sim.get_moments())
+        sim.close()
+    assert np.max(np.abs(out[0] - out[1])) <= 1e-4
+
+
+def test_state_changes_between_runs_are_seen():
+    """put_moments, FP64 and structured Monte Carlo between LLG runs: precision 3 follows
+    the same sequence as the FP64 path to FP32 accuracy."""
+    lat = lattice.square_dmi(16, 1.0, 0.3, 0.0, 0.5, 1.0).with_ensembles(2)
+    rng = np.random.default_rng(45)
+    e0, e1 = _rand_unit(rng, (2, lat.natom, 3)), _rand_unit(rng, (2, lat.natom, 3))
+    res = []
+    for prec in (0, 3):
+        sim = GpuSimulation(lat, sdealgh=1, delta_t=1e-16, damping=0.1, temperature=0.0, seed=9, emom=e0,
+                            precision=prec)
+        sim.evolve(20)
+        sim.relax("H", 30.0, 1)
+        sim.evolve(20)
+        sim.relax("H", 30.0, 2, structured=True)
+        sim.evolve(20)
+        sim.put_moments(e1)
+        sim.evolve(20)
+        res.append(sim.get_moments())
+        sim.close()
+    assert np.max(np.abs(res[0] - res[1])) <= 1e-4
+
+
+def test_scope():
+    lat = lattice.square_dmi(16)
+    with pytest.raises(_lib.UppasdGpuError) as ex:
+        GpuSimulation(lat, sdealgh=4, precision=3)
+    assert ex.value.rc == -7
+    sim = GpuSimulation(lat, sdealgh=1, precision=3)
+    with pytest.raises(_lib.UppasdGpuError) as ex:
+        _lib.call("uppasd_gpu_set_perp", sim._h, 1)
+    assert ex.value.rc == -7
+    sim.close()

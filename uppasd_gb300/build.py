@@ -29,6 +29,7 @@ UNITS = [
     ("observables.cu", ["--fmad=false"]),
     ("mc.cu", ["--fmad=false"]),
     ("llg_stencil.cu", []),
+    ("llg_mixed.cu", []),
     ("noalloc.cu", []),
     ("mc_batch.cu", []),
     ("tc_host.cu", []),

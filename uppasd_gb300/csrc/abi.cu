@@ -28,6 +28,10 @@ int structured_step(Sim &s, int64_t step_offset, int phase);
 int structured_sync_state(Sim &s);  // master state -> s.e / s.eM
 int structured_load_state(Sim &s);  // s.e -> master state
 void structured_free(Sim &s);
+int mixed_init(Sim &s);  // llg_mixed.cu
+void mixed_free(Sim &s);
+int mixed_ready(Sim &s);
+int mixed_step(Sim &s, int64_t step_offset, int phase);
 
 namespace {
 
@@ -203,7 +207,7 @@ int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
         return bad("SDEalgh must be 1, 4, 5, 6 or 11");
     if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
     if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
-    if (c->precision < 0 || c->precision > 2) return bad("precision must be 0, 1 or 2");
+    if (c->precision < 0 || c->precision > 3) return bad("precision must be 0, 1, 2 or 3");
     for (int i = 0; i < c->natom; ++i)
         if (a->aham[i] < 1 || a->aham[i] > c->nham) return bad("aham out of range");
     for (int h = 0; h < c->nham; ++h) {
@@ -336,8 +340,10 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     if (c->sdealgh == 11 && (rc = alloc_vec3(s, s.mpast, NM))) return rc;  // zeroed by put_moments
     if ((rc = build_colouring(s, c, nlT, nsize, dmT, dmsize))) return rc;
     s.precision = c->precision;
-    if (c->precision >= 1) {
+    if (structured(s)) {
         if ((rc = structured_init(s, c, a))) return rc;
+    } else if (c->precision == 3) {
+        if ((rc = mixed_init(s))) return rc;
     }
     if ((rc = uppasd_gpu_put_moments(reinterpret_cast<uppasd_gpu_sim *>(&s), a->emom))) return rc;
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
@@ -348,6 +354,7 @@ void destroy(Sim &s) {
     if (s.stream) cudaStreamSynchronize(s.stream);
     if (s.graph) cudaGraphExecDestroy(s.graph);
     structured_free(s);
+    mixed_free(s);
     HamDev &h = s.ham;
     void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
@@ -366,13 +373,19 @@ void destroy(Sim &s) {
 }
 
 int one_step(Sim &s, int64_t off, int phase = 3) {
-    return s.precision >= 1 ? structured_step(s, off, phase) : llg_generic_step(s, off, phase);
+    if (structured(s)) return structured_step(s, off, phase);
+    return s.precision == 3 ? mixed_step(s, off, phase) : llg_generic_step(s, off, phase);
 }
 
 int run_steps(Sim &s, int64_t n) {
     const int G = 16;
     int rc;
-    square_mirror_stale(s);
+    if (s.precision == 3) {
+        s.sqm_valid = 0;  // the mixed steps keep their own mirror current
+        if ((rc = mixed_ready(s))) return rc;
+    } else {
+        square_mirror_stale(s);
+    }
     if (!s.graph && n >= G) {
         cudaGraph_t g;
         UPPASD_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
@@ -488,7 +501,7 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
         uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
         return UPPASD_GPU_ECUDA;
     }
-    if (s.precision >= 1) return uppasd::structured_load_state(s);
+    if (uppasd::structured(s)) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;
 }
 
@@ -499,7 +512,7 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
     }
     Sim &s = w->s;
     int rc;
-    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     double *d = nullptr;
     UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
@@ -538,7 +551,7 @@ int uppasd_gpu_set_perp(uppasd_gpu_sim *w, int32_t perp) {
     }
     Sim &s = w->s;
     if (perp && s.precision >= 1) {
-        uppasd::set_error("set_perp: the structured path (precision >= 1) has no field projection; use precision 0");
+        uppasd::set_error("set_perp: only the FP64 path (precision 0) has the field projection");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     uppasd::drop_graph(s);  // the step arguments are captured by value
@@ -561,8 +574,8 @@ int uppasd_gpu_set_jtensor(uppasd_gpu_sim *w, const double *j_tens) {
     if (!w) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     uppasd::HamDev &h = s.ham;
-    if (s.precision >= 1) {
-        uppasd::set_error("set_jtensor: the structured path (precision >= 1) covers scalar exchange; use precision 0");
+    if (uppasd::structured(s)) {
+        uppasd::set_error("set_jtensor: the structured path (precision 1, 2) covers scalar exchange; use precision 0 or 3");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     std::vector<double> jt;
@@ -642,7 +655,7 @@ int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {
     if (!w || !beff) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     return uppasd::field_to_host(s, beff);
 }
 
@@ -653,10 +666,10 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t 
     }
     Sim &s = w->s;
     int rc;
-    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     rc = uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
     if (rc) return rc;
-    if (s.precision >= 1) return uppasd::structured_load_state(s);
+    if (uppasd::structured(s)) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;
 }
 
@@ -681,7 +694,12 @@ int uppasd_gpu_time_kernels(uppasd_gpu_sim *w, int32_t nrep, double *ms) {
     for (auto &e : ev) UPPASD_CUDA_TRY(cudaEventCreate(&e));
     double acc[3] = {0.0, 0.0, 0.0};
     int rc = UPPASD_GPU_OK;
-    uppasd::square_mirror_stale(s);
+    if (s.precision == 3) {
+        s.sqm_valid = 0;
+        if ((rc = uppasd::mixed_ready(s))) return rc;
+    } else {
+        uppasd::square_mirror_stale(s);
+    }
     for (int r = 0; r < nrep && rc == UPPASD_GPU_OK; ++r) {
         cudaEventRecord(ev[0], s.stream);
         rc = uppasd::one_step(s, 0, 1);
@@ -712,7 +730,7 @@ int uppasd_gpu_observables(uppasd_gpu_sim *w, double *mvec, double *mabs, double
     if (!w) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     return uppasd::observables(s, mvec, mabs, energy, nullptr);
 }
 
@@ -720,7 +738,7 @@ int uppasd_gpu_energy_terms(uppasd_gpu_sim *w, double *terms) {
     if (!w || !terms) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (s.precision >= 1 && (rc = uppasd::structured_sync_state(s))) return rc;
+    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     return uppasd::observables(s, nullptr, nullptr, nullptr, nullptr, terms);
 }
 

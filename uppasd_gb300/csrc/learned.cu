@@ -1235,6 +1235,7 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     if (e == cudaSuccess) e = cudaMemsetAsync(p->dE_sum, 0, sizeof(double), st);
     if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
     const double beta_mub = kMub / (kKbolt * temperature);
+    s.mix.valid = 0;  // the precision-3 LLG mirror does not follow the learned moves
     if (s.sq.L == p->L) {
         // learned moves on the square lattice read and write the FP32 mirror as well
         if ((rc = square_mirror_ready(s))) return rc;

@@ -210,10 +210,11 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = w->s;
-    if (s.precision >= 1) {
-        set_error("mc_run_square: needs the FP64 state path (precision 0)");
+    if (structured(s)) {
+        set_error("mc_run_square: needs the FP64 state (precision 0 or 3)");
         return UPPASD_GPU_EUNSUPPORTED;
     }
+    s.mix.valid = 0;  // the precision-3 LLG mirror does not follow these updates
     if (s.sq.L != L) {
         const int rc = square_recognise(s, L);
         if (rc) return rc;

@@ -59,6 +59,15 @@ struct LlgDev {
 
 struct StructuredFast;  // mixed-precision structured-lattice path (llg_stencil.cu)
 
+// precision 3 (llg_mixed.cu): FP32 gather over the caller's neighbour lists with
+// the FP64 state e / eM as master.  mt mirrors e (unit vector, w = moment), mp is
+// the predictor, b2 the Depondt predictor's damped field.
+struct MixedDev {
+    float4 *mt = nullptr, *mp = nullptr;
+    float *b2x = nullptr, *b2y = nullptr, *b2z = nullptr;
+    int valid = 0;  // mt equals e / mmom
+};
+
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
 // (mc_square.cu): per neighbour direction (+x, -x, +y, -y) the exchange field per
 // unit neighbour and the DMI vector, uniform moment and Zeeman field.
@@ -96,6 +105,7 @@ struct Sim {
     // every update to both it and e / eM; any other writer of e marks it stale.
     float4 *sqm = nullptr;
     int sqm_valid = 0;
+    MixedDev mix;
     // scratch for observables
     double *red = nullptr;             // [mensemble][8]
     size_t bytes_allocated = 0;
@@ -124,7 +134,13 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
 // mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
 int square_recognise(Sim &s, int L);
 int square_mirror_ready(Sim &s);  // builds the FP32 mirror from e when it is stale
-inline void square_mirror_stale(Sim &s) { s.sqm_valid = 0; }
+// every FP32 mirror of e is stale (a writer of e other than the mirror's own users)
+inline void square_mirror_stale(Sim &s) {
+    s.sqm_valid = 0;
+    s.mix.valid = 0;
+}
+// precision 1 / 2: the structured bcc path owns the state between sync points
+inline bool structured(const Sim &s) { return s.precision == 1 || s.precision == 2; }
 
 void set_error(const std::string &msg);
 
