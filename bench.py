@@ -56,6 +56,11 @@ WORKLOADS = {
     "square256": dict(kind="square", L=256, ens=1, solver=1, dt=1e-16, damping=0.05, temp=50.0,
                       desc="square monolayer 256^2, J=1.0, interfacial D=0.3, Kz=-0.05 mRy, Bz=0.5 T, midpoint, "
                            "T=50 K"),
+    # the square DMI Hamiltonian at a size where the GPU is filled: the general-Hamiltonian
+    # variant line (FP64 path against the FP32-gather / FP64-master path)
+    "square1024x4": dict(kind="square", L=1024, ens=4, solver=1, dt=1e-16, damping=0.05, temp=50.0,
+                         desc="square monolayer 1024^2 x 4 ensembles, J=1.0, interfacial D=0.3, Kz=-0.05 mRy, "
+                              "Bz=0.5 T, midpoint, T=50 K"),
 }
 
 
@@ -630,7 +635,7 @@ def run_gb300(args, w):
     e2e_val = nspin * inner * max(1, args.e2e_rounds) * world / e2e_s
     sim.close()
     variants = {}
-    if args.variants and prec == 1:
+    if not args.no_variants and prec == 1:
         try:
             alt = _make_sim(lat, w, 2, 1000 + rank, e0)
             alt.set_stream(stream.cuda_stream)
@@ -642,6 +647,22 @@ def run_gb300(args, w):
                 "kernel_ms": kt2, "roofline": _roofline(kt2, nspin, 8, ms2 / args.steps, peak, peak_kind, None)}
         except Exception as exc:
             variants["double_single_master"] = {"error": str(exc)}
+        # general Hamiltonians (neighbour lists, DMI, anisotropy): FP64 path and FP32 gather
+        # with the FP64 state as master, on the same lattice
+        try:
+            wg = WORKLOADS["square1024x4"]
+            lg = build_lattice(wg)
+            eg = random_state(lg.mensemble, lg.natom, seed=11 + rank)
+            gen = {"workload": "square1024x4", "description": wg["desc"], "spins": lg.natom * lg.mensemble}
+            for pg, key in ((0, "fp64"), (3, "fp32_gather_fp64_master")):
+                sg = _make_sim(lg, wg, pg, 3000 + rank, eg)
+                sg.set_stream(stream.cuda_stream)
+                msg = _time_steps(sg, stream, 16, 4, world)
+                sg.close()
+                gen[key] = {"ms_per_step": msg / 16, "value": lg.natom * lg.mensemble * 16 * world / (msg * 1e-3)}
+            variants["general_hamiltonian"] = gen
+        except Exception as exc:
+            variants["general_hamiltonian"] = {"error": str(exc)}
     mc = None
     if not args.no_mc:
         mc = run_mc(args, world, rank, peak, peak_kind)
@@ -691,7 +712,8 @@ def main():
     ap.add_argument("--e2e-inner", type=int, default=10)
     ap.add_argument("--e2e-rounds", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--variants", action="store_true", help="also time the double-single master variant")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the double-single master and general-Hamiltonian variant timings")
     ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
     ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
