@@ -24,7 +24,13 @@ namespace {
 struct MixArgs {
     HamDev h;
     const double *lambda, *temp, *landeg, *mmom;
-    double delta_t, bn, temprescale;
+    // per-step constants, computed once on the host (per-site FP64 divisions and square
+    // roots would cost more than the whole FP32 step on GB300's FP64 pipe)
+    float dt_dep;   // delta_t gama: Depondt rotation angle per |B| is dt_dep / (1 + lambda^2)
+    float dt_mid;   // delta_t bn gama: midpoint dt = dt_mid / (1 + lambda^2)
+    float c_dp;     // 2 kB / (delta_t gama muB): Depondt D = c_dp lambda
+    float c_dk;     // kB / (muB bn): midpoint D = c_dk lambda / (1 + lambda^2)
+    float temprescale;
     int noise_on;
     NoiseArgs nz;          // Philox (FP32 Box-Muller here), injected normals, or none
     const int64_t *d_step;
@@ -160,13 +166,12 @@ __device__ __forceinline__ void noise_f32(const MixArgs &a, int i, int k, int64_
         z[1] = (float)zd[1];
         z[2] = (float)zd[2];
     }
+    const float T = (float)a.temp[i] * a.temprescale;
     float sigma;
     if (ALG == 5) {
-        const double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
-        sigma = sqrtf((float)(Dp * a.temprescale * a.temp[i]) / mm);
+        sigma = sqrtf(a.c_dp * lam * T / mm);
     } else {
-        const double Dk = (((lam / (1.0 + (double)lam * lam)) * kKbolt) / kGama / kMub) * (kGama / a.bn);
-        sigma = sqrtf(2.0f * (float)(Dk * a.temp[i] * a.temprescale) / mm);
+        sigma = sqrtf(2.0f * (a.c_dk * lam / (1.0f + lam * lam)) * T / mm);
     }
     out[0] = z[0] * sigma;
     out[1] = z[1] * sigma;
@@ -194,7 +199,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         const float bd[3] = {bl[0] + lam * (e[1] * bl[2] - e[2] * bl[1]), bl[1] + lam * (e[2] * bl[0] - e[0] * bl[2]),
                              bl[2] + lam * (e[0] * bl[1] - e[1] * bl[0])};
         float d[3];
-        rotation_delta_f32(bd, e, (float)(a.delta_t * kGama / (1.0 + (double)lam * lam)), d);
+        rotation_delta_f32(bd, e, a.dt_dep / (1.0f + lam * lam), d);
         p[0] = e[0] + d[0];
         p[1] = e[1] + d[1];
         p[2] = e[2] + d[2];
@@ -202,9 +207,9 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         a.b2y[o] = bd[1];
         a.b2z[o] = bd[2];
     } else {
-        const double dt = a.delta_t * a.bn * kGama / (1.0 + (double)lam * lam);
+        const float dt = a.dt_mid / (1.0f + lam * lam);
         const float g = (float)a.landeg[i];
-        const float dtg = (float)dt * g, sqrtdtg = (float)sqrt(dt) * g;
+        const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
         float A[3], et[3];
         midpoint_A_f32(lam, dtg, sqrtdtg, e, B, r, A);
         cayley_f32(A, e, et);
@@ -238,11 +243,11 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         bd[0] = 0.5f * bd[0] + 0.5f * a.b2x[o];
         bd[1] = 0.5f * bd[1] + 0.5f * a.b2y[o];
         bd[2] = 0.5f * bd[2] + 0.5f * a.b2z[o];
-        rotation_delta_f32(bd, e, (float)(a.delta_t * kGama / (1.0 + (double)lam * lam)), d);
+        rotation_delta_f32(bd, e, a.dt_dep / (1.0f + lam * lam), d);
     } else {
-        const double dt = a.delta_t * a.bn * kGama / (1.0 + (double)lam * lam);
+        const float dt = a.dt_mid / (1.0f + lam * lam);
         const float g = (float)a.landeg[i];
-        const float dtg = (float)dt * g, sqrtdtg = (float)sqrt(dt) * g;
+        const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
         float A[3], et[3];
         midpoint_A_f32(lam, dtg, sqrtdtg, pr, B, r, A);
         cayley_f32(A, e, et);
@@ -317,9 +322,11 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     a.temp = s.llg.temp;
     a.landeg = s.llg.landeg;
     a.mmom = s.llg.mmom;
-    a.delta_t = s.llg.delta_t;
-    a.bn = s.llg.bn;
-    a.temprescale = s.llg.temprescale;
+    a.dt_dep = (float)(s.llg.delta_t * kGama);
+    a.dt_mid = (float)(s.llg.delta_t * s.llg.bn * kGama);
+    a.c_dp = (float)(2.0 * kKbolt / (s.llg.delta_t * kGama * kMub));
+    a.c_dk = (float)(kKbolt / (kMub * s.llg.bn));
+    a.temprescale = (float)s.llg.temprescale;
     a.noise_on = s.llg.noise_on;
     a.nz.mode = s.llg.noise_mode;
     a.nz.seed = s.llg.seed;
