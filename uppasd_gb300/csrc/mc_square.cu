@@ -8,9 +8,8 @@
 // nlist/ncoup/dmlist/dm_vect, and the heat-bath draw (flip_h,
 // MonteCarlo/montecarlo_common.f90:371-422) runs in FP32 on the FP64 spin state.
 // Neighbours are read from an FP32 mirror of the state (the values the draw uses
-// anyway), and every new spin is written to the mirror and to e / eM: on GB300
-// the double-to-float conversions of the neighbours, which run on the FP64 pipe,
-// would otherwise set the sweep's time.
+// anyway), and every new spin is written to the mirror and to e / eM: four 16-byte
+// loads per site instead of twelve 8-byte loads and conversions from e.
 // The chain is the checkerboard chain of mc.cu (colours x + y even, then odd)
 // with the same Philox counters (site, ensemble, sweep), so it agrees with the
 // FP64 path to FP32 rounding.
