@@ -63,7 +63,8 @@ typedef struct {
                                             spin master and renormalisation (same scope);
                                           3 FP32 field gather over any neighbour list (scalar
                                             or tensor exchange, DMI, anisotropy, Zeeman) + FP64
-                                            spin master and renormalisation (Depondt, midpoint) */
+                                            spin master and renormalisation (Depondt, midpoint);
+                                            mc_run 'H' draws in FP32 on the same mirror */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;

@@ -126,3 +126,32 @@ def test_scope():
         _lib.call("uppasd_gpu_set_perp", sim._h, 1)
     assert ex.value.rc == -7
     sim.close()
+
+
+@pytest.mark.parametrize("kind", ["kagome_tensor", "square_dmi_aniso"])
+def test_heat_bath_chain_against_oracle(kind):
+    """mc_run 'H' at precision 3: the FP64 path's checkerboard chain (same colouring,
+    same Philox draws) with the field and the draw in FP32, per spin within 2e-4
+    after 3 sweeps; Metropolis stays on the FP64 path."""
+    lat = (lattice.kagome(12, -1.0, 0.1, 0.05, 1.0, 0.2) if kind == "kagome_tensor"
+           else lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0)).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(46), (2, lat.natom, 3))
+    T = 30.0
+    sim = GpuSimulation(lat, emom=e0, seed=61, precision=3, sdealgh=5)
+    sim.relax("H", T, 3)
+    g = sim.get_moments()
+    sim.relax("M", T, 2)  # FP64 Metropolis on the same state
+    gm = sim.get_moments()
+    sim.close()
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    _, order, start = lattice.greedy_colouring(lat)
+    for sw in range(3):
+        o.mc_sweep_checkerboard("H", T, order, start, 61, sw)
+    assert np.max(np.abs(g - o.emom)) < 2e-4
+    ref = GpuSimulation(lat, emom=g, seed=61, precision=0)
+    ref.relax("H", T, 3)  # advances the sweep counter to 3
+    ref.put_moments(g)
+    ref.relax("M", T, 2)
+    assert np.array_equal(ref.get_moments(), gm)
+    ref.close()

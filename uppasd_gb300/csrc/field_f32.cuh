@@ -1,0 +1,107 @@
+// field_f32.cuh -- FP32 building blocks shared by the FP32-gather paths
+// (precision 3 LLG and heat bath, the structured square heat bath):
+//   field_f32      effective field of one site from an FP32 float4 mirror (unit
+//                  vector, moment in w), same terms and order as the FP64 field
+//                  (Hamiltonian/hamiltonianactions.f90:187-243)
+//   heat_bath_f32  flip_h (MonteCarlo/montecarlo_common.f90:371-422) in FP32, with
+//                  the field frame built from the field's own components
+#pragma once
+#include "common.cuh"
+#include "sim.h"
+
+namespace uppasd {
+
+// FP32 effective field of site i from full moments m.w * m.xyz, in the FP64 field's
+// term order (exchange or tensor, DMI, anisotropy, Zeeman).
+__device__ __forceinline__ void field_f32(const HamDev &h, const float4 *m, int i, int k, float B[3]) {
+    const int N = h.natom;
+    const size_t off = (size_t)k * N;
+    const int ih = h.aham[i];
+    const int nn = h.nsize[i];
+    float bs[3] = {0.f, 0.f, 0.f}, bq[3] = {0.f, 0.f, 0.f};
+    if (h.do_jtensor) {
+        for (int s = 0; s < nn; ++s) {
+            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const float4 v = m[off + j];
+            const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
+            const double *J = h.jt + ((size_t)s * h.nham + ih) * 9;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                bs[a] += (float)__ldg(&J[3 * a]) * m1 + (float)__ldg(&J[3 * a + 1]) * m2 +
+                         (float)__ldg(&J[3 * a + 2]) * m3;
+        }
+    } else {
+        for (int s = 0; s < nn; ++s) {
+            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const float4 v = m[off + j];
+            const float c = (float)__ldg(&h.ncoup[(size_t)s * h.nham + ih]) * v.w;
+            bs[0] = fmaf(c, v.x, bs[0]);
+            bs[1] = fmaf(c, v.y, bs[1]);
+            bs[2] = fmaf(c, v.z, bs[2]);
+        }
+    }
+    if (h.do_dm) {
+        const int nd = h.dmsize[i];
+        for (int s = 0; s < nd; ++s) {
+            const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
+            const size_t d = (size_t)s * h.nham + ih;
+            const float d0 = (float)h.dmx[d], d1 = (float)h.dmy[d], d2 = (float)h.dmz[d];
+            const float4 v = m[off + j];
+            const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
+            bs[0] += d2 * m2 - d1 * m3;
+            bs[1] += d0 * m3 - d2 * m1;
+            bs[2] += d1 * m1 - d0 * m2;
+        }
+    }
+    if (h.do_aniso) {
+        const float4 me = m[off + i];
+        const float m1 = me.w * me.x, m2 = me.w * me.y, m3 = me.w * me.z;
+        const int ta = h.taniso[i];
+        const float e0 = (float)h.eax[i], e1 = (float)h.eay[i], e2 = (float)h.eaz[i];
+        const float ka0 = (float)h.k1[i], ka1 = (float)h.k2[i];
+        if (ta == 1 || ta == 7) {
+            const float tt1 = m1 * e0 + m2 * e1 + m3 * e2;
+            const float tt3 = 2.0f * tt1 * (ka0 + 2.0f * ka1 * (1.0f - tt1 * tt1));
+            bs[0] -= tt3 * e0;
+            bs[1] -= tt3 * e1;
+            bs[2] -= tt3 * e2;
+        }
+        if (ta == 2 || ta == 7) {
+            const float t0 = 2.0f * ka0 * m1 * (m2 * m2 + m3 * m3) + 2.0f * ka1 * m1 * (m2 * m2 * (m3 * m3));
+            const float t1 = 2.0f * ka0 * m2 * (m3 * m3 + m1 * m1) + 2.0f * ka1 * m2 * (m3 * m3 * (m1 * m1));
+            const float t2 = 2.0f * ka0 * m3 * (m1 * m1 + m2 * m2) + 2.0f * ka1 * m3 * (m1 * m1 * (m2 * m2));
+            const float sc = ta == 2 ? 1.0f : (float)h.sb[i];
+            float *dst = ta == 2 ? bs : bq;
+            dst[0] += t0 * sc;
+            dst[1] += t1 * sc;
+            dst[2] += t2 * sc;
+        }
+    }
+    B[0] = bs[0] + (bq[0] + (float)h.ext.x[off + i]);
+    B[1] = bs[1] + (bq[1] + (float)h.ext.y[off + i]);
+    B[2] = bs[2] + (bq[2] + (float)h.ext.z[off + i]);
+}
+
+// flip_h in FP32: x = beta_mu |h|; 1 - cos(theta) = -ln((1 - e^-2x) q + e^-2x + tol) / x
+// formed directly, and the frame from (zx, zy) so it stays orthonormal in FP32.
+__device__ __forceinline__ float3 heat_bath_f32(float3 h, float beta_mu, float q, float fp) {
+    const float zx = beta_mu * h.x, zy = beta_mu * h.y, zz = beta_mu * h.z;
+    const float rxy = sqrtf(zx * zx + zy * zy);
+    const float zarg = sqrtf(fmaf(rxy, rxy, zz * zz));
+    const float izarg = 1.0f / zarg;
+    const float zct = zz * izarg, zst = rxy * izarg;
+    const float zcp = rxy > 0.0f ? zx / rxy : 1.0f, zsp = rxy > 0.0f ? zy / rxy : 0.0f;
+    const float e2 = __expf(-2.0f * zarg);
+    const float omc = fminf(2.0f, fmaxf(0.0f, -__logf(fmaf(1.0f - e2, q, e2) + 1e-14f) * izarg));
+    const float ct = 1.0f - omc, st = sqrtf(omc * (2.0f - omc));
+    float sp, cp;
+    __sincosf(3.14159265358979f * (2.0f * fp - 1.0f), &sp, &cp);
+    const float s0 = st * cp, s1 = st * sp;
+    const float nx = zcp * zct * s0 - zsp * s1 + zcp * zst * ct;
+    const float ny = zsp * zct * s0 + zcp * s1 + zsp * zst * ct;
+    const float nz = -zst * s0 + zct * ct;
+    const float il = rsqrtf(nx * nx + ny * ny + nz * nz);
+    return make_float3(nx * il, ny * il, nz * il);
+}
+
+}  // namespace uppasd

@@ -14,6 +14,7 @@
 // The noise is the FP64 path's Philox stream (site, ensemble, step), drawn with the
 // FP32 Box-Muller of the structured path.
 #include "common.cuh"
+#include "field_f32.cuh"
 #include "field_fp64.cuh"
 #include "sim.h"
 
@@ -39,77 +40,6 @@ struct MixArgs {
     float4 *mt, *mp;       // mirror at t, predictor
     float *b2x, *b2y, *b2z;
 };
-
-// FP32 effective field of site i from full moments m.w * m.xyz, in the FP64 field's
-// term order (exchange or tensor, DMI, anisotropy, Zeeman).
-__device__ __forceinline__ void field_f32(const HamDev &h, const float4 *m, int i, int k, float B[3]) {
-    const int N = h.natom;
-    const size_t off = (size_t)k * N;
-    const int ih = h.aham[i];
-    const int nn = h.nsize[i];
-    float bs[3] = {0.f, 0.f, 0.f}, bq[3] = {0.f, 0.f, 0.f};
-    if (h.do_jtensor) {
-        for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
-            const float4 v = m[off + j];
-            const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            const double *J = h.jt + ((size_t)s * h.nham + ih) * 9;
-#pragma unroll
-            for (int a = 0; a < 3; ++a)
-                bs[a] += (float)__ldg(&J[3 * a]) * m1 + (float)__ldg(&J[3 * a + 1]) * m2 +
-                         (float)__ldg(&J[3 * a + 2]) * m3;
-        }
-    } else {
-        for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
-            const float4 v = m[off + j];
-            const float c = (float)__ldg(&h.ncoup[(size_t)s * h.nham + ih]) * v.w;
-            bs[0] = fmaf(c, v.x, bs[0]);
-            bs[1] = fmaf(c, v.y, bs[1]);
-            bs[2] = fmaf(c, v.z, bs[2]);
-        }
-    }
-    if (h.do_dm) {
-        const int nd = h.dmsize[i];
-        for (int s = 0; s < nd; ++s) {
-            const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
-            const size_t d = (size_t)s * h.nham + ih;
-            const float d0 = (float)h.dmx[d], d1 = (float)h.dmy[d], d2 = (float)h.dmz[d];
-            const float4 v = m[off + j];
-            const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            bs[0] += d2 * m2 - d1 * m3;
-            bs[1] += d0 * m3 - d2 * m1;
-            bs[2] += d1 * m1 - d0 * m2;
-        }
-    }
-    if (h.do_aniso) {
-        const float4 me = m[off + i];
-        const float m1 = me.w * me.x, m2 = me.w * me.y, m3 = me.w * me.z;
-        const int ta = h.taniso[i];
-        const float e0 = (float)h.eax[i], e1 = (float)h.eay[i], e2 = (float)h.eaz[i];
-        const float ka0 = (float)h.k1[i], ka1 = (float)h.k2[i];
-        if (ta == 1 || ta == 7) {
-            const float tt1 = m1 * e0 + m2 * e1 + m3 * e2;
-            const float tt3 = 2.0f * tt1 * (ka0 + 2.0f * ka1 * (1.0f - tt1 * tt1));
-            bs[0] -= tt3 * e0;
-            bs[1] -= tt3 * e1;
-            bs[2] -= tt3 * e2;
-        }
-        if (ta == 2 || ta == 7) {
-            const float t0 = 2.0f * ka0 * m1 * (m2 * m2 + m3 * m3) + 2.0f * ka1 * m1 * (m2 * m2 * (m3 * m3));
-            const float t1 = 2.0f * ka0 * m2 * (m3 * m3 + m1 * m1) + 2.0f * ka1 * m2 * (m3 * m3 * (m1 * m1));
-            const float t2 = 2.0f * ka0 * m3 * (m1 * m1 + m2 * m2) + 2.0f * ka1 * m3 * (m1 * m1 * (m2 * m2));
-            const float sc = ta == 2 ? 1.0f : (float)h.sb[i];
-            float *dst = ta == 2 ? bs : bq;
-            dst[0] += t0 * sc;
-            dst[1] += t1 * sc;
-            dst[2] += t2 * sc;
-        }
-    }
-    B[0] = bs[0] + (bq[0] + (float)h.ext.x[off + i]);
-    B[1] = bs[1] + (bq[1] + (float)h.ext.y[off + i]);
-    B[2] = bs[2] + (bq[2] + (float)h.ext.z[off + i]);
-}
 
 // Rodrigues rotation increment R e - e about h = bd/|bd| by v = |bd| dtg.
 __device__ __forceinline__ void rotation_delta_f32(const float bd[3], const float e[3], float dtg, float d[3]) {
@@ -272,6 +202,36 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     a.mt[o] = make_float4((float)e0, (float)e1, (float)e2, mm);
 }
 
+// Heat bath of one colour (flip_h, MonteCarlo/montecarlo_common.f90:371-422) on the
+// FP32 mirror: the field over the caller's neighbour lists, the draw in FP32 with the
+// FP64 path's Philox counters (site, ensemble, sweep), the new spin written to the
+// mirror and to e / eM.  Same checkerboard chain as mc_colour_kernel.
+__global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, float4 *mt, Vec3D e, Vec3D eM, const double *mmom,
+                                                       const int32_t *sites, int nsites, float beta_mub,
+                                                       uint64_t seed, int64_t sweep) {
+    const int N = h.natom;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nsites * h.mensemble) return;
+    const int k = (int)(t / nsites);
+    const int i = sites[t - (int64_t)k * nsites];
+    const size_t o = (size_t)k * N + i;
+    float B[3];
+    field_f32(h, mt, i, k, B);
+    const float mm = mt[o].w;
+    const Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
+    const float k32 = 2.3283064365386963e-10f;
+    const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
+    const float3 n = heat_bath_f32(make_float3(B[0], B[1], B[2]), beta_mub * mm, q, fp);
+    mt[o] = make_float4(n.x, n.y, n.z, mm);
+    const double md = mmom[o];
+    e.x[o] = n.x;
+    e.y[o] = n.y;
+    e.z[o] = n.z;
+    eM.x[o] = md * n.x;
+    eM.y[o] = md * n.y;
+    eM.z[o] = md * n.z;
+}
+
 __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) mt[t] = make_float4((float)e.x[t], (float)e.y[t], (float)e.z[t], (float)mmom[t]);
@@ -312,6 +272,30 @@ int mixed_ready(Sim &s) {
     mixed_mirror<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.e, s.llg.mmom, s.mix.mt, n);
     UPPASD_CUDA_TRY(cudaGetLastError());
     s.mix.valid = 1;
+    return UPPASD_GPU_OK;
+}
+
+// precision 3 heat-bath sweeps (mc_run mode 'H')
+int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps) {
+    if (s.ncolour <= 0) {
+        set_error("no colouring available for Monte Carlo");
+        return UPPASD_GPU_ESTATE;
+    }
+    int rc = mixed_ready(s);
+    if (rc) return rc;
+    s.sqm_valid = 0;  // the square path's mirror does not follow these updates
+    const float beta_mub = (float)(kMub / (kKbolt * temperature));
+    for (int64_t sw = 0; sw < nsweeps; ++sw) {
+        for (int c = 0; c < s.ncolour; ++c) {
+            const int beg = s.colour_start_h[c], n = s.colour_start_h[c + 1] - beg;
+            if (n == 0) continue;
+            const int64_t tot = (int64_t)n * s.ham.mensemble;
+            mixed_heat_bath<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
+                s.ham, s.mix.mt, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, s.llg.seed, s.mc_sweep);
+        }
+        s.mc_sweep += 1;
+    }
+    UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }
 

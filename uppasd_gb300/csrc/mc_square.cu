@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "field_f32.cuh"
 #include "sim.h"
 
 namespace uppasd {
@@ -29,26 +30,6 @@ struct SqArgs {
     uint64_t seed;
     long long sweep;
 };
-
-__device__ __forceinline__ float3 heat_bath_f32(float3 h, float beta_mu, float q, float fp) {
-    const float zx = beta_mu * h.x, zy = beta_mu * h.y, zz = beta_mu * h.z;
-    const float rxy = sqrtf(zx * zx + zy * zy);
-    const float zarg = sqrtf(fmaf(rxy, rxy, zz * zz));
-    const float izarg = 1.0f / zarg;
-    const float zct = zz * izarg, zst = rxy * izarg;
-    const float zcp = rxy > 0.0f ? zx / rxy : 1.0f, zsp = rxy > 0.0f ? zy / rxy : 0.0f;
-    const float e2 = __expf(-2.0f * zarg);
-    const float omc = fminf(2.0f, fmaxf(0.0f, -__logf(fmaf(1.0f - e2, q, e2) + 1e-14f) * izarg));
-    const float ct = 1.0f - omc, st = sqrtf(omc * (2.0f - omc));
-    float sp, cp;
-    __sincosf(3.14159265358979f * (2.0f * fp - 1.0f), &sp, &cp);
-    const float s0 = st * cp, s1 = st * sp;
-    const float nx = zcp * zct * s0 - zsp * s1 + zcp * zst * ct;
-    const float ny = zsp * zct * s0 + zcp * s1 + zsp * zst * ct;
-    const float nz = -zst * s0 + zct * ct;
-    const float il = rsqrtf(nx * nx + ny * ny + nz * nz);
-    return make_float3(nx * il, ny * il, nz * il);
-}
 
 __global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e, Vec3D eM) {
     const int half = a.L >> 1;
