@@ -33,6 +33,7 @@ void mixed_free(Sim &s);
 int mixed_ready(Sim &s);
 int mixed_step(Sim &s, int64_t step_offset, int phase);
 int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps);
+int mixed_coefficients(Sim &s);
 
 namespace {
 
@@ -602,11 +603,12 @@ int uppasd_gpu_set_jtensor(uppasd_gpu_sim *w, const double *j_tens) {
     h.jt = nullptr;
     h.do_jtensor = 0;
     s.sq.L = 0;  // the structured square recognition no longer holds
-    if (!j_tens) return UPPASD_GPU_OK;
+    if (!j_tens) return s.precision == 3 ? uppasd::mixed_coefficients(s) : UPPASD_GPU_OK;
     int rc = uppasd::upload(s, &h.jt, jt);
     if (rc) return rc;
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
     h.do_jtensor = 1;
+    if (s.precision == 3) return uppasd::mixed_coefficients(s);
     return UPPASD_GPU_OK;
 }
 

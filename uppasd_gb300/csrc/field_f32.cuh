@@ -1,8 +1,8 @@
 // field_f32.cuh -- FP32 building blocks shared by the FP32-gather paths
 // (precision 3 LLG and heat bath, the structured square heat bath):
 //   field_f32      effective field of one site from an FP32 float4 mirror (unit
-//                  vector, moment in w), same terms and order as the FP64 field
-//                  (Hamiltonian/hamiltonianactions.f90:187-243)
+//                  vector, moment in w) and FP32 copies of the couplings, same terms
+//                  and order as the FP64 field (Hamiltonian/hamiltonianactions.f90:187-243)
 //   heat_bath_f32  flip_h (MonteCarlo/montecarlo_common.f90:371-422) in FP32, with
 //                  the field frame built from the field's own components
 #pragma once
@@ -12,8 +12,10 @@
 namespace uppasd {
 
 // FP32 effective field of site i from full moments m.w * m.xyz, in the FP64 field's
-// term order (exchange or tensor, DMI, anisotropy, Zeeman).
-__device__ __forceinline__ void field_f32(const HamDev &h, const float4 *m, int i, int k, float B[3]) {
+// term order (exchange or tensor, DMI, anisotropy, Zeeman), with the couplings from
+// the FP32 copies in MixedDev.
+__device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, const float4 *m, int i, int k,
+                                          float B[3]) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
     const int ih = h.aham[i];
@@ -24,41 +26,40 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const float4 *m, int 
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            const double *J = h.jt + ((size_t)s * h.nham + ih) * 9;
+            const float *J = c.jt + ((size_t)s * h.nham + ih) * 9;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                bs[a] += (float)__ldg(&J[3 * a]) * m1 + (float)__ldg(&J[3 * a + 1]) * m2 +
-                         (float)__ldg(&J[3 * a + 2]) * m3;
+                bs[a] += __ldg(&J[3 * a]) * m1 + __ldg(&J[3 * a + 1]) * m2 + __ldg(&J[3 * a + 2]) * m3;
         }
     } else {
         for (int s = 0; s < nn; ++s) {
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
-            const float c = (float)__ldg(&h.ncoup[(size_t)s * h.nham + ih]) * v.w;
-            bs[0] = fmaf(c, v.x, bs[0]);
-            bs[1] = fmaf(c, v.y, bs[1]);
-            bs[2] = fmaf(c, v.z, bs[2]);
+            const float cj = __ldg(&c.nc[(size_t)s * h.nham + ih]) * v.w;
+            bs[0] = fmaf(cj, v.x, bs[0]);
+            bs[1] = fmaf(cj, v.y, bs[1]);
+            bs[2] = fmaf(cj, v.z, bs[2]);
         }
     }
     if (h.do_dm) {
         const int nd = h.dmsize[i];
         for (int s = 0; s < nd; ++s) {
             const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
-            const size_t d = (size_t)s * h.nham + ih;
-            const float d0 = (float)h.dmx[d], d1 = (float)h.dmy[d], d2 = (float)h.dmz[d];
+            const float4 d = __ldg(&c.dm[(size_t)s * h.nham + ih]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            bs[0] += d2 * m2 - d1 * m3;
-            bs[1] += d0 * m3 - d2 * m1;
-            bs[2] += d1 * m1 - d0 * m2;
+            bs[0] += d.z * m2 - d.y * m3;
+            bs[1] += d.x * m3 - d.z * m1;
+            bs[2] += d.y * m1 - d.x * m2;
         }
     }
     if (h.do_aniso) {
         const float4 me = m[off + i];
         const float m1 = me.w * me.x, m2 = me.w * me.y, m3 = me.w * me.z;
         const int ta = h.taniso[i];
-        const float e0 = (float)h.eax[i], e1 = (float)h.eay[i], e2 = (float)h.eaz[i];
-        const float ka0 = (float)h.k1[i], ka1 = (float)h.k2[i];
+        const float4 an = __ldg(&c.an[i]);
+        const float2 an2 = __ldg(&c.an2[i]);
+        const float e0 = an.x, e1 = an.y, e2 = an.z, ka0 = an.w, ka1 = an2.x;
         if (ta == 1 || ta == 7) {
             const float tt1 = m1 * e0 + m2 * e1 + m3 * e2;
             const float tt3 = 2.0f * tt1 * (ka0 + 2.0f * ka1 * (1.0f - tt1 * tt1));
@@ -70,16 +71,17 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const float4 *m, int 
             const float t0 = 2.0f * ka0 * m1 * (m2 * m2 + m3 * m3) + 2.0f * ka1 * m1 * (m2 * m2 * (m3 * m3));
             const float t1 = 2.0f * ka0 * m2 * (m3 * m3 + m1 * m1) + 2.0f * ka1 * m2 * (m3 * m3 * (m1 * m1));
             const float t2 = 2.0f * ka0 * m3 * (m1 * m1 + m2 * m2) + 2.0f * ka1 * m3 * (m1 * m1 * (m2 * m2));
-            const float sc = ta == 2 ? 1.0f : (float)h.sb[i];
+            const float sc = ta == 2 ? 1.0f : an2.y;
             float *dst = ta == 2 ? bs : bq;
             dst[0] += t0 * sc;
             dst[1] += t1 * sc;
             dst[2] += t2 * sc;
         }
     }
-    B[0] = bs[0] + (bq[0] + (float)h.ext.x[off + i]);
-    B[1] = bs[1] + (bq[1] + (float)h.ext.y[off + i]);
-    B[2] = bs[2] + (bq[2] + (float)h.ext.z[off + i]);
+    const float4 ex = __ldg(&c.ext[off + i]);
+    B[0] = bs[0] + (bq[0] + ex.x);
+    B[1] = bs[1] + (bq[1] + ex.y);
+    B[2] = bs[2] + (bq[2] + ex.z);
 }
 
 // flip_h in FP32: x = beta_mu |h|; 1 - cos(theta) = -ln((1 - e^-2x) q + e^-2x + tol) / x

@@ -13,6 +13,10 @@
 //   midpoint  Evolution/midpoint.f90:34-323, noise rannum (RNG/randomnumbers.f90:625-771)
 // The noise is the FP64 path's Philox stream (site, ensemble, step), drawn with the
 // FP32 Box-Muller of the structured path.
+#include <algorithm>
+#include <string>
+#include <vector>
+
 #include "common.cuh"
 #include "field_f32.cuh"
 #include "field_fp64.cuh"
@@ -37,8 +41,7 @@ struct MixArgs {
     const int64_t *d_step;
     int64_t step_off;
     Vec3D e, eM;           // FP64 master
-    float4 *mt, *mp;       // mirror at t, predictor
-    float *b2x, *b2y, *b2z;
+    MixedDev c;            // mirrors, predictor, b2, FP32 couplings
 };
 
 // Rodrigues rotation increment R e - e about h = bd/|bd| by v = |bd| dtg.
@@ -117,8 +120,8 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
     const size_t o = (size_t)k * N + i;
     const int64_t step = *a.d_step + a.step_off;
     float B[3];
-    field_f32(a.h, a.mt, i, k, B);
-    const float4 me = a.mt[o];
+    field_f32(a.h, a.c, a.c.mt, i, k, B);
+    const float4 me = a.c.mt[o];
     const float e[3] = {me.x, me.y, me.z};
     const float lam = (float)a.lambda[i], mm = me.w;
     float r[3];
@@ -133,9 +136,9 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         p[0] = e[0] + d[0];
         p[1] = e[1] + d[1];
         p[2] = e[2] + d[2];
-        a.b2x[o] = bd[0];
-        a.b2y[o] = bd[1];
-        a.b2z[o] = bd[2];
+        a.c.b2x[o] = bd[0];
+        a.c.b2y[o] = bd[1];
+        a.c.b2z[o] = bd[2];
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
         const float g = (float)a.landeg[i];
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         p[1] = 0.5f * (e[1] + et[1]);
         p[2] = 0.5f * (e[2] + et[2]);
     }
-    a.mp[o] = make_float4(p[0], p[1], p[2], mm);
+    a.c.mp[o] = make_float4(p[0], p[1], p[2], mm);
 }
 
 template <int ALG>
@@ -159,8 +162,8 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     const size_t o = (size_t)k * N + i;
     const int64_t step = *a.d_step + a.step_off;
     float B[3];
-    field_f32(a.h, a.mp, i, k, B);
-    const float4 me = a.mt[o], mpv = a.mp[o];
+    field_f32(a.h, a.c, a.c.mp, i, k, B);
+    const float4 me = a.c.mt[o], mpv = a.c.mp[o];
     const float e[3] = {me.x, me.y, me.z}, pr[3] = {mpv.x, mpv.y, mpv.z};
     const float lam = (float)a.lambda[i], mm = me.w;
     float r[3];
@@ -170,9 +173,9 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         const float bl[3] = {B[0] + r[0], B[1] + r[1], B[2] + r[2]};
         float bd[3] = {bl[0] + lam * (pr[1] * bl[2] - pr[2] * bl[1]), bl[1] + lam * (pr[2] * bl[0] - pr[0] * bl[2]),
                        bl[2] + lam * (pr[0] * bl[1] - pr[1] * bl[0])};
-        bd[0] = 0.5f * bd[0] + 0.5f * a.b2x[o];
-        bd[1] = 0.5f * bd[1] + 0.5f * a.b2y[o];
-        bd[2] = 0.5f * bd[2] + 0.5f * a.b2z[o];
+        bd[0] = 0.5f * bd[0] + 0.5f * a.c.b2x[o];
+        bd[1] = 0.5f * bd[1] + 0.5f * a.c.b2y[o];
+        bd[2] = 0.5f * bd[2] + 0.5f * a.c.b2z[o];
         rotation_delta_f32(bd, e, a.dt_dep / (1.0f + lam * lam), d);
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
@@ -199,14 +202,14 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     a.eM.x[o] = mmd * e0;
     a.eM.y[o] = mmd * e1;
     a.eM.z[o] = mmd * e2;
-    a.mt[o] = make_float4((float)e0, (float)e1, (float)e2, mm);
+    a.c.mt[o] = make_float4((float)e0, (float)e1, (float)e2, mm);
 }
 
 // Heat bath of one colour (flip_h, MonteCarlo/montecarlo_common.f90:371-422) on the
 // FP32 mirror: the field over the caller's neighbour lists, the draw in FP32 with the
 // FP64 path's Philox counters (site, ensemble, sweep), the new spin written to the
 // mirror and to e / eM.  Same checkerboard chain as mc_colour_kernel.
-__global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, float4 *mt, Vec3D e, Vec3D eM, const double *mmom,
+__global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec3D e, Vec3D eM, const double *mmom,
                                                        const int32_t *sites, int nsites, float beta_mub,
                                                        uint64_t seed, int64_t sweep) {
     const int N = h.natom;
@@ -215,8 +218,9 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, float4 *mt, Vec
     const int k = (int)(t / nsites);
     const int i = sites[t - (int64_t)k * nsites];
     const size_t o = (size_t)k * N + i;
+    float4 *mt = c.mt;
     float B[3];
-    field_f32(h, mt, i, k, B);
+    field_f32(h, c, mt, i, k, B);
     const float mm = mt[o].w;
     const Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
     const float k32 = 2.3283064365386963e-10f;
@@ -239,6 +243,71 @@ __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n)
 
 }  // namespace
 
+namespace {
+template <typename T>
+bool fetch(std::vector<T> &h, const T *d, size_t n) {
+    h.resize(n);
+    return n == 0 || cudaMemcpy(h.data(), d, n * sizeof(T), cudaMemcpyDeviceToHost) == cudaSuccess;
+}
+template <typename T>
+bool store(T **d, const std::vector<T> &h) {
+    cudaFree(*d);
+    *d = nullptr;
+    if (h.empty()) return true;
+    return cudaMalloc(d, h.size() * sizeof(T)) == cudaSuccess &&
+           cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
+}
+}  // namespace
+
+// (Re)builds the FP32 copies of the couplings from the FP64 Hamiltonian on the device.
+int mixed_coefficients(Sim &s) {
+    const HamDev &h = s.ham;
+    const size_t N = h.natom, M = h.mensemble, ne = (size_t)std::max(h.mnn, 1) * h.nham;
+    MixedDev &m = s.mix;
+    std::vector<double> d, dx, dy, dz;
+    bool ok = cudaStreamSynchronize(s.stream) == cudaSuccess;
+    ok = ok && fetch(d, h.ncoup, ne);
+    std::vector<float> nc(d.begin(), d.end());
+    ok = ok && store(&m.nc, nc);
+    if (ok && h.do_dm) {
+        const size_t nd = (size_t)h.mnn_dm * h.nham;
+        ok = fetch(dx, h.dmx, nd) && fetch(dy, h.dmy, nd) && fetch(dz, h.dmz, nd);
+        std::vector<float4> v(nd);
+        for (size_t q = 0; q < nd && ok; ++q) v[q] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+        ok = ok && store(&m.dm, v);
+    }
+    if (ok && h.do_jtensor) {
+        ok = fetch(d, h.jt, ne * 9);
+        std::vector<float> v(d.begin(), d.end());
+        ok = ok && store(&m.jt, v);
+    } else if (ok) {
+        ok = store(&m.jt, std::vector<float>());
+    }
+    if (ok && h.do_aniso) {
+        std::vector<double> k1, k2, sb;
+        ok = fetch(dx, h.eax, N) && fetch(dy, h.eay, N) && fetch(dz, h.eaz, N) && fetch(k1, h.k1, N) &&
+             fetch(k2, h.k2, N) && fetch(sb, h.sb, N);
+        std::vector<float4> a(N);
+        std::vector<float2> a2(N);
+        for (size_t i = 0; i < N && ok; ++i) {
+            a[i] = make_float4((float)dx[i], (float)dy[i], (float)dz[i], (float)k1[i]);
+            a2[i] = make_float2((float)k2[i], (float)sb[i]);
+        }
+        ok = ok && store(&m.an, a) && store(&m.an2, a2);
+    }
+    if (ok) {
+        ok = fetch(dx, h.ext.x, N * M) && fetch(dy, h.ext.y, N * M) && fetch(dz, h.ext.z, N * M);
+        std::vector<float4> v(N * M);
+        for (size_t q = 0; q < N * M && ok; ++q) v[q] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+        ok = ok && store(&m.ext, v);
+    }
+    if (!ok) {
+        set_error("precision 3: copying the couplings to FP32 failed");
+        return UPPASD_GPU_ECUDA;
+    }
+    return UPPASD_GPU_OK;
+}
+
 int mixed_init(Sim &s) {
     if (!(s.llg.sdealgh == 1 || s.llg.sdealgh == 5)) {
         set_error("precision 3 (FP32 gather, FP64 master) implements SDEalgh 1 and 5");
@@ -256,12 +325,14 @@ int mixed_init(Sim &s) {
     }
     s.bytes_allocated += n * (2 * sizeof(float4) + 3 * sizeof(float));
     m.valid = 0;
-    return UPPASD_GPU_OK;
+    return mixed_coefficients(s);
 }
 
 void mixed_free(Sim &s) {
     MixedDev &m = s.mix;
-    for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z}) cudaFree(q);
+    for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
+                    (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext})
+        cudaFree(q);
     m = MixedDev{};
 }
 
@@ -291,7 +362,7 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps) {
             if (n == 0) continue;
             const int64_t tot = (int64_t)n * s.ham.mensemble;
             mixed_heat_bath<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
-                s.ham, s.mix.mt, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, s.llg.seed, s.mc_sweep);
+                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, s.llg.seed, s.mc_sweep);
         }
         s.mc_sweep += 1;
     }
@@ -320,11 +391,7 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     a.step_off = step_offset;
     a.e = s.e;
     a.eM = s.eM;
-    a.mt = s.mix.mt;
-    a.mp = s.mix.mp;
-    a.b2x = s.mix.b2x;
-    a.b2y = s.mix.b2y;
-    a.b2z = s.mix.b2z;
+    a.c = s.mix;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const int grid = (int)((n + 255) / 256);
     if (s.llg.sdealgh == 5) {

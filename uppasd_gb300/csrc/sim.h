@@ -66,6 +66,14 @@ struct MixedDev {
     float4 *mt = nullptr, *mp = nullptr;
     float *b2x = nullptr, *b2y = nullptr, *b2z = nullptr;
     int valid = 0;  // mt equals e / mmom
+    // FP32 copies of the Hamiltonian (HamDev layouts): half the bytes of the FP64
+    // arrays, which a non-reduced Hamiltonian reads per site
+    float *nc = nullptr;     // [mnn][nham]
+    float4 *dm = nullptr;    // [mnn_dm][nham] (Dx, Dy, Dz, 0)
+    float *jt = nullptr;     // [mnn][nham][9]
+    float4 *an = nullptr;    // [natom] (ex, ey, ez, k1)
+    float2 *an2 = nullptr;   // [natom] (k2, sb)
+    float4 *ext = nullptr;   // [mensemble][natom] (Bx, By, Bz, 0)
 };
 
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
