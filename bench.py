@@ -658,8 +658,18 @@ def run_gb300(args, w):
                 sg = _make_sim(lg, wg, pg, 3000 + rank, eg)
                 sg.set_stream(stream.cuda_stream)
                 msg = _time_steps(sg, stream, 16, 4, world)
+                # heat-bath sweeps of the same simulation (mc_run 'H')
+                sg.relax("H", wg["temp"], 2)
+                torch.cuda.synchronize()
+                ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                ev0.record(stream)
+                sg.relax("H", wg["temp"], 8)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                msw = ev0.elapsed_time(ev1) / 8
                 sg.close()
-                gen[key] = {"ms_per_step": msg / 16, "value": lg.natom * lg.mensemble * 16 * world / (msg * 1e-3)}
+                gen[key] = {"ms_per_step": msg / 16, "value": lg.natom * lg.mensemble * 16 * world / (msg * 1e-3),
+                            "heat_bath_ms_per_sweep": msw}
             variants["general_hamiltonian"] = gen
         except Exception as exc:
             variants["general_hamiltonian"] = {"error": str(exc)}
