@@ -63,8 +63,9 @@ typedef struct {
                                             spin master and renormalisation (same scope);
                                           3 FP32 field gather over any neighbour list (scalar
                                             or tensor exchange, DMI, anisotropy, Zeeman) + FP64
-                                            spin master and renormalisation (Depondt, midpoint);
-                                            mc_run 'H' draws in FP32 on the same mirror */
+                                            spin master and renormalisation (every SDEalgh of
+                                            precision 0, perp included); mc_run 'H' draws in FP32
+                                            on the same mirror */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;
@@ -106,7 +107,7 @@ int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
 
 /* Input keyword perp = 'Y' (Input/inputhandler.f90:784): before each half-step the
  * effective field loses its component along emom (Evolution/evolution.f90:104-112,
- * :327-335).  0 or 1; -7 on the structured path. */
+ * :327-335).  0 or 1; -7 on the structured path (precision 1, 2). */
 int uppasd_gpu_set_perp(uppasd_gpu_sim *s, int32_t perp);
 
 /* Relaxation time of the inertial regime for SDEalgh 11 (LLGI, Evolution/llgi.f90;

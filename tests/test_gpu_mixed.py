@@ -116,12 +116,48 @@ def test_state_changes_between_runs_are_seen():
     assert np.max(np.abs(res[0] - res[1])) <= 1e-4
 
 
+@pytest.mark.parametrize("solver", [4, 6, 11])
+def test_other_solvers_T0_against_oracle(solver):
+    lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(47), (2, lat.natom, 3))
+    tau = 1e-15 if solver == 11 else 0.0
+    sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=0.0, seed=31, emom=e0,
+                        precision=3, relaxtime=tau)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, 1e-16, 0.05, 0.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=31, relaxtime=tau)
+    done = 0
+    for n, tol in CHECKPOINTS.items():
+        sim.evolve(n - done)
+        for _ in range(n - done):
+            o.sd_step()
+        done = n
+        g = sim.get_moments()
+        assert np.max(np.abs(g - o.emom)) <= tol, (n, np.max(np.abs(g - o.emom)))
+        assert np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)) <= 1e-12
+    sim.close()
+
+
+@pytest.mark.parametrize("solver", [1, 4, 5, 6, 11])
+def test_perp_against_oracle(solver):
+    lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(48), (2, lat.natom, 3))
+    tau = 1e-15 if solver == 11 else 0.0
+    sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=50.0, seed=33, emom=e0,
+                        precision=3, relaxtime=tau, perp=True)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, 1e-16, 0.05, 50.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=33, relaxtime=tau, perp=True)
+    sim.evolve(100)
+    for _ in range(100):
+        o.sd_step()
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= THERMAL_TOL
+    sim.close()
+
+
 def test_scope():
-    lat = lattice.square_dmi(16)
-    with pytest.raises(_lib.UppasdGpuError) as ex:
-        GpuSimulation(lat, sdealgh=4, precision=3)
-    assert ex.value.rc == -7
-    sim = GpuSimulation(lat, sdealgh=1, precision=3)
+    lat = lattice.bcc_alloy(6, seed=9)
+    sim = GpuSimulation(lat, sdealgh=5, precision=1)
     with pytest.raises(_lib.UppasdGpuError) as ex:
         _lib.call("uppasd_gpu_set_perp", sim._h, 1)
     assert ex.value.rc == -7

@@ -552,8 +552,8 @@ int uppasd_gpu_set_perp(uppasd_gpu_sim *w, int32_t perp) {
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = w->s;
-    if (perp && s.precision >= 1) {
-        uppasd::set_error("set_perp: only the FP64 path (precision 0) has the field projection");
+    if (perp && uppasd::structured(s)) {
+        uppasd::set_error("set_perp: the structured path (precision 1, 2) has no field projection");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     uppasd::drop_graph(s);  // the step arguments are captured by value

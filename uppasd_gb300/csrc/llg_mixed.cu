@@ -15,6 +15,7 @@
 // FP32 Box-Muller of the structured path.
 #include <algorithm>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "common.cuh"
@@ -35,12 +36,17 @@ struct MixArgs {
     float dt_mid;   // delta_t bn gama: midpoint dt = dt_mid / (1 + lambda^2)
     float c_dp;     // 2 kB / (delta_t gama muB): Depondt D = c_dp lambda
     float c_dk;     // kB / (muB bn): midpoint D = c_dk lambda / (1 + lambda^2)
+    float c_heun;   // delta_t gama kB / muB: Heun sigma^2 / 2 = c_heun lambda / (1 + lambda^2) T / m
+    float tau_dt;   // LLGI relaxtime / delta_t
+    float dtg_llgi; // LLGI -delta_t gama
     float temprescale;
     int noise_on;
+    int perp;       // field projected perpendicular to emom before each half-step
     NoiseArgs nz;          // Philox (FP32 Box-Muller here), injected normals, or none
     const int64_t *d_step;
     int64_t step_off;
     Vec3D e, eM;           // FP64 master
+    Vec3D mpast;           // LLGI m(t - dt), FP64
     MixedDev c;            // mirrors, predictor, b2, FP32 couplings
 };
 
@@ -81,12 +87,99 @@ __device__ __forceinline__ void cayley_f32(const float A[3], const float e[3], f
     out[2] = (a0 * (A[2] * A[0] + A[1]) + a1 * (A[2] * A[1] - A[0]) + a2 * (1.0f + A[2] * A[2])) * detAi;
 }
 
-// thermal field / midpoint noise of site i at `step` (regenerated by the corrector)
+// SIB (sphmidpoint.f90:36-477) in FP32: a1 = -b - lam e x b, s1 likewise with the
+// noise, then the fixed point of e' = e + dtg f x a1 + sqrt(dt) g f x s1 with
+// f = (e + e')/2.  The FP64 path stops at 1e-12 per component; FP32 converges to
+// its rounding, so the tolerance here is 2e-7.
+__device__ __forceinline__ void sib_f32(float lam, const float e[3], const float b[3], const float r[3],
+                                        const float e1[3], float dtg, float sqrtdtg, float out[3]) {
+    const float a1[3] = {-b[0] - lam * (e[1] * b[2] - e[2] * b[1]), -b[1] - lam * (e[2] * b[0] - e[0] * b[2]),
+                         -b[2] - lam * (e[0] * b[1] - e[1] * b[0])};
+    const float s1[3] = {-r[0] - lam * (e[1] * r[2] - e[2] * r[1]), -r[1] - lam * (e[2] * r[0] - e[0] * r[2]),
+                         -r[2] - lam * (e[0] * r[1] - e[1] * r[0])};
+    float f0[3] = {e1[0], e1[1], e1[2]};
+    for (int it = 0; it < 100; ++it) {
+        float fd[3], fs[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float f1 = 0.5f * (e1[c] + f0[c]);
+            fd[c] = dtg * f1;
+            fs[c] = sqrtdtg * f1;
+        }
+        out[0] = e1[0] + fd[1] * a1[2] - fd[2] * a1[1] + fs[1] * s1[2] - fs[2] * s1[1];
+        out[1] = e1[1] + fd[2] * a1[0] - fd[0] * a1[2] + fs[2] * s1[0] - fs[0] * s1[2];
+        out[2] = e1[2] + fd[0] * a1[1] - fd[1] * a1[0] + fs[0] * s1[1] - fs[1] * s1[0];
+        const bool done = fabsf(f0[0] - out[0]) < 2e-7f && fabsf(f0[1] - out[1]) < 2e-7f &&
+                          fabsf(f0[2] - out[2]) < 2e-7f;
+        f0[0] = out[0];
+        f0[1] = out[1];
+        f0[2] = out[2];
+        if (done) break;
+    }
+}
+
+// Heun drift a = lam h + e x h - e (e . lam h) and diffusion matrix b of one half
+// (heun_proper.f90:28-161, 261-530); zzq reproduces the corrector's b1zz expression.
+__device__ __forceinline__ void heun_ab(float lam, const float e[3], const float h[3], bool zzq, float a[3],
+                                        float bm[9]) {
+    const float hl[3] = {lam * h[0], lam * h[1], lam * h[2]};
+    const float prot = e[0] * hl[0] + e[1] * hl[1] + e[2] * hl[2];
+    a[0] = hl[0] + e[2] * h[1] - e[1] * h[2] - e[0] * prot;
+    a[1] = hl[1] - e[2] * h[0] + e[0] * h[2] - e[1] * prot;
+    a[2] = hl[2] + e[1] * h[0] - e[0] * h[1] - e[2] * prot;
+    bm[0] = lam - e[0] * e[0] * lam;
+    bm[1] = e[2] - e[0] * e[1] * lam;
+    bm[2] = -e[1] - e[0] * e[2] * lam;
+    bm[3] = -e[2] - e[1] * e[0] * lam;
+    bm[4] = lam - e[1] * e[1] * lam;
+    bm[5] = e[0] - e[1] * e[2] * lam;
+    bm[6] = e[1] - e[2] * e[0] * lam;
+    bm[7] = -e[0] - e[2] * e[1] * lam;
+    bm[8] = zzq ? lam - e[2] * e[2] - lam : lam - e[2] * e[2] * lam;
+}
+
+// llgiheun (llgi.f90:178-278) in FP32: m = A^-1 B, A = I + beta [e1]x
+__device__ __forceinline__ void llgi_f32(float lam, float tau_dt, float dtg, const float et[3], const float e1[3],
+                                         const float h[3], float out[3]) {
+    const float beta = -lam * (1.0f + tau_dt), zeta = -lam * tau_dt;
+    const float A12 = -beta * e1[2], A13 = beta * e1[1], A21 = beta * e1[2], A23 = -beta * e1[0];
+    const float A31 = -beta * e1[1], A32 = beta * e1[0];
+    const float det = 1.0f / (1.0f - A23 * A32 - A12 * A21 - A13 * A31);
+    const float B1 = e1[0] + dtg * (e1[1] * h[2] - e1[2] * h[1]) + zeta * (e1[2] * et[1] - e1[1] * et[2]);
+    const float B2 = e1[1] + dtg * (e1[2] * h[0] - e1[0] * h[2]) + zeta * (e1[0] * et[2] - e1[2] * et[0]);
+    const float B3 = e1[2] + dtg * (e1[0] * h[1] - e1[1] * h[0]) + zeta * (e1[1] * et[0] - e1[0] * et[1]);
+    out[0] = ((1.0f - A32 * A23) * B1 + (A13 * A32 - A12) * B2 + (A12 * A23 - A13) * B3) * det;
+    out[1] = ((A23 * A31 - A21) * B1 + (1.0f - A31 * A13) * B2 + (A13 * A21 - A23) * B3) * det;
+    out[2] = ((A21 * A32 - A31) * B1 + (A12 * A31 - A32) * B2 + (1.0f - A21 * A12) * B3) * det;
+}
+
+// 1 / sqrt(1 + x) in FP64: the second-order series when |x| < 1e-7 (the rotating
+// solvers; truncation below 1e-21), else two Newton steps from the FP32 estimate
+// (Heun and LLGI leave the sphere at first order, |x| up to ~1e-4).
+__device__ __forceinline__ double renorm_scale(double x) {
+    if (fabs(x) < 1e-7) return fma(x, fma(0.375, x, -0.5), 1.0);
+    const double n2 = 1.0 + x;
+    double y = (double)rsqrtf((float)n2);
+    y = y * fma(-0.5 * n2, y * y, 1.5);
+    y = y * fma(-0.5 * n2, y * y, 1.5);
+    return y;
+}
+
+__device__ __forceinline__ void perp_f32(float B[3], const float e[3]) {
+    const float d = B[0] * e[0] + B[1] * e[1] + B[2] * e[2];
+    B[0] -= e[0] * d;
+    B[1] -= e[1] * d;
+    B[2] -= e[2] * d;
+}
+
+// Noise of site i at `step` (the corrector draws the same numbers again), scaled as
+// each solver scales it: Depondt / LLGI thermal field, rannum (midpoint, SIB; off
+// when min(lambda) <= 1e-12), Heun's dW (with the Lande factor applied by the caller).
 template <int ALG>
 __device__ __forceinline__ void noise_f32(const MixArgs &a, int i, int k, int64_t step, float lam, float mm,
                                           float out[3]) {
     float z[3];
-    if (ALG == 1 && !a.noise_on) {
+    if ((ALG == 1 || ALG == 6) && !a.noise_on) {
         out[0] = out[1] = out[2] = 0.f;
         return;
     }
@@ -101,11 +194,9 @@ __device__ __forceinline__ void noise_f32(const MixArgs &a, int i, int k, int64_
     }
     const float T = (float)a.temp[i] * a.temprescale;
     float sigma;
-    if (ALG == 5) {
-        sigma = sqrtf(a.c_dp * lam * T / mm);
-    } else {
-        sigma = sqrtf(2.0f * (a.c_dk * lam / (1.0f + lam * lam)) * T / mm);
-    }
+    if (ALG == 5 || ALG == 11) sigma = sqrtf(a.c_dp * lam * T / mm);
+    else if (ALG == 4) sigma = sqrtf(2.0f * (a.c_heun * lam / (1.0f + lam * lam)) * T / mm);
+    else sigma = sqrtf(2.0f * (a.c_dk * lam / (1.0f + lam * lam)) * T / mm);
     out[0] = z[0] * sigma;
     out[1] = z[1] * sigma;
     out[2] = z[2] * sigma;
@@ -123,6 +214,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
     field_f32(a.h, a.c, a.c.mt, i, k, B);
     const float4 me = a.c.mt[o];
     const float e[3] = {me.x, me.y, me.z};
+    if (a.perp) perp_f32(B, e);
     const float lam = (float)a.lambda[i], mm = me.w;
     float r[3];
     noise_f32<ALG>(a, i, k, step, lam, mm, r);
@@ -139,13 +231,37 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         a.c.b2x[o] = bd[0];
         a.c.b2y[o] = bd[1];
         a.c.b2z[o] = bd[2];
+    } else if (ALG == 11) {
+        const float bd[3] = {B[0] + r[0], B[1] + r[1], B[2] + r[2]};
+        const float et[3] = {(float)a.mpast.x[o], (float)a.mpast.y[o], (float)a.mpast.z[o]};
+        llgi_f32(lam, a.tau_dt, a.dtg_llgi, et, e, bd, p);
+        a.c.b2x[o] = bd[0];
+        a.c.b2y[o] = bd[1];
+        a.c.b2z[o] = bd[2];
+    } else if (ALG == 4) {
+        const float g = (float)a.landeg[i];
+        const float dtg = a.dt_dep * g / (1.0f + lam * lam);
+        const float dw[3] = {r[0] * g, r[1] * g, r[2] * g};
+        float ah[3], bm[9];
+        heun_ab(lam, e, B, false, ah, bm);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            p[c] = e[c] + ah[c] * dtg + bm[3 * c] * dw[0] + bm[3 * c + 1] * dw[1] + bm[3 * c + 2] * dw[2];
+        a.c.b2x[o] = B[0];
+        a.c.b2y[o] = B[1];
+        a.c.b2z[o] = B[2];
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
         const float g = (float)a.landeg[i];
         const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
-        float A[3], et[3];
-        midpoint_A_f32(lam, dtg, sqrtdtg, e, B, r, A);
-        cayley_f32(A, e, et);
+        float et[3];
+        if (ALG == 1) {
+            float A[3];
+            midpoint_A_f32(lam, dtg, sqrtdtg, e, B, r, A);
+            cayley_f32(A, e, et);
+        } else {
+            sib_f32(lam, e, B, r, e, dtg, sqrtdtg, et);
+        }
         p[0] = 0.5f * (e[0] + et[0]);
         p[1] = 0.5f * (e[1] + et[1]);
         p[2] = 0.5f * (e[2] + et[2]);
@@ -165,10 +281,13 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     field_f32(a.h, a.c, a.c.mp, i, k, B);
     const float4 me = a.c.mt[o], mpv = a.c.mp[o];
     const float e[3] = {me.x, me.y, me.z}, pr[3] = {mpv.x, mpv.y, mpv.z};
+    // emom at the second half-step: m(t) for midpoint and SIB, the predictor otherwise
+    if (a.perp) perp_f32(B, (ALG == 1 || ALG == 6) ? e : pr);
     const float lam = (float)a.lambda[i], mm = me.w;
     float r[3];
     noise_f32<ALG>(a, i, k, step, lam, mm, r);
-    float d[3];
+    float out[3];
+    bool unit = false;  // out is the new spin (else e + out)
     if (ALG == 5) {
         const float bl[3] = {B[0] + r[0], B[1] + r[1], B[2] + r[2]};
         float bd[3] = {bl[0] + lam * (pr[1] * bl[2] - pr[2] * bl[1]), bl[1] + lam * (pr[2] * bl[0] - pr[0] * bl[2]),
@@ -176,22 +295,56 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         bd[0] = 0.5f * bd[0] + 0.5f * a.c.b2x[o];
         bd[1] = 0.5f * bd[1] + 0.5f * a.c.b2y[o];
         bd[2] = 0.5f * bd[2] + 0.5f * a.c.b2z[o];
-        rotation_delta_f32(bd, e, a.dt_dep / (1.0f + lam * lam), d);
+        rotation_delta_f32(bd, e, a.dt_dep / (1.0f + lam * lam), out);
+    } else if (ALG == 11) {
+        const float bd[3] = {0.5f * (B[0] + r[0]) + 0.5f * a.c.b2x[o], 0.5f * (B[1] + r[1]) + 0.5f * a.c.b2y[o],
+                             0.5f * (B[2] + r[2]) + 0.5f * a.c.b2z[o]};
+        const float et[3] = {(float)a.mpast.x[o], (float)a.mpast.y[o], (float)a.mpast.z[o]};
+        // m(t) becomes the previous step (FP64, from the master)
+        a.mpast.x[o] = a.e.x[o];
+        a.mpast.y[o] = a.e.y[o];
+        a.mpast.z[o] = a.e.z[o];
+        llgi_f32(lam, a.tau_dt, a.dtg_llgi, et, e, bd, out);
+        unit = true;
+    } else if (ALG == 4) {
+        const float g = (float)a.landeg[i];
+        const float dtg = a.dt_dep * g / (1.0f + lam * lam);
+        const float dw[3] = {r[0] * g, r[1] * g, r[2] * g};
+        const float h2[3] = {a.c.b2x[o], a.c.b2y[o], a.c.b2z[o]};
+        float a1[3], b1[9], a2[3], b2[9];
+        heun_ab(lam, pr, B, true, a1, b1);
+        heun_ab(lam, e, h2, false, a2, b2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            out[c] = e[c] + 0.5f * ((a1[c] + a2[c]) * dtg + (b1[3 * c] + b2[3 * c]) * dw[0] +
+                                    (b1[3 * c + 1] + b2[3 * c + 1]) * dw[1] + (b1[3 * c + 2] + b2[3 * c + 2]) * dw[2]);
+        unit = true;
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
         const float g = (float)a.landeg[i];
         const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
-        float A[3], et[3];
-        midpoint_A_f32(lam, dtg, sqrtdtg, pr, B, r, A);
-        cayley_f32(A, e, et);
-        d[0] = et[0] - e[0];
-        d[1] = et[1] - e[1];
-        d[2] = et[2] - e[2];
+        if (ALG == 1) {
+            float A[3];
+            midpoint_A_f32(lam, dtg, sqrtdtg, pr, B, r, A);
+            cayley_f32(A, e, out);
+        } else {
+            sib_f32(lam, pr, B, r, e, dtg, sqrtdtg, out);
+        }
+        unit = true;
+    }
+    float d[3];
+    if (unit) {
+        d[0] = out[0] - e[0];
+        d[1] = out[1] - e[1];
+        d[2] = out[2] - e[2];
+    } else {
+        d[0] = out[0];
+        d[1] = out[1];
+        d[2] = out[2];
     }
     // FP64 master: add the change, renormalise, refresh the mirror
     double e0 = a.e.x[o] + (double)d[0], e1 = a.e.y[o] + (double)d[1], e2 = a.e.z[o] + (double)d[2];
-    const double xx = fma(e2, e2, fma(e1, e1, e0 * e0)) - 1.0;
-    const double sc = fma(xx, fma(0.375, xx, -0.5), 1.0);  // 1/sqrt(1+x) to second order, |x| ~ 1e-7
+    const double sc = renorm_scale(fma(e2, e2, fma(e1, e1, e0 * e0)) - 1.0);
     e0 *= sc;
     e1 *= sc;
     e2 *= sc;
@@ -309,8 +462,9 @@ int mixed_coefficients(Sim &s) {
 }
 
 int mixed_init(Sim &s) {
-    if (!(s.llg.sdealgh == 1 || s.llg.sdealgh == 5)) {
-        set_error("precision 3 (FP32 gather, FP64 master) implements SDEalgh 1 and 5");
+    if (!(s.llg.sdealgh == 1 || s.llg.sdealgh == 4 || s.llg.sdealgh == 5 || s.llg.sdealgh == 6 ||
+          s.llg.sdealgh == 11)) {
+        set_error("precision 3 (FP32 gather, FP64 master): unknown SDEalgh");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     const size_t n = (size_t)s.ham.natom * s.ham.mensemble;
@@ -381,6 +535,11 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     a.dt_mid = (float)(s.llg.delta_t * s.llg.bn * kGama);
     a.c_dp = (float)(2.0 * kKbolt / (s.llg.delta_t * kGama * kMub));
     a.c_dk = (float)(kKbolt / (kMub * s.llg.bn));
+    a.c_heun = (float)(s.llg.delta_t * kGama * kKbolt / kMub);
+    a.tau_dt = (float)(s.llg.relaxtime / s.llg.delta_t);
+    a.dtg_llgi = (float)(-s.llg.delta_t * kGama);
+    a.perp = s.llg.perp;
+    a.mpast = s.mpast;
     a.temprescale = (float)s.llg.temprescale;
     a.noise_on = s.llg.noise_on;
     a.nz.mode = s.llg.noise_mode;
@@ -394,12 +553,18 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     a.c = s.mix;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const int grid = (int)((n + 255) / 256);
-    if (s.llg.sdealgh == 5) {
-        if (phase & 1) mixed_predict<5><<<grid, 256, 0, s.stream>>>(a);
-        if (phase & 2) mixed_correct<5><<<grid, 256, 0, s.stream>>>(a);
-    } else {
-        if (phase & 1) mixed_predict<1><<<grid, 256, 0, s.stream>>>(a);
-        if (phase & 2) mixed_correct<1><<<grid, 256, 0, s.stream>>>(a);
+    auto run = [&](auto alg) {
+        constexpr int ALG = decltype(alg)::value;
+        if (phase & 1) mixed_predict<ALG><<<grid, 256, 0, s.stream>>>(a);
+        if (phase & 2) mixed_correct<ALG><<<grid, 256, 0, s.stream>>>(a);
+    };
+    switch (s.llg.sdealgh) {
+    case 1: run(std::integral_constant<int, 1>{}); break;
+    case 4: run(std::integral_constant<int, 4>{}); break;
+    case 5: run(std::integral_constant<int, 5>{}); break;
+    case 6: run(std::integral_constant<int, 6>{}); break;
+    case 11: run(std::integral_constant<int, 11>{}); break;
+    default: set_error("unsupported SDEalgh"); return UPPASD_GPU_EUNSUPPORTED;
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
