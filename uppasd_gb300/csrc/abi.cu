@@ -360,7 +360,7 @@ void destroy(Sim &s) {
     HamDev &h = s.ham;
     void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
-                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm};
+                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm, s.stage};
     for (void *q : ptrs) cudaFree(q);
     free_vec3(h.ext);
     free_vec3(s.e);
@@ -488,8 +488,8 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
     Sim &s = w->s;
     uppasd::square_mirror_stale(s);
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
-    double *d = nullptr;
-    UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
+    double *d = uppasd::stage_buffer(s);
+    if (!d) return UPPASD_GPU_ENOMEM;
     cudaError_t e = cudaMemcpyAsync(d, emom, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.stream);
     if (e == cudaSuccess) {
         uppasd::aos_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(d, s.e, s.eM, s.llg.mmom, n);
@@ -498,7 +498,6 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
     // SDEalgh 11: a new state has no previous step (the reference's mpast starts at zero, llgi.f90:295)
     for (double *q : {s.mpast.x, s.mpast.y, s.mpast.z})
         if (e == cudaSuccess && q) e = cudaMemsetAsync(q, 0, n * sizeof(double), s.stream);
-    cudaFreeAsync(d, s.stream);
     if (e != cudaSuccess) {
         uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
         return UPPASD_GPU_ECUDA;
@@ -516,8 +515,8 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
     int rc;
     if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
-    double *d = nullptr;
-    UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
+    double *d = uppasd::stage_buffer(s);
+    if (!d) return UPPASD_GPU_ENOMEM;
     cudaError_t e = cudaSuccess;
     const unsigned grid = (unsigned)((n + 255) / 256);
     if (emom) {
@@ -528,7 +527,6 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
         uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.eM, d, n);
         e = cudaMemcpyAsync(emomM, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
     }
-    cudaFreeAsync(d, s.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) {
         uppasd::set_error(std::string("get_moments: ") + cudaGetErrorString(e));

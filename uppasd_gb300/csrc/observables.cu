@@ -140,12 +140,11 @@ __global__ void __launch_bounds__(256) field_kernel(HamDev h, Vec3D m, double *b
 
 int field_to_host(Sim &s, double *beff_h) {
     const size_t n = (size_t)s.ham.natom * s.ham.mensemble;
-    double *d = nullptr;
-    UPPASD_CUDA_TRY(cudaMallocAsync(&d, 3 * n * sizeof(double), s.stream));
+    double *d = stage_buffer(s);
+    if (!d) return UPPASD_GPU_ENOMEM;
     field_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.ham, s.eM, d);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaMemcpyAsync(beff_h, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
-    cudaFreeAsync(d, s.stream);
     if (err == cudaSuccess) err = cudaStreamSynchronize(s.stream);
     if (err != cudaSuccess) {
         set_error(std::string("field_to_host: ") + cudaGetErrorString(err));

@@ -114,6 +114,8 @@ struct Sim {
     float4 *sqm = nullptr;
     int sqm_valid = 0;
     MixedDev mix;
+    // (3, natom, mensemble) staging array of the host transfers, kept between calls
+    double *stage = nullptr;
     // scratch for observables
     double *red = nullptr;             // [mensemble][8]
     size_t bytes_allocated = 0;
@@ -142,6 +144,20 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
 // mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
 int square_recognise(Sim &s, int L);
 int square_mirror_ready(Sim &s);  // builds the FP32 mirror from e when it is stale
+void set_error(const std::string &msg);
+// the host-transfer staging array (allocated on first use); nullptr with the error set
+inline double *stage_buffer(Sim &s) {
+    if (!s.stage) {
+        const size_t bytes = 3 * sizeof(double) * (size_t)s.ham.natom * s.ham.mensemble;
+        if (cudaMalloc(&s.stage, bytes) != cudaSuccess) {
+            s.stage = nullptr;
+            set_error("staging array: cudaMalloc failed");
+            return nullptr;
+        }
+        s.bytes_allocated += bytes;
+    }
+    return s.stage;
+}
 // every FP32 mirror of e is stale (a writer of e other than the mirror's own users)
 inline void square_mirror_stale(Sim &s) {
     s.sqm_valid = 0;

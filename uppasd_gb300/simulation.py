@@ -128,9 +128,17 @@ class GpuSimulation:
         e = np.ascontiguousarray(np.broadcast_to(emom, (self.lat.mensemble, self.lat.natom, 3)), dtype=np.float64)
         _lib.call("uppasd_gpu_put_moments", self._h, _ptr(e))
 
-    def get_moments(self, full: bool = False):
+    def get_moments(self, full: bool = False, out: Optional[np.ndarray] = None):
+        """Unit moments (mensemble, natom, 3); with full=True also the full moments.
+        `out`: a C-contiguous float64 array of that shape to copy into (e.g. pinned
+        host memory, which the device-to-host copy reads at full speed)."""
         shape = (self.lat.mensemble, self.lat.natom, 3)
-        e = np.empty(shape)
+        if out is not None:
+            if out.shape != shape or out.dtype != np.float64 or not out.flags.c_contiguous:
+                raise ValueError(f"out must be a C-contiguous float64 array of shape {shape}")
+            e = out
+        else:
+            e = np.empty(shape)
         em = np.empty(shape) if full else None
         _lib.call("uppasd_gpu_get_moments", self._h, _ptr(e), _ptr(em))
         return (e, em) if full else e
