@@ -145,6 +145,24 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *s, char mode, double temperature, int64_t 
  * all ensembles per launch. */
 int uppasd_gpu_mc_run_square(uppasd_gpu_sim *s, int32_t L, double temperature, int64_t nsweeps);
 
+/* Monte Carlo sweeps with one temperature per ensemble (temps[mensemble], K): the
+ * chain of uppasd_gpu_mc_run with T taken per ensemble (on precision 3 the heat bath
+ * draws in FP32 as there). */
+int uppasd_gpu_mc_run_temps(uppasd_gpu_sim *s, char mode, const double *temps, int64_t nsweeps);
+
+/* Parallel tempering of pt_iphase (pt_driver.f90:58-367) with the ensembles as its
+ * replicas: heat-bath sweeps at temps[replica]; every pt_step sweeps during the
+ * first 90 % of nsweeps, swap attempts between replica positions (r, r + 1),
+ * r = 0, 2, ... then 1, 3, ..., accepted with min(1, exp((e_{r+1} - e_r)(b_{r+1} - b_r)))
+ * on energies per atom (J) and b = 1 / kB / (T + 1e-15), one uniform per position
+ * from the Philox stream (position, 0, sweep).  temps comes back permuted (the
+ * temperature each replica ended with); selected = the replica of lowest energy,
+ * the one pt_iphase continues from.  The replica energy is calc_energy's total,
+ * which pt_iphase's effective_field energy equals except for the weight of the
+ * cubic-anisotropy term. */
+int uppasd_gpu_pt_run(uppasd_gpu_sim *s, double *temps, int64_t nsweeps, int32_t pt_step, int64_t *n_trial,
+                      int64_t *n_hit, int32_t *selected);
+
 /* Per-ensemble total moment (3, mensemble), |M|/natom (mensemble) and energy per
  * atom in mRy (mensemble); any output may be NULL. */
 int uppasd_gpu_observables(uppasd_gpu_sim *s, double *mvec, double *mabs, double *energy);

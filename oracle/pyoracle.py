@@ -100,6 +100,8 @@ def load():
                                       C.POINTER(OrcMT), C.POINTER(OrcZig), F64P, F64P, F64P, F64P]
     lib.orc_mc_sweep_checkerboard.argtypes = [C.POINTER(OrcHam), C.c_char, C.c_double, I32P, I32P, C.c_int,
                                               C.c_uint64, C.c_int64, F64P, F64P, F64P]
+    lib.orc_mc_sweep_checkerboard_temps.argtypes = [C.POINTER(OrcHam), C.c_char, C.c_double, F64P, I32P, I32P,
+                                                    C.c_int, C.c_uint64, C.c_int64, F64P, F64P, F64P]
     lib.orc_mavg.argtypes = [C.c_int, C.c_int, F64P, F64P, F64P]
     lib.orc_energy.argtypes = [C.POINTER(OrcHam), F64P, F64P, F64P, F64P, F64P, F64P]
     lib.orc_cumulant_update.argtypes = [C.POINTER(OrcCumulant), C.c_int, C.c_int, F64P, C.c_double, F64P, F64P]
@@ -259,12 +261,50 @@ class Oracle:
         self.lib.orc_choose_random_atom_x(C.byref(self.mt), self.lat.natom, _p(out, I32P))
         return out
 
-    def mc_sweep_checkerboard(self, mode: str, temperature: float, colour_sites, colour_start, seed: int, sweep: int):
+    def mc_sweep_checkerboard(self, mode: str, temperature: float, colour_sites, colour_start, seed: int, sweep: int,
+                              temps=None):
+        """One checkerboard sweep; temps: one temperature per ensemble (overrides temperature)."""
         cs = np.ascontiguousarray(colour_sites, dtype=np.int32)
         st = np.ascontiguousarray(colour_start, dtype=np.int32)
-        return self.lib.orc_mc_sweep_checkerboard(C.byref(self.ham), mode.encode(), temperature, _p(cs, I32P),
-                                                  _p(st, I32P), len(st) - 1, seed, sweep, _p(self.emom),
-                                                  _p(self.emomM), _p(self.mmom))
+        tk = None if temps is None else np.ascontiguousarray(temps, dtype=np.float64)
+        return self.lib.orc_mc_sweep_checkerboard_temps(C.byref(self.ham), mode.encode(), temperature, _p(tk),
+                                                        _p(cs, I32P), _p(st, I32P), len(st) - 1, seed, sweep,
+                                                        _p(self.emom), _p(self.emomM), _p(self.mmom))
+
+    def pt_iphase(self, temps, nsweeps: int, pt_step: int, colour_sites, colour_start, seed: int, sweep0: int = 0):
+        """pt_iphase (pt_driver.f90:58-367) with the ensembles as replicas on the checkerboard
+        heat bath: swap attempts every pt_step sweeps during the first 90 %, positions
+        (r, r + 1) for r = 0, 2, ... then 1, 3, ..., one Philox uniform per position
+        (position, 0, step, stream 8), acceptance min(1, exp((e2 - e1)(b2 - b1))) on the
+        per-atom energies in J.  Returns (temps, trials, accepted, lowest-energy replica)."""
+        kb = 1.38064852e-23
+        T = np.array(temps, dtype=np.float64)
+        M = self.lat.mensemble
+        trial = hit = 0
+        for step in range(1, nsweeps + 1):
+            self.mc_sweep_checkerboard("H", 0.0, colour_sites, colour_start, seed, sweep0 + step - 1, temps=T)
+            if step % pt_step or step / nsweeps >= 0.90:
+                continue
+            ene = self.energy()["total"] * 2.179872325e-21
+            u = [uniform4(seed, r, 0, step, 8)[0] for r in range(M)]
+            for ishift in (0, 1):
+                for r in range(ishift, M - 1, 2):
+                    trial += 1
+                    b1, b2 = 1.0 / kb / (T[r] + 1e-15), 1.0 / kb / (T[r + 1] + 1e-15)
+                    prob = min(1.0, np.exp((ene[r + 1] - ene[r]) * (b2 - b1)))
+                    if u[r] <= prob:
+                        T[r], T[r + 1] = T[r + 1], T[r]
+                        hit += 1
+        ene = self.energy()["total"]
+        return T, trial, hit, int(np.argmin(ene))
+
+
+def uniform4(seed: int, site: int, ens: int, step: int, stream: int):
+    """The four (0, 1) uniforms of one Philox draw (site, ensemble, step, stream)."""
+    lib = load()
+    u = np.zeros(4)
+    lib.orc_philox_uniform4(seed, site, ens, step, stream, _p(u))
+    return u
 
 
 def philox(ctr, key):

@@ -1059,21 +1059,30 @@ int orc_mc_evolve_ref(const orc_ham *h, char mode, double temperature, double te
 int orc_mc_sweep_checkerboard(const orc_ham *h, char mode, double temperature,
                               const int32_t *colour_sites, const int32_t *colour_start, int ncolour,
                               uint64_t seed, int64_t sweep, double *emom, double *emomM, const double *mmom) {
+    return orc_mc_sweep_checkerboard_temps(h, mode, temperature, NULL, colour_sites, colour_start, ncolour, seed,
+                                           sweep, emom, emomM, mmom);
+}
+
+/* The same sweep with one temperature per ensemble (temps[k]; NULL: `temperature`
+ * for all), as the replicas of pt_iphase (pt_driver.f90:58-367) run it. */
+int orc_mc_sweep_checkerboard_temps(const orc_ham *h, char mode, double temperature, const double *temps,
+                                    const int32_t *colour_sites, const int32_t *colour_start, int ncolour,
+                                    uint64_t seed, int64_t sweep, double *emom, double *emomM, const double *mmom) {
     const int N = h->natom, M = h->mensemble;
-    double delta = F32(2.0 / 25.0) * pow(ORC_KBOLT * temperature / ORC_MUB, 0.20);
     for (int col = 0; col < ncolour; ++col) {
         int beg = colour_start[col], end = colour_start[col + 1];
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
         for (int t = beg; t < end; ++t) {
             int i = colour_sites[t];
             for (int k = 0; k < M; ++k) {
+                const double Tk = temps ? temps[k] : temperature;
                 double u[4];
                 orc_philox_uniform4(seed, i, k, sweep, 1u, u);
                 double mm = M2(mmom, i, k, N);
                 if (mode == 'H') {
                     double tf[3], nm[3];
                     orc_effective_field_single(h, emomM, i, k, tf);
-                    flip_h(mm, temperature, 1.0, u[1], tf, u[0], nm);
+                    flip_h(mm, Tk, 1.0, u[1], tf, u[0], nm);
                     for (int cc = 0; cc < 3; ++cc) {
                         V3(emom, cc, i, k, N) = nm[cc];
                         V3(emomM, cc, i, k, N) = mm * nm[cc];
@@ -1082,10 +1091,11 @@ int orc_mc_sweep_checkerboard(const orc_ham *h, char mode, double temperature,
                     double gn[3] = {0.0, 0.0, 0.0}, nm[3], ext[3];
                     double rn[3] = {u[0], u[1], u[2]};
                     if ((int)floor(3.0 * rn[0]) == 1) orc_philox_normal3(seed, i, k, sweep, 2u, gn);
+                    const double delta = F32(2.0 / 25.0) * pow(ORC_KBOLT * Tk / ORC_MUB, 0.20);
                     choose_random_flip(&V3(emom, 0, i, k, N), delta, rn, gn, nm);
                     for (int cc = 0; cc < 3; ++cc) ext[cc] = V3(h->extfield, cc, i, k, N) + 0.0;
                     double de = calculate_energy(h, emomM, emom, mmom, i, nm, ext, k);
-                    if (flip_a(de, temperature, 1.0, u[3])) {
+                    if (flip_a(de, Tk, 1.0, u[3])) {
                         for (int cc = 0; cc < 3; ++cc) {
                             V3(emom, cc, i, k, N) = nm[cc];
                             V3(emomM, cc, i, k, N) = mm * nm[cc];

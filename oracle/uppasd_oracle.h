@@ -142,6 +142,10 @@ int orc_mc_sweep_checkerboard(const orc_ham *h, char mode, double temperature,
                               const int32_t *colour_sites, const int32_t *colour_start,
                               int ncolour, uint64_t seed, int64_t sweep,
                               double *emom, double *emomM, const double *mmom);
+/* The same with one temperature per ensemble (temps[k]; NULL: `temperature`). */
+int orc_mc_sweep_checkerboard_temps(const orc_ham *h, char mode, double temperature, const double *temps,
+                                    const int32_t *colour_sites, const int32_t *colour_start, int ncolour,
+                                    uint64_t seed, int64_t sweep, double *emom, double *emomM, const double *mmom);
 
 /* ---- observables ---- */
 /* |M| per ensemble / natom (measurements.f90:211-235, prn_averages.f90:118) */

@@ -32,7 +32,7 @@ int mixed_init(Sim &s);  // llg_mixed.cu
 void mixed_free(Sim &s);
 int mixed_ready(Sim &s);
 int mixed_step(Sim &s, int64_t step_offset, int phase);
-int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps);
+int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak = nullptr);
 int mixed_coefficients(Sim &s);
 
 namespace {
@@ -360,7 +360,7 @@ void destroy(Sim &s) {
     HamDev &h = s.ham;
     void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
-                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm, s.stage};
+                    s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm, s.stage, s.tk, s.betak};
     for (void *q : ptrs) cudaFree(q);
     free_vec3(h.ext);
     free_vec3(s.e);
@@ -674,6 +674,98 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t 
                                           : uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
     if (rc) return rc;
     if (uppasd::structured(s)) return uppasd::structured_load_state(s);
+    return UPPASD_GPU_OK;
+}
+
+}  // extern "C"
+
+namespace uppasd {
+namespace {
+// per-ensemble temperatures (K) and muB / (kB T) to the device
+int upload_temps(Sim &s, const double *temps) {
+    const int M = s.ham.mensemble;
+    for (int k = 0; k < M; ++k)
+        if (!(temps[k] > 0.0) || !std::isfinite(temps[k])) {
+            set_error("temperatures must be finite and > 0");
+            return UPPASD_GPU_EINVAL;
+        }
+    if (!s.tk) {
+        UPPASD_CUDA_TRY(cudaMalloc(&s.tk, M * sizeof(double)));
+        UPPASD_CUDA_TRY(cudaMalloc(&s.betak, M * sizeof(float)));
+    }
+    std::vector<float> b(M);
+    for (int k = 0; k < M; ++k) b[k] = (float)(kMub / (kKbolt * temps[k]));
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    UPPASD_CUDA_TRY(cudaMemcpy(s.tk, temps, M * sizeof(double), cudaMemcpyHostToDevice));
+    UPPASD_CUDA_TRY(cudaMemcpy(s.betak, b.data(), M * sizeof(float), cudaMemcpyHostToDevice));
+    return UPPASD_GPU_OK;
+}
+
+int sweeps_with_temps(Sim &s, char mode, int64_t nsweeps) {
+    int rc;
+    if (structured(s) && (rc = structured_sync_state(s))) return rc;
+    rc = s.precision == 3 && mode == 'H' ? mixed_heat_bath_sweeps(s, 0.0, nsweeps, s.betak)
+                                         : mc_checkerboard_sweeps(s, mode, 0.0, nsweeps, s.tk);
+    if (rc) return rc;
+    if (structured(s)) return structured_load_state(s);
+    return UPPASD_GPU_OK;
+}
+}  // namespace
+}  // namespace uppasd
+
+extern "C" {
+
+int uppasd_gpu_mc_run_temps(uppasd_gpu_sim *w, char mode, const double *temps, int64_t nsweeps) {
+    if (!w || !temps || nsweeps < 0 || (mode != 'M' && mode != 'H')) {
+        uppasd::set_error("mc_run_temps: mode 'M' or 'H', one temperature per ensemble, nsweeps >= 0");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    int rc = uppasd::upload_temps(s, temps);
+    return rc ? rc : uppasd::sweeps_with_temps(s, mode, nsweeps);
+}
+
+int uppasd_gpu_pt_run(uppasd_gpu_sim *w, double *temps, int64_t nsweeps, int32_t pt_step, int64_t *n_trial,
+                      int64_t *n_hit, int32_t *selected) {
+    if (!w || !temps || nsweeps < 0 || pt_step < 1) {
+        uppasd::set_error("pt_run: one temperature per ensemble, nsweeps >= 0, pt_step >= 1");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    const int M = s.ham.mensemble;
+    std::vector<double> T(temps, temps + M), E(M), u(M);
+    int64_t trial = 0, hit = 0;
+    int rc = uppasd::upload_temps(s, T.data());
+    for (int64_t step = 1; step <= nsweeps && !rc; ++step) {
+        if ((rc = uppasd::sweeps_with_temps(s, 'H', 1))) break;
+        // swap attempts every pt_step sweeps during the first 90 % (pt_driver.f90:196-233)
+        if (step % pt_step || step / (1.0 * nsweeps) >= 0.90) continue;
+        if ((rc = uppasd::observables(s, nullptr, nullptr, E.data(), nullptr))) break;
+        for (int r = 0; r < M; ++r) u[r] = uppasd::u01_open(uppasd::philox_draw(s.llg.seed, r, 0, step, uppasd::kStreamPT).x);
+        bool swapped = false;
+        for (int ishift = 0; ishift < 2; ++ishift)
+            for (int r = ishift; r + 1 < M; r += 2) {
+                ++trial;
+                const double b1 = 1.0 / uppasd::kKbolt / (T[r] + 1.0e-15), b2 = 1.0 / uppasd::kKbolt / (T[r + 1] + 1.0e-15);
+                const double e1 = E[r] * uppasd::kMry, e2 = E[r + 1] * uppasd::kMry;  // J per atom
+                const double prob = std::min(1.0, exp((e2 - e1) * (b2 - b1)));
+                if (u[r] <= prob) {
+                    std::swap(T[r], T[r + 1]);
+                    ++hit;
+                    swapped = true;
+                }
+            }
+        if (swapped) rc = uppasd::upload_temps(s, T.data());
+    }
+    if (!rc) rc = uppasd::observables(s, nullptr, nullptr, E.data(), nullptr);
+    if (rc) return rc;
+    int sel = 0;
+    for (int r = 1; r < M; ++r)
+        if (E[r] < E[sel]) sel = r;
+    std::copy(T.begin(), T.end(), temps);
+    if (n_trial) *n_trial = trial;
+    if (n_hit) *n_hit = hit;
+    if (selected) *selected = sel;
     return UPPASD_GPU_OK;
 }
 

@@ -16,7 +16,7 @@ constexpr double kMry = 2.179872325e-21;   // J
 constexpr double kPi = 3.141592653589793238462643383279502884197;
 
 // Philox streams: one per consumer so draws never collide.
-enum : uint32_t { kStreamLLG = 0u, kStreamMC = 1u, kStreamMCGauss = 2u, kStreamLearned = 3u };
+enum : uint32_t { kStreamLLG = 0u, kStreamMC = 1u, kStreamMCGauss = 2u, kStreamLearned = 3u, kStreamPT = 8u };
 
 struct Philox4 {
     uint32_t x, y, z, w;

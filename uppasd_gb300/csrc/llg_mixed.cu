@@ -360,11 +360,11 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
 
 // Heat bath of one colour (flip_h, MonteCarlo/montecarlo_common.f90:371-422) on the
 // FP32 mirror: the field over the caller's neighbour lists, the draw in FP32 with the
-// FP64 path's Philox counters (site, ensemble, sweep), the new spin written to the
-// mirror and to e / eM.  Same checkerboard chain as mc_colour_kernel.
+// FP64 path's Philox counters (site, ensemble, sweep), the new spin renormalised in
+// FP64 and written to e / eM and the mirror.  Same checkerboard chain as mc_colour_kernel.
 __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec3D e, Vec3D eM, const double *mmom,
                                                        const int32_t *sites, int nsites, float beta_mub,
-                                                       uint64_t seed, int64_t sweep) {
+                                                       const float *betak, uint64_t seed, int64_t sweep) {
     const int N = h.natom;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nsites * h.mensemble) return;
@@ -378,15 +378,21 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec
     const Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
     const float k32 = 2.3283064365386963e-10f;
     const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
-    const float3 n = heat_bath_f32(make_float3(B[0], B[1], B[2]), beta_mub * mm, q, fp);
-    mt[o] = make_float4(n.x, n.y, n.z, mm);
+    const float3 n = heat_bath_f32(make_float3(B[0], B[1], B[2]), (betak ? betak[k] : beta_mub) * mm, q, fp);
+    // the FP64 state gets the draw renormalised in FP64, as the LLG steps leave it
+    double x = n.x, y = n.y, z = n.z;
+    const double sc = renorm_scale(fma(z, z, fma(y, y, x * x)) - 1.0);
+    x *= sc;
+    y *= sc;
+    z *= sc;
+    mt[o] = make_float4((float)x, (float)y, (float)z, mm);
     const double md = mmom[o];
-    e.x[o] = n.x;
-    e.y[o] = n.y;
-    e.z[o] = n.z;
-    eM.x[o] = md * n.x;
-    eM.y[o] = md * n.y;
-    eM.z[o] = md * n.z;
+    e.x[o] = x;
+    e.y[o] = y;
+    e.z[o] = z;
+    eM.x[o] = md * x;
+    eM.y[o] = md * y;
+    eM.z[o] = md * z;
 }
 
 __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n) {
@@ -501,7 +507,7 @@ int mixed_ready(Sim &s) {
 }
 
 // precision 3 heat-bath sweeps (mc_run mode 'H')
-int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps) {
+int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak) {
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");
         return UPPASD_GPU_ESTATE;
@@ -509,14 +515,15 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps) {
     int rc = mixed_ready(s);
     if (rc) return rc;
     s.sqm_valid = 0;  // the square path's mirror does not follow these updates
-    const float beta_mub = (float)(kMub / (kKbolt * temperature));
+    const float beta_mub = betak ? 0.f : (float)(kMub / (kKbolt * temperature));
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
         for (int c = 0; c < s.ncolour; ++c) {
             const int beg = s.colour_start_h[c], n = s.colour_start_h[c + 1] - beg;
             if (n == 0) continue;
             const int64_t tot = (int64_t)n * s.ham.mensemble;
             mixed_heat_bath<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
-                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, s.llg.seed, s.mc_sweep);
+                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, betak, s.llg.seed,
+                s.mc_sweep);
         }
         s.mc_sweep += 1;
     }

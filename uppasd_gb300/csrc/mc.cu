@@ -137,13 +137,17 @@ __device__ __forceinline__ void heat_bath(double mm, double temperature, double 
 
 __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D eM, const double *mmom,
                                                         const int32_t *sites, int nsites, int heatbath,
-                                                        double temperature, double delta, uint64_t seed,
-                                                        int64_t sweep) {
+                                                        double temperature, double delta, const double *tk,
+                                                        uint64_t seed, int64_t sweep) {
     const int N = h.natom;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nsites * h.mensemble) return;
     const int k = (int)(t / nsites);
     const int i = sites[t - (int64_t)k * nsites];
+    if (tk) {  // one temperature per ensemble (replicas of pt_iphase)
+        temperature = tk[k];
+        if (!heatbath) delta = (double)(2.0f / 25.0f) * pow(kKbolt * temperature / kMub, 0.20);
+    }
     const size_t o = (size_t)k * N + i;
     Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
     double u[4] = {u01_open(w.x), u01_open(w.y), u01_open(w.z), u01_open(w.w)};
@@ -172,7 +176,7 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
     eM.z[o] = mm * nm[2];
 }
 
-int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps) {
+int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps, const double *tk) {
     square_mirror_stale(s);
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");
@@ -188,7 +192,7 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
             if (n == 0) continue;
             int64_t tot = (int64_t)n * s.ham.mensemble;
             mc_colour_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
-                s.ham, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, hb, temperature, delta, s.llg.seed,
+                s.ham, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, hb, temperature, delta, tk, s.llg.seed,
                 s.mc_sweep);
         }
         s.mc_sweep += 1;

@@ -116,6 +116,9 @@ struct Sim {
     MixedDev mix;
     // (3, natom, mensemble) staging array of the host transfers, kept between calls
     double *stage = nullptr;
+    // per-ensemble temperatures of mc_run_temps / pt_run: K and muB / (kB T) (FP32)
+    double *tk = nullptr;
+    float *betak = nullptr;
     // scratch for observables
     double *red = nullptr;             // [mensemble][8]
     size_t bytes_allocated = 0;
@@ -140,7 +143,8 @@ int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const 
                 double *terms_h = nullptr);
 int field_to_host(Sim &s, double *beff_h);
 // mc.cu
-int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps);
+// tk: temperature per ensemble on the device (nullptr: `temperature` for all)
+int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps, const double *tk = nullptr);
 // mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
 int square_recognise(Sim &s, int L);
 int square_mirror_ready(Sim &s);  // builds the FP32 mirror from e when it is stale

@@ -179,6 +179,24 @@ class GpuSimulation:
             return
         _lib.call("uppasd_gpu_mc_run", self._h, mode.encode()[:1], float(temperature), int(nsweeps))
 
+    def relax_temps(self, mode: str, temps, nsweeps: int):
+        """Monte Carlo sweeps with one temperature per ensemble."""
+        t = np.ascontiguousarray(temps, dtype=np.float64)
+        if t.shape != (self.lat.mensemble,):
+            raise ValueError("one temperature per ensemble")
+        _lib.call("uppasd_gpu_mc_run_temps", self._h, mode.encode()[:1], _ptr(t), int(nsweeps))
+
+    def parallel_tempering(self, temps, nsweeps: int, pt_step: int = 1):
+        """pt_iphase with the ensembles as replicas: returns (temperatures per replica at the
+        end, swap trials, accepted swaps, replica of lowest energy)."""
+        t = np.array(temps, dtype=np.float64)
+        if t.shape != (self.lat.mensemble,):
+            raise ValueError("one temperature per ensemble")
+        nt, nh, sel = C.c_int64(), C.c_int64(), C.c_int32()
+        _lib.call("uppasd_gpu_pt_run", self._h, _ptr(t), int(nsweeps), int(pt_step), C.byref(nt), C.byref(nh),
+                  C.byref(sel))
+        return t, nt.value, nh.value, sel.value
+
     def set_stream(self, cuda_stream_handle: int):
         """Issue all work on the caller's CUDA stream (0 = the library's own)."""
         _lib.call("uppasd_gpu_set_stream", self._h, C.c_void_p(cuda_stream_handle or None))
