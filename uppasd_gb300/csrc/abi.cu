@@ -120,9 +120,9 @@ int check_device(Sim &s) {
 }
 
 // Colouring of the coupling graph so that same-colour sites share no bond.
-// Tries the cell-parity x sublattice colouring first (exact for the simple
-// and bcc lattices with nearest and next-nearest shells), verifies it, and
-// falls back to greedy colouring.
+// Tries the sublattices alone, then cell parity x sublattice (exact for the
+// simple and bcc lattices with nearest and next-nearest shells), verifying each,
+// and falls back to greedy colouring.
 int build_colouring(Sim &s, const uppasd_gpu_consts *c, const std::vector<int32_t> &nlT,
                     const std::vector<int32_t> &nsize, const std::vector<int32_t> &dmT,
                     const std::vector<int32_t> &dmsize) {
@@ -139,13 +139,20 @@ int build_colouring(Sim &s, const uppasd_gpu_consts *c, const std::vector<int32_
     };
     bool done = false;
     if (c->n1 > 0 && c->n2 > 0 && c->n3 > 0 && c->na > 0 && (int64_t)c->n1 * c->n2 * c->n3 * c->na == N) {
+        // the sublattices alone (kagome, honeycomb, bcc with nearest neighbours only),
+        // then sublattice x cell parity
         std::vector<int32_t> cand(N);
-        for (int i = 0; i < N; ++i) {
+        for (int i = 0; i < N; ++i) cand[i] = i % c->na;
+        if (c->na > 1 && ok(cand)) {
+            col = cand;
+            done = true;
+        }
+        for (int i = 0; i < N && !done; ++i) {
             int b = i % c->na, cell = i / c->na;
             int x = cell % c->n1, y = (cell / c->n1) % c->n2, z = cell / (c->n1 * c->n2);
             cand[i] = b * 2 + ((x + y + z) & 1);
         }
-        if (ok(cand)) {
+        if (!done && ok(cand)) {
             col = cand;
             done = true;
         }

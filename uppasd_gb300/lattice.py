@@ -338,9 +338,9 @@ def kagome(L: int, j_mry: float = -1.0, d_mry: float = 0.1, g_mry: float = 0.05,
 def greedy_colouring(lat: Lattice):
     """Colour sites so that no two coupled sites (exchange or DMI) share a colour.
 
-    Returns (colour_of_site, colour_sites, colour_start).  Uses the sublattice /
-    cell-parity structure first (exact for the shipped lattices) and verifies
-    it; falls back to a greedy colouring of the coupling graph.
+    Returns (colour_of_site, colour_sites, colour_start).  Tries the sublattices
+    alone, then sublattice x cell parity (exact for the shipped lattices), verifying
+    each; falls back to a greedy colouring of the coupling graph.
     """
     n = lat.natom
     nl = lat.nlist.astype(np.int64) - 1
@@ -352,9 +352,13 @@ def greedy_colouring(lat: Lattice):
         b = idx % lat.nbasis
         c = idx // lat.nbasis
         x, y, z = c % n1, (c // n1) % n2, c // (n1 * n2)
-        cand = (b * 2 + ((x + y + z) % 2)).astype(np.int32)
-        if _colouring_ok(cand, nl, mask, lat):
-            col = cand
+        # the sublattices alone, then sublattice x cell parity (the library's order)
+        if lat.nbasis > 1 and _colouring_ok(b.astype(np.int32), nl, mask, lat):
+            col = b.astype(np.int32)
+        else:
+            cand = (b * 2 + ((x + y + z) % 2)).astype(np.int32)
+            if _colouring_ok(cand, nl, mask, lat):
+                col = cand
     if col is None:
         col = np.full(n, -1, dtype=np.int32)
         for i in range(n):
