@@ -16,7 +16,7 @@ import re
 import sys
 
 CASES = [
-    # (name, workingdir, outfile, select value, comparison)
+    # (name, workingdir, outfile, select value (iteration, or iteration and projection), comparison)
     ("solvers_midpoint", "./Solvers", "averages.1", 8000, "similar"),
     ("solvers_heun", "./Solvers", "averages.4", 8000, "similar"),
     ("solvers_depondt", "./Solvers", "averages.5", 8000, "similar"),
@@ -28,10 +28,29 @@ CASES = [
     ("bccfe_mc_cumulants", "./bccFe/", "./cumulants.M", 41, "similar"),
     ("bccfe_hb_iter0", "./bccFe/", "./averages.H", 0, "sloppy"),
     ("bccfe_hb_iter2700", "./bccFe/", "./averages.H", 2700, "sloppy"),
+    ("heisstripe_iter1190", "./HeisStripe", "averages.HeisStri.out", 1190, "similar"),
+    ("heisstripe_energy1460", "./HeisStripe", "./totenergy.HeisStri.out", 1460, "similar"),
+    ("kagome_iter13000", "./kagome", "averages.kagome_T.out", 13000, "similar"),
+    ("kagome_traj2400", "./kagome", "trajectory.kagome_T.001.1.out", 2400, "similar"),
+    ("heischain_iter1000", "./HeisChain", "averages.HeisWire.out", 1000, "similar"),
+    ("heischain_energy1400", "./HeisChain", "totenergy.HeisWire.out", 1400, "similar"),
+    ("heischainaf_iter1000", "./HeisChainAF", "./averages.AF_WireT.out", 1000, "similar"),
+    ("heischainaf_proj5000_type1", "./HeisChainAF", "./projavgs.AF_WireT.out", (5000, 1), "similar"),
+    ("heischainaf_proj5000_type2", "./HeisChainAF", "./projavgs.AF_WireT.out", (5000, 2), "similar"),
+    ("heischainaf_energy1500", "./HeisChainAF", "./totenergy.AF_WireT.out", 1500, "similar"),
+    ("feco_iter4700", "./FeCo/", "./averages.test", 4700, "sloppy"),
+    ("feco_cumulants221", "./FeCo/", "./cumulants.test", 221, "sloppy"),
 ]
 
 
+def _bracketed(line):
+    """The [...] list of a YAML `key: [...]  # comment` line."""
+    v = line.split(":", 1)[1]
+    return v[v.index("["):v.rindex("]") + 1]
+
+
 def extract(text, workingdir, outfile, select):
+    select, atom = select if isinstance(select, tuple) else (select, None)
     lines = text.splitlines()
     out = None
     in_case = False
@@ -39,18 +58,20 @@ def extract(text, workingdir, outfile, select):
     for n, ln in enumerate(lines):
         s = ln.strip()
         if s.startswith("- workingdir:"):
-            in_case = workingdir in s
+            in_case = s.split(":", 1)[1].split("#")[0].strip().strip('"') == workingdir
             in_file = False
         elif in_case and s.startswith("- outfile:"):
             in_file = s.split(":", 1)[1].strip() == outfile
-        elif in_case and in_file and re.match(r'"#_Iter\.":\s*%d\s*$' % select, s):
+        elif in_case and in_file and re.match(r'"#_Iter\.":\s*%d\s*(#.*)?$' % select, s):
+            if atom is not None and not re.match(r'"#_Atom"\s*:\s*%d\s*(#.*)?$' % atom, lines[n + 1].strip()):
+                continue
             extract_line = None
             for m in range(n + 1, min(n + 30, len(lines))):
                 t = lines[m].strip()
                 if t.startswith("extract:") and extract_line is None:
-                    extract_line = json.loads(t.split(":", 1)[1].strip())
+                    extract_line = json.loads(_bracketed(t))
                 if t.startswith("expected:"):
-                    vals = json.loads(t.split(":", 1)[1].strip())
+                    vals = json.loads(_bracketed(t))
                     out = {"extract": extract_line, "expected": vals}
                     break
             break
@@ -75,6 +96,41 @@ def read_inputs(testdir):
             d.setdefault(t[0].lower(), t[1:])
         return d
 
+    def nums(fn):
+        return [[float(v.replace("d", "e").replace("D", "e")) for v in r] for r in rows(fn)]
+
+    def system(d):
+        """Keywords and tables of one test directory (Cartesian posfile, maptype 1)."""
+        k = keys(d + "/inpsd.dat")
+        lines = [ln.split() for ln in open(os.path.join(testdir, d, "inpsd.dat"))]
+        heads = [t[0].lower() if t else "" for t in lines]
+        c0 = heads.index("cell")
+        cell = [[float(v) for v in lines[c0][1:4]]] + [[float(v) for v in lines[c0 + q][0:3]] for q in (1, 2)]
+        pos = {int(r[0]): r for r in nums(d + "/posfile")}
+        mom = {int(r[0]): r for r in nums(d + "/momfile")}
+        sites = [[pos[i][1]] + pos[i][2:5] + mom[i][2:6] for i in sorted(pos)]
+        out = {"ncell": [int(v) for v in k["ncell"][:3]], "bc": k["bc"][:3], "cell": cell,
+               "sym": int(k.get("sym", ["0"])[0]), "sites": sites,
+               "jfile": nums(d + "/" + os.path.basename(k["exchange"][0])),
+               "damping": float(k["damping"][0]), "temp": float(k["temp"][0]),
+               "timestep": float(k["timestep"][0].replace("d", "e")), "nstep": int(k["nstep"][0]),
+               "initmag": int(k["initmag"][0]), "sdealgh": int(k.get("sdealgh", ["1"])[0]),
+               "do_reduced": k.get("do_reduced", ["N"])[0].upper() == "Y", "tseed_default": 1,
+               "maptype": int(k.get("maptype", ["1"])[0]),
+               "source": f"tests/{d}/inpsd.dat and the files it names"}
+        if "dm" in k:
+            out["dmfile"] = nums(d + "/" + os.path.basename(k["dm"][0]))
+        if "anisotropy" in k:
+            out["kfile"] = nums(d + "/" + os.path.basename(k["anisotropy"][0]))
+        if "ip_nphase" in heads and k.get("ip_mode", ["N"])[0].upper() == "S":
+            q = heads.index("ip_nphase")
+            out["ip_phases"] = [[float(v.replace("d", "e")) for v in lines[q + 1 + p][:4]]
+                                for p in range(int(lines[q][1]))]
+        if "restartfile" in k:
+            rs = nums(d + "/" + os.path.basename(k["restartfile"][0]))
+            out["restart"] = [r[3:7] for r in rs]   # |m|, m_x, m_y, m_z per atom
+        return out
+
     sol = keys("Solvers/inpsd.dat.base")
     sj = rows("Solvers/jfile")[0]
     sm = rows("Solvers/momfile")[0]
@@ -96,6 +152,13 @@ def read_inputs(testdir):
                   "timestep_default_real4": 1.0e-16, "avrg_step": int(bfe["avrg_step"][0]),
                   "cumu_step": int(bfe["cumu_step"][0]), "cumu_buff": int(bfe["cumu_buff"][0]),
                   "source": "tests/bccFe/{inpsd.dat.base,jfile,momfile}; Input/inputdata.f90:457"},
+        "heisstripe": system("HeisStripe"),
+        "kagome": system("kagome"),
+        "heischain": system("HeisChain"),
+        "heischainaf": system("HeisChainAF"),
+        "feco": dict(system("FeCo"), cumu_step=int(keys("FeCo/inpsd.dat")["cumu_step"][0]),
+                     cumu_buff=int(keys("FeCo/inpsd.dat")["cumu_buff"][0]),
+                     avrg_step=int(keys("FeCo/inpsd.dat").get("avrg_step", ["100"])[0])),
     }
 
 
@@ -106,7 +169,8 @@ def main():
     for name, wd, of, sel, cmp in CASES:
         e = extract(text, wd, of, sel)
         e["comparison"] = cmp
-        e["source"] = f"tests/regulartests.yaml {wd} {of} #_Iter.={sel}"
+        e["source"] = f"tests/regulartests.yaml {wd} {of} #_Iter.={sel}" if not isinstance(sel, tuple) else \
+            f"tests/regulartests.yaml {wd} {of} #_Iter.={sel[0]} #_Atom={sel[1]}"
         pins[name] = e
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_pins.json")
     with open(dst, "w") as f:

@@ -143,3 +143,149 @@ def test_bccfe_mc_cumulants(pins):
 
     out = _cumulant_row(o, lat, inp, step, 41)
     _check(out, pins["bccfe_mc_cumulants"])
+
+
+def from_tables(inp):
+    """The lattice of a reference test directory, from the tables make_golden.py stored."""
+    return lattice.from_tables(inp["cell"], inp["ncell"], inp["bc"], inp["sites"], inp["jfile"], sym=inp["sym"],
+                               dmfile=inp.get("dmfile"), kfile=inp.get("kfile"), reduce=inp["do_reduced"],
+                               maptype=inp.get("maptype", 1))
+
+
+def restart_moments(inp):
+    """Initmag 4: the restart file's moments, normalised (System/restart.f90:320-381)."""
+    r = np.asarray(inp["restart"], dtype=np.float64)
+    return (r[:, 1:4] / np.sqrt(np.sum(r[:, 1:4] ** 2, axis=1))[:, None])[None]
+
+
+def _energy_columns(e, pin):
+    cols = {"E_tot": e["total"], "E_xc": e["xc"], "E_ani": e["ani"], "E_DM": e["dm"]}
+    return [float(cols[c][0]) for c in pin["extract"]]
+
+
+def test_heisstripe(pins):
+    """tests/HeisStripe: 10 x 1 x 100 simple-cubic stripe, vacuum in x and y (edge atoms keep 3
+    of the 4 neighbours the cubic images of (0, 0, 1) give), uniaxial anisotropy along y,
+    midpoint at T = 0 from the mtprng initmag-1 draw: <m> after 1190 steps and the
+    totenergy columns E_tot, E_xc, E_ani after 1460."""
+    inp = pins["inputs"]["heisstripe"]
+    lat, _ = from_tables(inp)
+    assert sorted(set(lat.nlistsize.tolist())) == [3, 4]
+    o = po.Oracle(lat, threads=1)
+    o.init_random(inp["tseed_default"])
+    o.setup_ziggurat(inp["tseed_default"])
+    o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    for _ in range(1190):
+        o.sd_step()
+    mv, ma = o.mavg()
+    _check(list(mv[0] / lat.natom) + [ma[0]], pins["heisstripe_iter1190"])
+    for _ in range(1460 - 1190):
+        o.sd_step()
+    _check(_energy_columns(o.energy(), pins["heisstripe_energy1460"]), pins["heisstripe_energy1460"])
+
+
+def test_kagome(pins):
+    """tests/kagome: 12 x 12 kagome cells, exchange and DMI from the jfile / dmfile, reduced
+    Hamiltonian (three coupling rows), Initmag 3, midpoint at T = 0: the trajectory of
+    atom 2 after 2400 steps and <m> after 13000."""
+    inp = pins["inputs"]["kagome"]
+    lat, e0 = from_tables(inp)
+    assert lat.nham == 3 and lat.do_dm
+    o = po.Oracle(lat, threads=1)
+    o.set_moments(e0)
+    o.setup_ziggurat(inp["tseed_default"])
+    o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    for _ in range(2400):
+        o.sd_step()
+    pin = pins["kagome_traj2400"]
+    _check([2.0] + list(o.emom[0, 1]) + [o.mmom[0, 1]], pin)
+    for _ in range(13000 - 2400):
+        o.sd_step()
+    mv, ma = o.mavg()
+    _check(list(mv[0] / lat.natom) + [ma[0]], pins["kagome_iter13000"])
+
+
+def test_heischain(pins):
+    """tests/HeisChain: 100-spin chain from its restart file (Initmag 4), an initial phase of
+    20000 midpoint steps at 0.1 K with damping 4 on the ziggurat stream, then undamped T = 0
+    precession: <m> after 1000 measurement steps and E_tot after 1400."""
+    inp = pins["inputs"]["heischain"]
+    lat, _ = from_tables(inp)
+    o = po.Oracle(lat, threads=1)
+    o.set_moments(restart_moments(inp))
+    o.setup_ziggurat(inp["tseed_default"])
+    for nstep, temp, dt, damping in inp["ip_phases"]:
+        o.make_llg(inp["sdealgh"], dt, damping, temp, 1.0, noise_mode=po.NOISE_ZIGGURAT)
+        for _ in range(int(nstep)):
+            o.sd_step()
+    o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    for _ in range(1000):
+        o.sd_step()
+    mv, ma = o.mavg()
+    _check(list(mv[0] / lat.natom) + [ma[0]], pins["heischain_iter1000"])
+    for _ in range(400):
+        o.sd_step()
+    _check(_energy_columns(o.energy(), pins["heischain_energy1400"]), pins["heischain_energy1400"])
+
+
+def test_heischainaf(pins, tmp_path):
+    """tests/HeisChainAF: ferrimagnetic chain, two basis atoms of moments 1 and 2, two shells
+    per type from the cubic images of the jfile vectors, midpoint at T = 0 from the mtprng
+    initmag-1 draw: <m> after 1000 steps, E_tot after 1500 and the per-type projected
+    averages after 5000, read back from a projavgs file by the suite's columns."""
+    inp = pins["inputs"]["heischainaf"]
+    lat, _ = from_tables(inp)
+    o = po.Oracle(lat, threads=1)
+    o.init_random(inp["tseed_default"])
+    o.setup_ziggurat(inp["tseed_default"])
+    o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    for _ in range(1000):
+        o.sd_step()
+    mv, ma = o.mavg()
+    _check(list(mv[0] / lat.natom) + [ma[0]], pins["heischainaf_iter1000"])
+    for _ in range(500):
+        o.sd_step()
+    _check(_energy_columns(o.energy(), pins["heischainaf_energy1500"]), pins["heischainaf_energy1500"])
+    for _ in range(3500):
+        o.sd_step()
+    check_projavgs(o.emomM, lat, inp, pins, str(tmp_path / "projavgs.AF_WireT.out"))
+
+
+def check_projavgs(emomM, lat, inp, pins, path):
+    from uppasd_gb300 import output
+    types = [int(s[0]) for s in inp["sites"]]
+    output.ProjAvgsFile(path, types, int(np.prod(inp["ncell"]))).write(5000, emomM)
+    cols = ["#_Iter.", "#_Atom", "M_avg", "M_avg_d", "M_avg_x", "M_avg_y", "M_avg_z"]
+    rows = output.read_columns(path)
+    for t in (1, 2):
+        row = dict(zip(cols, rows[(rows[:, 0] == 5000) & (rows[:, 1] == t)][0]))
+        pin = pins["heischainaf_proj5000_type%d" % t]
+        _check([row[c] for c in pin["extract"]], pin)
+
+
+def test_feco(pins):
+    """tests/FeCo: B2 FeCo, 6^3 cells, two species of moments 2.72 and 1.72, 258 neighbours per
+    atom from a maptype-2 exchange table (cell offsets), reduced Hamiltonian, Initmag 3 with
+    canted sublattices, midpoint at T = 0 with damping 0.001: the cumulant row 221 (sampled
+    every 20 steps) and <M> after 4700 steps, both compared as the suite does (``sloppy``).
+    The cumulants agree with the reference's to all printed digits; <M> differs by 2e-4."""
+    inp = pins["inputs"]["feco"]
+    lat, e0 = from_tables(inp)
+    assert lat.nham == 2 and lat.max_no_neigh == 258
+    o = po.Oracle(lat, threads=1)
+    o.set_moments(e0)
+    o.setup_ziggurat(inp["tseed_default"])
+    o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    steps = {"n": 0}
+
+    def step(s):
+        o.sd_step()
+        steps["n"] += 1
+
+    out = _cumulant_row(o, lat, inp, step, 221)
+    _check(out[:4], pins["feco_cumulants221"])
+    assert np.allclose(out[:4], pins["feco_cumulants221"]["expected"], rtol=5e-9, atol=0)
+    for _ in range(4700 - steps["n"]):
+        o.sd_step()
+    mv, ma = o.mavg()
+    _check([ma[0]], pins["feco_iter4700"])

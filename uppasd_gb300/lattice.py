@@ -257,6 +257,186 @@ def square_dmi(L: int, j_mry: float = 1.0, d_mry: float = 0.3, k_mry: float = -0
                    stencil=np.array([[s[:4] for s in stencil[0]]], dtype=np.int32))
 
 
+def cubic_images(r, tol: float = 1.0e-5):
+    """The distinct images of bond vector r under the 48 cubic operations, in the order
+    get_symops (isym = 1) generates the operations and get_fullnnlist keeps the first of
+    equal images (Hamiltonian/neighbourmap.f90:392-414, :560-640)."""
+    r = np.asarray(r, dtype=np.float64)
+    out = []
+    for i in (1, 2, 3):
+        for js in (1, -1):
+            for x in (0, 1):
+                for y in (0, 1):
+                    for z in (0, 1):
+                        s = np.zeros((3, 3))
+                        s[0, (i - js) % 3] = (-1.0) ** x
+                        s[1, i % 3] = (-1.0) ** y
+                        s[2, (i + js) % 3] = (-1.0) ** z
+                        t = s @ r
+                        if all(np.sum((t - u) ** 2) >= tol for u in out):
+                            out.append(t)
+    return out
+
+
+def _table_neighbours(cell, ncell, periodic, pos, types, shells):
+    """Neighbour lists of a Bravais lattice with a basis, in the reference's order.
+
+    shells[t] lists (image vectors, neighbour type or None) per shell of atom type t.
+    For each atom, shells in order, images in order; a neighbour outside a vacuum
+    boundary is dropped and one already in the list is not added again (map_multiple
+    off), as setup_nm and setup_neighbour_hamiltonian do (Hamiltonian/neighbourmap.f90:
+    180-300, Hamiltonian/hamiltonianinit.f90:1044-1092).  Returns 1-based nlist,
+    nlistsize and, per slot, the shell index (0-based, -1 when empty)."""
+    na = len(pos)
+    n1, n2, n3 = ncell
+    natom = na * n1 * n2 * n3
+    cmat = np.asarray(cell, dtype=np.float64).T   # columns C1, C2, C3
+    stencil = []
+    for b in range(na):
+        st = []
+        for k, (images, jtype) in enumerate(shells[types[b]]):
+            for v in images:
+                for b2 in range(na):
+                    if jtype is not None and types[b2] != jtype:
+                        continue
+                    f = np.linalg.solve(cmat, pos[b] + v - pos[b2])
+                    if np.all(np.abs(f - np.rint(f)) < 1.0e-4):
+                        d = np.rint(f).astype(np.int64)
+                        st.append((int(d[0]), int(d[1]), int(d[2]), b2, k))
+                        break
+        stencil.append(st)
+    mnn = max(1, max(len(s) for s in stencil))
+    nlist = np.zeros((natom, mnn), dtype=np.int32)
+    shell = np.full((natom, mnn), -1, dtype=np.int32)
+    nsize = np.zeros(natom, dtype=np.int32)
+    idx = np.arange(natom, dtype=np.int64)
+    bb, cidx = idx % na, idx // na
+    x, y, z = cidx % n1, (cidx // n1) % n2, cidx // (n1 * n2)
+    for b in range(na):
+        sel = np.nonzero(bb == b)[0]
+        for dx, dy, dz, b2, k in stencil[b]:
+            xx, yy, zz = x[sel] + dx, y[sel] + dy, z[sel] + dz
+            ok = np.ones(sel.size, dtype=bool)
+            for vv, nn, per in ((xx, n1, periodic[0]), (yy, n2, periodic[1]), (zz, n3, periodic[2])):
+                if per:
+                    vv %= nn
+                else:
+                    ok &= (vv >= 0) & (vv < nn)
+            j = _site_index(b2, xx, yy, zz, na, n1, n2) + 1
+            rows, j = sel[ok], j[ok]
+            fresh = ~np.any(nlist[rows] == j[:, None].astype(np.int32), axis=1)
+            rows, j = rows[fresh], j[fresh]
+            slot = nsize[rows]
+            nlist[rows, slot] = j
+            shell[rows, slot] = k
+            nsize[rows] += 1
+    return nlist, nsize, shell
+
+
+def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=None, reduce: bool = False,
+                maptype: int = 1):
+    """A Hamiltonian built from the reference's own input tables: the ``cell``, ``ncell``,
+    ``BC`` and ``Sym`` keywords of inpsd.dat, the posfile and momfile rows (``sites``:
+    per basis site ``(type, x, y, z, mom, ex, ey, ez)``, Cartesian, posfiletype 'C'),
+    jfile rows ``(isite, jsite, rx, ry, rz, J)`` (Cartesian bond vectors, maptype 1, or
+    cell offsets n1 n2 n3 from site isite to site jsite, maptype 2:
+    r = Bas(jsite) - Bas(isite) + n1 C1 + n2 C2 + n3 C3, read_exchange_getNeighVec),
+    optional dmfile rows ``(isite, jsite, rx, ry, rz, Dx, Dy, Dz)`` (Sym 0) and kfile rows
+    ``(isite, type, K1, K2, ex, ey, ez, ratio)``; J, D and K in mRy, no chemical disorder.
+
+    Shells follow read_exchange (Input/inputhandler_ext.f90:444-618): per atom type, one
+    shell per distinct bond vector in file order, a repeated vector overwriting the
+    coupling, the neighbour's type fixed by the jsite column; each shell is expanded by
+    the lattice symmetry (``cubic_images`` for Sym 1).  Couplings are scaled by
+    2 mRy/muB/(m_i m_j) (zero when m_i m_j < 1e-6), anisotropies by mRy/muB/m^2, m^4
+    (uniaxial) or m^4, m^6 (cubic) (Hamiltonian/hamiltonianinit.f90:895-909, :1060-1068).
+    ``reduce`` gives the reduced Hamiltonian (do_reduced 'Y').
+
+    Returns the lattice and the momfile directions normalised per atom (Initmag 3)."""
+    sites = [tuple(float(v) for v in s) for s in sites]
+    na = len(sites)
+    types = [int(s[0]) for s in sites]
+    pos = [np.array(s[1:4]) for s in sites]
+    moms = np.array([s[4] for s in sites])
+    periodic = tuple(str(c).upper() == "P" for c in bc)
+    if maptype not in (1, 2):
+        raise ValueError("maptype 1 (Cartesian bond vectors) and 2 (cell offsets) are supported")
+    if sym not in (0, 1):
+        raise ValueError("Sym 0 (none) and 1 (cubic) are supported")
+    expand = (lambda r: [np.asarray(r, dtype=np.float64)]) if sym == 0 else cubic_images
+
+    def read_shells(rows, width):
+        shells, values = {t: [] for t in set(types)}, {t: [] for t in set(types)}
+        for row in rows:
+            isite, jsite = int(row[0]), int(row[1])
+            it, jt = types[isite - 1], types[jsite - 1]
+            r = np.array([float(v) for v in row[2:5]])
+            if maptype == 2:
+                r = pos[jsite - 1] - pos[isite - 1] + np.asarray(cell, dtype=np.float64).T @ r
+            val = np.array([float(v) for v in row[5:5 + width]])
+            for k, (r0, _) in enumerate(shells[it]):
+                if np.sum((r - r0) ** 2) < 1.0e-5:
+                    values[it][k] = val
+                    break
+            else:
+                shells[it].append((r, jt))
+                values[it].append(val)
+        return ({t: [(expand(r), jt) for r, jt in v] for t, v in shells.items()}, values)
+
+    natom = na * int(np.prod(ncell))
+    b_of = np.arange(natom) % na
+    m_of = moms[b_of]
+
+    def coupled(rows, width):
+        shells, values = read_shells(rows, width)
+        nl, ns, sh = _table_neighbours(cell, ncell, periodic, pos, types, shells)
+        c = np.zeros(nl.shape + (width,))
+        for i_b in range(na):
+            t = types[i_b]
+            for k, val in enumerate(values[t]):
+                sel = (b_of[:, None] == i_b) & (sh == k)
+                ii, ss = np.nonzero(sel)
+                mj = m_of[nl[ii, ss] - 1]
+                mm = m_of[ii] * mj
+                c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, val[None, :] * FC2 / mm[:, None])
+        return nl, ns, c
+
+    nlist, nsize, c = coupled(jfile, 1)
+    lat = Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=np.ascontiguousarray(c[..., 0]),
+                  aham=np.arange(1, natom + 1, dtype=np.int32), mmom=m_of[None, :].copy(),
+                  extfield=np.zeros((1, natom, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
+                  periodic=periodic, meta={"types": types})
+    if dmfile is not None and len(dmfile):
+        if sym != 0:
+            raise ValueError("DM tables are supported with Sym 0 only")
+        dl, ds, dv = coupled(dmfile, 3)
+        lat.dmlist, lat.dmlistsize, lat.dm_vect = dl, ds, np.ascontiguousarray(dv)
+    if kfile is not None and len(kfile):
+        kt = {int(r[0]): r for r in kfile}
+        taniso = np.zeros(natom, dtype=np.int32)
+        eaniso = np.zeros((natom, 3))
+        kaniso = np.zeros((natom, 2))
+        sb = np.zeros(natom)
+        for b in range(na):
+            if b + 1 not in kt:
+                continue
+            r = [float(v) for v in kt[b + 1]]
+            sel = b_of == b
+            e = np.array(r[4:7])
+            taniso[sel] = int(r[1])
+            eaniso[sel] = e / np.sqrt(e @ e + 1.0e-15)
+            p1, p2 = (4, 6) if int(r[1]) == 2 else (2, 4)
+            kaniso[sel, 0] = FC * r[2] / moms[b] ** p1
+            kaniso[sel, 1] = FC * r[3] / moms[b] ** p2
+            sb[sel] = r[7] if len(r) > 7 else 0.0
+        lat.taniso, lat.eaniso, lat.kaniso, lat.sb = taniso, eaniso, kaniso, sb
+    if reduce:
+        lat = reduced(lat)
+    d = np.array([s[5:8] for s in sites])
+    d = d / np.sqrt(np.sum(d * d, axis=1))[:, None]
+    return lat, np.ascontiguousarray(d[b_of][None, :, :])
+
+
 def tensor_from_matrices(mats) -> np.ndarray:
     """(nham, mnn, 3, 3) matrices J[ih, j, a, b] -> the Fortran memory image of j_tens."""
     return np.ascontiguousarray(np.swapaxes(np.asarray(mats, dtype=np.float64), -1, -2))

@@ -16,6 +16,9 @@ by the reference's own regression harness (its tests read these files by column)
   with an exchange tensor the pair-energy layout, header ``(a8,11a16)``, rows
   ``(i8,11es16.8)``.  The deviation file holds calculate_mean_and_deviation's value
   (:577-602): the ensemble variance over M - 1, times mub/mry.
+* ``ProjAvgsFile`` -- ``projavgs.<simid>.out`` of prn_proj_avrg
+  (prn_averages.f90:662-804): averages projected per atom type ('Y') or per basis
+  atom ('A'), see ``projected_averages``.
 * ``write_restart`` -- the legacy ``restart.<simid>.out`` of prnrestart
   (System/restart.f90): ``(i8)`` step, then ``(i8,i8,2x,4es16.8)`` per atom.
 * ``sd_run_with_averages`` -- the measurement cadence of sd_mphase: a row every
@@ -164,6 +167,53 @@ class TotEnergyFile:
             devs = [np.sum((c / fcinv - mu / fcinv) ** 2) / (m - 1.0) * fcinv for c, mu in zip(cols, means)]
             self._write(self.std_path, index, devs)
         return means
+
+
+def projected_averages(emomM, types, ncells: int, mode: str = "Y"):
+    """The rows of prn_proj_avrg (Measurement/prn_averages.f90:462-513, :662-804): the
+    moments summed per basis atom (atom i belongs to basis atom mod(i-1, NA)+1), divided
+    by the number of cells and summed per atom type (mode 'Y') or kept per basis atom
+    ('A'); then per projection the ensemble means of the vector and of its norm and the
+    ensemble deviation of the norm.  emomM (Mensemble, Natom, 3); types: the type of
+    each basis atom (1-based).  Returns (nproj, 5) rows <M>, M_stdv, <M>_x, <M>_y, <M>_z."""
+    e = np.asarray(emomM, dtype=np.float64)
+    types = np.asarray(types, dtype=np.int64)
+    na = types.size
+    per_b = np.stack([e[:, b::na].sum(axis=1) for b in range(na)], axis=1) / ncells   # (M, NA, 3)
+    if mode.upper() == "Y":
+        proj = np.stack([per_b[:, types == t].sum(axis=1) for t in range(1, int(types.max()) + 1)], axis=1)
+    elif mode.upper() == "A":
+        proj = per_b
+    else:
+        raise ValueError("mode is 'Y' (per type) or 'A' (per basis atom)")
+    norm = np.sqrt(np.sum(proj * proj, axis=2))                                       # (M, nproj)
+    mm = norm.mean(axis=0)
+    ms = np.mean(norm * norm, axis=0) - mm * mm
+    ms = np.where(ms < 0.0, 0.0, np.sqrt(np.maximum(ms, 0.0)))
+    return np.column_stack([mm, ms, proj.mean(axis=0)])
+
+
+class ProjAvgsFile:
+    """``projavgs.<simid>.out`` of prn_proj_avrg: header ``(a8,a,5a16)``, per projection a
+    row ``(i8,i8,5es16.8)`` (``(es16.4,i8,5es16.8)`` with real time)."""
+    HEADER = ("#Iter", "Proj", "<M>", "M_{stdv}", "<M>_x", "<M>_y", "<M>_z")
+
+    def __init__(self, path: str, types, ncells: int, mode: str = "Y", real_time: bool = False):
+        self.path, self.types, self.ncells, self.mode, self.real_time = path, types, int(ncells), mode, real_time
+        self._first = not os.path.exists(path)
+
+    def write(self, index, emomM):
+        rows = projected_averages(emomM, self.types, self.ncells, self.mode)
+        with open(self.path, "a") as f:
+            if self._first:
+                head = ("Time[s]",) + self.HEADER[1:] if self.real_time else self.HEADER
+                f.write(fortran_a(head[0], 16 if self.real_time else 8) + head[1] +
+                        "".join(fortran_a(h, 16) for h in head[2:]) + "\n")
+                self._first = False
+            lead = fortran_es(index, 16, 4) if self.real_time else f"{int(index):8d}"
+            for k, r in enumerate(rows):
+                f.write(lead + f"{k + 1:8d}" + "".join(fortran_es(v) for v in r) + "\n")
+        return rows
 
 
 def write_restart(path: str, mstep: int, emom, mmom):
