@@ -102,6 +102,8 @@ int uppasd_gpu_finalize(uppasd_gpu_sim *s);
 /* Spin state transfer in the reference layout (3, natom, mensemble). */
 int uppasd_gpu_put_moments(uppasd_gpu_sim *s, const double *emom);
 int uppasd_gpu_get_moments(uppasd_gpu_sim *s, double *emom, double *emomM);
+/* Per-atom temperatures (natom).  The structured path (precision 1, 2) takes a uniform
+ * temperature only (-7 otherwise). */
 int uppasd_gpu_set_temperature(uppasd_gpu_sim *s, const double *temp_array);
 int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
 
@@ -109,6 +111,14 @@ int uppasd_gpu_set_step(uppasd_gpu_sim *s, int64_t step);
  * effective field loses its component along emom (Evolution/evolution.f90:104-112,
  * :327-335).  0 or 1; -7 on the structured path (precision 1, 2). */
 int uppasd_gpu_set_perp(uppasd_gpu_sim *s, int32_t perp);
+
+/* The physical constants fortrandata_setconstants_ passes (gama, k_bolt, mub; gpu_files/
+ * fortranData.cpp:67-98) and mry, for every LLG and Monte Carlo path of the simulation
+ * (noise amplitudes, time scale, Boltzmann factors, energies in mRy).  SI
+ * (Parameters/constants.f90:14-19) until called; aunits = 'Y' passes 1, 1, 1, 1
+ * (Input/inputhandler.f90:1685-1704).  Each must be finite and > 0.  The batched
+ * replica table (uppasd_gpu_mcbatch_*) stays in SI units. */
+int uppasd_gpu_set_units(uppasd_gpu_sim *s, double gama, double k_bolt, double mub, double mry);
 
 /* Relaxation time of the inertial regime for SDEalgh 11 (LLGI, Evolution/llgi.f90;
  * input keyword relaxtime, Input/inputhandler.f90:768, default 0).  Seconds, >= 0. */

@@ -107,8 +107,29 @@ def load():
     lib.orc_cumulant_update.argtypes = [C.POINTER(OrcCumulant), C.c_int, C.c_int, F64P, C.c_double, F64P, F64P]
     lib.orc_set_threads.argtypes = [C.c_int]
     lib.orc_get_threads.restype = C.c_int
+    lib.orc_set_units.argtypes = [C.c_double] * 4
     _lib = lib
     return lib
+
+
+SI_UNITS = (1.760859644e11, 1.38064852e-23, 9.274009994e-24, 2.179872325e-21)   # gama, k_bolt, mub, mry
+ATOMIC_UNITS = (1.0, 1.0, 1.0, 1.0)   # aunits 'Y' (Input/inputhandler.f90:1685-1704)
+
+
+class units:
+    """Context manager: the oracle computes with (gama, k_bolt, mub, mry) inside the
+    block and with SI units again after it."""
+
+    def __init__(self, values):
+        self.values = tuple(float(v) for v in values)
+
+    def __enter__(self):
+        load().orc_set_units(*self.values)
+        return self
+
+    def __exit__(self, *exc):
+        load().orc_set_units(*SI_UNITS)
+        return False
 
 
 def _p(a, t=F64P):

@@ -20,6 +20,14 @@
 /* Parameters/parameters.f90:12  dbl_tolerance=1e-14 (a REAL(4) literal) */
 static const double DBL_TOLERANCE = (double)(float)1e-14;
 
+double orc_gama = ORC_GAMA_SI, orc_kbolt = ORC_KBOLT_SI, orc_mub = ORC_MUB_SI, orc_mry = ORC_MRY_SI;
+void orc_set_units(double gama, double kbolt, double mub, double mry) {
+    orc_gama = gama;
+    orc_kbolt = kbolt;
+    orc_mub = mub;
+    orc_mry = mry;
+}
+
 static int g_threads = 0;
 void orc_set_threads(int n) { g_threads = n; }
 int orc_get_threads(void) {

@@ -23,10 +23,18 @@ extern "C" {
 #endif
 
 /* ---- constants (Parameters/constants.f90:14-19) ---- */
-#define ORC_GAMA   1.760859644e11
-#define ORC_KBOLT  1.38064852e-23
-#define ORC_MUB    9.274009994e-24
-#define ORC_MRY    2.179872325e-21
+#define ORC_GAMA_SI   1.760859644e11
+#define ORC_KBOLT_SI  1.38064852e-23
+#define ORC_MUB_SI    9.274009994e-24
+#define ORC_MRY_SI    2.179872325e-21
+/* The values in use: SI unless orc_set_units changed them (aunits = 'Y' sets gama,
+ * k_bolt, mub and mry to 1, Input/inputhandler.f90:1685-1704). */
+extern double orc_gama, orc_kbolt, orc_mub, orc_mry;
+void orc_set_units(double gama, double kbolt, double mub, double mry);
+#define ORC_GAMA   orc_gama
+#define ORC_KBOLT  orc_kbolt
+#define ORC_MUB    orc_mub
+#define ORC_MRY    orc_mry
 #define ORC_PI     3.141592653589793238462643383279502884197
 
 /* ---- Mersenne twister variant (RNG/mtprng.f90:118-325) ---- */

@@ -40,6 +40,7 @@ CASES = [
     ("heischainaf_energy1500", "./HeisChainAF", "./totenergy.AF_WireT.out", 1500, "similar"),
     ("feco_iter4700", "./FeCo/", "./averages.test", 4700, "sloppy"),
     ("feco_cumulants221", "./FeCo/", "./cumulants.test", 221, "sloppy"),
+    ("scsurf_iter800", "./SCsurf", "averages.SCsurf_T.out", 800, "similar"),
 ]
 
 
@@ -62,7 +63,7 @@ def extract(text, workingdir, outfile, select):
             in_file = False
         elif in_case and s.startswith("- outfile:"):
             in_file = s.split(":", 1)[1].strip() == outfile
-        elif in_case and in_file and re.match(r'"#_Iter\.":\s*%d\s*(#.*)?$' % select, s):
+        elif in_case and in_file and re.match(r'"#_Iter\."\s*:\s*%d\s*(#.*)?$' % select, s):
             if atom is not None and not re.match(r'"#_Atom"\s*:\s*%d\s*(#.*)?$' % atom, lines[n + 1].strip()):
                 continue
             extract_line = None
@@ -117,6 +118,7 @@ def read_inputs(testdir):
                "initmag": int(k["initmag"][0]), "sdealgh": int(k.get("sdealgh", ["1"])[0]),
                "do_reduced": k.get("do_reduced", ["N"])[0].upper() == "Y", "tseed_default": 1,
                "maptype": int(k.get("maptype", ["1"])[0]),
+               "aunits": k.get("aunits", ["N"])[0].upper() == "Y",
                "source": f"tests/{d}/inpsd.dat and the files it names"}
         if "dm" in k:
             out["dmfile"] = nums(d + "/" + os.path.basename(k["dm"][0]))
@@ -156,6 +158,7 @@ def read_inputs(testdir):
         "kagome": system("kagome"),
         "heischain": system("HeisChain"),
         "heischainaf": system("HeisChainAF"),
+        "scsurf": system("SCsurf"),
         "feco": dict(system("FeCo"), cumu_step=int(keys("FeCo/inpsd.dat")["cumu_step"][0]),
                      cumu_buff=int(keys("FeCo/inpsd.dat")["cumu_buff"][0]),
                      avrg_step=int(keys("FeCo/inpsd.dat").get("avrg_step", ["100"])[0])),

@@ -2,7 +2,8 @@
 HeisStripe (vacuum edges, ragged neighbour lists, uniaxial anisotropy, totenergy columns),
 kagome (DMI, reduced Hamiltonian), HeisChain (restart start, initial phase on the
 reference's ziggurat stream, undamped precession), HeisChainAF (two moments, per-type
-projected averages) and FeCo (maptype-2 table, 258 neighbours, reduced, cumulants).  Lattices are built from the reference's
+projected averages), FeCo (maptype-2 table, 258 neighbours, reduced, cumulants) and SCsurf
+(atomic units through uppasd_gpu_set_units).  Lattices are built from the reference's
 input tables by ``lattice.from_tables``; start states the reference draws from its own
 generators (mtprng initmag 1, ziggurat noise) come from the oracle's restatement of them.
 Same comparison as the suite (``similar``: 1e-8 plus the 9-digit print rounding)."""
@@ -105,4 +106,18 @@ def test_feco_on_gpu(pins, tmp_path):
     assert np.allclose(out[:4], pins["feco_cumulants221"]["expected"], rtol=5e-9, atol=0)
     sim.evolve(4700 - done)
     _check([_mavg(sim, lat)[3]], pins["feco_iter4700"])
+    sim.close()
+
+
+def test_scsurf_atomic_units_on_gpu(pins):
+    inp = pins["inputs"]["scsurf"]
+    lat, _ = from_tables(inp)
+    with po.units(po.ATOMIC_UNITS):
+        o = po.Oracle(lat)
+        o.init_random(inp["tseed_default"])
+    sim = GpuSimulation(lat, sdealgh=inp["sdealgh"], delta_t=inp["timestep"], damping=inp["damping"],
+                        temperature=inp["temp"], emom=o.emom.copy())
+    sim.set_atomic_units()
+    sim.evolve(800)
+    _check(_mavg(sim, lat), pins["scsurf_iter800"])
     sim.close()

@@ -149,7 +149,7 @@ def from_tables(inp):
     """The lattice of a reference test directory, from the tables make_golden.py stored."""
     return lattice.from_tables(inp["cell"], inp["ncell"], inp["bc"], inp["sites"], inp["jfile"], sym=inp["sym"],
                                dmfile=inp.get("dmfile"), kfile=inp.get("kfile"), reduce=inp["do_reduced"],
-                               maptype=inp.get("maptype", 1))
+                               maptype=inp.get("maptype", 1), aunits=inp.get("aunits", False))
 
 
 def restart_moments(inp):
@@ -289,3 +289,21 @@ def test_feco(pins):
         o.sd_step()
     mv, ma = o.mavg()
     _check([ma[0]], pins["feco_iter4700"])
+
+
+def test_scsurf_atomic_units(pins):
+    """tests/SCsurf: 16 x 16 square monolayer in atomic units (aunits 'Y': gama = k_bolt =
+    mub = mry = 1), antiferromagnetic exchange, DMI and anisotropy from maptype-2 tables,
+    time step 0.01, midpoint at T = 0 from the mtprng initmag-1 draw: <m> after 800 steps."""
+    inp = pins["inputs"]["scsurf"]
+    assert inp["aunits"]
+    lat, _ = from_tables(inp)
+    with po.units(po.ATOMIC_UNITS):
+        o = po.Oracle(lat, threads=1)
+        o.init_random(inp["tseed_default"])
+        o.setup_ziggurat(inp["tseed_default"])
+        o.make_llg(inp["sdealgh"], inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+        for _ in range(800):
+            o.sd_step()
+        mv, ma = o.mavg()
+    _check(list(mv[0] / lat.natom) + [ma[0]], pins["scsurf_iter800"])

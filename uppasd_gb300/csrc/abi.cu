@@ -25,6 +25,8 @@ void set_error(const std::string &msg) { g_err = msg; }
 
 int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a);  // llg_stencil.cu
 int structured_step(Sim &s, int64_t step_offset, int phase);
+int structured_set_temperature(Sim &s, const double *temp_array);
+void structured_refresh(Sim &s);
 int structured_sync_state(Sim &s);  // master state -> s.e / s.eM
 int structured_load_state(Sim &s);  // s.e -> master state
 void structured_free(Sim &s);
@@ -545,6 +547,12 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
 int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
     if (!w || !temp_array) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
+    if (uppasd::structured(s)) {
+        // the structured kernels take the thermal amplitude by value
+        int rc = uppasd::structured_set_temperature(s, temp_array);
+        if (rc) return rc;
+        uppasd::drop_graph(s);
+    }
     UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.temp, temp_array, sizeof(double) * s.ham.natom, cudaMemcpyHostToDevice,
                                     s.stream));
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
@@ -563,6 +571,23 @@ int uppasd_gpu_set_perp(uppasd_gpu_sim *w, int32_t perp) {
     }
     uppasd::drop_graph(s);  // the step arguments are captured by value
     s.llg.perp = perp;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_units(uppasd_gpu_sim *w, double gama, double k_bolt, double mub, double mry) {
+    if (!w) return UPPASD_GPU_EINVAL;
+    for (double v : {gama, k_bolt, mub, mry})
+        if (!std::isfinite(v) || !(v > 0.0)) {
+            uppasd::set_error("set_units: gama, k_bolt, mub and mry must be finite and > 0");
+            return UPPASD_GPU_EINVAL;
+        }
+    Sim &s = w->s;
+    uppasd::drop_graph(s);  // the step arguments are captured by value
+    s.ham.gama = gama;
+    s.ham.kbolt = k_bolt;
+    s.ham.mub = mub;
+    s.ham.mry = mry;
+    uppasd::structured_refresh(s);
     return UPPASD_GPU_OK;
 }
 
@@ -701,7 +726,7 @@ int upload_temps(Sim &s, const double *temps) {
         UPPASD_CUDA_TRY(cudaMalloc(&s.betak, M * sizeof(float)));
     }
     std::vector<float> b(M);
-    for (int k = 0; k < M; ++k) b[k] = (float)(kMub / (kKbolt * temps[k]));
+    for (int k = 0; k < M; ++k) b[k] = (float)(s.ham.mub / (s.ham.kbolt * temps[k]));
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
     UPPASD_CUDA_TRY(cudaMemcpy(s.tk, temps, M * sizeof(double), cudaMemcpyHostToDevice));
     UPPASD_CUDA_TRY(cudaMemcpy(s.betak, b.data(), M * sizeof(float), cudaMemcpyHostToDevice));
@@ -753,8 +778,8 @@ int uppasd_gpu_pt_run(uppasd_gpu_sim *w, double *temps, int64_t nsweeps, int32_t
         for (int ishift = 0; ishift < 2; ++ishift)
             for (int r = ishift; r + 1 < M; r += 2) {
                 ++trial;
-                const double b1 = 1.0 / uppasd::kKbolt / (T[r] + 1.0e-15), b2 = 1.0 / uppasd::kKbolt / (T[r + 1] + 1.0e-15);
-                const double e1 = E[r] * uppasd::kMry, e2 = E[r + 1] * uppasd::kMry;  // J per atom
+                const double b1 = 1.0 / s.ham.kbolt / (T[r] + 1.0e-15), b2 = 1.0 / s.ham.kbolt / (T[r + 1] + 1.0e-15);
+                const double e1 = E[r] * s.ham.mry, e2 = E[r + 1] * s.ham.mry;  // J per atom
                 const double prob = std::min(1.0, exp((e2 - e1) * (b2 - b1)));
                 if (u[r] <= prob) {
                     std::swap(T[r], T[r + 1]);

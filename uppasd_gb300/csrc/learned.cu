@@ -1234,7 +1234,7 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     cudaError_t e = cudaMemsetAsync(p->accepted, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->dE_sum, 0, sizeof(double), st);
     if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
-    const double beta_mub = kMub / (kKbolt * temperature);
+    const double beta_mub = s.ham.mub / (s.ham.kbolt * temperature);
     s.mix.valid = 0;  // the precision-3 LLG mirror does not follow the learned moves
     if (s.sq.L == p->L) {
         // learned moves on the square lattice read and write the FP32 mirror as well
@@ -1284,7 +1284,7 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
     if (accepted) *accepted = (int64_t)a;
     if (proposed) *proposed = (int64_t)rows * 4 * ncycles;
-    if (dE_accepted) *dE_accepted = de * kMub;
+    if (dE_accepted) *dE_accepted = de * s.ham.mub;
     return UPPASD_GPU_OK;
 }
 

@@ -22,12 +22,12 @@
 
 namespace uppasd {
 
-__device__ __forceinline__ void rodrigues(const double bdup[3], const double e[3], double dt, double lldamp,
-                                          double mr[3]) {
+__device__ __forceinline__ void rodrigues(const double bdup[3], const double e[3], double dt, double gama,
+                                          double lldamp, double mr[3]) {
     double Bnorm = bdup[0] * bdup[0] + bdup[1] * bdup[1] + bdup[2] * bdup[2];
     Bnorm = sqrt(Bnorm) + 1.0e-15;
     double hx = bdup[0] / Bnorm, hy = bdup[1] / Bnorm, hz = bdup[2] / Bnorm;
-    double v = Bnorm * dt * kGama * lldamp;
+    double v = Bnorm * dt * gama * lldamp;
     double cosv = cos(v), sinv = sin(v), u = 1.0 - cosv;
     mr[0] = hx * hx * u * e[0] + cosv * e[0] + hx * hy * u * e[1] - hz * sinv * e[1] + hx * hz * u * e[2] + hy * sinv * e[2];
     mr[1] = hy * hx * u * e[0] + hz * sinv * e[0] + hy * hy * u * e[1] + cosv * e[1] + hy * hz * u * e[2] - hx * sinv * e[2];
@@ -100,12 +100,12 @@ __device__ __forceinline__ void sib_fixed_point(const double e1[3], const double
 
 // llgiheun (Evolution/llgi.f90:178-278): m_new = A^-1 B, A = I + beta [e1]x, from
 // m(t) = e1, m(t - dt) = et and the field h.
-__device__ __forceinline__ void llgi_heun(double lam, double delta_t, double relaxtime, const double et[3],
-                                          const double e1[3], const double h[3], double out[3]) {
+__device__ __forceinline__ void llgi_heun(double lam, double delta_t, double gama, double relaxtime,
+                                          const double et[3], const double e1[3], const double h[3], double out[3]) {
     const double alfa = lam;
     const double beta = -alfa * (1.0 + relaxtime / delta_t);
     const double zeta = -alfa * (relaxtime / delta_t);
-    const double dtg = -delta_t * kGama;
+    const double dtg = -delta_t * gama;
     const double A12 = -beta * e1[2], A13 = beta * e1[1];
     const double A21 = beta * e1[2], A23 = -beta * e1[0];
     const double A31 = -beta * e1[1], A32 = beta * e1[0];
@@ -159,13 +159,13 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
     double z[3];
     if (ALG == 5) {
         noise3(a.nz, i, k, N, M, step, z);
-        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double Dp = (2.0 * lam * a.h.kbolt) / (a.delta_t * a.h.gama * a.h.mub);
         double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
         double bloc[3], bdup[3], mr[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) bloc[c] = B[c] + z[c] * sigma;
         damped_field(bloc, e, lam, bdup);
-        rodrigues(bdup, e, a.delta_t, 1.0 / (1.0 + lam * lam), mr);
+        rodrigues(bdup, e, a.delta_t, a.h.gama, 1.0 / (1.0 + lam * lam), mr);
         a.p.x[o] = mr[0];
         a.p.y[o] = mr[1];
         a.p.z[o] = mr[2];
@@ -179,7 +179,7 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
         double r[3] = {0.0, 0.0, 0.0};
         if (a.noise_on) {
             noise3(a.nz, i, k, N, M, step, z);
-            double Dk = (((lam / (1.0 + lam * lam)) * kKbolt) / kGama / kMub) * (kGama / a.bn);
+            double Dk = (((lam / (1.0 + lam * lam)) * a.h.kbolt) / a.h.gama / a.h.mub) * (a.h.gama / a.bn);
             double D = Dk * (1.0 / mm) * a.temp[i] * a.temprescale;
             double sigma = sqrt(2.00 * D);
             r[0] = z[0] * sigma;
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
             r[2] = z[2] * sigma;
         }
         double lldamp = 1.0 / (1.0 + lam * lam);
-        double dt = a.delta_t * a.bn * kGama * lldamp;
+        double dt = a.delta_t * a.bn * a.h.gama * lldamp;
         double g = a.landeg[i];
         double dtg = dt * g, sqrtdtg = sqrt(dt) * g;
         double v[3];
@@ -212,8 +212,8 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
         a.pM.z[o] = v[2] * mm;
     } else if (ALG == 4) {
         noise3(a.nz, i, k, N, M, step, z);
-        double dt = a.delta_t * kGama;
-        double Dk = lam / (1.0 + lam * lam) * kKbolt / kMub;
+        double dt = a.delta_t * a.h.gama;
+        double Dk = lam / (1.0 + lam * lam) * a.h.kbolt / a.h.mub;
         double D = Dk * (1.0 / mm) * a.temp[i] * a.temprescale;
         double sigma = sqrt(dt * 2.0 * D);
         double g = a.landeg[i];
@@ -244,12 +244,12 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
     } else if (ALG == 11) {
         // llgi_evolve_first: thermfield (Depondt amplitude), bdup = beff + btherm
         noise3(a.nz, i, k, N, M, step, z);
-        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double Dp = (2.0 * lam * a.h.kbolt) / (a.delta_t * a.h.gama * a.h.mub);
         double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
         double bdup[3], et[3] = {a.mpast.x[o], a.mpast.y[o], a.mpast.z[o]}, mt[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) bdup[c] = B[c] + z[c] * sigma;
-        llgi_heun(lam, a.delta_t, a.relaxtime, et, e, bdup, mt);
+        llgi_heun(lam, a.delta_t, a.h.gama, a.relaxtime, et, e, bdup, mt);
         a.p.x[o] = mt[0];
         a.p.y[o] = mt[1];
         a.p.z[o] = mt[2];
@@ -283,7 +283,7 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
     double z[3];
     if (ALG == 5) {
         noise3(a.nz, i, k, N, M, step, z);
-        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double Dp = (2.0 * lam * a.h.kbolt) / (a.delta_t * a.h.gama * a.h.mub);
         double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
         double bloc[3], bdup[3];
 #pragma unroll
@@ -292,12 +292,12 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
         bdup[0] = 0.50 * bdup[0] + 0.50 * a.b2.x[o];
         bdup[1] = 0.50 * bdup[1] + 0.50 * a.b2.y[o];
         bdup[2] = 0.50 * bdup[2] + 0.50 * a.b2.z[o];
-        rodrigues(bdup, e, a.delta_t, 1.0 / (1.0 + lam * lam), out);
+        rodrigues(bdup, e, a.delta_t, a.h.gama, 1.0 / (1.0 + lam * lam), out);
     } else if (ALG == 1 || ALG == 6) {
         double r[3] = {0.0, 0.0, 0.0};
         if (a.noise_on) {
             noise3(a.nz, i, k, N, M, step, z);
-            double Dk = (((lam / (1.0 + lam * lam)) * kKbolt) / kGama / kMub) * (kGama / a.bn);
+            double Dk = (((lam / (1.0 + lam * lam)) * a.h.kbolt) / a.h.gama / a.h.mub) * (a.h.gama / a.bn);
             double D = Dk * (1.0 / mm) * a.temp[i] * a.temprescale;
             double sigma = sqrt(2.00 * D);
             r[0] = z[0] * sigma;
@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
             r[2] = z[2] * sigma;
         }
         double lldamp = 1.0 / (1.0 + lam * lam);
-        double dt = a.delta_t * a.bn * kGama * lldamp;
+        double dt = a.delta_t * a.bn * a.h.gama * lldamp;
         double g = a.landeg[i];
         double dtg = dt * g, sqrtdtg = sqrt(dt) * g;
         if (ALG == 1) {
@@ -323,13 +323,13 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
         // llgi_evolve_second: the same btherm as the predictor (same counter), averaged
         // field, corrector from (m(t - dt), m(t)); m(t) becomes the new m(t - dt)
         noise3(a.nz, i, k, N, M, step, z);
-        double Dp = (2.0 * lam * kKbolt) / (a.delta_t * kGama * kMub);
+        double Dp = (2.0 * lam * a.h.kbolt) / (a.delta_t * a.h.gama * a.h.mub);
         double sigma = sqrt(Dp * a.temprescale * a.temp[i] / mm);
         double b2v[3] = {a.b2.x[o], a.b2.y[o], a.b2.z[o]};
         double bdup[3], et[3] = {a.mpast.x[o], a.mpast.y[o], a.mpast.z[o]}, mt[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) bdup[c] = 0.5 * (B[c] + z[c] * sigma) + 0.5 * b2v[c];
-        llgi_heun(lam, a.delta_t, a.relaxtime, et, e, bdup, mt);
+        llgi_heun(lam, a.delta_t, a.h.gama, a.relaxtime, et, e, bdup, mt);
         a.mpast.x[o] = e[0];
         a.mpast.y[o] = e[1];
         a.mpast.z[o] = e[2];
@@ -339,8 +339,8 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
         out[2] = mt[2] * etot;
     } else {  // ALG == 4
         noise3(a.nz, i, k, N, M, step, z);
-        double dt = a.delta_t * kGama;
-        double Dk = lam / (1.0 + lam * lam) * kKbolt / kMub;
+        double dt = a.delta_t * a.h.gama;
+        double Dk = lam / (1.0 + lam * lam) * a.h.kbolt / a.h.mub;
         double D = Dk * (1.0 / mm) * a.temp[i] * a.temprescale;
         double sigma = sqrt(dt * 2.0 * D);
         double g = a.landeg[i];

@@ -515,7 +515,7 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const fl
     int rc = mixed_ready(s);
     if (rc) return rc;
     s.sqm_valid = 0;  // the square path's mirror does not follow these updates
-    const float beta_mub = betak ? 0.f : (float)(kMub / (kKbolt * temperature));
+    const float beta_mub = betak ? 0.f : (float)(s.ham.mub / (s.ham.kbolt * temperature));
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
         for (int c = 0; c < s.ncolour; ++c) {
             const int beg = s.colour_start_h[c], n = s.colour_start_h[c + 1] - beg;
@@ -538,13 +538,14 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     a.temp = s.llg.temp;
     a.landeg = s.llg.landeg;
     a.mmom = s.llg.mmom;
-    a.dt_dep = (float)(s.llg.delta_t * kGama);
-    a.dt_mid = (float)(s.llg.delta_t * s.llg.bn * kGama);
-    a.c_dp = (float)(2.0 * kKbolt / (s.llg.delta_t * kGama * kMub));
-    a.c_dk = (float)(kKbolt / (kMub * s.llg.bn));
-    a.c_heun = (float)(s.llg.delta_t * kGama * kKbolt / kMub);
+    const double gama = s.ham.gama, kbolt = s.ham.kbolt, mub = s.ham.mub;
+    a.dt_dep = (float)(s.llg.delta_t * gama);
+    a.dt_mid = (float)(s.llg.delta_t * s.llg.bn * gama);
+    a.c_dp = (float)(2.0 * kbolt / (s.llg.delta_t * gama * mub));
+    a.c_dk = (float)(kbolt / (mub * s.llg.bn));
+    a.c_heun = (float)(s.llg.delta_t * gama * kbolt / mub);
     a.tau_dt = (float)(s.llg.relaxtime / s.llg.delta_t);
-    a.dtg_llgi = (float)(-s.llg.delta_t * kGama);
+    a.dtg_llgi = (float)(-s.llg.delta_t * gama);
     a.perp = s.llg.perp;
     a.mpast = s.mpast;
     a.temprescale = (float)s.llg.temprescale;

@@ -553,7 +553,37 @@ struct StructuredFast {
     int nshell = 0, master = 1, lc = 0;
     dim3 grid, block;
     int8_t *species = nullptr;
+    // what the thermal amplitude and the rotation scale are computed from
+    double lam = 0.0, temp = 0.0, delta_t = 0.0, temprescale = 1.0, mom[2] = {1.0, 1.0};
 };
+
+// Depondt thermal amplitude per species (depondt.f90:143-145) and rotation scale from the
+// uniform damping and temperature and the simulation's physical constants; again after
+// set_temperature and set_units.
+static void structured_coefficients(const Sim &s, StructuredFast *f) {
+    const HamDev &h = s.ham;
+    for (int ti = 0; ti < 2; ++ti) {
+        double Dp = (2.0 * f->lam * h.kbolt) / (f->delta_t * h.gama * h.mub);
+        f->p.sigma[ti] = (float)sqrt(Dp * f->temprescale * f->temp / f->mom[ti]);
+    }
+    f->p.lam = (float)f->lam;
+    f->p.dtg = (float)(f->delta_t * h.gama / (1.0 + f->lam * f->lam));
+}
+
+int structured_set_temperature(Sim &s, const double *temp_array) {
+    for (int i = 1; i < s.ham.natom; ++i)
+        if (temp_array[i] != temp_array[0]) {
+            set_error("set_temperature: the structured path (precision 1, 2) needs a uniform temperature");
+            return UPPASD_GPU_EUNSUPPORTED;
+        }
+    s.fast->temp = temp_array[0];
+    structured_coefficients(s, s.fast);
+    return UPPASD_GPU_OK;
+}
+
+void structured_refresh(Sim &s) {
+    if (s.fast) structured_coefficients(s, s.fast);
+}
 
 static void fast_free(StructuredFast *f) {
     if (!f) return;
@@ -663,14 +693,12 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
             p.cA[sh][ti] = (float)v[0];
             p.cD[sh][ti] = (float)(v[1] - v[0]);
         }
-    const double lam = a->lambda1_array[0], T = a->temp_array[0];
-    for (int ti = 0; ti < 2; ++ti) {
-        double Dp = (2.0 * lam * kKbolt) / (c->delta_t * kGama * kMub);
-        double m = mom[ti] > 0 ? mom[ti] : 1.0;
-        p.sigma[ti] = (float)sqrt(Dp * c->temprescale * T / m);
-    }
-    p.lam = (float)lam;
-    p.dtg = (float)(c->delta_t * kGama / (1.0 + lam * lam));
+    f->lam = a->lambda1_array[0];
+    f->temp = a->temp_array[0];
+    f->delta_t = c->delta_t;
+    f->temprescale = c->temprescale;
+    for (int ti = 0; ti < 2; ++ti) f->mom[ti] = mom[ti] > 0 ? mom[ti] : 1.0;
+    structured_coefficients(s, f);
     for (int q = 0; q < 3; ++q) p.ext[q] = (float)a->external_field[q];
     p.seed = c->gpu_rng_seed;
     p.d_step = s.llg.d_step;

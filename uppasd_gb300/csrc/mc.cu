@@ -114,13 +114,13 @@ __device__ double delta_energy(const HamDev &h, const Vec3D &eM, const Vec3D &e,
     }
     e_c = e_c - ext[0] * mi[0] - ext[1] * mi[1] - ext[2] * mi[2];
     e_t = e_t - ext[0] * tm[0] - ext[1] * tm[1] - ext[2] * tm[2];
-    return kMub * (e_t - e_c);
+    return h.mub * (e_t - e_c);
 }
 
-__device__ __forceinline__ void heat_bath(double mm, double temperature, double flipprob, const double tf[3], double q,
-                                          double out[3]) {
-    double beta = 1.0 / kKbolt / (1.0 * temperature);
-    double zfc[3] = {beta * tf[0] * kMub * mm, beta * tf[1] * kMub * mm, beta * tf[2] * kMub * mm};
+__device__ __forceinline__ void heat_bath(const HamDev &h, double mm, double temperature, double flipprob,
+                                          const double tf[3], double q, double out[3]) {
+    double beta = 1.0 / h.kbolt / (1.0 * temperature);
+    double zfc[3] = {beta * tf[0] * h.mub * mm, beta * tf[1] * h.mub * mm, beta * tf[2] * h.mub * mm};
     double zarg = sqrt(zfc[0] * zfc[0] + zfc[1] * zfc[1] + zfc[2] * zfc[2]);
     double zctheta = zfc[2] / zarg;
     double zstheta = sqrt(1.0 - zctheta * zctheta) + kDblTol;
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
     const int i = sites[t - (int64_t)k * nsites];
     if (tk) {  // one temperature per ensemble (replicas of pt_iphase)
         temperature = tk[k];
-        if (!heatbath) delta = (double)(2.0f / 25.0f) * pow(kKbolt * temperature / kMub, 0.20);
+        if (!heatbath) delta = (double)(2.0f / 25.0f) * pow(h.kbolt * temperature / h.mub, 0.20);
     }
     const size_t o = (size_t)k * N + i;
     Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
     if (heatbath) {
         double tf[3];
         site_field(h, eM, i, k, tf);
-        heat_bath(mm, temperature, u[1], tf, u[0], nm);
+        heat_bath(h, mm, temperature, u[1], tf, u[0], nm);
     } else {
         double ecur[3] = {e.x[o], e.y[o], e.z[o]};
         double rn[3] = {u[0], u[1], u[2]};
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
         choose_random_flip(ecur, delta, rn, gn, nm);
         double ext[3] = {h.ext.x[o] + 0.0, h.ext.y[o] + 0.0, h.ext.z[o] + 0.0};
         double de = delta_energy(h, eM, e, mm, i, k, nm, ext);
-        double beta = 1.0 / kKbolt / (1.0 * temperature + 1.0e-15);
+        double beta = 1.0 / h.kbolt / (1.0 * temperature + 1.0e-15);
         if (!(de <= 0.0 || u[3] < exp(-beta * de))) return;
     }
     e.x[o] = nm[0];
@@ -183,7 +183,7 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
         return UPPASD_GPU_ESTATE;
     }
     // montecarlo.f90:142, (2.0/25.0) is a REAL(4) constant
-    const double delta = (double)(2.0f / 25.0f) * pow(kKbolt * temperature / kMub, 0.20);
+    const double delta = (double)(2.0f / 25.0f) * pow(s.ham.kbolt * temperature / s.ham.mub, 0.20);
     const int hb = mode == 'H' ? 1 : 0;
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
         for (int c = 0; c < s.ncolour; ++c) {

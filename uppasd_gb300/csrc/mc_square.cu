@@ -210,7 +210,7 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
     }
     for (int c = 0; c < 3; ++c) a.ext[c] = s.sq.ext[c];
     a.mom = s.sq.mom;
-    a.beta_mu = (float)(kMub * s.sq.mom / (kKbolt * temperature));
+    a.beta_mu = (float)(s.ham.mub * s.sq.mom / (s.ham.kbolt * temperature));
     a.seed = s.llg.seed;
     const long long per = (long long)L * (L / 2) * a.mensemble;
     const unsigned blocks = (unsigned)((per + 255) / 256);

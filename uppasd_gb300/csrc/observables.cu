@@ -101,7 +101,7 @@ int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const 
         set_error(std::string("observables: ") + cudaGetErrorString(err));
         return UPPASD_GPU_ECUDA;
     }
-    const double fcinv = kMub / kMry;
+    const double fcinv = s.ham.mub / s.ham.mry;
     for (int k = 0; k < M; ++k) {
         const double *r = h + (size_t)k * kRedCount;
         if (mvec_h) {

@@ -14,6 +14,7 @@
 #include <string>
 
 #include "../../include/uppasd_gpu.h"
+#include "common.cuh"
 
 namespace uppasd {
 
@@ -40,6 +41,9 @@ struct HamDev {
     // jt[(s * nham + ih) * 9 + 3 a + b]; replaces ncoup in fields and energies
     int do_jtensor = 0;
     double *jt = nullptr;
+    // the caller's physical constants (fortrandata_setconstants_ passes gama, k_bolt and
+    // mub): SI by default, all 1 under aunits = 'Y' (Input/inputhandler.f90:1685-1704)
+    double gama = kGama, kbolt = kKbolt, mub = kMub, mry = kMry;
 };
 
 struct LlgDev {

@@ -334,7 +334,7 @@ def _table_neighbours(cell, ncell, periodic, pos, types, shells):
 
 
 def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=None, reduce: bool = False,
-                maptype: int = 1):
+                maptype: int = 1, aunits: bool = False):
     """A Hamiltonian built from the reference's own input tables: the ``cell``, ``ncell``,
     ``BC`` and ``Sym`` keywords of inpsd.dat, the posfile and momfile rows (``sites``:
     per basis site ``(type, x, y, z, mom, ex, ey, ez)``, Cartesian, posfiletype 'C'),
@@ -350,7 +350,8 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
     the lattice symmetry (``cubic_images`` for Sym 1).  Couplings are scaled by
     2 mRy/muB/(m_i m_j) (zero when m_i m_j < 1e-6), anisotropies by mRy/muB/m^2, m^4
     (uniaxial) or m^4, m^6 (cubic) (Hamiltonian/hamiltonianinit.f90:895-909, :1060-1068).
-    ``reduce`` gives the reduced Hamiltonian (do_reduced 'Y').
+    ``reduce`` gives the reduced Hamiltonian (do_reduced 'Y'); ``aunits`` the atomic units of
+    aunits 'Y' (mry = mub = 1, Input/inputhandler.f90:1685-1704).
 
     Returns the lattice and the momfile directions normalised per atom (Initmag 3)."""
     sites = [tuple(float(v) for v in s) for s in sites]
@@ -383,6 +384,7 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
                 values[it].append(val)
         return ({t: [(expand(r), jt) for r, jt in v] for t, v in shells.items()}, values)
 
+    fc, fc2 = (1.0, 2.0) if aunits else (FC, FC2)
     natom = na * int(np.prod(ncell))
     b_of = np.arange(natom) % na
     m_of = moms[b_of]
@@ -398,7 +400,7 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
                 ii, ss = np.nonzero(sel)
                 mj = m_of[nl[ii, ss] - 1]
                 mm = m_of[ii] * mj
-                c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, val[None, :] * FC2 / mm[:, None])
+                c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, val[None, :] * fc2 / mm[:, None])
         return nl, ns, c
 
     nlist, nsize, c = coupled(jfile, 1)
@@ -426,8 +428,8 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
             taniso[sel] = int(r[1])
             eaniso[sel] = e / np.sqrt(e @ e + 1.0e-15)
             p1, p2 = (4, 6) if int(r[1]) == 2 else (2, 4)
-            kaniso[sel, 0] = FC * r[2] / moms[b] ** p1
-            kaniso[sel, 1] = FC * r[3] / moms[b] ** p2
+            kaniso[sel, 0] = fc * r[2] / moms[b] ** p1
+            kaniso[sel, 1] = fc * r[3] / moms[b] ** p2
             sb[sel] = r[7] if len(r) > 7 else 0.0
         lat.taniso, lat.eaniso, lat.kaniso, lat.sb = taniso, eaniso, kaniso, sb
     if reduce:

@@ -152,6 +152,14 @@ class GpuSimulation:
         t = np.ascontiguousarray(np.broadcast_to(np.asarray(temperature, float), (self.lat.natom,)))
         _lib.call("uppasd_gpu_set_temperature", self._h, _ptr(t))
 
+    def set_units(self, gama: float, k_bolt: float, mub: float, mry: float):
+        """The physical constants every path computes with (SI until set)."""
+        _lib.call("uppasd_gpu_set_units", self._h, float(gama), float(k_bolt), float(mub), float(mry))
+
+    def set_atomic_units(self):
+        """aunits = 'Y': gama, k_bolt, mub and mry all 1 (Input/inputhandler.f90:1685-1704)."""
+        self.set_units(1.0, 1.0, 1.0, 1.0)
+
     def set_step(self, step: int):
         _lib.call("uppasd_gpu_set_step", self._h, int(step))
 
