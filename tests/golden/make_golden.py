@@ -1,7 +1,7 @@
 """Extract the reference's golden values used to pin the oracle.
 
-Reads UppASD's own regression definitions (tests/regulartests.yaml in the
-reference tree) as text -- PyYAML is not needed -- and writes
+Reads UppASD's own regression definitions (tests/regulartests.yaml and
+tests/cudatests.yaml in the reference tree) as text -- PyYAML is not needed -- and writes
 ``reference_pins.json`` next to this script.  Run it where the reference tree
 is available:
 
@@ -13,6 +13,7 @@ commented-out history in the YAML is ignored.
 import json
 import os
 import re
+import struct
 import sys
 
 CASES = [
@@ -41,6 +42,12 @@ CASES = [
     ("feco_iter4700", "./FeCo/", "./averages.test", 4700, "sloppy"),
     ("feco_cumulants221", "./FeCo/", "./cumulants.test", 221, "sloppy"),
     ("scsurf_iter800", "./SCsurf", "averages.SCsurf_T.out", 800, "similar"),
+    ("kagome_cuda_iter1300", "./kagome_cuda", "averages.kagome_T.out", 1300, "similar"),
+    ("kagome_cuda_cumulants171", "./kagome_cuda", "cumulants.kagome_T.out", 171, "similar"),
+    ("feco_cuda_iter4700", "./FeCo_cuda/", "./averages.test", 4700, "sloppy"),
+    ("feco_cuda_cumulants221", "./FeCo_cuda/", "./cumulants.test", 221, "sloppy"),
+    ("bccfe_cuda_iter1700", "./bccFe_cuda/", "./averages.test", 1700, "sloppy"),
+    ("bccfe_cuda_cumulants41", "./bccFe_cuda/", "./cumulants.test", 41, "sloppy"),
 ]
 
 
@@ -101,24 +108,29 @@ def read_inputs(testdir):
         return [[float(v.replace("d", "e").replace("D", "e")) for v in r] for r in rows(fn)]
 
     def system(d):
-        """Keywords and tables of one test directory (Cartesian posfile, maptype 1)."""
+        """Keywords and the tables they name in one test directory."""
         k = keys(d + "/inpsd.dat")
         lines = [ln.split() for ln in open(os.path.join(testdir, d, "inpsd.dat"))]
         heads = [t[0].lower() if t else "" for t in lines]
         c0 = heads.index("cell")
         cell = [[float(v) for v in lines[c0][1:4]]] + [[float(v) for v in lines[c0 + q][0:3]] for q in (1, 2)]
-        pos = {int(r[0]): r for r in nums(d + "/posfile")}
-        mom = {int(r[0]): r for r in nums(d + "/momfile")}
+        pos = {int(r[0]): r for r in nums(d + "/" + os.path.basename(k["posfile"][0]))}
+        mom = {int(r[0]): r for r in nums(d + "/" + os.path.basename(k["momfile"][0]))}
         sites = [[pos[i][1]] + pos[i][2:5] + mom[i][2:6] for i in sorted(pos)]
         out = {"ncell": [int(v) for v in k["ncell"][:3]], "bc": k["bc"][:3], "cell": cell,
                "sym": int(k.get("sym", ["0"])[0]), "sites": sites,
                "jfile": nums(d + "/" + os.path.basename(k["exchange"][0])),
                "damping": float(k["damping"][0]), "temp": float(k["temp"][0]),
-               "timestep": float(k["timestep"][0].replace("d", "e")), "nstep": int(k["nstep"][0]),
+               # without the keyword, delta_t keeps its default, a REAL(4) literal (Input/inputdata.f90:457)
+               "timestep": (float(k["timestep"][0].replace("d", "e")) if "timestep" in k
+                            else struct.unpack("f", struct.pack("f", 1.0e-16))[0]),
+               "nstep": int(k["nstep"][0]),
                "initmag": int(k["initmag"][0]), "sdealgh": int(k.get("sdealgh", ["1"])[0]),
                "do_reduced": k.get("do_reduced", ["N"])[0].upper() == "Y", "tseed_default": 1,
                "maptype": int(k.get("maptype", ["1"])[0]),
                "aunits": k.get("aunits", ["N"])[0].upper() == "Y",
+               "posfiletype": k.get("posfiletype", ["C"])[0].upper(),
+               "do_jtensor": int(k.get("do_jtensor", ["0"])[0]),
                "source": f"tests/{d}/inpsd.dat and the files it names"}
         if "dm" in k:
             out["dmfile"] = nums(d + "/" + os.path.basename(k["dm"][0]))
@@ -159,6 +171,15 @@ def read_inputs(testdir):
         "heischain": system("HeisChain"),
         "heischainaf": system("HeisChainAF"),
         "scsurf": system("SCsurf"),
+        "feco_cuda": dict(system("FeCo_cuda"), cumu_step=int(keys("FeCo_cuda/inpsd.dat")["cumu_step"][0]),
+                          cumu_buff=int(keys("FeCo_cuda/inpsd.dat")["cumu_buff"][0]),
+                          avrg_step=int(keys("FeCo_cuda/inpsd.dat").get("avrg_step", ["100"])[0])),
+        "bccfe_cuda": dict(system("bccFe_cuda"), cumu_step=int(keys("bccFe_cuda/inpsd.dat")["cumu_step"][0]),
+                           cumu_buff=int(keys("bccFe_cuda/inpsd.dat")["cumu_buff"][0]),
+                           avrg_step=int(keys("bccFe_cuda/inpsd.dat")["avrg_step"][0])),
+        "kagome_cuda": dict(system("kagome_cuda"), cumu_step=int(keys("kagome_cuda/inpsd.dat")["cumu_step"][0]),
+                            cumu_buff=int(keys("kagome_cuda/inpsd.dat")["cumu_buff"][0]),
+                            avrg_step=int(keys("kagome_cuda/inpsd.dat")["avrg_step"][0])),
         "feco": dict(system("FeCo"), cumu_step=int(keys("FeCo/inpsd.dat")["cumu_step"][0]),
                      cumu_buff=int(keys("FeCo/inpsd.dat")["cumu_buff"][0]),
                      avrg_step=int(keys("FeCo/inpsd.dat").get("avrg_step", ["100"])[0])),
@@ -167,13 +188,15 @@ def read_inputs(testdir):
 
 def main():
     src = sys.argv[1] if len(sys.argv) > 1 else "regulartests.yaml"
-    text = open(src).read()
+    # the GPU cases of the suite live in a second file beside it
+    text = open(src).read() + "\n" + open(os.path.join(os.path.dirname(os.path.abspath(src)), "cudatests.yaml")).read()
     pins = {"inputs": read_inputs(os.path.dirname(os.path.abspath(src)))}
     for name, wd, of, sel, cmp in CASES:
         e = extract(text, wd, of, sel)
         e["comparison"] = cmp
-        e["source"] = f"tests/regulartests.yaml {wd} {of} #_Iter.={sel}" if not isinstance(sel, tuple) else \
-            f"tests/regulartests.yaml {wd} {of} #_Iter.={sel[0]} #_Atom={sel[1]}"
+        yaml = "cudatests.yaml" if "_cuda" in wd else "regulartests.yaml"
+        e["source"] = f"tests/{yaml} {wd} {of} #_Iter.={sel}" if not isinstance(sel, tuple) else \
+            f"tests/{yaml} {wd} {of} #_Iter.={sel[0]} #_Atom={sel[1]}"
         pins[name] = e
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_pins.json")
     with open(dst, "w") as f:

@@ -2,8 +2,9 @@
 HeisStripe (vacuum edges, ragged neighbour lists, uniaxial anisotropy, totenergy columns),
 kagome (DMI, reduced Hamiltonian), HeisChain (restart start, initial phase on the
 reference's ziggurat stream, undamped precession), HeisChainAF (two moments, per-type
-projected averages), FeCo (maptype-2 table, 258 neighbours, reduced, cumulants) and SCsurf
-(atomic units through uppasd_gpu_set_units).  Lattices are built from the reference's
+projected averages), FeCo (maptype-2 table, 258 neighbours, reduced, cumulants), SCsurf
+(atomic units through uppasd_gpu_set_units) and the suite's GPU cases kagome_cuda (exchange
+tensors), bccFe_cuda and FeCo_cuda.  Lattices are built from the reference's
 input tables by ``lattice.from_tables``; start states the reference draws from its own
 generators (mtprng initmag 1, ziggurat noise) come from the oracle's restatement of them.
 Same comparison as the suite (``similar``: 1e-8 plus the 9-digit print rounding)."""
@@ -11,7 +12,8 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from test_oracle_golden import _check, _energy_columns, check_projavgs, from_tables, restart_moments
+from test_oracle_golden import (GPU_CASES, _check, _energy_columns, check_projavgs, check_reference_gpu_case,
+                                from_tables, replay_reference_gpu_case, restart_moments)
 from uppasd_gb300.simulation import GpuSimulation
 
 pytestmark = pytest.mark.gpu
@@ -120,4 +122,22 @@ def test_scsurf_atomic_units_on_gpu(pins):
     sim.set_atomic_units()
     sim.evolve(800)
     _check(_mavg(sim, lat), pins["scsurf_iter800"])
+    sim.close()
+
+
+@pytest.mark.parametrize("name,mavg_at,cumulant_row", GPU_CASES)
+def test_reference_gpu_cases_on_gpu(pins, name, mavg_at, cumulant_row):
+    """The reference's own GPU cases (its CUDA path integrates with Depondt)."""
+    inp = pins["inputs"][name]
+    lat, e0 = from_tables(inp)
+    if inp["initmag"] == 1:
+        o = po.Oracle(lat)
+        o.init_random(inp["tseed_default"])
+        e0 = o.emom.copy()
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=inp["timestep"], damping=inp["damping"], temperature=inp["temp"],
+                        emom=e0)
+    mrow, crow = replay_reference_gpu_case(pins, name, mavg_at, cumulant_row,
+                                           {"step": lambda n: sim.evolve(n) if n else None,
+                                            "mavg": lambda: _mavg(sim, lat)})
+    check_reference_gpu_case(pins, name, mrow, crow)
     sim.close()

@@ -7,6 +7,7 @@ reference printed, using the suite's own comparison (``similar``: |d| <= 1e-8 pl
 ``sloppy``: |d| <= 2e-2 and relative < 2e-2; tests/bergtest.py:42-75).
 """
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -149,7 +150,8 @@ def from_tables(inp):
     """The lattice of a reference test directory, from the tables make_golden.py stored."""
     return lattice.from_tables(inp["cell"], inp["ncell"], inp["bc"], inp["sites"], inp["jfile"], sym=inp["sym"],
                                dmfile=inp.get("dmfile"), kfile=inp.get("kfile"), reduce=inp["do_reduced"],
-                               maptype=inp.get("maptype", 1), aunits=inp.get("aunits", False))
+                               maptype=inp.get("maptype", 1), aunits=inp.get("aunits", False),
+                               posfiletype=inp.get("posfiletype", "C"), tensor=bool(inp.get("do_jtensor", 0)))
 
 
 def restart_moments(inp):
@@ -307,3 +309,68 @@ def test_scsurf_atomic_units(pins):
             o.sd_step()
         mv, ma = o.mavg()
     _check(list(mv[0] / lat.natom) + [ma[0]], pins["scsurf_iter800"])
+
+
+# The reference's GPU cases (tests/cudatests.yaml) run its CUDA path (gpu_mode 1), whose only
+# integrator is Depondt (gpu_files/cudaDepondtIntegrator.cu) whatever SDEalgh says; with
+# SDEalgh 5 the oracle reproduces their cumulant rows to all printed digits.  Their <M> rows
+# for bccFe_cuda and FeCo_cuda do not follow from those same runs (the suite compares them
+# ``sloppy``) and are kept at that bound.
+GPU_CASES = [("kagome_cuda", 1300, 171), ("bccfe_cuda", 1700, 41), ("feco_cuda", 4700, 221)]
+
+
+def replay_reference_gpu_case(pins, name, mavg_at, cumulant_row, run):
+    """Drives `run(nsteps)` (advance) and returns (<M> row at mavg_at, cumulant row) with the
+    sampling order of sd_mphase: a cumulant sample every cumu_step steps, taken before the step."""
+    from uppasd_gb300 import output
+    inp = pins["inputs"][name]
+    cf = output.CumulantsFile(os.devnull, 1, inp["temp"], 10 ** 9)
+    done, mrow, crow = 0, None, None
+    for row in range(1, max(cumulant_row, mavg_at // inp["cumu_step"] + 1) + 1):
+        target = row * inp["cumu_step"] - 1
+        if mrow is None and mavg_at <= target:
+            run["step"](mavg_at - done)
+            done = mavg_at
+            mrow = run["mavg"]()
+        run["step"](target - done)
+        done = target
+        if row <= cumulant_row:
+            out = cf.add(np.linalg.norm(run["mavg"]()[:3]))
+            if row == cumulant_row:
+                crow = out[:4]
+    return mrow, crow
+
+
+def check_reference_gpu_case(pins, name, mrow, crow):
+    exact = pins[name + "_cumulants%d" % {"kagome_cuda": 171, "bccfe_cuda": 41, "feco_cuda": 221}[name]]
+    _check(crow, exact)
+    assert np.allclose(crow, exact["expected"], rtol=5e-9, atol=0), (crow, exact["expected"])
+    mpin = pins[name + "_iter%d" % {"kagome_cuda": 1300, "bccfe_cuda": 1700, "feco_cuda": 4700}[name]]
+    _check(mrow[-len(mpin["expected"]):], mpin)
+
+
+@pytest.mark.parametrize("name,mavg_at,cumulant_row", GPU_CASES)
+def test_reference_gpu_cases(pins, name, mavg_at, cumulant_row):
+    """kagome_cuda (SKKR exchange tensors from a 9-column jfile, direct coordinates, 13068
+    atoms), bccFe_cuda (four cubic shells, two sublattice directions) and FeCo_cuda, all at
+    T = 0 with Depondt."""
+    inp = pins["inputs"][name]
+    lat, e0 = from_tables(inp)
+    o = po.Oracle(lat)
+    if inp["initmag"] == 1:
+        o.init_random(inp["tseed_default"])
+    else:
+        o.set_moments(e0)
+    o.setup_ziggurat(inp["tseed_default"])
+    o.make_llg(5, inp["timestep"], inp["damping"], inp["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+
+    def step(n):
+        for _ in range(n):
+            o.sd_step()
+
+    def mavg():
+        mv, ma = o.mavg()
+        return list(mv[0] / lat.natom) + [ma[0]]
+
+    mrow, crow = replay_reference_gpu_case(pins, name, mavg_at, cumulant_row, {"step": step, "mavg": mavg})
+    check_reference_gpu_case(pins, name, mrow, crow)

@@ -334,7 +334,7 @@ def _table_neighbours(cell, ncell, periodic, pos, types, shells):
 
 
 def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=None, reduce: bool = False,
-                maptype: int = 1, aunits: bool = False):
+                maptype: int = 1, aunits: bool = False, posfiletype: str = "C", tensor: bool = False):
     """A Hamiltonian built from the reference's own input tables: the ``cell``, ``ncell``,
     ``BC`` and ``Sym`` keywords of inpsd.dat, the posfile and momfile rows (``sites``:
     per basis site ``(type, x, y, z, mom, ex, ey, ez)``, Cartesian, posfiletype 'C'),
@@ -351,13 +351,18 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
     2 mRy/muB/(m_i m_j) (zero when m_i m_j < 1e-6), anisotropies by mRy/muB/m^2, m^4
     (uniaxial) or m^4, m^6 (cubic) (Hamiltonian/hamiltonianinit.f90:895-909, :1060-1068).
     ``reduce`` gives the reduced Hamiltonian (do_reduced 'Y'); ``aunits`` the atomic units of
-    aunits 'Y' (mry = mub = 1, Input/inputhandler.f90:1685-1704).
+    aunits 'Y' (mry = mub = 1, Input/inputhandler.f90:1685-1704); ``posfiletype`` 'D' reads
+    the site positions in units of the cell vectors; ``tensor`` reads jfile rows with nine
+    couplings J_xx J_xy ... J_zz (row by row, read_exchange_tensor_base,
+    Input/inputhandler_ext.f90:658-741) into ``j_tens`` (do_jtensor = 1), scaled like ncoup.
 
     Returns the lattice and the momfile directions normalised per atom (Initmag 3)."""
     sites = [tuple(float(v) for v in s) for s in sites]
     na = len(sites)
     types = [int(s[0]) for s in sites]
     pos = [np.array(s[1:4]) for s in sites]
+    if str(posfiletype).upper() == "D":
+        pos = [np.asarray(cell, dtype=np.float64).T @ p for p in pos]
     moms = np.array([s[4] for s in sites])
     periodic = tuple(str(c).upper() == "P" for c in bc)
     if maptype not in (1, 2):
@@ -403,8 +408,13 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
                 c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, val[None, :] * fc2 / mm[:, None])
         return nl, ns, c
 
-    nlist, nsize, c = coupled(jfile, 1)
+    nlist, nsize, c = coupled(jfile, 9 if tensor else 1)
+    jt = None
+    if tensor:
+        jt = tensor_from_matrices(c.reshape(c.shape[:2] + (3, 3)))
+        c = np.zeros(c.shape[:2] + (1,))
     lat = Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=np.ascontiguousarray(c[..., 0]),
+                  j_tens=jt,
                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=m_of[None, :].copy(),
                   extfield=np.zeros((1, natom, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
                   periodic=periodic, meta={"types": types})
