@@ -700,6 +700,84 @@ static void sib_second(const orc_llg *p, int N, int M, orc_state *s) {
     }
 }
 
+/* Fixed-point iteration of sispht / sisphf (Evolution/sphmidpoint.f90:485-923, SDEalgh 7):
+ * SIB's with the midpoint direction normalised, u = (e1 + efp0) / |e1 + efp0|.  efp is the
+ * last iterate, efp0 the one before it when the tolerance ended the loop (else the last). */
+static inline void sisph_fixed_point(const double e1[3], const double a1[3], const double s1[3], double dtg,
+                                     double sqrtdtg, double efp[3], double efp0[3]) {
+    const double epsilona = F32(1e-12);
+    efp0[0] = e1[0]; efp0[1] = e1[1]; efp0[2] = e1[2];
+    for (int k = 1; k <= 100; ++k) {
+        double unorm = sqrt((e1[0] + efp0[0]) * (e1[0] + efp0[0]) + (e1[1] + efp0[1]) * (e1[1] + efp0[1]) +
+                            (e1[2] + efp0[2]) * (e1[2] + efp0[2]));
+        double fd[3], fs[3];
+        for (int c = 0; c < 3; ++c) {
+            double u = (e1[c] + efp0[c]) / unorm;
+            fd[c] = dtg * u;
+            fs[c] = sqrtdtg * u;
+        }
+        efp[0] = e1[0] + fd[1] * a1[2] - fd[2] * a1[1] + fs[1] * s1[2] - fs[2] * s1[1];
+        efp[1] = e1[1] + fd[2] * a1[0] - fd[0] * a1[2] + fs[2] * s1[0] - fs[0] * s1[2];
+        efp[2] = e1[2] + fd[0] * a1[1] - fd[1] * a1[0] + fs[0] * s1[1] - fs[1] * s1[0];
+        double dx = sqrt((efp0[0] - efp[0]) * (efp0[0] - efp[0]));
+        double dy = sqrt((efp0[1] - efp[1]) * (efp0[1] - efp[1]));
+        double dz = sqrt((efp0[2] - efp[2]) * (efp0[2] - efp[2]));
+        if (dx < epsilona && dy < epsilona && dz < epsilona) break;
+        efp0[0] = efp[0]; efp0[1] = efp[1]; efp0[2] = efp[2];
+    }
+}
+
+/* sispht (Evolution/sphmidpoint.f90:485-713): emom2 = the normalised midpoint of e1 and the
+ * iterate the loop continues from */
+static void sisph_first(const orc_llg *p, int N, int M, orc_state *s) {
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t ij = 0; ij < (int64_t)N * M; ++ij) {
+        int i = (int)(ij % N), j = (int)(ij / N);
+        double lam = p->lambda1[i];
+        double lldamp = 1.0 / (1.0 + lam * lam);
+        double dt = p->delta_t * p->bn * ORC_GAMA * lldamp;
+        double dtg = dt * p->landeg[i], sqrtdtg = sqrt(dt) * p->landeg[i];
+        double e1[3], b[3], f[3], a1[3], s1[3], efp[3], efp0[3];
+        for (int c = 0; c < 3; ++c) {
+            e1[c] = V3(s->emom, c, i, j, N);
+            b[c] = V3(s->beff, c, i, j, N);
+            f[c] = V3(s->ranv, c, i, j, N);
+        }
+        sib_a1s1(lam, e1, b, f, a1, s1);
+        sisph_fixed_point(e1, a1, s1, dtg, sqrtdtg, efp, efp0);
+        double unorm = sqrt((e1[0] + efp0[0]) * (e1[0] + efp0[0]) + (e1[1] + efp0[1]) * (e1[1] + efp0[1]) +
+                            (e1[2] + efp0[2]) * (e1[2] + efp0[2]));
+        double mm = M2(s->mmom, i, j, N);
+        for (int c = 0; c < 3; ++c) {
+            double v = (e1[c] + efp0[c]) / unorm;
+            V3(s->emom2, c, i, j, N) = v;
+            V3(s->emomM, c, i, j, N) = v * mm;
+        }
+    }
+}
+
+/* sisphf (Evolution/sphmidpoint.f90:721-923): a1, s1 at the midpoint, emom2 = last iterate */
+static void sisph_second(const orc_llg *p, int N, int M, orc_state *s) {
+#pragma omp parallel for schedule(static) num_threads(orc_get_threads())
+    for (int64_t ij = 0; ij < (int64_t)N * M; ++ij) {
+        int i = (int)(ij % N), j = (int)(ij / N);
+        double lam = p->lambda1[i];
+        double lldamp = 1.0 / (1.0 + lam * lam);
+        double dt = p->delta_t * p->bn * ORC_GAMA * lldamp;
+        double dtg = dt * p->landeg[i], sqrtdtg = sqrt(dt) * p->landeg[i];
+        double e1[3], etp[3], b[3], f[3], a1[3], s1[3], efp[3], efp0[3];
+        for (int c = 0; c < 3; ++c) {
+            e1[c] = V3(s->emom, c, i, j, N);
+            etp[c] = V3(s->emom2, c, i, j, N);
+            b[c] = V3(s->beff, c, i, j, N);
+            f[c] = V3(s->ranv, c, i, j, N);
+        }
+        sib_a1s1(lam, etp, b, f, a1, s1);
+        sisph_fixed_point(e1, a1, s1, dtg, sqrtdtg, efp, efp0);
+        for (int c = 0; c < 3; ++c) V3(s->emom2, c, i, j, N) = efp[c];
+    }
+}
+
 /* llgiheun (Evolution/llgi.f90:178-278): one implicit step of the inertial LLG,
  * m_new = A^-1 B with A = I + beta [e1]x, from m(t) = e1, m(t - dt) = et and the
  * field h; no Lande factor and no 1/(1 + lambda^2), as there. */
@@ -823,10 +901,12 @@ int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
     switch (p->sdealgh) {
     case 1:
     case 6:
+    case 7:
         if (min_lambda_gt(p, N, 1e-12)) rannum(p, N, M, s->mmom, s->ranv);
         else memset(s->ranv, 0, sizeof(double) * 3 * (size_t)N * M);
         if (p->sdealgh == 1) midpoint_first(p, N, M, s);
-        else sib_first(p, N, M, s);
+        else if (p->sdealgh == 6) sib_first(p, N, M, s);
+        else sisph_first(p, N, M, s);
         break;
     case 4: heun_first(p, N, M, s); break;
     case 5: depondt_first(p, N, M, s); break;
@@ -841,6 +921,7 @@ int orc_sd_step(const orc_ham *h, const orc_llg *p, orc_state *s) {
     switch (p->sdealgh) {
     case 1: midpoint_second(p, N, M, s); break;
     case 6: sib_second(p, N, M, s); break;
+    case 7: sisph_second(p, N, M, s); break;
     case 4: heun_second(p, N, M, s); break;
     case 5: depondt_second(p, N, M, s); break;
     case 11: llgi_second(p, N, M, s); break;

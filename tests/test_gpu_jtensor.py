@@ -39,7 +39,7 @@ def test_kagome_field_and_energy_match_oracle():
     sim.close()
 
 
-@pytest.mark.parametrize("solver,temp", [(1, 0.0), (4, 0.0), (5, 0.0), (5, 300.0), (1, 300.0)])
+@pytest.mark.parametrize("solver,temp", [(1, 0.0), (4, 0.0), (5, 0.0), (5, 300.0), (1, 300.0), (7, 0.0)])
 def test_kagome_llg_1000_steps(solver, temp):
     lat = _kagome(2)
     e0 = _rand_unit(np.random.default_rng(22), (2, lat.natom, 3))

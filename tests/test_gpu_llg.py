@@ -29,11 +29,11 @@ def _pair(lat, solver, dt, damping, temp, seed, e0, noise_mode):
     return sim, o
 
 
-@pytest.mark.parametrize("solver", [1, 4, 5, 6])
+@pytest.mark.parametrize("solver", [1, 4, 5, 6, 7])
 def test_bcc_T0_1000_steps(solver):
     lat = lattice.bcc(4, [1.3, 0.7], 2.2).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(1), (2, lat.natom, 3))
-    nsteps = 1000 if solver != 6 else 200
+    nsteps = 1000 if solver not in (6, 7) else 200
     sim, o = _pair(lat, solver, 1e-16, 0.1, 0.0, 5, e0, po.NOISE_PHILOX)
     sim.evolve(nsteps)
     for _ in range(nsteps):
@@ -43,7 +43,7 @@ def test_bcc_T0_1000_steps(solver):
     sim.close()
 
 
-@pytest.mark.parametrize("solver", [1, 5])
+@pytest.mark.parametrize("solver", [1, 5, 7])
 def test_bcc_philox_T300_1000_steps(solver):
     lat = lattice.bcc(4, [1.3, 0.7], 2.2).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(2), (2, lat.natom, 3))
@@ -56,7 +56,7 @@ def test_bcc_philox_T300_1000_steps(solver):
     sim.close()
 
 
-@pytest.mark.parametrize("solver", [1, 4, 5])
+@pytest.mark.parametrize("solver", [1, 4, 5, 7])
 def test_injected_reference_noise_1000_steps(solver):
     """The reference's own ziggurat normal stream injected into the GPU."""
     lat = lattice.bcc(3, [1.3, 0.7], 2.2)
@@ -195,7 +195,7 @@ def test_llgi_1000_steps(kind, temp, tau):
     sim.close()
 
 
-@pytest.mark.parametrize("solver", [1, 4, 5, 6, 11])
+@pytest.mark.parametrize("solver", [1, 4, 5, 6, 7, 11])
 def test_perp_projection(solver):
     """Input perp = 'Y': the field loses its component along emom before each half-step."""
     lat = lattice.square_dmi(16, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)

@@ -116,7 +116,7 @@ def test_state_changes_between_runs_are_seen():
     assert np.max(np.abs(res[0] - res[1])) <= 1e-4
 
 
-@pytest.mark.parametrize("solver", [4, 6, 11])
+@pytest.mark.parametrize("solver", [4, 6, 7, 11])
 def test_other_solvers_T0_against_oracle(solver):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(47), (2, lat.natom, 3))
@@ -138,7 +138,7 @@ def test_other_solvers_T0_against_oracle(solver):
     sim.close()
 
 
-@pytest.mark.parametrize("solver", [1, 4, 5, 6, 11])
+@pytest.mark.parametrize("solver", [1, 4, 5, 6, 7, 11])
 def test_perp_against_oracle(solver):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(48), (2, lat.natom, 3))

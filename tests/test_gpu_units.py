@@ -29,7 +29,8 @@ def _lattice(kind):
 
 
 @pytest.mark.parametrize("prec,solver,kind", [(0, 1, "square"), (0, 4, "square"), (0, 5, "square"), (0, 6, "square"),
-                                              (0, 11, "square"), (3, 1, "square"), (3, 5, "square"), (3, 11, "square"),
+                                              (0, 7, "square"), (0, 11, "square"), (3, 1, "square"), (3, 5, "square"),
+                                              (3, 7, "square"), (3, 11, "square"),
                                               (1, 5, "alloy"), (2, 5, "alloy")])
 def test_llg_time_scale(prec, solver, kind):
     lat = _lattice(kind)

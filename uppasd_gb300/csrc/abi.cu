@@ -214,8 +214,9 @@ int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     if (c->do_dm && (!a->dmlist || !a->dmlistsize || !a->dm_vect || c->max_no_dmneigh <= 0))
         return bad("do_dm set but DM arrays missing");
     if (c->do_aniso && (!a->taniso || !a->eaniso || !a->kaniso)) return bad("do_aniso set but anisotropy arrays missing");
-    if (!(c->sdealgh == 1 || c->sdealgh == 4 || c->sdealgh == 5 || c->sdealgh == 6 || c->sdealgh == 11))
-        return bad("SDEalgh must be 1, 4, 5, 6 or 11");
+    if (!(c->sdealgh == 1 || c->sdealgh == 4 || c->sdealgh == 5 || c->sdealgh == 6 || c->sdealgh == 7 ||
+          c->sdealgh == 11))
+        return bad("SDEalgh must be 1, 4, 5, 6, 7 or 11");
     if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
     if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
     if (c->precision < 0 || c->precision > 3) return bad("precision must be 0, 1, 2 or 3");

@@ -98,6 +98,38 @@ __device__ __forceinline__ void sib_fixed_point(const double e1[3], const double
     }
 }
 
+// sispht / sisphf (Evolution/sphmidpoint.f90:485-923, SDEalgh 7): the SIB iteration with
+// the midpoint direction normalised, u = (e1 + efp0) / |e1 + efp0|.  efp is the last
+// iterate; f0 the one before it when the tolerance ended the loop (else the last one).
+__device__ __forceinline__ void sisph_fixed_point(const double e1[3], const double a1[3], const double s1[3],
+                                                  double dtg, double sqrtdtg, double efp[3], double f0[3]) {
+    const double epsilona = (double)1e-12f;  // REAL(4) literal in sphmidpoint.f90
+    f0[0] = e1[0];
+    f0[1] = e1[1];
+    f0[2] = e1[2];
+    for (int it = 1; it <= 100; ++it) {
+        const double unorm = sqrt((e1[0] + f0[0]) * (e1[0] + f0[0]) + (e1[1] + f0[1]) * (e1[1] + f0[1]) +
+                                  (e1[2] + f0[2]) * (e1[2] + f0[2]));
+        double fd[3], fs[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double u = (e1[c] + f0[c]) / unorm;
+            fd[c] = dtg * u;
+            fs[c] = sqrtdtg * u;
+        }
+        efp[0] = e1[0] + fd[1] * a1[2] - fd[2] * a1[1] + fs[1] * s1[2] - fs[2] * s1[1];
+        efp[1] = e1[1] + fd[2] * a1[0] - fd[0] * a1[2] + fs[2] * s1[0] - fs[0] * s1[2];
+        efp[2] = e1[2] + fd[0] * a1[1] - fd[1] * a1[0] + fs[0] * s1[1] - fs[1] * s1[0];
+        double dx = sqrt((f0[0] - efp[0]) * (f0[0] - efp[0]));
+        double dy = sqrt((f0[1] - efp[1]) * (f0[1] - efp[1]));
+        double dz = sqrt((f0[2] - efp[2]) * (f0[2] - efp[2]));
+        if (dx < epsilona && dy < epsilona && dz < epsilona) break;
+        f0[0] = efp[0];
+        f0[1] = efp[1];
+        f0[2] = efp[2];
+    }
+}
+
 // llgiheun (Evolution/llgi.f90:178-278): m_new = A^-1 B, A = I + beta [e1]x, from
 // m(t) = e1, m(t - dt) = et and the field h.
 __device__ __forceinline__ void llgi_heun(double lam, double delta_t, double gama, double relaxtime,
@@ -175,7 +207,7 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
         a.b2.x[o] = bdup[0];
         a.b2.y[o] = bdup[1];
         a.b2.z[o] = bdup[2];
-    } else if (ALG == 1 || ALG == 6) {
+    } else if (ALG == 1 || ALG == 6 || ALG == 7) {
         double r[3] = {0.0, 0.0, 0.0};
         if (a.noise_on) {
             noise3(a.nz, i, k, N, M, step, z);
@@ -197,12 +229,20 @@ __global__ void __launch_bounds__(256) llg_predict(StepArgs a) {
             cayley(A, e, et, detAi);
 #pragma unroll
             for (int c = 0; c < 3; ++c) v[c] = 0.5 * (e[c] + et[c] * detAi);
-        } else {
+        } else if (ALG == 6) {
             double a1[3], s1[3], efp[3];
             sib_a1s1(lam, e, B, r, a1, s1);
             sib_fixed_point(e, a1, s1, dtg, sqrtdtg, efp);
 #pragma unroll
             for (int c = 0; c < 3; ++c) v[c] = 0.5 * (e[c] + efp[c]);
+        } else {  // sispht: the normalised midpoint of e and the iterate it continues from
+            double a1[3], s1[3], efp[3], f0[3];
+            sib_a1s1(lam, e, B, r, a1, s1);
+            sisph_fixed_point(e, a1, s1, dtg, sqrtdtg, efp, f0);
+            const double unorm = sqrt((e[0] + f0[0]) * (e[0] + f0[0]) + (e[1] + f0[1]) * (e[1] + f0[1]) +
+                                      (e[2] + f0[2]) * (e[2] + f0[2]));
+#pragma unroll
+            for (int c = 0; c < 3; ++c) v[c] = (e[c] + f0[c]) / unorm;
         }
         a.p.x[o] = v[0];
         a.p.y[o] = v[1];
@@ -278,7 +318,7 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
     double pr[3] = {a.p.x[o], a.p.y[o], a.p.z[o]};
     // after the first half-step emom is m(t) for midpoint and SIB, the predictor for
     // Heun, Depondt and LLGI
-    if (a.perp) perp_project(B, (ALG == 1 || ALG == 6) ? e : pr);
+    if (a.perp) perp_project(B, (ALG == 1 || ALG == 6 || ALG == 7) ? e : pr);
     double out[3];
     double z[3];
     if (ALG == 5) {
@@ -293,7 +333,7 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
         bdup[1] = 0.50 * bdup[1] + 0.50 * a.b2.y[o];
         bdup[2] = 0.50 * bdup[2] + 0.50 * a.b2.z[o];
         rodrigues(bdup, e, a.delta_t, a.h.gama, 1.0 / (1.0 + lam * lam), out);
-    } else if (ALG == 1 || ALG == 6) {
+    } else if (ALG == 1 || ALG == 6 || ALG == 7) {
         double r[3] = {0.0, 0.0, 0.0};
         if (a.noise_on) {
             noise3(a.nz, i, k, N, M, step, z);
@@ -314,10 +354,14 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
             cayley(A, e, et, detAi);
 #pragma unroll
             for (int c = 0; c < 3; ++c) out[c] = et[c] * detAi;
-        } else {
+        } else if (ALG == 6) {
             double a1[3], s1[3];
             sib_a1s1(lam, pr, B, r, a1, s1);
             sib_fixed_point(e, a1, s1, dtg, sqrtdtg, out);
+        } else {  // sisphf keeps the last iterate
+            double a1[3], s1[3], f0[3];
+            sib_a1s1(lam, pr, B, r, a1, s1);
+            sisph_fixed_point(e, a1, s1, dtg, sqrtdtg, out, f0);
         }
     } else if (ALG == 11) {
         // llgi_evolve_second: the same btherm as the predictor (same counter), averaged
@@ -426,6 +470,7 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     case 4: launch_pair<4>(s, a, grid, phase); break;
     case 5: launch_pair<5>(s, a, grid, phase); break;
     case 6: launch_pair<6>(s, a, grid, phase); break;
+    case 7: launch_pair<7>(s, a, grid, phase); break;
     case 11: launch_pair<11>(s, a, grid, phase); break;
     default: set_error("unsupported SDEalgh"); return UPPASD_GPU_EUNSUPPORTED;
     }

@@ -118,6 +118,37 @@ __device__ __forceinline__ void sib_f32(float lam, const float e[3], const float
     }
 }
 
+// Spherical SIB (sispht / sisphf, sphmidpoint.f90:485-923) in FP32: the SIB iteration with
+// the midpoint direction u = (e1 + f0) / |e1 + f0|.  out is the last iterate, f0 the one
+// before it when the tolerance ended the loop (else the last one).
+__device__ __forceinline__ void sisph_f32(float lam, const float e[3], const float b[3], const float r[3],
+                                          const float e1[3], float dtg, float sqrtdtg, float out[3], float f0[3]) {
+    const float a1[3] = {-b[0] - lam * (e[1] * b[2] - e[2] * b[1]), -b[1] - lam * (e[2] * b[0] - e[0] * b[2]),
+                         -b[2] - lam * (e[0] * b[1] - e[1] * b[0])};
+    const float s1[3] = {-r[0] - lam * (e[1] * r[2] - e[2] * r[1]), -r[1] - lam * (e[2] * r[0] - e[0] * r[2]),
+                         -r[2] - lam * (e[0] * r[1] - e[1] * r[0])};
+    f0[0] = e1[0];
+    f0[1] = e1[1];
+    f0[2] = e1[2];
+    for (int it = 0; it < 100; ++it) {
+        const float w[3] = {e1[0] + f0[0], e1[1] + f0[1], e1[2] + f0[2]};
+        const float inv = 1.0f / sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+        float fd[3], fs[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            fd[c] = dtg * w[c] * inv;
+            fs[c] = sqrtdtg * w[c] * inv;
+        }
+        out[0] = e1[0] + fd[1] * a1[2] - fd[2] * a1[1] + fs[1] * s1[2] - fs[2] * s1[1];
+        out[1] = e1[1] + fd[2] * a1[0] - fd[0] * a1[2] + fs[2] * s1[0] - fs[0] * s1[2];
+        out[2] = e1[2] + fd[0] * a1[1] - fd[1] * a1[0] + fs[0] * s1[1] - fs[1] * s1[0];
+        if (fabsf(f0[0] - out[0]) < 2e-7f && fabsf(f0[1] - out[1]) < 2e-7f && fabsf(f0[2] - out[2]) < 2e-7f) break;
+        f0[0] = out[0];
+        f0[1] = out[1];
+        f0[2] = out[2];
+    }
+}
+
 // Heun drift a = lam h + e x h - e (e . lam h) and diffusion matrix b of one half
 // (heun_proper.f90:28-161, 261-530); zzq reproduces the corrector's b1zz expression.
 __device__ __forceinline__ void heun_ab(float lam, const float e[3], const float h[3], bool zzq, float a[3],
@@ -179,7 +210,7 @@ template <int ALG>
 __device__ __forceinline__ void noise_f32(const MixArgs &a, int i, int k, int64_t step, float lam, float mm,
                                           float out[3]) {
     float z[3];
-    if ((ALG == 1 || ALG == 6) && !a.noise_on) {
+    if ((ALG == 1 || ALG == 6 || ALG == 7) && !a.noise_on) {
         out[0] = out[1] = out[2] = 0.f;
         return;
     }
@@ -255,16 +286,26 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         const float g = (float)a.landeg[i];
         const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
         float et[3];
-        if (ALG == 1) {
-            float A[3];
-            midpoint_A_f32(lam, dtg, sqrtdtg, e, B, r, A);
-            cayley_f32(A, e, et);
+        if (ALG == 7) {
+            float f0[3];
+            sisph_f32(lam, e, B, r, e, dtg, sqrtdtg, et, f0);
+            const float w[3] = {e[0] + f0[0], e[1] + f0[1], e[2] + f0[2]};
+            const float inv = 1.0f / sqrtf(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            p[0] = w[0] * inv;
+            p[1] = w[1] * inv;
+            p[2] = w[2] * inv;
         } else {
-            sib_f32(lam, e, B, r, e, dtg, sqrtdtg, et);
+            if (ALG == 1) {
+                float A[3];
+                midpoint_A_f32(lam, dtg, sqrtdtg, e, B, r, A);
+                cayley_f32(A, e, et);
+            } else {
+                sib_f32(lam, e, B, r, e, dtg, sqrtdtg, et);
+            }
+            p[0] = 0.5f * (e[0] + et[0]);
+            p[1] = 0.5f * (e[1] + et[1]);
+            p[2] = 0.5f * (e[2] + et[2]);
         }
-        p[0] = 0.5f * (e[0] + et[0]);
-        p[1] = 0.5f * (e[1] + et[1]);
-        p[2] = 0.5f * (e[2] + et[2]);
     }
     a.c.mp[o] = make_float4(p[0], p[1], p[2], mm);
 }
@@ -282,7 +323,7 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     const float4 me = a.c.mt[o], mpv = a.c.mp[o];
     const float e[3] = {me.x, me.y, me.z}, pr[3] = {mpv.x, mpv.y, mpv.z};
     // emom at the second half-step: m(t) for midpoint and SIB, the predictor otherwise
-    if (a.perp) perp_f32(B, (ALG == 1 || ALG == 6) ? e : pr);
+    if (a.perp) perp_f32(B, (ALG == 1 || ALG == 6 || ALG == 7) ? e : pr);
     const float lam = (float)a.lambda[i], mm = me.w;
     float r[3];
     noise_f32<ALG>(a, i, k, step, lam, mm, r);
@@ -327,8 +368,11 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
             float A[3];
             midpoint_A_f32(lam, dtg, sqrtdtg, pr, B, r, A);
             cayley_f32(A, e, out);
-        } else {
+        } else if (ALG == 6) {
             sib_f32(lam, pr, B, r, e, dtg, sqrtdtg, out);
+        } else {
+            float f0[3];
+            sisph_f32(lam, pr, B, r, e, dtg, sqrtdtg, out, f0);
         }
         unit = true;
     }
@@ -469,7 +513,7 @@ int mixed_coefficients(Sim &s) {
 
 int mixed_init(Sim &s) {
     if (!(s.llg.sdealgh == 1 || s.llg.sdealgh == 4 || s.llg.sdealgh == 5 || s.llg.sdealgh == 6 ||
-          s.llg.sdealgh == 11)) {
+          s.llg.sdealgh == 7 || s.llg.sdealgh == 11)) {
         set_error("precision 3 (FP32 gather, FP64 master): unknown SDEalgh");
         return UPPASD_GPU_EUNSUPPORTED;
     }
@@ -571,6 +615,7 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     case 4: run(std::integral_constant<int, 4>{}); break;
     case 5: run(std::integral_constant<int, 5>{}); break;
     case 6: run(std::integral_constant<int, 6>{}); break;
+    case 7: run(std::integral_constant<int, 7>{}); break;
     case 11: run(std::integral_constant<int, 11>{}); break;
     default: set_error("unsupported SDEalgh"); return UPPASD_GPU_EUNSUPPORTED;
     }

@@ -18,7 +18,7 @@ import numpy as np
 from . import _lib
 from .lattice import Lattice
 
-SOLVERS = {"midpoint": 1, "heun": 4, "depondt": 5, "sib": 6, "llgi": 11}
+SOLVERS = {"midpoint": 1, "heun": 4, "depondt": 5, "sib": 6, "sisph": 7, "llgi": 11}
 
 
 def _ptr(a, t=_lib.F64P):
