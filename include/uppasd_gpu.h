@@ -52,7 +52,8 @@ typedef struct {
     int32_t max_no_neigh, nham;        /* ncoup is (max_no_neigh, nham) */
     int32_t do_dm, max_no_dmneigh;
     int32_t do_aniso;
-    int32_t sdealgh;                   /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point, 11 LLGI */
+    int32_t sdealgh;                   /* 1 midpoint, 4 Heun, 5 Depondt, 6 SIB fixed point,
+                                          7 spherical SIB fixed point, 11 LLGI */
     double delta_t, bn, temprescale;
     uint64_t gpu_rng_seed;             /* Philox key (gpu_rng_seed keyword) */
     int32_t gpu_rng;                   /* 0 Philox in-kernel, 1 caller-injected normals */
