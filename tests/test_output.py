@@ -86,3 +86,21 @@ def test_totenergy_layout_and_deviation(tmp_path):
     lines = open(tmp_path / "totenergy.j.out").read().splitlines()
     assert lines[0].split()[2] == "Heis-Tens" and len(lines[0]) == 8 + 11 * 16
     assert len(lines[1]) == 8 + 11 * 16
+
+
+def test_restart_layouts_round_trip(tmp_path, pins):
+    """The reference's default restart layout (prn_mag_conf_iter) and the legacy one read back
+    by read_restart as read_mag_conf_std does; the HeisChain start file's moments (taken from
+    the reference's tests/HeisChain/startmom) survive a write and a read to the printed digits."""
+    rows = np.asarray(pins["inputs"]["heischain"]["restart"])
+    e = rows[:, 1:4][None]
+    m = rows[:, 0][None]
+    for writer, name in ((output.write_restart_std, "restart.std.out"), (output.write_restart, "restart.leg.out")):
+        p = str(tmp_path / name)
+        writer(p, 0, e, m)
+        step, e2, m2 = output.read_restart(p, rows.shape[0], 1)
+        assert step == 0 and np.array_equal(m2, m)
+        assert np.max(np.abs(e2 - e / np.linalg.norm(e, axis=-1, keepdims=True))) < 1e-8
+    lines = open(tmp_path / "restart.std.out").read().splitlines()
+    assert lines[0] == "#" * 80 and lines[1] == "# File type: R" and len(lines) == 7 + rows.shape[0]
+    assert lines[7].split()[:3] == ["0", "1", "1"] and len(lines[7]) == 24 + 2 + 4 * 16

@@ -20,7 +20,12 @@ by the reference's own regression harness (its tests read these files by column)
   (prn_averages.f90:662-804): averages projected per atom type ('Y') or per basis
   atom ('A'), see ``projected_averages``.
 * ``write_restart`` -- the legacy ``restart.<simid>.out`` of prnrestart
-  (System/restart.f90): ``(i8)`` step, then ``(i8,i8,2x,4es16.8)`` per atom.
+  (System/restart.f90:720-751): ``(i8)`` step, then ``(i8,i8,2x,4es16.8)`` per atom.
+* ``write_restart_std`` -- the restart file of prn_mag_conf_iter with type 'R'
+  (System/restart.f90:186-246), what the reference writes and reads by default
+  (do_mom_legacy = 'N'): a seven-line header, then ``(i8,i8,i8,2x,4es16.8)`` per atom.
+* ``read_restart`` -- read_mag_conf_std (System/restart.f90:320-381) for either layout:
+  moments normalised as there, the step from the file.
 * ``sd_run_with_averages`` -- the measurement cadence of sd_mphase: a row every
   ``avrg_step`` steps starting at iteration 0.
 """
@@ -226,6 +231,47 @@ def write_restart(path: str, mstep: int, emom, mmom):
             for i in range(emom.shape[1]):
                 f.write(f"{k + 1:8d}{i + 1:8d}  " + fortran_es(mmom[k, i]) +
                         "".join(fortran_es(v) for v in emom[k, i]) + "\n")
+
+
+def write_restart_std(path: str, mstep: int, emom, mmom, mode: str = "S"):
+    """emom (Mensemble, Natom, 3) unit vectors, mmom (Mensemble, Natom)."""
+    emom = np.asarray(emom, dtype=np.float64)
+    mmom = np.broadcast_to(np.asarray(mmom, dtype=np.float64), emom.shape[:2])
+    m, n = emom.shape[:2]
+    with open(path, "w") as f:
+        f.write("#" * 80 + "\n")
+        f.write("# File type: R\n")
+        f.write(f"# Simulation type: {mode}\n")
+        f.write(f"# Number of atoms:  {n:8d}\n")
+        f.write(f"# Number of ensembles:  {m:8d}\n")
+        f.write("#" * 80 + "\n")
+        f.write("".join(fortran_a(h, w) for h, w in (("# iter", 8), ("ens", 8), ("iatom", 8), ("|Mom|", 16),
+                                                      ("M_x", 16), ("M_y", 16), ("M_z", 16))) + "\n")
+        for k in range(m):
+            for i in range(n):
+                f.write(f"{int(mstep):8d}{k + 1:8d}{i + 1:8d}  " + fortran_es(mmom[k, i]) +
+                        "".join(fortran_es(v) for v in emom[k, i]) + "\n")
+
+
+def read_restart(path: str, natom: int, mensemble: int):
+    """(step, emom (Mensemble, Natom, 3) normalised, mmom (Mensemble, Natom)) from either the
+    standard (seven header lines) or the legacy restart layout."""
+    with open(path) as f:
+        lines = f.read().splitlines()
+    if lines and lines[0].startswith("#"):
+        rows = [ln.split() for ln in lines[7:] if ln.strip()]
+        step = int(rows[0][0])
+        vals = np.array([[float(v) for v in r[3:7]] for r in rows[:natom * mensemble]])
+    else:
+        step = int(lines[0].split()[0])
+        rows = [ln.split() for ln in lines[1:] if ln.strip()]
+        vals = np.array([[float(v) for v in r[2:6]] for r in rows[:natom * mensemble]])
+    if vals.shape[0] != natom * mensemble:
+        raise ValueError(f"{path}: {vals.shape[0]} moments, expected {natom * mensemble}")
+    vals = vals.reshape(mensemble, natom, 4)
+    e = vals[..., 1:4]
+    e = e / np.sqrt(np.sum(e * e, axis=-1))[..., None]
+    return step, np.ascontiguousarray(e), np.ascontiguousarray(vals[..., 0])
 
 
 def read_columns(path: str):
