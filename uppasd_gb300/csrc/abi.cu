@@ -95,6 +95,53 @@ __global__ void soa_to_aos(Vec3D v, double *aos, int64_t n) {
     aos[3 * t + 2] = v.z[t];
 }
 
+// The same conversions one 256-site block at a time through shared memory, so that every
+// warp access to the AoS side is one contiguous run of doubles: these read or write the
+// caller's page-locked host buffer directly (over the CPU-GPU link, no staging copy).
+__global__ void __launch_bounds__(256) aos_to_soa_blocked(const double *aos, Vec3D e, Vec3D eM, const double *mmom,
+                                                          int64_t n) {
+    __shared__ double buf[3 * 256];
+    const int64_t base = (int64_t)blockIdx.x * 256;
+    const int cnt = (int)(n - base < 256 ? n - base : 256);
+    for (int q = threadIdx.x; q < 3 * cnt; q += 256) buf[q] = aos[3 * base + q];
+    __syncthreads();
+    if ((int)threadIdx.x >= cnt) return;
+    const int64_t t = base + threadIdx.x;
+    const double x = buf[3 * threadIdx.x], y = buf[3 * threadIdx.x + 1], z = buf[3 * threadIdx.x + 2];
+    const double m = mmom[t];
+    e.x[t] = x;
+    e.y[t] = y;
+    e.z[t] = z;
+    eM.x[t] = x * m;
+    eM.y[t] = y * m;
+    eM.z[t] = z * m;
+}
+
+__global__ void __launch_bounds__(256) soa_to_aos_blocked(Vec3D v, double *aos, int64_t n) {
+    __shared__ double buf[3 * 256];
+    const int64_t base = (int64_t)blockIdx.x * 256;
+    const int cnt = (int)(n - base < 256 ? n - base : 256);
+    if ((int)threadIdx.x < cnt) {
+        const int64_t t = base + threadIdx.x;
+        buf[3 * threadIdx.x] = v.x[t];
+        buf[3 * threadIdx.x + 1] = v.y[t];
+        buf[3 * threadIdx.x + 2] = v.z[t];
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < 3 * cnt; q += 256) aos[3 * base + q] = buf[q];
+}
+
+// A device-usable address of `p` when it is page-locked host memory (cudaHostAlloc or
+// cudaHostRegister: mapped under unified addressing); nullptr for pageable memory.
+static void *mapped_host(const void *p) {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pa.type == cudaMemoryTypeHost ? pa.devicePointer : nullptr;
+}
+
 __global__ void advance_step(int64_t *d_step, int64_t n) { *d_step += n; }
 
 int check_device(Sim &s) {
@@ -498,21 +545,34 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
     Sim &s = w->s;
     uppasd::square_mirror_stale(s);
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
-    double *d = uppasd::stage_buffer(s);
-    if (!d) return UPPASD_GPU_ENOMEM;
-    cudaError_t e = cudaMemcpyAsync(d, emom, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.stream);
-    if (e == cudaSuccess) {
-        uppasd::aos_to_soa<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(d, s.e, s.eM, s.llg.mmom, n);
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    cudaError_t e = cudaSuccess;
+    if (const double *h = static_cast<const double *>(uppasd::mapped_host(emom))) {
+        // page-locked caller buffer: the conversion kernel reads it in place
+        uppasd::aos_to_soa_blocked<<<grid, 256, 0, s.stream>>>(h, s.e, s.eM, s.llg.mmom, n);
         e = cudaGetLastError();
+    } else {
+        double *d = uppasd::stage_buffer(s);
+        if (!d) return UPPASD_GPU_ENOMEM;
+        e = cudaMemcpyAsync(d, emom, 3 * n * sizeof(double), cudaMemcpyHostToDevice, s.stream);
+        if (e == cudaSuccess) {
+            uppasd::aos_to_soa<<<grid, 256, 0, s.stream>>>(d, s.e, s.eM, s.llg.mmom, n);
+            e = cudaGetLastError();
+        }
     }
     // SDEalgh 11: a new state has no previous step (the reference's mpast starts at zero, llgi.f90:295)
     for (double *q : {s.mpast.x, s.mpast.y, s.mpast.z})
         if (e == cudaSuccess && q) e = cudaMemsetAsync(q, 0, n * sizeof(double), s.stream);
+    if (e == cudaSuccess && uppasd::structured(s)) {
+        int rc = uppasd::structured_load_state(s);
+        if (rc) return rc;
+    }
+    // the caller may reuse its buffer once this returns
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) {
         uppasd::set_error(std::string("put_moments: ") + cudaGetErrorString(e));
         return UPPASD_GPU_ECUDA;
     }
-    if (uppasd::structured(s)) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;
 }
 
@@ -525,18 +585,21 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
     int rc;
     if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
-    double *d = uppasd::stage_buffer(s);
-    if (!d) return UPPASD_GPU_ENOMEM;
     cudaError_t e = cudaSuccess;
     const unsigned grid = (unsigned)((n + 255) / 256);
-    if (emom) {
-        uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.e, d, n);
-        e = cudaMemcpyAsync(emom, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
-    }
-    if (e == cudaSuccess && emomM) {
-        uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.eM, d, n);
-        e = cudaMemcpyAsync(emomM, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
-    }
+    auto copy_out = [&](const uppasd::Vec3D &v, double *out) {
+        if (double *h = static_cast<double *>(uppasd::mapped_host(out))) {
+            // page-locked caller buffer: the conversion kernel writes it in place
+            uppasd::soa_to_aos_blocked<<<grid, 256, 0, s.stream>>>(v, h, n);
+            return cudaGetLastError();
+        }
+        double *d = uppasd::stage_buffer(s);
+        if (!d) return cudaErrorMemoryAllocation;
+        uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(v, d, n);
+        return cudaMemcpyAsync(out, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);
+    };
+    if (emom) e = copy_out(s.e, emom);
+    if (e == cudaSuccess && emomM) e = copy_out(s.eM, emomM);  // stream order keeps the staging array safe
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
     if (e != cudaSuccess) {
         uppasd::set_error(std::string("get_moments: ") + cudaGetErrorString(e));
