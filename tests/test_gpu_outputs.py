@@ -51,4 +51,5 @@ def test_energy_terms_match_oracle_and_write_totenergy(tmp_path, kind):
     f.write(0, t)
     row = output.read_columns(str(tmp_path / "totenergy.x.out"))[0]
     assert np.isclose(row[1], ref["total"].mean(), rtol=1e-8)
+    assert np.isclose(sim.calculate_energy(), ref["total"].mean(), rtol=1e-12) and sim.energy == sim.calculate_energy()
     sim.close()

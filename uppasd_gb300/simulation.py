@@ -230,6 +230,13 @@ class GpuSimulation:
         _lib.call("uppasd_gpu_energy_terms", self._h, _ptr(t))
         return dict(zip(("total", "xc", "ani", "dm", "ext"), t.T.copy()))
 
+    def calculate_energy(self) -> float:
+        """The reference simulator's calculate_energy (uppasd/simulator.py): the total
+        energy in mRy per atom, averaged over the ensembles as calc_energy prints it;
+        also kept in ``self.energy``."""
+        self.energy = float(np.mean(self.energy_terms()["total"]))
+        return self.energy
+
 
 def device_info():
     sm = C.c_int32()
