@@ -374,3 +374,22 @@ def test_reference_gpu_cases(pins, name, mavg_at, cumulant_row):
 
     mrow, crow = replay_reference_gpu_case(pins, name, mavg_at, cumulant_row, {"step": step, "mavg": mavg})
     check_reference_gpu_case(pins, name, mrow, crow)
+
+
+def test_from_tables_matches_the_bcc_builder(pins):
+    """The table-driven builder on the bccFe_cuda tables (one type, two sites, four cubic
+    shells) gives the same neighbours and couplings as the bcc builder, site by site, and
+    the cubic images of the first two shells come in the order get_fullnnlist keeps them."""
+    inp = pins["inputs"]["bccfe_cuda"]
+    lat, _ = from_tables(inp)
+    js = [r[5] for r in inp["jfile"]]
+    ref = lattice.bcc(inp["ncell"][0], js, inp["sites"][0][4])
+    assert lat.natom == ref.natom and np.array_equal(lat.nlistsize, ref.nlistsize)
+    for i in range(lat.natom):
+        a = sorted(zip(lat.nlist[i, :lat.nlistsize[i]], lat.ncoup[i, :lat.nlistsize[i]]))
+        b = sorted(zip(ref.nlist[i, :ref.nlistsize[i]], ref.ncoup[i, :ref.nlistsize[i]]))
+        assert [x[0] for x in a] == [x[0] for x in b]
+        assert np.allclose([x[1] for x in a], [x[1] for x in b], rtol=1e-14, atol=0)
+    img = [tuple(v) for v in lattice.cubic_images((0.5, 0.5, 0.5))]
+    assert len(img) == 8 and img[0] == (0.5, 0.5, 0.5) and img[-1] == (-0.5, -0.5, -0.5)
+    assert [tuple(v) for v in lattice.cubic_images((1.0, 0.0, 0.0))][:2] == [(1.0, 0.0, 0.0), (-1.0, 0.0, 0.0)]
