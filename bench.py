@@ -94,6 +94,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.first = 0
 
     def __enter__(self):
         try:
@@ -107,6 +108,7 @@ class ClockSampler:
             t0 = time.perf_counter()
             while not self.lines and time.perf_counter() - t0 < 3.0 and self.proc.poll() is None:
                 time.sleep(0.01)
+            self.first = len(self.lines)
         except OSError:
             self.proc = None
         return self
@@ -126,7 +128,8 @@ class ClockSampler:
     def summary(self):
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # the samples taken once the region had begun (the one before it when there are none)
+        for ln in self.lines[self.first:] or self.lines:
             f = [x.strip() for x in ln.split(",")]
             if len(f) < 9:
                 continue
