@@ -142,6 +142,21 @@ int uppasd_gpu_set_noise(uppasd_gpu_sim *s, const double *normals, int64_t nstep
 
 /* nsteps full LLG steps (field, predictor, field, corrector, moment update). */
 int uppasd_gpu_sd_run(uppasd_gpu_sim *s, int64_t nsteps);
+
+/* Measurement callback: the state after `step` steps, emom and emomM in the reference
+ * layout (3, natom, mensemble), library-owned host memory valid during the call.  A
+ * nonzero return stops the run. */
+typedef int (*uppasd_gpu_measure_cb)(int64_t step, const double *emom, const double *emomM, void *user);
+
+/* nsteps LLG steps with a measurement every `every` steps (the measure() cadence of
+ * sd_mphase, sd_driver.f90:554-579; the reference's GPU path hands its measurements to a
+ * host thread, gpu_files/measurementQueue.cpp:10-80).  The copy of each snapshot to the
+ * host overlaps the next block of steps; the callbacks come in order on the calling
+ * thread, each once the following block has been issued.  A nonzero callback value ends
+ * the run after the block in flight and is returned.  Steps beyond the last whole block
+ * run without a measurement. */
+int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *s, int64_t nsteps, int64_t every, uppasd_gpu_measure_cb cb,
+                               void *user);
 /* Effective field of the current state, (3, natom, mensemble). */
 int uppasd_gpu_get_field(uppasd_gpu_sim *s, double *beff);
 

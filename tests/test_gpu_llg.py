@@ -250,3 +250,31 @@ def test_page_locked_buffers_read_and_written_in_place(prec):
         sim.close()
     for a, b in zip(res[0], res[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_measured_run_equals_blocks_of_steps(prec):
+    """sd_run_measured hands over the same states, at the same steps, as blocks of sd_run
+    followed by get_moments; a callback that asks to stop ends the run after the block in
+    flight."""
+    lat = lattice.bcc_alloy(6, seed=4).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(22), (2, lat.natom, 3))
+    make = lambda: GpuSimulation(lat, sdealgh=5, temperature=300.0, seed=8, emom=e0, precision=prec)
+    a, snaps = make(), []
+    a.sd_run_measured(53, 10, lambda st, e, m: snaps.append((st, e.copy(), m.copy())))
+    b = make()
+    assert [s[0] for s in snaps] == [10, 20, 30, 40, 50]
+    for st, e, m in snaps:
+        b.evolve(10)
+        eb, mb = b.get_moments(full=True)
+        assert np.array_equal(e, eb) and np.array_equal(m, mb), st
+    b.evolve(3)
+    assert np.array_equal(a.get_moments(), b.get_moments())
+    c, seen = make(), []
+    rc = c.sd_run_measured(100, 10, lambda st, e, m: seen.append(st) or st == 20)
+    assert rc == 1 and seen == [10, 20]
+    d = make()
+    d.evolve(30)
+    assert np.array_equal(c.get_moments(), d.get_moments())
+    for s in (a, b, c, d):
+        s.close()

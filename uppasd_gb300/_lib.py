@@ -43,6 +43,9 @@ class Arrays(C.Structure):
     ]
 
 
+# uppasd_gpu_measure_cb: (step, emom, emomM, user) -> int
+MEASURE_CB = C.CFUNCTYPE(C.c_int, C.c_int64, F64P, F64P, C.c_void_p)
+
 # name -> (argtypes) ; all return int status
 SIGNATURES = {
     "uppasd_gpu_device_info": [I32P, I32P, I32P, C.POINTER(C.c_int64)],
@@ -58,6 +61,7 @@ SIGNATURES = {
     "uppasd_gpu_set_perp": [C.c_void_p, C.c_int32],
     "uppasd_gpu_set_noise": [C.c_void_p, F64P, C.c_int64],
     "uppasd_gpu_sd_run": [C.c_void_p, C.c_int64],
+    "uppasd_gpu_sd_run_measured": [C.c_void_p, C.c_int64, C.c_int64, MEASURE_CB, C.c_void_p],
     "uppasd_gpu_get_field": [C.c_void_p, F64P],
     "uppasd_gpu_mc_run": [C.c_void_p, C.c_char, C.c_double, C.c_int64],
     "uppasd_gpu_observables": [C.c_void_p, F64P, F64P, F64P],

@@ -419,6 +419,13 @@ void destroy(Sim &s) {
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
                     s.llg.inj, s.llg.d_step, s.red, s.colour_sites, s.sqm, s.stage, s.tk, s.betak};
     for (void *q : ptrs) cudaFree(q);
+    for (int b = 0; b < 2; ++b) {
+        cudaFree(s.snap_d[b]);
+        cudaFreeHost(s.snap_h[b]);
+        if (s.snap_ev[b]) cudaEventDestroy(s.snap_ev[b]);
+        if (s.copy_ev[b]) cudaEventDestroy(s.copy_ev[b]);
+    }
+    if (s.copy_stream) cudaStreamDestroy(s.copy_stream);
     free_vec3(h.ext);
     free_vec3(s.e);
     free_vec3(s.eM);
@@ -746,6 +753,64 @@ int uppasd_gpu_sd_run(uppasd_gpu_sim *w, int64_t nsteps) {
         return UPPASD_GPU_ESTATE;
     }
     return uppasd::run_steps(s, nsteps);
+}
+
+int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every, uppasd_gpu_measure_cb cb,
+                               void *user) {
+    if (!w || nsteps < 0 || every < 1 || !cb) {
+        uppasd::set_error("sd_run_measured: nsteps >= 0, every >= 1 and a callback are required");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    if (s.llg.noise_mode == 1 && (s.step < s.llg.inj_first || s.step + nsteps > s.llg.inj_first + s.llg.inj_steps)) {
+        uppasd::set_error("injected noise does not cover the requested steps");
+        return UPPASD_GPU_ESTATE;
+    }
+    const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
+    const size_t bytes = 6 * sizeof(double) * (size_t)n;  // emom then emomM
+    if (!s.copy_stream) {
+        UPPASD_CUDA_TRY(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; ++b) {
+            UPPASD_CUDA_TRY(cudaMalloc(&s.snap_d[b], bytes));
+            UPPASD_CUDA_TRY(cudaHostAlloc(&s.snap_h[b], bytes, cudaHostAllocDefault));
+            UPPASD_CUDA_TRY(cudaEventCreateWithFlags(&s.snap_ev[b], cudaEventDisableTiming));
+            UPPASD_CUDA_TRY(cudaEventCreateWithFlags(&s.copy_ev[b], cudaEventDisableTiming));
+            UPPASD_CUDA_TRY(cudaEventRecord(s.copy_ev[b], s.copy_stream));
+            s.bytes_allocated += bytes;
+        }
+    }
+    const unsigned grid = (unsigned)((n + 255) / 256);
+    const int64_t nblocks = nsteps / every;
+    int64_t pending_step = -1;
+    int rc = UPPASD_GPU_OK;
+    // Block i runs on the library's stream and leaves its snapshot in buffer i % 2; the copy
+    // stream brings it to the host while block i + 1 runs; the callback of block i is made
+    // once block i + 1 has been issued.
+    for (int64_t i = 0; i <= nblocks && rc == UPPASD_GPU_OK; ++i) {
+        const int b = (int)(i % 2);
+        if (i < nblocks) {
+            if ((rc = uppasd::run_steps(s, every))) break;
+            if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) break;
+            UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.copy_ev[b], 0));  // buffer b copied out
+            uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.e, s.snap_d[b], n);
+            uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.eM, s.snap_d[b] + 3 * n, n);
+            UPPASD_CUDA_TRY(cudaGetLastError());
+            UPPASD_CUDA_TRY(cudaEventRecord(s.snap_ev[b], s.stream));
+            UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.copy_stream, s.snap_ev[b], 0));
+            UPPASD_CUDA_TRY(cudaMemcpyAsync(s.snap_h[b], s.snap_d[b], bytes, cudaMemcpyDeviceToHost, s.copy_stream));
+            UPPASD_CUDA_TRY(cudaEventRecord(s.copy_ev[b], s.copy_stream));
+        }
+        if (pending_step >= 0) {
+            const int pb = (int)((i - 1) % 2);
+            UPPASD_CUDA_TRY(cudaEventSynchronize(s.copy_ev[pb]));
+            const int r = cb(pending_step, s.snap_h[pb], s.snap_h[pb] + 3 * n, user);
+            if (r != 0) rc = r;
+        }
+        pending_step = i < nblocks ? s.step : -1;
+    }
+    if (rc == UPPASD_GPU_OK && nsteps % every) rc = uppasd::run_steps(s, nsteps % every);
+    if (rc == UPPASD_GPU_OK) UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return rc;
 }
 
 int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {

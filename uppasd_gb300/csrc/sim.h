@@ -119,6 +119,11 @@ struct Sim {
     int sqm_valid = 0;
     MixedDev mix;
     // (3, natom, mensemble) staging array of the host transfers, kept between calls
+    // measured runs: two device snapshot pairs (emom, emomM in the reference layout), their
+    // page-locked host copies, a copy stream and the events that order them
+    double *snap_d[2] = {nullptr, nullptr}, *snap_h[2] = {nullptr, nullptr};
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t snap_ev[2] = {nullptr, nullptr}, copy_ev[2] = {nullptr, nullptr};
     double *stage = nullptr;
     // per-ensemble temperatures of mc_run_temps / pt_run: K and muB / (kB T) (FP32)
     double *tk = nullptr;

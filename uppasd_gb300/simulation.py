@@ -175,6 +175,36 @@ class GpuSimulation:
     def evolve(self, nsteps: int):
         _lib.call("uppasd_gpu_sd_run", self._h, int(nsteps))
 
+    def sd_run_measured(self, nsteps: int, every: int, fn):
+        """nsteps steps with fn(step, emom, emomM) after every `every` of them; the arrays are
+        (mensemble, natom, 3) views of library memory, valid during the call (copy to keep).
+        Each snapshot's transfer to the host overlaps the next block of steps.  A truthy
+        return value of fn stops the run after the block in flight."""
+        shape = (self.lat.mensemble, self.lat.natom, 3)
+        count = 3 * self.lat.natom * self.lat.mensemble
+        stopped = []
+
+        def cb(step, pe, pm, user):
+            try:
+                e = np.ctypeslib.as_array(pe, shape=(count,)).reshape(shape)
+                m = np.ctypeslib.as_array(pm, shape=(count,)).reshape(shape)
+                if fn(int(step), e, m):
+                    stopped.append(int(step))
+                    return 1
+                return 0
+            except Exception as exc:  # an exception ends the run; it is raised after it
+                stopped.append(exc)
+                return 1
+
+        c_cb = _lib.MEASURE_CB(cb)
+        rc = _lib.load().uppasd_gpu_sd_run_measured(self._h, int(nsteps), int(every), c_cb, None)
+        if stopped and isinstance(stopped[-1], Exception):
+            raise stopped[-1]
+        if rc < 0:
+            msg = _lib.load().uppasd_gpu_last_error()
+            raise _lib.UppasdGpuError("uppasd_gpu_sd_run_measured", rc, msg.decode() if msg else "")
+        return rc
+
     def relax(self, mode: str = "H", temperature: float = 1.0, nsweeps: int = 1, structured: bool = False):
         """Monte Carlo sweeps: mode 'M' (Metropolis) or 'H' (heat bath).  structured=True
         runs the square-lattice heat bath (FP32 draws, uniform couplings recognised at
