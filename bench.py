@@ -694,9 +694,17 @@ def run_gb300(args, w):
                 ev1.record(stream)
                 torch.cuda.synchronize()
                 msw = ev0.elapsed_time(ev1) / 8
+                # Metropolis sweeps (mc_run 'M')
+                sg.relax("M", wg["temp"], 2)
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                sg.relax("M", wg["temp"], 8)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                mswm = ev0.elapsed_time(ev1) / 8
                 sg.close()
                 gen[key] = {"ms_per_step": msg / 16, "value": lg.natom * lg.mensemble * 16 * world / (msg * 1e-3),
-                            "heat_bath_ms_per_sweep": msw}
+                            "heat_bath_ms_per_sweep": msw, "metropolis_ms_per_sweep": mswm}
             variants["general_hamiltonian"] = gen
         except Exception as exc:
             variants["general_hamiltonian"] = {"error": str(exc)}

@@ -48,7 +48,7 @@ def test_llg_time_scale(prec, solver, kind):
     assert np.array_equal(out[0], out[1])
 
 
-@pytest.mark.parametrize("prec,mode,structured", [(0, "H", False), (0, "M", False), (3, "H", False),
+@pytest.mark.parametrize("prec,mode,structured", [(0, "H", False), (0, "M", False), (3, "H", False), (3, "M", False),
                                                   (0, "H", True)])
 def test_mc_temperature_scale(prec, mode, structured):
     lat = _lattice("square")

@@ -35,6 +35,7 @@ void mixed_free(Sim &s);
 int mixed_ready(Sim &s);
 int mixed_step(Sim &s, int64_t step_offset, int phase);
 int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak = nullptr);
+int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps);
 int mixed_coefficients(Sim &s);
 
 namespace {
@@ -829,10 +830,12 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t 
     Sim &s = w->s;
     int rc;
     if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
-    // precision 3: the heat bath in FP32 on the mirror (Metropolis keeps the FP64
-    // path: its energy change follows the reference's mixed unit / full-moment terms)
-    rc = s.precision == 3 && mode == 'H' ? uppasd::mixed_heat_bath_sweeps(s, temperature, nsweeps)
-                                          : uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
+    // precision 3: heat bath and Metropolis in FP32 on the mirror
+    if (s.precision == 3)
+        rc = mode == 'H' ? uppasd::mixed_heat_bath_sweeps(s, temperature, nsweeps)
+                         : uppasd::mixed_metropolis_sweeps(s, temperature, nsweeps);
+    else
+        rc = uppasd::mc_checkerboard_sweeps(s, mode, temperature, nsweeps);
     if (rc) return rc;
     if (uppasd::structured(s)) return uppasd::structured_load_state(s);
     return UPPASD_GPU_OK;

@@ -5,6 +5,9 @@
 //                  and order as the FP64 field (Hamiltonian/hamiltonianactions.f90:187-243)
 //   heat_bath_f32  flip_h (MonteCarlo/montecarlo_common.f90:371-422) in FP32, with
 //                  the field frame built from the field's own components
+//   delta_energy_f32  calculate_energy's E(trial) - E(current) of one site in FP32
+//                  (MonteCarlo/montecarlo_common.f90:431-865), the same terms and the
+//                  same mixed unit / full-moment DM current-energy term as the FP64 path
 #pragma once
 #include "common.cuh"
 #include "sim.h"
@@ -82,6 +85,87 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
     B[0] = bs[0] + (bq[0] + ex.x);
     B[1] = bs[1] + (bq[1] + ex.y);
     B[2] = bs[2] + (bq[2] + ex.z);
+}
+
+// E(trial) - E(current) of site i for the trial unit vector nm (before the factor mub),
+// exchange (scalar or tensor) and DMI from the neighbours on the mirror m, anisotropy and
+// Zeeman; the DM current energy keeps the reference's unit-moment components
+// (montecarlo_common.f90:609-617).
+__device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDev &c, const float4 *m, int i, int k,
+                                                  const float nm[3]) {
+    const int N = h.natom;
+    const size_t off = (size_t)k * N;
+    const int ih = h.aham[i];
+    const float4 me = m[off + i];
+    const float mm = me.w;
+    const float ei[3] = {me.x, me.y, me.z};
+    const float mi[3] = {mm * me.x, mm * me.y, mm * me.z};
+    const float tm[3] = {mm * nm[0], mm * nm[1], mm * nm[2]};
+    const float dm[3] = {tm[0] - mi[0], tm[1] - mi[1], tm[2] - mi[2]};
+    float b[3] = {0.f, 0.f, 0.f};
+    const int nn = h.nsize[i];
+    if (h.do_jtensor) {
+        for (int s = 0; s < nn; ++s) {
+            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const float4 v = m[off + j];
+            const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
+            const float *J = c.jt + ((size_t)s * h.nham + ih) * 9;
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                b[a] += __ldg(&J[3 * a]) * m1 + __ldg(&J[3 * a + 1]) * m2 + __ldg(&J[3 * a + 2]) * m3;
+        }
+    } else {
+        for (int s = 0; s < nn; ++s) {
+            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const float4 v = m[off + j];
+            const float cj = __ldg(&c.nc[(size_t)s * h.nham + ih]) * v.w;
+            b[0] = fmaf(cj, v.x, b[0]);
+            b[1] = fmaf(cj, v.y, b[1]);
+            b[2] = fmaf(cj, v.z, b[2]);
+        }
+    }
+    // bilinear exchange: E_t - E_c = -(t - m_i) . b
+    float de = -(dm[0] * b[0] + dm[1] * b[1] + dm[2] * b[2]);
+    if (h.do_dm) {
+        const int nd = h.dmsize[i];
+        for (int s = 0; s < nd; ++s) {
+            const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
+            const float4 d = __ldg(&c.dm[(size_t)s * h.nham + ih]);
+            const float4 v = m[off + j];
+            const float mj0 = v.w * v.x, mj1 = v.w * v.y, mj2 = v.w * v.z;
+            const float et = d.x * (tm[1] * mj2 - tm[2] * mj1) + d.y * (tm[2] * mj0 - tm[0] * mj2) +
+                             d.z * (tm[0] * mj1 - tm[1] * mj0);
+            const float ec = d.x * (mi[1] * mj2 - ei[2] * mj1) + d.y * (mi[2] * mj0 - mi[0] * mj2) +
+                             d.z * (ei[0] * mj1 - mi[1] * mj0);
+            de -= et - ec;
+        }
+    }
+    if (h.do_aniso) {
+        const int ta = h.taniso[i];
+        const float4 an = __ldg(&c.an[i]);
+        const float2 an2 = __ldg(&c.an2[i]);
+        const float ka0 = an.w, ka1 = an2.x;
+        if (ta == 1 || ta == 7) {
+            const float tta = mi[0] * an.x + mi[1] * an.y + mi[2] * an.z;
+            const float ttb = tm[0] * an.x + tm[1] * an.y + tm[2] * an.z;
+            const float a2 = tta * tta, b2 = ttb * ttb;
+            de += ka0 * (b2 - a2) + ka1 * (b2 * b2 - a2 * a2);
+        }
+        if (ta == 2 || ta == 7) {
+            // cubic: -K (x2 y2 + y2 z2 + z2 x2) - K2 x2 y2 z2 (ta 2), +sb times that (ta 7)
+            const float sgn = ta == 2 ? -1.0f : an2.y;
+            float x2 = mi[0] * mi[0], y2 = mi[1] * mi[1], z2 = mi[2] * mi[2];
+            const float cc = ka0 * (x2 * y2 + y2 * z2 + z2 * x2) + ka1 * (x2 * y2 * z2);
+            x2 = tm[0] * tm[0];
+            y2 = tm[1] * tm[1];
+            z2 = tm[2] * tm[2];
+            const float ct = ka0 * (x2 * y2 + y2 * z2 + z2 * x2) + ka1 * (x2 * y2 * z2);
+            de += sgn * (ct - cc);
+        }
+    }
+    const float4 ex = __ldg(&c.ext[off + i]);
+    de -= ex.x * dm[0] + ex.y * dm[1] + ex.z * dm[2];
+    return de;
 }
 
 // flip_h in FP32: x = beta_mu |h|; 1 - cos(theta) = -ln((1 - e^-2x) q + e^-2x + tol) / x

@@ -439,6 +439,65 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec
     eM.z[o] = md * z;
 }
 
+// Metropolis on the mirror (mc_evolve with flip_a, MonteCarlo/montecarlo.f90:44-273,
+// montecarlo_common.f90:139-200): the trial of choose_random_flip (:25-79) from the same
+// Philox words as the FP64 path, the energy change in FP32, acceptance when it is <= 0 or
+// u < exp(-beta de); an accepted spin is renormalised in FP64 and written to the mirror and
+// the FP64 state.
+__global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, Vec3D e, Vec3D eM, const double *mmom,
+                                                        const int32_t *sites, int nsites, float beta_mub, float delta,
+                                                        uint64_t seed, int64_t sweep) {
+    const int N = h.natom;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nsites * h.mensemble) return;
+    const int k = (int)(t / nsites);
+    const int i = sites[t - (int64_t)k * nsites];
+    const size_t o = (size_t)k * N + i;
+    float4 *mt = c.mt;
+    const float4 cur = mt[o];
+    const Philox4 w = philox_draw(seed, i, k, sweep, kStreamMC);
+    const float k32 = 2.3283064365386963e-10f;
+    const float u0 = fmaf((float)w.x, k32, 0.5f * k32), u1 = fmaf((float)w.y, k32, 0.5f * k32);
+    const float u2 = fmaf((float)w.z, k32, 0.5f * k32), u3 = fmaf((float)w.w, k32, 0.5f * k32);
+    float nm[3];
+    const int ftype = (int)floorf(3.0f * u0);
+    if (ftype == 0) {  // uniform on the sphere
+        const float ct = 1.0f - 2.0f * u2, st = sqrtf(fmaxf(0.0f, 1.0f - ct * ct));
+        float sp, cp;
+        __sincosf(u1 * 2.0f * 3.14159265358979f, &sp, &cp);
+        nm[0] = st * cp;
+        nm[1] = st * sp;
+        nm[2] = ct;
+    } else if (ftype == 1) {  // Gaussian displacement of width delta, renormalised
+        float g[3];
+        normal3_f32_fast(seed, i, k, sweep, kStreamMCGauss, g);
+        const float a0 = cur.x + g[0] * delta, a1 = cur.y + g[1] * delta, a2 = cur.z + g[2] * delta;
+        const float il = rsqrtf(a0 * a0 + a1 * a1 + a2 * a2);
+        nm[0] = a0 * il;
+        nm[1] = a1 * il;
+        nm[2] = a2 * il;
+    } else {  // flip
+        nm[0] = -cur.x;
+        nm[1] = -cur.y;
+        nm[2] = -cur.z;
+    }
+    const float de = delta_energy_f32(h, c, mt, i, k, nm);
+    if (!(de <= 0.0f || u3 < __expf(-beta_mub * de))) return;
+    double x = nm[0], y = nm[1], z = nm[2];
+    const double sc = renorm_scale(fma(z, z, fma(y, y, x * x)) - 1.0);
+    x *= sc;
+    y *= sc;
+    z *= sc;
+    mt[o] = make_float4((float)x, (float)y, (float)z, cur.w);
+    const double md = mmom[o];
+    e.x[o] = x;
+    e.y[o] = y;
+    e.z[o] = z;
+    eM.x[o] = md * x;
+    eM.y[o] = md * y;
+    eM.z[o] = md * z;
+}
+
 __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) mt[t] = make_float4((float)e.x[t], (float)e.y[t], (float)e.z[t], (float)mmom[t]);
@@ -551,6 +610,33 @@ int mixed_ready(Sim &s) {
 }
 
 // precision 3 heat-bath sweeps (mc_run mode 'H')
+int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps) {
+    if (s.ncolour <= 0) {
+        set_error("no colouring available for Monte Carlo");
+        return UPPASD_GPU_ESTATE;
+    }
+    int rc = mixed_ready(s);
+    if (rc) return rc;
+    s.sqm_valid = 0;  // the square path's mirror does not follow these updates
+    // flip_a's beta = 1 / (k_B (T + 1e-15)) and the Gaussian width (2/25)(k_B T / mu_B)^0.2
+    // (montecarlo.f90:142, a REAL(4) constant), as the FP64 path forms them
+    const float beta_mub = (float)(s.ham.mub / s.ham.kbolt / (1.0 * temperature + 1.0e-15));
+    const float delta = (float)((double)(2.0f / 25.0f) * pow(s.ham.kbolt * temperature / s.ham.mub, 0.20));
+    for (int64_t sw = 0; sw < nsweeps; ++sw) {
+        for (int c = 0; c < s.ncolour; ++c) {
+            const int beg = s.colour_start_h[c], n = s.colour_start_h[c + 1] - beg;
+            if (n == 0) continue;
+            const int64_t tot = (int64_t)n * s.ham.mensemble;
+            mixed_metropolis<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
+                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, delta, s.llg.seed,
+                s.mc_sweep);
+        }
+        s.mc_sweep += 1;
+    }
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
 int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak) {
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");
