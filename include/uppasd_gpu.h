@@ -65,8 +65,9 @@ typedef struct {
                                           3 FP32 field gather over any neighbour list (scalar
                                             or tensor exchange, DMI, anisotropy, Zeeman) + FP64
                                             spin master and renormalisation (every SDEalgh of
-                                            precision 0, perp included); mc_run 'H' draws in FP32
-                                            on the same mirror */
+                                            precision 0, perp included); mc_run 'H' and 'M'
+                                            run in FP32 on the same mirror (mc_run_temps 'M'
+                                            on the FP64 path) */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;
