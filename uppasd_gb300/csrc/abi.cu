@@ -412,6 +412,7 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
 
 void destroy(Sim &s) {
     if (s.stream) cudaStreamSynchronize(s.stream);
+    if (s.copy_stream) cudaStreamSynchronize(s.copy_stream);  // a measured run's last copy
     if (s.graph) cudaGraphExecDestroy(s.graph);
     structured_free(s);
     mixed_free(s);
