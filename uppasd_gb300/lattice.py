@@ -464,6 +464,40 @@ def with_isotropic_tensor(lat: Lattice) -> Lattice:
     return out
 
 
+def fold_dm_into_tensor(lat: Lattice) -> Lattice:
+    """The block form of the reference's sparse path (setupSparseBlock,
+    Hamiltonian/sparse.f90:122-268): per neighbour one 3x3 block with J on the diagonal and
+    +-D off it, B_i += sum_j (J_ij I + [D_ij]) m_j with [D] m = m x D, so that the exchange
+    tensor gather carries exchange and DMI together.  Every DM neighbour must be an
+    exchange neighbour, in the same slot for all atoms of one Hamiltonian row.  The field
+    and the dynamics are those of the separate terms; the energy is then the tensor's pair
+    energy, as the reference computes it with do_jtensor."""
+    if lat.dmlist is None:
+        raise ValueError("no DM interaction to fold")
+    if lat.j_tens is not None:
+        mats = np.swapaxes(np.asarray(lat.j_tens, dtype=np.float64), -1, -2).copy()
+    else:
+        mats = lat.ncoup[:, :, None, None] * np.eye(3)
+    ih_of = np.asarray(lat.aham) - 1
+    slot = {}
+    for i in range(lat.natom):
+        ih = ih_of[i]
+        row = lat.nlist[i, :lat.nlistsize[ih]]
+        for sd in range(lat.dmlistsize[ih]):
+            hit = np.nonzero(row == lat.dmlist[i, sd])[0]
+            if hit.size == 0:
+                raise ValueError(f"DM neighbour {lat.dmlist[i, sd]} of atom {i + 1} is not an exchange neighbour")
+            if slot.setdefault((ih, sd), int(hit[0])) != int(hit[0]):
+                raise ValueError("DM slots differ between atoms of one Hamiltonian row")
+    for (ih, sd), s in slot.items():
+        d0, d1, d2 = lat.dm_vect[ih, sd]
+        mats[ih, s] += np.array([[0.0, d2, -d1], [-d2, 0.0, d0], [d1, -d0, 0.0]])
+    out = Lattice(**{k: getattr(lat, k) for k in lat.__dataclass_fields__})
+    out.j_tens = tensor_from_matrices(mats)
+    out.dmlist = out.dmlistsize = out.dm_vect = None
+    return out
+
+
 def reduced(lat: Lattice) -> Lattice:
     """The reduced Hamiltonian (do_reduced = 'Y'): one coupling row per basis atom,
     aHam(i) = anumb(i) (Hamiltonian/hamiltonianinit.f90:818-838, nHam = NA at :185).
