@@ -162,7 +162,9 @@ int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *s, int64_t nsteps, int64_t every,
 int uppasd_gpu_get_field(uppasd_gpu_sim *s, double *beff);
 
 /* Monte Carlo sweeps on a colouring of the coupling graph ('M' Metropolis with
- * Hinzke-Nowak trials, 'H' heat bath). */
+ * Hinzke-Nowak trials, temperature >= 0 (at 0 only moves that do not raise the energy,
+ * the relax entry of the reference's Python layer, pyasd.f90:255-298); 'H' heat bath,
+ * temperature > 0). */
 int uppasd_gpu_mc_run(uppasd_gpu_sim *s, char mode, double temperature, int64_t nsweeps);
 
 /* Structured heat bath for a uniform square lattice of edge L (site i = x + L y;

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from uppasd_gb300 import lattice
+from uppasd_gb300 import _lib, lattice
 from uppasd_gb300.simulation import GpuSimulation
 
 pytestmark = pytest.mark.gpu
@@ -172,3 +172,24 @@ def test_square_mirror_follows_every_state_change():
     o.set_moments(e1)
     o.mc_sweep_checkerboard("H", T, order, start, 77, 5)
     assert np.max(np.abs(g2 - o.emom)) < 2e-4
+
+
+@pytest.mark.parametrize("prec", [0, 3])
+def test_zero_temperature_metropolis_never_raises_the_energy(prec):
+    """relax() with the reference simulator's defaults (Metropolis at T = 0): every taken
+    move lowers or keeps the energy, so each sweep's total energy does not rise; the heat
+    bath refuses T = 0."""
+    lat = lattice.square_dmi(24, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
+    rng = np.random.default_rng(91)
+    e0 = rng.normal(size=(2, lat.natom, 3))
+    e0 /= np.linalg.norm(e0, axis=-1, keepdims=True)
+    sim = GpuSimulation(lat, emom=e0, seed=5, precision=prec, sdealgh=5)
+    e_prev = sim.observables()["energy"]
+    for _ in range(5):
+        sim.relax()
+        e_now = sim.observables()["energy"]
+        assert np.all(e_now <= e_prev + 1e-9 * np.abs(e_prev)), (e_prev, e_now)
+        e_prev = e_now
+    with pytest.raises(_lib.UppasdGpuError):
+        sim.relax("H", 0.0)
+    sim.close()

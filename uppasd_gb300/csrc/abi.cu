@@ -824,8 +824,11 @@ int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {
 }
 
 int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t nsweeps) {
-    if (!w || nsweeps < 0 || !(temperature > 0.0) || (mode != 'M' && mode != 'H')) {
-        uppasd::set_error("mc_run: mode must be 'M' or 'H', temperature > 0, nsweeps >= 0");
+    // Metropolis also at T = 0 (only moves that do not raise the energy are taken, as flip_a
+    // does with its + 1e-15); the heat bath needs T > 0
+    if (!w || nsweeps < 0 || (mode != 'M' && mode != 'H') || !std::isfinite(temperature) ||
+        !(mode == 'M' ? temperature >= 0.0 : temperature > 0.0)) {
+        uppasd::set_error("mc_run: mode 'M' (temperature >= 0) or 'H' (temperature > 0), nsweeps >= 0");
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = w->s;

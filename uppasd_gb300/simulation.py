@@ -205,10 +205,11 @@ class GpuSimulation:
             raise _lib.UppasdGpuError("uppasd_gpu_sd_run_measured", rc, msg.decode() if msg else "")
         return rc
 
-    def relax(self, mode: str = "H", temperature: float = 1.0, nsweeps: int = 1, structured: bool = False):
-        """Monte Carlo sweeps: mode 'M' (Metropolis) or 'H' (heat bath).  structured=True
-        runs the square-lattice heat bath (FP32 draws, uniform couplings recognised at
-        the first call)."""
+    def relax(self, mode: str = "M", temperature: float = 0.0, nsweeps: int = 1, structured: bool = False):
+        """Monte Carlo sweeps: mode 'M' (Metropolis, T >= 0) or 'H' (heat bath, T > 0); the
+        defaults are those of the reference simulator's relax (uppasd/simulator.py), a
+        zero-temperature Metropolis sweep.  structured=True runs the square-lattice heat
+        bath (FP32 draws, uniform couplings recognised at the first call)."""
         if structured:
             if mode != "H":
                 raise ValueError("the structured path is a heat bath")
