@@ -104,3 +104,19 @@ def test_restart_layouts_round_trip(tmp_path, pins):
     lines = open(tmp_path / "restart.std.out").read().splitlines()
     assert lines[0] == "#" * 80 and lines[1] == "# File type: R" and len(lines) == 7 + rows.shape[0]
     assert lines[7].split()[:3] == ["0", "1", "1"] and len(lines[7]) == 24 + 2 + 4 * 16
+
+
+def test_lattice_coordinates(pins):
+    """Positions in the reference's numbering: the HeisStripe tables (x fastest), the bcc
+    pair basis and the kagome basis."""
+    from uppasd_gb300 import lattice
+    inp = pins["inputs"]["heisstripe"]
+    lat, _ = lattice.from_tables(inp["cell"], inp["ncell"], inp["bc"], inp["sites"], inp["jfile"], sym=inp["sym"])
+    c = lat.coords
+    i = np.arange(lat.natom)
+    assert np.array_equal(c, np.stack([i % 10, np.zeros_like(i), i // 10], axis=1).astype(float))
+    b = lattice.bcc(3, [1.0], 1.0).coords
+    assert np.allclose(b[1], [0.5, 0.5, 0.5]) and np.allclose(b[2], [1.0, 0.0, 0.0])
+    k = lattice.kagome(2).coords
+    assert np.allclose(k[1], [0.5, 0.0, 0.0]) and np.allclose(k[3], [1.0, 0.0, 0.0])
+    assert np.allclose(np.linalg.norm(k[2]), 0.5)

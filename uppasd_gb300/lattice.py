@@ -77,6 +77,20 @@ class Lattice:
     def do_aniso(self) -> int:
         return 1 if self.taniso is not None else 0
 
+    @property
+    def coords(self) -> np.ndarray:
+        """Atom positions (natom, 3) in the reference's numbering, from the cell vectors and
+        basis positions the builder recorded (``meta['cell']``, ``meta['basis']``, Cartesian;
+        the identity cell and the stencil builders' basis otherwise)."""
+        cell = np.asarray(self.meta.get("cell", np.eye(3)), dtype=np.float64)
+        basis = np.asarray(self.meta.get("basis", _DEFAULT_BASIS.get(self.nbasis, np.zeros((1, 3)))),
+                           dtype=np.float64)
+        n1, n2, _ = self.cells
+        idx = np.arange(self.natom)
+        b, c = idx % self.nbasis, idx // self.nbasis
+        frac = np.stack([c % n1, (c // n1) % n2, c // (n1 * n2)], axis=1).astype(np.float64)
+        return frac @ cell + basis[b]
+
     def with_ensembles(self, mensemble: int) -> "Lattice":
         """Same Hamiltonian, `mensemble` copies of the moment arrays."""
         lat = Lattice(**{k: getattr(self, k) for k in self.__dataclass_fields__})
@@ -84,6 +98,11 @@ class Lattice:
         lat.mmom = np.ascontiguousarray(np.broadcast_to(self.mmom[:1], (mensemble, self.natom)))
         lat.extfield = np.ascontiguousarray(np.broadcast_to(self.extfield[:1], (mensemble, self.natom, 3)))
         return lat
+
+
+# basis positions (Cartesian, identity cell) of the stencil builders: one atom at the
+# origin, or the bcc pair
+_DEFAULT_BASIS = {1: np.zeros((1, 3)), 2: np.array([[0.0, 0.0, 0.0], [0.5, 0.5, 0.5]])}
 
 
 def _site_index(b, x, y, z, nb, n1, n2):
@@ -417,7 +436,8 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
                   j_tens=jt,
                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=m_of[None, :].copy(),
                   extfield=np.zeros((1, natom, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
-                  periodic=periodic, meta={"types": types})
+                  periodic=periodic, meta={"types": types, "cell": np.asarray(cell, dtype=np.float64).tolist(),
+                                           "basis": np.asarray(pos).tolist()})
     if dmfile is not None and len(dmfile):
         if sym != 0:
             raise ValueError("DM tables are supported with Sym 0 only")
@@ -558,7 +578,9 @@ def kagome(L: int, j_mry: float = -1.0, d_mry: float = 0.1, g_mry: float = 0.05,
                    ncoup=np.zeros((natom, 4)), aham=np.arange(1, natom + 1, dtype=np.int32),
                    mmom=np.full((1, natom), mom), extfield=ext, j_tens=jt,
                    cells=(L, L, 1), nbasis=3, periodic=(True, True, False),
-                   stencil=np.array([[s[:4] for s in b] for b in _KAGOME_STENCIL], dtype=np.int32))
+                   stencil=np.array([[s[:4] for s in b] for b in _KAGOME_STENCIL], dtype=np.int32),
+                   meta={"cell": [a1.tolist(), a2.tolist(), [0.0, 0.0, 1.0]],
+                         "basis": [(f[0] * a1 + f[1] * a2).tolist() for f in _KAGOME_BASIS]})
 
 
 def greedy_colouring(lat: Lattice):

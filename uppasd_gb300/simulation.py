@@ -143,6 +143,10 @@ class GpuSimulation:
         _lib.call("uppasd_gpu_get_moments", self._h, _ptr(e), _ptr(em))
         return (e, em) if full else e
 
+    def get_coords(self):
+        """Atom positions (natom, 3), as the reference simulator's get_coords."""
+        return self.lat.coords
+
     def get_fields(self):
         b = np.empty((self.lat.mensemble, self.lat.natom, 3))
         _lib.call("uppasd_gpu_get_field", self._h, _ptr(b))
