@@ -9,6 +9,7 @@
   the Metropolis energy change of one spin matches a full-energy difference.
 """
 import numpy as np
+import pytest
 
 from oracle import pyoracle as po
 from uppasd_gb300 import lattice
@@ -116,3 +117,13 @@ def test_block_form_of_exchange_and_dmi():
         scale = np.max(np.abs(res[0][0]))
         assert np.max(np.abs(res[0][0] - res[1][0])) <= 1e-12 * scale
         assert np.max(np.abs(res[0][1] - res[1][1])) <= 1e-10
+
+
+def test_block_form_needs_dm_neighbours_among_the_exchange_ones():
+    lat = lattice.square_dmi(4, 1.0, 0.3, 0.0, 0.0, 1.0)
+    lat.dmlist = lat.dmlist.copy()
+    lat.dmlist[0, 0] = 11   # not a neighbour of atom 1
+    with pytest.raises(ValueError):
+        lattice.fold_dm_into_tensor(lat)
+    with pytest.raises(ValueError):
+        lattice.fold_dm_into_tensor(lattice.bcc(2, [1.0]))
