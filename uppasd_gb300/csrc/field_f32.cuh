@@ -21,7 +21,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
                                           float B[3]) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
-    const int ih = h.aham[i];
+    const int ih = __ldg(&c.row[i]);
     const int nn = h.nsize[i];
     float bs[3] = {0.f, 0.f, 0.f}, bq[3] = {0.f, 0.f, 0.f};
     if (h.do_jtensor) {
@@ -29,7 +29,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            const float *J = c.jt + ((size_t)s * h.nham + ih) * 9;
+            const float *J = c.jt + ((size_t)s * c.nrow + ih) * 9;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
                 bs[a] += __ldg(&J[3 * a]) * m1 + __ldg(&J[3 * a + 1]) * m2 + __ldg(&J[3 * a + 2]) * m3;
@@ -38,7 +38,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
         for (int s = 0; s < nn; ++s) {
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
-            const float cj = __ldg(&c.nc[(size_t)s * h.nham + ih]) * v.w;
+            const float cj = __ldg(&c.nc[(size_t)s * c.nrow + ih]) * v.w;
             bs[0] = fmaf(cj, v.x, bs[0]);
             bs[1] = fmaf(cj, v.y, bs[1]);
             bs[2] = fmaf(cj, v.z, bs[2]);
@@ -48,7 +48,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
         const int nd = h.dmsize[i];
         for (int s = 0; s < nd; ++s) {
             const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
-            const float4 d = __ldg(&c.dm[(size_t)s * h.nham + ih]);
+            const float4 d = __ldg(&c.dm[(size_t)s * c.nrow + ih]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
             bs[0] += d.z * m2 - d.y * m3;
@@ -60,8 +60,9 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
         const float4 me = m[off + i];
         const float m1 = me.w * me.x, m2 = me.w * me.y, m3 = me.w * me.z;
         const int ta = h.taniso[i];
-        const float4 an = __ldg(&c.an[i]);
-        const float2 an2 = __ldg(&c.an2[i]);
+        const int ar = __ldg(&c.arow[i]);
+        const float4 an = __ldg(&c.an[ar]);
+        const float2 an2 = __ldg(&c.an2[ar]);
         const float e0 = an.x, e1 = an.y, e2 = an.z, ka0 = an.w, ka1 = an2.x;
         if (ta == 1 || ta == 7) {
             const float tt1 = m1 * e0 + m2 * e1 + m3 * e2;
@@ -95,7 +96,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
                                                   const float nm[3]) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
-    const int ih = h.aham[i];
+    const int ih = __ldg(&c.row[i]);
     const float4 me = m[off + i];
     const float mm = me.w;
     const float ei[3] = {me.x, me.y, me.z};
@@ -109,7 +110,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
-            const float *J = c.jt + ((size_t)s * h.nham + ih) * 9;
+            const float *J = c.jt + ((size_t)s * c.nrow + ih) * 9;
 #pragma unroll
             for (int a = 0; a < 3; ++a)
                 b[a] += __ldg(&J[3 * a]) * m1 + __ldg(&J[3 * a + 1]) * m2 + __ldg(&J[3 * a + 2]) * m3;
@@ -118,7 +119,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
         for (int s = 0; s < nn; ++s) {
             const int j = __ldg(&h.nlist[(size_t)s * N + i]);
             const float4 v = m[off + j];
-            const float cj = __ldg(&c.nc[(size_t)s * h.nham + ih]) * v.w;
+            const float cj = __ldg(&c.nc[(size_t)s * c.nrow + ih]) * v.w;
             b[0] = fmaf(cj, v.x, b[0]);
             b[1] = fmaf(cj, v.y, b[1]);
             b[2] = fmaf(cj, v.z, b[2]);
@@ -130,7 +131,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
         const int nd = h.dmsize[i];
         for (int s = 0; s < nd; ++s) {
             const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
-            const float4 d = __ldg(&c.dm[(size_t)s * h.nham + ih]);
+            const float4 d = __ldg(&c.dm[(size_t)s * c.nrow + ih]);
             const float4 v = m[off + j];
             const float mj0 = v.w * v.x, mj1 = v.w * v.y, mj2 = v.w * v.z;
             const float et = d.x * (tm[1] * mj2 - tm[2] * mj1) + d.y * (tm[2] * mj0 - tm[0] * mj2) +
@@ -142,8 +143,9 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
     }
     if (h.do_aniso) {
         const int ta = h.taniso[i];
-        const float4 an = __ldg(&c.an[i]);
-        const float2 an2 = __ldg(&c.an2[i]);
+        const int ar = __ldg(&c.arow[i]);
+        const float4 an = __ldg(&c.an[ar]);
+        const float2 an2 = __ldg(&c.an2[ar]);
         const float ka0 = an.w, ka1 = an2.x;
         if (ta == 1 || ta == 7) {
             const float tta = mi[0] * an.x + mi[1] * an.y + mi[2] * an.z;

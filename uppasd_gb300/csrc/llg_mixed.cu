@@ -16,6 +16,8 @@
 #include <algorithm>
 #include <string>
 #include <type_traits>
+#include <cstring>
+#include <map>
 #include <vector>
 
 #include "common.cuh"
@@ -521,27 +523,69 @@ bool store(T **d, const std::vector<T> &h) {
 }
 }  // namespace
 
-// (Re)builds the FP32 copies of the couplings from the FP64 Hamiltonian on the device.
+// (Re)builds the FP32 copies of the couplings from the FP64 Hamiltonian on the device,
+// one row per distinct coupling row (compared bit for bit in FP32) and one anisotropy
+// row per distinct (axis, K1, K2, sb).
 int mixed_coefficients(Sim &s) {
     const HamDev &h = s.ham;
-    const size_t N = h.natom, M = h.mensemble, ne = (size_t)std::max(h.mnn, 1) * h.nham;
+    const size_t N = h.natom, M = h.mensemble, nh = h.nham, mnn = std::max(h.mnn, 1), mdm = h.do_dm ? h.mnn_dm : 0;
     MixedDev &m = s.mix;
-    std::vector<double> d, dx, dy, dz;
+    std::vector<double> d, dx, dy, dz, jtd;
+    std::vector<int32_t> aham;
     bool ok = cudaStreamSynchronize(s.stream) == cudaSuccess;
-    ok = ok && fetch(d, h.ncoup, ne);
-    std::vector<float> nc(d.begin(), d.end());
-    ok = ok && store(&m.nc, nc);
+    ok = ok && fetch(d, h.ncoup, mnn * nh) && fetch(aham, h.aham, N);
+    if (ok && h.do_dm) ok = fetch(dx, h.dmx, mdm * nh) && fetch(dy, h.dmy, mdm * nh) && fetch(dz, h.dmz, mdm * nh);
+    if (ok && h.do_jtensor) ok = fetch(jtd, h.jt, mnn * nh * 9);
+    // the FP32 content of Hamiltonian row ih, as bits, for the comparison
+    const size_t width = mnn + 3 * mdm + (h.do_jtensor ? 9 * mnn : 0);
+    auto key = [&](size_t ih) {
+        std::vector<uint32_t> k(width);
+        size_t q = 0;
+        auto put = [&](double v) {
+            float f = (float)v;
+            std::memcpy(&k[q++], &f, 4);
+        };
+        for (size_t sl = 0; sl < mnn; ++sl) put(d[sl * nh + ih]);
+        for (size_t sl = 0; sl < mdm; ++sl) {
+            put(dx[sl * nh + ih]);
+            put(dy[sl * nh + ih]);
+            put(dz[sl * nh + ih]);
+        }
+        if (h.do_jtensor)
+            for (size_t sl = 0; sl < mnn; ++sl)
+                for (int a = 0; a < 9; ++a) put(jtd[(sl * nh + ih) * 9 + a]);
+        return k;
+    };
+    std::map<std::vector<uint32_t>, int> seen;
+    std::vector<int> urow(nh), first;
+    for (size_t ih = 0; ih < nh && ok; ++ih) {
+        auto it = seen.emplace(key(ih), (int)first.size());
+        if (it.second) first.push_back((int)ih);
+        urow[ih] = it.first->second;
+    }
+    const size_t nr = first.size();
+    m.nrow = (int)nr;
+    std::vector<int32_t> row(N);
+    for (size_t i = 0; i < N; ++i) row[i] = urow[aham[i]];
+    std::vector<float> nc(mnn * nr);
+    for (size_t sl = 0; sl < mnn; ++sl)
+        for (size_t r = 0; r < nr; ++r) nc[sl * nr + r] = (float)d[sl * nh + first[r]];
+    ok = ok && store(&m.row, row) && store(&m.nc, nc);
     if (ok && h.do_dm) {
-        const size_t nd = (size_t)h.mnn_dm * h.nham;
-        ok = fetch(dx, h.dmx, nd) && fetch(dy, h.dmy, nd) && fetch(dz, h.dmz, nd);
-        std::vector<float4> v(nd);
-        for (size_t q = 0; q < nd && ok; ++q) v[q] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
-        ok = ok && store(&m.dm, v);
+        std::vector<float4> v(mdm * nr);
+        for (size_t sl = 0; sl < mdm; ++sl)
+            for (size_t r = 0; r < nr; ++r) {
+                const size_t q = sl * nh + first[r];
+                v[sl * nr + r] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+            }
+        ok = store(&m.dm, v);
     }
     if (ok && h.do_jtensor) {
-        ok = fetch(d, h.jt, ne * 9);
-        std::vector<float> v(d.begin(), d.end());
-        ok = ok && store(&m.jt, v);
+        std::vector<float> v(mnn * nr * 9);
+        for (size_t sl = 0; sl < mnn; ++sl)
+            for (size_t r = 0; r < nr; ++r)
+                for (int a = 0; a < 9; ++a) v[(sl * nr + r) * 9 + a] = (float)jtd[(sl * nh + first[r]) * 9 + a];
+        ok = store(&m.jt, v);
     } else if (ok) {
         ok = store(&m.jt, std::vector<float>());
     }
@@ -549,13 +593,22 @@ int mixed_coefficients(Sim &s) {
         std::vector<double> k1, k2, sb;
         ok = fetch(dx, h.eax, N) && fetch(dy, h.eay, N) && fetch(dz, h.eaz, N) && fetch(k1, h.k1, N) &&
              fetch(k2, h.k2, N) && fetch(sb, h.sb, N);
-        std::vector<float4> a(N);
-        std::vector<float2> a2(N);
+        std::map<std::vector<uint32_t>, int> aseen;
+        std::vector<float4> a;
+        std::vector<float2> a2;
+        std::vector<int32_t> arow(N);
         for (size_t i = 0; i < N && ok; ++i) {
-            a[i] = make_float4((float)dx[i], (float)dy[i], (float)dz[i], (float)k1[i]);
-            a2[i] = make_float2((float)k2[i], (float)sb[i]);
+            const float f[6] = {(float)dx[i], (float)dy[i], (float)dz[i], (float)k1[i], (float)k2[i], (float)sb[i]};
+            std::vector<uint32_t> k(6);
+            std::memcpy(k.data(), f, sizeof f);
+            auto it = aseen.emplace(k, (int)a.size());
+            if (it.second) {
+                a.push_back(make_float4(f[0], f[1], f[2], f[3]));
+                a2.push_back(make_float2(f[4], f[5]));
+            }
+            arow[i] = it.first->second;
         }
-        ok = ok && store(&m.an, a) && store(&m.an2, a2);
+        ok = ok && store(&m.an, a) && store(&m.an2, a2) && store(&m.arow, arow);
     }
     if (ok) {
         ok = fetch(dx, h.ext.x, N * M) && fetch(dy, h.ext.y, N * M) && fetch(dz, h.ext.z, N * M);
@@ -594,7 +647,8 @@ int mixed_init(Sim &s) {
 void mixed_free(Sim &s) {
     MixedDev &m = s.mix;
     for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
-                    (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext})
+                    (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext, (void *)m.row,
+                    (void *)m.arow})
         cudaFree(q);
     m = MixedDev{};
 }

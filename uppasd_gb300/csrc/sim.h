@@ -70,13 +70,17 @@ struct MixedDev {
     float4 *mt = nullptr, *mp = nullptr;
     float *b2x = nullptr, *b2y = nullptr, *b2z = nullptr;
     int valid = 0;  // mt equals e / mmom
-    // FP32 copies of the Hamiltonian (HamDev layouts): half the bytes of the FP64
-    // arrays, which a non-reduced Hamiltonian reads per site
-    float *nc = nullptr;     // [mnn][nham]
-    float4 *dm = nullptr;    // [mnn_dm][nham] (Dx, Dy, Dz, 0)
-    float *jt = nullptr;     // [mnn][nham][9]
-    float4 *an = nullptr;    // [natom] (ex, ey, ez, k1)
-    float2 *an2 = nullptr;   // [natom] (k2, sb)
+    // FP32 copies of the Hamiltonian, one row per distinct coupling row: equal rows of a
+    // non-reduced Hamiltonian (a translation-invariant lattice) share one, so the per-site
+    // reads hit the caches instead of streaming per-site copies from DRAM
+    int nrow = 0;            // distinct (exchange, DM, tensor) rows
+    int32_t *row = nullptr;  // [natom] row of atom i
+    float *nc = nullptr;     // [mnn][nrow]
+    float4 *dm = nullptr;    // [mnn_dm][nrow] (Dx, Dy, Dz, 0)
+    float *jt = nullptr;     // [mnn][nrow][9]
+    int32_t *arow = nullptr; // [natom] anisotropy row of atom i
+    float4 *an = nullptr;    // [distinct anisotropy rows] (ex, ey, ez, k1)
+    float2 *an2 = nullptr;   // [distinct anisotropy rows] (k2, sb)
     float4 *ext = nullptr;   // [mensemble][natom] (Bx, By, Bz, 0)
 };
 
