@@ -82,7 +82,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
             dst[2] += t2 * sc;
         }
     }
-    const float4 ex = __ldg(&c.ext[off + i]);
+    const float4 ex = __ldg(&c.ext[c.ext_uniform ? 0 : off + i]);
     B[0] = bs[0] + (bq[0] + ex.x);
     B[1] = bs[1] + (bq[1] + ex.y);
     B[2] = bs[2] + (bq[2] + ex.z);
@@ -165,7 +165,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
             de += sgn * (ct - cc);
         }
     }
-    const float4 ex = __ldg(&c.ext[off + i]);
+    const float4 ex = __ldg(&c.ext[c.ext_uniform ? 0 : off + i]);
     de -= ex.x * dm[0] + ex.y * dm[1] + ex.z * dm[2];
     return de;
 }

@@ -613,7 +613,13 @@ int mixed_coefficients(Sim &s) {
     if (ok) {
         ok = fetch(dx, h.ext.x, N * M) && fetch(dy, h.ext.y, N * M) && fetch(dz, h.ext.z, N * M);
         std::vector<float4> v(N * M);
-        for (size_t q = 0; q < N * M && ok; ++q) v[q] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+        bool uniform = true;
+        for (size_t q = 0; q < N * M && ok; ++q) {
+            v[q] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+            uniform = uniform && v[q].x == v[0].x && v[q].y == v[0].y && v[q].z == v[0].z;
+        }
+        m.ext_uniform = uniform ? 1 : 0;
+        if (uniform) v.resize(1);
         ok = ok && store(&m.ext, v);
     }
     if (!ok) {

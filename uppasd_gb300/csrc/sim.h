@@ -81,7 +81,8 @@ struct MixedDev {
     int32_t *arow = nullptr; // [natom] anisotropy row of atom i
     float4 *an = nullptr;    // [distinct anisotropy rows] (ex, ey, ez, k1)
     float2 *an2 = nullptr;   // [distinct anisotropy rows] (k2, sb)
-    float4 *ext = nullptr;   // [mensemble][natom] (Bx, By, Bz, 0)
+    float4 *ext = nullptr;   // [mensemble][natom] (Bx, By, Bz, 0), or one entry when uniform
+    int ext_uniform = 0;     // every spin sees ext[0]
 };
 
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
