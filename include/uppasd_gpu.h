@@ -154,8 +154,10 @@ typedef int (*uppasd_gpu_measure_cb)(int64_t step, const double *emom, const dou
  * host thread, gpu_files/measurementQueue.cpp:10-80).  The copy of each snapshot to the
  * host overlaps the next block of steps; the callbacks come in order on the calling
  * thread, each once the following block has been issued.  A nonzero callback value ends
- * the run after the block in flight and is returned.  Steps beyond the last whole block
- * run without a measurement. */
+ * the run after the block in flight and is returned: that block has run, so the state
+ * then stands `every` steps past the snapshot of the callback that stopped it (and the
+ * call returns once that block's snapshot copy has finished).  Steps beyond the last whole
+ * block run without a measurement. */
 int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *s, int64_t nsteps, int64_t every, uppasd_gpu_measure_cb cb,
                                void *user);
 /* Effective field of the current state, (3, natom, mensemble). */
@@ -228,7 +230,9 @@ int uppasd_gpu_time_kernels(uppasd_gpu_sim *s, int32_t nrep, double *ms);
  * exits.  Limit: mensemble <= 64 (larger values return UPPASD_GPU_EINVAL);
  * natom is not limited.  The first call on each device looks up that array's
  * device address (cudaGetSymbolAddress) with the device current, so make the
- * first call on a device before any stream capture.  All calls share the
+ * first call on a device before any stream capture.  The address is kept per
+ * device context: after a cudaDeviceReset the next call on that device looks it
+ * up again (that call, too, should come before any stream capture).  All calls share the
  * array: calls that overlap on the GPU (different streams) race and must be
  * serialised by the caller.  The result is asynchronous on `cuda_stream`. */
 int uppasd_gpu_moment_sums_noalloc(const double *d_emomM, int32_t natom, int32_t mensemble, double *d_out,

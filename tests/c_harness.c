@@ -3,8 +3,8 @@
  * (sd_mphaseCUDA, sd_driver.f90:1118-1153; mc_mphase, mc_driver.f90:234): module arrays in
  * Fortran layout (nlist(mnn, natom) 1-based, ncoup(mnn, nham), emom(3, natom, mensemble)),
  * couplings scaled as setup_neighbour_hamiltonian / setup_anisotropies scale them, every
- * status checked.  No Fortran compiler exists here, so this stands in for the bind(c)
- * module of INTEGRATION.md.
+ * status checked.  No Fortran compiler exists here, so this stands in for the Fortran
+ * driver's bind(c) interface module.
  *
  *   c_harness reject           init with an out-of-range neighbour index: expects -1 and
  *                              a message (runs without a GPU: arguments are checked first)

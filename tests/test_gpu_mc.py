@@ -193,3 +193,63 @@ def test_zero_temperature_metropolis_never_raises_the_energy(prec):
     with pytest.raises(_lib.UppasdGpuError):
         sim.relax("H", 0.0)
     sim.close()
+
+
+@pytest.mark.parametrize("mode", ["H", "M"])
+def test_binder_and_susceptibility_near_tc(mode):
+    """Near the L = 6 lattice's ordering temperature (U_L falls from 0.66 to 0.49 between
+    1200 and 1400 K) the Binder cumulant and the susceptibility are at their most
+    sensitive: the FP64 checkerboard chain (32 replicas) against the reference's
+    random-permutation chain (four independent chains, mtprng + ziggurat), within 3 sigma
+    of the combined jackknife errors."""
+    from uppasd_gb300 import analysis
+
+    lat = lattice.bcc(6, [1.3, 0.7], 2.2)
+    T = 1300.0
+    ntherm, nmeas = 1000, 12000
+    kchi = analysis.MUB ** 2 * lat.natom / analysis.KBOLT ** 2 / T
+
+    def binder(m2, m4):
+        return 1.0 - m4 / 3.0 / (m2 * m2)
+
+    def chi(m, m2):
+        return (m2 - m * m) * kchi
+
+    # reference chains: blocks of each chain are the jackknife units
+    ref_m = []
+    for seed in (17, 18, 19, 20):
+        o = po.Oracle(lat, threads=1)
+        e0 = _rand_unit(np.random.default_rng(seed), (1, lat.natom, 3))
+        o.set_moments(e0)
+        o.mt = po.OrcMT()
+        o.lib.orc_mt_init(C.byref(o.mt), seed)
+        o.setup_ziggurat(seed)
+        iflip = o.choose_random_atom_x()
+        ms = []
+        for s in range(ntherm + nmeas):
+            o.mc_sweep_ref(mode, T, iflip)
+            if (s + 1) % 100 == 0:
+                iflip = o.choose_random_atom_x()
+            if s >= ntherm:
+                ms.append(o.mavg()[1][0])
+        ref_m.append(np.array(ms))
+    ref_m = np.concatenate(ref_m)  # 4 chains back to back: 80 blocks of 600 sweeps
+    ref = {"U": analysis.jackknife(binder, [ref_m ** 2, ref_m ** 4], nbin=80),
+           "chi": analysis.jackknife(chi, [ref_m, ref_m ** 2], nbin=80)}
+    # GPU: independent replicas are the jackknife units
+    nrep = 32
+    latg = lat.with_ensembles(nrep)
+    sim = GpuSimulation(latg, emom=_rand_unit(np.random.default_rng(5), (nrep, lat.natom, 3)), seed=71)
+    sim.relax(mode, T, ntherm)
+    gm = []
+    for _ in range(nmeas // 2):
+        sim.relax(mode, T, 2)
+        gm.append(sim.observables()["mabs"].copy())
+    sim.close()
+    gm = np.array(gm).T.reshape(-1)  # replica-major: one block per replica
+    gpu = {"U": analysis.jackknife(binder, [gm ** 2, gm ** 4], nbin=nrep),
+           "chi": analysis.jackknife(chi, [gm, gm ** 2], nbin=nrep)}
+    for k in ("U", "chi"):
+        (gv, ge), (rv, re_) = gpu[k], ref[k]
+        print(f"{mode} T={T} {k}: GPU {gv:.5g} +- {ge:.2g}, reference chain {rv:.5g} +- {re_:.2g}")
+        assert abs(gv - rv) <= 3.0 * np.hypot(ge, re_), (k, gv, ge, rv, re_)

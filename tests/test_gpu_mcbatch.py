@@ -210,7 +210,7 @@ def test_replica_exchange_keeps_the_distribution():
     the same table run without exchange within 3 sigma (independent replicas per
     temperature on each side)."""
     Ts = list(np.linspace(900.0, 1500.0, 8))
-    copies = 6
+    copies = 24
     L = [6] * (8 * copies)
     T = Ts * copies
     res = {}
@@ -239,4 +239,4 @@ def test_replica_exchange_keeps_the_distribution():
         per_t = s.reshape(copies, 8, -1, 2).mean(axis=2)  # (copies, T, 2)
         res[ex] = (per_t.mean(axis=0), per_t.std(axis=0, ddof=1) / np.sqrt(copies))
     (m0, s0), (m1, s1) = res[False], res[True]
-    assert np.all(np.abs(m0 - m1) <= 3.5 * np.hypot(s0, s1) + 1e-12), (m0, m1, s0, s1)
+    assert np.all(np.abs(m0 - m1) <= 3.0 * np.hypot(s0, s1) + 1e-12), (m0, m1, s0, s1)

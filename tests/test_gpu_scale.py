@@ -1,0 +1,147 @@
+"""GPU parity at the benchmarked and configured sizes.
+
+The other GPU tests use lattices of a few hundred to a few thousand atoms.  This
+file runs the CUDA path through the C ABI on the lattices the benchmark times and
+on the sizes of the configured runs, against the FP64 CPU oracle:
+
+* the structured FP32-gather kernels with the pitches compiled for L = 100 and
+  L = 64 (the 2 M-atom bcc alloy of the headline line and its 64^3 profiling
+  case), FP64 and double-single master, T = 0 and 300 K;
+* the bcc ferromagnet of 20^3 cells (16,000 atoms), Depondt, 1000 steps at T = 0
+  then 1000 at 300 K on the FP64 path, 1e-9 per component;
+* the 256^2 square monolayer with J, interfacial DMI, uniaxial anisotropy and a
+  Zeeman field, semi-implicit midpoint, 20,000 steps at T = 0 and at 50 K;
+* the SIB solver (SDEalgh 6) at 300 K without the perp projection.
+
+Every test prints the measured deviation, so a run with ``-s`` records the
+numbers behind the stated bounds.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from uppasd_gb300 import lattice
+from uppasd_gb300.simulation import GpuSimulation
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-9
+# FP32 gather against the FP64 oracle (the structured path's bounds on small lattices):
+# T = 0 from a random start, and 300 K where the FP32 Box-Muller noise adds its rounding
+STRUCT_T0 = {10: 2e-6, 20: 2e-5}
+STRUCT_T300 = 2e-4
+
+
+def _rand_unit(rng, shape):
+    e = rng.normal(size=shape)
+    return e / np.linalg.norm(e, axis=-1, keepdims=True)
+
+
+def _oracle(lat, solver, dt, damping, temp, seed, e0):
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, dt, damping, temp, 1.0, noise_mode=po.NOISE_PHILOX, seed=seed)
+    return o
+
+
+@pytest.fixture(scope="module")
+def alloy100():
+    return lattice.bcc_alloy(100, seed=2024)
+
+
+def _structured_case(lat, e0, prec, temp, checkpoints, seed=7):
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=temp, seed=seed, emom=e0,
+                        precision=prec)
+    o = _oracle(lat, 5, 1e-16, 0.1, temp, seed, e0)
+    done = 0
+    for n, tol in sorted(checkpoints.items()):
+        sim.evolve(n - done)
+        for _ in range(n - done):
+            o.sd_step()
+        done = n
+        g = sim.get_moments()
+        err = float(np.max(np.abs(g - o.emom)))
+        rms = float(np.sqrt(np.mean((g - o.emom) ** 2)))
+        nrm = float(np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)))
+        print(f"L={lat.cells[0]} ens={lat.mensemble} prec={prec} T={temp} steps={n}: "
+              f"max|GPU-oracle|={err:.3e} rms={rms:.3e} norm dev={nrm:.1e}")
+        assert err <= tol
+        assert nrm <= 1e-12
+    sim.close()
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("temp", [0.0, 300.0])
+def test_structured_l100_alloy(alloy100, prec, temp):
+    """stencil_zblock<4, 2, 100, *, *>: the kernels of the headline line, one ensemble of
+    the 2 M-atom alloy, 20 steps."""
+    e0 = _rand_unit(np.random.default_rng(50 + int(temp)), (1, alloy100.natom, 3))
+    cps = STRUCT_T0 if temp == 0.0 else {20: STRUCT_T300}
+    _structured_case(alloy100, e0, prec, temp, cps)
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+def test_structured_l64_alloy_two_ensembles(prec):
+    """stencil_zblock<4, 2, 64, *, *> (the profiled case) with two ensembles, so the
+    ensemble index of the Philox counter and of the padded boxes is exercised."""
+    lat = lattice.bcc_alloy(64, seed=2024).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(64), (2, lat.natom, 3))
+    _structured_case(lat, e0, prec, 300.0, {20: STRUCT_T300})
+    _structured_case(lat, e0, prec, 0.0, STRUCT_T0)
+
+
+def test_bcc20_depondt_t0_then_300k():
+    """bcc 20^3 cells (16,000 atoms), J1 = 1.3, J2 = 0.7 mRy, 2.2 muB, Depondt, lambda 0.1,
+    dt 0.1 fs: 1000 steps at T = 0, then 1000 at 300 K, FP64 path."""
+    lat = lattice.bcc(20, [1.3, 0.7], 2.2)
+    e0 = _rand_unit(np.random.default_rng(20), (1, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=0.0, seed=13, emom=e0)
+    o = _oracle(lat, 5, 1e-16, 0.1, 0.0, 13, e0)
+    sim.evolve(1000)
+    for _ in range(1000):
+        o.sd_step()
+    err0 = float(np.max(np.abs(sim.get_moments() - o.emom)))
+    sim.set_temperature(300.0)
+    o._temp[:] = 300.0
+    sim.evolve(1000)
+    for _ in range(1000):
+        o.sd_step()
+    err1 = float(np.max(np.abs(sim.get_moments() - o.emom)))
+    print(f"bcc 20^3 Depondt: after 1000 steps at 0 K {err0:.3e}, after 1000 more at 300 K {err1:.3e}")
+    sim.close()
+    assert err0 <= TOL and err1 <= TOL
+
+
+@pytest.mark.parametrize("temp", [0.0, 50.0])
+def test_square256_midpoint_20000_steps(temp):
+    """256^2 square monolayer (65,536 spins): J = 1.0, D = 0.3, Kz = -0.05 mRy, Bz = 0.5 T,
+    midpoint (SDEalgh 1), lambda 0.05, dt 0.1 fs, 20,000 steps, FP64 path."""
+    lat = lattice.square_dmi(256, 1.0, 0.3, -0.05, 0.5, 1.0)
+    e0 = _rand_unit(np.random.default_rng(256 + int(temp)), (1, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=1, delta_t=1e-16, damping=0.05, temperature=temp, seed=29, emom=e0)
+    o = _oracle(lat, 1, 1e-16, 0.05, temp, 29, e0)
+    done, errs = 0, {}
+    for n in (1000, 5000, 20000):
+        sim.evolve(n - done)
+        for _ in range(n - done):
+            o.sd_step()
+        done = n
+        errs[n] = float(np.max(np.abs(sim.get_moments() - o.emom)))
+    print(f"square 256^2 midpoint T={temp}: " + ", ".join(f"{k} steps {v:.3e}" for k, v in errs.items()))
+    sim.close()
+    assert max(errs.values()) <= TOL, errs
+
+
+def test_sib_300k_without_perp():
+    """SIB (sibt/sibf, SDEalgh 6) with Philox noise at 300 K and no perp projection."""
+    lat = lattice.bcc(4, [1.3, 0.7], 2.2).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(66), (2, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=6, delta_t=1e-16, damping=0.1, temperature=300.0, seed=61, emom=e0)
+    o = _oracle(lat, 6, 1e-16, 0.1, 300.0, 61, e0)
+    sim.evolve(1000)
+    for _ in range(1000):
+        o.sd_step()
+    err = float(np.max(np.abs(sim.get_moments() - o.emom)))
+    print(f"SIB 300 K 1000 steps: {err:.3e}")
+    sim.close()
+    assert err <= TOL

@@ -45,6 +45,10 @@ def test_noalloc_sums_match_observables_twice():
         out = d_out.cpu().numpy()
         assert np.allclose(out[:, :3], ref["mvec"], rtol=1e-12, atol=1e-10), (call, out[:, :3], ref["mvec"])
         assert np.allclose(out[:, 3], ref["mabs"], rtol=1e-12, atol=1e-14), (call, out[:, 3], ref["mabs"])
+        # and against a direct sum of the moments it was given
+        tot = emomM.sum(axis=1)
+        assert np.allclose(out[:, :3], tot, rtol=1e-12, atol=1e-10), (call, out[:, :3], tot)
+        assert np.allclose(out[:, 3], np.linalg.norm(tot, axis=-1) / lat.natom, rtol=1e-12, atol=1e-14)
 
 
 def test_noalloc_rejects_too_many_ensembles():

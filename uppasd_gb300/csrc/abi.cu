@@ -757,6 +757,48 @@ int uppasd_gpu_sd_run(uppasd_gpu_sim *w, int64_t nsteps) {
     return uppasd::run_steps(s, nsteps);
 }
 
+namespace uppasd {
+
+// The measured-run resources (copy stream, two device and two page-locked snapshot
+// buffers, their events), made into locals and installed in s only when every one
+// of them exists, so that a failed set-up leaves nothing half-made behind and the
+// next call tries again from the start.
+int snapshot_setup(Sim &s, size_t bytes) {
+    cudaStream_t cs = nullptr;
+    double *dd[2] = {nullptr, nullptr}, *hh[2] = {nullptr, nullptr};
+    cudaEvent_t se[2] = {nullptr, nullptr}, ce[2] = {nullptr, nullptr};
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaMalloc(&dd[b], bytes);
+        if (e == cudaSuccess) e = cudaHostAlloc(&hh[b], bytes, cudaHostAllocDefault);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&se[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ce[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ce[b], cs);
+    }
+    if (e != cudaSuccess) {
+        for (int b = 0; b < 2; ++b) {
+            if (dd[b]) cudaFree(dd[b]);
+            if (hh[b]) cudaFreeHost(hh[b]);
+            if (se[b]) cudaEventDestroy(se[b]);
+            if (ce[b]) cudaEventDestroy(ce[b]);
+        }
+        if (cs) cudaStreamDestroy(cs);
+        set_error(std::string("sd_run_measured: snapshot buffers: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? UPPASD_GPU_ENOMEM : UPPASD_GPU_ECUDA;
+    }
+    for (int b = 0; b < 2; ++b) {
+        s.snap_d[b] = dd[b];
+        s.snap_h[b] = hh[b];
+        s.snap_ev[b] = se[b];
+        s.copy_ev[b] = ce[b];
+        s.bytes_allocated += bytes;
+    }
+    s.copy_stream = cs;
+    return UPPASD_GPU_OK;
+}
+
+}  // namespace uppasd
+
 int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every, uppasd_gpu_measure_cb cb,
                                void *user) {
     if (!w || nsteps < 0 || every < 1 || !cb) {
@@ -771,15 +813,8 @@ int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every,
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const size_t bytes = 6 * sizeof(double) * (size_t)n;  // emom then emomM
     if (!s.copy_stream) {
-        UPPASD_CUDA_TRY(cudaStreamCreateWithFlags(&s.copy_stream, cudaStreamNonBlocking));
-        for (int b = 0; b < 2; ++b) {
-            UPPASD_CUDA_TRY(cudaMalloc(&s.snap_d[b], bytes));
-            UPPASD_CUDA_TRY(cudaHostAlloc(&s.snap_h[b], bytes, cudaHostAllocDefault));
-            UPPASD_CUDA_TRY(cudaEventCreateWithFlags(&s.snap_ev[b], cudaEventDisableTiming));
-            UPPASD_CUDA_TRY(cudaEventCreateWithFlags(&s.copy_ev[b], cudaEventDisableTiming));
-            UPPASD_CUDA_TRY(cudaEventRecord(s.copy_ev[b], s.copy_stream));
-            s.bytes_allocated += bytes;
-        }
+        int src = uppasd::snapshot_setup(s, bytes);
+        if (src) return src;
     }
     const unsigned grid = (unsigned)((n + 255) / 256);
     const int64_t nblocks = nsteps / every;
@@ -810,6 +845,9 @@ int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every,
         }
         pending_step = i < nblocks ? s.step : -1;
     }
+    // a callback that stopped the run leaves the copy of the block issued after it in
+    // flight: wait for it, so that the host buffers are quiet when this call returns
+    if (rc != UPPASD_GPU_OK) cudaStreamSynchronize(s.copy_stream);
     if (rc == UPPASD_GPU_OK && nsteps % every) rc = uppasd::run_steps(s, nsteps % every);
     if (rc == UPPASD_GPU_OK) UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
     return rc;

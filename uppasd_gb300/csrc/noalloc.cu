@@ -9,6 +9,8 @@
 // is being captured on its stream elsewhere, or an embedding runtime that
 // pre-reserves the device at start-up.  See the declaration in
 // include/uppasd_gpu.h for the exact contract.
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 #include <string>
@@ -30,8 +32,39 @@ constexpr int kNaMaxDevices = 64;
 // two calls that overlap on the GPU (different streams) race on this array.
 __device__ __align__(256) double g_partials[kNaMaxEnsembles * kNaBlocks * 3];
 
+// The looked-up address per device, with the unique id of the context it belongs to:
+// a device reset makes a new primary context (with a new id), and the address is then
+// looked up again.
 double *g_partials_addr[kNaMaxDevices] = {};
+unsigned long long g_partials_ctx[kNaMaxDevices] = {};
 std::mutex g_partials_mutex;
+
+// cuCtxGetCurrent / cuCtxGetId through the runtime's driver entry point (nothing links
+// libcuda); both only read the calling thread's state.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_current = nullptr;
+CtxGetIdFn g_ctx_id = nullptr;
+
+// Id of the current context; 0 when no context is current yet.
+int current_context_id(unsigned long long *id) {
+    *id = 0;
+    if (!g_ctx_current || !g_ctx_id) {
+        void *f1 = nullptr, *f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return UPPASD_GPU_ECUDA;
+        g_ctx_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+        g_ctx_id = reinterpret_cast<CtxGetIdFn>(f2);
+    }
+    CUcontext ctx = nullptr;
+    if (g_ctx_current(&ctx) != CUDA_SUCCESS) return UPPASD_GPU_ECUDA;
+    if (ctx && g_ctx_id(ctx, id) != CUDA_SUCCESS) return UPPASD_GPU_ECUDA;
+    return UPPASD_GPU_OK;
+}
 
 __device__ __forceinline__ double warp_sum_na(double v) {
 #pragma unroll
@@ -46,10 +79,11 @@ __global__ void __launch_bounds__(kNaThreads) na_partials(const double *__restri
     const int k = blockIdx.y;
     const double *m = emomM + (size_t)3 * natom * k;
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-    for (int i = blockIdx.x * kNaThreads + threadIdx.x; i < natom; i += kNaBlocks * kNaThreads) {
-        s0 += m[3 * (size_t)i];
-        s1 += m[3 * (size_t)i + 1];
-        s2 += m[3 * (size_t)i + 2];
+    // 64-bit site index: natom close to INT32_MAX must not overflow the stride
+    for (int64_t i = (int64_t)blockIdx.x * kNaThreads + threadIdx.x; i < natom; i += (int64_t)kNaBlocks * kNaThreads) {
+        s0 += m[3 * i];
+        s1 += m[3 * i + 1];
+        s2 += m[3 * i + 2];
     }
     __shared__ double part[kNaThreads / 32][3];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -101,7 +135,8 @@ __global__ void na_finish(const double *__restrict__ partials, int natom, int me
     (void)mensemble;
 }
 
-// Device address of g_partials for the current device, resolved once per device.
+// Device address of g_partials for the current device, resolved once per device
+// context.
 int partials_address(double **out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -114,14 +149,25 @@ int partials_address(double **out) {
         return UPPASD_GPU_ENODEV;
     }
     std::lock_guard<std::mutex> lock(g_partials_mutex);
-    if (!g_partials_addr[dev]) {
+    unsigned long long ctx = 0;
+    if (current_context_id(&ctx)) {
+        set_error("moment_sums_noalloc: the driver's context query failed");
+        return UPPASD_GPU_ECUDA;
+    }
+    // ctx == 0: no context is current yet, so nothing can have been looked up in it
+    if (!g_partials_addr[dev] || ctx == 0 || g_partials_ctx[dev] != ctx) {
         double *ptr = nullptr;
-        e = cudaGetSymbolAddress((void **)&ptr, g_partials);
+        e = cudaGetSymbolAddress((void **)&ptr, g_partials);  // makes the primary context current
         if (e != cudaSuccess || !ptr) {
             set_error(std::string("moment_sums_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             return UPPASD_GPU_ECUDA;
         }
+        if (current_context_id(&ctx) || ctx == 0) {
+            set_error("moment_sums_noalloc: no current CUDA context after the address lookup");
+            return UPPASD_GPU_ECUDA;
+        }
         g_partials_addr[dev] = ptr;
+        g_partials_ctx[dev] = ctx;
     }
     *out = g_partials_addr[dev];
     return UPPASD_GPU_OK;

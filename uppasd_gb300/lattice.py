@@ -119,9 +119,10 @@ def _build_from_stencil(cells, nbasis, periodic, stencil, coup_fn, natom):
     """
     n1, n2, n3 = cells
     mnn = max(len(s) for s in stencil)
-    nlist = np.zeros((natom, mnn), dtype=np.int32)
+    # built slot-major (one contiguous row per slot), transposed to (natom, mnn) at the end
+    nlist_t = np.zeros((mnn, natom), dtype=np.int32)
     nsize = np.zeros(natom, dtype=np.int32)
-    ncoup = np.zeros((natom, mnn), dtype=np.float64)
+    ncoup_t = np.zeros((mnn, natom), dtype=np.float64)
     idx = np.arange(natom, dtype=np.int64)
     b = idx % nbasis
     cell = idx // nbasis
@@ -140,12 +141,19 @@ def _build_from_stencil(cells, nbasis, periodic, stencil, coup_fn, natom):
                 else:
                     ok &= (vv >= 0) & (vv < nn)
             j = _site_index(bj, xx, yy, zz, nbasis, n1, n2)
+            if ok.all():
+                # every site keeps this neighbour: the slot is the same for all of them
+                slot = nsize[sel[0]] if sel.size else 0
+                nlist_t[slot, sel] = (j + 1).astype(np.int32)
+                ncoup_t[slot, sel] = coup_fn(sel, j, shell)
+                nsize[sel] += 1
+                continue
             rows = sel[ok]
             slot = nsize[rows]
-            nlist[rows, slot] = (j[ok] + 1).astype(np.int32)
-            ncoup[rows, slot] = coup_fn(rows, j[ok], shell)
+            nlist_t[slot, rows] = (j[ok] + 1).astype(np.int32)
+            ncoup_t[slot, rows] = coup_fn(rows, j[ok], shell)
             nsize[rows] += 1
-    return nlist, nsize, ncoup
+    return np.ascontiguousarray(nlist_t.T), nsize, np.ascontiguousarray(ncoup_t.T)
 
 
 def chain(n: int, j_mry: float, mom: float = 1.0, periodic: bool = True) -> Lattice:
