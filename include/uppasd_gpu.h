@@ -293,6 +293,18 @@ int uppasd_gpu_mcbatch_get_spins(uppasd_gpu_mcbatch *b, double *emom);
 int uppasd_gpu_mcbatch_put_spins(uppasd_gpu_mcbatch *b, const double *emom);
 /* Sweep counter (the Philox step of the next sweep). */
 int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
+/* This batch as a contiguous share of a larger replica table (one share per GPU;
+ * the reference's replica loop, pt_driver.f90:58-367, has no such split): its
+ * replica r draws its Philox numbers, and its initial state, as replica
+ * first_id + r of the whole table, so every replica's chain is the same whichever
+ * GPU runs it.  Redraws the initial state; call right after create. */
+int uppasd_gpu_mcbatch_set_replica_ids(uppasd_gpu_mcbatch *b, int32_t first_id);
+/* Iteration limit of the replica-group barrier's wait (0 = the default, about a
+ * second or more).  A wait that runs past it records an error and its group leaves the
+ * launch; run/check then return UPPASD_GPU_ESTATE and reset the barrier state, so the
+ * batch stays usable (its spins are those the groups had reached).  For testing the
+ * error path: a limit of 1 makes any group of two or more CTAs give up. */
+int uppasd_gpu_mcbatch_set_spin_limit(uppasd_gpu_mcbatch *b, int64_t limit);
 /* Replica exchange (the swap step of MonteCarlo/pt_driver.f90:58-367 on the batch):
  * after every launch, replicas holding adjacent temperatures of one size swap
  * their temperatures with probability min(1, exp((beta_a - beta_b)(E_a - E_b))),
@@ -313,6 +325,12 @@ int uppasd_gpu_mcbatch_exchange_state(uppasd_gpu_mcbatch *b, int32_t *slot_of_re
  * 2 Cb = tanh(AB^T + bias) in bf16; 3 Cb = AB^T * (1 - Y^2) in bf16 (Y: M x N bf16). */
 int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_t *A, const uint16_t *B, const float *bias,
                        const uint16_t *Y, int32_t epilogue, int32_t bn, float *Cf, uint16_t *Cb);
+/* Self-test of the tensor-core pipeline's bounded waits: one CTA waits, with the
+ * wait the GEMM uses, on an mbarrier that nothing arrives at.  Expected result:
+ * UPPASD_GPU_ESTATE with the message "a pipeline wait ran past its limit (code 4)"
+ * after about a quarter of a second, the context still usable.  No copy or MMA is in
+ * flight during the wait.  No counterpart in the reference. */
+int uppasd_gpu_tc_wait_selftest(void);
 
 /* ---- Learned 4x4-patch proposal with exact Metropolis-Hastings -------------
  * No counterpart in the reference; it acts beside the heat bath of mc_mphase

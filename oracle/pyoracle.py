@@ -14,8 +14,11 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
+# the timed build (-O3, default contraction): the CPU baseline, never the checker
+LIB_FAST = os.path.join(HERE, "liboracle_fast.so")
 
 _lib = None
+_lib_fast = None
 
 I32P = C.POINTER(C.c_int32)
 F64P = C.POINTER(C.c_double)
@@ -64,17 +67,29 @@ NOISE_NONE, NOISE_ZIGGURAT, NOISE_ARRAY, NOISE_PHILOX = 0, 1, 2, 3
 
 
 def build() -> str:
-    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so", "liboracle_fast.so"], check=True)
     return LIB
 
 
-def load():
-    global _lib
+def load(fast: bool = False):
+    """The parity build (default) or, with fast=True, the -O3 build used to time the
+    CPU baseline."""
+    global _lib, _lib_fast
+    if fast:
+        if _lib_fast is None:
+            if not os.path.exists(LIB_FAST):
+                build()
+            _lib_fast = _declare(C.CDLL(LIB_FAST))
+        return _lib_fast
     if _lib is not None:
         return _lib
     if not os.path.exists(LIB):
         build()
-    lib = C.CDLL(LIB)
+    _lib = _declare(C.CDLL(LIB))
+    return _lib
+
+
+def _declare(lib):
     lib.orc_mt_init.argtypes = [C.POINTER(OrcMT), C.c_int32]
     lib.orc_mt_rand64.argtypes = [C.POINTER(OrcMT)]
     lib.orc_mt_rand64.restype = C.c_uint64
@@ -108,7 +123,6 @@ def load():
     lib.orc_set_threads.argtypes = [C.c_int]
     lib.orc_get_threads.restype = C.c_int
     lib.orc_set_units.argtypes = [C.c_double] * 4
-    _lib = lib
     return lib
 
 
@@ -139,8 +153,8 @@ def _p(a, t=F64P):
 class Oracle:
     """Holds one Hamiltonian and one spin state in the reference's layout."""
 
-    def __init__(self, lat, threads: int = 0):
-        self.lib = load()
+    def __init__(self, lat, threads: int = 0, fast: bool = False):
+        self.lib = load(fast)
         self.lib.orc_set_threads(threads)
         self.lat = lat
         N, M = lat.natom, lat.mensemble

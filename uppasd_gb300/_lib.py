@@ -93,6 +93,9 @@ SIGNATURES = {
     "uppasd_gpu_mcbatch_set_exchange": [C.c_void_p, C.c_int32],
     "uppasd_gpu_mcbatch_exchange_state": [C.c_void_p, I32P, I32P, I32P, C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)],
+    "uppasd_gpu_mcbatch_set_replica_ids": [C.c_void_p, C.c_int32],
+    "uppasd_gpu_mcbatch_set_spin_limit": [C.c_void_p, C.c_int64],
+    "uppasd_gpu_tc_wait_selftest": [],
     # tcgen05 BF16 GEMM on host buffers (validation entry point)
     "uppasd_gpu_tc_gemm": [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_int32, C.c_int32, C.c_void_p, C.c_void_p],

@@ -30,7 +30,10 @@ def _f64(a):
 
 class ReplicaBatch:
     def __init__(self, L, temperature, heatbath=True, j_shells_mry=(1.3, 0.7), mom: float = 2.2, bfield=None,
-                 seed: int = 1, series_len: int = 0, max_sweeps_per_launch: int = 256):
+                 seed: int = 1, series_len: int = 0, max_sweeps_per_launch: int = 256, first_id: int = 0):
+        """first_id: the id of this batch's first replica in a larger table that is split
+        over processes (``replicas.partition``); its chains are then those of the whole
+        table's replicas first_id, first_id + 1, ..."""
         self.lib = _lib.load()
         self.L = _i32(L)
         self.T = _f64(temperature)
@@ -51,6 +54,9 @@ class ReplicaBatch:
                   None if bf is None else self._p(bf), seed, self.series_len, self.max_spl, C.byref(h))
         self.h = h
         self._keep = (js, bf)
+        self.first_id = int(first_id)
+        if self.first_id:
+            _lib.call("uppasd_gpu_mcbatch_set_replica_ids", self.h, self.first_id)
 
     @staticmethod
     def _p(a, t=_lib.F64P):
@@ -91,6 +97,10 @@ class ReplicaBatch:
 
     def set_sweep(self, sweep: int):
         _lib.call("uppasd_gpu_mcbatch_set_sweep", self.h, int(sweep))
+
+    def set_spin_limit(self, limit: int = 0):
+        """Iteration limit of the replica-group barrier's wait (0: the default)."""
+        _lib.call("uppasd_gpu_mcbatch_set_spin_limit", self.h, int(limit))
 
     # ---- replica exchange ----
     def set_exchange(self, enable: bool = True):

@@ -92,6 +92,7 @@ struct MBParams {
     long long *sweep_ctr;     // device sweep counter (Philox step)
     long long *rep_ns;        // per replica: ns the group spent in the last launch
     uint64_t seed;
+    int rep_id0;              // id of replica 0 in the Philox counters (a share of a larger table)
     long long spin_limit;
     // replica exchange (parallel tempering) between adjacent temperatures of one size
     int *rep_of_slot;             // replica currently at each temperature slot
@@ -228,7 +229,7 @@ __device__ __forceinline__ void update_site(const MBParams &p, const MBRep &R, c
                                             long long sweep, int b, int par, int x, int y, int z, int t,
                                             float4 *own, float &dE, float3 &dM) {
     const int site = b + 2 * (x + R.L * (y + R.L * z));
-    const Philox4 w = philox_draw(p.seed, site, r, sweep, kStreamMC);
+    const Philox4 w = philox_draw(p.seed, site, r + p.rep_id0, sweep, kStreamMC);
     const float3 hx = exchange_field(rep, R, b, par, x, y, z, t);
     const float3 h = make_float3(hx.x + R.ext[0], hx.y + R.ext[1], hx.z + R.ext[2]);
     const float4 cur = *own;
@@ -246,7 +247,7 @@ __device__ __forceinline__ void update_site(const MBParams &p, const MBRep &R, c
             nm = make_float3(st * cp, st * sp, ct);
         } else if (ftype == 1) {
             float g[3];
-            normal3_f32(p.seed, site, r, sweep, kStreamMCGauss, g);
+            normal3_f32(p.seed, site, r + p.rep_id0, sweep, kStreamMCGauss, g);
             const float ax = fmaf(g[0], R.delta, cur.x), ay = fmaf(g[1], R.delta, cur.y),
                         az = fmaf(g[2], R.delta, cur.z);
             const float il = rsqrtf(ax * ax + ay * ay + az * az);
@@ -657,12 +658,49 @@ int enqueue_chunk(uppasd_gpu_mcbatch *b, int n) {
     return UPPASD_GPU_OK;
 }
 
+// iterations of a group barrier's wait (~32-100 ns naps each): a stalled group gives
+// up within seconds
+constexpr long long kDefaultSpinLimit = 1LL << 25;
+
+// Initial state: uniform on the sphere, Philox (site, replica id, 0, stream
+// kStreamLearned + 1), replica ids rep_id0, rep_id0 + 1, ...
+int draw_initial_state(uppasd_gpu_mcbatch *b) {
+    std::vector<float4> h((size_t)b->pool_f4);
+    const uint64_t seed = b->p.seed;
+    for (size_t i = 0; i < b->reps.size(); ++i) {
+        const MBRep &R = b->reps[i];
+        const int id = (int)i + b->p.rep_id0;
+        for (int c = 0; c < 4; ++c)
+            for (long long t = 0; t < R.nhalf; ++t) {
+                const int bb = c >> 1, par = c & 1;
+                const long long row = t / R.Lh;
+                const int xh = (int)(t - row * R.Lh), z = (int)(row / R.L), y = (int)(row - (long long)z * R.L);
+                const int x = 2 * xh + ((par + y + z) & 1);
+                const long long site = bb + 2LL * (x + (long long)R.L * (y + (long long)R.L * z));
+                const uppasd::Philox4 w = uppasd::philox_draw(seed, site, id, 0, uppasd::kStreamLearned + 1u);
+                const double ct = 1.0 - 2.0 * uppasd::u01_open(w.x), st = sqrt(std::max(0.0, 1.0 - ct * ct));
+                const double ph = 2.0 * uppasd::kPi * uppasd::u01_open(w.y);
+                h[(size_t)(R.off + c * R.nhalf + t)] =
+                    make_float4((float)(st * cos(ph)), (float)(st * sin(ph)), (float)ct, 0.f);
+            }
+    }
+    cudaError_t e = cudaMemcpy(b->p.pool, h.data(), (size_t)b->pool_f4 * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail("mcbatch initial state", e);
+    return UPPASD_GPU_OK;
+}
+
 int check_err(uppasd_gpu_mcbatch *b) {
     cudaError_t e = cudaStreamSynchronize(b->stream);
     int err = 0;
     if (e == cudaSuccess) e = cudaMemcpy(&err, b->p.err, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_fail("mcbatch", e);
     if (err) {
+        // the groups that gave up left their arrive counters out of step: start every
+        // counter and the flag afresh, so that the next launch's barriers line up again
+        const int zero = 0;
+        e = cudaMemset(b->p.bar, 0, b->reps.size() * uppasd::kBarStride * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMemcpy(b->p.err, &zero, sizeof(int), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return cuda_fail("mcbatch barrier reset", e);
         set_error("mcbatch: a replica group barrier wait ran past its limit");
         return UPPASD_GPU_ESTATE;
     }
@@ -908,29 +946,11 @@ int uppasd_gpu_mcbatch_create(int32_t nrep, const int32_t *L, const double *temp
     b->p.rep_of_slot = b->rep_of_slot_d;
     b->p.slot_beta = b->slot_beta_d;
     b->p.pt_ctr = b->pt_ctr_d;
-    b->p.spin_limit = 1LL << 25;  // x ~32-100 ns naps: a stalled group gives up within seconds
-    // initial state: uniform on the sphere, Philox (site, replica, 0, stream kStreamLearned + 1)
+    b->p.spin_limit = kDefaultSpinLimit;
+    b->p.rep_id0 = 0;
     {
-        std::vector<float4> h((size_t)pool);
-        for (int i = 0; i < nrep; ++i) {
-            const MBRep &R = b->reps[i];
-            for (int c = 0; c < 4; ++c)
-                for (long long t = 0; t < R.nhalf; ++t) {
-                    const int bb = c >> 1, par = c & 1;
-                    const long long row = t / R.Lh;
-                    const int xh = (int)(t - row * R.Lh), z = (int)(row / R.L), y = (int)(row - (long long)z * R.L);
-                    const int x = 2 * xh + ((par + y + z) & 1);
-                    const long long site = bb + 2LL * (x + (long long)R.L * (y + (long long)R.L * z));
-                    const uppasd::Philox4 w = uppasd::philox_draw(seed, site, i, 0, uppasd::kStreamLearned + 1u);
-                    const double ct = 1.0 - 2.0 * uppasd::u01_open(w.x), st = sqrt(std::max(0.0, 1.0 - ct * ct));
-                    const double ph = 2.0 * uppasd::kPi * uppasd::u01_open(w.y);
-                    h[(size_t)(R.off + c * R.nhalf + t)] =
-                        make_float4((float)(st * cos(ph)), (float)(st * sin(ph)), (float)ct, 0.f);
-                }
-        }
-        e = cudaMemcpy(b->p.pool, h.data(), (size_t)pool * sizeof(float4), cudaMemcpyHostToDevice);
-        if (e != cudaSuccess) {
-            int rc = cuda_fail("mcbatch_create", e);
+        const int rc = draw_initial_state(b);
+        if (rc) {
             mb_free(b);
             return rc;
         }
@@ -1287,6 +1307,36 @@ int uppasd_gpu_mcbatch_exchange_state(uppasd_gpu_mcbatch *b, int32_t *slot_of_re
             pairs[2 * q] = b->pairs_h[q].x;
             pairs[2 * q + 1] = b->pairs_h[q].y;
         }
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_mcbatch_set_replica_ids(uppasd_gpu_mcbatch *b, int32_t first_id) {
+    if (!b || first_id < 0) {
+        set_error("mcbatch_set_replica_ids: null handle or negative id");
+        return UPPASD_GPU_EINVAL;
+    }
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_fail("mcbatch_set_replica_ids", e);
+    b->p.rep_id0 = first_id;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    return draw_initial_state(b);
+}
+
+int uppasd_gpu_mcbatch_set_spin_limit(uppasd_gpu_mcbatch *b, int64_t limit) {
+    if (!b || limit < 0) {
+        set_error("mcbatch_set_spin_limit: null handle or negative limit");
+        return UPPASD_GPU_EINVAL;
+    }
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) return cuda_fail("mcbatch_set_spin_limit", e);
+    b->p.spin_limit = limit ? (long long)limit : kDefaultSpinLimit;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
     return UPPASD_GPU_OK;
 }
 

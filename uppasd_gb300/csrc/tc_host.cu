@@ -224,3 +224,47 @@ extern "C" int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_
     cudaFree(derr);
     return rc;
 }
+
+namespace uppasd {
+namespace tc {
+namespace {
+
+// One CTA waits on an mbarrier that nothing arrives at, through the GEMM pipeline's own
+// bounded wait: it gives up after kWaitLimit polls and records code 4.  No copy or MMA
+// is issued, so nothing is left in flight when the CTA returns.
+__global__ void wait_selftest_kernel(int *err) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (!mbar_wait(&bar, 0)) atomicExch(err, 4);
+    }
+}
+
+}  // namespace
+}  // namespace tc
+}  // namespace uppasd
+
+extern "C" int uppasd_gpu_tc_wait_selftest(void) {
+    using namespace uppasd;
+    int *derr = nullptr, herr = 0;
+    cudaError_t e = cudaMalloc(&derr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(derr, 0, sizeof(int));
+    if (e == cudaSuccess) {
+        tc::wait_selftest_kernel<<<1, 32>>>(derr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, derr, sizeof(int), cudaMemcpyDeviceToHost);
+    cudaFree(derr);
+    if (e != cudaSuccess) {
+        set_error(std::string("tc_wait_selftest: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ECUDA;
+    }
+    if (herr) {
+        set_error("tc_wait_selftest: a pipeline wait ran past its limit (code " + std::to_string(herr) + ")");
+        return UPPASD_GPU_ESTATE;
+    }
+    set_error("tc_wait_selftest: the wait completed although nothing arrived");
+    return UPPASD_GPU_ECUDA;
+}
