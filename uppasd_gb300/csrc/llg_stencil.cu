@@ -89,8 +89,8 @@ struct SParams {
     long long pbox;             // cells per padded sublattice box = P2 * (L3 + 4)
     long long nsite;            // sites per ensemble (2 L1 L2 L3)
     float4 *mt, *mp;            // padded mirrors at t and at the predictor
-    float *b2x, *b2y, *b2z;     // predictor's damped field (Depondt b2eff)
-    float *thx, *thy, *thz;     // thermal field drawn by the predictor, reused by the corrector
+    // the predictor's damped field b2eff plus the corrector's thermal term (see predict_update)
+    float *b2x, *b2y, *b2z;
     float *lox, *loy, *loz;     // double-single residuals (precision 2)
     double *mx, *my, *mz;       // FP64 master (precision 1)
     float cA[4][2], cD[4][2];   // coupling on unit vectors: cA[sh][s_i] + s_j * cD[sh][s_i]
@@ -226,7 +226,12 @@ __device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
 }
 
 // Predictor update of one site from its field B: thermal field, Depondt damped
-// field, Rodrigues rotation; writes m_pred (with ghosts), b2eff and the thermal field.
+// field, Rodrigues rotation; writes m_pred (with ghosts) and one 3-vector for the
+// corrector.  The corrector's damped field at the predicted spin ep splits as
+//   bdup(ep, B(ep) + th) = bdup(ep, B(ep)) + [th + lambda ep x th],
+// and the bracket is known here (ep is this thread's own result), so the predictor
+// stores b2eff + th + lambda ep x th (depondt.f90:152-154, 290-301) and the thermal field
+// itself is neither stored nor drawn again.
 __device__ __forceinline__ void predict_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &me,
                                                const float B[3]) {
     const int si = me.w != 0.f ? 1 : 0;
@@ -240,14 +245,14 @@ __device__ __forceinline__ void predict_update(const SParams &p, int k, int b, i
     float bd[3], d[3];
     depondt_bdup(p.lam, e, bl, bd);
     rotation_delta(bd, e, p.dtg, d);
-    store_mirror(p, p.mp, k, b, x, y, z, make_float4(e[0] + d[0], e[1] + d[1], e[2] + d[2], me.w));
+    const float ep[3] = {e[0] + d[0], e[1] + d[1], e[2] + d[2]};
+    store_mirror(p, p.mp, k, b, x, y, z, make_float4(ep[0], ep[1], ep[2], me.w));
+    float tc[3];
+    depondt_bdup(p.lam, ep, th, tc);
     const long long u = uidx(p, k, b, x, y, z);
-    p.b2x[u] = bd[0];
-    p.b2y[u] = bd[1];
-    p.b2z[u] = bd[2];
-    p.thx[u] = th[0];
-    p.thy[u] = th[1];
-    p.thz[u] = th[2];
+    p.b2x[u] = bd[0] + tc[0];
+    p.b2y[u] = bd[1] + tc[1];
+    p.b2z[u] = bd[2] + tc[2];
 }
 
 template <int NSH, int b, int LC>
@@ -289,9 +294,8 @@ __device__ __forceinline__ void correct_update(const SParams &p, int k, int b, i
     const long long o = pidx(p, k, b, x, y, z);
     const long long u = uidx(p, k, b, x, y, z);
     const float ep[3] = {mp.x, mp.y, mp.z};
-    float bl[3] = {B[0] + p.thx[u], B[1] + p.thy[u], B[2] + p.thz[u]};
     float bd[3];
-    depondt_bdup(p.lam, ep, bl, bd);
+    depondt_bdup(p.lam, ep, B, bd);   // the thermal term is in b2 (predict_update)
     bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[u];
     bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[u];
     bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[u];
@@ -587,7 +591,7 @@ void structured_refresh(Sim &s) {
 
 static void fast_free(StructuredFast *f) {
     if (!f) return;
-    void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.thx, f->p.thy, f->p.thz, f->p.lox, f->p.loy, f->p.loz,
+    void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.lox, f->p.loy, f->p.loz,
                     f->p.mx, f->p.my, f->p.mz, f->species};
     for (void *q : ptrs) cudaFree(q);
     delete f;
@@ -716,9 +720,6 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     al((void **)&p.b2x, n * sizeof(float));
     al((void **)&p.b2y, n * sizeof(float));
     al((void **)&p.b2z, n * sizeof(float));
-    al((void **)&p.thx, n * sizeof(float));
-    al((void **)&p.thy, n * sizeof(float));
-    al((void **)&p.thz, n * sizeof(float));
     if (f->master == 1) {
         al((void **)&p.mx, n * sizeof(double));
         al((void **)&p.my, n * sizeof(double));

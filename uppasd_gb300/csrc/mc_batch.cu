@@ -128,8 +128,10 @@ __device__ __forceinline__ bool group_barrier(const MBParams &p, int r, int n) {
         const unsigned long long old = atomicAdd(ctr, 1ull);
         const unsigned long long target = (old / (unsigned long long)n + 1ull) * (unsigned long long)n;
         long long it = 0;
+        const long long t0 = globaltimer_ns();
         while (ld_acquire_u64(ctr) < target) {
-            if (++it > p.spin_limit) {
+            // give up after spin_limit polls or about two seconds, whichever comes first
+            if (++it > p.spin_limit || ((it & 63) == 0 && globaltimer_ns() - t0 > 2000000000LL)) {
                 atomicExch(p.err, 1);
                 failed = 1;
                 break;
@@ -658,9 +660,9 @@ int enqueue_chunk(uppasd_gpu_mcbatch *b, int n) {
     return UPPASD_GPU_OK;
 }
 
-// iterations of a group barrier's wait (~32-100 ns naps each): a stalled group gives
-// up within seconds
-constexpr long long kDefaultSpinLimit = 1LL << 25;
+// polls of a group barrier's wait by default: beyond any real wait; the wait's own time
+// limit (about two seconds) is what ends a stalled group
+constexpr long long kDefaultSpinLimit = 1LL << 40;
 
 // Initial state: uniform on the sphere, Philox (site, replica id, 0, stream
 // kStreamLearned + 1), replica ids rep_id0, rep_id0 + 1, ...

@@ -28,7 +28,8 @@ constexpr int kBM = 128;
 constexpr int kBK = 64;       // bf16 elements per K slice = one 128-byte swizzle row
 constexpr int kMaxStages = 4;
 constexpr int kThreads = 128;
-constexpr long long kWaitLimit = 1LL << 22;
+// a pipeline wait gives up after about a second of %globaltimer time
+constexpr long long kWaitLimitNs = 1000000000LL;
 
 enum Epilogue : int {
     kEpiStoreF32 = 0,     // C_f32 = acc
@@ -59,10 +60,18 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Bounded wait for the phase with parity `parity` to complete; false after the limit.
+__device__ __forceinline__ long long tc_globaltimer() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait for the phase with parity `parity` to complete; false once about
+// kWaitLimitNs have passed.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     const uint32_t a = smem_u32(bar);
-    for (long long it = 0; it < kWaitLimit; ++it) {
+    long long t0 = 0;
+    for (long long it = 0;; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -72,9 +81,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if (it > 64) __nanosleep(64);
+        if (it == 64) t0 = tc_globaltimer();
+        if (it > 64) {
+            if ((it & 63) == 0 && tc_globaltimer() - t0 > kWaitLimitNs) return false;
+            __nanosleep(64);
+        }
     }
-    return false;
 }
 
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {

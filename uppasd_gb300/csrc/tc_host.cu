@@ -230,7 +230,7 @@ namespace tc {
 namespace {
 
 // One CTA waits on an mbarrier that nothing arrives at, through the GEMM pipeline's own
-// bounded wait: it gives up after kWaitLimit polls and records code 4.  No copy or MMA
+// bounded wait: it gives up after about kWaitLimitNs and records code 4.  No copy or MMA
 // is issued, so nothing is left in flight when the CTA returns.
 __global__ void wait_selftest_kernel(int *err) {
     __shared__ __align__(8) uint64_t bar;
