@@ -30,6 +30,7 @@
 // basis and one ensemble per block.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <utility>
 #include <vector>
 
@@ -491,6 +492,144 @@ __global__ void __launch_bounds__(256) stencil_zblock(SParams p) {
     else zb_sites<NSH, 1, NZ, LC, KIND, MASTER>(p, k, x, y, z0);
 }
 
+// ---------------------------------------------------------------------------
+// Cell-blocked gather: a thread produces both sites (corner b = 0 and centre
+// b = 1) of NZ cells stacked in z.  The two sublattices' neighbourhoods overlap
+// (the centre's corner neighbours include the corner's own same-sublattice
+// neighbours and vice versa), so the union of the 4 NZ sites' 50-point stencils
+// is 24 points per site for NZ = 2 (36 with one sublattice per thread, 50 with one
+// site).  Points and (site, shell) pairs come from the constexpr evaluator as above;
+// site index = b * NZ + q.
+__host__ __device__ constexpr ZbTables make_cb(int nsh, int nz) {
+    ZbTables t{};
+    int np = 0, nq = 0;
+    for (int bj = 0; bj < 2; ++bj)
+        for (int zz = -2; zz <= nz + 1; ++zz)
+            for (int dy = -2; dy <= 2; ++dy)
+                for (int dx = -2; dx <= 2; ++dx) {
+                    const int first = nq;
+                    for (int b = 0; b < 2; ++b)
+                        for (int q = 0; q < nz; ++q)
+                            for (int s = 0; s < nb_of_shells(nsh); ++s) {
+                                const St e = stencil_entry(b, s);
+                                if (e.bj == bj && e.dx == dx && e.dy == dy && q + e.dz == zz)
+                                    t.pairs[nq++] = ZbPair{(int8_t)(b * nz + q), e.sh};
+                            }
+                    if (nq > first)
+                        t.pts[np++] = ZbPt{(int8_t)bj, (int8_t)dx, (int8_t)dy, (int8_t)zz, (uint8_t)first,
+                                           (uint8_t)(nq - first)};
+                }
+    t.npts = np;
+    t.npairs = nq;
+    return t;
+}
+
+template <int NSH, int NZ>
+struct CB {
+    static constexpr ZbTables t = make_cb(NSH, NZ);
+};
+
+template <int NSH, int NZ, int I>
+__device__ __forceinline__ void cb_pair(const float4 &v, const float (&cA)[2 * NZ][4], const float (&cD)[2 * NZ][4],
+                                        float (&acc)[2 * NZ][3]) {
+    constexpr ZbPair pr = CB<NSH, NZ>::t.pairs[I];
+    const float c = fmaf(v.w, cD[pr.q][pr.sh - 1], cA[pr.q][pr.sh - 1]);
+    acc[pr.q][0] = fmaf(c, v.x, acc[pr.q][0]);
+    acc[pr.q][1] = fmaf(c, v.y, acc[pr.q][1]);
+    acc[pr.q][2] = fmaf(c, v.z, acc[pr.q][2]);
+}
+
+template <int NSH, int NZ, int FIRST, int... R>
+__device__ __forceinline__ void cb_pairs(const float4 &v, const float (&cA)[2 * NZ][4], const float (&cD)[2 * NZ][4],
+                                         float (&acc)[2 * NZ][3], std::integer_sequence<int, R...>) {
+    (cb_pair<NSH, NZ, FIRST + R>(v, cA, cD, acc), ...);
+}
+
+// Point source of the gather: the padded global mirror, read through the
+// read-only data cache.  (bj, dx, dy, dz) are compile-time offsets from the
+// thread's cell at its first z.
+template <int LC>
+struct GlobalSrc {
+    const float4 *base0, *base1;
+    template <int BJ, int DX, int DY, int DZ>
+    __device__ __forceinline__ float4 get() const {
+        constexpr int off = DZ * pitch2(LC) + DY * pitch1(LC) + DX;
+        return __ldg((BJ ? base1 : base0) + off);
+    }
+};
+
+template <int NSH, int NZ, class Src, int Q>
+__device__ __forceinline__ void cb_point(const Src &src, const float (&cA)[2 * NZ][4], const float (&cD)[2 * NZ][4],
+                                         float (&acc)[2 * NZ][3]) {
+    constexpr ZbPt pt = CB<NSH, NZ>::t.pts[Q];
+    const float4 v = src.template get<pt.bj, pt.dx, pt.dy, pt.dz>();
+    cb_pairs<NSH, NZ, pt.first>(v, cA, cD, acc, std::make_integer_sequence<int, pt.count>{});
+}
+
+template <int NSH, int NZ, class Src, int... Q>
+__device__ __forceinline__ void cb_points(const Src &src, const float (&cA)[2 * NZ][4], const float (&cD)[2 * NZ][4],
+                                          float (&acc)[2 * NZ][3], std::integer_sequence<int, Q...>) {
+    (cb_point<NSH, NZ, Src, Q>(src, cA, cD, acc), ...);
+}
+
+// Both sites of NZ cells: own values, the gather, then the predictor or corrector
+// update of every site.
+template <int NSH, int NZ, int KIND, int MASTER, class Src>
+__device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k, int x, int y, int z0) {
+    float4 me[2 * NZ];
+    float cA[2 * NZ][4], cD[2 * NZ][4], acc[2 * NZ][3];
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) {
+            const int i = b * NZ + q;
+            me[i] = b ? src.template get<1, 0, 0, 0>(q) : src.template get<0, 0, 0, 0>(q);
+            const int si = me[i].w != 0.f ? 1 : 0;
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                cA[i][s] = si ? p.cA[s][1] : p.cA[s][0];
+                cD[i][s] = si ? p.cD[s][1] : p.cD[s][0];
+            }
+            acc[i][0] = acc[i][1] = acc[i][2] = 0.f;
+        }
+    cb_points<NSH, NZ>(src, cA, cD, acc, std::make_integer_sequence<int, CB<NSH, NZ>::t.npts>{});
+#pragma unroll
+    for (int b = 0; b < 2; ++b)
+#pragma unroll
+        for (int q = 0; q < NZ; ++q) {
+            const int i = b * NZ + q;
+            const float Bf[3] = {acc[i][0] + p.ext[0], acc[i][1] + p.ext[1], acc[i][2] + p.ext[2]};
+            if (KIND == 0) predict_update(p, k, b, x, y, z0 + q, me[i], Bf);
+            else correct_update<MASTER>(p, k, b, x, y, z0 + q, me[i], Bf);
+        }
+}
+
+template <int LC>
+struct GlobalSrcQ : GlobalSrc<LC> {
+    using GlobalSrc<LC>::get;
+    // own site of sublattice BJ at z offset q (runtime q, unrolled by the caller)
+    template <int BJ, int DX, int DY, int DZ>
+    __device__ __forceinline__ float4 get(int q) const {
+        return (BJ ? this->base1 : this->base0)[q * pitch2(LC)];
+    }
+};
+
+template <int NSH, int NZ, int LC, int KIND, int MASTER>
+__global__ void __launch_bounds__(256) stencil_cells(SParams p) {
+    const int nyt = (p.L2 + blockDim.y - 1) / blockDim.y;
+    const int x = threadIdx.x;
+    const int y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
+    const int z0 = (blockIdx.x / nyt) * NZ;
+    const int k = blockIdx.z;
+    if (x >= p.L1 || y >= p.L2) return;
+    const float4 *m = KIND == 0 ? p.mt : p.mp;
+    const long long own = (long long)(z0 + 2) * pitch2(LC) + (long long)(y + 2) * pitch1(LC) + (x + XOFF);
+    GlobalSrcQ<LC> src;
+    src.base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
+    src.base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
+    cb_sites<NSH, NZ, KIND, MASTER>(p, src, k, x, y, z0);
+}
+
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
 // and the structured state.
 __global__ void to_structured(SParams p, const double *ex, const double *ey, const double *ez,
@@ -555,6 +694,7 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
 struct StructuredFast {
     SParams p{};
     int nshell = 0, master = 1, lc = 0;
+    int kernel = 1;  // compiled sizes: 0 one sublattice per thread (stencil_zblock), 1 both (stencil_cells)
     dim3 grid, block;
     int8_t *species = nullptr;
     // what the thermal amplitude and the rotation scale are computed from
@@ -674,6 +814,7 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     if (!f) return UPPASD_GPU_ENOMEM;
     f->nshell = nshell;
     f->master = c->precision;
+    if (const char *kv = getenv("UPPASD_STENCIL_KERNEL")) f->kernel = atoi(kv);
     SParams &p = f->p;
     p.L1 = L1;
     p.L2 = L2;
@@ -777,6 +918,15 @@ static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
         constexpr int NZP = 2;
         constexpr int NZC = 2;
         const unsigned nyt = (unsigned)((f->p.L2 + f->block.y - 1) / f->block.y);
+        if (f->kernel == 1) {
+            const dim3 g(nyt * (LC / 2), 1, (unsigned)f->p.nens);
+            if (phase & 1) stencil_cells<NSH, 2, LC, 0, 2><<<g, f->block, 0, st>>>(f->p);
+            if (phase & 2) {
+                if (f->master == 1) stencil_cells<NSH, 2, LC, 1, 1><<<g, f->block, 0, st>>>(f->p);
+                else stencil_cells<NSH, 2, LC, 1, 2><<<g, f->block, 0, st>>>(f->p);
+            }
+            return;
+        }
         if (phase & 1)
             stencil_zblock<NSH, NZP, LC, 0, 2>
                 <<<dim3(nyt * (LC / NZP), 2, (unsigned)f->p.nens), f->block, 0, st>>>(f->p);
