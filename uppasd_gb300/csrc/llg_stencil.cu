@@ -36,6 +36,8 @@
 
 #include "common.cuh"
 #include "sim.h"
+#include "tc_gemm.cuh"
+#include "tc_host.h"
 
 namespace uppasd {
 
@@ -101,6 +103,7 @@ struct SParams {
     uint64_t seed;
     const int64_t *d_step;
     long long step_off;
+    int *err;                   // set when a plane wait of the staged kernels ran past its limit
 };
 
 __device__ __forceinline__ long long pidx(const SParams &p, int k, int b, int x, int y, int z) {
@@ -572,18 +575,23 @@ __device__ __forceinline__ void cb_points(const Src &src, const float (&cA)[2 * 
     (cb_point<NSH, NZ, Src, Q>(src, cA, cD, acc), ...);
 }
 
+template <int NZ, class Src, int... I>
+__device__ __forceinline__ void cb_own(const Src &src, float4 (&me)[2 * NZ], std::integer_sequence<int, I...>) {
+    ((me[I] = src.template get<I / NZ, 0, 0, I % NZ>()), ...);
+}
+
 // Both sites of NZ cells: own values, the gather, then the predictor or corrector
 // update of every site.
 template <int NSH, int NZ, int KIND, int MASTER, class Src>
 __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k, int x, int y, int z0) {
     float4 me[2 * NZ];
     float cA[2 * NZ][4], cD[2 * NZ][4], acc[2 * NZ][3];
+    cb_own<NZ>(src, me, std::make_integer_sequence<int, 2 * NZ>{});
 #pragma unroll
     for (int b = 0; b < 2; ++b)
 #pragma unroll
         for (int q = 0; q < NZ; ++q) {
             const int i = b * NZ + q;
-            me[i] = b ? src.template get<1, 0, 0, 0>(q) : src.template get<0, 0, 0, 0>(q);
             const int si = me[i].w != 0.f ? 1 : 0;
 #pragma unroll
             for (int s = 0; s < 4; ++s) {
@@ -604,16 +612,6 @@ __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k
         }
 }
 
-template <int LC>
-struct GlobalSrcQ : GlobalSrc<LC> {
-    using GlobalSrc<LC>::get;
-    // own site of sublattice BJ at z offset q (runtime q, unrolled by the caller)
-    template <int BJ, int DX, int DY, int DZ>
-    __device__ __forceinline__ float4 get(int q) const {
-        return (BJ ? this->base1 : this->base0)[q * pitch2(LC)];
-    }
-};
-
 template <int NSH, int NZ, int LC, int KIND, int MASTER>
 __global__ void __launch_bounds__(256) stencil_cells(SParams p) {
     const int nyt = (p.L2 + blockDim.y - 1) / blockDim.y;
@@ -624,10 +622,131 @@ __global__ void __launch_bounds__(256) stencil_cells(SParams p) {
     if (x >= p.L1 || y >= p.L2) return;
     const float4 *m = KIND == 0 ? p.mt : p.mp;
     const long long own = (long long)(z0 + 2) * pitch2(LC) + (long long)(y + 2) * pitch1(LC) + (x + XOFF);
-    GlobalSrcQ<LC> src;
+    GlobalSrc<LC> src;
     src.base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
     src.base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
     cb_sites<NSH, NZ, KIND, MASTER>(p, src, k, x, y, z0);
+}
+
+
+// ---------------------------------------------------------------------------
+// Plane-staged gather (TMA).  A CTA owns a TX x TY tile of cells of one ensemble and
+// a chunk of ZC planes, and marches up z two planes at a time.  The planes it reads
+// arrive by TMA (cp.async.bulk.tensor, 5-D map over the padded mirror: float lane,
+// x, y, z, ensemble x sublattice) into a ring of kRing slots in shared memory; slot
+// u holds the (TX + 3) x (TY + 3) box of the centre sublattice at plane pz and of the
+// corner sublattice at plane pz + 1 (pz = zs - 2 + u), which is exactly what output
+// plane z needs from slots pz = z - 2 .. z + 1 (the corner sites' centre neighbours
+// lie at dz in [-2, 1], the centre sites' corner neighbours at dz in [-1, 2]).  Each
+// iteration computes both sites of two planes of the tile (cb_sites) from shared
+// memory while the slots of the next iteration load; every neighbour is fetched from
+// DRAM / L2 once per tile instead of once per reading site.
+constexpr int kRing = 7;
+
+template <int TX, int TY>
+struct TileGeom {
+    static constexpr int BW = TX + 3, BH = TY + 3;
+    static constexpr uint32_t kBox = (uint32_t)BW * BH * 16;          // bytes the TMA box moves
+    static constexpr uint32_t kBoxA = (kBox + 127) / 128 * 128;       // box stride in shared memory
+    static constexpr uint32_t kSlot = 2 * kBoxA;
+    static constexpr size_t kSmem = (size_t)kRing * kSlot + 128;      // + alignment slack
+};
+
+// Tile geometry of the plane-staged kernels per compiled size: (TX, TY, ZC).
+template <int LC>
+struct TmaTile {
+    static constexpr int TX = LC == 100 ? 50 : (LC == 64 ? 32 : LC);
+    static constexpr int TY = LC == 100 ? 5 : (LC == 64 ? 8 : LC);
+    static constexpr int ZC = LC == 100 ? 20 : (LC == 64 ? 16 : LC);
+};
+
+// Point source of the gather: this thread's cell in the five slots of the
+// current iteration (slot of plane z - 2 + j at pj[j]).
+template <int TX, int TY>
+struct SmemSrc {
+    const uint8_t *pj[5];
+    template <int BJ, int DX, int DY, int DZ>
+    __device__ __forceinline__ float4 get() const {
+        using G = TileGeom<TX, TY>;
+        constexpr int j = DZ + 1 + BJ;
+        constexpr int off = BJ * (int)G::kBoxA + 16 * ((DY + 1 + BJ) * G::BW + DX + 1 + BJ);
+        static_assert(j >= 0 && j < 5, "plane outside the iteration's slots");
+        return *reinterpret_cast<const float4 *>(pj[j] + off);
+    }
+};
+
+__device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2,
+                                            int c3, int c4) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5, %6, %7}], "
+        "[%2];" ::"r"(tc::smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(tc::smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4)
+        : "memory");
+}
+
+template <int NSH, int LC, int TX, int TY, int ZC, int KIND, int MASTER>
+__global__ void __launch_bounds__(TX * TY, 2) stencil_tma(const __grid_constant__ CUtensorMap mapm, SParams p, int ntx,
+                                                       int nty) {
+    using G = TileGeom<TX, TY>;
+    static_assert(ZC % 2 == 0 && ZC >= 4, "two planes per iteration, at least two iterations");
+    constexpr int kSlots = ZC + 3;  // pz = zs - 2 .. zs + ZC
+    extern __shared__ uint8_t tma_smem_raw[];
+    uint8_t *ring = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(tma_smem_raw) + 127) & ~(uintptr_t)127);
+    __shared__ __align__(8) uint64_t full[kRing];
+    __shared__ int fail;
+    const int t = threadIdx.x;
+    const int bid = blockIdx.x;
+    const int x0 = (bid % ntx) * TX, y0 = ((bid / ntx) % nty) * TY, zs = (bid / (ntx * nty)) * ZC;
+    const int k = blockIdx.z;
+    const int tx = t % TX, ty = t / TX;
+    const int x = x0 + tx, y = y0 + ty;
+    const bool active = x < p.L1 && y < p.L2;
+    if (t == 0) {
+        for (int r = 0; r < kRing; ++r) tc::mbar_init(&full[r], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        fail = 0;
+    }
+    __syncthreads();
+    // slot u: corner plane pz + 1 and centre plane pz, pz = zs - 2 + u, padded z = pz + 2
+    auto issue = [&](int u) {
+        const int r = u % kRing, pz = zs - 2 + u;
+        uint8_t *dst = ring + r * G::kSlot;
+        tc::mbar_expect_tx(&full[r], 2 * G::kBox);
+        tma_load_5d(dst, &mapm, &full[r], 0, x0 - 1 + XOFF, y0 + 1, pz + 3, 2 * k);
+        tma_load_5d(dst + G::kBoxA, &mapm, &full[r], 0, x0 - 2 + XOFF, y0, pz + 2, 2 * k + 1);
+    };
+    int issued = 0;  // slots issued so far (thread 0)
+    if (t == 0)
+        for (; issued < kRing && issued < kSlots; ++issued) issue(issued);
+    const uint8_t *cell = ring + 16 * (ty * G::BW + tx);
+    for (int i = 0; i < ZC / 2; ++i) {
+        if (i > 0) {
+            __syncthreads();  // the previous iteration's reads of its oldest slots are done
+            if (fail) break;
+            if (t == 0)
+                for (int u = 2 * i + 5; u <= 2 * i + 6 && u < kSlots; ++u, ++issued) issue(u);
+        }
+        bool ok = true;
+        for (int u = i == 0 ? 0 : 2 * i + 3; u <= 2 * i + 4; ++u) ok = ok && tc::mbar_wait(&full[u % kRing], (u / kRing) & 1);
+        if (!ok) {
+            fail = 1;
+            atomicExch(p.err, 1);
+            continue;
+        }
+        if (active) {
+            SmemSrc<TX, TY> src;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) src.pj[j] = cell + ((2 * i + j) % kRing) * G::kSlot;
+            cb_sites<NSH, 2, KIND, MASTER>(p, src, k, x, y, zs + 2 * i);
+        }
+    }
+    __syncthreads();
+    if (fail && t == 0) {
+        // a wait ran out: let the copies still in flight land (each wait bounded too)
+        // before the CTA's shared memory is given back
+        for (int u = issued - kRing < 0 ? 0 : issued - kRing; u < issued; ++u)
+            tc::mbar_wait(&full[u % kRing], (u / kRing) & 1);
+    }
 }
 
 // Conversions between the generic FP64 state (s.e / s.eM, [k][i] reference order)
@@ -694,12 +813,25 @@ __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, d
 struct StructuredFast {
     SParams p{};
     int nshell = 0, master = 1, lc = 0;
-    int kernel = 1;  // compiled sizes: 0 one sublattice per thread (stencil_zblock), 1 both (stencil_cells)
+    // compiled sizes: 0 one sublattice per thread (stencil_zblock), 1 both sublattices
+    // (stencil_cells), 2 both sublattices from TMA-staged planes (stencil_tma)
+    int kernel = 2;
+    CUtensorMap map_mt, map_mp;  // 5-D maps of the padded mirrors (kernel 2)
     dim3 grid, block;
     int8_t *species = nullptr;
     // what the thermal amplitude and the rotation scale are computed from
     double lam = 0.0, temp = 0.0, delta_t = 0.0, temprescale = 1.0, mom[2] = {1.0, 1.0};
 };
+
+// 5-D TMA map over a padded mirror array: (float lane, x, y, z, ensemble x sublattice)
+// with the box of one plane of a TX x TY tile plus its three-cell halo.
+static int mirror_map(CUtensorMap *m, const StructuredFast *f, const float4 *base, int tx, int ty) {
+    const SParams &p = f->p;
+    const uint64_t dims[5] = {4, (uint64_t)p.P1, (uint64_t)p.L2 + 4, (uint64_t)p.L3 + 4, (uint64_t)2 * p.nens};
+    const uint64_t strides[4] = {16, (uint64_t)p.P1 * 16, (uint64_t)p.P2 * 16, (uint64_t)p.pbox * 16};
+    const uint32_t box[5] = {4, (uint32_t)tx + 3, (uint32_t)ty + 3, 1, 1};
+    return tc::encode_tiled(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 5, base, dims, strides, box);
+}
 
 // Depondt thermal amplitude per species (depondt.f90:143-145) and rotation scale from the
 // uniform damping and temperature and the simulation's physical constants; again after
@@ -732,7 +864,7 @@ void structured_refresh(Sim &s) {
 static void fast_free(StructuredFast *f) {
     if (!f) return;
     void *ptrs[] = {f->p.mt, f->p.mp, f->p.b2x, f->p.b2y, f->p.b2z, f->p.lox, f->p.loy, f->p.loz,
-                    f->p.mx, f->p.my, f->p.mz, f->species};
+                    f->p.mx, f->p.my, f->p.mz, f->species, f->p.err};
     for (void *q : ptrs) cudaFree(q);
     delete f;
 }
@@ -871,6 +1003,8 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
         al((void **)&p.loz, n * sizeof(float));
     }
     al((void **)&f->species, N);
+    al((void **)&p.err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p.err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(f->species, sp.data(), N, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         fast_free(f);
@@ -885,6 +1019,17 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     const int by = std::max(1, 256 / bx);
     f->block = dim3(bx, by, 1);
     f->grid = dim3((unsigned)(((L2 + by - 1) / by) * L3), 2, (unsigned)M);
+    if (f->lc == 0 && f->kernel != 0) f->kernel = 0;  // runtime pitches: one sublattice per thread
+    if (f->kernel == 2) {
+        const int tx = f->lc == 100 ? TmaTile<100>::TX : (f->lc == 64 ? TmaTile<64>::TX : TmaTile<6>::TX);
+        const int ty = f->lc == 100 ? TmaTile<100>::TY : (f->lc == 64 ? TmaTile<64>::TY : TmaTile<6>::TY);
+        int rc = mirror_map(&f->map_mt, f, p.mt, tx, ty);
+        if (!rc) rc = mirror_map(&f->map_mp, f, p.mp, tx, ty);
+        if (rc) {
+            fast_free(f);
+            return rc;
+        }
+    }
     s.fast = f;
     return UPPASD_GPU_OK;
 }
@@ -901,11 +1046,49 @@ int structured_load_state(Sim &s) {
 int structured_sync_state(Sim &s) {
     square_mirror_stale(s);
     StructuredFast *f = s.fast;
+    {
+        // a plane wait of the staged kernels that ran past its limit (reset once reported)
+        int herr = 0;
+        UPPASD_CUDA_TRY(cudaMemcpyAsync(&herr, f->p.err, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+        UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+        if (herr) {
+            UPPASD_CUDA_TRY(cudaMemsetAsync(f->p.err, 0, sizeof(int), s.stream));
+            set_error("structured LLG: a TMA plane wait ran past its limit");
+            return UPPASD_GPU_ESTATE;
+        }
+    }
     long long total = f->p.nsite * f->p.nens;
     from_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y,
                                                                            s.eM.z, s.llg.mmom, f->master);
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
+}
+
+template <int NSH, int LC, int KIND, int MASTER>
+static void launch_tma_kernel(StructuredFast *f, cudaStream_t st) {
+    using T = TmaTile<LC>;
+    using G = TileGeom<T::TX, T::TY>;
+    auto kern = stencil_tma<NSH, LC, T::TX, T::TY, T::ZC, KIND, MASTER>;
+    static bool attr = false;  // per instantiation
+    if (!attr) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem) != cudaSuccess)
+            return;  // the launch below then fails and the step reports it
+        attr = true;
+    }
+    const int ntx = (LC + T::TX - 1) / T::TX, nty = (LC + T::TY - 1) / T::TY;
+    const dim3 g((unsigned)(ntx * nty * (LC / T::ZC)), 1, (unsigned)f->p.nens);
+    kern<<<g, T::TX * T::TY, G::kSmem, st>>>(KIND == 0 ? f->map_mt : f->map_mp, f->p, ntx, nty);
+}
+
+template <int NSH, int LC>
+static void launch_tma(StructuredFast *f, cudaStream_t st, int phase) {
+    if constexpr (LC != 0) {
+        if (phase & 1) launch_tma_kernel<NSH, LC, 0, 2>(f, st);
+        if (phase & 2) {
+            if (f->master == 1) launch_tma_kernel<NSH, LC, 1, 1>(f, st);
+            else launch_tma_kernel<NSH, LC, 1, 2>(f, st);
+        }
+    }
 }
 
 template <int NSH, int LC>
@@ -918,6 +1101,10 @@ static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
         constexpr int NZP = 2;
         constexpr int NZC = 2;
         const unsigned nyt = (unsigned)((f->p.L2 + f->block.y - 1) / f->block.y);
+        if (f->kernel == 2) {
+            launch_tma<NSH, LC>(f, st, phase);
+            return;
+        }
         if (f->kernel == 1) {
             const dim3 g(nyt * (LC / 2), 1, (unsigned)f->p.nens);
             if (phase & 1) stencil_cells<NSH, 2, LC, 0, 2><<<g, f->block, 0, st>>>(f->p);

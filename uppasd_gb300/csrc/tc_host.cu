@@ -57,6 +57,42 @@ int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows) 
     return UPPASD_GPU_OK;
 }
 
+int encode_tiled(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, int rank, const void *ptr,
+                 const uint64_t *dims, const uint64_t *strides, const uint32_t *box) {
+    int rc = encode_fn();
+    if (rc) return rc;
+    if (rank < 1 || rank > 5 || (reinterpret_cast<uintptr_t>(ptr) & 15) || ((uint64_t)box[0] * elem_bytes) % 16) {
+        set_error("tensor map: rank 1..5, 16-byte aligned base and inner box a multiple of 16 bytes");
+        return UPPASD_GPU_EINVAL;
+    }
+    cuuint64_t d[5], st[4];
+    cuuint32_t b[5], es[5];
+    for (int i = 0; i < rank; ++i) {
+        d[i] = dims[i];
+        b[i] = box[i];
+        es[i] = 1;
+        if (box[i] < 1 || box[i] > 256) {
+            set_error("tensor map: box extents must be 1..256");
+            return UPPASD_GPU_EINVAL;
+        }
+    }
+    for (int i = 0; i + 1 < rank; ++i) {
+        st[i] = strides[i];
+        if (strides[i] % 16) {
+            set_error("tensor map: strides must be multiples of 16 bytes");
+            return UPPASD_GPU_EINVAL;
+        }
+    }
+    CUresult r = g_encode(m, dt, (cuuint32_t)rank, const_cast<void *>(ptr), d, st, b, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                          CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed with " + std::to_string((int)r));
+        return UPPASD_GPU_ECUDA;
+    }
+    return UPPASD_GPU_OK;
+}
+
 namespace {
 
 template <int BN, int EPI, int ST>

@@ -20,6 +20,11 @@ int gemm_prepare(Gemm &op, const __nv_bfloat16 *A, const __nv_bfloat16 *B, int M
 // 2-D bf16 TMA map over a rows x cols row-major matrix (box 64 columns x box_rows,
 // 128-byte swizzle); checks base alignment and row pitch.
 int make_map(CUtensorMap *m, const void *ptr, int rows, int cols, int box_rows);
+// Any tiled TMA map (no interleave, no swizzle, L2 promotion 128 B, out-of-range
+// elements filled with zeros): rank <= 5, dims / box innermost first, strides in bytes
+// of dims 1 .. rank-1.  Checks the 16-byte rules on the base, strides and inner box.
+int encode_tiled(CUtensorMap *m, CUtensorMapDataType dt, int elem_bytes, int rank, const void *ptr,
+                 const uint64_t *dims, const uint64_t *strides, const uint32_t *box);
 // Launch on `st` (capturable).  Outputs/extra operands by epilogue (see tc_gemm.cuh).
 int gemm_run(const Gemm &op, const float *bias, const __nv_bfloat16 *Y, float *Cf, __nv_bfloat16 *Cb, int *err,
              cudaStream_t st);
