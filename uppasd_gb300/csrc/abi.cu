@@ -37,6 +37,7 @@ int mixed_step(Sim &s, int64_t step_offset, int phase);
 int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak = nullptr);
 int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps);
 int mixed_coefficients(Sim &s);
+void mixed_temperature(Sim &s, const double *temp_array);
 
 namespace {
 
@@ -625,6 +626,10 @@ int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
         int rc = uppasd::structured_set_temperature(s, temp_array);
         if (rc) return rc;
         uppasd::drop_graph(s);
+    }
+    if (s.precision == 3) {
+        uppasd::mixed_temperature(s, temp_array);
+        uppasd::drop_graph(s);  // the uniform temperature is a step argument, captured by value
     }
     UPPASD_CUDA_TRY(cudaMemcpyAsync(s.llg.temp, temp_array, sizeof(double) * s.ham.natom, cudaMemcpyHostToDevice,
                                     s.stream));

@@ -14,6 +14,45 @@
 
 namespace uppasd {
 
+// What a site's field needs besides the spins: its coupling row, list sizes, anisotropy
+// row and type, and where its neighbour indices come from (the class tables, with
+// offsets from i, or the caller's per-site lists, slot-major, absolute).
+struct SiteView {
+    int ih, nn, nd, ta, ar, base;
+    const int32_t *nb, *dl;
+    size_t nbs, dls;
+    __device__ __forceinline__ int nbr(int s) const { return base + __ldg(&nb[s * nbs]); }
+    __device__ __forceinline__ int dmn(int s) const { return base + __ldg(&dl[s * dls]); }
+};
+
+__device__ __forceinline__ SiteView site_view(const HamDev &h, const MixedDev &c, int i) {
+    SiteView v;
+    if (c.ncls) {
+        const int cl = __ldg(&c.cls[i]);
+        const int4 ci = __ldg(&c.cinfo[cl]);
+        v.nn = ci.x & 0xffff;
+        v.nd = (int)((unsigned)ci.x >> 16);
+        v.ih = ci.y;
+        v.ar = ci.z;
+        v.ta = ci.w;
+        v.nb = c.cnb + (size_t)cl * h.mnn;
+        v.dl = c.cdm + (size_t)cl * h.mnn_dm;
+        v.nbs = v.dls = 1;
+        v.base = i;
+    } else {
+        v.ih = __ldg(&c.row[i]);
+        v.nn = h.nsize[i];
+        v.nd = h.do_dm ? h.dmsize[i] : 0;
+        v.ta = h.do_aniso ? h.taniso[i] : 0;
+        v.ar = h.do_aniso ? __ldg(&c.arow[i]) : 0;
+        v.nb = h.nlist + i;
+        v.dl = h.dmlist + i;
+        v.nbs = v.dls = (size_t)h.natom;
+        v.base = 0;
+    }
+    return v;
+}
+
 // FP32 effective field of site i from full moments m.w * m.xyz, in the FP64 field's
 // term order (exchange or tensor, DMI, anisotropy, Zeeman), with the couplings from
 // the FP32 copies in MixedDev.
@@ -21,12 +60,13 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
                                           float B[3]) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
-    const int ih = __ldg(&c.row[i]);
-    const int nn = h.nsize[i];
+    const SiteView sv = site_view(h, c, i);
+    const int ih = sv.ih;
+    const int nn = sv.nn;
     float bs[3] = {0.f, 0.f, 0.f}, bq[3] = {0.f, 0.f, 0.f};
     if (h.do_jtensor) {
         for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const int j = sv.nbr(s);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
             const float *J = c.jt + ((size_t)s * c.nrow + ih) * 9;
@@ -36,7 +76,7 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
         }
     } else {
         for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const int j = sv.nbr(s);
             const float4 v = m[off + j];
             const float cj = __ldg(&c.nc[(size_t)s * c.nrow + ih]) * v.w;
             bs[0] = fmaf(cj, v.x, bs[0]);
@@ -45,9 +85,9 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
         }
     }
     if (h.do_dm) {
-        const int nd = h.dmsize[i];
+        const int nd = sv.nd;
         for (int s = 0; s < nd; ++s) {
-            const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
+            const int j = sv.dmn(s);
             const float4 d = __ldg(&c.dm[(size_t)s * c.nrow + ih]);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
@@ -59,8 +99,8 @@ __device__ __forceinline__ void field_f32(const HamDev &h, const MixedDev &c, co
     if (h.do_aniso) {
         const float4 me = m[off + i];
         const float m1 = me.w * me.x, m2 = me.w * me.y, m3 = me.w * me.z;
-        const int ta = h.taniso[i];
-        const int ar = __ldg(&c.arow[i]);
+        const int ta = sv.ta;
+        const int ar = sv.ar;
         const float4 an = __ldg(&c.an[ar]);
         const float2 an2 = __ldg(&c.an2[ar]);
         const float e0 = an.x, e1 = an.y, e2 = an.z, ka0 = an.w, ka1 = an2.x;
@@ -96,7 +136,8 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
                                                   const float nm[3]) {
     const int N = h.natom;
     const size_t off = (size_t)k * N;
-    const int ih = __ldg(&c.row[i]);
+    const SiteView sv = site_view(h, c, i);
+    const int ih = sv.ih;
     const float4 me = m[off + i];
     const float mm = me.w;
     const float ei[3] = {me.x, me.y, me.z};
@@ -104,10 +145,10 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
     const float tm[3] = {mm * nm[0], mm * nm[1], mm * nm[2]};
     const float dm[3] = {tm[0] - mi[0], tm[1] - mi[1], tm[2] - mi[2]};
     float b[3] = {0.f, 0.f, 0.f};
-    const int nn = h.nsize[i];
+    const int nn = sv.nn;
     if (h.do_jtensor) {
         for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const int j = sv.nbr(s);
             const float4 v = m[off + j];
             const float m1 = v.w * v.x, m2 = v.w * v.y, m3 = v.w * v.z;
             const float *J = c.jt + ((size_t)s * c.nrow + ih) * 9;
@@ -117,7 +158,7 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
         }
     } else {
         for (int s = 0; s < nn; ++s) {
-            const int j = __ldg(&h.nlist[(size_t)s * N + i]);
+            const int j = sv.nbr(s);
             const float4 v = m[off + j];
             const float cj = __ldg(&c.nc[(size_t)s * c.nrow + ih]) * v.w;
             b[0] = fmaf(cj, v.x, b[0]);
@@ -128,9 +169,9 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
     // bilinear exchange: E_t - E_c = -(t - m_i) . b
     float de = -(dm[0] * b[0] + dm[1] * b[1] + dm[2] * b[2]);
     if (h.do_dm) {
-        const int nd = h.dmsize[i];
+        const int nd = sv.nd;
         for (int s = 0; s < nd; ++s) {
-            const int j = __ldg(&h.dmlist[(size_t)s * N + i]);
+            const int j = sv.dmn(s);
             const float4 d = __ldg(&c.dm[(size_t)s * c.nrow + ih]);
             const float4 v = m[off + j];
             const float mj0 = v.w * v.x, mj1 = v.w * v.y, mj2 = v.w * v.z;
@@ -142,8 +183,8 @@ __device__ __forceinline__ float delta_energy_f32(const HamDev &h, const MixedDe
         }
     }
     if (h.do_aniso) {
-        const int ta = h.taniso[i];
-        const int ar = __ldg(&c.arow[i]);
+        const int ta = sv.ta;
+        const int ar = sv.ar;
         const float4 an = __ldg(&c.an[ar]);
         const float2 an2 = __ldg(&c.an2[ar]);
         const float ka0 = an.w, ka1 = an2.x;

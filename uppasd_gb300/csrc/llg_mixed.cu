@@ -18,6 +18,7 @@
 #include <type_traits>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <vector>
 
 #include "common.cuh"
@@ -225,7 +226,7 @@ __device__ __forceinline__ void noise_f32(const MixArgs &a, int i, int k, int64_
         z[1] = (float)zd[1];
         z[2] = (float)zd[2];
     }
-    const float T = (float)a.temp[i] * a.temprescale;
+    const float T = (a.c.uni_T ? a.c.T_u : (float)a.temp[i]) * a.temprescale;
     float sigma;
     if (ALG == 5 || ALG == 11) sigma = sqrtf(a.c_dp * lam * T / mm);
     else if (ALG == 4) sigma = sqrtf(2.0f * (a.c_heun * lam / (1.0f + lam * lam)) * T / mm);
@@ -248,7 +249,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
     const float4 me = a.c.mt[o];
     const float e[3] = {me.x, me.y, me.z};
     if (a.perp) perp_f32(B, e);
-    const float lam = (float)a.lambda[i], mm = me.w;
+    const float lam = (a.c.uni_lam ? a.c.lam_u : (float)a.lambda[i]), mm = me.w;
     float r[3];
     noise_f32<ALG>(a, i, k, step, lam, mm, r);
     float p[3];
@@ -272,7 +273,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         a.c.b2y[o] = bd[1];
         a.c.b2z[o] = bd[2];
     } else if (ALG == 4) {
-        const float g = (float)a.landeg[i];
+        const float g = (a.c.uni_g ? a.c.g_u : (float)a.landeg[i]);
         const float dtg = a.dt_dep * g / (1.0f + lam * lam);
         const float dw[3] = {r[0] * g, r[1] * g, r[2] * g};
         float ah[3], bm[9];
@@ -285,7 +286,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
         a.c.b2z[o] = B[2];
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
-        const float g = (float)a.landeg[i];
+        const float g = (a.c.uni_g ? a.c.g_u : (float)a.landeg[i]);
         const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
         float et[3];
         if (ALG == 7) {
@@ -326,7 +327,7 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     const float e[3] = {me.x, me.y, me.z}, pr[3] = {mpv.x, mpv.y, mpv.z};
     // emom at the second half-step: m(t) for midpoint and SIB, the predictor otherwise
     if (a.perp) perp_f32(B, (ALG == 1 || ALG == 6 || ALG == 7) ? e : pr);
-    const float lam = (float)a.lambda[i], mm = me.w;
+    const float lam = (a.c.uni_lam ? a.c.lam_u : (float)a.lambda[i]), mm = me.w;
     float r[3];
     noise_f32<ALG>(a, i, k, step, lam, mm, r);
     float out[3];
@@ -350,7 +351,7 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         llgi_f32(lam, a.tau_dt, a.dtg_llgi, et, e, bd, out);
         unit = true;
     } else if (ALG == 4) {
-        const float g = (float)a.landeg[i];
+        const float g = (a.c.uni_g ? a.c.g_u : (float)a.landeg[i]);
         const float dtg = a.dt_dep * g / (1.0f + lam * lam);
         const float dw[3] = {r[0] * g, r[1] * g, r[2] * g};
         const float h2[3] = {a.c.b2x[o], a.c.b2y[o], a.c.b2z[o]};
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         unit = true;
     } else {
         const float dt = a.dt_mid / (1.0f + lam * lam);
-        const float g = (float)a.landeg[i];
+        const float g = (a.c.uni_g ? a.c.g_u : (float)a.landeg[i]);
         const float dtg = dt * g, sqrtdtg = sqrtf(dt) * g;
         if (ALG == 1) {
             float A[3];
@@ -394,7 +395,7 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     e0 *= sc;
     e1 *= sc;
     e2 *= sc;
-    const double mmd = a.mmom[o];
+    const double mmd = a.c.uni_m ? a.c.mmom_u : a.mmom[o];
     a.e.x[o] = e0;
     a.e.y[o] = e1;
     a.e.z[o] = e2;
@@ -432,7 +433,7 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec
     y *= sc;
     z *= sc;
     mt[o] = make_float4((float)x, (float)y, (float)z, mm);
-    const double md = mmom[o];
+    const double md = c.uni_m ? c.mmom_u : mmom[o];
     e.x[o] = x;
     e.y[o] = y;
     e.z[o] = z;
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, Ve
     y *= sc;
     z *= sc;
     mt[o] = make_float4((float)x, (float)y, (float)z, cur.w);
-    const double md = mmom[o];
+    const double md = c.uni_m ? c.mmom_u : mmom[o];
     e.x[o] = x;
     e.y[o] = y;
     e.z[o] = z;
@@ -522,6 +523,9 @@ bool store(T **d, const std::vector<T> &h) {
            cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
 }
 }  // namespace
+
+bool mixed_site_classes(Sim &s, const std::vector<int32_t> &row);
+bool mixed_uniforms(Sim &s);
 
 // (Re)builds the FP32 copies of the couplings from the FP64 Hamiltonian on the device,
 // one row per distinct coupling row (compared bit for bit in FP32) and one anisotropy
@@ -622,11 +626,115 @@ int mixed_coefficients(Sim &s) {
         if (uniform) v.resize(1);
         ok = ok && store(&m.ext, v);
     }
+    if (ok) ok = mixed_site_classes(s, row) && mixed_uniforms(s);
     if (!ok) {
         set_error("precision 3: copying the couplings to FP32 failed");
         return UPPASD_GPU_ECUDA;
     }
     return UPPASD_GPU_OK;
+}
+
+// Site classes (see MixedDev): the key of site i is its coupling row, anisotropy row and
+// type, list sizes and neighbour offsets j - i.  Kept only when there are at most
+// natom / 4 classes (else the per-site lists are the smaller form).
+bool mixed_site_classes(Sim &s, const std::vector<int32_t> &row) {
+    const HamDev &h = s.ham;
+    MixedDev &m = s.mix;
+    const size_t N = h.natom, mnn = h.mnn, mdm = h.do_dm ? h.mnn_dm : 0;
+    std::vector<int32_t> nl, ns, dl, ds, ta, ar;
+    bool ok = fetch(nl, h.nlist, mnn * N) && fetch(ns, h.nsize, N);
+    if (ok && h.do_dm) ok = fetch(dl, h.dmlist, mdm * N) && fetch(ds, h.dmsize, N);
+    if (ok && h.do_aniso) ok = fetch(ta, h.taniso, N) && fetch(ar, m.arow, N);
+    if (!ok) return false;
+    std::vector<int32_t> keys;      // the classes' keys back to back
+    const size_t width = 5 + mnn + mdm;
+    std::unordered_map<uint64_t, std::vector<int>> byhash;
+    std::vector<int32_t> cls(N), key(width);
+    size_t ncls = 0;
+    const size_t cap = std::max<size_t>(1, N / 4);
+    for (size_t i = 0; i < N; ++i) {
+        std::fill(key.begin(), key.end(), 0);
+        const int nn = ns[i], nd = h.do_dm ? ds[i] : 0;
+        key[0] = row[i];
+        key[1] = h.do_aniso ? ar[i] : 0;
+        key[2] = h.do_aniso ? ta[i] : 0;
+        key[3] = nn;
+        key[4] = nd;
+        for (int q = 0; q < nn; ++q) key[5 + q] = nl[(size_t)q * N + i] - (int32_t)i;
+        for (int q = 0; q < nd; ++q) key[5 + mnn + q] = dl[(size_t)q * N + i] - (int32_t)i;
+        uint64_t hsh = 1469598103934665603ull;  // FNV-1a over the key words
+        for (int32_t w : key) {
+            hsh ^= (uint32_t)w;
+            hsh *= 1099511628211ull;
+        }
+        std::vector<int> &cand = byhash[hsh];
+        int id = -1;
+        for (int c : cand)
+            if (std::equal(key.begin(), key.end(), keys.begin() + (size_t)c * width)) {
+                id = c;
+                break;
+            }
+        if (id < 0) {
+            if (ncls == cap) {
+                // too many distinct sites: keep reading the per-site lists
+                for (void *q : {(void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm}) cudaFree(q);
+                m.cls = nullptr;
+                m.cinfo = nullptr;
+                m.cnb = m.cdm = nullptr;
+                m.ncls = 0;
+                return true;
+            }
+            id = (int)ncls++;
+            cand.push_back(id);
+            keys.insert(keys.end(), key.begin(), key.end());
+        }
+        cls[i] = id;
+    }
+    std::vector<int4> info(ncls);
+    std::vector<int32_t> cnb(ncls * std::max<size_t>(mnn, 1)), cdm(ncls * std::max<size_t>(mdm, 1));
+    for (size_t c = 0; c < ncls; ++c) {
+        const int32_t *k = keys.data() + c * width;
+        info[c] = make_int4(k[3] | (k[4] << 16), k[0], k[1], k[2]);
+        for (size_t q = 0; q < mnn; ++q) cnb[c * mnn + q] = k[5 + q];
+        for (size_t q = 0; q < mdm; ++q) cdm[c * mdm + q] = k[5 + mnn + q];
+    }
+    ok = store(&m.cls, cls) && store(&m.cinfo, info) && store(&m.cnb, cnb) && store(&m.cdm, cdm);
+    m.ncls = ok ? (int)ncls : 0;
+    return ok;
+}
+
+// Damping, Lande factor, temperature and moment passed as scalars when they are the
+// same for every site (and ensemble); again after set_temperature.
+bool mixed_uniforms(Sim &s) {
+    const HamDev &h = s.ham;
+    MixedDev &m = s.mix;
+    const size_t N = h.natom, M = h.mensemble;
+    std::vector<double> v;
+    auto uniform = [&](const double *d, size_t n, int &flag, double &val) {
+        if (!fetch(v, d, n)) return false;
+        flag = 1;
+        for (size_t q = 1; q < n && flag; ++q) flag = v[q] == v[0];
+        val = v.empty() ? 0.0 : v[0];
+        return true;
+    };
+    double lam, g, T, mm;
+    if (!(uniform(s.llg.lambda, N, m.uni_lam, lam) && uniform(s.llg.landeg, N, m.uni_g, g) &&
+          uniform(s.llg.temp, N, m.uni_T, T) && uniform(s.llg.mmom, N * M, m.uni_m, mm)))
+        return false;
+    m.lam_u = (float)lam;
+    m.g_u = (float)g;
+    m.T_u = (float)T;
+    m.mmom_u = mm;
+    return true;
+}
+
+// set_temperature on precision 3: the uniform-temperature scalar follows the new array.
+void mixed_temperature(Sim &s, const double *temp_array) {
+    MixedDev &m = s.mix;
+    const int N = s.ham.natom;
+    m.uni_T = 1;
+    for (int i = 1; i < N && m.uni_T; ++i) m.uni_T = temp_array[i] == temp_array[0];
+    m.T_u = (float)temp_array[0];
 }
 
 int mixed_init(Sim &s) {
@@ -654,7 +762,7 @@ void mixed_free(Sim &s) {
     MixedDev &m = s.mix;
     for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
                     (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext, (void *)m.row,
-                    (void *)m.arow})
+                    (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm})
         cudaFree(q);
     m = MixedDev{};
 }

@@ -83,6 +83,20 @@ struct MixedDev {
     float2 *an2 = nullptr;   // [distinct anisotropy rows] (k2, sb)
     float4 *ext = nullptr;   // [mensemble][natom] (Bx, By, Bz, 0), or one entry when uniform
     int ext_uniform = 0;     // every spin sees ext[0]
+    // Site classes: sites with the same coupling row, anisotropy row and type, list sizes
+    // and neighbour offsets j - i share one class, so a site reads one 4-byte class id
+    // instead of its neighbour and DM lists, sizes and rows (a translation-invariant
+    // lattice has a handful of classes: the interior and its periodic edges).  ncls = 0:
+    // too many distinct sites, the per-site lists are read.
+    int ncls = 0;
+    int32_t *cls = nullptr;    // [natom] class of site i
+    int4 *cinfo = nullptr;     // [ncls] (nn | nd << 16, coupling row, anisotropy row, anisotropy type)
+    int32_t *cnb = nullptr;    // [ncls][mnn] exchange neighbour offsets j - i
+    int32_t *cdm = nullptr;    // [ncls][mnn_dm] DM neighbour offsets j - i
+    // per-site parameters that are the same everywhere are passed as scalars
+    int uni_lam = 0, uni_g = 0, uni_T = 0, uni_m = 0;
+    float lam_u = 0.f, g_u = 0.f, T_u = 0.f;
+    double mmom_u = 0.0;       // moment of every (ensemble, site) when uni_m
 };
 
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
