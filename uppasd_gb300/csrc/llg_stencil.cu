@@ -292,24 +292,52 @@ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
 
 // Corrector update of one site from the field B at the predictor: Depondt
 // average with b2eff, rotation of m(t), master update and renormalisation.
+// What the corrector of one site reads besides the gather: m(t) (the mirror), the
+// predictor's stored field, and the master (FP64, or the double-single residual).
+// Loaded before the gather so that these DRAM reads overlap it.
+template <int MASTER>
+struct CorrIn {
+    float4 mt;
+    float b2[3];
+    float lo[3];    // MASTER 2
+    double m[3];    // MASTER 1
+};
+
+template <int MASTER>
+__device__ __forceinline__ void correct_load(const SParams &p, int k, int b, int x, int y, int z, CorrIn<MASTER> &c) {
+    const long long u = uidx(p, k, b, x, y, z);
+    c.mt = p.mt[pidx(p, k, b, x, y, z)];
+    c.b2[0] = p.b2x[u];
+    c.b2[1] = p.b2y[u];
+    c.b2[2] = p.b2z[u];
+    if constexpr (MASTER == 1) {
+        c.m[0] = p.mx[u];
+        c.m[1] = p.my[u];
+        c.m[2] = p.mz[u];
+    } else {
+        c.lo[0] = p.lox[u];
+        c.lo[1] = p.loy[u];
+        c.lo[2] = p.loz[u];
+    }
+}
+
 template <int MASTER>  // MASTER 1: FP64, 2: double-single
-__device__ __forceinline__ void correct_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &mp,
-                                               const float B[3]) {
-    const long long o = pidx(p, k, b, x, y, z);
+__device__ __forceinline__ void correct_finish(const SParams &p, int k, int b, int x, int y, int z, const float4 &mp,
+                                               const float B[3], const CorrIn<MASTER> &ci) {
     const long long u = uidx(p, k, b, x, y, z);
     const float ep[3] = {mp.x, mp.y, mp.z};
     float bd[3];
     depondt_bdup(p.lam, ep, B, bd);   // the thermal term is in b2 (predict_update)
-    bd[0] = 0.5f * bd[0] + 0.5f * p.b2x[u];
-    bd[1] = 0.5f * bd[1] + 0.5f * p.b2y[u];
-    bd[2] = 0.5f * bd[2] + 0.5f * p.b2z[u];
-    const float4 mt = p.mt[o];
+    bd[0] = 0.5f * bd[0] + 0.5f * ci.b2[0];
+    bd[1] = 0.5f * bd[1] + 0.5f * ci.b2[1];
+    bd[2] = 0.5f * bd[2] + 0.5f * ci.b2[2];
+    const float4 mt = ci.mt;
     const float eh[3] = {mt.x, mt.y, mt.z};
     float d[3];
     rotation_delta(bd, eh, p.dtg, d);
     float4 out;
     if (MASTER == 1) {
-        double e0 = p.mx[u] + (double)d[0], e1 = p.my[u] + (double)d[1], e2 = p.mz[u] + (double)d[2];
+        double e0 = ci.m[0] + (double)d[0], e1 = ci.m[1] + (double)d[1], e2 = ci.m[2] + (double)d[2];
         double n2 = fma(e2, e2, fma(e1, e1, e0 * e0));
         double xx = n2 - 1.0;
         double sc = fma(xx, fma(0.375, xx, -0.5), 1.0);  // 1/sqrt(1+x) to second order, |x| ~ 1e-7
@@ -321,7 +349,7 @@ __device__ __forceinline__ void correct_update(const SParams &p, int k, int b, i
         p.mz[u] = e2;
         out = make_float4((float)e0, (float)e1, (float)e2, mt.w);
     } else {
-        float lo[3] = {p.lox[u], p.loy[u], p.loz[u]};
+        float lo[3] = {ci.lo[0], ci.lo[1], ci.lo[2]};
         float hi[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -356,6 +384,14 @@ __device__ __forceinline__ void correct_update(const SParams &p, int k, int b, i
         out = make_float4(hi[0], hi[1], hi[2], mt.w);
     }
     store_mirror(p, p.mt, k, b, x, y, z, out);
+}
+
+template <int MASTER>
+__device__ __forceinline__ void correct_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &mp,
+                                               const float B[3]) {
+    CorrIn<MASTER> ci;
+    correct_load<MASTER>(p, k, b, x, y, z, ci);
+    correct_finish<MASTER>(p, k, b, x, y, z, mp, B, ci);
 }
 
 template <int NSH, int MASTER, int b, int LC>
@@ -586,6 +622,14 @@ template <int NSH, int NZ, int KIND, int MASTER, class Src>
 __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k, int x, int y, int z0) {
     float4 me[2 * NZ];
     float cA[2 * NZ][4], cD[2 * NZ][4], acc[2 * NZ][3];
+    CorrIn<MASTER == 1 ? 1 : 2> ci[KIND == 1 ? 2 * NZ : 1];
+    if constexpr (KIND == 1) {
+        // the corrector's own-site DRAM reads first: they overlap the gather
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int q = 0; q < NZ; ++q) correct_load<MASTER == 1 ? 1 : 2>(p, k, b, x, y, z0 + q, ci[b * NZ + q]);
+    }
     cb_own<NZ>(src, me, std::make_integer_sequence<int, 2 * NZ>{});
 #pragma unroll
     for (int b = 0; b < 2; ++b)
@@ -607,8 +651,8 @@ __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k
         for (int q = 0; q < NZ; ++q) {
             const int i = b * NZ + q;
             const float Bf[3] = {acc[i][0] + p.ext[0], acc[i][1] + p.ext[1], acc[i][2] + p.ext[2]};
-            if (KIND == 0) predict_update(p, k, b, x, y, z0 + q, me[i], Bf);
-            else correct_update<MASTER>(p, k, b, x, y, z0 + q, me[i], Bf);
+            if constexpr (KIND == 0) predict_update(p, k, b, x, y, z0 + q, me[i], Bf);
+            else correct_finish<MASTER == 1 ? 1 : 2>(p, k, b, x, y, z0 + q, me[i], Bf, ci[i]);
         }
 }
 
