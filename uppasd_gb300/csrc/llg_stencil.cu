@@ -192,8 +192,11 @@ __device__ __forceinline__ void depondt_bdup(float lam, const float e[3], const 
 // Rodrigues rotation increment: R e - e = (1-cos v)[(h.e)h - e] + sin v (h x e),
 // with h = bdup/|bdup| and v = |bdup| dt gama/(1+lambda^2)  (depondt.f90:156-179).
 __device__ __forceinline__ void rotation_delta(const float bd[3], const float e[3], float dtg, float d[3]) {
-    float bn = sqrtf(bd[0] * bd[0] + bd[1] * bd[1] + bd[2] * bd[2]) + 1e-15f;
-    float inv = 1.0f / bn;
+    // |bd| and 1/|bd| from one reciprocal square root; the tiny addend keeps a zero field
+    // at zero rotation, as the reference's + 1e-15 on the norm does (depondt.f90:159)
+    const float n2 = bd[0] * bd[0] + bd[1] * bd[1] + bd[2] * bd[2];
+    const float inv = rsqrtf(n2 + 1e-30f);
+    const float bn = n2 * inv;
     float hx = bd[0] * inv, hy = bd[1] * inv, hz = bd[2] * inv;
     float v = bn * dtg;
     float sv, u;
@@ -685,36 +688,39 @@ __global__ void __launch_bounds__(256) stencil_cells(SParams p) {
 // iteration computes both sites of two planes of the tile (cb_sites) from shared
 // memory while the slots of the next iteration load; every neighbour is fetched from
 // DRAM / L2 once per tile instead of once per reading site.
-constexpr int kRing = 7;
-
-template <int TX, int TY>
+template <int TX, int TY, int R>
 struct TileGeom {
     static constexpr int BW = TX + 3, BH = TY + 3;
     static constexpr uint32_t kBox = (uint32_t)BW * BH * 16;          // bytes the TMA box moves
     static constexpr uint32_t kBoxA = (kBox + 127) / 128 * 128;       // box stride in shared memory
     static constexpr uint32_t kSlot = 2 * kBoxA;
-    static constexpr size_t kSmem = (size_t)kRing * kSlot + 128;      // + alignment slack
+    static constexpr size_t kSmem = (size_t)R * kSlot + 128;          // + alignment slack
 };
 
-// Tile geometry of the plane-staged kernels per compiled size: (TX, TY, ZC).
-template <int LC>
+// Tile geometry of the plane-staged kernels per compiled size: the tile (TX, TY), the
+// planes of a z chunk (ZC), the planes per iteration (NZ), the ring's slots (R) and the
+// CTAs per SM the registers are sized for (MINB).
+// V = 0: two planes per iteration, 7 slots, registers for 2 CTAs per SM; V = 1: one
+// plane, 5 slots, registers for 3 CTAs per SM (more warps, more reads per site).
+template <int LC, int V = 0>
 struct TmaTile {
     static constexpr int TX = LC == 100 ? 50 : (LC == 64 ? 32 : LC);
     static constexpr int TY = LC == 100 ? 5 : (LC == 64 ? 8 : LC);
     static constexpr int ZC = LC == 100 ? 20 : (LC == 64 ? 16 : LC);
+    static constexpr int NZ = V ? 1 : 2, R = V ? 5 : 7, MINB = V ? 3 : 2;
 };
 
-// Point source of the gather: this thread's cell in the five slots of the
-// current iteration (slot of plane z - 2 + j at pj[j]).
-template <int TX, int TY>
+// Point source of the gather: this thread's cell in the NZ + 3 slots of the current
+// iteration (slot of plane z - 2 + j at pj[j]).
+template <int TX, int TY, int NZ, int R>
 struct SmemSrc {
-    const uint8_t *pj[5];
+    const uint8_t *pj[NZ + 3];
     template <int BJ, int DX, int DY, int DZ>
     __device__ __forceinline__ float4 get() const {
-        using G = TileGeom<TX, TY>;
+        using G = TileGeom<TX, TY, R>;
         constexpr int j = DZ + 1 + BJ;
         constexpr int off = BJ * (int)G::kBoxA + 16 * ((DY + 1 + BJ) * G::BW + DX + 1 + BJ);
-        static_assert(j >= 0 && j < 5, "plane outside the iteration's slots");
+        static_assert(j >= 0 && j < NZ + 3, "plane outside the iteration's slots");
         return *reinterpret_cast<const float4 *>(pj[j] + off);
     }
 };
@@ -728,15 +734,19 @@ __device__ __forceinline__ void tma_load_5d(void *dst, const CUtensorMap *map, u
         : "memory");
 }
 
-template <int NSH, int LC, int TX, int TY, int ZC, int KIND, int MASTER>
-__global__ void __launch_bounds__(TX * TY, 2) stencil_tma(const __grid_constant__ CUtensorMap mapm, SParams p, int ntx,
-                                                       int nty) {
-    using G = TileGeom<TX, TY>;
-    static_assert(ZC % 2 == 0 && ZC >= 4, "two planes per iteration, at least two iterations");
+// Iteration i covers planes zs + NZ i .. + NZ - 1 and reads slots u = NZ i .. NZ i + NZ + 2;
+// slot u may be (re)filled once slot u - R is no longer read, i.e. u < NZ i + R at the
+// top of iteration i.
+template <int NSH, int LC, int TX, int TY, int ZC, int NZ, int R, int MINB, int KIND, int MASTER>
+__global__ void __launch_bounds__(TX * TY, MINB) stencil_tma(const __grid_constant__ CUtensorMap mapm, SParams p,
+                                                             int ntx, int nty) {
+    using G = TileGeom<TX, TY, R>;
+    static_assert(ZC % NZ == 0 && ZC / NZ >= 2, "whole iterations, at least two of them");
+    static_assert(R >= NZ + 4, "one slot of look-ahead at least");
     constexpr int kSlots = ZC + 3;  // pz = zs - 2 .. zs + ZC
     extern __shared__ uint8_t tma_smem_raw[];
     uint8_t *ring = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(tma_smem_raw) + 127) & ~(uintptr_t)127);
-    __shared__ __align__(8) uint64_t full[kRing];
+    __shared__ __align__(8) uint64_t full[R];
     __shared__ int fail;
     const int t = threadIdx.x;
     const int bid = blockIdx.x;
@@ -746,50 +756,50 @@ __global__ void __launch_bounds__(TX * TY, 2) stencil_tma(const __grid_constant_
     const int x = x0 + tx, y = y0 + ty;
     const bool active = x < p.L1 && y < p.L2;
     if (t == 0) {
-        for (int r = 0; r < kRing; ++r) tc::mbar_init(&full[r], 1);
+        for (int r = 0; r < R; ++r) tc::mbar_init(&full[r], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         fail = 0;
     }
     __syncthreads();
     // slot u: corner plane pz + 1 and centre plane pz, pz = zs - 2 + u, padded z = pz + 2
     auto issue = [&](int u) {
-        const int r = u % kRing, pz = zs - 2 + u;
+        const int r = u % R, pz = zs - 2 + u;
         uint8_t *dst = ring + r * G::kSlot;
         tc::mbar_expect_tx(&full[r], 2 * G::kBox);
         tma_load_5d(dst, &mapm, &full[r], 0, x0 - 1 + XOFF, y0 + 1, pz + 3, 2 * k);
         tma_load_5d(dst + G::kBoxA, &mapm, &full[r], 0, x0 - 2 + XOFF, y0, pz + 2, 2 * k + 1);
     };
     int issued = 0;  // slots issued so far (thread 0)
+    int waited = 0;  // slots this thread has seen complete
     if (t == 0)
-        for (; issued < kRing && issued < kSlots; ++issued) issue(issued);
+        for (; issued < R && issued < kSlots; ++issued) issue(issued);
     const uint8_t *cell = ring + 16 * (ty * G::BW + tx);
-    for (int i = 0; i < ZC / 2; ++i) {
+    for (int i = 0; i < ZC / NZ; ++i) {
         if (i > 0) {
             __syncthreads();  // the previous iteration's reads of its oldest slots are done
             if (fail) break;
             if (t == 0)
-                for (int u = 2 * i + 5; u <= 2 * i + 6 && u < kSlots; ++u, ++issued) issue(u);
+                for (; issued < kSlots && issued < NZ * i + R; ++issued) issue(issued);
         }
         bool ok = true;
-        for (int u = i == 0 ? 0 : 2 * i + 3; u <= 2 * i + 4; ++u) ok = ok && tc::mbar_wait(&full[u % kRing], (u / kRing) & 1);
+        for (; waited <= NZ * i + NZ + 2; ++waited) ok = ok && tc::mbar_wait(&full[waited % R], (waited / R) & 1);
         if (!ok) {
             fail = 1;
             atomicExch(p.err, 1);
             continue;
         }
         if (active) {
-            SmemSrc<TX, TY> src;
+            SmemSrc<TX, TY, NZ, R> src;
 #pragma unroll
-            for (int j = 0; j < 5; ++j) src.pj[j] = cell + ((2 * i + j) % kRing) * G::kSlot;
-            cb_sites<NSH, 2, KIND, MASTER>(p, src, k, x, y, zs + 2 * i);
+            for (int j = 0; j < NZ + 3; ++j) src.pj[j] = cell + ((NZ * i + j) % R) * G::kSlot;
+            cb_sites<NSH, NZ, KIND, MASTER>(p, src, k, x, y, zs + NZ * i);
         }
     }
     __syncthreads();
     if (fail && t == 0) {
         // a wait ran out: let the copies still in flight land (each wait bounded too)
         // before the CTA's shared memory is given back
-        for (int u = issued - kRing < 0 ? 0 : issued - kRing; u < issued; ++u)
-            tc::mbar_wait(&full[u % kRing], (u / kRing) & 1);
+        for (int u = issued - R < 0 ? 0 : issued - R; u < issued; ++u) tc::mbar_wait(&full[u % R], (u / R) & 1);
     }
 }
 
@@ -1064,7 +1074,7 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     f->block = dim3(bx, by, 1);
     f->grid = dim3((unsigned)(((L2 + by - 1) / by) * L3), 2, (unsigned)M);
     if (f->lc == 0 && f->kernel != 0) f->kernel = 0;  // runtime pitches: one sublattice per thread
-    if (f->kernel == 2) {
+    if (f->kernel >= 2) {
         const int tx = f->lc == 100 ? TmaTile<100>::TX : (f->lc == 64 ? TmaTile<64>::TX : TmaTile<6>::TX);
         const int ty = f->lc == 100 ? TmaTile<100>::TY : (f->lc == 64 ? TmaTile<64>::TY : TmaTile<6>::TY);
         int rc = mirror_map(&f->map_mt, f, p.mt, tx, ty);
@@ -1108,11 +1118,11 @@ int structured_sync_state(Sim &s) {
     return UPPASD_GPU_OK;
 }
 
-template <int NSH, int LC, int KIND, int MASTER>
+template <int NSH, int LC, int V, int KIND, int MASTER>
 static void launch_tma_kernel(StructuredFast *f, cudaStream_t st) {
-    using T = TmaTile<LC>;
-    using G = TileGeom<T::TX, T::TY>;
-    auto kern = stencil_tma<NSH, LC, T::TX, T::TY, T::ZC, KIND, MASTER>;
+    using T = TmaTile<LC, V>;
+    using G = TileGeom<T::TX, T::TY, T::R>;
+    auto kern = stencil_tma<NSH, LC, T::TX, T::TY, T::ZC, T::NZ, T::R, T::MINB, KIND, MASTER>;
     static bool attr = false;  // per instantiation
     if (!attr) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem) != cudaSuccess)
@@ -1124,14 +1134,20 @@ static void launch_tma_kernel(StructuredFast *f, cudaStream_t st) {
     kern<<<g, T::TX * T::TY, G::kSmem, st>>>(KIND == 0 ? f->map_mt : f->map_mp, f->p, ntx, nty);
 }
 
+template <int NSH, int LC, int V>
+static void launch_tma_v(StructuredFast *f, cudaStream_t st, int phase) {
+    if (phase & 1) launch_tma_kernel<NSH, LC, V, 0, 2>(f, st);
+    if (phase & 2) {
+        if (f->master == 1) launch_tma_kernel<NSH, LC, V, 1, 1>(f, st);
+        else launch_tma_kernel<NSH, LC, V, 1, 2>(f, st);
+    }
+}
+
 template <int NSH, int LC>
 static void launch_tma(StructuredFast *f, cudaStream_t st, int phase) {
     if constexpr (LC != 0) {
-        if (phase & 1) launch_tma_kernel<NSH, LC, 0, 2>(f, st);
-        if (phase & 2) {
-            if (f->master == 1) launch_tma_kernel<NSH, LC, 1, 1>(f, st);
-            else launch_tma_kernel<NSH, LC, 1, 2>(f, st);
-        }
+        if (f->kernel == 3) launch_tma_v<NSH, LC, 1>(f, st, phase);
+        else launch_tma_v<NSH, LC, 0>(f, st, phase);
     }
 }
 
@@ -1145,7 +1161,7 @@ static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
         constexpr int NZP = 2;
         constexpr int NZC = 2;
         const unsigned nyt = (unsigned)((f->p.L2 + f->block.y - 1) / f->block.y);
-        if (f->kernel == 2) {
+        if (f->kernel >= 2) {
             launch_tma<NSH, LC>(f, st, phase);
             return;
         }
