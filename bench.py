@@ -476,49 +476,90 @@ def run_mc(args, world, rank, peak, peak_kind):
     return out
 
 
-C3 = dict(L=128, chains=64, T=10.0, bz=20.0, J=1.0, D=0.3, eta_scale=16.0, therm=30000, snapshots=16,
-          snap_every=50, train_steps=3000, train_rows=16384, lr=1e-3)
+# Learned-proposal workload: 128^2 square DMI lattice (J = 1 mRy, D/J = 0.3), a grid of
+# 19 temperatures 5-30 K x 8 chains (152 chains: 38,912 patch rows per colour, 304
+# tensor-core row tiles = two full waves on 152 SMs), the field chosen by a scan for the
+# largest skyrmion density.
+C3 = dict(L=128, temps=(5.0, 30.0, 19), copies=8, J=1.0, D=0.3, bz_scan=(5.0, 10.0, 15.0, 20.0, 25.0, 30.0),
+          scan_chains=16, eta_scale=16.0, therm=20000, snapshots=96, snap_every=50, train_steps=3000,
+          train_rows=16384, lr=1e-3)
 
 
-def _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms):
-    """Run each (name, hb, learned, cycles) mode from the same snapshot: tau_int of E and
-    |M| per chain (median over chains), cost per cycle, independent samples/s."""
+def _c3_temps():
+    c = C3
+    Ts = np.linspace(*c["temps"])
+    return np.repeat(Ts, c["copies"]), Ts
+
+
+def _bz_scan(seed=1):
+    """Field scan at the grid's lowest temperature: each field's chains are field-cooled by
+    the heat bath (2000 sweeps at 30 K, 4000 at 5 K) from a random start; reported per
+    field: mean |Q| (skyrmion number) and m_z per spin.  The skyrmion-lattice window is
+    where |Q| is large and m_z below saturation."""
+    from uppasd_gb300 import analysis, lattice
+    from uppasd_gb300.simulation import GpuSimulation
+
+    c = C3
+    out = []
+    for bz in c["bz_scan"]:
+        lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, bz, 1.0).with_ensembles(c["scan_chains"])
+        sim = GpuSimulation(lat, emom=random_state(c["scan_chains"], lat.natom, seed=seed), seed=seed + 1)
+        sim.relax("H", 30.0, 2000, structured=True)
+        sim.relax("H", c["temps"][0], 4000, structured=True)
+        e = sim.get_moments()
+        sim.close()
+        q = analysis.topological_charge(e, c["L"])
+        out.append({"bz": bz, "abs_Q_mean": float(np.mean(np.abs(q))), "Q": [round(float(v), 2) for v in q],
+                    "mz": float(np.mean(e[..., 2]))})
+    best = max(out, key=lambda r: r["abs_Q_mean"])
+    return out, best["bz"]
+
+
+def _tau_modes(sim, prop, snap, temps, Ts, modes, structured_ms, learned_ms, plain_ms):
+    """Run each (name, hb sweeps, learned sweeps, cycles, plain) mode from the same snapshot;
+    per temperature of the grid: tau_int of E and |M| (median over the copies), cost per
+    cycle, independent samples/s, E and |M| with their errors over the copies."""
     from uppasd_gb300 import analysis
 
     out = {}
-    chains = snap.shape[0]
+    ncopy = C3["copies"]
     for name, k_hb, k_l, n, plain in modes:
         sim.put_moments(snap)
         es, ms = [], []
         acc = prop_n = 0
         for _ in range(n):
             if plain:
-                sim.relax("H", T, 1)
+                sim.relax_temps("H", temps, 1)
             elif k_l:
-                a, p_, _ = prop.mix(T, 1, k_hb)
+                a, p_, _ = prop.mix_temps(temps, 1, k_hb)
                 acc += a
                 prop_n += p_
             else:
-                sim.relax("H", T, k_hb, structured=True)
+                sim.relax_temps_square(temps, k_hb)
             ob = sim.observables()
             es.append(ob["energy"].copy())
             ms.append(ob["mabs"].copy())
         es, ms = np.array(es), np.array(ms)
-        te = float(np.median([analysis.tau_int(es[:, k])[0] for k in range(chains)]))
-        tm = float(np.median([analysis.tau_int(ms[:, k])[0] for k in range(chains)]))
         cost = plain_ms if plain else k_hb * structured_ms + k_l * learned_ms
-        e_chain, m_chain = es.mean(axis=0), ms.mean(axis=0)
+        per_t = []
+        for it, T in enumerate(Ts):
+            cols = range(it * ncopy, (it + 1) * ncopy)
+            te = float(np.median([analysis.tau_int(es[:, k])[0] for k in cols]))
+            tm = float(np.median([analysis.tau_int(ms[:, k])[0] for k in cols]))
+            ec, mc = es[:, list(cols)].mean(axis=0), ms[:, list(cols)].mean(axis=0)
+            per_t.append({"T": round(float(T), 3), "tau_E": te, "tau_M": tm,
+                          "indep_samples_per_s": ncopy / (2.0 * max(te, tm) * cost * 1e-3),
+                          "E": [float(ec.mean()), float(ec.std(ddof=1) / np.sqrt(ncopy))],
+                          "M": [float(mc.mean()), float(mc.std(ddof=1) / np.sqrt(ncopy))]})
         out[name] = {"heat_bath_sweeps_per_cycle": k_hb, "learned_sweeps_per_cycle": k_l, "cycles": n,
-                     "tau_E": te, "tau_M": tm, "ms_per_cycle": cost,
-                     "indep_samples_per_s": chains / (2.0 * max(te, tm) * cost * 1e-3),
-                     "acceptance": acc / prop_n if prop_n else None,
-                     "E": [float(e_chain.mean()), float(e_chain.std(ddof=1) / np.sqrt(chains))],
-                     "M": [float(m_chain.mean()), float(m_chain.std(ddof=1) / np.sqrt(chains))]}
+                     "ms_per_cycle": cost, "acceptance": acc / prop_n if prop_n else None,
+                     "indep_samples_per_s": float(sum(r["indep_samples_per_s"] for r in per_t)), "per_T": per_t}
     return out
 
 
 def run_c3(args, peak_tf):
-    """Learned-proposal MC on the square DMI lattice against the plain heat bath."""
+    """Learned-proposal MC on the square DMI lattice over the temperature grid, against the
+    batched heat bath alone and the plain FP64 heat bath."""
     import torch
 
     from uppasd_gb300 import lattice
@@ -526,16 +567,19 @@ def run_c3(args, peak_tf):
     from uppasd_gb300.simulation import GpuSimulation
 
     c = C3
-    lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, c["bz"], 1.0).with_ensembles(c["chains"])
-    e0 = random_state(c["chains"], lat.natom, seed=1)
+    scan, bz = _bz_scan()
+    temps, Ts = _c3_temps()
+    chains = temps.size
+    lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, bz, 1.0).with_ensembles(chains)
+    e0 = random_state(chains, lat.natom, seed=1)
     sim = GpuSimulation(lat, emom=e0, seed=2)
-    T = c["T"]
-    sim.relax("H", T, c["therm"], structured=True)
-    prop = LearnedProposal(sim, c["L"], eta_scale=c["eta_scale"], data_capacity=c["chains"] * 1024 * c["snapshots"],
-                           seed=3)
-    untrained = prop.mix(T, 2, 0)
+    sim.relax_temps_square(np.full(chains, 30.0), 2000)      # field-cooled start, as in the scan
+    sim.relax_temps_square(temps, c["therm"])
+    prop = LearnedProposal(sim, c["L"], eta_scale=c["eta_scale"],
+                           data_capacity=chains * 1024 * c["snapshots"], seed=3)
+    untrained = prop.mix_temps(temps, 2, 0)
     for _ in range(c["snapshots"]):
-        sim.relax("H", T, c["snap_every"], structured=True)
+        sim.relax_temps_square(temps, c["snap_every"])
         prop.collect()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -551,43 +595,42 @@ def run_c3(args, peak_tf):
         torch.cuda.synchronize()
         return (time.perf_counter() - t) / n * 1e3
 
-    learned_ms = timed(lambda n: prop.mix(T, n, 0), 100)
-    structured_ms = timed(lambda n: sim.relax("H", T, n, structured=True), 2000)
-    plain_ms = timed(lambda n: sim.relax("H", T, n), 200)
-    # run lengths in sweeps: 24000 (batched heat bath), 6000 (plain), 24000 (learned), 27000 (8+1):
-    # the slow |M| mode needs long runs for its tau_int estimate to settle, and the modes
-    # are compared at (nearly) equal numbers of sweeps
-    modes = [("plain_fp64_heat_bath", 1, 0, 6000, True), ("batched_heat_bath", 1, 0, 24000, False),
-             ("learned", 0, 1, 24000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
-    res = _tau_modes(sim, prop, snap, T, modes, structured_ms, learned_ms, plain_ms)
-    # the plain and the batched heat bath run the same Markov chain (same colours, same
-    # Philox draws): the plain path's samples/s use the longer run's tau_int
-    pb = res["plain_fp64_heat_bath"]
-    pb["tau_M_own_run"], pb["tau_E_own_run"] = pb["tau_M"], pb["tau_E"]
-    pb["tau_M"], pb["tau_E"] = res["batched_heat_bath"]["tau_M"], res["batched_heat_bath"]["tau_E"]
-    pb["indep_samples_per_s"] = c["chains"] / (2.0 * max(pb["tau_M"], pb["tau_E"]) * plain_ms * 1e-3)
-    rows = c["chains"] * (c["L"] // 8) ** 2
+    learned_ms = timed(lambda n: prop.mix_temps(temps, n, 0), 50)
+    structured_ms = timed(lambda n: sim.relax_temps_square(temps, n), 1000)
+    plain_ms = timed(lambda n: sim.relax_temps("H", temps, n), 50)
+    modes = [("plain_fp64_heat_bath", 1, 0, 4000, True), ("batched_heat_bath", 1, 0, 24000, False),
+             ("learned", 0, 1, 6000, False), ("batched_heat_bath_x8+learned", 8, 1, 3000, False)]
+    res = _tau_modes(sim, prop, snap, temps, Ts, modes, structured_ms, learned_ms, plain_ms)
+    rows = chains * (c["L"] // 8) ** 2
     flop_pass = 2.0 * rows * (192 * 256 + 2 * 256 * 256 + 256 * 64)
     flops_sweep = 4 * 4 * flop_pass  # 4 colours x 4 passes
     achieved_tf = flops_sweep / (learned_ms * 1e-3) / 1e12
+    hb, mix = res["batched_heat_bath"], res["batched_heat_bath_x8+learned"]
+    gain_per_T = [{"T": a["T"], "mix_over_heat_bath": b["indep_samples_per_s"] / a["indep_samples_per_s"]}
+                  for a, b in zip(hb["per_T"], mix["per_T"])]
     plain = res["plain_fp64_heat_bath"]["indep_samples_per_s"]
     prop.close()
     sim.close()
     return {
-        "metric": "MC independent samples/s, learned + batched vs plain heat bath",
-        "workload": f"square {c['L']}x{c['L']} J={c['J']} mRy, D/J={c['D']/c['J']}, Bz={c['bz']} T, T={T} K, "
-                    f"{c['chains']} chains; MADE 4x4-patch proposal (3x8x8 input, 3x256 tanh, vMF per spin)",
-        "value": res["batched_heat_bath_x8+learned"]["indep_samples_per_s"], "unit": "samples/s",
-        "speedup_vs_plain": res["batched_heat_bath_x8+learned"]["indep_samples_per_s"] / plain,
-        "learned_only_vs_plain": res["learned"]["indep_samples_per_s"] / plain,
-        "batched_heat_bath_vs_plain": res["batched_heat_bath"]["indep_samples_per_s"] / plain,
-        "learned_tau_M_gain_per_sweep": res["batched_heat_bath"]["tau_M"] / res["learned"]["tau_M"],
+        "metric": "MC independent samples/s, learned + batched vs batched heat bath alone and plain FP64 heat bath",
+        "workload": f"square {c['L']}x{c['L']} J={c['J']} mRy, D/J={c['D']/c['J']}, Bz={bz} T (scan below), "
+                    f"T grid {Ts[0]}-{Ts[-1]} K x {len(Ts)} x {c['copies']} chains; MADE 4x4-patch proposal "
+                    "(3x8x8 input, 3x256 tanh, vMF per spin), one network for the whole grid",
+        "value": mix["indep_samples_per_s"], "unit": "samples/s",
+        "speedup_vs_plain": mix["indep_samples_per_s"] / plain,
+        "learned_plus_batched_vs_batched_alone": mix["indep_samples_per_s"] / hb["indep_samples_per_s"],
+        "learned_only_vs_batched_alone": res["learned"]["indep_samples_per_s"] / hb["indep_samples_per_s"],
+        "batched_heat_bath_vs_plain": hb["indep_samples_per_s"] / plain,
+        "gain_per_T": gain_per_T,
+        "max_gain_over_grid": max(g["mix_over_heat_bath"] for g in gain_per_T),
+        "bz_scan": scan, "bz": bz,
         "acceptance_untrained": untrained[0] / max(untrained[1], 1),
         "modes": res,
         "ms_per_sweep": {"plain_fp64_heat_bath": plain_ms, "batched_heat_bath": structured_ms,
                          "learned": learned_ms},
-        "training": {"windows": int(c["chains"] * 1024 * c["snapshots"]), "steps": c["train_steps"],
-                     "rows_per_step": c["train_rows"], "samples": c["train_steps"] * c["train_rows"],
+        "training": {"configurations": int(chains * c["snapshots"]),
+                     "windows": int(chains * 1024 * c["snapshots"]), "steps": c["train_steps"],
+                     "rows_per_step": c["train_rows"], "window_samples": c["train_steps"] * c["train_rows"],
                      "seconds": t_train, "loss_first": float(losses[0]),
                      "loss_last100": float(np.mean(losses[-100:]))},
         "roofline": {"bound": "tensor", "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s",
@@ -763,7 +806,11 @@ def run_gb300(args, w):
     lat = build_lattice(w)
     e0 = random_state(lat.mensemble, lat.natom, seed=7 + rank)
     nspin = lat.natom * lat.mensemble
-    order = [int(args.precision)] if args.precision != "auto" else [1, 0]
+    # default: the double-single master (FP32 gather; the master and its renormalisation
+    # in hi + lo FP32 pairs, ~48-bit), whose error against the FP64 oracle on this lattice
+    # equals the FP64 master's (both ~1e-7 after 20 steps at T = 0, ~4e-6 at 300 K: the
+    # FP32 gather sets it); the FP64 master is timed as a variant
+    order = [int(args.precision)] if args.precision != "auto" else [2, 1, 0]
     sim, prec = None, None
     for p in order:
         try:
@@ -827,18 +874,20 @@ def run_gb300(args, w):
                     "stream while the next block runs; the host callback (here empty) runs while the "
                     "GPU works on the following block"}
     sim.close()
-    if not args.no_variants and prec == 1:
+    if not args.no_variants and prec in (1, 2):
+        other = 1 if prec == 2 else 2
+        vname = "fp64_master" if other == 1 else "double_single_master"
         try:
-            alt = _make_sim(lat, w, 2, 1000 + rank, e0)
+            alt = _make_sim(lat, w, other, 1000 + rank, e0)
             alt.set_stream(stream.cuda_stream)
             ms2 = _time_steps(alt, stream, args.steps, args.warmup, world)
             kt2 = alt.time_kernels(3)
             alt.close()
-            variants["double_single_master"] = {
+            variants[vname] = {
                 "value": nspin * args.steps * world / (ms2 * 1e-3), "ms_per_step": ms2 / args.steps,
                 "kernel_ms": kt2, "roofline": _roofline(kt2, nspin, 8, ms2 / args.steps, peak, peak_kind, None)}
         except Exception as exc:
-            variants["double_single_master"] = {"error": str(exc)}
+            variants[vname] = {"error": str(exc)}
         # general Hamiltonians (neighbour lists, DMI, anisotropy): FP64 path and FP32 gather
         # with the FP64 state as master, on the same lattice
         try:
@@ -897,7 +946,7 @@ def run_gb300(args, w):
         "metric": "LLG atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == 0 else "f32-gather/f64-state",
+        "dtype": {0: "f64", 1: "f32-gather/f64-state", 2: "f32-gather/double-single-state"}[prec],
         "data": "synthetic (seeded lattice, species and spins)",
         "config": {"workload": args.workload, "description": w["desc"], "natom": lat.natom,
                    "ensembles": lat.mensemble, "spins": nspin,
@@ -963,10 +1012,11 @@ def main():
 
         b.build()
         c = C3
-        lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, c["bz"], 1.0).with_ensembles(c["chains"])
-        sim = GpuSimulation(lat, emom=random_state(c["chains"], lat.natom, seed=1), seed=2)
+        temps, _ = _c3_temps()
+        lat = lattice.square_dmi(c["L"], c["J"], c["D"], 0.0, 15.0, 1.0).with_ensembles(temps.size)
+        sim = GpuSimulation(lat, emom=random_state(temps.size, lat.natom, seed=1), seed=2)
         prop = LearnedProposal(sim, c["L"], eta_scale=c["eta_scale"], seed=3)
-        print(json.dumps({"learned_sweeps": 2, "accepted_proposed": prop.mix(c["T"], 2, 0)[:2]}), flush=True)
+        print(json.dumps({"learned_sweeps": 2, "accepted_proposed": prop.mix_temps(temps, 2, 0)[:2]}), flush=True)
     elif args.c3_only:
         import torch
 

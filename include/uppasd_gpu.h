@@ -175,6 +175,9 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *s, char mode, double temperature, int64_t 
  * checkerboard chain of uppasd_gpu_mc_run 'H' with FP32 draws on the FP64 state,
  * all ensembles per launch. */
 int uppasd_gpu_mc_run_square(uppasd_gpu_sim *s, int32_t L, double temperature, int64_t nsweeps);
+/* The same with one temperature per ensemble (temps[mensemble], K): a temperature grid
+ * swept in one launch per colour, as uppasd_gpu_mc_run_temps does on the general path. */
+int uppasd_gpu_mc_run_square_temps(uppasd_gpu_sim *s, int32_t L, const double *temps, int64_t nsweeps);
 
 /* Monte Carlo sweeps with one temperature per ensemble (temps[mensemble], K): the
  * chain of uppasd_gpu_mc_run with T taken per ensemble (on precision 3 the heat bath
@@ -372,6 +375,11 @@ int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_
  * graph) with one synchronisation at the end; counts as for proposal_sweep. */
 int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t ncycles, int32_t hb_per_cycle,
                             int64_t *accepted, int64_t *proposed, double *dE_accepted);
+/* The same with one temperature per ensemble (temps[mensemble], K), for the heat-bath
+ * sweeps and for every learned move's acceptance: a temperature grid in one learned
+ * sweep.  The network is shared by all temperatures; the acceptance stays exact. */
+int uppasd_gpu_proposal_mix_temps(uppasd_gpu_proposal *p, const double *temps, int64_t ncycles,
+                                  int32_t hb_per_cycle, int64_t *accepted, int64_t *proposed, double *dE_accepted);
 
 #ifdef __cplusplus
 }

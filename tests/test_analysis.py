@@ -68,3 +68,17 @@ def test_cumulants_match_oracle_running_form():
     u = 1 - wm(ms ** 4) / 3 / wm(ms ** 2) ** 2
     assert abs(out[3] - u) < 1e-12
     assert abs(c["binder"] - (1 - (ms ** 4).mean() / 3 / (ms ** 2).mean() ** 2)) < 1e-12
+
+
+def test_topological_charge_of_a_skyrmion_and_uniform_states():
+    from uppasd_gb300.analysis import topological_charge
+    L = 32
+    y, x = np.mgrid[0:L, 0:L]
+    r = np.hypot(x - L / 2 + 0.5, y - L / 2 + 0.5)
+    th = np.pi * np.exp(-(r / 5) ** 2)
+    ph = np.arctan2(y - L / 2 + 0.5, x - L / 2 + 0.5)
+    e = np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], -1).reshape(L * L, 3)
+    assert abs(topological_charge(e, L) + 1.0) < 1e-9          # one skyrmion, core against +z
+    assert abs(topological_charge(-e, L) - 1.0) < 1e-9         # the reversed texture
+    two = np.stack([e, np.tile([0.0, 0.0, 1.0], (L * L, 1))])
+    assert np.allclose(topological_charge(two, L), [-1.0, 0.0], atol=1e-9)

@@ -67,6 +67,7 @@ SIGNATURES = {
     "uppasd_gpu_observables": [C.c_void_p, F64P, F64P, F64P],
     "uppasd_gpu_energy_terms": [C.c_void_p, F64P],
     "uppasd_gpu_mc_run_square": [C.c_void_p, C.c_int32, C.c_double, C.c_int64],
+    "uppasd_gpu_mc_run_square_temps": [C.c_void_p, C.c_int32, F64P, C.c_int64],
     "uppasd_gpu_mc_run_temps": [C.c_void_p, C.c_char, F64P, C.c_int64],
     "uppasd_gpu_pt_run": [C.c_void_p, F64P, C.c_int64, C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                           I32P],
@@ -114,6 +115,8 @@ SIGNATURES = {
                                   F64P],
     "uppasd_gpu_proposal_mix": [C.c_void_p, C.c_double, C.c_int64, C.c_int32, C.POINTER(C.c_int64),
                                 C.POINTER(C.c_int64), F64P],
+    "uppasd_gpu_proposal_mix_temps": [C.c_void_p, F64P, C.c_int64, C.c_int32, C.POINTER(C.c_int64),
+                                      C.POINTER(C.c_int64), F64P],
 }
 
 _lib = None

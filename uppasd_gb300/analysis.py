@@ -79,3 +79,25 @@ def jackknife(fn, columns, nbin: int = 20):
     loo = np.array([fn(*[(t - b[i]) / (m - k) for t, b in zip(tot, blocks)]) for i in range(nbin)])
     err = np.sqrt((nbin - 1) / nbin * np.sum((loo - loo.mean()) ** 2))
     return float(full), float(err)
+
+
+def topological_charge(emom, L: int):
+    """Skyrmion number of each configuration of an L x L square monolayer with periodic
+    edges (site i = x + L y), from unit spins of shape (..., L*L, 3): every plaquette
+    split into two triangles, each contributing its signed solid angle
+    2 atan2(a.(b x c), 1 + a.b + b.c + c.a) (Berg and Luescher), summed and divided by 4 pi."""
+    s = np.asarray(emom, dtype=np.float64)
+    s = s.reshape(s.shape[:-2] + (L, L, 3))           # [..., y, x, 3]
+    a = s
+    b = np.roll(s, -1, axis=-2)                       # (x + 1, y)
+    c = np.roll(b, -1, axis=-3)                       # (x + 1, y + 1)
+    d = np.roll(s, -1, axis=-3)                       # (x, y + 1)
+
+    def omega(p, q, r):
+        num = np.einsum("...k,...k->...", p, np.cross(q, r))
+        den = 1.0 + np.einsum("...k,...k->...", p, q) + np.einsum("...k,...k->...", q, r) + \
+            np.einsum("...k,...k->...", r, p)
+        return 2.0 * np.arctan2(num, den)
+
+    tot = omega(a, b, c) + omega(a, c, d)
+    return tot.sum(axis=(-2, -1)) / (4.0 * np.pi)

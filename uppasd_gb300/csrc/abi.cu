@@ -912,6 +912,11 @@ int upload_temps(Sim &s, const double *temps) {
     return UPPASD_GPU_OK;
 }
 
+}  // namespace
+
+int set_ensemble_temps(Sim &s, const double *temps) { return upload_temps(s, temps); }
+
+namespace {
 int sweeps_with_temps(Sim &s, char mode, int64_t nsweeps) {
     int rc;
     if (structured(s) && (rc = structured_sync_state(s))) return rc;

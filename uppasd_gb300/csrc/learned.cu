@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, float4
                                                    int rows,
                                                    const float *win, const float *old_patch, const float *new_patch,
                                                    const float *logq_old, const float *logq_new, float beta_mub,
-                                                   uint64_t seed, const long long *dctr, int sub,
+                                                   const float *betak, uint64_t seed, const long long *dctr, int sub,
                                                    unsigned long long *accepted, double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     // rows is a multiple of 128 and blocks hold 8 warps: every warp of the grid is a patch
@@ -386,7 +386,7 @@ __global__ void __launch_bounds__(256) k_accept_sq(PatchGeom g, SqCoup q, float4
     for (int o = 8; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
     int acc = 0;
     if (lane == 0) {
-        const float loga = -beta_mub * dE + (logq_old[r] - logq_new[r]);
+        const float loga = -(betak ? betak[k] : beta_mub) * dE + (logq_old[r] - logq_new[r]);
         const Philox4 w = philox_draw(seed, r, 16, ctr, kStreamLearned);
         const float u = u01_openf(w.z);
         acc = (loga >= 0.f || logf(u) < loga) ? 1 : 0;
@@ -495,9 +495,10 @@ __device__ double patch_spin_energy(const HamDev &h, const Vec3D &eM, const doub
 }
 
 // One warp per patch: exact energy change, Metropolis-Hastings decision, write-back.
+// tk: temperature per ensemble (K) or null (beta_mub for all)
 __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double *mmom, int rows,
                          const float *new_patch, const float *logq_old, const float *logq_new, double beta_mub,
-                         uint64_t seed, const long long *dctr, int sub, unsigned long long *accepted,
+                         const double *tk, uint64_t seed, const long long *dctr, int sub, unsigned long long *accepted,
                          double *dE_sum) {
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     // rows is a multiple of 128 and blocks hold 8 warps: every warp of the grid is a patch
@@ -516,7 +517,8 @@ __global__ void k_accept(PatchGeom g, HamDev h, Vec3D e, Vec3D eM, const double 
     for (int o = 16; o > 0; o >>= 1) dE += __shfl_xor_sync(0xffffffffu, dE, o);
     int acc = 0;
     if (lane == 0) {
-        const double loga = -beta_mub * dE + (double)(logq_old[r] - logq_new[r]);
+        const double b = tk ? h.mub / (h.kbolt * tk[k]) : beta_mub;
+        const double loga = -b * dE + (double)(logq_old[r] - logq_new[r]);
         const Philox4 w = philox_draw(seed, r, 16, ctr, kStreamLearned);
         const float u = u01_openf(w.z);
         acc = (loga >= 0.0 || (double)logf(u) < loga) ? 1 : 0;
@@ -833,7 +835,7 @@ PatchGeom geom(const uppasd_gpu_proposal *p, int colour) {
 }
 
 // One learned sweep (the four patch colours) enqueued on `st`; capturable.
-int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_t st) {
+int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, bool per_ensemble, cudaStream_t st) {
     Sim &s = p->sim->s;
     const long long nt = (long long)rows * 64;
     int rc;
@@ -859,11 +861,13 @@ int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, cudaStream_
             k_accept_sq<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, q, s.sqm, s.e, s.eM, s.ham.natom, rows, p->win,
                                                                   p->old_patch,
                                                                   p->new_patch, p->logq_old, p->logq_new, beta_mub,
-                                                                  p->seed, p->dctr, c, p->accepted, p->dE_sum);
+                                                                  per_ensemble ? s.betak : nullptr, p->seed, p->dctr,
+                                                                  c, p->accepted, p->dE_sum);
         } else {
             k_accept<<<(rows * 32 + 255) / 256, 256, 0, st>>>(g, s.ham, s.e, s.eM, s.llg.mmom, rows,
                                                                p->new_patch, p->logq_old, p->logq_new, beta_mub,
-                                                               p->seed, p->dctr, c, p->accepted, p->dE_sum);
+                                                               per_ensemble ? s.tk : nullptr, p->seed, p->dctr, c,
+                                                               p->accepted, p->dE_sum);
         }
     }
     k_advance<<<1, 1, 0, st>>>(p->dctr);
@@ -1214,15 +1218,25 @@ int uppasd_gpu_proposal_sweep(uppasd_gpu_proposal *p, double temperature, int64_
     return uppasd_gpu_proposal_mix(p, temperature, nsweeps, 0, accepted, proposed, dE_accepted);
 }
 
+}  // extern "C"
+
+namespace {
 // ncycles of (hb_per_cycle structured heat-bath sweeps, then one learned sweep), all
-// enqueued on the simulation's stream; one synchronisation at the end.
-int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t ncycles, int32_t hb_per_cycle,
-                            int64_t *accepted, int64_t *proposed, double *dE_accepted) {
-    if (!p || !(temperature > 0.0) || ncycles < 0 || hb_per_cycle < 0) {
+// enqueued on the simulation's stream; one synchronisation at the end.  temps: one
+// temperature per ensemble, or null for `temperature`.
+int proposal_mix(uppasd_gpu_proposal *p, double temperature, const double *temps, int64_t ncycles,
+                 int32_t hb_per_cycle, int64_t *accepted, int64_t *proposed, double *dE_accepted) {
+    if (!p || !(temps || temperature > 0.0) || ncycles < 0 || hb_per_cycle < 0) {
         set_error("proposal_mix: bad arguments");
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = p->sim->s;
+    const bool per_ens = temps != nullptr;
+    if (per_ens) {
+        const int rc0 = set_ensemble_temps(s, temps);
+        if (rc0) return rc0;
+        temperature = -1.0;  // the graph's key: per-ensemble temperatures (read on the device)
+    }
     if (s.ham.do_jtensor) {
         set_error("proposal_mix: the exchange became a tensor after the proposal was created");
         return UPPASD_GPU_EUNSUPPORTED;
@@ -1234,7 +1248,7 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     cudaError_t e = cudaMemsetAsync(p->accepted, 0, sizeof(unsigned long long), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(p->dE_sum, 0, sizeof(double), st);
     if (e != cudaSuccess) return cuda_fail("proposal_mix", e);
-    const double beta_mub = s.ham.mub / (s.ham.kbolt * temperature);
+    const double beta_mub = per_ens ? 0.0 : s.ham.mub / (s.ham.kbolt * temperature);
     s.mix.valid = 0;  // the precision-3 LLG mirror does not follow the learned moves
     if (s.sq.L == p->L) {
         // learned moves on the square lattice read and write the FP32 mirror as well
@@ -1244,11 +1258,11 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     }
     int64_t done = 0;
     auto heat_bath = [&]() -> int {
-        return hb_per_cycle > 0 ? uppasd_gpu_mc_run_square(p->sim, p->L, temperature, hb_per_cycle) : 0;
+        return hb_per_cycle > 0 ? square_sweeps(s, p->L, temperature, per_ens ? s.betak : nullptr, hb_per_cycle) : 0;
     };
     if (ncycles > 0 && !p->warmed) {
         // first sweep eagerly: sets the GEMM kernels' shared-memory attributes before any capture
-        if ((rc = heat_bath()) || (rc = enqueue_sweep(p, rows, beta_mub, st))) return rc;
+        if ((rc = heat_bath()) || (rc = enqueue_sweep(p, rows, beta_mub, per_ens, st))) return rc;
         p->warmed = true;
         done = 1;
     }
@@ -1258,7 +1272,7 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
         cudaGraph_t g = nullptr;
         e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return cuda_fail("proposal_mix capture", e);
-        rc = enqueue_sweep(p, rows, beta_mub, st);
+        rc = enqueue_sweep(p, rows, beta_mub, per_ens, st);
         e = cudaStreamEndCapture(st, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -1286,6 +1300,27 @@ int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t 
     if (proposed) *proposed = (int64_t)rows * 4 * ncycles;
     if (dE_accepted) *dE_accepted = de * s.ham.mub;
     return UPPASD_GPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int uppasd_gpu_proposal_mix(uppasd_gpu_proposal *p, double temperature, int64_t ncycles, int32_t hb_per_cycle,
+                            int64_t *accepted, int64_t *proposed, double *dE_accepted) {
+    if (!(temperature > 0.0)) {
+        set_error("proposal_mix: temperature must be > 0");
+        return UPPASD_GPU_EINVAL;
+    }
+    return proposal_mix(p, temperature, nullptr, ncycles, hb_per_cycle, accepted, proposed, dE_accepted);
+}
+
+int uppasd_gpu_proposal_mix_temps(uppasd_gpu_proposal *p, const double *temps, int64_t ncycles, int32_t hb_per_cycle,
+                                  int64_t *accepted, int64_t *proposed, double *dE_accepted) {
+    if (!temps) {
+        set_error("proposal_mix_temps: temperatures required");
+        return UPPASD_GPU_EINVAL;
+    }
+    return proposal_mix(p, 0.0, temps, ncycles, hb_per_cycle, accepted, proposed, dE_accepted);
 }
 
 }  // extern "C"

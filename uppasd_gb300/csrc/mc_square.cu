@@ -31,7 +31,8 @@ struct SqArgs {
     long long sweep;
 };
 
-__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e, Vec3D eM) {
+// betak: muB / (kB T) per ensemble (one temperature per ensemble), or null (a.beta_mu)
+__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e, Vec3D eM, const float *betak) {
     const int half = a.L >> 1;
     const long long per = (long long)a.L * half;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -59,7 +60,7 @@ __global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e
     const Philox4 w = philox_draw(a.seed, i, k, a.sweep, kStreamMC);
     const float k32 = 2.3283064365386963e-10f;
     const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
-    const float3 n = heat_bath_f32(make_float3(hx, hy, hz), a.beta_mu, q, fp);
+    const float3 n = heat_bath_f32(make_float3(hx, hy, hz), betak ? betak[k] * a.mom : a.beta_mu, q, fp);
     const size_t o = off + i;
     m[o] = make_float4(n.x, n.y, n.z, 0.f);
     e.x[o] = n.x;
@@ -183,13 +184,11 @@ int square_mirror_ready(Sim &s) {
 
 }  // namespace uppasd
 
-extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double temperature, int64_t nsweeps) {
-    using namespace uppasd;
-    if (!w || nsweeps < 0 || !(temperature > 0.0) || L < 2) {
-        set_error("mc_run_square: temperature > 0, nsweeps >= 0, L >= 2");
-        return UPPASD_GPU_EINVAL;
-    }
-    Sim &s = w->s;
+namespace uppasd {
+
+// Structured heat-bath sweeps; betak (muB / (kB T) per ensemble, on the device) or
+// null for the single `temperature`.
+int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t nsweeps) {
     if (structured(s)) {
         set_error("mc_run_square: needs the FP64 state (precision 0 or 3)");
         return UPPASD_GPU_EUNSUPPORTED;
@@ -210,7 +209,7 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
     }
     for (int c = 0; c < 3; ++c) a.ext[c] = s.sq.ext[c];
     a.mom = s.sq.mom;
-    a.beta_mu = (float)(s.ham.mub * s.sq.mom / (s.ham.kbolt * temperature));
+    a.beta_mu = betak ? 0.f : (float)(s.ham.mub * s.sq.mom / (s.ham.kbolt * temperature));
     a.seed = s.llg.seed;
     const long long per = (long long)L * (L / 2) * a.mensemble;
     const unsigned blocks = (unsigned)((per + 255) / 256);
@@ -218,10 +217,32 @@ extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double tem
         a.sweep = s.mc_sweep;
         for (int c = 0; c < 2; ++c) {
             a.colour = c;
-            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.sqm, s.e, s.eM);
+            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.sqm, s.e, s.eM, betak);
         }
         s.mc_sweep += 1;
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
+}
+
+}  // namespace uppasd
+
+extern "C" int uppasd_gpu_mc_run_square(uppasd_gpu_sim *w, int32_t L, double temperature, int64_t nsweeps) {
+    using namespace uppasd;
+    if (!w || nsweeps < 0 || !(temperature > 0.0) || L < 2) {
+        set_error("mc_run_square: temperature > 0, nsweeps >= 0, L >= 2");
+        return UPPASD_GPU_EINVAL;
+    }
+    return square_sweeps(w->s, L, temperature, nullptr, nsweeps);
+}
+
+extern "C" int uppasd_gpu_mc_run_square_temps(uppasd_gpu_sim *w, int32_t L, const double *temps, int64_t nsweeps) {
+    using namespace uppasd;
+    if (!w || !temps || nsweeps < 0 || L < 2) {
+        set_error("mc_run_square_temps: temperatures, nsweeps >= 0, L >= 2");
+        return UPPASD_GPU_EINVAL;
+    }
+    const int rc = set_ensemble_temps(w->s, temps);
+    if (rc) return rc;
+    return square_sweeps(w->s, L, 0.0, w->s.betak, nsweeps);
 }

@@ -176,6 +176,10 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
 // mc_square.cu: recognise a uniform square-lattice Hamiltonian (fills s.sq)
 int square_recognise(Sim &s, int L);
 int square_mirror_ready(Sim &s);  // builds the FP32 mirror from e when it is stale
+// structured heat-bath sweeps at one temperature, or per ensemble (betak on the device)
+int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t nsweeps);
+// abi.cu: one temperature per ensemble (K) to s.tk and muB / (kB T) to s.betak
+int set_ensemble_temps(Sim &s, const double *temps);
 void set_error(const std::string &msg);
 // the host-transfer staging array (allocated on first use); nullptr with the error set
 inline double *stage_buffer(Sim &s) {

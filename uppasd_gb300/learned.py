@@ -109,6 +109,14 @@ class LearnedProposal:
                   C.byref(a), C.byref(p), C.byref(de))
         return int(a.value), int(p.value), float(de.value)
 
+    def mix_temps(self, temps, ncycles: int, hb_per_cycle: int = 1):
+        """mix() with one temperature per ensemble of the simulation."""
+        t = np.ascontiguousarray(temps, dtype=np.float64)
+        a, p, de = C.c_int64(), C.c_int64(), C.c_double()
+        _lib.call("uppasd_gpu_proposal_mix_temps", self.h, t.ctypes.data_as(_lib.F64P), int(ncycles),
+                  int(hb_per_cycle), C.byref(a), C.byref(p), C.byref(de))
+        return int(a.value), int(p.value), float(de.value)
+
     def close(self):
         if getattr(self, "h", None) is not None and self.h.value:
             _lib.call("uppasd_gpu_proposal_destroy", self.h)

@@ -229,6 +229,14 @@ class GpuSimulation:
             raise ValueError("one temperature per ensemble")
         _lib.call("uppasd_gpu_mc_run_temps", self._h, mode.encode()[:1], _ptr(t), int(nsweeps))
 
+    def relax_temps_square(self, temps, nsweeps: int):
+        """Structured square-lattice heat bath (uppasd_gpu_mc_run_square) with one
+        temperature per ensemble."""
+        t = np.ascontiguousarray(temps, dtype=np.float64)
+        if t.shape != (self.lat.mensemble,):
+            raise ValueError("one temperature per ensemble")
+        _lib.call("uppasd_gpu_mc_run_square_temps", self._h, int(self.lat.cells[0]), _ptr(t), int(nsweeps))
+
     def parallel_tempering(self, temps, nsweeps: int, pt_step: int = 1):
         """pt_iphase with the ensembles as replicas: returns (temperatures per replica at the
         end, swap trials, accepted swaps, replica of lowest energy)."""
