@@ -106,31 +106,56 @@ struct SParams {
     int *err;                   // set when a plane wait of the staged kernels ran past its limit
 };
 
-__device__ __forceinline__ long long pidx(const SParams &p, int k, int b, int x, int y, int z) {
-    return (long long)(k * 2 + b) * p.pbox + ((long long)(z + 2) * p.P2 + (long long)(y + 2) * p.P1 + (x + XOFF));
+// Padded pitches of a cubic L^3 lattice; LC = 0 selects the runtime pitches.
+__host__ __device__ constexpr int pitch1(int L) { return ((L + XOFF + 2) + 7) / 8 * 8; }
+__host__ __device__ constexpr int pitch2(int L) { return pitch1(L) * (L + 4); }
+
+// Lattice edges and pitches: compile-time for the compiled cubic sizes (LC > 0), so the
+// index arithmetic folds into immediates; from the parameters otherwise.
+template <int LC> __device__ __forceinline__ int gl1(const SParams &p) { if constexpr (LC) return LC; else return p.L1; }
+template <int LC> __device__ __forceinline__ int gl2(const SParams &p) { if constexpr (LC) return LC; else return p.L2; }
+template <int LC> __device__ __forceinline__ int gl3(const SParams &p) { if constexpr (LC) return LC; else return p.L3; }
+template <int LC> __device__ __forceinline__ int gp1(const SParams &p) {
+    if constexpr (LC) return pitch1(LC); else return p.P1;
 }
+template <int LC> __device__ __forceinline__ long long gp2(const SParams &p) {
+    if constexpr (LC) return pitch2(LC); else return p.P2;
+}
+template <int LC> __device__ __forceinline__ long long gpbox(const SParams &p) {
+    if constexpr (LC) return (long long)pitch2(LC) * (LC + 4); else return p.pbox;
+}
+
+template <int LC = 0>
+__device__ __forceinline__ long long pidx(const SParams &p, int k, int b, int x, int y, int z) {
+    return (long long)(k * 2 + b) * gpbox<LC>(p) +
+           ((long long)(z + 2) * gp2<LC>(p) + (long long)(y + 2) * gp1<LC>(p) + (x + XOFF));
+}
+template <int LC = 0>
 __device__ __forceinline__ long long uidx(const SParams &p, int k, int b, int x, int y, int z) {
-    return (((long long)(k * 2 + b) * p.L3 + z) * p.L2 + y) * (long long)p.L1 + x;
+    return (((long long)(k * 2 + b) * gl3<LC>(p) + z) * gl2<LC>(p) + y) * (long long)gl1<LC>(p) + x;
 }
 // Reference numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3)) (0-based) for the Philox
 // counter, so the structured and the generic path draw the same thermal-field stream.
+template <int LC = 0>
 __device__ __forceinline__ long long ref_site(const SParams &p, int b, int x, int y, int z) {
-    return b + 2LL * (x + (long long)p.L1 * (y + (long long)p.L2 * z));
+    return b + 2LL * (x + (long long)gl1<LC>(p) * (y + (long long)gl2<LC>(p) * z));
 }
 
 // Store a site's mirror value and its periodic ghost copies.
+template <int LC = 0>
 __device__ __forceinline__ void store_mirror(const SParams &p, float4 *m, int k, int b, int x, int y, int z,
                                              float4 v) {
-    float4 *bx = m + (long long)(k * 2 + b) * p.pbox;
+    const int L1 = gl1<LC>(p), L2 = gl2<LC>(p), L3 = gl3<LC>(p);
+    float4 *bx = m + (long long)(k * 2 + b) * gpbox<LC>(p);
     const int gx0 = x + XOFF, gy0 = y + 2, gz0 = z + 2;
     // second (ghost) coordinate per axis, -1 when the site is not within 2 cells of that face
-    const int gx1 = x < 2 ? gx0 + p.L1 : (x >= p.L1 - 2 ? gx0 - p.L1 : -1);
-    const int gy1 = y < 2 ? gy0 + p.L2 : (y >= p.L2 - 2 ? gy0 - p.L2 : -1);
-    const int gz1 = z < 2 ? gz0 + p.L3 : (z >= p.L3 - 2 ? gz0 - p.L3 : -1);
-    const long long py0 = (long long)gy0 * p.P1, pz0 = (long long)gz0 * p.P2;
+    const int gx1 = x < 2 ? gx0 + L1 : (x >= L1 - 2 ? gx0 - L1 : -1);
+    const int gy1 = y < 2 ? gy0 + L2 : (y >= L2 - 2 ? gy0 - L2 : -1);
+    const int gz1 = z < 2 ? gz0 + L3 : (z >= L3 - 2 ? gz0 - L3 : -1);
+    const long long py0 = (long long)gy0 * gp1<LC>(p), pz0 = (long long)gz0 * gp2<LC>(p);
     bx[pz0 + py0 + gx0] = v;
     if (gx1 < 0 && gy1 < 0 && gz1 < 0) return;
-    const long long py1 = (long long)gy1 * p.P1, pz1 = (long long)gz1 * p.P2;
+    const long long py1 = (long long)gy1 * gp1<LC>(p), pz1 = (long long)gz1 * gp2<LC>(p);
     if (gx1 >= 0) bx[pz0 + py0 + gx1] = v;
     if (gy1 >= 0) {
         bx[pz0 + py1 + gx0] = v;
@@ -146,9 +171,6 @@ __device__ __forceinline__ void store_mirror(const SParams &p, float4 *m, int k,
     }
 }
 
-// Padded pitches of a cubic L^3 lattice; LC = 0 selects the runtime pitches.
-__host__ __device__ constexpr int pitch1(int L) { return ((L + XOFF + 2) + 7) / 8 * 8; }
-__host__ __device__ constexpr int pitch2(int L) { return pitch1(L) * (L + 4); }
 
 template <int NSH, int b, int LC>
 __device__ __forceinline__ void gather_b(const SParams &p, const float4 *__restrict__ m, int k, int x, int y, int z,
@@ -239,12 +261,13 @@ __device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
 // and the bracket is known here (ep is this thread's own result), so the predictor
 // stores b2eff + th + lambda ep x th (depondt.f90:152-154, 290-301) and the thermal field
 // itself is neither stored nor drawn again.
+template <int LC = 0>
 __device__ __forceinline__ void predict_update(const SParams &p, int k, int b, int x, int y, int z, const float4 &me,
                                                const float B[3]) {
     const int si = me.w != 0.f ? 1 : 0;
     const long long step = *p.d_step + p.step_off;
     float zr[3];
-    normal3_f32_fast(p.seed, ref_site(p, b, x, y, z), k, step, kStreamLLG, zr);
+    normal3_f32_fast(p.seed, ref_site<LC>(p, b, x, y, z), k, step, kStreamLLG, zr);
     const float sg = p.sigma[si];
     const float e[3] = {me.x, me.y, me.z};
     const float th[3] = {zr[0] * sg, zr[1] * sg, zr[2] * sg};
@@ -253,10 +276,10 @@ __device__ __forceinline__ void predict_update(const SParams &p, int k, int b, i
     depondt_bdup(p.lam, e, bl, bd);
     rotation_delta(bd, e, p.dtg, d);
     const float ep[3] = {e[0] + d[0], e[1] + d[1], e[2] + d[2]};
-    store_mirror(p, p.mp, k, b, x, y, z, make_float4(ep[0], ep[1], ep[2], me.w));
+    store_mirror<LC>(p, p.mp, k, b, x, y, z, make_float4(ep[0], ep[1], ep[2], me.w));
     float tc[3];
     depondt_bdup(p.lam, ep, th, tc);
-    const long long u = uidx(p, k, b, x, y, z);
+    const long long u = uidx<LC>(p, k, b, x, y, z);
     p.b2x[u] = bd[0] + tc[0];
     p.b2y[u] = bd[1] + tc[1];
     p.b2z[u] = bd[2] + tc[2];
@@ -306,10 +329,10 @@ struct CorrIn {
     double m[3];    // MASTER 1
 };
 
-template <int MASTER>
+template <int MASTER, int LC = 0>
 __device__ __forceinline__ void correct_load(const SParams &p, int k, int b, int x, int y, int z, CorrIn<MASTER> &c) {
-    const long long u = uidx(p, k, b, x, y, z);
-    c.mt = p.mt[pidx(p, k, b, x, y, z)];
+    const long long u = uidx<LC>(p, k, b, x, y, z);
+    c.mt = p.mt[pidx<LC>(p, k, b, x, y, z)];
     c.b2[0] = p.b2x[u];
     c.b2[1] = p.b2y[u];
     c.b2[2] = p.b2z[u];
@@ -324,10 +347,10 @@ __device__ __forceinline__ void correct_load(const SParams &p, int k, int b, int
     }
 }
 
-template <int MASTER>  // MASTER 1: FP64, 2: double-single
+template <int MASTER, int LC = 0>  // MASTER 1: FP64, 2: double-single
 __device__ __forceinline__ void correct_finish(const SParams &p, int k, int b, int x, int y, int z, const float4 &mp,
                                                const float B[3], const CorrIn<MASTER> &ci) {
-    const long long u = uidx(p, k, b, x, y, z);
+    const long long u = uidx<LC>(p, k, b, x, y, z);
     const float ep[3] = {mp.x, mp.y, mp.z};
     float bd[3];
     depondt_bdup(p.lam, ep, B, bd);   // the thermal term is in b2 (predict_update)
@@ -386,7 +409,7 @@ __device__ __forceinline__ void correct_finish(const SParams &p, int k, int b, i
         p.loz[u] = lo[2];
         out = make_float4(hi[0], hi[1], hi[2], mt.w);
     }
-    store_mirror(p, p.mt, k, b, x, y, z, out);
+    store_mirror<LC>(p, p.mt, k, b, x, y, z, out);
 }
 
 template <int MASTER>
@@ -621,7 +644,7 @@ __device__ __forceinline__ void cb_own(const Src &src, float4 (&me)[2 * NZ], std
 
 // Both sites of NZ cells: own values, the gather, then the predictor or corrector
 // update of every site.
-template <int NSH, int NZ, int KIND, int MASTER, class Src>
+template <int NSH, int NZ, int LC, int KIND, int MASTER, class Src>
 __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k, int x, int y, int z0) {
     float4 me[2 * NZ];
     float cA[2 * NZ][4], cD[2 * NZ][4], acc[2 * NZ][3];
@@ -631,7 +654,7 @@ __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k
 #pragma unroll
         for (int b = 0; b < 2; ++b)
 #pragma unroll
-            for (int q = 0; q < NZ; ++q) correct_load<MASTER == 1 ? 1 : 2>(p, k, b, x, y, z0 + q, ci[b * NZ + q]);
+            for (int q = 0; q < NZ; ++q) correct_load<MASTER == 1 ? 1 : 2, LC>(p, k, b, x, y, z0 + q, ci[b * NZ + q]);
     }
     cb_own<NZ>(src, me, std::make_integer_sequence<int, 2 * NZ>{});
 #pragma unroll
@@ -654,8 +677,8 @@ __device__ __forceinline__ void cb_sites(const SParams &p, const Src &src, int k
         for (int q = 0; q < NZ; ++q) {
             const int i = b * NZ + q;
             const float Bf[3] = {acc[i][0] + p.ext[0], acc[i][1] + p.ext[1], acc[i][2] + p.ext[2]};
-            if constexpr (KIND == 0) predict_update(p, k, b, x, y, z0 + q, me[i], Bf);
-            else correct_finish<MASTER == 1 ? 1 : 2>(p, k, b, x, y, z0 + q, me[i], Bf, ci[i]);
+            if constexpr (KIND == 0) predict_update<LC>(p, k, b, x, y, z0 + q, me[i], Bf);
+            else correct_finish<MASTER == 1 ? 1 : 2, LC>(p, k, b, x, y, z0 + q, me[i], Bf, ci[i]);
         }
 }
 
@@ -672,7 +695,7 @@ __global__ void __launch_bounds__(256) stencil_cells(SParams p) {
     GlobalSrc<LC> src;
     src.base0 = m + (long long)(k * 2 + 0) * p.pbox + own;
     src.base1 = m + (long long)(k * 2 + 1) * p.pbox + own;
-    cb_sites<NSH, NZ, KIND, MASTER>(p, src, k, x, y, z0);
+    cb_sites<NSH, NZ, LC, KIND, MASTER>(p, src, k, x, y, z0);
 }
 
 
@@ -792,7 +815,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) stencil_tma(const __grid_consta
             SmemSrc<TX, TY, NZ, R> src;
 #pragma unroll
             for (int j = 0; j < NZ + 3; ++j) src.pj[j] = cell + ((NZ * i + j) % R) * G::kSlot;
-            cb_sites<NSH, NZ, KIND, MASTER>(p, src, k, x, y, zs + NZ * i);
+            cb_sites<NSH, NZ, LC, KIND, MASTER>(p, src, k, x, y, zs + NZ * i);
         }
     }
     __syncthreads();
@@ -1143,10 +1166,14 @@ static void launch_tma_v(StructuredFast *f, cudaStream_t st, int phase) {
     }
 }
 
+// Two planes per iteration (V = 0) is the faster schedule with the double-single master
+// (fewer shared-memory reads per site); with the FP64 master the FP64 pipe holds the
+// corrector back and the extra warps of V = 1 hide more of it (both measured on the
+// 100^3 alloy).  kernel 3 forces V = 1 throughout.
 template <int NSH, int LC>
 static void launch_tma(StructuredFast *f, cudaStream_t st, int phase) {
     if constexpr (LC != 0) {
-        if (f->kernel == 3) launch_tma_v<NSH, LC, 1>(f, st, phase);
+        if (f->kernel == 3 || f->master == 1) launch_tma_v<NSH, LC, 1>(f, st, phase);
         else launch_tma_v<NSH, LC, 0>(f, st, phase);
     }
 }
