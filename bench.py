@@ -480,7 +480,8 @@ def run_mc(args, world, rank, peak, peak_kind):
 # 19 temperatures 5-30 K x 8 chains (152 chains: 38,912 patch rows per colour, 304
 # tensor-core row tiles = two full waves on 152 SMs), the field chosen by a scan for the
 # largest skyrmion density.
-C3 = dict(L=128, temps=(5.0, 30.0, 19), copies=8, J=1.0, D=0.3, bz_scan=(5.0, 10.0, 15.0, 20.0, 25.0, 30.0),
+C3 = dict(L=128, temps=(5.0, 30.0, 19), copies=8, J=1.0, D=0.3,
+          bz_scan=(5.0, 10.0, 15.0, 20.0, 25.0, 30.0, 35.0, 40.0, 50.0, 60.0),
           scan_chains=16, eta_scale=16.0, therm=20000, snapshots=96, snap_every=50, train_steps=3000,
           train_rows=16384, lr=1e-3)
 
@@ -700,8 +701,8 @@ def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic, traffic_sou
 
 
 PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master"}
-KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_zblock_predict", "stencil_zblock_correct"),
-                2: ("stencil_zblock_predict", "stencil_zblock_correct")}
+KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_tma_predict", "stencil_tma_correct"),
+                2: ("stencil_tma_predict", "stencil_tma_correct")}
 
 
 def oracle_error(lat, w, prec, e0, stream, nsteps=20, seed=5):
