@@ -166,8 +166,8 @@ def measured_peaks():
 # dram__bytes_write.sum, one capture each, not measured by this run): (bytes, how the
 # figure was obtained).  A kernel that has none reports traffic null.
 PROFILED_TRAFFIC = {
-    "stencil_zblock_correct:alloy2m:p1": (1.928e9, "ncu capture of the 64^3 x 8 alloy, scaled by sites x 3.815"),
-    "stencil_zblock_predict:alloy2m:p1": (0.858e9, "ncu capture of the 64^3 x 8 alloy, scaled by sites x 3.815"),
+    "stencil_tma_correct:alloy2m:p2": (1.421e9, "ncu capture at the benchmark size (100^3 x 8 ensembles, one pass)"),
+    "stencil_tma_predict:alloy2m:p2": (0.757e9, "ncu capture at the benchmark size (100^3 x 8 ensembles, one pass)"),
     "mb_sweeps:mc64": (12.8e9, "ncu capture of a 40-sweep launch of the 64-replica table, scaled x 250/40"),
 }
 

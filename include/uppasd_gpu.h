@@ -302,12 +302,13 @@ int uppasd_gpu_mcbatch_set_sweep(uppasd_gpu_mcbatch *b, int64_t sweep);
  * first_id + r of the whole table, so every replica's chain is the same whichever
  * GPU runs it.  Redraws the initial state; call right after create. */
 int uppasd_gpu_mcbatch_set_replica_ids(uppasd_gpu_mcbatch *b, int32_t first_id);
-/* Iteration limit of the replica-group barrier's wait (0 = the default, about a
- * second or more).  A wait that runs past it records an error and its group leaves the
+/* Poll limit of the replica-group barrier's wait (0 = the default, beyond any real
+ * wait).  A wait that runs past it records an error and its group leaves the
  * launch; run/check then return UPPASD_GPU_ESTATE and reset the barrier state, so the
  * batch stays usable (its spins are those the groups had reached).  Whatever the
- * iteration limit, a wait also gives up after about two seconds.  For testing the error
- * path: a limit of 1 makes any group of two or more CTAs give up. */
+ * poll limit, a wait also gives up after about two seconds.  For testing the error path:
+ * a limit of 1 makes a CTA give up at the first poll that finds its group's barrier
+ * incomplete, which a group of two or more CTAs meets within a few barriers. */
 int uppasd_gpu_mcbatch_set_spin_limit(uppasd_gpu_mcbatch *b, int64_t limit);
 /* Replica exchange (the swap step of MonteCarlo/pt_driver.f90:58-367 on the batch):
  * after every launch, replicas holding adjacent temperatures of one size swap

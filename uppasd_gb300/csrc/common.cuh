@@ -97,8 +97,12 @@ __device__ inline void normal3_f32_fast(uint64_t seed, int64_t site, int32_t ens
     Philox4 w = philox_draw(seed, site, ens, step, stream);
     const float k32 = 2.3283064365386963e-10f;
     const float twopi = 6.283185307179586f;
-    float r0 = sqrtf(-2.0f * __logf(fmaf((float)w.x, k32, 0.5f * k32)));
-    float r1 = sqrtf(-2.0f * __logf(fmaf((float)w.z, k32, 0.5f * k32)));
+    // radii as x rsqrt(x) (the approximate reciprocal square root, two instructions);
+    // x is 0 when u rounds to 1, hence the floor inside the rsqrt
+    const float x0 = -2.0f * __logf(fmaf((float)w.x, k32, 0.5f * k32));
+    const float x1 = -2.0f * __logf(fmaf((float)w.z, k32, 0.5f * k32));
+    const float r0 = x0 * rsqrtf(fmaxf(x0, 1e-30f));
+    const float r1 = x1 * rsqrtf(fmaxf(x1, 1e-30f));
     // angles shifted into [-pi, pi] (the approximations' accurate range):
     // cos(2 pi u) = -cos(2 pi (u - 1/2)), sin(2 pi u) = -sin(2 pi (u - 1/2))
     float s0, c0;

@@ -127,11 +127,13 @@ __device__ __forceinline__ bool group_barrier(const MBParams &p, int r, int n) {
         __threadfence();
         const unsigned long long old = atomicAdd(ctr, 1ull);
         const unsigned long long target = (old / (unsigned long long)n + 1ull) * (unsigned long long)n;
-        long long it = 0;
-        const long long t0 = globaltimer_ns();
+        long long it = 0, t0 = 0;
         while (ld_acquire_u64(ctr) < target) {
-            // give up after spin_limit polls or about two seconds, whichever comes first
-            if (++it > p.spin_limit || ((it & 63) == 0 && globaltimer_ns() - t0 > 2000000000LL)) {
+            // give up after spin_limit polls that found the barrier incomplete, or after
+            // about two seconds, whichever comes first (the clock is read from poll 64 on)
+            ++it;
+            if (it == 64) t0 = globaltimer_ns();
+            if (it >= p.spin_limit || (it > 64 && (it & 63) == 0 && globaltimer_ns() - t0 > 2000000000LL)) {
                 atomicExch(p.err, 1);
                 failed = 1;
                 break;
