@@ -40,6 +40,8 @@ class OrcHam(C.Structure):
         ("dm_vect", F64P), ("do_aniso", C.c_int), ("taniso", I32P), ("eaniso", F64P),
         ("kaniso", F64P), ("sb", F64P), ("extfield", F64P),
         ("do_jtensor", C.c_int), ("j_tens", F64P),
+        ("do_dip", C.c_int), ("dip_na", C.c_int), ("dip_n1", C.c_int), ("dip_n2", C.c_int), ("dip_n3", C.c_int),
+        ("dip_cell", F64P), ("dip_bas", F64P), ("dip_alat", C.c_double), ("dip_work", F64P),
     ]
 
 
@@ -123,6 +125,7 @@ def _declare(lib):
     lib.orc_set_threads.argtypes = [C.c_int]
     lib.orc_get_threads.restype = C.c_int
     lib.orc_set_units.argtypes = [C.c_double] * 4
+    lib.orc_dipole_field.argtypes = [C.POINTER(OrcHam), F64P, F64P]
     return lib
 
 
@@ -153,7 +156,9 @@ def _p(a, t=F64P):
 class Oracle:
     """Holds one Hamiltonian and one spin state in the reference's layout."""
 
-    def __init__(self, lat, threads: int = 0, fast: bool = False):
+    def __init__(self, lat, threads: int = 0, fast: bool = False, dipole_alat: float = 0.0):
+        """dipole_alat > 0 adds the brute-force dipole-dipole field (do_dip = 1) with that
+        lattice constant (m), on the lattice's cell and basis."""
         self.lib = load(fast)
         self.lib.orc_set_threads(threads)
         self.lat = lat
@@ -189,6 +194,15 @@ class Oracle:
             h.j_tens = _p(keep(lat.j_tens, np.float64))
         self.extfield = keep(np.broadcast_to(lat.extfield, (M, N, 3)), np.float64)
         h.extfield = _p(self.extfield)
+        if dipole_alat > 0.0:
+            cell, bas = lat.dipole_geometry()
+            h.do_dip = 1
+            h.dip_na = lat.nbasis
+            h.dip_n1, h.dip_n2, h.dip_n3 = lat.cells
+            h.dip_cell = _p(keep(cell, np.float64))
+            h.dip_bas = _p(keep(bas, np.float64))
+            h.dip_alat = float(dipole_alat)
+            h.dip_work = _p(keep(np.zeros((M, N, 3)), np.float64))
         self.ham = h
         self.mmom = keep(np.broadcast_to(lat.mmom, (M, N)), np.float64)
         shape3 = (M, N, 3)
@@ -238,6 +252,12 @@ class Oracle:
         out = [np.zeros(M) for _ in range(5)]
         self.lib.orc_energy(C.byref(self.ham), _p(self.emomM), *[_p(o) for o in out])
         return {"total": out[0], "xc": out[1], "dm": out[2], "ani": out[3], "ext": out[4]}
+
+    def dipole_field(self):
+        """The brute-force dipolar field of the current full moments, (M, N, 3)."""
+        out = np.zeros(self.emom.shape)
+        self.lib.orc_dipole_field(C.byref(self.ham), _p(self.emomM), _p(out))
+        return out
 
     def mavg(self):
         M = self.lat.mensemble

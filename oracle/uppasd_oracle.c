@@ -314,9 +314,68 @@ static void site_field(const orc_ham *h, const double *emomM, int i, int k, doub
     site_field_aniso(h, emomM, i, k, bs, bq);
 }
 
+/* dipoleMatrix (Hamiltonian/dipolecommon.f90:51-84): Q(nu, mu) for the separation Rij
+ * in units of alat; zero below R^2 = 1e-9 */
+static void dipole_matrix(double alat, const double Rij[3], double Q[3][3]) {
+    const double tol = 1e-9;
+    const double fac = (1.0e-7 / (alat * alat * alat)) * ORC_MUB;
+    const double R2 = Rij[0] * Rij[0] + Rij[1] * Rij[1] + Rij[2] * Rij[2];
+    const double Rm5 = pow(R2, -2.5) * fac;
+    for (int mu = 0; mu < 3; ++mu)
+        for (int nu = 0; nu < 3; ++nu) Q[nu][mu] = 0.0;
+    if (R2 > tol) {
+        for (int mu = 0; mu < 3; ++mu) {
+            for (int nu = 0; nu < 3; ++nu) Q[nu][mu] = 3.0 * Rm5 * Rij[nu] * Rij[mu];
+            Q[mu][mu] = Q[mu][mu] - Rm5 * R2;
+        }
+    }
+}
+
+static void dipole_coord(const orc_ham *h, int i, double r[3]) {
+    const int NA = h->dip_na, N1 = h->dip_n1, N2 = h->dip_n2;
+    const int I0 = i % NA, c = i / NA;
+    const int I1 = c % N1, I2 = (c / N1) % N2, I3 = c / (N1 * N2);
+    for (int q = 0; q < 3; ++q)
+        r[q] = I1 * h->dip_cell[q] + I2 * h->dip_cell[3 + q] + I3 * h->dip_cell[6 + q] + h->dip_bas[3 * I0 + q];
+}
+
+/* dipolar_field (dipolemanager.f90:223-243) for every (atom, ensemble), Qdip set up as
+ * setup_qdip does (dipolecommon.f90:114-159): Qdip(:,:,j,i) = dipoleMatrix(r_i - r_j),
+ * zero on the diagonal */
+void orc_dipole_field(const orc_ham *h, const double *emomM, double *out) {
+    const int N = h->natom, M = h->mensemble;
+#pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
+    for (int k = 0; k < M; ++k)
+        for (int i = 0; i < N; ++i) {
+            double ri[3], f[3] = {0.0, 0.0, 0.0};
+            dipole_coord(h, i, ri);
+            for (int j = 0; j < N; ++j) {
+                double rj[3], R[3], Q[3][3];
+                dipole_coord(h, j, rj);
+                for (int q = 0; q < 3; ++q) R[q] = ri[q] - rj[q];
+                dipole_matrix(h->dip_alat, R, Q);
+                if (j == i)
+                    for (int a = 0; a < 3; ++a)
+                        for (int b = 0; b < 3; ++b) Q[a][b] = 0.0;
+                const double m1 = V3(emomM, 0, j, k, N), m2 = V3(emomM, 1, j, k, N), m3 = V3(emomM, 2, j, k, N);
+                for (int nu = 0; nu < 3; ++nu) f[nu] = f[nu] + Q[0][nu] * m1 + Q[1][nu] * m2 + Q[2][nu] * m3;
+            }
+            for (int nu = 0; nu < 3; ++nu) V3(out, nu, i, k, N) = f[nu];
+        }
+}
+
 double orc_effective_field(const orc_ham *h, const double *emomM, double *beff) {
     const int N = h->natom, M = h->mensemble;
     double energy = 0.0;
+    if (h->do_dip) {
+        /* the dipolar field first, with its energy (dipolemanager.f90:147-158) */
+        orc_dipole_field(h, emomM, h->dip_work);
+        for (int k = 0; k < M; ++k)
+            for (int i = 0; i < N; ++i)
+                energy = energy - 0.5 * (V3(h->dip_work, 0, i, k, N) * V3(emomM, 0, i, k, N) +
+                                         V3(h->dip_work, 1, i, k, N) * V3(emomM, 1, i, k, N) +
+                                         V3(h->dip_work, 2, i, k, N) * V3(emomM, 2, i, k, N));
+    }
 #pragma omp parallel for collapse(2) schedule(static) reduction(+ : energy) num_threads(orc_get_threads())
     for (int k = 0; k < M; ++k) {
         for (int i = 0; i < N; ++i) {
@@ -326,7 +385,8 @@ double orc_effective_field(const orc_ham *h, const double *emomM, double *beff) 
             for (int c = 0; c < 3; ++c) {
                 double ext = V3(h->extfield, c, i, k, N);
                 double b2 = bq[c] + ext + 0.0;   /* beff2 = beff_q + external + time_external */
-                V3(beff, c, i, k, N) = 0.0 + bs[c] + b2;
+                const double bd = h->do_dip ? V3(h->dip_work, c, i, k, N) : 0.0;
+                V3(beff, c, i, k, N) = bd + bs[c] + b2;
                 tf[c] = 0.5 * (bs[c] + 2.0 * bq[c] + 2.0 * ext + 0.0);
             }
             energy = energy - V3(emomM, 0, i, k, N) * tf[0] - V3(emomM, 1, i, k, N) * tf[1] -

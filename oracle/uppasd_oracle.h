@@ -92,7 +92,22 @@ typedef struct {
      * with do_jtensor == 1 it replaces ncoup in the field and energies. */
     int do_jtensor;
     const double  *j_tens;     /* (3, 3, max_no_neigh, nham) */
+    /* dipole-dipole field (do_dip = 1, brute force: Hamiltonian/dipolemanager.f90:147-158
+     * with the tensor of dipolecommon.f90:51-84); the supercell's geometry: atom
+     * i = I0 + NA (I1 + N1 (I2 + N2 I3)) (0-based) at I1 C1 + I2 C2 + I3 C3 + Bas(I0), in
+     * units of alat (m); dip_work (3, natom, mensemble) receives the dipolar field. */
+    int do_dip;
+    int dip_na, dip_n1, dip_n2, dip_n3;
+    const double *dip_cell;    /* (3, 3): column a is C_{a+1} */
+    const double *dip_bas;     /* (3, NA) */
+    double dip_alat;
+    double *dip_work;
 } orc_ham;
+
+/* The dipolar field of every atom from the full moments emomM (3, natom, mensemble), into
+ * out (same layout): B_i = sum_j Q(r_i - r_j) m_j over all atoms j != i, no periodic
+ * images, Q(R) = 1e-7 mub / alat^3 (3 R R^T - R^2 I) / R^5 (dipoleMatrix). */
+void orc_dipole_field(const orc_ham *h, const double *emomM, double *out);
 
 /* effective_field_full (hamiltonianactions.f90:108-252).  Returns energy in mRy
  * (the routine's own energy*mub/mry).  beff is (3,natom,mensemble). */

@@ -91,6 +91,15 @@ class Lattice:
         frac = np.stack([c % n1, (c // n1) % n2, c // (n1 * n2)], axis=1).astype(np.float64)
         return frac @ cell + basis[b]
 
+    def dipole_geometry(self):
+        """(cell (3, 3), basis (nbasis, 3)): rows of `cell` are the cell vectors C1, C2, C3,
+        rows of `basis` the basis positions, Cartesian in units of the lattice constant
+        (the geometry the dipolar field is summed over)."""
+        cell = np.asarray(self.meta.get("cell", np.eye(3)), dtype=np.float64)
+        basis = np.asarray(self.meta.get("basis", _DEFAULT_BASIS.get(self.nbasis, np.zeros((1, 3)))),
+                           dtype=np.float64)
+        return np.ascontiguousarray(cell), np.ascontiguousarray(basis)
+
     def with_ensembles(self, mensemble: int) -> "Lattice":
         """Same Hamiltonian, `mensemble` copies of the moment arrays."""
         lat = Lattice(**{k: getattr(self, k) for k in self.__dataclass_fields__})
