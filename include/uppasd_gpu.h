@@ -136,6 +136,27 @@ int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *s, double relaxtime);
  * NULL switches back to ncoup.  -7 on the structured path (precision >= 1). */
 int uppasd_gpu_set_jtensor(uppasd_gpu_sim *s, const double *j_tens);
 
+/* Dipole-dipole field (input keyword do_dip, Hamiltonian/dipolemanager.f90:54-113).
+ * Added first to every effective field of the FP64 LLG step and of get_field, its
+ * energy -1/2 m.B_dip per atom to the total energy (Hamiltonian/energy.f90:286-291,
+ * :372-374).  Open boundaries: every pair of the supercell, no periodic images.
+ *   do_dip = 0  off;
+ *   do_dip = 1  brute force, the tensor of dipoleMatrix (dipolecommon.f90:51-84) for every
+ *               pair, as setup_qdip (dipolecommon.f90:114-143) builds it from coord
+ *               (3, natom), in units of alat; with coord NULL the coordinates are those of
+ *               the cell grid below;
+ *   do_dip = 3  FFT (geometrical_DFFT_wrapper, fftdipole_fftw.f90:51-78): the same sum as a
+ *               convolution over the cell grid zero-padded to 2 N - 1 cells per axis;
+ *               needs na, n1, n2, n3 with na*n1*n2*n3 == natom, site I0 + NA (I1 + N1 (I2 +
+ *               N2 I3)) at I1 C1 + I2 C2 + I3 C3 + Bas(I0); cell holds the rows C1, C2, C3
+ *               and bas (3, na) the basis, both Cartesian in units of alat.  cuFFT is
+ *               loaded at run time: -6 when it cannot be.
+ * alat in metres (the field is 1e-7 mub / alat^3 (3 R R^T - R^2 I) / R^5 . m).  Only on
+ * the FP64 path (precision 0; -7 otherwise); Monte Carlo and the learned moves return -7
+ * while it is on. */
+int uppasd_gpu_set_dipole(uppasd_gpu_sim *s, int32_t do_dip, double alat, const double *coord, int32_t na,
+                          int32_t n1, int32_t n2, int32_t n3, const double *cell, const double *bas);
+
 /* Caller-provided N(0,1) numbers for the next `nsteps` steps, laid out as
  * nsteps consecutive (3, natom, mensemble) blocks (the order the reference's
  * fill_rngarray draws them).  Selects gpu_rng = 1 until exhausted. */

@@ -1276,9 +1276,11 @@ void orc_energy(const orc_ham *h, const double *emomM, double *e_tot, double *e_
                 double *e_ani, double *e_ext) {
     const int N = h->natom, M = h->mensemble;
     const double fcinv = ORC_MUB / ORC_MRY;
+    /* the dipolar field of the same moments (energy.f90:154-167) */
+    if (h->do_dip) orc_dipole_field(h, emomM, h->dip_work);
     for (int k = 0; k < M; ++k) {
-        double exc = 0.0, edm = 0.0, eani = 0.0, eext = 0.0;
-#pragma omp parallel for schedule(static) reduction(+ : exc, edm, eani, eext) num_threads(orc_get_threads())
+        double exc = 0.0, edm = 0.0, eani = 0.0, eext = 0.0, edip = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : exc, edm, eani, eext, edip) num_threads(orc_get_threads())
         for (int i = 0; i < N; ++i) {
             const double *mi = &V3(emomM, 0, i, k, N);
             int ih = h->aham[i] - 1;
@@ -1316,9 +1318,15 @@ void orc_energy(const orc_ham *h, const double *emomM, double *e_tot, double *e_
             double be[3];
             for (int cc = 0; cc < 3; ++cc) be[cc] = 0.0 + V3(h->extfield, cc, i, k, N);
             eext = eext + (-1.0 * (mi[0] * be[0] + mi[1] * be[1] + mi[2] * be[2]));
+            /* update_ene(emomM, bfield_dip, 0.5) (energy.f90:286-291) */
+            if (h->do_dip) {
+                const double *bd = &V3(h->dip_work, 0, i, k, N);
+                edip = edip + (-0.5 * (mi[0] * bd[0] + mi[1] * bd[1] + mi[2] * bd[2]));
+            }
         }
-        double xc = exc / N, dm = edm / N, an = eani / N, ex = eext / N;
-        double tot = xc + dm + ex + an;
+        double xc = exc / N, dm = edm / N, an = eani / N, ex = eext / N, dp = edip / N;
+        /* ene_xc + ene_dm + ene_ext + ene_ani + ene_dip (energy.f90:372-374) */
+        double tot = xc + dm + ex + an + dp;
         if (e_xc) e_xc[k] = xc * fcinv;
         if (e_dm) e_dm[k] = dm * fcinv;
         if (e_ani) e_ani[k] = an * fcinv;

@@ -56,6 +56,8 @@ SIGNATURES = {
     "uppasd_gpu_set_temperature": [C.c_void_p, F64P],
     "uppasd_gpu_set_step": [C.c_void_p, C.c_int64],
     "uppasd_gpu_set_jtensor": [C.c_void_p, F64P],
+    "uppasd_gpu_set_dipole": [C.c_void_p, C.c_int32, C.c_double, F64P, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                              F64P, F64P],
     "uppasd_gpu_set_relaxtime": [C.c_void_p, C.c_double],
     "uppasd_gpu_set_units": [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double],
     "uppasd_gpu_set_perp": [C.c_void_p, C.c_int32],

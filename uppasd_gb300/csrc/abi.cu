@@ -417,6 +417,7 @@ void destroy(Sim &s) {
     if (s.graph) cudaGraphExecDestroy(s.graph);
     structured_free(s);
     mixed_free(s);
+    dipole_free(s);
     HamDev &h = s.ham;
     void *ptrs[] = {h.nlist, h.nsize, h.aham, h.ncoup, h.jt, h.dmlist, h.dmsize, h.dmx, h.dmy, h.dmz, h.taniso,
                     h.eax, h.eay, h.eaz, h.k1, h.k2, h.sb, s.llg.lambda, s.llg.temp, s.llg.landeg, s.llg.mmom,
@@ -455,7 +456,8 @@ int run_steps(Sim &s, int64_t n) {
     } else {
         square_mirror_stale(s);
     }
-    if (!s.graph && n >= G) {
+    // the FFT form of the dipolar field issues cuFFT launches, kept out of the captured graph
+    if (!s.graph && n >= G && s.ham.do_dip != 3) {
         cudaGraph_t g;
         UPPASD_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
         for (int j = 0; j < G; ++j)
@@ -718,6 +720,48 @@ int uppasd_gpu_set_jtensor(uppasd_gpu_sim *w, const double *j_tens) {
     h.do_jtensor = 1;
     if (s.precision == 3) return uppasd::mixed_coefficients(s);
     return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_set_dipole(uppasd_gpu_sim *w, int32_t do_dip, double alat, const double *coord, int32_t na,
+                          int32_t n1, int32_t n2, int32_t n3, const double *cell, const double *bas) {
+    if (!w || (do_dip != 0 && do_dip != 1 && do_dip != 3)) {
+        uppasd::set_error("set_dipole: do_dip 0 (off), 1 (brute force) or 3 (FFT)");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    if (do_dip) {
+        if (s.precision != 0) {
+            uppasd::set_error("set_dipole: the dipolar field runs on the FP64 path (precision 0)");
+            return UPPASD_GPU_EUNSUPPORTED;
+        }
+        if (!(alat > 0.0) || !std::isfinite(alat)) {
+            uppasd::set_error("set_dipole: alat must be finite and > 0");
+            return UPPASD_GPU_EINVAL;
+        }
+        const bool grid = do_dip == 3 || !coord;
+        if (grid && (!cell || !bas || na < 1 || n1 < 1 || n2 < 1 || n3 < 1 ||
+                     (int64_t)na * n1 * n2 * n3 != s.ham.natom)) {
+            uppasd::set_error("set_dipole: need coord, or cell, bas and NA * N1 * N2 * N3 == natom");
+            return UPPASD_GPU_EINVAL;
+        }
+        auto finite = [](const double *v, size_t n) {
+            for (size_t q = 0; q < n; ++q)
+                if (!std::isfinite(v[q])) return false;
+            return true;
+        };
+        if (grid ? !(finite(cell, 9) && finite(bas, 3 * (size_t)na)) : !finite(coord, 3 * (size_t)s.ham.natom)) {
+            uppasd::set_error("set_dipole: non-finite coordinate");
+            return UPPASD_GPU_EINVAL;
+        }
+        // the padded grids index in 32-bit FFT dimensions
+        if (do_dip == 3 && (int64_t)(2 * n1 - 1) * (2 * n2 - 1) * (2 * n3 - 1) > (int64_t)1 << 31) {
+            uppasd::set_error("set_dipole: padded grid too large");
+            return UPPASD_GPU_EINVAL;
+        }
+    }
+    uppasd::drop_graph(s);
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return uppasd::dipole_setup(s, do_dip, alat, do_dip == 1 ? coord : nullptr, na, n1, n2, n3, cell, bas);
 }
 
 int uppasd_gpu_set_step(uppasd_gpu_sim *w, int64_t step) {

@@ -113,9 +113,16 @@ __device__ __forceinline__ void site_field(const HamDev &h, const Vec3D &m, int 
         }
     }
     if (h.do_aniso) aniso_field(h, i, m.x[off + i], m.y[off + i], m.z[off + i], bs, bq);
-    B[0] = 0.0 + bs[0] + (bq[0] + h.ext.x[off + i] + 0.0);
-    B[1] = 0.0 + bs[1] + (bq[1] + h.ext.y[off + i] + 0.0);
-    B[2] = 0.0 + bs[2] + (bq[2] + h.ext.z[off + i] + 0.0);
+    // beff = beff1 + beff2 with the dipolar field first in beff1 (hamiltonianactions.f90:173-181)
+    double bd[3] = {0.0, 0.0, 0.0};
+    if (h.do_dip) {
+        bd[0] = h.dip.x[off + i];
+        bd[1] = h.dip.y[off + i];
+        bd[2] = h.dip.z[off + i];
+    }
+    B[0] = bd[0] + bs[0] + (bq[0] + h.ext.x[off + i] + 0.0);
+    B[1] = bd[1] + bs[1] + (bq[1] + h.ext.y[off + i] + 0.0);
+    B[2] = bd[2] + bs[2] + (bq[2] + h.ext.z[off + i] + 0.0);
 }
 
 }  // namespace uppasd

@@ -837,6 +837,10 @@ PatchGeom geom(const uppasd_gpu_proposal *p, int colour) {
 // One learned sweep (the four patch colours) enqueued on `st`; capturable.
 int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, bool per_ensemble, cudaStream_t st) {
     Sim &s = p->sim->s;
+    if (s.ham.do_dip) {
+        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     const long long nt = (long long)rows * 64;
     int rc;
     for (int c = 0; c < 4; ++c) {

@@ -432,10 +432,20 @@ __global__ void __launch_bounds__(256) llg_correct(StepArgs a) {
     a.eM.z[o] = out[2] * mm;
 }
 
+// with dipoles on, the dipolar field of the moments each half step reads is enqueued
+// before it (the predictor's from emomM, the corrector's from the predictor's mpM)
 template <int ALG>
-static void launch_pair(Sim &s, const StepArgs &a, int grid, int phase) {
-    if (phase & 1) llg_predict<ALG><<<grid, 256, 0, s.stream>>>(a);
-    if (phase & 2) llg_correct<ALG><<<grid, 256, 0, s.stream>>>(a);
+static int launch_pair(Sim &s, const StepArgs &a, int grid, int phase) {
+    int rc;
+    if (phase & 1) {
+        if (s.ham.do_dip && (rc = dipole_field(s, s.eM))) return rc;
+        llg_predict<ALG><<<grid, 256, 0, s.stream>>>(a);
+    }
+    if (phase & 2) {
+        if (s.ham.do_dip && (rc = dipole_field(s, s.pM))) return rc;
+        llg_correct<ALG><<<grid, 256, 0, s.stream>>>(a);
+    }
+    return UPPASD_GPU_OK;
 }
 
 int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
@@ -465,15 +475,17 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase) {
     a.mpast = s.mpast;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const int grid = (int)((n + 255) / 256);
+    int rc;
     switch (s.llg.sdealgh) {
-    case 1: launch_pair<1>(s, a, grid, phase); break;
-    case 4: launch_pair<4>(s, a, grid, phase); break;
-    case 5: launch_pair<5>(s, a, grid, phase); break;
-    case 6: launch_pair<6>(s, a, grid, phase); break;
-    case 7: launch_pair<7>(s, a, grid, phase); break;
-    case 11: launch_pair<11>(s, a, grid, phase); break;
+    case 1: rc = launch_pair<1>(s, a, grid, phase); break;
+    case 4: rc = launch_pair<4>(s, a, grid, phase); break;
+    case 5: rc = launch_pair<5>(s, a, grid, phase); break;
+    case 6: rc = launch_pair<6>(s, a, grid, phase); break;
+    case 7: rc = launch_pair<7>(s, a, grid, phase); break;
+    case 11: rc = launch_pair<11>(s, a, grid, phase); break;
     default: set_error("unsupported SDEalgh"); return UPPASD_GPU_EUNSUPPORTED;
     }
+    if (rc) return rc;
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }

@@ -177,6 +177,10 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
 }
 
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps, const double *tk) {
+    if (s.ham.do_dip) {
+        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     square_mirror_stale(s);
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");

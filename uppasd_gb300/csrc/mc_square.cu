@@ -189,6 +189,10 @@ namespace uppasd {
 // Structured heat-bath sweeps; betak (muB / (kB T) per ensemble, on the device) or
 // null for the single `temperature`.
 int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t nsweeps) {
+    if (s.ham.do_dip) {
+        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     if (structured(s)) {
         set_error("mc_run_square: needs the FP64 state (precision 0 or 3)");
         return UPPASD_GPU_EUNSUPPORTED;

@@ -12,7 +12,7 @@
 
 namespace uppasd {
 
-enum { kRedMx = 0, kRedMy, kRedMz, kRedXc, kRedDm, kRedAni, kRedExt, kRedCount = 8 };
+enum { kRedMx = 0, kRedMy, kRedMz, kRedXc, kRedDm, kRedAni, kRedExt, kRedDip, kRedCount = 8 };
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -25,7 +25,7 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
     const int k = blockIdx.y;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const size_t off = (size_t)k * N;
-    double v[7] = {0, 0, 0, 0, 0, 0, 0};
+    double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (i < N) {
         double mi[3] = {m.x[off + i], m.y[off + i], m.z[off + i]};
         v[0] = mi[0];
@@ -66,11 +66,13 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
         }
         double be[3] = {0.0 + h.ext.x[off + i], 0.0 + h.ext.y[off + i], 0.0 + h.ext.z[off + i]};
         v[6] = -1.0 * (mi[0] * be[0] + mi[1] * be[1] + mi[2] * be[2]);
+        // dipolar energy with the field evaluated for m (energy.f90:286-291)
+        if (h.do_dip) v[7] = -0.5 * (mi[0] * h.dip.x[off + i] + mi[1] * h.dip.y[off + i] + mi[2] * h.dip.z[off + i]);
     }
-    __shared__ double part[8][7];
+    __shared__ double part[8][8];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int q = 0; q < 7; ++q) {
+    for (int q = 0; q < 8; ++q) {
         double w = warp_sum(v[q]);
         if (lane == 0) part[wid][q] = w;
     }
@@ -78,7 +80,7 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
     if (wid == 0) {
         const int nw = blockDim.x >> 5;
 #pragma unroll
-        for (int q = 0; q < 7; ++q) {
+        for (int q = 0; q < 8; ++q) {
             double w = lane < nw ? part[lane][q] : 0.0;
             w = warp_sum(w);
             if (lane == 0) atomicAdd(&red[k * kRedCount + q], w);
@@ -89,6 +91,10 @@ __global__ void __launch_bounds__(256) obs_kernel(HamDev h, Vec3D m, double *red
 int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src, double *terms_h) {
     const int N = s.ham.natom, M = s.ham.mensemble;
     const Vec3D &m = src ? *src : s.eM;
+    if (s.ham.do_dip) {
+        int rc = dipole_field(s, m);
+        if (rc) return rc;
+    }
     UPPASD_CUDA_TRY(cudaMemsetAsync(s.red, 0, sizeof(double) * kRedCount * M, s.stream));
     dim3 grid((N + 255) / 256, M);
     obs_kernel<<<grid, 256, 0, s.stream>>>(s.ham, m, s.red);
@@ -111,10 +117,11 @@ int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const 
         }
         if (mabs_h) mabs_h[k] = sqrt(r[kRedMx] * r[kRedMx] + r[kRedMy] * r[kRedMy] + r[kRedMz] * r[kRedMz]) / N;
         double xc = r[kRedXc] / N, dm = r[kRedDm] / N, an = r[kRedAni] / N, ex = r[kRedExt] / N;
-        if (energy_h) energy_h[k] = (xc + dm + ex + an) * fcinv;
+        const double dp = r[kRedDip] / N;
+        if (energy_h) energy_h[k] = (xc + dm + ex + an + dp) * fcinv;
         if (terms_h) {
             double *t = terms_h + 5 * (size_t)k;
-            t[0] = (xc + dm + ex + an) * fcinv;
+            t[0] = (xc + dm + ex + an + dp) * fcinv;
             t[1] = xc * fcinv;
             t[2] = an * fcinv;
             t[3] = dm * fcinv;
@@ -142,6 +149,10 @@ int field_to_host(Sim &s, double *beff_h) {
     const size_t n = (size_t)s.ham.natom * s.ham.mensemble;
     double *d = stage_buffer(s);
     if (!d) return UPPASD_GPU_ENOMEM;
+    if (s.ham.do_dip) {
+        int rc = dipole_field(s, s.eM);
+        if (rc) return rc;
+    }
     field_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.ham, s.eM, d);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaMemcpyAsync(beff_h, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, s.stream);

@@ -44,6 +44,10 @@ struct HamDev {
     // the caller's physical constants (fortrandata_setconstants_ passes gama, k_bolt and
     // mub): SI by default, all 1 under aunits = 'Y' (Input/inputhandler.f90:1685-1704)
     double gama = kGama, kbolt = kKbolt, mub = kMub, mry = kMry;
+    // dipole-dipole field (do_dip 1 brute force, 3 FFT): dip holds the field of the
+    // moments the caller last evaluated it for, added first in site_field
+    int do_dip = 0;
+    Vec3D dip;                  // [mensemble][natom]
 };
 
 struct LlgDev {
@@ -61,6 +65,7 @@ struct LlgDev {
     int64_t *d_step = nullptr;     // device step counter (read by kernels, advanced in-stream)
 };
 
+struct DipoleDev;       // dipolar field state (dipole.cu)
 struct StructuredFast;  // mixed-precision structured-lattice path (llg_stencil.cu)
 
 // precision 3 (llg_mixed.cu): FP32 gather over the caller's neighbour lists with
@@ -137,6 +142,7 @@ struct Sim {
     float4 *sqm = nullptr;
     int sqm_valid = 0;
     MixedDev mix;
+    DipoleDev *dip = nullptr;
     // (3, natom, mensemble) staging array of the host transfers, kept between calls
     // measured runs: two device snapshot pairs (emom, emomM in the reference layout), their
     // page-locked host copies, a copy stream and the events that order them
@@ -170,6 +176,13 @@ int llg_generic_step(Sim &s, int64_t step_offset, int phase = 3);
 int observables(Sim &s, double *mvec_h, double *mabs_h, double *energy_h, const Vec3D *src,
                 double *terms_h = nullptr);
 int field_to_host(Sim &s, double *beff_h);
+// dipole.cu: set up (mode 0 removes), free, and enqueue the field of the full moments m
+// into ham.dip
+// coord (3, natom) or nullptr for the cell grid of na, n1..n3, cell (rows C1..C3), bas
+int dipole_setup(Sim &s, int mode, double alat, const double *coord, int na, int n1, int n2, int n3,
+                 const double *cell, const double *bas);
+void dipole_free(Sim &s);
+int dipole_field(Sim &s, const Vec3D &m);
 // mc.cu
 // tk: temperature per ensemble on the device (nullptr: `temperature` for all)
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps, const double *tk = nullptr);

@@ -105,6 +105,29 @@ class GpuSimulation:
             raise ValueError(f"j_tens must be (nham, mnn, 3, 3), got {jt.shape}")
         _lib.call("uppasd_gpu_set_jtensor", self._h, _ptr(jt))
 
+    def set_dipole(self, do_dip: int, alat: float = 2.87e-10, coord: Optional[np.ndarray] = None):
+        """Dipole-dipole field (input keyword do_dip): 0 off, 1 brute force, 3 FFT.
+
+        alat is the lattice constant in metres.  Brute force sums over `coord` (natom, 3),
+        Cartesian in units of alat, when given, else over the lattice's cell grid
+        (Lattice.dipole_geometry); the FFT form always uses the cell grid.  FP64 path only.
+        """
+        if do_dip == 0:
+            _lib.call("uppasd_gpu_set_dipole", self._h, 0, 0.0, None, 0, 0, 0, 0, None, None)
+            return
+        cell, bas = self.lat.dipole_geometry()
+        n1, n2, n3 = (int(v) for v in self.lat.cells)
+        cell = np.ascontiguousarray(cell, dtype=np.float64)
+        bas = np.ascontiguousarray(bas, dtype=np.float64)
+        cp = None
+        if coord is not None:
+            coord = np.ascontiguousarray(coord, dtype=np.float64)
+            if coord.shape != (self.lat.natom, 3):
+                raise ValueError(f"coord must be (natom, 3), got {coord.shape}")
+            cp = _ptr(coord)
+        _lib.call("uppasd_gpu_set_dipole", self._h, int(do_dip), float(alat), cp, int(self.lat.nbasis), n1, n2, n3,
+                  _ptr(cell), _ptr(bas))
+
     # -- lifecycle --
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
