@@ -796,6 +796,68 @@ def run_fp64_config(key, world, rank, stream, peak, peak_kind, cpu):
     return res
 
 
+# LLG with the dipole-dipole field on the FP64 path: (bcc cells per axis, do_dip)
+DIPOLE_CASES = [(20, 1), (20, 3), (64, 3), (100, 3)]
+DIPOLE_ALAT = 2.87e-10
+
+
+def run_dipole(world, rank, stream, cpu):
+    """Depondt steps (bcc ferromagnet J1=1.3 J2=0.7 mRy, 300 K, one ensemble) without and with
+    the dipolar field, timed with CUDA events on the library's stream; the difference over
+    two field evaluations per step is the field's cost.  The field of the 20^3 lattice is
+    checked against the oracle's brute-force sum, which is also timed as the CPU figure."""
+    import torch
+    from uppasd_gb300 import lattice
+
+    w = dict(solver=5, dt=1e-16, damping=0.1, temp=300.0)
+    cases = []
+    field_err = {}
+    for L, mode in DIPOLE_CASES:
+        lat = lattice.bcc(L, [1.3, 0.7], 2.2)
+        e0 = random_state(1, lat.natom, seed=31)
+        sim = _make_sim(lat, w, 0, 900 + rank, e0)
+        sim.set_stream(stream.cuda_stream)
+        n = 32 if lat.natom <= 20000 else 16
+        ms0 = _time_steps(sim, stream, n, 3, world)
+        sim.put_moments(e0)
+        sim.set_dipole(mode, DIPOLE_ALAT)
+        if L == 20:
+            b = sim.get_fields()
+            field_err[mode] = b
+        ms1 = _time_steps(sim, stream, n, 3, world)
+        sim.close()
+        torch.cuda.synchronize()
+        field_ms = (ms1 - ms0) / n / 2
+        cases.append({"cells": L, "atoms": lat.natom, "do_dip": mode, "steps": n,
+                      "ms_per_step_without": ms0 / n, "ms_per_step_with": ms1 / n,
+                      "field_ms_per_evaluation": field_ms,
+                      "atom_steps_per_s_with": lat.natom * n * world / (ms1 * 1e-3),
+                      "field_evaluations_per_s": 1e3 / field_ms if field_ms > 0 else None})
+    res = {"workload": "bcc ferromagnet with the dipole-dipole field (alat 2.87 A), FP64 path, Depondt, 300 K",
+           "cases": cases, "launches_per_field": {"1": 1, "3": "memset + pad + 2 cuFFT + multiply + unpad"}}
+    if rank == 0:
+        from oracle import pyoracle as po
+
+        lat = lattice.bcc(20, [1.3, 0.7], 2.2)
+        e0 = random_state(1, lat.natom, seed=31)
+        o = po.Oracle(lat, threads=os.cpu_count() or 1, fast=True, dipole_alat=DIPOLE_ALAT)
+        o.set_moments(e0)
+        ref_b, _ = o.field()
+        # relative to the largest dipolar field component (the exchange field is ~100x larger)
+        scale = float(np.max(np.abs(o.dipole_field())))
+        res["field_error_vs_oracle"] = {str(m): float(np.max(np.abs(b - ref_b)) / scale) for m, b in field_err.items()}
+        res["field_error_note"] = "max |B_gpu - B_oracle| over the full field / max |B_dip|, 20^3 bcc"
+        if cpu:
+            t0 = time.perf_counter()
+            o.dipole_field()
+            dt = time.perf_counter() - t0
+            res["cpu_baseline"] = {"value": 1.0 / dt, "unit": "field evaluations/s", "cores": o.lib.orc_get_threads(),
+                                   "kind": "port",
+                                   "sample": "one brute-force dipolar field of the 20^3 bcc lattice (16,000 atoms), "
+                                             "oracle built -O3, OpenMP over sites"}
+    return res
+
+
 def run_gb300(args, w):
     import torch
 
@@ -930,6 +992,9 @@ def run_gb300(args, w):
     if not args.no_configs:
         for key in FP64_CONFIGS:
             configs[key] = run_fp64_config(key, world, rank, stream, peak, peak_kind, not args.no_cpu_baseline)
+    dipole = None
+    if not args.no_dipole:
+        dipole = run_dipole(world, rank, stream, not args.no_cpu_baseline)
     mc = None
     if not args.no_mc:
         mc = run_mc(args, world, rank, peak, peak_kind)
@@ -968,6 +1033,7 @@ def run_gb300(args, w):
         "variants": variants,
         "mc": mc,
         "mc_learned": c3,
+        "dipole": dipole,
     }
     print(json.dumps(line), flush=True)
 
@@ -988,6 +1054,7 @@ def main():
     ap.add_argument("--no-mc", action="store_true", help="skip the batched Monte Carlo section")
     ap.add_argument("--no-configs", action="store_true", help="skip the configured FP64 runs (bcc16k, square256)")
     ap.add_argument("--no-oracle-error", action="store_true", help="skip the FP64-oracle error of the headline")
+    ap.add_argument("--no-dipole", action="store_true", help="skip the dipole-dipole field runs")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
     ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
     ap.add_argument("--c3-profile", action="store_true",

@@ -35,7 +35,7 @@ UNITS = [
     ("tc_host.cu", []),
     ("learned.cu", []),
     ("mc_square.cu", []),
-    ("dipole.cu", ["--fmad=false"]),
+    ("dipole.cu", []),
 ]
 
 
