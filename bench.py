@@ -905,18 +905,26 @@ def run_gb300(args, w):
     host = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
     host_out = torch.empty((lat.mensemble, lat.natom, 3), dtype=torch.float64, pin_memory=True).numpy()
     host[...] = e0
-    sim.put_moments(host)
-    sim.evolve(inner)
-    sim.get_moments(out=host_out)
+    # one sd_run_io call per block: the block's input copied in, `inner` steps, the result
+    # copied out; on the structured path the ensemble groups' copies overlap the other
+    # groups' steps
+    sim.run_io(host, inner, host_out)
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.e2e_rounds)):
+        sim.run_io(host, inner, host_out)
+    torch.cuda.synchronize()
+    e2e_s = dist_max(time.perf_counter() - t0, world)
+    e2e_val = nspin * inner * max(1, args.e2e_rounds) * world / e2e_s
+    # the same blocks as three calls in turn (put_moments, sd_run, get_moments)
     t0 = time.perf_counter()
     for _ in range(max(1, args.e2e_rounds)):
         sim.put_moments(host)
         sim.evolve(inner)
         sim.get_moments(out=host_out)
     torch.cuda.synchronize()
-    e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e_val = nspin * inner * max(1, args.e2e_rounds) * world / e2e_s
+    seq_s = dist_max(time.perf_counter() - t0, world)
+    e2e_seq = nspin * inner * max(1, args.e2e_rounds) * world / seq_s
     variants = {}
     if not args.no_variants:
         # the same blocks of `inner` steps with the state handed to the host after each
@@ -1023,8 +1031,11 @@ def run_gb300(args, w):
         "e2e": {"value": e2e_val, "unit": "atom-steps/s", "h2d_bytes_per_step": host.nbytes / inner,
                 "d2h_bytes_per_step": host.nbytes / inner, "inner_steps_per_call": inner,
                 "bytes_per_call": {"h2d": host.nbytes, "d2h": host.nbytes},
-                "note": "put_moments(pinned host) + sd_run(inner steps) + get_moments(pinned host) per e2e call; "
-                        "the per-step bytes are one call's copies over its steps"},
+                "note": "one sd_run_io call per block (emom in from pinned host memory, inner steps, emom out "
+                        "to pinned host memory; the ensemble groups' copies overlap the other groups' steps); "
+                        "the per-step bytes are one call's copies over its steps",
+                "sequential_calls": {"value": e2e_seq, "unit": "atom-steps/s",
+                                     "note": "put_moments + sd_run + get_moments in turn, same blocks and bytes"}},
         "oracle_error": oracle_err,
         "configs": configs,
         "clocks": clk.summary(),

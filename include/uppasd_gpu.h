@@ -165,6 +165,15 @@ int uppasd_gpu_set_noise(uppasd_gpu_sim *s, const double *normals, int64_t nstep
 /* nsteps full LLG steps (field, predictor, field, corrector, moment update). */
 int uppasd_gpu_sd_run(uppasd_gpu_sim *s, int64_t nsteps);
 
+/* One block of the reference's step loop from and to host arrays: the same result as
+ * put_moments(emom_in) + sd_run(nsteps) + get_moments(emom_out, emomM_out), any of the
+ * three arrays NULL to skip it.  On the structured path (precision 1, 2) with
+ * mensemble > 1 and page-locked arrays, the ensembles are split into up to eight groups,
+ * each copied in, stepped and copied out on its own stream, so that one group's host
+ * copies run while the others step; otherwise the three calls run in turn. */
+int uppasd_gpu_sd_run_io(uppasd_gpu_sim *s, const double *emom_in, int64_t nsteps, double *emom_out,
+                         double *emomM_out);
+
 /* Measurement callback: the state after `step` steps, emom and emomM in the reference
  * layout (3, natom, mensemble), library-owned host memory valid during the call.  A
  * nonzero return stops the run. */

@@ -114,3 +114,39 @@ def test_structured_observables_and_mc_roundtrip():
     e2 = sim.get_moments()
     assert np.max(np.abs(np.linalg.norm(e2, axis=-1) - 1.0)) <= 1e-12
     sim.close()
+
+
+def _pinned(shape):
+    torch = pytest.importorskip("torch")
+    return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+
+@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("M", [3, 8])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_run_io_equals_put_run_get(prec, M, pinned):
+    """sd_run_io (pipelined over ensemble groups with page-locked arrays) gives exactly
+    what put_moments + sd_run + get_moments give, and keeps the step counter."""
+    lat = lattice.bcc_alloy(6, seed=3).with_ensembles(M)
+    rng = np.random.default_rng(40 + M)
+    e0 = _rand_unit(rng, (M, lat.natom, 3))
+    e1 = _rand_unit(rng, (M, lat.natom, 3))
+    shape = (M, lat.natom, 3)
+    a = _sim(lat, prec, 300.0, e0, seed=8)
+    b = _sim(lat, prec, 300.0, e0, seed=8)
+    a.evolve(3)
+    b.evolve(3)
+    a.put_moments(e1)
+    a.evolve(7)
+    ea, ema = a.get_moments(full=True)
+    mk = _pinned if pinned else np.empty
+    inp, out, outm = mk(shape), mk(shape), mk(shape)
+    inp[...] = e1
+    b.run_io(inp, 7, out, outm)
+    assert np.array_equal(out, ea) and np.array_equal(outm, ema)
+    # a second block from the resident state: the counters continue
+    a.evolve(5)
+    b.run_io(None, 5, out)
+    assert np.array_equal(out, a.get_moments())
+    a.close()
+    b.close()

@@ -63,6 +63,7 @@ SIGNATURES = {
     "uppasd_gpu_set_perp": [C.c_void_p, C.c_int32],
     "uppasd_gpu_set_noise": [C.c_void_p, F64P, C.c_int64],
     "uppasd_gpu_sd_run": [C.c_void_p, C.c_int64],
+    "uppasd_gpu_sd_run_io": [C.c_void_p, F64P, C.c_int64, F64P, F64P],
     "uppasd_gpu_sd_run_measured": [C.c_void_p, C.c_int64, C.c_int64, MEASURE_CB, C.c_void_p],
     "uppasd_gpu_get_field": [C.c_void_p, F64P],
     "uppasd_gpu_mc_run": [C.c_void_p, C.c_char, C.c_double, C.c_int64],

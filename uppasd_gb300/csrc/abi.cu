@@ -9,9 +9,11 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -28,6 +30,10 @@ int structured_step(Sim &s, int64_t step_offset, int phase);
 int structured_set_temperature(Sim &s, const double *temp_array);
 void structured_refresh(Sim &s);
 int structured_sync_state(Sim &s);  // master state -> s.e / s.eM
+int structured_load_range(Sim &s, int k0, int kn, cudaStream_t st);  // ensemble ranges
+int structured_steps_range(Sim &s, int64_t nsteps, int k0, int kn, cudaStream_t st);
+int structured_store_range(Sim &s, int k0, int kn, cudaStream_t st);
+int structured_check_flag(Sim &s);
 int structured_load_state(Sim &s);  // s.e -> master state
 void structured_free(Sim &s);
 int mixed_init(Sim &s);  // llg_mixed.cu
@@ -430,6 +436,12 @@ void destroy(Sim &s) {
         if (s.copy_ev[b]) cudaEventDestroy(s.copy_ev[b]);
     }
     if (s.copy_stream) cudaStreamDestroy(s.copy_stream);
+    for (int g = 0; g < Sim::kIoGroups; ++g) {
+        if (s.io_stream[g]) cudaStreamDestroy(s.io_stream[g]);
+        if (s.io_ev[g]) cudaEventDestroy(s.io_ev[g]);
+        if (s.io_in[g]) cudaEventDestroy(s.io_in[g]);
+    }
+    if (s.io_start) cudaEventDestroy(s.io_start);
     free_vec3(h.ext);
     free_vec3(s.e);
     free_vec3(s.eM);
@@ -808,6 +820,91 @@ int uppasd_gpu_sd_run(uppasd_gpu_sim *w, int64_t nsteps) {
 
 namespace uppasd {
 
+static int io_streams(Sim &s) {
+    if (s.io_start) return UPPASD_GPU_OK;
+    cudaStream_t st[Sim::kIoGroups] = {};
+    cudaEvent_t ev[Sim::kIoGroups] = {}, in[Sim::kIoGroups] = {}, start = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    for (int g = 0; g < Sim::kIoGroups && e == cudaSuccess; ++g) {
+        e = cudaStreamCreateWithFlags(&st[g], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&in[g], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        for (int g = 0; g < Sim::kIoGroups; ++g) {
+            if (st[g]) cudaStreamDestroy(st[g]);
+            if (ev[g]) cudaEventDestroy(ev[g]);
+            if (in[g]) cudaEventDestroy(in[g]);
+        }
+        if (start) cudaEventDestroy(start);
+        set_error(std::string("sd_run_io: streams: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ECUDA;
+    }
+    for (int g = 0; g < Sim::kIoGroups; ++g) {
+        s.io_stream[g] = st[g];
+        s.io_ev[g] = ev[g];
+        s.io_in[g] = in[g];
+    }
+    s.io_start = start;
+    return UPPASD_GPU_OK;
+}
+
+// put + steps + get of the structured path, pipelined: the ensembles split into up to
+// kIoGroups contiguous groups, each on its own stream copying its slice of the
+// caller's (page-locked) arrays in, converting, stepping, converting and copying out,
+// so one group's copies run under the other groups' steps.  Every group reads the
+// same device step counter, advanced once at the end: the Philox counters, and so the
+// results, are those of put_moments + sd_run + get_moments.
+static int sd_run_io_pipelined(Sim &s, const double *in, int64_t nsteps, double *out, double *outM) {
+    int rc = io_streams(s);
+    if (rc) return rc;
+    double *stage = stage_buffer(s);
+    if (!stage) return UPPASD_GPU_ENOMEM;
+    square_mirror_stale(s);
+    const int M = s.ham.mensemble, N = s.ham.natom;
+    // groups: UPPASD_IO_GROUPS (1 .. kIoGroups) when set, else kIoGroups
+    static const int groups = [] {
+        const char *v = std::getenv("UPPASD_IO_GROUPS");
+        const int n = v ? std::atoi(v) : Sim::kIoGroups;
+        return n >= 1 && n <= Sim::kIoGroups ? n : (int)Sim::kIoGroups;
+    }();
+    const int G = std::min(M, groups);
+    UPPASD_CUDA_TRY(cudaEventRecord(s.io_start, s.stream));
+    for (int g = 0; g < G; ++g) {
+        const int k0 = (int)((int64_t)M * g / G), kn = (int)((int64_t)M * (g + 1) / G) - k0;
+        cudaStream_t st = s.io_stream[g];
+        const size_t off = (size_t)k0 * N, cnt = (size_t)kn * N;
+        const unsigned grid = (unsigned)((cnt + 255) / 256);
+        auto slice = [&](const Vec3D &v) { return Vec3D{v.x + off, v.y + off, v.z + off}; };
+        // the input copies one after another in group order, so the first group has its
+        // slice at the full host-link rate and starts stepping while the rest arrive
+        UPPASD_CUDA_TRY(cudaStreamWaitEvent(st, g ? s.io_in[g - 1] : s.io_start, 0));
+        UPPASD_CUDA_TRY(cudaMemcpyAsync(stage + 3 * off, in + 3 * off, 3 * cnt * sizeof(double),
+                                        cudaMemcpyHostToDevice, st));
+        UPPASD_CUDA_TRY(cudaEventRecord(s.io_in[g], st));
+        aos_to_soa<<<grid, 256, 0, st>>>(stage + 3 * off, slice(s.e), slice(s.eM), s.llg.mmom + off, (int64_t)cnt);
+        UPPASD_CUDA_TRY(cudaGetLastError());
+        if ((rc = structured_load_range(s, k0, kn, st)) || (rc = structured_steps_range(s, nsteps, k0, kn, st)) ||
+            (rc = structured_store_range(s, k0, kn, st)))
+            return rc;
+        // the two outputs share the group's slice of the staging array in stream order
+        for (auto [v, h] : {std::pair<const Vec3D *, double *>{&s.e, out}, {&s.eM, outM}}) {
+            if (!h) continue;
+            soa_to_aos<<<grid, 256, 0, st>>>(slice(*v), stage + 3 * off, (int64_t)cnt);
+            UPPASD_CUDA_TRY(cudaGetLastError());
+            UPPASD_CUDA_TRY(cudaMemcpyAsync(h + 3 * off, stage + 3 * off, 3 * cnt * sizeof(double),
+                                            cudaMemcpyDeviceToHost, st));
+        }
+        UPPASD_CUDA_TRY(cudaEventRecord(s.io_ev[g], st));
+        UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.io_ev[g], 0));
+    }
+    advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, nsteps);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    s.step += nsteps;
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    return structured_check_flag(s);
+}
+
 // The measured-run resources (copy stream, two device and two page-locked snapshot
 // buffers, their events), made into locals and installed in s only when every one
 // of them exists, so that a failed set-up leaves nothing half-made behind and the
@@ -847,6 +944,26 @@ int snapshot_setup(Sim &s, size_t bytes) {
 }
 
 }  // namespace uppasd
+
+int uppasd_gpu_sd_run_io(uppasd_gpu_sim *w, const double *emom_in, int64_t nsteps, double *emom_out,
+                         double *emomM_out) {
+    if (!w || nsteps < 0) {
+        uppasd::set_error("bad arguments");
+        return UPPASD_GPU_EINVAL;
+    }
+    Sim &s = w->s;
+    // the pipelined form needs the structured path, an input, several ensembles and
+    // page-locked caller arrays (copies from pageable memory do not overlap anything)
+    bool pipelined = uppasd::structured(s) && emom_in && s.ham.mensemble > 1 && s.llg.noise_mode != 1 &&
+                     uppasd::mapped_host(emom_in) &&
+                     (!emom_out || uppasd::mapped_host(emom_out)) && (!emomM_out || uppasd::mapped_host(emomM_out));
+    if (pipelined) return uppasd::sd_run_io_pipelined(s, emom_in, nsteps, emom_out, emomM_out);
+    int rc;
+    if (emom_in && (rc = uppasd_gpu_put_moments(w, emom_in))) return rc;
+    if ((rc = uppasd_gpu_sd_run(w, nsteps))) return rc;
+    if (emom_out || emomM_out) return uppasd_gpu_get_moments(w, emom_out, emomM_out);
+    return UPPASD_GPU_OK;
+}
 
 int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every, uppasd_gpu_measure_cb cb,
                                void *user) {

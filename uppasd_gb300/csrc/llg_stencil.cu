@@ -88,6 +88,7 @@ constexpr int nb_of_shells(int nsh) { return nsh >= 4 ? 50 : nsh == 3 ? 26 : nsh
 
 struct SParams {
     int L1, L2, L3, nens;
+    int k0, kn;                 // the ensembles a launch covers: k0 .. k0 + kn - 1 (all by default)
     int P1, P2;                 // padded row and plane pitch (cells)
     long long pbox;             // cells per padded sublattice box = P2 * (L3 + 4)
     long long nsite;            // sites per ensemble (2 L1 L2 L3)
@@ -250,7 +251,7 @@ __device__ __forceinline__ bool site_of_thread(const SParams &p, Site &s) {
     s.y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
     s.z = blockIdx.x / nyt;
     s.b = blockIdx.y;
-    s.k = blockIdx.z;
+    s.k = blockIdx.z + p.k0;
     return s.x < p.L1 && s.y < p.L2;
 }
 
@@ -551,7 +552,7 @@ __global__ void __launch_bounds__(256) stencil_zblock(SParams p) {
     const int x = threadIdx.x;
     const int y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
     const int z0 = (blockIdx.x / nyt) * NZ;
-    const int k = blockIdx.z;
+    const int k = blockIdx.z + p.k0;
     if (x >= p.L1 || y >= p.L2) return;
     if (blockIdx.y == 0) zb_sites<NSH, 0, NZ, LC, KIND, MASTER>(p, k, x, y, z0);
     else zb_sites<NSH, 1, NZ, LC, KIND, MASTER>(p, k, x, y, z0);
@@ -688,7 +689,7 @@ __global__ void __launch_bounds__(256) stencil_cells(SParams p) {
     const int x = threadIdx.x;
     const int y = (blockIdx.x % nyt) * blockDim.y + threadIdx.y;
     const int z0 = (blockIdx.x / nyt) * NZ;
-    const int k = blockIdx.z;
+    const int k = blockIdx.z + p.k0;
     if (x >= p.L1 || y >= p.L2) return;
     const float4 *m = KIND == 0 ? p.mt : p.mp;
     const long long own = (long long)(z0 + 2) * pitch2(LC) + (long long)(y + 2) * pitch1(LC) + (x + XOFF);
@@ -774,7 +775,7 @@ __global__ void __launch_bounds__(TX * TY, MINB) stencil_tma(const __grid_consta
     const int t = threadIdx.x;
     const int bid = blockIdx.x;
     const int x0 = (bid % ntx) * TX, y0 = ((bid / ntx) % nty) * TY, zs = (bid / (ntx * nty)) * ZC;
-    const int k = blockIdx.z;
+    const int k = blockIdx.z + p.k0;
     const int tx = t % TX, ty = t / TX;
     const int x = x0 + tx, y = y0 + ty;
     const bool active = x < p.L1 && y < p.L2;
@@ -830,8 +831,8 @@ __global__ void __launch_bounds__(TX * TY, MINB) stencil_tma(const __grid_consta
 // and the structured state.
 __global__ void to_structured(SParams p, const double *ex, const double *ey, const double *ez,
                               const int8_t *species, int master) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long total = p.nsite * p.nens;
+    long long t = (long long)p.k0 * p.nsite + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = p.nsite * (p.k0 + p.kn);
     if (t >= total) return;
     int k = (int)(t / p.nsite);
     long long i = t - (long long)k * p.nsite;  // reference site index
@@ -856,8 +857,8 @@ __global__ void to_structured(SParams p, const double *ex, const double *ey, con
 
 __global__ void from_structured(SParams p, double *ex, double *ey, double *ez, double *mx, double *my, double *mz,
                                 const double *mmom, int master) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long total = p.nsite * p.nens;
+    long long t = (long long)p.k0 * p.nsite + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long total = p.nsite * (p.k0 + p.kn);
     if (t >= total) return;
     int k = (int)(t / p.nsite);
     long long i = t - (long long)k * p.nsite;
@@ -1029,6 +1030,8 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     p.L2 = L2;
     p.L3 = L3;
     p.nens = M;
+    p.k0 = 0;
+    p.kn = M;
     p.nsite = N;
     p.P1 = pitch1(L1);
     p.P2 = p.P1 * (L2 + 4);
@@ -1113,7 +1116,7 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
 
 int structured_load_state(Sim &s) {
     StructuredFast *f = s.fast;
-    long long total = f->p.nsite * f->p.nens;
+    long long total = f->p.nsite * f->p.kn;
     to_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, f->species,
                                                                          f->master);
     UPPASD_CUDA_TRY(cudaGetLastError());
@@ -1134,7 +1137,7 @@ int structured_sync_state(Sim &s) {
             return UPPASD_GPU_ESTATE;
         }
     }
-    long long total = f->p.nsite * f->p.nens;
+    long long total = f->p.nsite * f->p.kn;
     from_structured<<<(unsigned)((total + 255) / 256), 256, 0, s.stream>>>(f->p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y,
                                                                            s.eM.z, s.llg.mmom, f->master);
     UPPASD_CUDA_TRY(cudaGetLastError());
@@ -1153,7 +1156,7 @@ static void launch_tma_kernel(StructuredFast *f, cudaStream_t st) {
         attr = true;
     }
     const int ntx = (LC + T::TX - 1) / T::TX, nty = (LC + T::TY - 1) / T::TY;
-    const dim3 g((unsigned)(ntx * nty * (LC / T::ZC)), 1, (unsigned)f->p.nens);
+    const dim3 g((unsigned)(ntx * nty * (LC / T::ZC)), 1, (unsigned)f->p.kn);
     kern<<<g, T::TX * T::TY, G::kSmem, st>>>(KIND == 0 ? f->map_mt : f->map_mp, f->p, ntx, nty);
 }
 
@@ -1193,7 +1196,7 @@ static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
             return;
         }
         if (f->kernel == 1) {
-            const dim3 g(nyt * (LC / 2), 1, (unsigned)f->p.nens);
+            const dim3 g(nyt * (LC / 2), 1, (unsigned)f->p.kn);
             if (phase & 1) stencil_cells<NSH, 2, LC, 0, 2><<<g, f->block, 0, st>>>(f->p);
             if (phase & 2) {
                 if (f->master == 1) stencil_cells<NSH, 2, LC, 1, 1><<<g, f->block, 0, st>>>(f->p);
@@ -1203,18 +1206,19 @@ static void launch_lc(StructuredFast *f, cudaStream_t st, int phase) {
         }
         if (phase & 1)
             stencil_zblock<NSH, NZP, LC, 0, 2>
-                <<<dim3(nyt * (LC / NZP), 2, (unsigned)f->p.nens), f->block, 0, st>>>(f->p);
+                <<<dim3(nyt * (LC / NZP), 2, (unsigned)f->p.kn), f->block, 0, st>>>(f->p);
         if (phase & 2) {
-            const dim3 g(nyt * (LC / NZC), 2, (unsigned)f->p.nens);
+            const dim3 g(nyt * (LC / NZC), 2, (unsigned)f->p.kn);
             if (f->master == 1) stencil_zblock<NSH, NZC, LC, 1, 1><<<g, f->block, 0, st>>>(f->p);
             else stencil_zblock<NSH, NZC, LC, 1, 2><<<g, f->block, 0, st>>>(f->p);
         }
         return;
     }
-    if (phase & 1) stencil_predict<NSH, LC><<<f->grid, f->block, 0, st>>>(f->p);
+    const dim3 g(f->grid.x, f->grid.y, (unsigned)f->p.kn);
+    if (phase & 1) stencil_predict<NSH, LC><<<g, f->block, 0, st>>>(f->p);
     if (phase & 2) {
-        if (f->master == 1) stencil_correct<NSH, 1, LC><<<f->grid, f->block, 0, st>>>(f->p);
-        else stencil_correct<NSH, 2, LC><<<f->grid, f->block, 0, st>>>(f->p);
+        if (f->master == 1) stencil_correct<NSH, 1, LC><<<g, f->block, 0, st>>>(f->p);
+        else stencil_correct<NSH, 2, LC><<<g, f->block, 0, st>>>(f->p);
     }
 }
 
@@ -1231,17 +1235,75 @@ static void launch(StructuredFast *f, cudaStream_t st, int phase) {
     launch_lc<NSH, 0>(f, st, phase);
 }
 
-int structured_step(Sim &s, int64_t step_offset, int phase) {
+// One step (or half step) of the ensembles k0 .. k0 + kn - 1 on stream st; the launch
+// parameters are taken by value, so the whole-range defaults are restored at once.
+static int step_range(Sim &s, int64_t step_offset, int phase, int k0, int kn, cudaStream_t st) {
     StructuredFast *f = s.fast;
     f->p.step_off = step_offset;
     f->p.d_step = s.llg.d_step;
+    f->p.k0 = k0;
+    f->p.kn = kn;
     switch (f->nshell) {
-    case 1: launch<1>(f, s.stream, phase); break;
-    case 2: launch<2>(f, s.stream, phase); break;
-    case 3: launch<3>(f, s.stream, phase); break;
-    default: launch<4>(f, s.stream, phase); break;
+    case 1: launch<1>(f, st, phase); break;
+    case 2: launch<2>(f, st, phase); break;
+    case 3: launch<3>(f, st, phase); break;
+    default: launch<4>(f, st, phase); break;
     }
+    f->p.k0 = 0;
+    f->p.kn = f->p.nens;
     UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
+int structured_step(Sim &s, int64_t step_offset, int phase) {
+    return step_range(s, step_offset, phase, 0, s.fast->p.nens, s.stream);
+}
+
+// The ensemble-range forms the pipelined host run (abi.cu:sd_run_io) issues per group:
+// conversions from and to the generic state and nsteps steps, all on stream st.  The
+// steps read the device step counter, which the caller advances once all groups are done.
+int structured_load_range(Sim &s, int k0, int kn, cudaStream_t st) {
+    StructuredFast *f = s.fast;
+    SParams p = f->p;
+    p.k0 = k0;
+    p.kn = kn;
+    const long long total = p.nsite * kn;
+    to_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, s.e.x, s.e.y, s.e.z, f->species, f->master);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
+int structured_steps_range(Sim &s, int64_t nsteps, int k0, int kn, cudaStream_t st) {
+    for (int64_t j = 0; j < nsteps; ++j) {
+        int rc = step_range(s, j, 3, k0, kn, st);
+        if (rc) return rc;
+    }
+    return UPPASD_GPU_OK;
+}
+
+int structured_store_range(Sim &s, int k0, int kn, cudaStream_t st) {
+    StructuredFast *f = s.fast;
+    SParams p = f->p;
+    p.k0 = k0;
+    p.kn = kn;
+    const long long total = p.nsite * kn;
+    from_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y, s.eM.z,
+                                                                      s.llg.mmom, f->master);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    return UPPASD_GPU_OK;
+}
+
+// the plane-wait flag of the staged kernels, read after a pipelined run (reset once reported)
+int structured_check_flag(Sim &s) {
+    StructuredFast *f = s.fast;
+    int herr = 0;
+    UPPASD_CUDA_TRY(cudaMemcpyAsync(&herr, f->p.err, sizeof(int), cudaMemcpyDeviceToHost, s.stream));
+    UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
+    if (herr) {
+        UPPASD_CUDA_TRY(cudaMemsetAsync(f->p.err, 0, sizeof(int), s.stream));
+        set_error("structured LLG: a TMA plane wait ran past its limit");
+        return UPPASD_GPU_ESTATE;
+    }
     return UPPASD_GPU_OK;
 }
 

@@ -149,6 +149,10 @@ struct Sim {
     double *snap_d[2] = {nullptr, nullptr}, *snap_h[2] = {nullptr, nullptr};
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t snap_ev[2] = {nullptr, nullptr}, copy_ev[2] = {nullptr, nullptr};
+    // pipelined host runs (sd_run_io): one stream and one completion event per ensemble group
+    static constexpr int kIoGroups = 8;
+    cudaStream_t io_stream[kIoGroups] = {};
+    cudaEvent_t io_ev[kIoGroups] = {}, io_in[kIoGroups] = {}, io_start = nullptr;
     double *stage = nullptr;
     // per-ensemble temperatures of mc_run_temps / pt_run: K and muB / (kB T) (FP32)
     double *tk = nullptr;

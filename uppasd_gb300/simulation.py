@@ -202,6 +202,20 @@ class GpuSimulation:
     def evolve(self, nsteps: int):
         _lib.call("uppasd_gpu_sd_run", self._h, int(nsteps))
 
+    def run_io(self, emom_in: Optional[np.ndarray], nsteps: int, out: Optional[np.ndarray] = None,
+               out_full: Optional[np.ndarray] = None):
+        """put_moments(emom_in) + evolve(nsteps) + get_moments into `out` (and the full
+        moments into `out_full`) as one call; the arrays are C-contiguous float64
+        (mensemble, natom, 3).  With page-locked arrays on the structured path the
+        ensembles' copies overlap the other ensembles' steps (same result)."""
+        shape = (self.lat.mensemble, self.lat.natom, 3)
+        arrs = []
+        for a in (emom_in, out, out_full):
+            if a is not None and (a.shape != shape or a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError(f"arrays must be C-contiguous float64 of shape {shape}")
+            arrs.append(_ptr(a) if a is not None else None)
+        _lib.call("uppasd_gpu_sd_run_io", self._h, arrs[0], int(nsteps), arrs[1], arrs[2])
+
     def sd_run_measured(self, nsteps: int, every: int, fn):
         """nsteps steps with fn(step, emom, emomM) after every `every` of them; the arrays are
         (mensemble, natom, 3) views of library memory, valid during the call (copy to keep).
