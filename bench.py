@@ -1066,6 +1066,7 @@ def main():
     ap.add_argument("--no-configs", action="store_true", help="skip the configured FP64 runs (bcc16k, square256)")
     ap.add_argument("--no-oracle-error", action="store_true", help="skip the FP64-oracle error of the headline")
     ap.add_argument("--no-dipole", action="store_true", help="skip the dipole-dipole field runs")
+    ap.add_argument("--dipole-only", action="store_true", help="only the dipole-dipole field runs")
     ap.add_argument("--mc-only", action="store_true", help="only the batched Monte Carlo section")
     ap.add_argument("--c3-only", action="store_true", help="only the learned-proposal Monte Carlo section")
     ap.add_argument("--c3-profile", action="store_true",
@@ -1104,6 +1105,15 @@ def main():
 
         b.build()
         print(json.dumps(run_c3(args, bf16_peak())), flush=True)
+    elif args.dipole_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        from uppasd_gb300 import build as b
+
+        b.build()
+        stream = torch.cuda.Stream()
+        print(json.dumps(run_dipole(1, 0, stream, not args.no_cpu_baseline)), flush=True)
     else:
         run_gb300(args, w)
 
