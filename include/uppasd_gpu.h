@@ -152,8 +152,11 @@ int uppasd_gpu_set_jtensor(uppasd_gpu_sim *s, const double *j_tens);
  *               and bas (3, na) the basis, both Cartesian in units of alat.  cuFFT is
  *               loaded at run time: -6 when it cannot be.
  * alat in metres (the field is 1e-7 mub / alat^3 (3 R R^T - R^2 I) / R^5 . m).  Only on
- * the FP64 path (precision 0; -7 otherwise); Monte Carlo and the learned moves return -7
- * while it is on. */
+ * the FP64 path (precision 0; -7 otherwise).  Monte Carlo (mc_run, mc_run_temps, pt_run)
+ * takes it as the reference does: Metropolis adds the field of the sweep's start to the
+ * external field of the energy change (montecarlo.f90:216-231); the heat bath has it in
+ * the site field, evaluated again before each colour of the checkerboard.  The structured
+ * square heat bath and the learned moves return -7 while it is on. */
 int uppasd_gpu_set_dipole(uppasd_gpu_sim *s, int32_t do_dip, double alat, const double *coord, int32_t na,
                           int32_t n1, int32_t n2, int32_t n3, const double *cell, const double *bas);
 

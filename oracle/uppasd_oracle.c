@@ -342,24 +342,32 @@ static void dipole_coord(const orc_ham *h, int i, double r[3]) {
 /* dipolar_field (dipolemanager.f90:223-243) for every (atom, ensemble), Qdip set up as
  * setup_qdip does (dipolecommon.f90:114-159): Qdip(:,:,j,i) = dipoleMatrix(r_i - r_j),
  * zero on the diagonal */
+/* dipolar_field of one site (dipolemanager.f90:223-243) */
+static void dipole_field_site(const orc_ham *h, const double *emomM, int i, int k, double f[3]) {
+    const int N = h->natom;
+    double ri[3];
+    dipole_coord(h, i, ri);
+    f[0] = f[1] = f[2] = 0.0;
+    for (int j = 0; j < N; ++j) {
+        double rj[3], R[3], Q[3][3];
+        dipole_coord(h, j, rj);
+        for (int q = 0; q < 3; ++q) R[q] = ri[q] - rj[q];
+        dipole_matrix(h->dip_alat, R, Q);
+        if (j == i)
+            for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b) Q[a][b] = 0.0;
+        const double m1 = V3(emomM, 0, j, k, N), m2 = V3(emomM, 1, j, k, N), m3 = V3(emomM, 2, j, k, N);
+        for (int nu = 0; nu < 3; ++nu) f[nu] = f[nu] + Q[0][nu] * m1 + Q[1][nu] * m2 + Q[2][nu] * m3;
+    }
+}
+
 void orc_dipole_field(const orc_ham *h, const double *emomM, double *out) {
     const int N = h->natom, M = h->mensemble;
 #pragma omp parallel for collapse(2) schedule(static) num_threads(orc_get_threads())
     for (int k = 0; k < M; ++k)
         for (int i = 0; i < N; ++i) {
-            double ri[3], f[3] = {0.0, 0.0, 0.0};
-            dipole_coord(h, i, ri);
-            for (int j = 0; j < N; ++j) {
-                double rj[3], R[3], Q[3][3];
-                dipole_coord(h, j, rj);
-                for (int q = 0; q < 3; ++q) R[q] = ri[q] - rj[q];
-                dipole_matrix(h->dip_alat, R, Q);
-                if (j == i)
-                    for (int a = 0; a < 3; ++a)
-                        for (int b = 0; b < 3; ++b) Q[a][b] = 0.0;
-                const double m1 = V3(emomM, 0, j, k, N), m2 = V3(emomM, 1, j, k, N), m3 = V3(emomM, 2, j, k, N);
-                for (int nu = 0; nu < 3; ++nu) f[nu] = f[nu] + Q[0][nu] * m1 + Q[1][nu] * m2 + Q[2][nu] * m3;
-            }
+            double f[3];
+            dipole_field_site(h, emomM, i, k, f);
             for (int nu = 0; nu < 3; ++nu) V3(out, nu, i, k, N) = f[nu];
         }
 }
@@ -396,13 +404,17 @@ double orc_effective_field(const orc_ham *h, const double *emomM, double *beff) 
     return energy * ORC_MUB / ORC_MRY;
 }
 
+/* effective_field_single (hamiltonianactions.f90:253-371): with dipoles on, the dipolar
+ * field in dip_work (the caller evaluates it for the moments the field is wanted for)
+ * comes first */
 void orc_effective_field_single(const orc_ham *h, const double *emomM, int i, int k, double out[3]) {
     const int N = h->natom;
     double bs[3], bq[3];
     site_field(h, emomM, i, k, bs, bq);
     for (int c = 0; c < 3; ++c) {
         double b2 = bq[c] + V3(h->extfield, c, i, k, N) + 0.0;
-        out[c] = 0.0 + bs[c] + b2;
+        const double bd = h->do_dip ? V3(h->dip_work, c, i, k, N) : 0.0;
+        out[c] = bd + bs[c] + b2;
     }
 }
 
@@ -1170,13 +1182,25 @@ int orc_mc_evolve_ref(const orc_ham *h, char mode, double temperature, double te
     if (mode == 'H')
         for (int64_t t = 0; t < n1; ++t) mflip[t] = orc_mt_real2(c);
     for (int64_t t = 0; t < n1; ++t) fa[t] = orc_mt_real2(c);    /* rng_uniformP(flipprob_a) */
+    /* dipoles: the field of the moments at the start of the step, an extra external field
+     * for Metropolis (montecarlo.f90:216-231); the heat bath's effective_field_hb evaluates
+     * the site's own dipolar field from the current moments */
+    if (h->do_dip && mode != 'H') orc_dipole_field(h, emomM, h->dip_work);
     for (int i = 0; i < N; ++i) {
         for (int k = 0; k < M; ++k) {
             int ia = iflip_a[i] - 1;
             double ext[3];
-            for (int cc = 0; cc < 3; ++cc) ext[cc] = V3(h->extfield, cc, ia, k, N) + 0.0;
+            for (int cc = 0; cc < 3; ++cc) {
+                const double bd = h->do_dip ? V3(h->dip_work, cc, ia, k, N) : 0.0;
+                ext[cc] = (V3(h->extfield, cc, ia, k, N) + bd) + 0.0;
+            }
             if (mode == 'H') {
                 double tf[3], nm[3];
+                if (h->do_dip) {
+                    double f[3];
+                    dipole_field_site(h, emomM, ia, k, f);
+                    for (int cc = 0; cc < 3; ++cc) V3(h->dip_work, cc, ia, k, N) = f[cc];
+                }
                 orc_effective_field_single(h, emomM, ia, k, tf);
                 for (int cc = 0; cc < 3; ++cc) V3(beff, cc, ia, k, N) = tf[cc];
                 double mm = M2(mmom, ia, k, N);
@@ -1218,8 +1242,14 @@ int orc_mc_sweep_checkerboard_temps(const orc_ham *h, char mode, double temperat
                                     const int32_t *colour_sites, const int32_t *colour_start, int ncolour,
                                     uint64_t seed, int64_t sweep, double *emom, double *emomM, const double *mmom) {
     const int N = h->natom, M = h->mensemble;
+    /* dipoles: Metropolis takes the field of the moments at the start of the sweep as an
+     * extra external field (montecarlo.f90:216-231); the heat bath takes the field in the
+     * site's effective field (effective_field_hb), evaluated here before each colour, the
+     * moments of the colour's sites changing only within it */
+    if (h->do_dip && mode != 'H') orc_dipole_field(h, emomM, h->dip_work);
     for (int col = 0; col < ncolour; ++col) {
         int beg = colour_start[col], end = colour_start[col + 1];
+        if (h->do_dip && mode == 'H') orc_dipole_field(h, emomM, h->dip_work);
 #pragma omp parallel for schedule(static) num_threads(orc_get_threads())
         for (int t = beg; t < end; ++t) {
             int i = colour_sites[t];
@@ -1242,7 +1272,11 @@ int orc_mc_sweep_checkerboard_temps(const orc_ham *h, char mode, double temperat
                     if ((int)floor(3.0 * rn[0]) == 1) orc_philox_normal3(seed, i, k, sweep, 2u, gn);
                     const double delta = F32(2.0 / 25.0) * pow(ORC_KBOLT * Tk / ORC_MUB, 0.20);
                     choose_random_flip(&V3(emom, 0, i, k, N), delta, rn, gn, nm);
-                    for (int cc = 0; cc < 3; ++cc) ext[cc] = V3(h->extfield, cc, i, k, N) + 0.0;
+                    /* loc_mag_fld = extfield + beff + loc_demag_fld (montecarlo.f90:231) */
+                    for (int cc = 0; cc < 3; ++cc) {
+                        const double bd = h->do_dip ? V3(h->dip_work, cc, i, k, N) : 0.0;
+                        ext[cc] = (V3(h->extfield, cc, i, k, N) + bd) + 0.0;
+                    }
                     double de = calculate_energy(h, emomM, emom, mmom, i, nm, ext, k);
                     if (flip_a(de, Tk, 1.0, u[3])) {
                         for (int cc = 0; cc < 3; ++cc) {

@@ -3,7 +3,7 @@
 The field alone to 1e-12 (brute force) and 1e-10 (FFT) of its largest component, on
 cubic, skewed and non-cubic cell grids; FP64 LLG trajectories with the field on within
 1e-9 per spin component of the oracle's after 200 steps; the energy with the dipolar
-term; the Monte Carlo paths refuse while it is on.
+term; checkerboard Monte Carlo chains with the field against the oracle's.
 """
 import numpy as np
 import pytest
@@ -102,15 +102,43 @@ def test_energy_and_field_with_exchange(mode):
     sim.close()
 
 
-def test_monte_carlo_refuses_while_on():
-    lat = lattice.bcc(3, [1.3, 0.7], 2.2)
+@pytest.mark.parametrize("mode", ["M", "H"])
+@pytest.mark.parametrize("do_dip", [1, 3])
+def test_monte_carlo_chain_with_dipoles(mode, do_dip):
+    """Checkerboard Metropolis (field of the sweep's start in the external field) and heat
+    bath (field refreshed before each colour) against the oracle's chain, per spin."""
+    # weak exchange at low temperature: dipolar energies comparable to k_B T
+    lat = lattice.bcc(4, [0.02, 0.01], 2.2).with_ensembles(2)
+    e0 = rand_moments(np.random.default_rng(8), lat)
+    T = 5.0
+    sim = GpuSimulation(lat, emom=e0, seed=123)
+    sim.set_dipole(do_dip, ALAT)
+    sim.relax(mode, T, 3)
+    o = po.Oracle(lat, dipole_alat=ALAT)
+    o.set_moments(e0)
+    _, order, start = lattice.greedy_colouring(lat)
+    for sw in range(3):
+        o.mc_sweep_checkerboard(mode, T, order, start, 123, sw)
+    tol = 1e-12 if do_dip == 1 else 1e-9
+    assert np.max(np.abs(sim.get_moments() - o.emom)) <= tol
+    # the dipolar field changes the chain
+    o0 = po.Oracle(lat)
+    o0.set_moments(e0)
+    for sw in range(3):
+        o0.mc_sweep_checkerboard(mode, T, order, start, 123, sw)
+    assert np.max(np.abs(o0.emom - o.emom)) > 1e-6
+    sim.close()
+
+
+def test_square_heat_bath_and_learned_refuse_while_on():
+    lat = lattice.square_dmi(16, 1.0, 0.3, 0.0, 0.5, 1.0)
     sim = GpuSimulation(lat)
     sim.set_dipole(1, ALAT)
     with pytest.raises(_lib.UppasdGpuError) as ei:
-        sim.relax("M", 100.0, 1)
+        sim.relax("H", 20.0, 1, structured=True)
     assert ei.value.rc == -7
     sim.set_dipole(0)
-    sim.relax("M", 100.0, 1)
+    sim.relax("H", 20.0, 1, structured=True)
     sim.close()
 
 

@@ -838,7 +838,7 @@ PatchGeom geom(const uppasd_gpu_proposal *p, int colour) {
 int enqueue_sweep(uppasd_gpu_proposal *p, int rows, double beta_mub, bool per_ensemble, cudaStream_t st) {
     Sim &s = p->sim->s;
     if (s.ham.do_dip) {
-        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
+        set_error("learned moves: the dipolar field is not taken; set_dipole(0) first, or use mc_run");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     const long long nt = (long long)rows * 64;

@@ -9,6 +9,9 @@
 //   energy change  calculate_energy     MonteCarlo/montecarlo_common.f90:431-865
 //   acceptance     flip_a               MonteCarlo/montecarlo_common.f90:139-200
 //   heat bath      flip_h               MonteCarlo/montecarlo_common.f90:371-422
+// With the dipolar field on (dipole.cu), Metropolis adds the field of the sweep's start
+// to the external field of the energy change and the heat bath has it, refreshed before
+// each colour, in the site field.
 // Random numbers come from Philox keyed by (site, ensemble, sweep): one draw
 // of four uniforms per update, and a second (Gaussian) draw for the Gaussian
 // trial move.  Compiled with --fmad=false.
@@ -163,7 +166,15 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
         double gn[3] = {0.0, 0.0, 0.0};
         if ((int)floor(3.0 * rn[0]) == 1) normal3_f64(seed, i, k, sweep, kStreamMCGauss, gn);
         choose_random_flip(ecur, delta, rn, gn, nm);
-        double ext[3] = {h.ext.x[o] + 0.0, h.ext.y[o] + 0.0, h.ext.z[o] + 0.0};
+        // loc_mag_fld = extfield + beff + loc_demag_fld (montecarlo.f90:231): beff is the
+        // dipolar field of the sweep's start when dipoles are on, zero otherwise
+        double bd[3] = {0.0, 0.0, 0.0};
+        if (h.do_dip) {
+            bd[0] = h.dip.x[o];
+            bd[1] = h.dip.y[o];
+            bd[2] = h.dip.z[o];
+        }
+        double ext[3] = {(h.ext.x[o] + bd[0]) + 0.0, (h.ext.y[o] + bd[1]) + 0.0, (h.ext.z[o] + bd[2]) + 0.0};
         double de = delta_energy(h, eM, e, mm, i, k, nm, ext);
         double beta = 1.0 / h.kbolt / (1.0 * temperature + 1.0e-15);
         if (!(de <= 0.0 || u[3] < exp(-beta * de))) return;
@@ -177,10 +188,6 @@ __global__ void __launch_bounds__(256) mc_colour_kernel(HamDev h, Vec3D e, Vec3D
 }
 
 int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweeps, const double *tk) {
-    if (s.ham.do_dip) {
-        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
-        return UPPASD_GPU_EUNSUPPORTED;
-    }
     square_mirror_stale(s);
     if (s.ncolour <= 0) {
         set_error("no colouring available for Monte Carlo");
@@ -189,11 +196,19 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
     // montecarlo.f90:142, (2.0/25.0) is a REAL(4) constant
     const double delta = (double)(2.0f / 25.0f) * pow(s.ham.kbolt * temperature / s.ham.mub, 0.20);
     const int hb = mode == 'H' ? 1 : 0;
+    int rc;
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
+        // dipoles: Metropolis takes the field of the sweep's start as an extra external
+        // field (montecarlo.f90:216-231); the heat bath has it in the site field
+        // (effective_field_hb), evaluated before each colour: within a colour only the
+        // colour's own sites change, and the long-range field of those changes is the
+        // one term the colouring cannot keep exact
+        if (s.ham.do_dip && !hb && (rc = dipole_field(s, s.eM))) return rc;
         for (int c = 0; c < s.ncolour; ++c) {
             int beg = s.colour_start_h[c], end = s.colour_start_h[c + 1];
             int n = end - beg;
             if (n == 0) continue;
+            if (s.ham.do_dip && hb && (rc = dipole_field(s, s.eM))) return rc;
             int64_t tot = (int64_t)n * s.ham.mensemble;
             mc_colour_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
                 s.ham, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, hb, temperature, delta, tk, s.llg.seed,

@@ -190,7 +190,7 @@ namespace uppasd {
 // null for the single `temperature`.
 int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t nsweeps) {
     if (s.ham.do_dip) {
-        set_error("Monte Carlo with the dipolar field is not supported; set_dipole(0) first");
+        set_error("mc_run_square: the dipolar field is not taken; set_dipole(0) first, or use mc_run");
         return UPPASD_GPU_EUNSUPPORTED;
     }
     if (structured(s)) {
