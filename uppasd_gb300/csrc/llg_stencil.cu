@@ -396,15 +396,13 @@ __device__ __forceinline__ void correct_finish(const SParams &p, int k, int b, i
         }
         float xs, xe;
         two_sum(n2h, -1.0f, xs, xe);
-        float xx = xs + (xe + n2l);                // |e|^2 - 1, ~1e-7
+        float xx = xs + (xe + n2l);                // |e|^2 - 1: the FP32 rounding of one step's rotation
         float sm1 = xx * fmaf(0.375f, xx, -0.5f);  // 1/sqrt(1+x) - 1
+        // e (1 + sm1): the correction hi sm1 is ~|xx| hi, far below half an ulp of hi, so it
+        // joins the low word (lo sm1, below 1e-15 of e, is dropped); the next step's update
+        // renormalises the pair
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            float corr = hi[c] * sm1 + lo[c] * sm1;
-            float sm, er;
-            two_sum(hi[c], corr, sm, er);
-            quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
-        }
+        for (int c = 0; c < 3; ++c) lo[c] = fmaf(hi[c], sm1, lo[c]);
         p.lox[u] = lo[0];
         p.loy[u] = lo[1];
         p.loz[u] = lo[2];
