@@ -121,12 +121,13 @@ def _pinned(shape):
     return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
 
 
-@pytest.mark.parametrize("prec", [1, 2])
+@pytest.mark.parametrize("prec", [0, 1, 2, 3])
 @pytest.mark.parametrize("M", [3, 8])
 @pytest.mark.parametrize("pinned", [True, False])
 def test_run_io_equals_put_run_get(prec, M, pinned):
-    """sd_run_io (pipelined over ensemble groups with page-locked arrays) gives exactly
-    what put_moments + sd_run + get_moments give, and keeps the step counter."""
+    """sd_run_io (pipelined over ensemble groups with page-locked arrays on the structured
+    path, the three calls in turn otherwise) gives exactly what put_moments + sd_run +
+    get_moments give, and keeps the step counter."""
     lat = lattice.bcc_alloy(6, seed=3).with_ensembles(M)
     rng = np.random.default_rng(40 + M)
     e0 = _rand_unit(rng, (M, lat.natom, 3))
