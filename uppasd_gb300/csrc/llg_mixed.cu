@@ -407,11 +407,15 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
 
 // Heat bath of one colour (flip_h, MonteCarlo/montecarlo_common.f90:371-422) on the
 // FP32 mirror: the field over the caller's neighbour lists, the draw in FP32 with the
-// FP64 path's Philox counters (site, ensemble, sweep), the new spin renormalised in
-// FP64 and written to e / eM and the mirror.  Same checkerboard chain as mc_colour_kernel.
-__global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec3D e, Vec3D eM, const double *mmom,
-                                                       const int32_t *sites, int nsites, float beta_mub,
-                                                       const float *betak, uint64_t seed, int64_t sweep) {
+// FP64 path's Philox counters (site, ensemble, sweep), written to the mirror only.  Every
+// site is drawn again each sweep and its FP64 value is the draw renormalised in FP64, so
+// e / eM are made from the mirror once after the sweeps (mixed_master_from_mirror) rather
+// than written on every update: each colour writes every other site, and the FP64 state's
+// 48 bytes per site went to DRAM as read-modify-writes of half-written sectors.  Same
+// checkerboard chain as mc_colour_kernel.
+__global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, const int32_t *sites, int nsites,
+                                                       float beta_mub, const float *betak, uint64_t seed,
+                                                       int64_t sweep) {
     const int N = h.natom;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nsites * h.mensemble) return;
@@ -426,13 +430,20 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, Vec
     const float k32 = 2.3283064365386963e-10f;
     const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
     const float3 n = heat_bath_f32(make_float3(B[0], B[1], B[2]), (betak ? betak[k] : beta_mub) * mm, q, fp);
-    // the FP64 state gets the draw renormalised in FP64, as the LLG steps leave it
-    double x = n.x, y = n.y, z = n.z;
+    mt[o] = make_float4(n.x, n.y, n.z, mm);
+}
+
+// The FP64 state from the mirror after heat-bath sweeps: the draw renormalised in FP64,
+// as the LLG steps leave a spin, and the full moment.
+__global__ void mixed_master_from_mirror(MixedDev c, Vec3D e, Vec3D eM, const double *mmom, int64_t n) {
+    const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const float4 v = c.mt[o];
+    double x = v.x, y = v.y, z = v.z;
     const double sc = renorm_scale(fma(z, z, fma(y, y, x * x)) - 1.0);
     x *= sc;
     y *= sc;
     z *= sc;
-    mt[o] = make_float4((float)x, (float)y, (float)z, mm);
     const double md = c.uni_m ? c.mmom_u : mmom[o];
     e.x[o] = x;
     e.y[o] = y;
@@ -820,10 +831,14 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const fl
             if (n == 0) continue;
             const int64_t tot = (int64_t)n * s.ham.mensemble;
             mixed_heat_bath<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
-                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, betak, s.llg.seed,
-                s.mc_sweep);
+                s.ham, s.mix, s.colour_sites + beg, n, beta_mub, betak, s.llg.seed, s.mc_sweep);
         }
         s.mc_sweep += 1;
+    }
+    if (nsweeps > 0) {
+        const int64_t nm = (int64_t)s.ham.natom * s.ham.mensemble;
+        mixed_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom,
+                                                                                   nm);
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;

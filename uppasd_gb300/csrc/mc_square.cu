@@ -8,8 +8,9 @@
 // nlist/ncoup/dmlist/dm_vect, and the heat-bath draw (flip_h,
 // MonteCarlo/montecarlo_common.f90:371-422) runs in FP32 on the FP64 spin state.
 // Neighbours are read from an FP32 mirror of the state (the values the draw uses
-// anyway), and every new spin is written to the mirror and to e / eM: four 16-byte
-// loads per site instead of twelve 8-byte loads and conversions from e.
+// anyway), and every new spin is written to the mirror, from which e / eM are made
+// once after the call's sweeps: four 16-byte loads per site instead of twelve 8-byte
+// loads and conversions from e, and one 16-byte store per update.
 // The chain is the checkerboard chain of mc.cu (colours x + y even, then odd)
 // with the same Philox counters (site, ensemble, sweep), so it agrees with the
 // FP64 path to FP32 rounding.
@@ -31,8 +32,11 @@ struct SqArgs {
     long long sweep;
 };
 
-// betak: muB / (kB T) per ensemble (one temperature per ensemble), or null (a.beta_mu)
-__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e, Vec3D eM, const float *betak) {
+// betak: muB / (kB T) per ensemble (one temperature per ensemble), or null (a.beta_mu).
+// The draw goes to the FP32 mirror only; e / eM, which hold exactly the draw (and the
+// uniform moment times it), are made from the mirror once after the sweeps
+// (sq_master_from_mirror) instead of on every update of every other site.
+__global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, const float *betak) {
     const int half = a.L >> 1;
     const long long per = (long long)a.L * half;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -61,14 +65,19 @@ __global__ void __launch_bounds__(256) sq_heat_bath(SqArgs a, float4 *m, Vec3D e
     const float k32 = 2.3283064365386963e-10f;
     const float q = fmaf((float)w.x, k32, 0.5f * k32), fp = fmaf((float)w.y, k32, 0.5f * k32);
     const float3 n = heat_bath_f32(make_float3(hx, hy, hz), betak ? betak[k] * a.mom : a.beta_mu, q, fp);
-    const size_t o = off + i;
-    m[o] = make_float4(n.x, n.y, n.z, 0.f);
-    e.x[o] = n.x;
-    e.y[o] = n.y;
-    e.z[o] = n.z;
-    eM.x[o] = (double)a.mom * n.x;
-    eM.y[o] = (double)a.mom * n.y;
-    eM.z[o] = (double)a.mom * n.z;
+    m[off + i] = make_float4(n.x, n.y, n.z, 0.f);
+}
+
+__global__ void sq_master_from_mirror(const float4 *m, Vec3D e, Vec3D eM, float mom, long long n) {
+    const long long o = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= n) return;
+    const float4 v = m[o];
+    e.x[o] = v.x;
+    e.y[o] = v.y;
+    e.z[o] = v.z;
+    eM.x[o] = (double)mom * v.x;
+    eM.y[o] = (double)mom * v.y;
+    eM.z[o] = (double)mom * v.z;
 }
 
 __global__ void to_mirror(Vec3D e, float4 *m, long long n) {
@@ -221,9 +230,13 @@ int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t
         a.sweep = s.mc_sweep;
         for (int c = 0; c < 2; ++c) {
             a.colour = c;
-            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.sqm, s.e, s.eM, betak);
+            sq_heat_bath<<<blocks, 256, 0, s.stream>>>(a, s.sqm, betak);
         }
         s.mc_sweep += 1;
+    }
+    if (nsweeps > 0) {
+        const long long nm = (long long)s.ham.natom * s.ham.mensemble;
+        sq_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.sqm, s.e, s.eM, a.mom, nm);
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;

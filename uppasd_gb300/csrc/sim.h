@@ -136,9 +136,10 @@ struct Sim {
     int32_t *colour_start_h = nullptr; // host copy, ncolour+1
     int64_t mc_sweep = 0;
     SquareMC sq;
-    // FP32 read mirror of the unit spins (x, y, z, 0), [mensemble][natom], for the
-    // structured square heat bath and the learned patch moves: they read it and write
-    // every update to both it and e / eM; any other writer of e marks it stale.
+    // FP32 mirror of the unit spins (x, y, z, 0), [mensemble][natom], for the structured
+    // square heat bath and the learned patch moves: the heat bath writes its draws to it
+    // and makes e / eM from it at the end of a call, the learned moves write every update
+    // to both it and e / eM; any other writer of e marks it stale.
     float4 *sqm = nullptr;
     int sqm_valid = 0;
     MixedDev mix;
