@@ -433,11 +433,17 @@ __global__ void __launch_bounds__(256) mixed_heat_bath(HamDev h, MixedDev c, con
     mt[o] = make_float4(n.x, n.y, n.z, mm);
 }
 
-// The FP64 state from the mirror after heat-bath sweeps: the draw renormalised in FP64,
-// as the LLG steps leave a spin, and the full moment.
-__global__ void mixed_master_from_mirror(MixedDev c, Vec3D e, Vec3D eM, const double *mmom, int64_t n) {
+// The FP64 state from the mirror after Monte Carlo sweeps: the draw renormalised in FP64,
+// as the LLG steps leave a spin, and the full moment; with `moved` (Metropolis) only at
+// the sites whose trial was accepted, whose marks it clears.
+__global__ void mixed_master_from_mirror(MixedDev c, Vec3D e, Vec3D eM, const double *mmom, int64_t n,
+                                         uint8_t *moved) {
     const int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (o >= n) return;
+    if (moved) {
+        if (!moved[o]) return;
+        moved[o] = 0;
+    }
     const float4 v = c.mt[o];
     double x = v.x, y = v.y, z = v.z;
     const double sc = renorm_scale(fma(z, z, fma(y, y, x * x)) - 1.0);
@@ -456,11 +462,11 @@ __global__ void mixed_master_from_mirror(MixedDev c, Vec3D e, Vec3D eM, const do
 // Metropolis on the mirror (mc_evolve with flip_a, MonteCarlo/montecarlo.f90:44-273,
 // montecarlo_common.f90:139-200): the trial of choose_random_flip (:25-79) from the same
 // Philox words as the FP64 path, the energy change in FP32, acceptance when it is <= 0 or
-// u < exp(-beta de); an accepted spin is renormalised in FP64 and written to the mirror and
-// the FP64 state.
-__global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, Vec3D e, Vec3D eM, const double *mmom,
-                                                        const int32_t *sites, int nsites, float beta_mub, float delta,
-                                                        uint64_t seed, int64_t sweep) {
+// u < exp(-beta de); an accepted trial is written to the mirror and its site marked moved;
+// after the sweeps mixed_master_from_mirror gives the moved sites the trial renormalised in
+// FP64 (rejected sites keep their FP64 state as it was).
+__global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, const int32_t *sites, int nsites,
+                                                        float beta_mub, float delta, uint64_t seed, int64_t sweep) {
     const int N = h.natom;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (int64_t)nsites * h.mensemble) return;
@@ -497,19 +503,8 @@ __global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, Ve
     }
     const float de = delta_energy_f32(h, c, mt, i, k, nm);
     if (!(de <= 0.0f || u3 < __expf(-beta_mub * de))) return;
-    double x = nm[0], y = nm[1], z = nm[2];
-    const double sc = renorm_scale(fma(z, z, fma(y, y, x * x)) - 1.0);
-    x *= sc;
-    y *= sc;
-    z *= sc;
-    mt[o] = make_float4((float)x, (float)y, (float)z, cur.w);
-    const double md = c.uni_m ? c.mmom_u : mmom[o];
-    e.x[o] = x;
-    e.y[o] = y;
-    e.z[o] = z;
-    eM.x[o] = md * x;
-    eM.y[o] = md * y;
-    eM.z[o] = md * z;
+    mt[o] = make_float4(nm[0], nm[1], nm[2], cur.w);
+    c.moved[o] = 1;
 }
 
 __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n) {
@@ -773,7 +768,7 @@ void mixed_free(Sim &s) {
     MixedDev &m = s.mix;
     for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
                     (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext, (void *)m.row,
-                    (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm})
+                    (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm, (void *)m.moved})
         cudaFree(q);
     m = MixedDev{};
 }
@@ -801,17 +796,32 @@ int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps) {
     // (montecarlo.f90:142, a REAL(4) constant), as the FP64 path forms them
     const float beta_mub = (float)(s.ham.mub / s.ham.kbolt / (1.0 * temperature + 1.0e-15));
     const float delta = (float)((double)(2.0f / 25.0f) * pow(s.ham.kbolt * temperature / s.ham.mub, 0.20));
+    const int64_t nm = (int64_t)s.ham.natom * s.ham.mensemble;
+    if (!s.mix.moved) {
+        // the moved marks, cleared once; the pass after the sweeps clears what it uses
+        uint8_t *mv = nullptr;
+        UPPASD_CUDA_TRY(cudaMalloc(&mv, (size_t)nm));
+        const cudaError_t e = cudaMemsetAsync(mv, 0, (size_t)nm, s.stream);
+        if (e != cudaSuccess) {
+            cudaFree(mv);
+            set_error(std::string("mc_run (precision 3): ") + cudaGetErrorString(e));
+            return UPPASD_GPU_ECUDA;
+        }
+        s.mix.moved = mv;
+    }
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
         for (int c = 0; c < s.ncolour; ++c) {
             const int beg = s.colour_start_h[c], n = s.colour_start_h[c + 1] - beg;
             if (n == 0) continue;
             const int64_t tot = (int64_t)n * s.ham.mensemble;
             mixed_metropolis<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
-                s.ham, s.mix, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, beta_mub, delta, s.llg.seed,
-                s.mc_sweep);
+                s.ham, s.mix, s.colour_sites + beg, n, beta_mub, delta, s.llg.seed, s.mc_sweep);
         }
         s.mc_sweep += 1;
     }
+    if (nsweeps > 0)
+        mixed_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom,
+                                                                                   nm, s.mix.moved);
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }
@@ -838,7 +848,7 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const fl
     if (nsweeps > 0) {
         const int64_t nm = (int64_t)s.ham.natom * s.ham.mensemble;
         mixed_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom,
-                                                                                   nm);
+                                                                                   nm, nullptr);
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;

@@ -102,6 +102,7 @@ struct MixedDev {
     int uni_lam = 0, uni_g = 0, uni_T = 0, uni_m = 0;
     float lam_u = 0.f, g_u = 0.f, T_u = 0.f;
     double mmom_u = 0.0;       // moment of every (ensemble, site) when uni_m
+    uint8_t *moved = nullptr;  // [mensemble][natom] Metropolis: mirror moved, FP64 state not yet
 };
 
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
