@@ -237,7 +237,8 @@ int uppasd_gpu_observables(uppasd_gpu_sim *s, double *mvec, double *mabs, double
 /* Per-ensemble energy terms of calc_energy (Hamiltonian/energy.f90:60-405) in mRy per
  * atom, terms(5, mensemble) = {total, exchange (the pair energy with the tensor),
  * anisotropy, DM, Zeeman}: the ene%energy / ene_xc / ene_ani / ene_dm / ene_ext values
- * that totenergy.<simid>.out averages over the ensembles (:407-500). */
+ * that totenergy.<simid>.out averages over the ensembles (:407-500).  With the dipolar
+ * field on (uppasd_gpu_set_dipole), total includes ene_dip, which has no column here. */
 int uppasd_gpu_energy_terms(uppasd_gpu_sim *s, double *terms);
 
 /* Run the library's work on the caller's CUDA stream (a cudaStream_t passed as
