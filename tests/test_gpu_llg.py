@@ -1,6 +1,6 @@
 """GPU LLG parity: the CUDA path through the C ABI against the CPU oracle.
 
-Tolerance (spec bar): FP64 trajectories within 1e-9 per spin component
+Tolerance: FP64 trajectories within 1e-9 per spin component
 after 1000 steps, at T = 0 and with fixed injected noise.  Runs on a GB300.
 """
 import ctypes as C
