@@ -30,9 +30,9 @@ int structured_step(Sim &s, int64_t step_offset, int phase);
 int structured_set_temperature(Sim &s, const double *temp_array);
 void structured_refresh(Sim &s);
 int structured_sync_state(Sim &s);  // master state -> s.e / s.eM
-int structured_load_range(Sim &s, int k0, int kn, cudaStream_t st);  // ensemble ranges
+int structured_load_range(Sim &s, const double *aos, int k0, int kn, cudaStream_t st);  // ensemble ranges
 int structured_steps_range(Sim &s, int64_t nsteps, int k0, int kn, cudaStream_t st);
-int structured_store_range(Sim &s, int k0, int kn, cudaStream_t st);
+int structured_store_range(Sim &s, double *aos, int full, int k0, int kn, cudaStream_t st);
 int structured_check_flag(Sim &s);
 int structured_load_state(Sim &s);  // s.e -> master state
 void structured_free(Sim &s);
@@ -880,24 +880,20 @@ static int sd_run_io_pipelined(Sim &s, const double *in, int64_t nsteps, double 
         const int k0 = (int)((int64_t)M * g / G), kn = (int)((int64_t)M * (g + 1) / G) - k0;
         cudaStream_t st = s.io_stream[g];
         const size_t off = (size_t)k0 * N, cnt = (size_t)kn * N;
-        const unsigned grid = (unsigned)((cnt + 255) / 256);
-        auto slice = [&](const Vec3D &v) { return Vec3D{v.x + off, v.y + off, v.z + off}; };
         // the input copies one after another in group order, so the first group has its
         // slice at the full host-link rate and starts stepping while the rest arrive
         UPPASD_CUDA_TRY(cudaStreamWaitEvent(st, g ? s.io_in[g - 1] : s.io_start, 0));
         UPPASD_CUDA_TRY(cudaMemcpyAsync(stage + 3 * off, in + 3 * off, 3 * cnt * sizeof(double),
                                         cudaMemcpyHostToDevice, st));
         UPPASD_CUDA_TRY(cudaEventRecord(s.io_in[g], st));
-        aos_to_soa<<<grid, 256, 0, st>>>(stage + 3 * off, slice(s.e), slice(s.eM), s.llg.mmom + off, (int64_t)cnt);
-        UPPASD_CUDA_TRY(cudaGetLastError());
-        if ((rc = structured_load_range(s, k0, kn, st)) || (rc = structured_steps_range(s, nsteps, k0, kn, st)) ||
-            (rc = structured_store_range(s, k0, kn, st)))
+        // the staging slice straight into the structured state and back (the generic e / eM
+        // are brought up to date by the next call that reads them)
+        if ((rc = structured_load_range(s, stage, k0, kn, st)) || (rc = structured_steps_range(s, nsteps, k0, kn, st)))
             return rc;
         // the two outputs share the group's slice of the staging array in stream order
-        for (auto [v, h] : {std::pair<const Vec3D *, double *>{&s.e, out}, {&s.eM, outM}}) {
+        for (auto [full, h] : {std::pair<int, double *>{0, out}, {1, outM}}) {
             if (!h) continue;
-            soa_to_aos<<<grid, 256, 0, st>>>(slice(*v), stage + 3 * off, (int64_t)cnt);
-            UPPASD_CUDA_TRY(cudaGetLastError());
+            if ((rc = structured_store_range(s, stage, full, k0, kn, st))) return rc;
             UPPASD_CUDA_TRY(cudaMemcpyAsync(h + 3 * off, stage + 3 * off, 3 * cnt * sizeof(double),
                                             cudaMemcpyDeviceToHost, st));
         }

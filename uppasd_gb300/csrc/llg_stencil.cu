@@ -1112,6 +1112,66 @@ int structured_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays 
     return UPPASD_GPU_OK;
 }
 
+// The same conversions between the caller's (3, natom, mensemble) layout (a device copy
+// of it) and the structured state, for the host blocks (abi.cu:sd_run_io): the generic
+// e / eM are left as they are (the structured state owns the spins until the next sync).
+// from_aos_structured writes what to_structured writes for e = aos; to_aos_structured
+// writes what from_structured and soa_to_aos give for e (full = 0) or eM (full = 1).
+__global__ void from_aos_structured(SParams p, const double *aos, const int8_t *species, int master) {
+    long long t = (long long)p.k0 * p.nsite + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nsite * (p.k0 + p.kn)) return;
+    int k = (int)(t / p.nsite);
+    long long i = t - (long long)k * p.nsite;
+    int b = (int)(i & 1);
+    long long cell = i >> 1;
+    int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
+    long long u = uidx(p, k, b, x, y, z);
+    double e0 = aos[3 * t], e1 = aos[3 * t + 1], e2 = aos[3 * t + 2];
+    float w = species ? (float)species[i] : 0.f;
+    float h0 = (float)e0, h1 = (float)e1, h2 = (float)e2;
+    store_mirror(p, p.mt, k, b, x, y, z, make_float4(h0, h1, h2, w));
+    if (master == 1) {
+        p.mx[u] = e0;
+        p.my[u] = e1;
+        p.mz[u] = e2;
+    } else {
+        p.lox[u] = (float)(e0 - (double)h0);
+        p.loy[u] = (float)(e1 - (double)h1);
+        p.loz[u] = (float)(e2 - (double)h2);
+    }
+}
+
+__global__ void to_aos_structured(SParams p, double *aos, const double *mmom, int master, int full) {
+    long long t = (long long)p.k0 * p.nsite + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.nsite * (p.k0 + p.kn)) return;
+    int k = (int)(t / p.nsite);
+    long long i = t - (long long)k * p.nsite;
+    int b = (int)(i & 1);
+    long long cell = i >> 1;
+    int x = (int)(cell % p.L1), y = (int)((cell / p.L1) % p.L2), z = (int)(cell / ((long long)p.L1 * p.L2));
+    long long u = uidx(p, k, b, x, y, z);
+    double e0, e1, e2;
+    if (master == 1) {
+        e0 = p.mx[u];
+        e1 = p.my[u];
+        e2 = p.mz[u];
+    } else {
+        float4 h = p.mt[pidx(p, k, b, x, y, z)];
+        e0 = (double)h.x + (double)p.lox[u];
+        e1 = (double)h.y + (double)p.loy[u];
+        e2 = (double)h.z + (double)p.loz[u];
+    }
+    if (full) {
+        const double m = mmom[t];
+        e0 *= m;
+        e1 *= m;
+        e2 *= m;
+    }
+    aos[3 * t] = e0;
+    aos[3 * t + 1] = e1;
+    aos[3 * t + 2] = e2;
+}
+
 int structured_load_state(Sim &s) {
     StructuredFast *f = s.fast;
     long long total = f->p.nsite * f->p.kn;
@@ -1258,15 +1318,16 @@ int structured_step(Sim &s, int64_t step_offset, int phase) {
 }
 
 // The ensemble-range forms the pipelined host run (abi.cu:sd_run_io) issues per group:
-// conversions from and to the generic state and nsteps steps, all on stream st.  The
+// conversions from and to the caller's layout and nsteps steps, all on stream st.  The
 // steps read the device step counter, which the caller advances once all groups are done.
-int structured_load_range(Sim &s, int k0, int kn, cudaStream_t st) {
+// aos: the device copy of the caller's (3, natom, mensemble) array
+int structured_load_range(Sim &s, const double *aos, int k0, int kn, cudaStream_t st) {
     StructuredFast *f = s.fast;
     SParams p = f->p;
     p.k0 = k0;
     p.kn = kn;
     const long long total = p.nsite * kn;
-    to_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, s.e.x, s.e.y, s.e.z, f->species, f->master);
+    from_aos_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, aos, f->species, f->master);
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }
@@ -1279,14 +1340,14 @@ int structured_steps_range(Sim &s, int64_t nsteps, int k0, int kn, cudaStream_t 
     return UPPASD_GPU_OK;
 }
 
-int structured_store_range(Sim &s, int k0, int kn, cudaStream_t st) {
+// the unit (full = 0) or full (full = 1) moments into aos, the caller's layout
+int structured_store_range(Sim &s, double *aos, int full, int k0, int kn, cudaStream_t st) {
     StructuredFast *f = s.fast;
     SParams p = f->p;
     p.k0 = k0;
     p.kn = kn;
     const long long total = p.nsite * kn;
-    from_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, s.e.x, s.e.y, s.e.z, s.eM.x, s.eM.y, s.eM.z,
-                                                                      s.llg.mmom, f->master);
+    to_aos_structured<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(p, aos, s.llg.mmom, f->master, full);
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }
