@@ -893,7 +893,10 @@ def run_gb300(args, w):
         ms = _time_steps(sim, stream, args.steps, args.warmup, world)
     value = nspin * args.steps * world / (ms * 1e-3)
     graphs, rem = divmod(args.steps, 16)
-    launches = graphs * (16 * 2 + 1) + rem * 2 + (1 if rem else 0)
+    # a captured 16-step graph: predictor and corrector per step, on the structured path once
+    # per ensemble half (two chains), and the step-counter kernel
+    chains = 2 if prec in (1, 2) and lat.mensemble >= 2 else 1
+    launches = graphs * (16 * 2 * chains + 1) + rem * 2 + (1 if rem else 0)
     kt = sim.time_kernels(3)
     peak, peak_kind = measured_peaks()
     kname = KERNEL_NAMES[prec][1 if kt["correct_ms"] >= kt["predict_ms"] else 0]
@@ -908,23 +911,34 @@ def run_gb300(args, w):
     # one sd_run_io call per block: the block's input copied in, `inner` steps, the result
     # copied out; on the structured path the ensemble groups' copies overlap the other
     # groups' steps
-    sim.run_io(host, inner, host_out)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(max(1, args.e2e_rounds)):
-        sim.run_io(host, inner, host_out)
-    torch.cuda.synchronize()
-    e2e_s = dist_max(time.perf_counter() - t0, world)
-    e2e_val = nspin * inner * max(1, args.e2e_rounds) * world / e2e_s
+    rounds = max(1, args.e2e_rounds)
+
+    def timed_blocks(block, reps=3):
+        # three warm-up blocks, then the median of `reps` timings of `rounds` blocks each (a
+        # single timing picks up the host's occasional multi-millisecond stalls)
+        for _ in range(3):
+            block()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            for _ in range(rounds):
+                block()
+            torch.cuda.synchronize()
+            ts.append(dist_max(time.perf_counter() - t0, world))
+        return statistics.median(ts), ts
+
+    e2e_s, e2e_reps = timed_blocks(lambda: sim.run_io(host, inner, host_out))
+    e2e_val = nspin * inner * rounds * world / e2e_s
     # the same blocks as three calls in turn (put_moments, sd_run, get_moments)
-    t0 = time.perf_counter()
-    for _ in range(max(1, args.e2e_rounds)):
+
+    def seq_block():
         sim.put_moments(host)
         sim.evolve(inner)
         sim.get_moments(out=host_out)
-    torch.cuda.synchronize()
-    seq_s = dist_max(time.perf_counter() - t0, world)
-    e2e_seq = nspin * inner * max(1, args.e2e_rounds) * world / seq_s
+
+    seq_s, seq_reps = timed_blocks(seq_block)
+    e2e_seq = nspin * inner * rounds * world / seq_s
     variants = {}
     if not args.no_variants:
         # the same blocks of `inner` steps with the state handed to the host after each
@@ -1033,9 +1047,12 @@ def run_gb300(args, w):
                 "bytes_per_call": {"h2d": host.nbytes, "d2h": host.nbytes},
                 "note": "one sd_run_io call per block (emom in from pinned host memory, inner steps, emom out "
                         "to pinned host memory; the ensemble groups' copies overlap the other groups' steps); "
-                        "the per-step bytes are one call's copies over its steps",
-                "sequential_calls": {"value": e2e_seq, "unit": "atom-steps/s",
-                                     "note": "put_moments + sd_run + get_moments in turn, same blocks and bytes"}},
+                        "the per-step bytes are one call's copies over its steps; after 3 warm-up blocks, the "
+                        "median of 3 timings of e2e_rounds blocks each (all three in rep_seconds)",
+                "blocks_per_timing": rounds, "rep_seconds": e2e_reps,
+                "sequential_calls": {"value": e2e_seq, "unit": "atom-steps/s", "rep_seconds": seq_reps,
+                                     "note": "put_moments + sd_run + get_moments in turn, same blocks, bytes "
+                                             "and timing"}},
         "oracle_error": oracle_err,
         "configs": configs,
         "clocks": clk.summary(),
@@ -1058,7 +1075,7 @@ def main():
     ap.add_argument("--workload", default="alloy2m", choices=sorted(WORKLOADS))
     ap.add_argument("--precision", default="auto", choices=["auto", "0", "1", "2"])
     ap.add_argument("--e2e-inner", type=int, default=10)
-    ap.add_argument("--e2e-rounds", type=int, default=3)
+    ap.add_argument("--e2e-rounds", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the double-single master and general-Hamiltonian variant timings")

@@ -45,6 +45,41 @@ int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps);
 int mixed_coefficients(Sim &s);
 void mixed_temperature(Sim &s, const double *temp_array);
 
+static int io_streams(Sim &s) {
+    if (s.io_start) return UPPASD_GPU_OK;
+    cudaStream_t st[Sim::kIoGroups] = {};
+    cudaEvent_t ev[Sim::kIoGroups] = {}, in[Sim::kIoGroups] = {}, start = nullptr;
+    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
+    // earlier groups at higher priority: their input arrives first, so they finish first
+    // and their output copies run under the later groups' steps (measured 2-3 % faster per
+    // block than equal priorities; the reverse order was slower)
+    int lowest = 0, highest = 0;
+    cudaDeviceGetStreamPriorityRange(&lowest, &highest);
+    for (int g = 0; g < Sim::kIoGroups && e == cudaSuccess; ++g) {
+        const int prio = highest + (lowest - highest) * g / (Sim::kIoGroups - 1);
+        e = cudaStreamCreateWithPriority(&st[g], cudaStreamNonBlocking, prio);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&in[g], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        for (int g = 0; g < Sim::kIoGroups; ++g) {
+            if (st[g]) cudaStreamDestroy(st[g]);
+            if (ev[g]) cudaEventDestroy(ev[g]);
+            if (in[g]) cudaEventDestroy(in[g]);
+        }
+        if (start) cudaEventDestroy(start);
+        set_error(std::string("sd_run_io: streams: ") + cudaGetErrorString(e));
+        return UPPASD_GPU_ECUDA;
+    }
+    for (int g = 0; g < Sim::kIoGroups; ++g) {
+        s.io_stream[g] = st[g];
+        s.io_ev[g] = ev[g];
+        s.io_in[g] = in[g];
+    }
+    s.io_start = start;
+    return UPPASD_GPU_OK;
+}
+
 namespace {
 
 template <typename T>
@@ -468,15 +503,37 @@ int run_steps(Sim &s, int64_t n) {
     } else {
         square_mirror_stale(s);
     }
+    // structured path with several ensembles: the captured steps run as two independent
+    // chains of ensemble halves on two streams, so the last partial wave of one half's
+    // kernels fills with the other half's CTAs (the step 4-5 % shorter on the 100^3 alloy
+    // x 8 than one chain; four or eight chains gained less)
+    const int SG = structured(s) && s.ham.mensemble >= 2 ? 2 : 1;
+    if (SG > 1 && (rc = io_streams(s))) return rc;
     // the FFT form of the dipolar field issues cuFFT launches, kept out of the captured graph
     if (!s.graph && n >= G && s.ham.do_dip != 3) {
         cudaGraph_t g;
         UPPASD_CUDA_TRY(cudaStreamBeginCapture(s.stream, cudaStreamCaptureModeThreadLocal));
-        for (int j = 0; j < G; ++j)
-            if ((rc = one_step(s, j))) {
-                cudaStreamEndCapture(s.stream, &g);
-                return rc;
+        if (SG > 1) {
+            // fork and join through events, inside the capture
+            UPPASD_CUDA_TRY(cudaEventRecord(s.io_start, s.stream));
+            const int M = s.ham.mensemble;
+            for (int q = 0; q < SG; ++q) {
+                const int k0 = (int)((int64_t)M * q / SG), kn = (int)((int64_t)M * (q + 1) / SG) - k0;
+                UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.io_stream[q], s.io_start, 0));
+                if ((rc = structured_steps_range(s, G, k0, kn, s.io_stream[q]))) {
+                    cudaStreamEndCapture(s.stream, &g);
+                    return rc;
+                }
+                UPPASD_CUDA_TRY(cudaEventRecord(s.io_ev[q], s.io_stream[q]));
+                UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.io_ev[q], 0));
             }
+        } else {
+            for (int j = 0; j < G; ++j)
+                if ((rc = one_step(s, j))) {
+                    cudaStreamEndCapture(s.stream, &g);
+                    return rc;
+                }
+        }
         advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, G);
         UPPASD_CUDA_TRY(cudaStreamEndCapture(s.stream, &g));
         cudaError_t e = cudaGraphInstantiate(&s.graph, g, 0);
@@ -819,41 +876,6 @@ int uppasd_gpu_sd_run(uppasd_gpu_sim *w, int64_t nsteps) {
 }
 
 namespace uppasd {
-
-static int io_streams(Sim &s) {
-    if (s.io_start) return UPPASD_GPU_OK;
-    cudaStream_t st[Sim::kIoGroups] = {};
-    cudaEvent_t ev[Sim::kIoGroups] = {}, in[Sim::kIoGroups] = {}, start = nullptr;
-    cudaError_t e = cudaEventCreateWithFlags(&start, cudaEventDisableTiming);
-    // earlier groups at higher priority: their input arrives first, so they finish first
-    // and their output copies run under the later groups' steps (measured 2-3 % faster per
-    // block than equal priorities; the reverse order was slower)
-    int lowest = 0, highest = 0;
-    cudaDeviceGetStreamPriorityRange(&lowest, &highest);
-    for (int g = 0; g < Sim::kIoGroups && e == cudaSuccess; ++g) {
-        const int prio = highest + (lowest - highest) * g / (Sim::kIoGroups - 1);
-        e = cudaStreamCreateWithPriority(&st[g], cudaStreamNonBlocking, prio);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[g], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&in[g], cudaEventDisableTiming);
-    }
-    if (e != cudaSuccess) {
-        for (int g = 0; g < Sim::kIoGroups; ++g) {
-            if (st[g]) cudaStreamDestroy(st[g]);
-            if (ev[g]) cudaEventDestroy(ev[g]);
-            if (in[g]) cudaEventDestroy(in[g]);
-        }
-        if (start) cudaEventDestroy(start);
-        set_error(std::string("sd_run_io: streams: ") + cudaGetErrorString(e));
-        return UPPASD_GPU_ECUDA;
-    }
-    for (int g = 0; g < Sim::kIoGroups; ++g) {
-        s.io_stream[g] = st[g];
-        s.io_ev[g] = ev[g];
-        s.io_in[g] = in[g];
-    }
-    s.io_start = start;
-    return UPPASD_GPU_OK;
-}
 
 // put + steps + get of the structured path, pipelined: the ensembles split into up to
 // kIoGroups contiguous groups, each on its own stream copying its slice of the
