@@ -341,8 +341,9 @@ int uppasd_gpu_mcbatch_set_replica_ids(uppasd_gpu_mcbatch *b, int32_t first_id);
  * launch; run/check then return UPPASD_GPU_ESTATE and reset the barrier state, so the
  * batch stays usable (its spins are those the groups had reached).  Whatever the
  * poll limit, a wait also gives up after about two seconds.  For testing the error path:
- * a limit of 1 makes a CTA give up at the first poll that finds its group's barrier
- * incomplete, which a group of two or more CTAs meets within a few barriers. */
+ * a limit of 1 makes every CTA of a group of two or more give up at the group's first
+ * barrier, on arrival (so no CTA waits for another and the outcome does not depend on
+ * timing). */
 int uppasd_gpu_mcbatch_set_spin_limit(uppasd_gpu_mcbatch *b, int64_t limit);
 /* Replica exchange (the swap step of MonteCarlo/pt_driver.f90:58-367 on the batch):
  * after every launch, replicas holding adjacent temperatures of one size swap

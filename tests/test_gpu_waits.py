@@ -1,9 +1,10 @@
 """Bounded device waits: a wait that runs past its limit returns an error status that
 the host reads, and the context stays usable.
 
-* the replica-group barrier of the batched Monte Carlo kernel: with its iteration
-  limit set to 1, any group of two or more CTAs gives up at its first barrier and
-  the run returns UPPASD_GPU_ESTATE; with the default limit the next run works;
+* the replica-group barrier of the batched Monte Carlo kernel: with its poll limit set
+  to 1, every CTA of a group of two or more gives up at the group's first barrier, on
+  arrival, and the run returns UPPASD_GPU_ESTATE; with the default limit the next run
+  works;
 * the tensor-core pipeline's mbarrier wait: a self-test CTA waits on an mbarrier that
   nothing arrives at (no copy or MMA in flight) and reports code 4; a GEMM
   afterwards is correct.

@@ -99,7 +99,8 @@ class ReplicaBatch:
         _lib.call("uppasd_gpu_mcbatch_set_sweep", self.h, int(sweep))
 
     def set_spin_limit(self, limit: int = 0):
-        """Iteration limit of the replica-group barrier's wait (0: the default)."""
+        """Poll limit of the replica-group barrier's wait (0: the default); 1 makes every
+        CTA of a multi-CTA group give up at the group's first barrier (the error path)."""
         _lib.call("uppasd_gpu_mcbatch_set_spin_limit", self.h, int(limit))
 
     # ---- replica exchange ----

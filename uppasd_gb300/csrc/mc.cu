@@ -197,6 +197,8 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
     const double delta = (double)(2.0f / 25.0f) * pow(s.ham.kbolt * temperature / s.ham.mub, 0.20);
     const int hb = mode == 'H' ? 1 : 0;
     int rc;
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, s.device);
     for (int64_t sw = 0; sw < nsweeps; ++sw) {
         // dipoles: Metropolis takes the field of the sweep's start as an extra external
         // field (montecarlo.f90:216-231); the heat bath has it in the site field
@@ -210,7 +212,10 @@ int mc_checkerboard_sweeps(Sim &s, char mode, double temperature, int64_t nsweep
             if (n == 0) continue;
             if (s.ham.do_dip && hb && (rc = dipole_field(s, s.eM))) return rc;
             int64_t tot = (int64_t)n * s.ham.mensemble;
-            mc_colour_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s.stream>>>(
+            // small colours in 64-thread blocks, spread over more SMs (one site's energy
+            // change and draw is a long dependent FP64 chain), as the FP64 LLG steps do
+            const int block = tot < (int64_t)sms * 1024 ? 64 : 256;
+            mc_colour_kernel<<<(unsigned)((tot + block - 1) / block), block, 0, s.stream>>>(
                 s.ham, s.e, s.eM, s.llg.mmom, s.colour_sites + beg, n, hb, temperature, delta, tk, s.llg.seed,
                 s.mc_sweep);
         }

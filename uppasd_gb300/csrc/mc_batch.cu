@@ -128,7 +128,13 @@ __device__ __forceinline__ bool group_barrier(const MBParams &p, int r, int n) {
         const unsigned long long old = atomicAdd(ctr, 1ull);
         const unsigned long long target = (old / (unsigned long long)n + 1ull) * (unsigned long long)n;
         long long it = 0, t0 = 0;
-        while (ld_acquire_u64(ctr) < target) {
+        if (p.spin_limit == 1) {
+            // the error path on demand: every CTA of the group gives up at its arrival,
+            // so none of them waits for another
+            atomicExch(p.err, 1);
+            failed = 1;
+        }
+        while (!failed && ld_acquire_u64(ctr) < target) {
             // give up after spin_limit polls that found the barrier incomplete, or after
             // about two seconds, whichever comes first (the clock is read from poll 64 on)
             ++it;
