@@ -974,13 +974,14 @@ def run_gb300(args, w):
         except Exception as exc:
             variants[vname] = {"error": str(exc)}
         # general Hamiltonians (neighbour lists, DMI, anisotropy): FP64 path and FP32 gather
-        # with the FP64 state as master, on the same lattice
+        # with the FP64 state (precision 3) or a double-single pair (precision 4) as master,
+        # on the same lattice
         try:
             wg = WORKLOADS["square1024x4"]
             lg = build_lattice(wg)
             eg = random_state(lg.mensemble, lg.natom, seed=11 + rank)
             gen = {"workload": "square1024x4", "description": wg["desc"], "spins": lg.natom * lg.mensemble}
-            for pg, key in ((0, "fp64"), (3, "fp32_gather_fp64_master")):
+            for pg, key in ((0, "fp64"), (3, "fp32_gather_fp64_master"), (4, "fp32_gather_double_single_master")):
                 sg = _make_sim(lg, wg, pg, 3000 + rank, eg)
                 sg.set_stream(stream.cuda_stream)
                 msg = _time_steps(sg, stream, 16, 4, world)

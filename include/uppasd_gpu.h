@@ -67,7 +67,14 @@ typedef struct {
                                             spin master and renormalisation (every SDEalgh of
                                             precision 0, perp included); mc_run 'H' and 'M'
                                             run in FP32 on the same mirror (mc_run_temps 'M'
-                                            on the FP64 path) */
+                                            on the FP64 path);
+                                          4 as 3 with a double-single (float-float) spin
+                                            master renormalised in error-free FP32
+                                            arithmetic, for the norm-preserving solvers
+                                            (SDEalgh 1, 5, 6, 7; -7 for 4 and 11): GB300's
+                                            FP64 pipe sets precision 3's step time; the FP64
+                                            state is made from the master when a call reads
+                                            it */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;
@@ -133,7 +140,7 @@ int uppasd_gpu_set_relaxtime(uppasd_gpu_sim *s, double relaxtime);
  * Carlo energy change (MonteCarlo/montecarlo_common.f90:502-510) and in the exchange
  * slot of the energy (the pair energy, Hamiltonian/energy.f90:244-247; as there, no
  * separate DM energy is evaluated while the tensor is on, the DM field stays).
- * NULL switches back to ncoup.  -7 on the structured path (precision >= 1). */
+ * NULL switches back to ncoup.  -7 on the structured path (precision 1, 2). */
 int uppasd_gpu_set_jtensor(uppasd_gpu_sim *s, const double *j_tens);
 
 /* Dipole-dipole field (input keyword do_dip, Hamiltonian/dipolemanager.f90:54-113).
@@ -213,8 +220,8 @@ int uppasd_gpu_mc_run_square(uppasd_gpu_sim *s, int32_t L, double temperature, i
 int uppasd_gpu_mc_run_square_temps(uppasd_gpu_sim *s, int32_t L, const double *temps, int64_t nsweeps);
 
 /* Monte Carlo sweeps with one temperature per ensemble (temps[mensemble], K): the
- * chain of uppasd_gpu_mc_run with T taken per ensemble (on precision 3 the heat bath
- * draws in FP32 as there). */
+ * chain of uppasd_gpu_mc_run with T taken per ensemble (on precision 3 and 4 the heat
+ * bath draws in FP32 as there). */
 int uppasd_gpu_mc_run_temps(uppasd_gpu_sim *s, char mode, const double *temps, int64_t nsweeps);
 
 /* Parallel tempering of pt_iphase (pt_driver.f90:58-367) with the ensembles as its

@@ -1,6 +1,9 @@
 """Precision 3: FP32 gather over the caller's neighbour lists with the FP64 state as
 master (renormalised in FP64 every step), on Hamiltonians outside the structured bcc
 path: exchange (scalar or tensor), DMI, anisotropy and Zeeman, midpoint and Depondt.
+Precision 4: the same with a double-single master (hi = the FP32 mirror, lo a residual,
+renormalised in error-free FP32 arithmetic), for the norm-preserving solvers; the tests
+of the solvers it takes run on both.
 
 The field, thermal field and rotation run in FP32, so trajectories are compared with
 the FP64 oracle at FP32-scale tolerances that grow with the step count (a random
@@ -24,22 +27,23 @@ def _rand_unit(rng, shape):
     return e / np.linalg.norm(e, axis=-1, keepdims=True)
 
 
-def _pair(lat, solver, temp, e0, seed=31, damping=0.05):
+def _pair(lat, solver, temp, e0, seed=31, damping=0.05, prec=3):
     sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=damping, temperature=temp, seed=seed,
-                        emom=e0, precision=3)
+                        emom=e0, precision=prec)
     o = po.Oracle(lat)
     o.set_moments(e0)
     o.make_llg(solver, 1e-16, damping, temp, 1.0, noise_mode=po.NOISE_PHILOX, seed=seed)
     return sim, o
 
 
+@pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("kind,solver", [("square_dmi_aniso", 1), ("square_dmi_aniso", 5), ("kagome_tensor", 5),
                                          ("kagome_tensor", 1)])
-def test_T0_against_oracle(kind, solver):
+def test_T0_against_oracle(kind, solver, prec):
     lat = (lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0) if kind == "square_dmi_aniso"
            else lattice.kagome(12, -1.0, 0.1, 0.05, 1.0, 0.2)).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(41), (2, lat.natom, 3))
-    sim, o = _pair(lat, solver, 0.0, e0)
+    sim, o = _pair(lat, solver, 0.0, e0, prec=prec)
     done = 0
     for n, tol in CHECKPOINTS.items():
         sim.evolve(n - done)
@@ -52,11 +56,12 @@ def test_T0_against_oracle(kind, solver):
     sim.close()
 
 
+@pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("solver", [1, 5])
-def test_thermal_philox_against_oracle(solver):
+def test_thermal_philox_against_oracle(solver, prec):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(42), (2, lat.natom, 3))
-    sim, o = _pair(lat, solver, 50.0, e0)
+    sim, o = _pair(lat, solver, 50.0, e0, prec=prec)
     sim.evolve(200)
     for _ in range(200):
         o.sd_step()
@@ -64,12 +69,13 @@ def test_thermal_philox_against_oracle(solver):
     sim.close()
 
 
-def test_injected_noise_against_oracle():
+@pytest.mark.parametrize("prec", [3, 4])
+def test_injected_noise_against_oracle(prec):
     lat = lattice.kagome(12).with_ensembles(1)
     e0 = _rand_unit(np.random.default_rng(43), (1, lat.natom, 3))
     nsteps = 100
     normals = po.ziggurat_stream(3, nsteps * 3 * lat.natom).reshape(nsteps, 1, lat.natom, 3)
-    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.05, temperature=100.0, emom=e0, precision=3)
+    sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.05, temperature=100.0, emom=e0, precision=prec)
     sim.set_noise(normals)
     sim.evolve(nsteps)
     o = po.Oracle(lat)
@@ -85,13 +91,14 @@ def test_agrees_with_structured_path_on_the_alloy():
     lat = lattice.bcc_alloy(6, seed=9).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(44), (2, lat.natom, 3))
     out = []
-    for prec in (1, 3):
+    for prec in (1, 3, 4):
         sim = GpuSimulation(lat, sdealgh=5, delta_t=1e-16, damping=0.1, temperature=300.0, seed=21, emom=e0,
                             precision=prec)
         sim.evolve(100)
         out.append(sim.get_moments())
         sim.close()
     assert np.max(np.abs(out[0] - out[1])) <= 1e-4
+    assert np.max(np.abs(out[0] - out[2])) <= 1e-4
 
 
 def test_state_changes_between_runs_are_seen():
@@ -101,7 +108,7 @@ def test_state_changes_between_runs_are_seen():
     rng = np.random.default_rng(45)
     e0, e1 = _rand_unit(rng, (2, lat.natom, 3)), _rand_unit(rng, (2, lat.natom, 3))
     res = []
-    for prec in (0, 3):
+    for prec in (0, 3, 4):
         sim = GpuSimulation(lat, sdealgh=1, delta_t=1e-16, damping=0.1, temperature=0.0, seed=9, emom=e0,
                             precision=prec)
         sim.evolve(20)
@@ -114,15 +121,16 @@ def test_state_changes_between_runs_are_seen():
         res.append(sim.get_moments())
         sim.close()
     assert np.max(np.abs(res[0] - res[1])) <= 1e-4
+    assert np.max(np.abs(res[0] - res[2])) <= 1e-4
 
 
-@pytest.mark.parametrize("solver", [4, 6, 7, 11])
-def test_other_solvers_T0_against_oracle(solver):
+@pytest.mark.parametrize("solver,prec", [(4, 3), (6, 3), (7, 3), (11, 3), (6, 4), (7, 4)])
+def test_other_solvers_T0_against_oracle(solver, prec):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(47), (2, lat.natom, 3))
     tau = 1e-15 if solver == 11 else 0.0
     sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=0.0, seed=31, emom=e0,
-                        precision=3, relaxtime=tau)
+                        precision=prec, relaxtime=tau)
     o = po.Oracle(lat)
     o.set_moments(e0)
     o.make_llg(solver, 1e-16, 0.05, 0.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=31, relaxtime=tau)
@@ -138,13 +146,14 @@ def test_other_solvers_T0_against_oracle(solver):
     sim.close()
 
 
-@pytest.mark.parametrize("solver", [1, 4, 5, 6, 7, 11])
-def test_perp_against_oracle(solver):
+@pytest.mark.parametrize("solver,prec", [(1, 3), (4, 3), (5, 3), (6, 3), (7, 3), (11, 3), (1, 4), (5, 4), (6, 4),
+                                         (7, 4)])
+def test_perp_against_oracle(solver, prec):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(48), (2, lat.natom, 3))
     tau = 1e-15 if solver == 11 else 0.0
     sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=50.0, seed=33, emom=e0,
-                        precision=3, relaxtime=tau, perp=True)
+                        precision=prec, relaxtime=tau, perp=True)
     o = po.Oracle(lat)
     o.set_moments(e0)
     o.make_llg(solver, 1e-16, 0.05, 50.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=33, relaxtime=tau, perp=True)
@@ -164,8 +173,9 @@ def test_scope():
     sim.close()
 
 
+@pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("kind", ["kagome_tensor", "square_dmi_aniso"])
-def test_heat_bath_chain_against_oracle(kind):
+def test_heat_bath_chain_against_oracle(kind, prec):
     """mc_run 'H' at precision 3: the FP64 path's checkerboard chain (same colouring,
     same Philox draws) with the field and the draw in FP32, per spin within 2e-4
     after 3 sweeps."""
@@ -173,7 +183,7 @@ def test_heat_bath_chain_against_oracle(kind):
            else lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0)).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(46), (2, lat.natom, 3))
     T = 30.0
-    sim = GpuSimulation(lat, emom=e0, seed=61, precision=3, sdealgh=5)
+    sim = GpuSimulation(lat, emom=e0, seed=61, precision=prec, sdealgh=5)
     sim.relax("H", T, 3)
     g = sim.get_moments()
     sim.close()
@@ -185,8 +195,9 @@ def test_heat_bath_chain_against_oracle(kind):
     assert np.max(np.abs(g - o.emom)) < 2e-4
 
 
+@pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("kind", ["kagome_tensor", "square_dmi_aniso"])
-def test_metropolis_sweep_follows_the_fp64_chain(kind):
+def test_metropolis_sweep_follows_the_fp64_chain(kind, prec):
     """mc_run 'M' at precision 3 makes the FP64 path's trials (same Philox words, same
     colouring) and decisions with the energy change in FP32: after one sweep from the same
     state nearly every spin agrees with the FP64 chain to FP32 rounding (a decision can
@@ -195,8 +206,8 @@ def test_metropolis_sweep_follows_the_fp64_chain(kind):
            else lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0)).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(49), (2, lat.natom, 3))
     out = []
-    for prec in (3, 0):
-        sim = GpuSimulation(lat, emom=e0, seed=63, precision=prec, sdealgh=5)
+    for p in (prec, 0):
+        sim = GpuSimulation(lat, emom=e0, seed=63, precision=p, sdealgh=5)
         sim.relax("M", 30.0, 1)
         out.append(sim.get_moments())
         sim.close()
@@ -230,8 +241,9 @@ def test_metropolis_statistics_match_the_fp64_path():
     assert abs(m0m - m3m) <= 3 * np.hypot(m0s, m3s), stats
 
 
+@pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("solver", [1, 5])
-def test_T0_per_site_field_and_anisotropy(solver):
+def test_T0_per_site_field_and_anisotropy(solver, prec):
     """Precision 3 with nothing uniform: a random external field per site and per
     ensemble (the per-site branch of the FP32 field, not the single uniform entry),
     per-site uniaxial and cubic anisotropy with random axes and constants (one FP32
@@ -249,7 +261,7 @@ def test_T0_per_site_field_and_anisotropy(solver):
     lat.sb = rng.uniform(0.0, 1.0, size=N)
     lat.ncoup = lat.ncoup * rng.uniform(0.8, 1.2, size=(N, 1))
     e0 = _rand_unit(np.random.default_rng(45), (2, N, 3))
-    sim, o = _pair(lat, solver, 0.0, e0)
+    sim, o = _pair(lat, solver, 0.0, e0, prec=prec)
     done = 0
     for n, tol in CHECKPOINTS.items():
         sim.evolve(n - done)
@@ -262,3 +274,35 @@ def test_T0_per_site_field_and_anisotropy(solver):
         assert err <= tol, (n, err)
         assert np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)) <= 1e-12
     sim.close()
+
+
+def test_precision4_takes_the_norm_preserving_solvers():
+    lat = lattice.square_dmi(16, 1.0, 0.3, -0.05, 0.5, 1.0)
+    for solver in (4, 11):
+        with pytest.raises(_lib.UppasdGpuError) as ei:
+            GpuSimulation(lat, sdealgh=solver, precision=4, relaxtime=1e-15 if solver == 11 else 0.0)
+        assert ei.value.rc == -7
+
+
+@pytest.mark.parametrize("solver", [1, 5])
+def test_precision4_reads_leave_the_trajectory_unchanged(solver):
+    """The double-single master is converted to e / eM whenever the caller reads them
+    (get_moments, observables, energy terms, the field); the master itself is not touched,
+    so a run with reads between its blocks is bit-identical to one without."""
+    lat = lattice.kagome(12, -1.0, 0.1, 0.05, 1.0, 0.2).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(52), (2, lat.natom, 3))
+    out = []
+    for reads in (False, True):
+        sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=50.0, seed=5, emom=e0,
+                            precision=4)
+        for _ in range(4):
+            sim.evolve(25)
+            if reads:
+                sim.get_moments(full=True)
+                sim.observables()
+                sim.energy_terms()
+                sim.get_fields()
+        out.append(sim.get_moments(full=True))
+        sim.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert np.max(np.abs(np.linalg.norm(out[0][0], axis=-1) - 1.0)) <= 1e-12

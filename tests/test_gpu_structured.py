@@ -121,7 +121,7 @@ def _pinned(shape):
     return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
 
 
-@pytest.mark.parametrize("prec", [0, 1, 2, 3])
+@pytest.mark.parametrize("prec", [0, 1, 2, 3, 4])
 @pytest.mark.parametrize("M", [3, 8])
 @pytest.mark.parametrize("pinned", [True, False])
 def test_run_io_equals_put_run_get(prec, M, pinned):

@@ -39,11 +39,19 @@ void structured_free(Sim &s);
 int mixed_init(Sim &s);  // llg_mixed.cu
 void mixed_free(Sim &s);
 int mixed_ready(Sim &s);
+int mixed_sync(Sim &s);  // precision 4: e / eM from the double-single master
 int mixed_step(Sim &s, int64_t step_offset, int phase);
 int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const float *betak = nullptr);
 int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps);
 int mixed_coefficients(Sim &s);
 void mixed_temperature(Sim &s, const double *temp_array);
+
+// e / eM up to date from the master of the path that owns the state between calls
+int sync_state(Sim &s) {
+    if (structured(s)) return structured_sync_state(s);
+    if (s.precision == 4) return mixed_sync(s);
+    return UPPASD_GPU_OK;
+}
 
 static int io_streams(Sim &s) {
     if (s.io_start) return UPPASD_GPU_OK;
@@ -309,7 +317,7 @@ int validate(const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
         return bad("SDEalgh must be 1, 4, 5, 6, 7 or 11");
     if (!(c->delta_t > 0.0) || !(c->bn > 0.0)) return bad("delta_t and bn must be positive");
     if (c->gpu_rng != 0 && c->gpu_rng != 1) return bad("gpu_rng must be 0 (Philox) or 1 (injected)");
-    if (c->precision < 0 || c->precision > 3) return bad("precision must be 0, 1, 2 or 3");
+    if (c->precision < 0 || c->precision > 4) return bad("precision must be 0, 1, 2, 3 or 4");
     for (int i = 0; i < c->natom; ++i)
         if (a->aham[i] < 1 || a->aham[i] > c->nham) return bad("aham out of range");
     for (int h = 0; h < c->nham; ++h) {
@@ -444,7 +452,7 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     s.precision = c->precision;
     if (structured(s)) {
         if ((rc = structured_init(s, c, a))) return rc;
-    } else if (c->precision == 3) {
+    } else if (c->precision == 3 || c->precision == 4) {
         if ((rc = mixed_init(s))) return rc;
     }
     if ((rc = uppasd_gpu_put_moments(reinterpret_cast<uppasd_gpu_sim *>(&s), a->emom))) return rc;
@@ -491,13 +499,13 @@ void destroy(Sim &s) {
 
 int one_step(Sim &s, int64_t off, int phase = 3) {
     if (structured(s)) return structured_step(s, off, phase);
-    return s.precision == 3 ? mixed_step(s, off, phase) : llg_generic_step(s, off, phase);
+    return mixed_path(s) ? mixed_step(s, off, phase) : llg_generic_step(s, off, phase);
 }
 
 int run_steps(Sim &s, int64_t n) {
     const int G = 16;
     int rc;
-    if (s.precision == 3) {
+    if (mixed_path(s)) {
         s.sqm_valid = 0;  // the mixed steps keep their own mirror current
         if ((rc = mixed_ready(s))) return rc;
     } else {
@@ -625,6 +633,7 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
     }
     Sim &s = w->s;
     uppasd::square_mirror_stale(s);
+    s.mix.e_stale = 0;  // e is written whole here: it is the state from now on
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     const unsigned grid = (unsigned)((n + 255) / 256);
     cudaError_t e = cudaSuccess;
@@ -664,7 +673,7 @@ int uppasd_gpu_get_moments(uppasd_gpu_sim *w, double *emom, double *emomM) {
     }
     Sim &s = w->s;
     int rc;
-    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
+    if ((rc = uppasd::sync_state(s))) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
     cudaError_t e = cudaSuccess;
     const unsigned grid = (unsigned)((n + 255) / 256);
@@ -698,7 +707,7 @@ int uppasd_gpu_set_temperature(uppasd_gpu_sim *w, const double *temp_array) {
         if (rc) return rc;
         uppasd::drop_graph(s);
     }
-    if (s.precision == 3) {
+    if (uppasd::mixed_path(s)) {
         uppasd::mixed_temperature(s, temp_array);
         uppasd::drop_graph(s);  // the uniform temperature is a step argument, captured by value
     }
@@ -782,12 +791,12 @@ int uppasd_gpu_set_jtensor(uppasd_gpu_sim *w, const double *j_tens) {
     h.jt = nullptr;
     h.do_jtensor = 0;
     s.sq.L = 0;  // the structured square recognition no longer holds
-    if (!j_tens) return s.precision == 3 ? uppasd::mixed_coefficients(s) : UPPASD_GPU_OK;
+    if (!j_tens) return uppasd::mixed_path(s) ? uppasd::mixed_coefficients(s) : UPPASD_GPU_OK;
     int rc = uppasd::upload(s, &h.jt, jt);
     if (rc) return rc;
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
     h.do_jtensor = 1;
-    if (s.precision == 3) return uppasd::mixed_coefficients(s);
+    if (uppasd::mixed_path(s)) return uppasd::mixed_coefficients(s);
     return UPPASD_GPU_OK;
 }
 
@@ -1017,7 +1026,7 @@ int uppasd_gpu_sd_run_measured(uppasd_gpu_sim *w, int64_t nsteps, int64_t every,
         const int b = (int)(i % 2);
         if (i < nblocks) {
             if ((rc = uppasd::run_steps(s, every))) break;
-            if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) break;
+            if ((rc = uppasd::sync_state(s))) break;
             UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.copy_ev[b], 0));  // buffer b copied out
             uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.e, s.snap_d[b], n);
             uppasd::soa_to_aos<<<grid, 256, 0, s.stream>>>(s.eM, s.snap_d[b] + 3 * n, n);
@@ -1047,7 +1056,7 @@ int uppasd_gpu_get_field(uppasd_gpu_sim *w, double *beff) {
     if (!w || !beff) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
+    if ((rc = uppasd::sync_state(s))) return rc;
     return uppasd::field_to_host(s, beff);
 }
 
@@ -1061,9 +1070,9 @@ int uppasd_gpu_mc_run(uppasd_gpu_sim *w, char mode, double temperature, int64_t 
     }
     Sim &s = w->s;
     int rc;
-    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
-    // precision 3: heat bath and Metropolis in FP32 on the mirror
-    if (s.precision == 3)
+    if ((rc = uppasd::sync_state(s))) return rc;
+    // precision 3 / 4: heat bath and Metropolis in FP32 on the mirror
+    if (uppasd::mixed_path(s))
         rc = mode == 'H' ? uppasd::mixed_heat_bath_sweeps(s, temperature, nsweeps)
                          : uppasd::mixed_metropolis_sweeps(s, temperature, nsweeps);
     else
@@ -1104,8 +1113,8 @@ int set_ensemble_temps(Sim &s, const double *temps) { return upload_temps(s, tem
 namespace {
 int sweeps_with_temps(Sim &s, char mode, int64_t nsweeps) {
     int rc;
-    if (structured(s) && (rc = structured_sync_state(s))) return rc;
-    rc = s.precision == 3 && mode == 'H' ? mixed_heat_bath_sweeps(s, 0.0, nsweeps, s.betak)
+    if ((rc = sync_state(s))) return rc;
+    rc = mixed_path(s) && mode == 'H' ? mixed_heat_bath_sweeps(s, 0.0, nsweeps, s.betak)
                                          : mc_checkerboard_sweeps(s, mode, 0.0, nsweeps, s.tk);
     if (rc) return rc;
     if (structured(s)) return structured_load_state(s);
@@ -1191,7 +1200,7 @@ int uppasd_gpu_time_kernels(uppasd_gpu_sim *w, int32_t nrep, double *ms) {
     for (auto &e : ev) UPPASD_CUDA_TRY(cudaEventCreate(&e));
     double acc[3] = {0.0, 0.0, 0.0};
     int rc = UPPASD_GPU_OK;
-    if (s.precision == 3) {
+    if (uppasd::mixed_path(s)) {
         s.sqm_valid = 0;
         if ((rc = uppasd::mixed_ready(s))) return rc;
     } else {
@@ -1227,7 +1236,7 @@ int uppasd_gpu_observables(uppasd_gpu_sim *w, double *mvec, double *mabs, double
     if (!w) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
+    if ((rc = uppasd::sync_state(s))) return rc;
     return uppasd::observables(s, mvec, mabs, energy, nullptr);
 }
 
@@ -1235,7 +1244,7 @@ int uppasd_gpu_energy_terms(uppasd_gpu_sim *w, double *terms) {
     if (!w || !terms) return UPPASD_GPU_EINVAL;
     Sim &s = w->s;
     int rc;
-    if (uppasd::structured(s) && (rc = uppasd::structured_sync_state(s))) return rc;
+    if ((rc = uppasd::sync_state(s))) return rc;
     return uppasd::observables(s, nullptr, nullptr, nullptr, nullptr, terms);
 }
 

@@ -113,4 +113,52 @@ __device__ inline void normal3_f32_fast(uint64_t seed, int64_t site, int32_t ens
     z[2] = -r1 * c1;
 }
 
+// Double-single helpers (Dekker / Knuth error-free transformations).
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    e = b - (s - a);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+
+// A unit vector held as double-single pairs (hi + lo per component, ~48 bits) plus a
+// change d: the sum, then |e|^2 - 1 from exact products, and the renormalisation by
+// 1/sqrt(1 + x) to second order (|x| below ~1e-7 for the norm-preserving updates, so the
+// truncation is below 1e-21), the correction added back with error-free sums.
+__device__ __forceinline__ void ds_add_renorm(float hi[3], float lo[3], const float d[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float sm, er;
+        two_sum(hi[c], d[c], sm, er);
+        quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
+    }
+    float n2h = 0.f, n2l = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float pp, pe, sm, er;
+        two_prod(hi[c], hi[c], pp, pe);
+        two_sum(n2h, pp, sm, er);
+        n2h = sm;
+        n2l += er + pe + 2.0f * hi[c] * lo[c];
+    }
+    float xs, xe;
+    two_sum(n2h, -1.0f, xs, xe);
+    const float xx = xs + (xe + n2l);
+    const float sm1 = xx * fmaf(0.375f, xx, -0.5f);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float corr = hi[c] * sm1 + lo[c] * sm1;
+        float sm, er;
+        two_sum(hi[c], corr, sm, er);
+        quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
+    }
+}
+
 }  // namespace uppasd

@@ -1154,6 +1154,7 @@ int uppasd_gpu_proposal_collect(uppasd_gpu_proposal *p) {
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = p->sim->s;
+    if (const int rc = sync_state(s)) return rc;  // precision 4: e from its master first
     const int rows = s.ham.mensemble * 4 * (p->L / 8) * (p->L / 8);
     if (rows > p->data_cap) {
         set_error("proposal_collect: the dataset buffer holds fewer rows than one snapshot");
@@ -1235,6 +1236,7 @@ int proposal_mix(uppasd_gpu_proposal *p, double temperature, const double *temps
         return UPPASD_GPU_EINVAL;
     }
     Sim &s = p->sim->s;
+    if (const int rc = sync_state(s)) return rc;  // precision 4: e from its master first
     const bool per_ens = temps != nullptr;
     if (per_ens) {
         const int rc0 = set_ensemble_temps(s, temps);

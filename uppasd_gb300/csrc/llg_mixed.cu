@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(256) mixed_predict(MixArgs a) {
     a.c.mp[o] = make_float4(p[0], p[1], p[2], mm);
 }
 
-template <int ALG>
+template <int ALG, bool DS>
 __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
     const int N = a.h.natom, M = a.h.mensemble;
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -388,6 +388,17 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         d[0] = out[0];
         d[1] = out[1];
         d[2] = out[2];
+    }
+    if constexpr (DS) {
+        // double-single master (precision 4): hi is the mirror, the change and the
+        // renormalisation in error-free FP32 arithmetic; e / eM are made on demand
+        float hi[3] = {e[0], e[1], e[2]}, lo[3] = {a.c.lox[o], a.c.loy[o], a.c.loz[o]};
+        ds_add_renorm(hi, lo, d);
+        a.c.lox[o] = lo[0];
+        a.c.loy[o] = lo[1];
+        a.c.loz[o] = lo[2];
+        a.c.mt[o] = make_float4(hi[0], hi[1], hi[2], mm);
+        return;
     }
     // FP64 master: add the change, renormalise, refresh the mirror
     double e0 = a.e.x[o] + (double)d[0], e1 = a.e.y[o] + (double)d[1], e2 = a.e.z[o] + (double)d[2];
@@ -510,6 +521,34 @@ __global__ void __launch_bounds__(256) mixed_metropolis(HamDev h, MixedDev c, co
 __global__ void mixed_mirror(Vec3D e, const double *mmom, float4 *mt, int64_t n) {
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) mt[t] = make_float4((float)e.x[t], (float)e.y[t], (float)e.z[t], (float)mmom[t]);
+}
+
+// precision 4: the double-single master from e (hi the mirror, lo the FP32 residual) and
+// e / eM from the master
+__global__ void mixed_mirror_ds(MixedDev c, Vec3D e, const double *mmom, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const double x = e.x[t], y = e.y[t], z = e.z[t];
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    c.mt[t] = make_float4(hx, hy, hz, (float)mmom[t]);
+    c.lox[t] = (float)(x - (double)hx);
+    c.loy[t] = (float)(y - (double)hy);
+    c.loz[t] = (float)(z - (double)hz);
+}
+
+__global__ void mixed_ds_to_master(MixedDev c, Vec3D e, Vec3D eM, const double *mmom, int64_t n) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const float4 h = c.mt[t];
+    const double x = (double)h.x + (double)c.lox[t], y = (double)h.y + (double)c.loy[t],
+                 z = (double)h.z + (double)c.loz[t];
+    const double md = c.uni_m ? c.mmom_u : mmom[t];
+    e.x[t] = x;
+    e.y[t] = y;
+    e.z[t] = z;
+    eM.x[t] = md * x;
+    eM.y[t] = md * y;
+    eM.z[t] = md * z;
 }
 
 }  // namespace
@@ -749,12 +788,23 @@ int mixed_init(Sim &s) {
         set_error("precision 3 (FP32 gather, FP64 master): unknown SDEalgh");
         return UPPASD_GPU_EUNSUPPORTED;
     }
+    const bool ds = s.precision == 4;
+    if (ds && (s.llg.sdealgh == 4 || s.llg.sdealgh == 11)) {
+        // Heun and LLGI leave the sphere at first order: their renormalisation needs more
+        // than the double-single master's second-order series
+        set_error("precision 4 (double-single master) takes SDEalgh 1, 5, 6, 7; use precision 3 for Heun and LLGI");
+        return UPPASD_GPU_EUNSUPPORTED;
+    }
     const size_t n = (size_t)s.ham.natom * s.ham.mensemble;
     MixedDev &m = s.mix;
+    m.ds = ds ? 1 : 0;
     cudaError_t e = cudaMalloc(&m.mt, n * sizeof(float4));
     if (e == cudaSuccess) e = cudaMalloc(&m.mp, n * sizeof(float4));
     for (float **q : {&m.b2x, &m.b2y, &m.b2z})
         if (e == cudaSuccess) e = cudaMalloc(q, n * sizeof(float));
+    if (ds)
+        for (float **q : {&m.lox, &m.loy, &m.loz})
+            if (e == cudaSuccess) e = cudaMalloc(q, n * sizeof(float));
     if (e != cudaSuccess) {
         set_error(std::string("precision 3 set-up: ") + cudaGetErrorString(e));
         return UPPASD_GPU_ENOMEM;
@@ -768,16 +818,34 @@ void mixed_free(Sim &s) {
     MixedDev &m = s.mix;
     for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
                     (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext, (void *)m.row,
-                    (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm, (void *)m.moved})
+                    (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm, (void *)m.moved,
+                    (void *)m.lox, (void *)m.loy, (void *)m.loz})
         cudaFree(q);
     m = MixedDev{};
 }
 
-// The mirror from the master when something else wrote e (put_moments, Monte Carlo).
+// precision 4: e / eM from the double-single master when the steps have moved it
+int mixed_sync(Sim &s) {
+    if (!s.mix.ds || !s.mix.e_stale) return UPPASD_GPU_OK;
+    const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
+    mixed_ds_to_master<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom, n);
+    UPPASD_CUDA_TRY(cudaGetLastError());
+    s.mix.e_stale = 0;
+    return UPPASD_GPU_OK;
+}
+
+// The mirror (and the double-single master) from e when something else wrote e
+// (put_moments, Monte Carlo).
 int mixed_ready(Sim &s) {
     if (s.mix.valid) return UPPASD_GPU_OK;
+    // the mirror was marked stale while the double-single master was ahead of e (by a
+    // caller that did not write e): e from the master first, so that nothing is lost
+    if (const int rc = mixed_sync(s)) return rc;
     const int64_t n = (int64_t)s.ham.natom * s.ham.mensemble;
-    mixed_mirror<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.e, s.llg.mmom, s.mix.mt, n);
+    if (s.mix.ds)
+        mixed_mirror_ds<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.llg.mmom, n);
+    else
+        mixed_mirror<<<(unsigned)((n + 255) / 256), 256, 0, s.stream>>>(s.e, s.llg.mmom, s.mix.mt, n);
     UPPASD_CUDA_TRY(cudaGetLastError());
     s.mix.valid = 1;
     return UPPASD_GPU_OK;
@@ -789,7 +857,8 @@ int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps) {
         set_error("no colouring available for Monte Carlo");
         return UPPASD_GPU_ESTATE;
     }
-    int rc = mixed_ready(s);
+    int rc = mixed_sync(s);  // sites the sweeps reject keep their FP64 state
+    if (!rc) rc = mixed_ready(s);
     if (rc) return rc;
     s.sqm_valid = 0;  // the square path's mirror does not follow these updates
     // flip_a's beta = 1 / (k_B (T + 1e-15)) and the Gaussian width (2/25)(k_B T / mu_B)^0.2
@@ -819,9 +888,11 @@ int mixed_metropolis_sweeps(Sim &s, double temperature, int64_t nsweeps) {
         }
         s.mc_sweep += 1;
     }
-    if (nsweeps > 0)
+    if (nsweeps > 0) {
         mixed_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom,
                                                                                    nm, s.mix.moved);
+        if (s.mix.ds) s.mix.valid = 0;  // the double-single residuals are made again from e
+    }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
 }
@@ -831,7 +902,8 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const fl
         set_error("no colouring available for Monte Carlo");
         return UPPASD_GPU_ESTATE;
     }
-    int rc = mixed_ready(s);
+    int rc = mixed_sync(s);
+    if (!rc) rc = mixed_ready(s);
     if (rc) return rc;
     s.sqm_valid = 0;  // the square path's mirror does not follow these updates
     const float beta_mub = betak ? 0.f : (float)(s.ham.mub / (s.ham.kbolt * temperature));
@@ -849,6 +921,7 @@ int mixed_heat_bath_sweeps(Sim &s, double temperature, int64_t nsweeps, const fl
         const int64_t nm = (int64_t)s.ham.natom * s.ham.mensemble;
         mixed_master_from_mirror<<<(unsigned)((nm + 255) / 256), 256, 0, s.stream>>>(s.mix, s.e, s.eM, s.llg.mmom,
                                                                                    nm, nullptr);
+        if (s.mix.ds) s.mix.valid = 0;
     }
     UPPASD_CUDA_TRY(cudaGetLastError());
     return UPPASD_GPU_OK;
@@ -887,8 +960,16 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
     auto run = [&](auto alg) {
         constexpr int ALG = decltype(alg)::value;
         if (phase & 1) mixed_predict<ALG><<<grid, 256, 0, s.stream>>>(a);
-        if (phase & 2) mixed_correct<ALG><<<grid, 256, 0, s.stream>>>(a);
+        if (phase & 2) {
+            if constexpr (ALG == 4 || ALG == 11) {
+                mixed_correct<ALG, false><<<grid, 256, 0, s.stream>>>(a);
+            } else {
+                if (s.mix.ds) mixed_correct<ALG, true><<<grid, 256, 0, s.stream>>>(a);
+                else mixed_correct<ALG, false><<<grid, 256, 0, s.stream>>>(a);
+            }
+        }
     };
+    if ((phase & 2) && s.mix.ds) s.mix.e_stale = 1;
     switch (s.llg.sdealgh) {
     case 1: run(std::integral_constant<int, 1>{}); break;
     case 4: run(std::integral_constant<int, 4>{}); break;

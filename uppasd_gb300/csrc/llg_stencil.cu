@@ -302,21 +302,6 @@ __global__ void __launch_bounds__(256) stencil_predict(SParams p) {
     else predict_site<NSH, 1, LC>(p, s);
 }
 
-// Double-single helpers (Dekker / Knuth error-free transformations).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    float bb = s - a;
-    e = (a - (s - bb)) + (b - bb);
-}
-__device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
-    s = a + b;
-    e = b - (s - a);
-}
-__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
-    p = a * b;
-    e = fmaf(a, b, -p);
-}
-
 // Corrector update of one site from the field B at the predictor: Depondt
 // average with b2eff, rotation of m(t), master update and renormalisation.
 // What the corrector of one site reads besides the gather: m(t) (the mirror), the

@@ -203,10 +203,11 @@ int square_sweeps(Sim &s, int L, double temperature, const float *betak, int64_t
         return UPPASD_GPU_EUNSUPPORTED;
     }
     if (structured(s)) {
-        set_error("mc_run_square: needs the FP64 state (precision 0 or 3)");
+        set_error("mc_run_square: needs the FP64 state (precision 0, 3 or 4)");
         return UPPASD_GPU_EUNSUPPORTED;
     }
-    s.mix.valid = 0;  // the precision-3 LLG mirror does not follow these updates
+    if (const int rc = sync_state(s)) return rc;  // precision 4: e from its master first
+    s.mix.valid = 0;  // the precision-3 / 4 LLG mirror does not follow these updates
     if (s.sq.L != L) {
         const int rc = square_recognise(s, L);
         if (rc) return rc;

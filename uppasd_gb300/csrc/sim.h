@@ -103,6 +103,10 @@ struct MixedDev {
     float lam_u = 0.f, g_u = 0.f, T_u = 0.f;
     double mmom_u = 0.0;       // moment of every (ensemble, site) when uni_m
     uint8_t *moved = nullptr;  // [mensemble][natom] Metropolis: mirror moved, FP64 state not yet
+    // precision 4: the master is double-single, hi = the mirror, lo here; e / eM are made
+    // from it when a caller reads them (e_stale: the steps have moved it since)
+    int ds = 0, e_stale = 0;
+    float *lox = nullptr, *loy = nullptr, *loz = nullptr;  // [mensemble][natom]
 };
 
 // Uniform square-lattice Hamiltonian recognised for the structured heat bath
@@ -129,7 +133,7 @@ struct Sim {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     int device = 0;
-    int precision = 0;  // 0 FP64 generic, 1 structured mixed precision
+    int precision = 0;  // 0 FP64 generic, 1 / 2 structured, 3 / 4 FP32 gather with FP64 / double-single master
     StructuredFast *fast = nullptr;
     // MC
     int ncolour = 0;
@@ -220,6 +224,10 @@ inline void square_mirror_stale(Sim &s) {
 }
 // precision 1 / 2: the structured bcc path owns the state between sync points
 inline bool structured(const Sim &s) { return s.precision == 1 || s.precision == 2; }
+// precision 3 / 4: FP32 gather over the caller's lists, FP64 (3) or double-single (4) master
+inline bool mixed_path(const Sim &s) { return s.precision == 3 || s.precision == 4; }
+// e / eM brought up to date from the master of the path that owns the state (abi.cu)
+int sync_state(Sim &s);
 
 void set_error(const std::string &msg);
 
