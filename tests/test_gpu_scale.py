@@ -11,7 +11,9 @@ on the sizes of the configured runs, against the FP64 CPU oracle:
   then 1000 at 300 K on the FP64 path, 1e-9 per component;
 * the 256^2 square monolayer with J, interfacial DMI, uniaxial anisotropy and a
   Zeeman field, semi-implicit midpoint, 20,000 steps at T = 0 and at 50 K;
-* the SIB solver (SDEalgh 6) at 300 K without the perp projection.
+* the SIB solver (SDEalgh 6) at 300 K without the perp projection;
+* the FP32 gather over the caller's lists (precision 3, FP64 master; precision 4,
+  double-single master) on the 256^2 DMI monolayer at T = 0 and 50 K.
 
 Every test prints the measured deviation, so a run with ``-s`` records the
 numbers behind the stated bounds.
@@ -154,3 +156,26 @@ def test_sib_300k_without_perp():
     print(f"SIB 300 K 1000 steps: {err:.3e}")
     sim.close()
     assert err <= TOL
+
+
+@pytest.mark.parametrize("prec", [3, 4])
+@pytest.mark.parametrize("temp", [0.0, 50.0])
+def test_square256_general_path(prec, temp):
+    """The general-Hamiltonian FP32 path on the configured 256^2 monolayer (J, DMI,
+    anisotropy, Zeeman; midpoint): against the FP64 oracle with the FP32 bounds of the
+    small-lattice tests, norms within 1e-12."""
+    lat = lattice.square_dmi(256, 1.0, 0.3, -0.05, 0.5, 1.0)
+    e0 = _rand_unit(np.random.default_rng(512 + int(temp)), (1, lat.natom, 3))
+    sim = GpuSimulation(lat, sdealgh=1, delta_t=1e-16, damping=0.05, temperature=temp, seed=37, emom=e0,
+                        precision=prec)
+    o = _oracle(lat, 1, 1e-16, 0.05, temp, 37, e0)
+    n = 20 if temp == 0.0 else 200
+    sim.evolve(n)
+    for _ in range(n):
+        o.sd_step()
+    g = sim.get_moments()
+    err = float(np.max(np.abs(g - o.emom)))
+    print(f"square 256^2 precision {prec} T={temp}, {n} steps: {err:.3e}")
+    sim.close()
+    assert err <= (STRUCT_T0[20] if temp == 0.0 else STRUCT_T300), err
+    assert np.max(np.abs(np.linalg.norm(g, axis=-1) - 1.0)) <= 1e-12
