@@ -123,3 +123,14 @@ def test_mcbatch_rejects_bad_tables(lib):
                      ("uppasd_gpu_mcbatch_stats", (None, None, None, None)), ("uppasd_gpu_mcbatch_check", (None,)),
                      ("uppasd_gpu_mcbatch_get_spins", (None, None)), ("uppasd_gpu_mcbatch_set_sweep", (None, 0))]:
         assert getattr(lib, fn)(*args) == -1, fn
+
+
+def test_host_block_and_dipole_reject_bad_calls(lib):
+    """sd_run_io and set_dipole refuse a null simulation and bad arguments with -1
+    before any device work."""
+    from uppasd_gb300 import _lib
+    buf = np.zeros(3, dtype=np.float64)
+    p = buf.ctypes.data_as(_lib.F64P)
+    assert lib.uppasd_gpu_sd_run_io(None, p, 10, p, None) == -1
+    assert lib.uppasd_gpu_set_dipole(None, 1, 2.87e-10, None, 1, 1, 1, 1, p, p) == -1
+    assert lib.uppasd_gpu_last_error()
