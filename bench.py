@@ -894,9 +894,9 @@ def run_gb300(args, w):
     value = nspin * args.steps * world / (ms * 1e-3)
     graphs, rem = divmod(args.steps, 16)
     # a captured 16-step graph: predictor and corrector per step, on the structured path once
-    # per ensemble half (two chains), and the step-counter kernel
+    # per ensemble half (two chains), and the step-counter kernel; the remaining steps the same
     chains = 2 if prec in (1, 2) and lat.mensemble >= 2 else 1
-    launches = graphs * (16 * 2 * chains + 1) + rem * 2 + (1 if rem else 0)
+    launches = graphs * (16 * 2 * chains + 1) + rem * 2 * chains + (1 if rem else 0)
     kt = sim.time_kernels(3)
     peak, peak_kind = measured_peaks()
     kname = KERNEL_NAMES[prec][1 if kt["correct_ms"] >= kt["predict_ms"] else 0]

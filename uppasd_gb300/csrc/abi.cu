@@ -557,8 +557,21 @@ int run_steps(Sim &s, int64_t n) {
     if (s.graph)
         for (; done + s.graph_steps <= n; done += s.graph_steps) UPPASD_CUDA_TRY(cudaGraphLaunch(s.graph, s.stream));
     int64_t rem = n - done;
-    for (int64_t j = 0; j < rem; ++j)
-        if ((rc = one_step(s, j))) return rc;
+    if (rem > 0 && SG > 1) {
+        // the steps a graph does not cover as the same two chains, launched directly
+        UPPASD_CUDA_TRY(cudaEventRecord(s.io_start, s.stream));
+        const int M = s.ham.mensemble;
+        for (int q = 0; q < SG; ++q) {
+            const int k0 = (int)((int64_t)M * q / SG), kn = (int)((int64_t)M * (q + 1) / SG) - k0;
+            UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.io_stream[q], s.io_start, 0));
+            if ((rc = structured_steps_range(s, rem, k0, kn, s.io_stream[q]))) return rc;
+            UPPASD_CUDA_TRY(cudaEventRecord(s.io_ev[q], s.io_stream[q]));
+            UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.io_ev[q], 0));
+        }
+    } else {
+        for (int64_t j = 0; j < rem; ++j)
+            if ((rc = one_step(s, j))) return rc;
+    }
     if (rem > 0) advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, rem);
     UPPASD_CUDA_TRY(cudaGetLastError());
     s.step += n;
