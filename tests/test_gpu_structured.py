@@ -149,5 +149,9 @@ def test_run_io_equals_put_run_get(prec, M, pinned):
     a.evolve(5)
     b.run_io(None, 5, out)
     assert np.array_equal(out, a.get_moments())
+    # no steps: the conversions in and out alone
+    a.put_moments(e1)
+    b.run_io(inp, 0, out)
+    assert np.array_equal(out, a.get_moments())
     a.close()
     b.close()
