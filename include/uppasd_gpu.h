@@ -70,11 +70,10 @@ typedef struct {
                                             on the FP64 path);
                                           4 as 3 with a double-single (float-float) spin
                                             master renormalised in error-free FP32
-                                            arithmetic, for the norm-preserving solvers
-                                            (SDEalgh 1, 5, 6, 7; -7 for 4 and 11): GB300's
-                                            FP64 pipe sets precision 3's step time; the FP64
-                                            state is made from the master when a call reads
-                                            it */
+                                            arithmetic (every SDEalgh of precision 3):
+                                            GB300's FP64 pipe sets precision 3's step time;
+                                            the FP64 state is made from the master when a
+                                            call reads it */
     /* geometry of the reference's atom numbering i = I0 + NA*(I1 + N1*(I2 + N2*I3));
        0 when unknown (the structured path then stays off) */
     int32_t n1, n2, n3, na;

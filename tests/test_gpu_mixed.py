@@ -2,8 +2,7 @@
 master (renormalised in FP64 every step), on Hamiltonians outside the structured bcc
 path: exchange (scalar or tensor), DMI, anisotropy and Zeeman, midpoint and Depondt.
 Precision 4: the same with a double-single master (hi = the FP32 mirror, lo a residual,
-renormalised in error-free FP32 arithmetic), for the norm-preserving solvers; the tests
-of the solvers it takes run on both.
+renormalised in error-free FP32 arithmetic); the tests run on both.
 
 The field, thermal field and rotation run in FP32, so trajectories are compared with
 the FP64 oracle at FP32-scale tolerances that grow with the step count (a random
@@ -124,7 +123,7 @@ def test_state_changes_between_runs_are_seen():
     assert np.max(np.abs(res[0] - res[2])) <= 1e-4
 
 
-@pytest.mark.parametrize("solver,prec", [(4, 3), (6, 3), (7, 3), (11, 3), (6, 4), (7, 4)])
+@pytest.mark.parametrize("solver,prec", [(4, 3), (6, 3), (7, 3), (11, 3), (4, 4), (6, 4), (7, 4), (11, 4)])
 def test_other_solvers_T0_against_oracle(solver, prec):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(47), (2, lat.natom, 3))
@@ -146,8 +145,8 @@ def test_other_solvers_T0_against_oracle(solver, prec):
     sim.close()
 
 
-@pytest.mark.parametrize("solver,prec", [(1, 3), (4, 3), (5, 3), (6, 3), (7, 3), (11, 3), (1, 4), (5, 4), (6, 4),
-                                         (7, 4)])
+@pytest.mark.parametrize("solver,prec", [(1, 3), (4, 3), (5, 3), (6, 3), (7, 3), (11, 3), (1, 4), (4, 4), (5, 4),
+                                         (6, 4), (7, 4), (11, 4)])
 def test_perp_against_oracle(solver, prec):
     lat = lattice.square_dmi(32, 1.0, 0.3, -0.05, 0.5, 1.0).with_ensembles(2)
     e0 = _rand_unit(np.random.default_rng(48), (2, lat.natom, 3))
@@ -276,15 +275,8 @@ def test_T0_per_site_field_and_anisotropy(solver, prec):
     sim.close()
 
 
-def test_precision4_takes_the_norm_preserving_solvers():
-    lat = lattice.square_dmi(16, 1.0, 0.3, -0.05, 0.5, 1.0)
-    for solver in (4, 11):
-        with pytest.raises(_lib.UppasdGpuError) as ei:
-            GpuSimulation(lat, sdealgh=solver, precision=4, relaxtime=1e-15 if solver == 11 else 0.0)
-        assert ei.value.rc == -7
 
-
-@pytest.mark.parametrize("solver", [1, 5])
+@pytest.mark.parametrize("solver", [1, 4, 5, 11])
 def test_precision4_reads_leave_the_trajectory_unchanged(solver):
     """The double-single master is converted to e / eM whenever the caller reads them
     (get_moments, observables, energy terms, the field); the master itself is not touched,
@@ -294,7 +286,7 @@ def test_precision4_reads_leave_the_trajectory_unchanged(solver):
     out = []
     for reads in (False, True):
         sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.05, temperature=50.0, seed=5, emom=e0,
-                            precision=4)
+                            precision=4, relaxtime=1e-15 if solver == 11 else 0.0)
         for _ in range(4):
             sim.evolve(25)
             if reads:

@@ -161,4 +161,46 @@ __device__ __forceinline__ void ds_add_renorm(float hi[3], float lo[3], const fl
     }
 }
 
+// The same for updates that leave the sphere at first order (Heun, LLGI: |x| reaches a
+// few 1e-2 at finite temperature): 1/sqrt(1 + x) - 1 as a double-single pair from one
+// Newton step on the FP32 estimate y0, y = y0 + y0 r / 2 with r = 1 - (1 + x) y0^2 formed
+// from exact products (1 - p and the difference of the two near-equal O(x) terms are exact
+// by Sterbenz's lemma for |x| < 1/2), so s_hi = y0 - 1 (exact) and s_lo = y0 r / 2; the
+// correction e (s_hi + s_lo) is added with an exact product for its leading term.
+__device__ __forceinline__ void ds_add_renorm_wide(float hi[3], float lo[3], const float d[3]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float sm, er;
+        two_sum(hi[c], d[c], sm, er);
+        quick_two_sum(sm, er + lo[c], hi[c], lo[c]);
+    }
+    float n2h = 0.f, n2l = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float pp, pe, sm, er;
+        two_prod(hi[c], hi[c], pp, pe);
+        two_sum(n2h, pp, sm, er);
+        n2h = sm;
+        n2l += er + pe + 2.0f * hi[c] * lo[c];
+    }
+    float xs, xe;
+    two_sum(n2h, -1.0f, xs, xe);
+    const float xl = xe + n2l;  // x = xs + xl
+    const float y0 = rsqrtf(1.0f + xs);
+    float p, pe, q, qe;
+    two_prod(y0, y0, p, pe);  // y0^2 = p + pe
+    two_prod(xs, p, q, qe);   // xs p = q + qe
+    const float r = ((1.0f - p) - q) - (pe + qe + xs * pe + xl * p);
+    const float s_hi = y0 - 1.0f;
+    const float s_lo = 0.5f * y0 * r;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float p, pe, sm, er;
+        two_prod(hi[c], s_hi, p, pe);
+        const float rest = pe + hi[c] * s_lo + lo[c] * (s_hi + s_lo);
+        two_sum(hi[c], p, sm, er);
+        quick_two_sum(sm, er + (lo[c] + rest), hi[c], lo[c]);
+    }
+}
+
 }  // namespace uppasd

@@ -345,9 +345,15 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
                              0.5f * (B[2] + r[2]) + 0.5f * a.c.b2z[o]};
         const float et[3] = {(float)a.mpast.x[o], (float)a.mpast.y[o], (float)a.mpast.z[o]};
         // m(t) becomes the previous step (FP64, from the master)
-        a.mpast.x[o] = a.e.x[o];
-        a.mpast.y[o] = a.e.y[o];
-        a.mpast.z[o] = a.e.z[o];
+        if constexpr (DS) {
+            a.mpast.x[o] = (double)e[0] + (double)a.c.lox[o];
+            a.mpast.y[o] = (double)e[1] + (double)a.c.loy[o];
+            a.mpast.z[o] = (double)e[2] + (double)a.c.loz[o];
+        } else {
+            a.mpast.x[o] = a.e.x[o];
+            a.mpast.y[o] = a.e.y[o];
+            a.mpast.z[o] = a.e.z[o];
+        }
         llgi_f32(lam, a.tau_dt, a.dtg_llgi, et, e, bd, out);
         unit = true;
     } else if (ALG == 4) {
@@ -393,7 +399,8 @@ __global__ void __launch_bounds__(256) mixed_correct(MixArgs a) {
         // double-single master (precision 4): hi is the mirror, the change and the
         // renormalisation in error-free FP32 arithmetic; e / eM are made on demand
         float hi[3] = {e[0], e[1], e[2]}, lo[3] = {a.c.lox[o], a.c.loy[o], a.c.loz[o]};
-        ds_add_renorm(hi, lo, d);
+        if constexpr (ALG == 4 || ALG == 11) ds_add_renorm_wide(hi, lo, d);  // off the sphere at first order
+        else ds_add_renorm(hi, lo, d);
         a.c.lox[o] = lo[0];
         a.c.loy[o] = lo[1];
         a.c.loz[o] = lo[2];
@@ -789,12 +796,6 @@ int mixed_init(Sim &s) {
         return UPPASD_GPU_EUNSUPPORTED;
     }
     const bool ds = s.precision == 4;
-    if (ds && (s.llg.sdealgh == 4 || s.llg.sdealgh == 11)) {
-        // Heun and LLGI leave the sphere at first order: their renormalisation needs more
-        // than the double-single master's second-order series
-        set_error("precision 4 (double-single master) takes SDEalgh 1, 5, 6, 7; use precision 3 for Heun and LLGI");
-        return UPPASD_GPU_EUNSUPPORTED;
-    }
     const size_t n = (size_t)s.ham.natom * s.ham.mensemble;
     MixedDev &m = s.mix;
     m.ds = ds ? 1 : 0;
@@ -961,12 +962,8 @@ int mixed_step(Sim &s, int64_t step_offset, int phase) {
         constexpr int ALG = decltype(alg)::value;
         if (phase & 1) mixed_predict<ALG><<<grid, 256, 0, s.stream>>>(a);
         if (phase & 2) {
-            if constexpr (ALG == 4 || ALG == 11) {
-                mixed_correct<ALG, false><<<grid, 256, 0, s.stream>>>(a);
-            } else {
-                if (s.mix.ds) mixed_correct<ALG, true><<<grid, 256, 0, s.stream>>>(a);
-                else mixed_correct<ALG, false><<<grid, 256, 0, s.stream>>>(a);
-            }
+            if (s.mix.ds) mixed_correct<ALG, true><<<grid, 256, 0, s.stream>>>(a);
+            else mixed_correct<ALG, false><<<grid, 256, 0, s.stream>>>(a);
         }
     };
     if ((phase & 2) && s.mix.ds) s.mix.e_stale = 1;

@@ -31,7 +31,7 @@ class GpuSimulation:
     precision: 0 FP64 throughout (any neighbour list, every solver); 1 / 2 the structured
     bcc kernels (FP32 gather, FP64 / double-single master; periodic bcc, up to four
     shells and two species, Depondt); 3 / 4 FP32 gather over any neighbour list with an
-    FP64 / double-single master (4: SDEalgh 1, 5, 6, 7)."""
+    FP64 / double-single master (every solver)."""
 
     def __init__(self, lat: Lattice, sdealgh: int = 5, delta_t: float = 1e-16, damping=0.1,
                  temperature=0.0, landeg=1.0, seed: int = 1, emom: Optional[np.ndarray] = None,
