@@ -700,9 +700,11 @@ def _roofline(kt, nspin, s_bytes, ms_step, peak, peak_kind, traffic, traffic_sou
                      "bytes_per_spin_step": 15 * s_bytes}}
 
 
-PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master"}
+PREC_NAMES = {0: "fp64-generic", 1: "fp32-gather/fp64-master", 2: "fp32-gather/double-single-master",
+              3: "fp32-gather-lists/fp64-master", 4: "fp32-gather-lists/double-single-master"}
 KERNEL_NAMES = {0: ("llg_predict", "llg_correct"), 1: ("stencil_tma_predict", "stencil_tma_correct"),
-                2: ("stencil_tma_predict", "stencil_tma_correct")}
+                2: ("stencil_tma_predict", "stencil_tma_correct"), 3: ("mixed_predict", "mixed_correct"),
+                4: ("mixed_predict", "mixed_correct")}
 
 
 def oracle_error(lat, w, prec, e0, stream, nsteps=20, seed=5):
@@ -1035,7 +1037,8 @@ def run_gb300(args, w):
         "metric": "LLG atom-steps/s", "value": value, "unit": "atom-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": {0: "f64", 1: "f32-gather/f64-state", 2: "f32-gather/double-single-state"}[prec],
+        "dtype": {0: "f64", 1: "f32-gather/f64-state", 2: "f32-gather/double-single-state", 3: "f32-gather/f64-state",
+                  4: "f32-gather/double-single-state"}[prec],
         "data": "synthetic (seeded lattice, species and spins)",
         "config": {"workload": args.workload, "description": w["desc"], "natom": lat.natom,
                    "ensembles": lat.mensemble, "spins": nspin,
@@ -1074,7 +1077,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="alloy2m", choices=sorted(WORKLOADS))
-    ap.add_argument("--precision", default="auto", choices=["auto", "0", "1", "2"])
+    ap.add_argument("--precision", default="auto", choices=["auto", "0", "1", "2", "3", "4"])
     ap.add_argument("--e2e-inner", type=int, default=10)
     ap.add_argument("--e2e-rounds", type=int, default=10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
