@@ -256,6 +256,15 @@ int uppasd_gpu_set_stream(uppasd_gpu_sim *s, void *cuda_stream);
  * time per launch in ms, measured with CUDA events on the launching stream:
  * ms[0] predictor kernel, ms[1] corrector kernel, ms[2] whole step. */
 int uppasd_gpu_time_kernels(uppasd_gpu_sim *s, int32_t nrep, double *ms);
+/* Which path and data forms init chose (diagnostics; no counterpart in the reference):
+ * info[0] precision, info[1] 1 on the structured stencil path, and on the FP32-gather
+ * path (precision 3 / 4): info[2] site classes (0: the per-site lists are read),
+ * info[3] distinct coupling rows, info[4] chemical types the exchange couplings are
+ * looked up by (0: none; a random alloy whose couplings are a function of the
+ * neighbours' types, with the types given in uppasd_gpu_arrays.species), info[5] 1
+ * when one external-field entry serves every spin; info[6] device bytes the
+ * simulation allocated; info[7] 0. */
+int uppasd_gpu_path_info(uppasd_gpu_sim *s, int64_t *info);
 
 /* Allocation-free magnetisation sums.  This entry point has no counterpart in
  * the reference; it is for callers that cannot call cudaMalloc: a host code

@@ -172,6 +172,63 @@ def test_scope():
     sim.close()
 
 
+def _alloy_runs(lat, e0, prec, solver):
+    """20 Philox steps at 300 K, then 2 heat-bath and 2 Metropolis sweeps: the path
+    info and the state after each stage."""
+    sim = GpuSimulation(lat, sdealgh=solver, delta_t=1e-16, damping=0.1, temperature=300.0, seed=21, emom=e0,
+                        precision=prec)
+    info = sim.path_info()
+    sim.evolve(20)
+    out = [sim.get_moments()]
+    sim.relax("H", 300.0, 2)
+    out.append(sim.get_moments())
+    sim.relax("M", 300.0, 2)
+    out.append(sim.get_moments())
+    sim.close()
+    return info, out
+
+
+@pytest.mark.parametrize("prec,solver", [(3, 5), (4, 5), (4, 1)])
+def test_chemical_classes_reproduce_the_per_site_lists(prec, solver, monkeypatch):
+    """Random bcc alloy (14^3 cells, four shells, couplings from a (type_i, type_j, shell)
+    table): every site's coupling row differs, so the plain site classes give way to the
+    per-site lists; with the chemical types the sites fall into classes keyed on their
+    own type and the neighbours' couplings are looked up by type.  Both forms give the
+    same LLG trajectory and Monte Carlo chains bit for bit, and the LLG steps follow the
+    FP64 oracle within the thermal tolerance."""
+    lat = lattice.bcc_alloy(14, seed=9).with_ensembles(2)
+    e0 = _rand_unit(np.random.default_rng(47), (2, lat.natom, 3))
+    info, got = _alloy_runs(lat, e0, prec, solver)
+    assert info["chemical_types"] == 2
+    assert 0 < info["site_classes"] <= lat.natom // 8
+    monkeypatch.setenv("UPPASD_CHEMICAL_CLASSES", "0")
+    info0, ref = _alloy_runs(lat, e0, prec, solver)
+    assert info0["chemical_types"] == 0 and info0["site_classes"] == 0
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+    o = po.Oracle(lat)
+    o.set_moments(e0)
+    o.make_llg(solver, 1e-16, 0.1, 300.0, 1.0, noise_mode=po.NOISE_PHILOX, seed=21)
+    for _ in range(20):
+        o.sd_step()
+    assert np.max(np.abs(got[0] - o.emom)) <= THERMAL_TOL
+
+
+def test_chemical_classes_need_type_resolved_couplings():
+    """One coupling that is not a function of the neighbour's type: the per-site lists
+    stay; with couplings that are, the classes are taken (and the simulation reports it)."""
+    lat = lattice.bcc_alloy(14, seed=9)
+    sim = GpuSimulation(lat, sdealgh=5, precision=3)
+    assert sim.path_info()["chemical_types"] == 2
+    sim.close()
+    lat.ncoup = lat.ncoup.copy()
+    lat.ncoup[5, 3] *= 1.01
+    sim = GpuSimulation(lat, sdealgh=5, precision=3)
+    info = sim.path_info()
+    sim.close()
+    assert info["chemical_types"] == 0 and info["site_classes"] == 0
+
+
 @pytest.mark.parametrize("prec", [3, 4])
 @pytest.mark.parametrize("kind", ["kagome_tensor", "square_dmi_aniso"])
 def test_heat_bath_chain_against_oracle(kind, prec):

@@ -76,6 +76,7 @@ SIGNATURES = {
                           I32P],
     "uppasd_gpu_set_stream": [C.c_void_p, C.c_void_p],
     "uppasd_gpu_time_kernels": [C.c_void_p, C.c_int32, F64P],
+    "uppasd_gpu_path_info": [C.c_void_p, C.POINTER(C.c_int64)],
     "uppasd_gpu_moment_sums_noalloc": [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p],
     # batched replica Monte Carlo
     "uppasd_gpu_mcbatch_create": [C.c_int32, I32P, F64P, I32P, F64P, C.c_double, F64P, C.c_uint64, C.c_int32,

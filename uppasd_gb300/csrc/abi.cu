@@ -36,7 +36,7 @@ int structured_store_range(Sim &s, double *aos, int full, int k0, int kn, cudaSt
 int structured_check_flag(Sim &s);
 int structured_load_state(Sim &s);  // s.e -> master state
 void structured_free(Sim &s);
-int mixed_init(Sim &s);  // llg_mixed.cu
+int mixed_init(Sim &s, const int32_t *species);  // llg_mixed.cu
 void mixed_free(Sim &s);
 int mixed_ready(Sim &s);
 int mixed_sync(Sim &s);  // precision 4: e / eM from the double-single master
@@ -453,7 +453,7 @@ int do_init(Sim &s, const uppasd_gpu_consts *c, const uppasd_gpu_arrays *a) {
     if (structured(s)) {
         if ((rc = structured_init(s, c, a))) return rc;
     } else if (c->precision == 3 || c->precision == 4) {
-        if ((rc = mixed_init(s))) return rc;
+        if ((rc = mixed_init(s, a->species))) return rc;
     }
     if ((rc = uppasd_gpu_put_moments(reinterpret_cast<uppasd_gpu_sim *>(&s), a->emom))) return rc;
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
@@ -1199,6 +1199,22 @@ int uppasd_gpu_set_stream(uppasd_gpu_sim *w, void *cuda_stream) {
     UPPASD_CUDA_TRY(cudaStreamSynchronize(s.stream));
     if (!s.own_stream) s.own_stream = s.stream;
     s.stream = cuda_stream ? (cudaStream_t)cuda_stream : s.own_stream;
+    return UPPASD_GPU_OK;
+}
+
+int uppasd_gpu_path_info(uppasd_gpu_sim *w, int64_t *info) {
+    if (!w || !info) return UPPASD_GPU_EINVAL;
+    const Sim &s = w->s;
+    const uppasd::MixedDev &m = s.mix;
+    const bool mixed = uppasd::mixed_path(s);
+    info[0] = s.precision;
+    info[1] = uppasd::structured(s) ? 1 : 0;
+    info[2] = mixed ? m.ncls : 0;
+    info[3] = mixed ? m.nrow : 0;
+    info[4] = mixed ? m.nsp : 0;
+    info[5] = mixed ? m.ext_uniform : 0;
+    info[6] = (int64_t)s.bytes_allocated;
+    info[7] = 0;
     return UPPASD_GPU_OK;
 }
 

@@ -14,6 +14,7 @@
 // The noise is the FP64 path's Philox stream (site, ensemble, step), drawn with the
 // FP32 Box-Muller of the structured path.
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 #include <type_traits>
 #include <cstring>
@@ -574,9 +575,61 @@ bool store(T **d, const std::vector<T> &h) {
     return cudaMalloc(d, h.size() * sizeof(T)) == cudaSuccess &&
            cudaMemcpy(*d, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) == cudaSuccess;
 }
+
+// Numbers fixed-width integer keys in order of first appearance (the site classes).
+struct KeyInterner {
+    size_t width, cap;
+    std::vector<int32_t> keys;  // the distinct keys back to back
+    std::unordered_map<uint64_t, std::vector<int>> byhash;
+    int n = 0;
+    KeyInterner(size_t w, size_t c) : width(w), cap(c) {}
+    // the id of key k (a new one when unseen), -1 when a new one would exceed cap
+    int id(const std::vector<int32_t> &k) {
+        uint64_t hsh = 1469598103934665603ull;  // FNV-1a over the key words
+        for (int32_t w : k) {
+            hsh ^= (uint32_t)w;
+            hsh *= 1099511628211ull;
+        }
+        std::vector<int> &cand = byhash[hsh];
+        for (int c : cand)
+            if (std::equal(k.begin(), k.end(), keys.begin() + (size_t)c * width)) return c;
+        if ((size_t)n == cap) return -1;
+        cand.push_back(n);
+        keys.insert(keys.end(), k.begin(), k.end());
+        return n++;
+    }
+    const int32_t *key(int c) const { return keys.data() + (size_t)c * width; }
+};
+
+// The class tables from the interned keys, laid out [K0 .. K0+4] = (coupling row,
+// anisotropy row, anisotropy type, nn, nd), then mnn exchange and mdm DM offsets.
+bool store_classes(MixedDev &m, const KeyInterner &ki, size_t k0, size_t mnn, size_t mdm,
+                   const std::vector<int32_t> &cls) {
+    const size_t ncls = ki.n;
+    std::vector<int4> info(ncls);
+    std::vector<int32_t> cnb(ncls * std::max<size_t>(mnn, 1)), cdm(ncls * std::max<size_t>(mdm, 1));
+    for (size_t c = 0; c < ncls; ++c) {
+        const int32_t *k = ki.key((int)c) + k0;
+        info[c] = make_int4(k[3] | (k[4] << 16), k[0], k[1], k[2]);
+        for (size_t q = 0; q < mnn; ++q) cnb[c * mnn + q] = k[5 + q];
+        for (size_t q = 0; q < mdm; ++q) cdm[c * mdm + q] = k[5 + mnn + q];
+    }
+    const bool ok = store(&m.cls, cls) && store(&m.cinfo, info) && store(&m.cnb, cnb) && store(&m.cdm, cdm);
+    m.ncls = ok ? (int)ncls : 0;
+    return ok;
+}
+
+void drop_classes(MixedDev &m) {
+    for (void *q : {(void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm}) cudaFree(q);
+    m.cls = nullptr;
+    m.cinfo = nullptr;
+    m.cnb = m.cdm = nullptr;
+    m.ncls = 0;
+}
 }  // namespace
 
 bool mixed_site_classes(Sim &s, const std::vector<int32_t> &row);
+bool mixed_species_classes(Sim &s);
 bool mixed_uniforms(Sim &s);
 
 // (Re)builds the FP32 copies of the couplings from the FP64 Hamiltonian on the device,
@@ -586,6 +639,7 @@ int mixed_coefficients(Sim &s) {
     const HamDev &h = s.ham;
     const size_t N = h.natom, M = h.mensemble, nh = h.nham, mnn = std::max(h.mnn, 1), mdm = h.do_dm ? h.mnn_dm : 0;
     MixedDev &m = s.mix;
+    m.nsp = 0;
     std::vector<double> d, dx, dy, dz, jtd;
     std::vector<int32_t> aham;
     bool ok = cudaStreamSynchronize(s.stream) == cudaSuccess;
@@ -678,7 +732,11 @@ int mixed_coefficients(Sim &s) {
         if (uniform) v.resize(1);
         ok = ok && store(&m.ext, v);
     }
-    if (ok) ok = mixed_site_classes(s, row) && mixed_uniforms(s);
+    if (ok) ok = mixed_site_classes(s, row);
+    // per-site lists (too many distinct rows, e.g. a random alloy): try classes that key
+    // on the site's own chemical type and look each neighbour's coupling up by its type
+    if (ok && m.ncls == 0 && m.spc && !h.do_jtensor) ok = mixed_species_classes(s);
+    if (ok) ok = mixed_uniforms(s);
     if (!ok) {
         set_error("precision 3: copying the couplings to FP32 failed");
         return UPPASD_GPU_ECUDA;
@@ -698,12 +756,9 @@ bool mixed_site_classes(Sim &s, const std::vector<int32_t> &row) {
     if (ok && h.do_dm) ok = fetch(dl, h.dmlist, mdm * N) && fetch(ds, h.dmsize, N);
     if (ok && h.do_aniso) ok = fetch(ta, h.taniso, N) && fetch(ar, m.arow, N);
     if (!ok) return false;
-    std::vector<int32_t> keys;      // the classes' keys back to back
     const size_t width = 5 + mnn + mdm;
-    std::unordered_map<uint64_t, std::vector<int>> byhash;
+    KeyInterner ki(width, std::max<size_t>(1, N / 4));
     std::vector<int32_t> cls(N), key(width);
-    size_t ncls = 0;
-    const size_t cap = std::max<size_t>(1, N / 4);
     for (size_t i = 0; i < N; ++i) {
         std::fill(key.begin(), key.end(), 0);
         const int nn = ns[i], nd = h.do_dm ? ds[i] : 0;
@@ -714,44 +769,110 @@ bool mixed_site_classes(Sim &s, const std::vector<int32_t> &row) {
         key[4] = nd;
         for (int q = 0; q < nn; ++q) key[5 + q] = nl[(size_t)q * N + i] - (int32_t)i;
         for (int q = 0; q < nd; ++q) key[5 + mnn + q] = dl[(size_t)q * N + i] - (int32_t)i;
-        uint64_t hsh = 1469598103934665603ull;  // FNV-1a over the key words
-        for (int32_t w : key) {
-            hsh ^= (uint32_t)w;
-            hsh *= 1099511628211ull;
-        }
-        std::vector<int> &cand = byhash[hsh];
-        int id = -1;
-        for (int c : cand)
-            if (std::equal(key.begin(), key.end(), keys.begin() + (size_t)c * width)) {
-                id = c;
-                break;
-            }
+        const int id = ki.id(key);
         if (id < 0) {
-            if (ncls == cap) {
-                // too many distinct sites: keep reading the per-site lists
-                for (void *q : {(void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm}) cudaFree(q);
-                m.cls = nullptr;
-                m.cinfo = nullptr;
-                m.cnb = m.cdm = nullptr;
-                m.ncls = 0;
-                return true;
-            }
-            id = (int)ncls++;
-            cand.push_back(id);
-            keys.insert(keys.end(), key.begin(), key.end());
+            // too many distinct sites: keep reading the per-site lists
+            drop_classes(m);
+            return true;
         }
         cls[i] = id;
     }
-    std::vector<int4> info(ncls);
-    std::vector<int32_t> cnb(ncls * std::max<size_t>(mnn, 1)), cdm(ncls * std::max<size_t>(mdm, 1));
-    for (size_t c = 0; c < ncls; ++c) {
-        const int32_t *k = keys.data() + c * width;
-        info[c] = make_int4(k[3] | (k[4] << 16), k[0], k[1], k[2]);
-        for (size_t q = 0; q < mnn; ++q) cnb[c * mnn + q] = k[5 + q];
-        for (size_t q = 0; q < mdm; ++q) cdm[c * mdm + q] = k[5 + mnn + q];
+    return store_classes(m, ki, 0, mnn, mdm, cls);
+}
+
+// Chemical classes (see MixedDev::nsp): the key of site i is its own chemical type, its
+// DM row, anisotropy row and type, list sizes and neighbour offsets j - i, and the
+// exchange coupling of each slot must then be a function of the chemical type of that
+// slot's neighbour (bit for bit in FP32): a random alloy whose couplings come from a
+// (type_i, type_j, shell) table, as the reference's chemical-type-resolved exchange of
+// random alloys builds them.  A site that breaks this, or more than natom / (4 nsp)
+// classes, leaves the per-site lists in place.
+bool mixed_species_classes(Sim &s) {
+    const HamDev &h = s.ham;
+    MixedDev &m = s.mix;
+    const size_t N = h.natom, nh = h.nham, mnn = h.mnn, mdm = h.do_dm ? h.mnn_dm : 0;
+    std::vector<int8_t> sp;
+    std::vector<double> d, dx, dy, dz;
+    std::vector<int32_t> aham, nl, ns, dl, ds, ta, ar;
+    bool ok = fetch(sp, m.spc, N) && fetch(d, h.ncoup, std::max<size_t>(mnn, 1) * nh) && fetch(aham, h.aham, N) &&
+              fetch(nl, h.nlist, mnn * N) && fetch(ns, h.nsize, N);
+    if (ok && h.do_dm)
+        ok = fetch(dx, h.dmx, mdm * nh) && fetch(dy, h.dmy, mdm * nh) && fetch(dz, h.dmz, mdm * nh) &&
+             fetch(dl, h.dmlist, mdm * N) && fetch(ds, h.dmsize, N);
+    if (ok && h.do_aniso) ok = fetch(ta, h.taniso, N) && fetch(ar, m.arow, N);
+    if (!ok) return false;
+    int nsp = 1;
+    for (int8_t v : sp) nsp = std::max(nsp, v + 1);
+    // distinct DM rows (FP32 bits) of the Hamiltonian rows
+    std::vector<int32_t> dmrow(nh, 0);
+    if (mdm) {
+        KeyInterner dk(3 * mdm, nh);
+        std::vector<int32_t> k(3 * mdm);
+        for (size_t ih = 0; ih < nh; ++ih) {
+            for (size_t sl = 0; sl < mdm; ++sl) {
+                const float f[3] = {(float)dx[sl * nh + ih], (float)dy[sl * nh + ih], (float)dz[sl * nh + ih]};
+                std::memcpy(&k[3 * sl], f, sizeof f);
+            }
+            dmrow[ih] = dk.id(k);
+        }
     }
-    ok = store(&m.cls, cls) && store(&m.cinfo, info) && store(&m.cnb, cnb) && store(&m.cdm, cdm);
-    m.ncls = ok ? (int)ncls : 0;
+    // key: (chemical type, DM row), then the class tables' layout
+    const size_t width = 7 + mnn + mdm;
+    KeyInterner ki(width, std::max<size_t>(1, N / (4 * (size_t)nsp)));
+    std::vector<int32_t> cls(N), key(width);
+    for (size_t i = 0; i < N; ++i) {
+        std::fill(key.begin(), key.end(), 0);
+        const int nn = ns[i], nd = h.do_dm ? ds[i] : 0;
+        key[0] = sp[i];
+        key[1] = dmrow[aham[i]];
+        key[2] = 0;  // coupling row: the class itself (filled below)
+        key[3] = h.do_aniso ? ar[i] : 0;
+        key[4] = h.do_aniso ? ta[i] : 0;
+        key[5] = nn;
+        key[6] = nd;
+        for (int q = 0; q < nn; ++q) key[7 + q] = nl[(size_t)q * N + i] - (int32_t)i;
+        for (int q = 0; q < nd; ++q) key[7 + mnn + q] = dl[(size_t)q * N + i] - (int32_t)i;
+        const int id = ki.id(key);
+        if (id < 0) return true;
+        cls[i] = id;
+    }
+    const size_t G = ki.n;
+    for (size_t g = 0; g < G; ++g) ki.keys[g * width + 2] = (int32_t)g;
+    // the coupling of (slot, class, neighbour type), checked against every site
+    const size_t stride = nsp;
+    std::vector<float> nc(std::max<size_t>(mnn, 1) * G * stride, 0.f);
+    std::vector<uint8_t> have(nc.size(), 0);
+    std::vector<int32_t> rep(G, -1);
+    for (size_t i = 0; i < N; ++i) {
+        const size_t g = cls[i], ih = aham[i];
+        if (rep[g] < 0) rep[g] = (int32_t)ih;
+        for (int q = 0; q < ns[i]; ++q) {
+            const int j = nl[(size_t)q * N + i];
+            const size_t x = ((size_t)q * G + g) * stride + sp[j];
+            const float v = (float)d[(size_t)q * nh + ih];
+            if (!have[x]) {
+                nc[x] = v;
+                have[x] = 1;
+            } else if (std::memcmp(&nc[x], &v, 4) != 0) {
+                return true;  // not a function of the neighbour's type: per-site lists
+            }
+        }
+    }
+    std::vector<int32_t> row(N);
+    for (size_t i = 0; i < N; ++i) row[i] = cls[i];
+    ok = store(&m.row, row) && store(&m.nc, nc);
+    if (ok && h.do_dm) {
+        std::vector<float4> v(mdm * G);
+        for (size_t sl = 0; sl < mdm; ++sl)
+            for (size_t g = 0; g < G; ++g) {
+                const size_t q = sl * nh + rep[g];
+                v[sl * G + g] = make_float4((float)dx[q], (float)dy[q], (float)dz[q], 0.f);
+            }
+        ok = store(&m.dm, v);
+    }
+    ok = ok && store_classes(m, ki, 2, mnn, mdm, cls);
+    m.nrow = (int)G;
+    m.nsp = ok ? nsp : 0;
     return ok;
 }
 
@@ -789,7 +910,7 @@ void mixed_temperature(Sim &s, const double *temp_array) {
     m.T_u = (float)temp_array[0];
 }
 
-int mixed_init(Sim &s) {
+int mixed_init(Sim &s, const int32_t *species) {
     if (!(s.llg.sdealgh == 1 || s.llg.sdealgh == 4 || s.llg.sdealgh == 5 || s.llg.sdealgh == 6 ||
           s.llg.sdealgh == 7 || s.llg.sdealgh == 11)) {
         set_error("precision 3 (FP32 gather, FP64 master): unknown SDEalgh");
@@ -812,6 +933,22 @@ int mixed_init(Sim &s) {
     }
     s.bytes_allocated += n * (2 * sizeof(float4) + 3 * sizeof(float));
     m.valid = 0;
+    // the caller's chemical types (0..15) for chemically resolved couplings;
+    // UPPASD_CHEMICAL_CLASSES=0 keeps the per-site lists (for comparisons)
+    const char *cc = getenv("UPPASD_CHEMICAL_CLASSES");
+    if (species && !(cc && cc[0] == '0')) {
+        const size_t N = s.ham.natom;
+        std::vector<int8_t> sp(N);
+        bool in_range = true;
+        for (size_t i = 0; i < N && in_range; ++i) {
+            in_range = species[i] >= 0 && species[i] < 16;
+            sp[i] = (int8_t)species[i];
+        }
+        if (in_range && !store(&m.spc, sp)) {
+            set_error("precision 3 set-up: chemical types");
+            return UPPASD_GPU_ENOMEM;
+        }
+    }
     return mixed_coefficients(s);
 }
 
@@ -820,7 +957,7 @@ void mixed_free(Sim &s) {
     for (void *q : {(void *)m.mt, (void *)m.mp, (void *)m.b2x, (void *)m.b2y, (void *)m.b2z, (void *)m.nc,
                     (void *)m.dm, (void *)m.jt, (void *)m.an, (void *)m.an2, (void *)m.ext, (void *)m.row,
                     (void *)m.arow, (void *)m.cls, (void *)m.cinfo, (void *)m.cnb, (void *)m.cdm, (void *)m.moved,
-                    (void *)m.lox, (void *)m.loy, (void *)m.loz})
+                    (void *)m.lox, (void *)m.loy, (void *)m.loz, (void *)m.spc})
         cudaFree(q);
     m = MixedDev{};
 }

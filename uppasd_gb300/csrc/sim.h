@@ -98,6 +98,13 @@ struct MixedDev {
     int4 *cinfo = nullptr;     // [ncls] (nn | nd << 16, coupling row, anisotropy row, anisotropy type)
     int32_t *cnb = nullptr;    // [ncls][mnn] exchange neighbour offsets j - i
     int32_t *cdm = nullptr;    // [ncls][mnn_dm] DM neighbour offsets j - i
+    // Chemical resolution (a random alloy, where each site's exchange row depends on its
+    // neighbours' chemical types): nsp > 0 when every scalar exchange coupling is a
+    // function of (class, slot, chemical type of the neighbour); the classes then key on
+    // the site's own type and geometry only, nc is [mnn][nrow][nsp] (nrow = ncls) and a
+    // neighbour's coupling is indexed by spc[j].
+    int nsp = 0;
+    int8_t *spc = nullptr;     // [natom] chemical type, 0-based, when the caller gave one
     // per-site parameters that are the same everywhere are passed as scalars
     int uni_lam = 0, uni_g = 0, uni_T = 0, uni_m = 0;
     float lam_u = 0.f, g_u = 0.f, T_u = 0.f;

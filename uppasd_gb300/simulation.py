@@ -300,6 +300,17 @@ class GpuSimulation:
         _lib.call("uppasd_gpu_time_kernels", self._h, int(nrep), _ptr(ms))
         return {"predict_ms": ms[0], "correct_ms": ms[1], "step_ms": ms[2]}
 
+    def path_info(self):
+        """Which path and data forms init chose: precision, structured stencil path, and on
+        the FP32-gather path the site classes (0: per-site lists), distinct coupling rows,
+        chemical types the exchange is looked up by (0: none), uniform external field;
+        device bytes allocated."""
+        info = np.zeros(8, dtype=np.int64)
+        _lib.call("uppasd_gpu_path_info", self._h, info.ctypes.data_as(C.POINTER(C.c_int64)))
+        keys = ("precision", "structured", "site_classes", "coupling_rows", "chemical_types", "uniform_field",
+                "device_bytes")
+        return {k: int(v) for k, v in zip(keys, info)}
+
     def observables(self):
         M = self.lat.mensemble
         mv = np.empty((M, 3))
