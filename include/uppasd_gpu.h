@@ -98,7 +98,10 @@ typedef struct {
     const double *temp_array;    /* (natom) */
     const double *landeg;        /* (natom); NULL means 1.0 (g = 2) */
     const double *emom;          /* (3, natom, mensemble) initial unit moments */
-    const int32_t *species;      /* (natom) chemical type, 0-based, or NULL (structured path) */
+    const int32_t *species;      /* (natom) chemical type, 0-based (achtype - 1,
+                                    System/chemicaldata.f90:9), or NULL: the structured
+                                    path's species and the FP32-gather path's chemical
+                                    site classes */
 } uppasd_gpu_arrays;
 
 const char *uppasd_gpu_last_error(void);
