@@ -975,6 +975,21 @@ def run_gb300(args, w):
                 "kernel_ms": kt2, "roofline": _roofline(kt2, nspin, 8, ms2 / args.steps, peak, peak_kind, None)}
         except Exception as exc:
             variants[vname] = {"error": str(exc)}
+        # the same lattice through the general neighbour-list path (precision 4: FP32 gather,
+        # double-single master), with the chemical site classes the alloy's types allow
+        try:
+            gp = _make_sim(lat, w, 4, 1000 + rank, e0)
+            gp.set_stream(stream.cuda_stream)
+            info = gp.path_info()
+            msg = _time_steps(gp, stream, 16, 4, world)
+            ktg = gp.time_kernels(3)
+            gp.close()
+            variants["general_path_same_lattice"] = {
+                "value": nspin * 16 * world / (msg * 1e-3), "ms_per_step": msg / 16, "kernel_ms": ktg,
+                "site_classes": info["site_classes"], "chemical_types": info["chemical_types"],
+                "note": "precision 4 over the caller's neighbour lists (no stencil, no shared-memory planes)"}
+        except Exception as exc:
+            variants["general_path_same_lattice"] = {"error": str(exc)}
         # general Hamiltonians (neighbour lists, DMI, anisotropy): FP64 path and FP32 gather
         # with the FP64 state (precision 3) or a double-single pair (precision 4) as master,
         # on the same lattice
