@@ -28,6 +28,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <mutex>
 #include <string>
@@ -422,12 +423,17 @@ int dipole_setup(Sim &s, int mode, double alat, const double *coord_in, int na, 
         d->npad = (long long)d->p1 * d->p2 * d->p3;
         d->nc = (long long)(d->p1 / 2 + 1) * d->p2 * d->p3;
         const size_t nb = (size_t)M * na * 3;
-        e = cudaMalloc(&d->mr, nb * d->npad * sizeof(double));
+        // cuFFT's batched plans take the distances between transforms as int
+        if (d->npad > INT_MAX || nb > (size_t)INT_MAX || (long long)na * na * 6 > INT_MAX) {
+            set_error("set_dipole: the padded grid is too large for the FFT form (more than 2^31 points)");
+            rc = UPPASD_GPU_EINVAL;
+        }
+        if (!rc) e = cudaMalloc(&d->mr, nb * d->npad * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&d->fr, nb * d->npad * sizeof(double));
         if (e == cudaSuccess) e = cudaMalloc(&d->mk, nb * d->nc * sizeof(cufftDoubleComplex));
         if (e == cudaSuccess) e = cudaMalloc(&d->fk, nb * d->nc * sizeof(cufftDoubleComplex));
         if (e == cudaSuccess) e = cudaMalloc(&d->kt, (size_t)na * na * 6 * d->nc * sizeof(cufftDoubleComplex));
-        if (e == cudaSuccess) {
+        if (e == cudaSuccess && !rc) {
             rc = plan3(&d->pf, *d, CUFFT_D2Z, (int)nb);
             if (!rc) rc = plan3(&d->pi, *d, CUFFT_Z2D, (int)nb);
             d->plans = rc == UPPASD_GPU_OK;
@@ -436,6 +442,7 @@ int dipole_setup(Sim &s, int mode, double alat, const double *coord_in, int na, 
         if (e == cudaSuccess && !rc) {
             double *treal = nullptr, *dcell = nullptr, *dbas = nullptr;
             cufftHandle pt = 0;
+            bool pt_made = false;
             const size_t nt = (size_t)na * na * 6;
             e = cudaMalloc(&treal, nt * d->npad * sizeof(double));
             if (e == cudaSuccess) e = cudaMalloc(&dcell, 9 * sizeof(double));
@@ -447,13 +454,16 @@ int dipole_setup(Sim &s, int mode, double alat, const double *coord_in, int na, 
                 dip_tensor<<<(unsigned)((tot + 255) / 256), 256>>>(*d, dcell, dbas, treal);
                 e = cudaGetLastError();
             }
-            if (e == cudaSuccess) rc = plan3(&pt, *d, CUFFT_D2Z, (int)nt);
+            if (e == cudaSuccess) {
+                rc = plan3(&pt, *d, CUFFT_D2Z, (int)nt);
+                pt_made = rc == UPPASD_GPU_OK;
+            }
             if (e == cudaSuccess && !rc && g_fft.exec_d2z(pt, treal, d->kt) != CUFFT_SUCCESS) {
                 set_error("set_dipole: cuFFT transform of the tensor failed");
                 rc = UPPASD_GPU_ECUDA;
             }
             if (e == cudaSuccess) e = cudaDeviceSynchronize();
-            if (pt) g_fft.destroy(pt);
+            if (pt_made) g_fft.destroy(pt);
             cudaFree(treal);
             cudaFree(dcell);
             cudaFree(dbas);
