@@ -182,7 +182,9 @@ int uppasd_gpu_sd_run(uppasd_gpu_sim *s, int64_t nsteps);
  * three arrays NULL to skip it.  On the structured path (precision 1, 2) with
  * mensemble > 1 and page-locked arrays, the ensembles are split into up to eight groups,
  * each copied in, stepped and copied out on its own stream, so that one group's host
- * copies run while the others step; otherwise the three calls run in turn. */
+ * copies run while the others step; otherwise the three calls run in turn.  The call
+ * returns (on success or on an error) after every copy it issued has finished, so the
+ * caller's arrays are free again. */
 int uppasd_gpu_sd_run_io(uppasd_gpu_sim *s, const double *emom_in, int64_t nsteps, double *emom_out,
                          double *emomM_out);
 

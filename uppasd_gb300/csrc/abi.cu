@@ -668,7 +668,10 @@ int uppasd_gpu_put_moments(uppasd_gpu_sim *w, const double *emom) {
         if (e == cudaSuccess && q) e = cudaMemsetAsync(q, 0, n * sizeof(double), s.stream);
     if (e == cudaSuccess && uppasd::structured(s)) {
         int rc = uppasd::structured_load_state(s);
-        if (rc) return rc;
+        if (rc) {
+            cudaStreamSynchronize(s.stream);  // the caller's buffer is free on return, error or not
+            return rc;
+        }
     }
     // the caller may reuse its buffer once this returns
     if (e == cudaSuccess) e = cudaStreamSynchronize(s.stream);
@@ -905,13 +908,42 @@ namespace uppasd {
 // so one group's copies run under the other groups' steps.  Every group reads the
 // same device step counter, advanced once at the end: the Philox counters, and so the
 // results, are those of put_moments + sd_run + get_moments.
+// One group of the pipelined block: its input slice in, its steps, its outputs back.
+static int sd_run_io_group(Sim &s, double *stage, int g, int k0, int kn, const double *in, int64_t nsteps,
+                           double *out, double *outM) {
+    const int N = s.ham.natom;
+    cudaStream_t st = s.io_stream[g];
+    const size_t off = (size_t)k0 * N, cnt = (size_t)kn * N;
+    int rc;
+    // the input copies one after another in group order, so the first group has its
+    // slice at the full host-link rate and starts stepping while the rest arrive
+    UPPASD_CUDA_TRY(cudaStreamWaitEvent(st, g ? s.io_in[g - 1] : s.io_start, 0));
+    UPPASD_CUDA_TRY(cudaMemcpyAsync(stage + 3 * off, in + 3 * off, 3 * cnt * sizeof(double), cudaMemcpyHostToDevice,
+                                    st));
+    UPPASD_CUDA_TRY(cudaEventRecord(s.io_in[g], st));
+    // the staging slice straight into the structured state and back (the generic e / eM
+    // are brought up to date by the next call that reads them)
+    if ((rc = structured_load_range(s, stage, k0, kn, st)) || (rc = structured_steps_range(s, nsteps, k0, kn, st)))
+        return rc;
+    // the two outputs share the group's slice of the staging array in stream order
+    for (auto [full, h] : {std::pair<int, double *>{0, out}, {1, outM}}) {
+        if (!h) continue;
+        if ((rc = structured_store_range(s, stage, full, k0, kn, st))) return rc;
+        UPPASD_CUDA_TRY(cudaMemcpyAsync(h + 3 * off, stage + 3 * off, 3 * cnt * sizeof(double),
+                                        cudaMemcpyDeviceToHost, st));
+    }
+    UPPASD_CUDA_TRY(cudaEventRecord(s.io_ev[g], st));
+    UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.io_ev[g], 0));
+    return UPPASD_GPU_OK;
+}
+
 static int sd_run_io_pipelined(Sim &s, const double *in, int64_t nsteps, double *out, double *outM) {
     int rc = io_streams(s);
     if (rc) return rc;
     double *stage = stage_buffer(s);
     if (!stage) return UPPASD_GPU_ENOMEM;
     square_mirror_stale(s);
-    const int M = s.ham.mensemble, N = s.ham.natom;
+    const int M = s.ham.mensemble;
     // groups: UPPASD_IO_GROUPS (1 .. kIoGroups) when set, else kIoGroups
     static const int groups = [] {
         const char *v = std::getenv("UPPASD_IO_GROUPS");
@@ -922,27 +954,11 @@ static int sd_run_io_pipelined(Sim &s, const double *in, int64_t nsteps, double 
     UPPASD_CUDA_TRY(cudaEventRecord(s.io_start, s.stream));
     for (int g = 0; g < G; ++g) {
         const int k0 = (int)((int64_t)M * g / G), kn = (int)((int64_t)M * (g + 1) / G) - k0;
-        cudaStream_t st = s.io_stream[g];
-        const size_t off = (size_t)k0 * N, cnt = (size_t)kn * N;
-        // the input copies one after another in group order, so the first group has its
-        // slice at the full host-link rate and starts stepping while the rest arrive
-        UPPASD_CUDA_TRY(cudaStreamWaitEvent(st, g ? s.io_in[g - 1] : s.io_start, 0));
-        UPPASD_CUDA_TRY(cudaMemcpyAsync(stage + 3 * off, in + 3 * off, 3 * cnt * sizeof(double),
-                                        cudaMemcpyHostToDevice, st));
-        UPPASD_CUDA_TRY(cudaEventRecord(s.io_in[g], st));
-        // the staging slice straight into the structured state and back (the generic e / eM
-        // are brought up to date by the next call that reads them)
-        if ((rc = structured_load_range(s, stage, k0, kn, st)) || (rc = structured_steps_range(s, nsteps, k0, kn, st)))
+        if ((rc = sd_run_io_group(s, stage, g, k0, kn, in, nsteps, out, outM))) {
+            // nothing issued so far may still touch the caller's arrays once the call returns
+            for (int q = 0; q <= g; ++q) cudaStreamSynchronize(s.io_stream[q]);
             return rc;
-        // the two outputs share the group's slice of the staging array in stream order
-        for (auto [full, h] : {std::pair<int, double *>{0, out}, {1, outM}}) {
-            if (!h) continue;
-            if ((rc = structured_store_range(s, stage, full, k0, kn, st))) return rc;
-            UPPASD_CUDA_TRY(cudaMemcpyAsync(h + 3 * off, stage + 3 * off, 3 * cnt * sizeof(double),
-                                            cudaMemcpyDeviceToHost, st));
         }
-        UPPASD_CUDA_TRY(cudaEventRecord(s.io_ev[g], st));
-        UPPASD_CUDA_TRY(cudaStreamWaitEvent(s.stream, s.io_ev[g], 0));
     }
     advance_step<<<1, 1, 0, s.stream>>>(s.llg.d_step, nsteps);
     UPPASD_CUDA_TRY(cudaGetLastError());
