@@ -113,26 +113,36 @@ __device__ inline void normal3_f32_fast(uint64_t seed, int64_t site, int32_t ens
     z[2] = -r1 * c1;
 }
 
-// Double-single helpers (Dekker / Knuth error-free transformations).
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+// Double-single helpers (Dekker / Knuth error-free transformations), host-callable so
+// that their error bounds are checked on the CPU too.
+__host__ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     float bb = s - a;
     e = (a - (s - bb)) + (b - bb);
 }
-__device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
+__host__ __device__ __forceinline__ void quick_two_sum(float a, float b, float &s, float &e) {
     s = a + b;
     e = b - (s - a);
 }
-__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+__host__ __device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
     p = a * b;
     e = fmaf(a, b, -p);
+}
+// FP32 estimate of 1/sqrt(x) for the Newton step below (the device's rsqrtf; on the host
+// the correctly rounded quotient, which the step refines the same way)
+__host__ __device__ __forceinline__ float rsqrt_estimate(float x) {
+#ifdef __CUDA_ARCH__
+    return rsqrtf(x);
+#else
+    return 1.0f / sqrtf(x);
+#endif
 }
 
 // A unit vector held as double-single pairs (hi + lo per component, ~48 bits) plus a
 // change d: the sum, then |e|^2 - 1 from exact products, and the renormalisation by
 // 1/sqrt(1 + x) to second order (|x| below ~1e-7 for the norm-preserving updates, so the
 // truncation is below 1e-21), the correction added back with error-free sums.
-__device__ __forceinline__ void ds_add_renorm(float hi[3], float lo[3], const float d[3]) {
+__host__ __device__ __forceinline__ void ds_add_renorm(float hi[3], float lo[3], const float d[3]) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         float sm, er;
@@ -167,7 +177,7 @@ __device__ __forceinline__ void ds_add_renorm(float hi[3], float lo[3], const fl
 // from exact products (1 - p and the difference of the two near-equal O(x) terms are exact
 // by Sterbenz's lemma for |x| < 1/2), so s_hi = y0 - 1 (exact) and s_lo = y0 r / 2; the
 // correction e (s_hi + s_lo) is added with an exact product for its leading term.
-__device__ __forceinline__ void ds_add_renorm_wide(float hi[3], float lo[3], const float d[3]) {
+__host__ __device__ __forceinline__ void ds_add_renorm_wide(float hi[3], float lo[3], const float d[3]) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         float sm, er;
@@ -186,7 +196,7 @@ __device__ __forceinline__ void ds_add_renorm_wide(float hi[3], float lo[3], con
     float xs, xe;
     two_sum(n2h, -1.0f, xs, xe);
     const float xl = xe + n2l;  // x = xs + xl
-    const float y0 = rsqrtf(1.0f + xs);
+    const float y0 = rsqrt_estimate(1.0f + xs);
     float p, pe, q, qe;
     two_prod(y0, y0, p, pe);  // y0^2 = p + pe
     two_prod(xs, p, q, qe);   // xs p = q + qe
