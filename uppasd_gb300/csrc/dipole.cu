@@ -52,7 +52,7 @@ struct DipoleDev {
     cufftDoubleComplex *mk = nullptr, *fk = nullptr; // [M][NA][3][nc]
     cufftDoubleComplex *kt = nullptr;                // [NA][NA][6][nc]
     cufftHandle pf = 0, pi = 0;
-    bool plans = false;
+    bool pf_made = false, pi_made = false;  // each plan destroyed only if it was made
 };
 
 namespace {
@@ -279,10 +279,8 @@ __global__ void dip_unpad(DipoleDev d, Vec3D out, int N, int M) {
 }
 
 void dipole_release(DipoleDev &d) {
-    if (d.plans && g_fft.ok) {
-        g_fft.destroy(d.pf);
-        g_fft.destroy(d.pi);
-    }
+    if (d.pf_made) g_fft.destroy(d.pf);
+    if (d.pi_made) g_fft.destroy(d.pi);
     for (void *q : {(void *)d.coord, (void *)d.part, (void *)d.mr, (void *)d.fr, (void *)d.mk, (void *)d.fk,
                     (void *)d.kt})
         cudaFree(q);
@@ -428,15 +426,20 @@ int dipole_setup(Sim &s, int mode, double alat, const double *coord_in, int na, 
             set_error("set_dipole: the padded grid is too large for the FFT form (more than 2^31 points)");
             rc = UPPASD_GPU_EINVAL;
         }
-        if (!rc) e = cudaMalloc(&d->mr, nb * d->npad * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&d->fr, nb * d->npad * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&d->mk, nb * d->nc * sizeof(cufftDoubleComplex));
-        if (e == cudaSuccess) e = cudaMalloc(&d->fk, nb * d->nc * sizeof(cufftDoubleComplex));
-        if (e == cudaSuccess) e = cudaMalloc(&d->kt, (size_t)na * na * 6 * d->nc * sizeof(cufftDoubleComplex));
+        if (!rc) {
+            e = cudaMalloc(&d->mr, nb * d->npad * sizeof(double));
+            if (e == cudaSuccess) e = cudaMalloc(&d->fr, nb * d->npad * sizeof(double));
+            if (e == cudaSuccess) e = cudaMalloc(&d->mk, nb * d->nc * sizeof(cufftDoubleComplex));
+            if (e == cudaSuccess) e = cudaMalloc(&d->fk, nb * d->nc * sizeof(cufftDoubleComplex));
+            if (e == cudaSuccess) e = cudaMalloc(&d->kt, (size_t)na * na * 6 * d->nc * sizeof(cufftDoubleComplex));
+        }
         if (e == cudaSuccess && !rc) {
             rc = plan3(&d->pf, *d, CUFFT_D2Z, (int)nb);
-            if (!rc) rc = plan3(&d->pi, *d, CUFFT_Z2D, (int)nb);
-            d->plans = rc == UPPASD_GPU_OK;
+            d->pf_made = rc == UPPASD_GPU_OK;
+            if (!rc) {
+                rc = plan3(&d->pi, *d, CUFFT_Z2D, (int)nb);
+                d->pi_made = rc == UPPASD_GPU_OK;
+            }
         }
         // the transformed tensors, once
         if (e == cudaSuccess && !rc) {
