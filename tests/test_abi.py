@@ -97,6 +97,8 @@ def test_null_arguments(lib):
     assert lib.uppasd_gpu_finalize(None) == -1
     assert lib.uppasd_gpu_sd_run(None, 1) == -1
     assert lib.uppasd_gpu_mc_run(None, b"H", 1.0, 1) == -1
+    info = np.zeros(8, dtype=np.int64)
+    assert lib.uppasd_gpu_path_info(None, info.ctypes.data_as(C.POINTER(C.c_int64))) == -1
 
 
 def test_mcbatch_rejects_bad_tables(lib):
