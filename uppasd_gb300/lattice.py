@@ -369,8 +369,99 @@ def _table_neighbours(cell, ncell, periodic, pos, types, shells):
     return nlist, nsize, shell
 
 
+_MT_N, _MT_M = 624, 397
+_U64 = 0xFFFFFFFFFFFFFFFF
+
+
+def _mt_twist(mt: np.ndarray) -> None:
+    """One regeneration of the 624 words in place (mtprng_rand64, RNG/mtprng.f90:213-232),
+    in the three dependency-free blocks of the sequential loops."""
+    upper, lower, one = np.uint64(0x80000000), np.uint64(0x7FFFFFFF), np.uint64(1)
+    mag1 = np.uint64(-1727483681 & _U64)
+
+    def mix(a, b, c):
+        y = (a & upper) | (b & lower)
+        return c ^ (y >> one) ^ np.where((y & one) != 0, mag1, np.uint64(0))
+
+    old = mt.copy()
+    k = _MT_N - _MT_M  # 227
+    mt[0:k] = mix(old[0:k], old[1:k + 1], old[_MT_M:_MT_N])
+    mt[k:2 * k] = mix(old[k:2 * k], old[k + 1:2 * k + 1], mt[0:k])
+    mt[2 * k:_MT_N - 1] = mix(old[2 * k:_MT_N - 1], old[2 * k + 1:_MT_N], mt[k:_MT_M - 1])
+    mt[_MT_N - 1] = mix(old[_MT_N - 1:], mt[0:1], mt[_MT_M - 1:_MT_M])[0]
+
+
+def mtprng_real2(seed: int, n: int) -> np.ndarray:
+    """The first n draws of mtprng_rand_real2 after mtprng_init(seed) (RNG/mtprng.f90:
+    118-138, 191-246, 309-325), the stream the reference's rng_uniform gives after
+    rng_init(tseed) (RNG/randomnumbers.f90:106-146).  Its Mersenne twister keeps INT64
+    words with a sign-extended mag01 and masks to 32 bits only inside the tempering, so a
+    regenerated word's upper bits leak into the first tempering shift: not textbook
+    MT19937 after the first 624 draws."""
+    mt = np.zeros(_MT_N, dtype=np.uint64)
+    p = seed & _U64
+    mt[0] = np.uint64(p)
+    for i in range(1, _MT_N):
+        p = (1812433253 * (p ^ (p >> 30)) + i) & 0xFFFFFFFF
+        mt[i] = np.uint64(p)
+    tb, tc = np.uint64(-1658038656 & _U64), np.uint64(-272236544 & _U64)
+    m32 = np.uint64(0xFFFFFFFF)
+    out = np.empty(n)
+    done = 0
+    while done < n:
+        _mt_twist(mt)
+        r = mt.copy()
+        r ^= r >> np.uint64(11)
+        r = m32 & (r ^ ((r << np.uint64(7)) & tb))
+        r = m32 & (r ^ ((r << np.uint64(15)) & tc))
+        r ^= r >> np.uint64(18)
+        take = min(_MT_N, n - done)
+        out[done:done + take] = r[:take].astype(np.float64) * (1.0 / 4294967296.0)
+        done += take
+    return out
+
+
+def _nint(x: float) -> int:
+    """Fortran nint of a non-negative real: the nearest integer, halves away from zero."""
+    q = int(x)
+    return q + 1 if x - q >= 0.5 else q
+
+
+def random_chemistry(ncells: int, conc, seed: Optional[int] = None, uniform=None) -> np.ndarray:
+    """Chemical types of a random alloy as setup_chemicaldata assigns them
+    (System/geometry.f90:190-329): for each basis site ia in turn, ncells uniform draws
+    (``uniform``, else the reference's stream after rng_init(seed): ``mtprng_real2``); the
+    cells taken in order of decreasing draw (maxloc, the first of equal draws first) go to
+    chemical type 1 for the first nint(c_1 ncells), then to type 2, and so on; cells left
+    over are vacancies (a dilute alloy).  ``conc[ia]`` lists the concentrations of the
+    site's types 1, 2, ....  Returns achtype over the full atom list (atom I0 + NA cell,
+    0-based, cells x fastest): 1-based types, 0 for a vacancy.  (An exact 0.0 draw, 2^-32
+    per draw, would make the reference's maxloc pick an already taken cell; here every
+    cell is taken once.)"""
+    na = len(conc)
+    if uniform is None:
+        if seed is None:
+            raise ValueError("random_chemistry needs the seed (tseed) or the uniform draws")
+        uniform = mtprng_real2(seed, na * ncells)
+    uniform = np.asarray(uniform, dtype=np.float64)
+    if uniform.size < na * ncells:
+        raise ValueError(f"need {na * ncells} uniform draws")
+    achtype = np.zeros(na * ncells, dtype=np.int32)
+    for ia in range(na):
+        q = [_nint(float(c) * ncells) for c in conc[ia]]
+        if sum(q) > ncells:
+            raise ValueError(f"concentrations of site {ia + 1} exceed one")
+        order = np.argsort(-uniform[ia * ncells:(ia + 1) * ncells], kind="stable")
+        start = 0
+        for ich, qq in enumerate(q, 1):
+            achtype[order[start:start + qq] * na + ia] = ich
+            start += qq
+    return achtype
+
+
 def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=None, reduce: bool = False,
-                maptype: int = 1, aunits: bool = False, posfiletype: str = "C", tensor: bool = False):
+                maptype: int = 1, aunits: bool = False, posfiletype: str = "C", tensor: bool = False,
+                chemistry=None, achtype=None, tseed: Optional[int] = None):
     """A Hamiltonian built from the reference's own input tables: the ``cell``, ``ncell``,
     ``BC`` and ``Sym`` keywords of inpsd.dat, the posfile and momfile rows (``sites``:
     per basis site ``(type, x, y, z, mom, ex, ey, ez)``, Cartesian, posfiletype 'C'),
@@ -392,6 +483,17 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
     couplings J_xx J_xy ... J_zz (row by row, read_exchange_tensor_base,
     Input/inputhandler_ext.f90:658-741) into ``j_tens`` (do_jtensor = 1), scaled like ncoup.
 
+    Random alloys (do_ralloy 1): ``chemistry`` maps each basis site (1-based) to its rows
+    ``(ichem, conc, mom, ex, ey, ez)`` (the posfile's chemical columns and the momfile
+    rows of that site); jfile rows are then ``(isite, jsite, ichem, jchem, rx, ry, rz, J)``
+    and a shell's coupling is taken by the chemical types of both atoms, scaled by their
+    moments (setup_neighbour_hamiltonian, Hamiltonian/hamiltonianinit.f90:1060-1068).  The
+    types are ``achtype`` (1-based over the full atom list, 0 a vacancy) or drawn as the
+    reference draws them from ``tseed`` (``random_chemistry``); vacancies leave the atom
+    list and every neighbour list, the remaining atoms numbered in order
+    (setup_chemicaldata's acellnumb).  ``Lattice.species`` holds the 0-based types.  With
+    chemistry the DM, anisotropy, tensor and reduced forms are not read.
+
     Returns the lattice and the momfile directions normalised per atom (Initmag 3)."""
     sites = [tuple(float(v) for v in s) for s in sites]
     na = len(sites)
@@ -407,28 +509,58 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
         raise ValueError("Sym 0 (none) and 1 (cubic) are supported")
     expand = (lambda r: [np.asarray(r, dtype=np.float64)]) if sym == 0 else cubic_images
 
+    chem = chemistry is not None
+    if chem and (tensor or reduce or (dmfile is not None and len(dmfile)) or (kfile is not None and len(kfile))):
+        raise ValueError("random alloys: exchange and moments are read; DM, anisotropy, tensor and reduced "
+                         "forms are not")
+    off = 4 if chem else 2  # (isite, jsite[, ichem, jchem]) before the vector
+
     def read_shells(rows, width):
+        # values[t][k]: the shell's coupling, or with chemistry {(ichem, jchem): coupling}
+        # (read_exchange, Input/inputhandler_ext.f90:484-530: a repeated vector overwrites
+        # the coupling of its chemical pair)
         shells, values = {t: [] for t in set(types)}, {t: [] for t in set(types)}
         for row in rows:
             isite, jsite = int(row[0]), int(row[1])
             it, jt = types[isite - 1], types[jsite - 1]
-            r = np.array([float(v) for v in row[2:5]])
+            r = np.array([float(v) for v in row[off:off + 3]])
             if maptype == 2:
                 r = pos[jsite - 1] - pos[isite - 1] + np.asarray(cell, dtype=np.float64).T @ r
-            val = np.array([float(v) for v in row[5:5 + width]])
+            val = np.array([float(v) for v in row[off + 3:off + 3 + width]])
+            key = (int(row[2]), int(row[3])) if chem else None
             for k, (r0, _) in enumerate(shells[it]):
                 if np.sum((r - r0) ** 2) < 1.0e-5:
-                    values[it][k] = val
+                    if chem:
+                        values[it][k][key] = val
+                    else:
+                        values[it][k] = val
                     break
             else:
                 shells[it].append((r, jt))
-                values[it].append(val)
+                values[it].append({key: val} if chem else val)
         return ({t: [(expand(r), jt) for r, jt in v] for t, v in shells.items()}, values)
 
     fc, fc2 = (1.0, 2.0) if aunits else (FC, FC2)
-    natom = na * int(np.prod(ncell))
+    ncells = int(np.prod(ncell))
+    natom = na * ncells
     b_of = np.arange(natom) % na
     m_of = moms[b_of]
+    if chem:
+        rows_of = {int(s): sorted((tuple(float(v) for v in r) for r in rs), key=lambda r: r[0])
+                   for s, rs in chemistry.items()}
+        if sorted(rows_of) != list(range(1, na + 1)):
+            raise ValueError("chemistry needs the rows of every basis site")
+        if achtype is None:
+            achtype = random_chemistry(ncells, [[r[1] for r in rows_of[s]] for s in range(1, na + 1)], seed=tseed)
+        achtype = np.asarray(achtype, dtype=np.int32).reshape(-1)
+        if achtype.size != natom or achtype.min() < 0:
+            raise ValueError(f"achtype needs {natom} non-negative entries")
+        mom_of = {(s, int(r[0])): r for s in rows_of for r in rows_of[s]}
+        for b, a in zip(b_of, achtype):
+            if a and (b + 1, int(a)) not in mom_of:
+                raise ValueError(f"chemical type {a} has no row on site {b + 1}")
+        rec = np.array([mom_of[(b + 1, int(a))] if a else (0.0,) * 6 for b, a in zip(b_of, achtype)])
+        m_of = rec[:, 2].copy()
 
     def coupled(rows, width):
         shells, values = read_shells(rows, width)
@@ -439,12 +571,38 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
             for k, val in enumerate(values[t]):
                 sel = (b_of[:, None] == i_b) & (sh == k)
                 ii, ss = np.nonzero(sel)
-                mj = m_of[nl[ii, ss] - 1]
+                jj = nl[ii, ss] - 1
+                mj = m_of[jj]
                 mm = m_of[ii] * mj
-                c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, val[None, :] * fc2 / mm[:, None])
+                if chem:
+                    # the coupling of this pair's chemical types, zero for a pair the file omits
+                    v = np.zeros((ii.size, width))
+                    for (ci, cj), vv in val.items():
+                        v[(achtype[ii] == ci) & (achtype[jj] == cj)] = vv
+                else:
+                    v = val[None, :]
+                c[ii, ss] = np.where((np.abs(mm) < 1.0e-6)[:, None], 0.0, v * fc2 / np.where(mm == 0, 1.0, mm)[:, None])
         return nl, ns, c
 
     nlist, nsize, c = coupled(jfile, 9 if tensor else 1)
+    species = None
+    if chem:
+        # vacancies leave the atom list and the neighbour lists (order kept), the rest
+        # renumbered in order
+        keep = achtype > 0
+        slot = np.arange(nlist.shape[1])[None, :]
+        live = (slot < nsize[:, None]) & keep[np.maximum(nlist, 1) - 1]
+        order = np.argsort(~live, axis=1, kind="stable")
+        nlist = np.take_along_axis(nlist, order, axis=1)
+        c = np.take_along_axis(c, np.broadcast_to(order[..., None], c.shape), axis=1)
+        nsize = live.sum(axis=1).astype(np.int32)
+        newidx = np.cumsum(keep).astype(np.int32)  # 1-based new number of a kept atom
+        nlist = np.where(slot < nsize[:, None], newidx[np.maximum(nlist, 1) - 1], 0).astype(np.int32)
+        c = np.where((slot < nsize[:, None])[..., None], c, 0.0)
+        nlist, nsize, c = nlist[keep], nsize[keep], c[keep]
+        m_of, b_of = m_of[keep], b_of[keep]
+        species = (achtype[keep] - 1).astype(np.int8)
+        natom = int(keep.sum())
     jt = None
     if tensor:
         jt = tensor_from_matrices(c.reshape(c.shape[:2] + (3, 3)))
@@ -453,8 +611,13 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
                   j_tens=jt,
                   aham=np.arange(1, natom + 1, dtype=np.int32), mmom=m_of[None, :].copy(),
                   extfield=np.zeros((1, natom, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
-                  periodic=periodic, meta={"types": types, "cell": np.asarray(cell, dtype=np.float64).tolist(),
-                                           "basis": np.asarray(pos).tolist()})
+                  periodic=periodic, species=species,
+                  meta={"types": types, "cell": np.asarray(cell, dtype=np.float64).tolist(),
+                        "basis": np.asarray(pos).tolist()})
+    if chem:
+        lat.meta["achtype"] = achtype
+        if natom != na * ncells:
+            lat.cells, lat.nbasis = (0, 0, 0), 1  # no cell structure once atoms are missing
     if dmfile is not None and len(dmfile):
         if sym != 0:
             raise ValueError("DM tables are supported with Sym 0 only")
@@ -481,6 +644,10 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
         lat.taniso, lat.eaniso, lat.kaniso, lat.sb = taniso, eaniso, kaniso, sb
     if reduce:
         lat = reduced(lat)
+    if chem:
+        d = rec[achtype > 0][:, 3:6]
+        d = d / np.sqrt(np.sum(d * d, axis=1))[:, None]
+        return lat, np.ascontiguousarray(d[None, :, :])
     d = np.array([s[5:8] for s in sites])
     d = d / np.sqrt(np.sum(d * d, axis=1))[:, None]
     return lat, np.ascontiguousarray(d[b_of][None, :, :])
