@@ -9,7 +9,8 @@
   atoms and their moments, checked against a brute-force search by distance on the
   reference's RandomAlloy example tables (examples/Mappings/RandomAlloy: bcc as a cubic
   cell with two sites, 80/20 and 20/80, two shells), and a dilute alloy drops its
-  vacancies from the atom and neighbour lists with every other coupling unchanged."""
+  vacancies from the atom and neighbour lists with every other coupling unchanged;
+  anisotropy and DM rows with chemical columns follow each atom's (site, type)."""
 import numpy as np
 import pytest
 
@@ -125,10 +126,38 @@ def test_dilute_alloy_drops_its_vacancies():
     assert lat.nlist.max() <= lat.natom and lat.cells == (0, 0, 0)
 
 
-def test_chemistry_rejects_missing_rows_and_other_tables():
+def test_chemistry_rejects_missing_rows_and_other_forms():
     with pytest.raises(ValueError):
         lattice.from_tables(np.eye(3), (2, 2, 2), "PPP", SITES, JFILE, sym=1, maptype=2,
                             chemistry={1: _chemistry()[1]}, tseed=1)
     with pytest.raises(ValueError):
         lattice.from_tables(np.eye(3), (2, 2, 2), "PPP", SITES, JFILE, sym=1, maptype=2, chemistry=_chemistry(),
-                            tseed=1, kfile=[(1, 1, 0.1, 0.0, 0.0, 0.0, 1.0, 0.0)])
+                            tseed=1, tensor=True)
+
+
+def test_alloy_anisotropy_and_dm_follow_the_types():
+    """kfile rows (isite, ichem, type, K1, K2, e, ratio) and DM rows with two chemical
+    columns: each atom's anisotropy is its (site, type) row scaled by its own moment, each DM
+    pair's vector that of the two types scaled by both moments (Sym 0: one bond vector)."""
+    L = 4
+    kfile = [(1, 1, 1, 0.10, 0.00, 0.0, 0.0, 1.0, 0.0), (1, 2, 1, 0.30, 0.02, 0.0, 0.0, 1.0, 0.0),
+             (2, 1, 2, 0.05, 0.01, 1.0, 0.0, 0.0, 0.5), (2, 2, 1, 0.20, 0.00, 0.0, 1.0, 0.0, 0.0)]
+    dtab = {(1, 1): (0.1, 0.0, 0.0), (1, 2): (0.0, 0.2, 0.0), (2, 1): (0.0, 0.0, 0.3), (2, 2): (0.4, 0.1, 0.0)}
+    jrows = [(1, 1, ci, cj, 0.5, 0.5, 0.5, JTAB[(ci, cj)][0]) for (ci, cj) in JTAB]
+    drows = [(1, 1, ci, cj, 0.5, 0.5, 0.5, *dtab[(ci, cj)]) for (ci, cj) in dtab]
+    lat, _ = lattice.from_tables(np.eye(3), (L, L, L), "PPP", SITES, jrows, sym=0, maptype=2,
+                                 chemistry=_chemistry(), tseed=5, kfile=kfile, dmfile=drows)
+    ach = lat.meta["achtype"]
+    rows = {(r[0], r[1]): r for r in kfile}
+    for i in range(lat.natom):
+        r = rows[(i % 2 + 1, int(ach[i]))]
+        m = MOM[int(ach[i])]
+        p1, p2 = (4, 6) if r[2] == 2 else (2, 4)
+        assert lat.taniso[i] == r[2] and lat.sb[i] == r[8]
+        assert lat.kaniso[i, 0] == pytest.approx(lattice.FC * r[3] / m ** p1, rel=1e-14)
+        assert lat.kaniso[i, 1] == pytest.approx(lattice.FC * r[4] / m ** p2, rel=1e-14)
+        assert np.allclose(lat.eaniso[i], np.array(r[5:8]) / np.linalg.norm(r[5:8]))
+        assert lat.dmlistsize[i] == 1
+        j = int(lat.dmlist[i, 0]) - 1
+        want = np.array(dtab[(int(ach[i]), int(ach[j]))]) * lattice.FC2 / (m * MOM[int(ach[j])])
+        assert np.allclose(lat.dm_vect[i, 0], want, rtol=1e-14, atol=0.0)

@@ -491,8 +491,9 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
     types are ``achtype`` (1-based over the full atom list, 0 a vacancy) or drawn as the
     reference draws them from ``tseed`` (``random_chemistry``); vacancies leave the atom
     list and every neighbour list, the remaining atoms numbered in order
-    (setup_chemicaldata's acellnumb).  ``Lattice.species`` holds the 0-based types.  With
-    chemistry the DM, anisotropy, tensor and reduced forms are not read.
+    (setup_chemicaldata's acellnumb).  ``Lattice.species`` holds the 0-based types.  DM
+    rows gain the same two chemical columns, kfile rows one (``isite, ichem, type, ...``);
+    the tensor and reduced forms are not read with chemistry.
 
     Returns the lattice and the momfile directions normalised per atom (Initmag 3)."""
     sites = [tuple(float(v) for v in s) for s in sites]
@@ -510,9 +511,8 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
     expand = (lambda r: [np.asarray(r, dtype=np.float64)]) if sym == 0 else cubic_images
 
     chem = chemistry is not None
-    if chem and (tensor or reduce or (dmfile is not None and len(dmfile)) or (kfile is not None and len(kfile))):
-        raise ValueError("random alloys: exchange and moments are read; DM, anisotropy, tensor and reduced "
-                         "forms are not")
+    if chem and (tensor or reduce):
+        raise ValueError("random alloys: the tensor and reduced forms are not read")
     off = 4 if chem else 2  # (isite, jsite[, ichem, jchem]) before the vector
 
     def read_shells(rows, width):
@@ -585,67 +585,78 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
         return nl, ns, c
 
     nlist, nsize, c = coupled(jfile, 9 if tensor else 1)
-    species = None
-    if chem:
-        # vacancies leave the atom list and the neighbour lists (order kept), the rest
-        # renumbered in order
-        keep = achtype > 0
-        slot = np.arange(nlist.shape[1])[None, :]
-        live = (slot < nsize[:, None]) & keep[np.maximum(nlist, 1) - 1]
+    keep = achtype > 0 if chem else None
+    newidx = np.cumsum(keep).astype(np.int32) if chem else None  # 1-based number of a kept atom
+
+    def drop_vacancies(nl, ns, cc):
+        """The lists without vacancies (the order of the rest kept), renumbered, and the
+        vacancies' own rows removed (setup_nm and setup_chemicaldata's acellnumb)."""
+        slot = np.arange(nl.shape[1])[None, :]
+        live = (slot < ns[:, None]) & keep[np.maximum(nl, 1) - 1]
         order = np.argsort(~live, axis=1, kind="stable")
-        nlist = np.take_along_axis(nlist, order, axis=1)
-        c = np.take_along_axis(c, np.broadcast_to(order[..., None], c.shape), axis=1)
-        nsize = live.sum(axis=1).astype(np.int32)
-        newidx = np.cumsum(keep).astype(np.int32)  # 1-based new number of a kept atom
-        nlist = np.where(slot < nsize[:, None], newidx[np.maximum(nlist, 1) - 1], 0).astype(np.int32)
-        c = np.where((slot < nsize[:, None])[..., None], c, 0.0)
-        nlist, nsize, c = nlist[keep], nsize[keep], c[keep]
-        m_of, b_of = m_of[keep], b_of[keep]
-        species = (achtype[keep] - 1).astype(np.int8)
-        natom = int(keep.sum())
+        nl = np.take_along_axis(nl, order, axis=1)
+        cc = np.take_along_axis(cc, np.broadcast_to(order[..., None], cc.shape), axis=1)
+        ns = live.sum(axis=1).astype(np.int32)
+        inside = slot < ns[:, None]
+        nl = np.where(inside, newidx[np.maximum(nl, 1) - 1], 0).astype(np.int32)
+        cc = np.where(inside[..., None], cc, 0.0)
+        return nl[keep], ns[keep], cc[keep]
+
+    if chem:
+        nlist, nsize, c = drop_vacancies(nlist, nsize, c)
     jt = None
     if tensor:
         jt = tensor_from_matrices(c.reshape(c.shape[:2] + (3, 3)))
         c = np.zeros(c.shape[:2] + (1,))
-    lat = Lattice(natom=natom, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=np.ascontiguousarray(c[..., 0]),
+    n_out = int(keep.sum()) if chem else natom
+    sel_out = keep if chem else slice(None)
+    lat = Lattice(natom=n_out, mensemble=1, nlist=nlist, nlistsize=nsize, ncoup=np.ascontiguousarray(c[..., 0]),
                   j_tens=jt,
-                  aham=np.arange(1, natom + 1, dtype=np.int32), mmom=m_of[None, :].copy(),
-                  extfield=np.zeros((1, natom, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
-                  periodic=periodic, species=species,
+                  aham=np.arange(1, n_out + 1, dtype=np.int32), mmom=m_of[sel_out][None, :].copy(),
+                  extfield=np.zeros((1, n_out, 3)), cells=tuple(int(n) for n in ncell), nbasis=na,
+                  periodic=periodic, species=(achtype[keep] - 1).astype(np.int8) if chem else None,
                   meta={"types": types, "cell": np.asarray(cell, dtype=np.float64).tolist(),
                         "basis": np.asarray(pos).tolist()})
     if chem:
         lat.meta["achtype"] = achtype
-        if natom != na * ncells:
+        if n_out != natom:
             lat.cells, lat.nbasis = (0, 0, 0), 1  # no cell structure once atoms are missing
     if dmfile is not None and len(dmfile):
         if sym != 0:
             raise ValueError("DM tables are supported with Sym 0 only")
         dl, ds, dv = coupled(dmfile, 3)
+        if chem:
+            dl, ds, dv = drop_vacancies(dl, ds, dv)
         lat.dmlist, lat.dmlistsize, lat.dm_vect = dl, ds, np.ascontiguousarray(dv)
     if kfile is not None and len(kfile):
-        kt = {int(r[0]): r for r in kfile}
+        # rows (isite, type, K1, K2, ex, ey, ez, ratio), with chemistry (isite, ichem, type,
+        # ...) (read_anisotropy / read_anisotropy_alloy, Input/inputhandler_ext.f90:1046-1080);
+        # scaled by the moment of the atom's site and type (hamiltonianinit.f90:895-960)
+        kc = 1 if chem else 0
+        kt = {(int(r[0]), int(r[1]) if chem else 0): [float(v) for v in r] for r in kfile}
         taniso = np.zeros(natom, dtype=np.int32)
         eaniso = np.zeros((natom, 3))
         kaniso = np.zeros((natom, 2))
         sb = np.zeros(natom)
-        for b in range(na):
-            if b + 1 not in kt:
+        for (site, ich), r in kt.items():
+            sel = (b_of == site - 1) & ((achtype == ich) if chem else True)
+            if not np.any(sel):
                 continue
-            r = [float(v) for v in kt[b + 1]]
-            sel = b_of == b
-            e = np.array(r[4:7])
-            taniso[sel] = int(r[1])
+            e = np.array(r[kc + 4:kc + 7])
+            typ = int(r[kc + 1])
+            taniso[sel] = typ
             eaniso[sel] = e / np.sqrt(e @ e + 1.0e-15)
-            p1, p2 = (4, 6) if int(r[1]) == 2 else (2, 4)
-            kaniso[sel, 0] = fc * r[2] / moms[b] ** p1
-            kaniso[sel, 1] = fc * r[3] / moms[b] ** p2
-            sb[sel] = r[7] if len(r) > 7 else 0.0
-        lat.taniso, lat.eaniso, lat.kaniso, lat.sb = taniso, eaniso, kaniso, sb
+            p1, p2 = (4, 6) if typ == 2 else (2, 4)
+            mom = m_of[sel]
+            kaniso[sel, 0] = fc * r[kc + 2] / mom ** p1
+            kaniso[sel, 1] = fc * r[kc + 3] / mom ** p2
+            sb[sel] = r[kc + 7] if len(r) > kc + 7 else 0.0
+        lat.taniso, lat.eaniso, lat.kaniso, lat.sb = (taniso[sel_out], eaniso[sel_out], kaniso[sel_out],
+                                                      sb[sel_out])
     if reduce:
         lat = reduced(lat)
     if chem:
-        d = rec[achtype > 0][:, 3:6]
+        d = rec[keep][:, 3:6]
         d = d / np.sqrt(np.sum(d * d, axis=1))[:, None]
         return lat, np.ascontiguousarray(d[None, :, :])
     d = np.array([s[5:8] for s in sites])
