@@ -1,0 +1,111 @@
+"""The reference's input directory read by ``inputs.load_system``: inpsd.dat keywords
+with the reference's parsing rules (case, comment markers, values continued on the next
+lines, Fortran d exponents, unknown keywords skipped) and the tables it names give the
+same lattice as ``lattice.from_tables`` handed the same tables, for a bcc ferromagnet with
+anisotropy and an external field and for a random alloy (do_ralloy 1, tseed).  The input
+files are written here; their numbers are this test's own."""
+import numpy as np
+import pytest
+
+from uppasd_gb300 import inputs, lattice
+
+
+def _write(d, name, text):
+    (d / name).write_text(text)
+
+
+def test_bcc_directory(tmp_path):
+    _write(tmp_path, "inpsd.dat", """simid  bccTest
+% a comment line
+ncell  4 4 4        System size
+BC     P P P        Boundary conditions
+Cell   1.00000 0.00000 0.00000
+       0.00000 1.00000 0.00000
+       0.00000 0.00000 1.00000
+SYM    1
+posfile   ./pos.dat
+momfile   ./mom.dat
+exchange  ./jij.dat
+anisotropy ./k.dat
+do_prnstruct 1
+Mensemble 3
+Initmag 3
+mode S
+SDEalgh 5
+Temp 250.0
+timestep 2.0d-16
+damping 0.05
+Nstep 1200
+hfield 0.0 0.0 1.5
+ip_mode S
+ip_nphase 2
+100 10.0 1d-16 0.5
+200 5.0 2d-16 0.1
+""")
+    _write(tmp_path, "pos.dat", "1 1 0.0 0.0 0.0\n2 1 0.5 0.5 0.5\n")
+    _write(tmp_path, "mom.dat", "1 1 2.2 0.0 0.0 1.0\n2 1 2.2 0.0 0.0 1.0\n")
+    _write(tmp_path, "jij.dat", "# isite jsite r J\n1 1 0.5 0.5 0.5 1.30\n1 1 1.0 0.0 0.0 0.70\n")
+    _write(tmp_path, "k.dat", "1 1 0.02 0.0 0.0 0.0 1.0 0.0\n2 1 0.02 0.0 0.0 0.0 1.0 0.0\n")
+    lat, emom, par = inputs.load_system(str(tmp_path))
+    want, e0 = lattice.from_tables(np.eye(3), (4, 4, 4), "PPP",
+                                   [(1, 0.0, 0.0, 0.0, 2.2, 0.0, 0.0, 1.0), (1, 0.5, 0.5, 0.5, 2.2, 0.0, 0.0, 1.0)],
+                                   [(1, 1, 0.5, 0.5, 0.5, 1.3), (1, 1, 1.0, 0.0, 0.0, 0.7)], sym=1,
+                                   kfile=[(1, 1, 0.02, 0.0, 0.0, 0.0, 1.0, 0.0), (2, 1, 0.02, 0.0, 0.0, 0.0, 1.0, 0.0)])
+    assert lat.mensemble == 3 and lat.natom == want.natom == 128
+    for name in ("nlist", "nlistsize", "ncoup", "taniso", "kaniso", "eaniso"):
+        assert np.array_equal(getattr(lat, name), getattr(want, name)), name
+    assert np.array_equal(lat.mmom, np.broadcast_to(want.mmom[:1], (3, 128)))
+    assert np.array_equal(lat.extfield, np.broadcast_to([0.0, 0.0, 1.5], (3, 128, 3)))
+    assert np.array_equal(emom, np.broadcast_to(e0[:1], (3, 128, 3)))
+    assert par["sdealgh"] == 5 and par["mode"] == "S" and par["nstep"] == 1200
+    assert par["temp"] == 250.0 and par["timestep"] == 2.0e-16 and par["damping"] == 0.05
+    assert par["simid"] == "bccTest" and par["initmag"] == 3
+    assert par["ip_phases"] == [[100, 10.0, 1e-16, 0.5], [200, 5.0, 2e-16, 0.1]]
+    assert "do_prnstruct" in par["raw"]
+
+
+def test_defaults(tmp_path):
+    _write(tmp_path, "inpsd.dat", "ncell 2 2 2\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n")
+    _write(tmp_path, "p", "1 1 0 0 0\n")
+    _write(tmp_path, "m", "1 1 1.0 1 0 0\n")
+    _write(tmp_path, "j", "1 1 1 0 0 1.0\n")
+    lat, _, par = inputs.load_system(str(tmp_path))
+    assert lat.natom == 8 and lat.mensemble == 1
+    # the reference's default time step is a REAL(4) literal
+    assert par["timestep"] == float(np.float32(1e-16)) and par["sdealgh"] == 1 and par["mode"] == "S"
+    with pytest.raises(ValueError):
+        _write(tmp_path, "inpsd.dat", "ncell 2 2 2\nposfile p\n")
+        inputs.load_system(str(tmp_path))
+
+
+def test_random_alloy_directory(tmp_path):
+    _write(tmp_path, "inpsd.dat", """ncell 6 6 6
+BC P P P
+cell 1.0 0.0 0.0
+     0.0 1.0 0.0
+     0.0 0.0 1.0
+Sym 1
+maptype 2
+do_ralloy 1
+tseed 11
+posfile ./posfile
+momfile ./momfile
+exchange ./jfile
+""")
+    _write(tmp_path, "posfile", "1 1 1 0.70 0.0 0.0 0.0\n1 1 2 0.30 0.0 0.0 0.0\n"
+                                "2 1 1 0.40 0.5 0.5 0.5\n2 1 2 0.60 0.5 0.5 0.5\n")
+    _write(tmp_path, "momfile", "1 1 2.00 1 0 0\n1 2 1.50 0 1 0\n2 1 2.00 1 0 0\n2 2 1.50 0 1 0\n")
+    jrows = [(1, 1, 1, 1, 0.5, 0.5, 0.5, 1.1), (1, 1, 1, 2, 0.5, 0.5, 0.5, 0.6), (1, 1, 2, 1, 0.5, 0.5, 0.5, 0.6),
+             (1, 1, 2, 2, 0.5, 0.5, 0.5, -0.4), (1, 1, 1, 1, 1.0, 0.0, 0.0, 0.3)]
+    _write(tmp_path, "jfile", "".join(" ".join(str(v) for v in r) + "\n" for r in jrows))
+    lat, emom, par = inputs.load_system(str(tmp_path))
+    chem = {1: [(1, 0.7, 2.0, 1, 0, 0), (2, 0.3, 1.5, 0, 1, 0)], 2: [(1, 0.4, 2.0, 1, 0, 0), (2, 0.6, 1.5, 0, 1, 0)]}
+    want, e0 = lattice.from_tables(np.eye(3), (6, 6, 6), "PPP", [(1, 0, 0, 0, 1, 1, 0, 0), (1, .5, .5, .5, 1, 1, 0, 0)],
+                                   jrows, sym=1, maptype=2, chemistry=chem, tseed=11)
+    for name in ("nlist", "nlistsize", "ncoup", "species", "mmom"):
+        assert np.array_equal(getattr(lat, name), getattr(want, name)), name
+    assert np.array_equal(lat.meta["achtype"], lattice.random_chemistry(216, [(0.7, 0.3), (0.4, 0.6)], seed=11))
+    # on 125 cells 0.7 / 0.3 round to 88 + 38 atoms: more than the cells, refused
+    with pytest.raises(ValueError):
+        lattice.random_chemistry(125, [(0.7, 0.3)], seed=11)
+    assert np.array_equal(emom, e0) and par["tseed"] == 11 and par["do_ralloy"] == 1

@@ -435,9 +435,11 @@ def random_chemistry(ncells: int, conc, seed: Optional[int] = None, uniform=None
     chemical type 1 for the first nint(c_1 ncells), then to type 2, and so on; cells left
     over are vacancies (a dilute alloy).  ``conc[ia]`` lists the concentrations of the
     site's types 1, 2, ....  Returns achtype over the full atom list (atom I0 + NA cell,
-    0-based, cells x fastest): 1-based types, 0 for a vacancy.  (An exact 0.0 draw, 2^-32
-    per draw, would make the reference's maxloc pick an already taken cell; here every
-    cell is taken once.)"""
+    0-based, cells x fastest): 1-based types, 0 for a vacancy.  Concentrations whose rounded
+    counts exceed the cells (0.7 and 0.3 on 125 cells: 88 + 38) are refused; the
+    reference's loop would index past its cell list.  (An exact 0.0 draw, 2^-32 per draw,
+    would make the reference's maxloc pick an already taken cell; here every cell is taken
+    once.)"""
     na = len(conc)
     if uniform is None:
         if seed is None:
