@@ -65,7 +65,8 @@ ip_nphase 2
 
 
 def test_defaults(tmp_path):
-    _write(tmp_path, "inpsd.dat", "ncell 2 2 2\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n")
+    _write(tmp_path, "inpsd.dat", "ncell 2 2 2\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n"
+                                  "initmag 3\n")
     _write(tmp_path, "p", "1 1 0 0 0\n")
     _write(tmp_path, "m", "1 1 1.0 1 0 0\n")
     _write(tmp_path, "j", "1 1 1 0 0 1.0\n")
@@ -88,6 +89,7 @@ Sym 1
 maptype 2
 do_ralloy 1
 tseed 11
+Initmag 1
 posfile ./posfile
 momfile ./momfile
 exchange ./jfile
@@ -108,4 +110,30 @@ exchange ./jfile
     # on 125 cells 0.7 / 0.3 round to 88 + 38 atoms: more than the cells, refused
     with pytest.raises(ValueError):
         lattice.random_chemistry(125, [(0.7, 0.3)], seed=11)
-    assert np.array_equal(emom, e0) and par["tseed"] == 11 and par["do_ralloy"] == 1
+    assert par["tseed"] == 11 and par["do_ralloy"] == 1 and par["initmag"] == 1
+    # Initmag 1 on the same stream, after the 2 x 216 chemical draws
+    s = lattice.MtprngStream(11)
+    s.real2(2 * 216)
+    assert np.array_equal(emom[0], lattice.initmag_random(432, s))
+
+
+def test_restart_start(tmp_path):
+    """Initmag 4 (the default): directions and moment lengths from the restart file."""
+    _write(tmp_path, "inpsd.dat", "ncell 2 2 1\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n"
+                                  "restartfile ./restart.in\nMensemble 2\n")
+    _write(tmp_path, "p", "1 1 0 0 0\n")
+    _write(tmp_path, "m", "1 1 1.0 1 0 0\n")
+    _write(tmp_path, "j", "1 1 1 0 0 1.0\n")
+    rng = np.random.default_rng(2)
+    e = rng.normal(size=(2, 4, 3))
+    e /= np.linalg.norm(e, axis=-1, keepdims=True)
+    mm = 1.0 + rng.random((2, 4))
+    from uppasd_gb300 import output
+    output.write_restart_std(str(tmp_path / "restart.in"), 0, e, mm)
+    lat, emom, par = inputs.load_system(str(tmp_path))
+    assert par["initmag"] == 4 and lat.mensemble == 2
+    assert np.allclose(emom, e, atol=1e-8) and np.allclose(lat.mmom, mm, atol=1e-8)
+    _write(tmp_path, "inpsd.dat", "ncell 2 2 1\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n"
+                                  "initmag 2\n")
+    with pytest.raises(ValueError):
+        inputs.load_system(str(tmp_path))

@@ -34,6 +34,20 @@ def test_mtprng_matches_the_oracle_stream(seed):
     assert np.array_equal(lattice.mtprng_real2(seed, 2500), po.mt_stream(seed, 2500, "real2"))
 
 
+def test_initmag_random_matches_the_oracle():
+    """Initmag 1 against the oracle's restatement (which the HeisStripe, HeisChainAF and
+    SCsurf pins fix), in chunks that split the stream, and the stream left where the
+    oracle's is."""
+    lat = lattice.bcc(5, [1.0], 2.0).with_ensembles(2)
+    o = po.Oracle(lat)
+    o.init_random(7)
+    s = lattice.MtprngStream(7)
+    u = lattice.initmag_random(lat.natom, s, chunk=37)
+    assert np.array_equal(u, o.emom[0]) and np.array_equal(u, o.emom[1])
+    nxt = [o.lib.orc_mt_real2(po.C.byref(o.mt)) for _ in range(5)]
+    assert np.array_equal(s.real2(5), nxt)
+
+
 def _fortran_assignment(ncells, conc, rn_all):
     """setup_chemicaldata's loop as written: per site, maxloc over the draws, the taken
     draw set to zero; the first nint(c ncells) taken cells get type 1, and so on."""

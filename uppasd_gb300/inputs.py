@@ -20,6 +20,7 @@ from typing import Optional
 import numpy as np
 
 from . import lattice as _lattice
+from . import output as _output
 
 _COMMENT = ("%", "#", "*", "=", "!")
 # keyword: (number of values, kind) read list-directed
@@ -100,8 +101,10 @@ def load_system(directory: str, inpsd: str = "inpsd.dat", mensemble: Optional[in
 
     The lattice is ``lattice.from_tables`` of the tables inpsd.dat names (random alloys
     with do_ralloy 1, their chemical types drawn from tseed as the reference draws them),
-    with Mensemble copies and hfield as the external field of every spin; emom is the
-    momfile direction of each atom (Initmag 3).  params holds the run keywords: mode,
+    with Mensemble copies and hfield as the external field of every spin.  emom follows
+    Initmag (default 4): 1 the reference's random start on its stream after rng_init(tseed)
+    (after the alloy's chemical draws), 3 the momfile directions, 4 the restart file
+    (directions and moment lengths); other values are refused.  params holds the run keywords: mode,
     SDEalgh, Temp, timestep (the reference's REAL(4) default 1e-16 when absent), damping,
     Nstep, mcNstep, Initmag, tseed, ip phases, simid and the rest of ``read_inpsd``."""
     k = read_inpsd(os.path.join(directory, inpsd))
@@ -132,22 +135,43 @@ def load_system(directory: str, inpsd: str = "inpsd.dat", mensemble: Optional[in
         m = {int(r[0]): r for r in mom}          # isite ichem mom ex ey ez
         sites = [(p[s][1], p[s][2], p[s][3], p[s][4], *m[s][2:6]) for s in sorted(p)]
     tseed = int(k.get("tseed", 1))
+    initmag = int(k.get("initmag", 4))
+    if initmag not in (1, 3, 4):
+        raise ValueError(f"Initmag {initmag} is not read (1, 3 and 4 are)")
+    # the main stream after rng_init(tseed): the alloy's chemical draws, then Initmag 1
+    stream = _lattice.MtprngStream(tseed)
+    ncells = int(np.prod(k["ncell"]))
+    achtype = None
+    if ralloy:
+        conc = [[r[1] for r in chemistry[s]] for s in sorted(chemistry)]
+        achtype = _lattice.random_chemistry(ncells, conc, uniform=stream.real2(len(conc) * ncells))
     lat, emom = _lattice.from_tables(
         cell, tuple(k["ncell"]), bc, sites, table("exchange"), sym=int(k.get("sym", 0)),
         dmfile=table("dm"), kfile=table("anisotropy"),
         reduce=str(k.get("do_reduced", "N")).upper() == "Y", maptype=int(k.get("maptype", 1)),
         aunits=str(k.get("aunits", "N")).upper() == "Y", posfiletype=str(k.get("posfiletype", "C")).upper(),
-        tensor=int(k.get("do_jtensor", 0)) == 1, chemistry=chemistry, tseed=tseed if ralloy else None)
+        tensor=int(k.get("do_jtensor", 0)) == 1, chemistry=chemistry, achtype=achtype)
     M = int(mensemble if mensemble is not None else k.get("mensemble", 1))
     lat = lat.with_ensembles(M)
     if "hfield" in k:
         lat.extfield = np.ascontiguousarray(np.broadcast_to(np.asarray(k["hfield"], dtype=np.float64),
                                                             (M, lat.natom, 3)))
-    emom = np.ascontiguousarray(np.broadcast_to(emom[:1], (M, lat.natom, 3)))
+    if initmag == 1:
+        u = _lattice.initmag_random(len(sites) * ncells, stream)
+        emom = u[achtype > 0] if ralloy else u
+        emom = np.ascontiguousarray(np.broadcast_to(emom[None], (M, lat.natom, 3)))
+    elif initmag == 4:
+        if "restartfile" not in k:
+            raise ValueError("Initmag 4 (the default) needs a restartfile")
+        _, emom, mm = _output.read_restart(os.path.join(directory, k["restartfile"]), lat.natom, M)
+        lat.mmom = mm
+    else:
+        emom = np.ascontiguousarray(np.broadcast_to(emom[:1], (M, lat.natom, 3)))
     params = {key: v for key, v in k.items() if key not in ("raw",)}
     params.setdefault("timestep", struct.unpack("f", struct.pack("f", 1.0e-16))[0])
     params.setdefault("mode", "S")
     params.setdefault("sdealgh", 1)
     params.setdefault("tseed", tseed)
+    params.setdefault("initmag", initmag)
     params["raw"] = k["raw"]
     return lat, emom, params

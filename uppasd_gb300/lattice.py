@@ -391,33 +391,80 @@ def _mt_twist(mt: np.ndarray) -> None:
     mt[_MT_N - 1] = mix(old[_MT_N - 1:], mt[0:1], mt[_MT_M - 1:_MT_M])[0]
 
 
-def mtprng_real2(seed: int, n: int) -> np.ndarray:
-    """The first n draws of mtprng_rand_real2 after mtprng_init(seed) (RNG/mtprng.f90:
-    118-138, 191-246, 309-325), the stream the reference's rng_uniform gives after
-    rng_init(tseed) (RNG/randomnumbers.f90:106-146).  Its Mersenne twister keeps INT64
-    words with a sign-extended mag01 and masks to 32 bits only inside the tempering, so a
-    regenerated word's upper bits leak into the first tempering shift: not textbook
-    MT19937 after the first 624 draws."""
-    mt = np.zeros(_MT_N, dtype=np.uint64)
-    p = seed & _U64
-    mt[0] = np.uint64(p)
-    for i in range(1, _MT_N):
-        p = (1812433253 * (p ^ (p >> 30)) + i) & 0xFFFFFFFF
-        mt[i] = np.uint64(p)
-    tb, tc = np.uint64(-1658038656 & _U64), np.uint64(-272236544 & _U64)
-    m32 = np.uint64(0xFFFFFFFF)
-    out = np.empty(n)
-    done = 0
-    while done < n:
-        _mt_twist(mt)
-        r = mt.copy()
+class MtprngStream:
+    """The reference's main uniform stream: mtprng_rand_real2 draws after
+    mtprng_init(seed) (RNG/mtprng.f90:118-138, 191-246, 309-325), as rng_uniform gives them
+    after rng_init(tseed) (RNG/randomnumbers.f90:106-146).  Its Mersenne twister keeps
+    INT64 words with a sign-extended mag01 and masks to 32 bits only inside the tempering,
+    so a regenerated word's upper bits leak into the first tempering shift: not textbook
+    MT19937 after the first 624 draws.  ``real2(n)`` returns the next n draws; draws a
+    consumer looked at but did not use stay for the next (``_fill`` / ``pos``)."""
+
+    def __init__(self, seed: int):
+        self.mt = np.zeros(_MT_N, dtype=np.uint64)
+        p = seed & _U64
+        self.mt[0] = np.uint64(p)
+        for i in range(1, _MT_N):
+            p = (1812433253 * (p ^ (p >> 30)) + i) & 0xFFFFFFFF
+            self.mt[i] = np.uint64(p)
+        self.buf = np.empty(0)
+        self.pos = 0
+
+    def _block(self) -> np.ndarray:
+        _mt_twist(self.mt)
+        tb, tc = np.uint64(-1658038656 & _U64), np.uint64(-272236544 & _U64)
+        m32 = np.uint64(0xFFFFFFFF)
+        r = self.mt.copy()
         r ^= r >> np.uint64(11)
         r = m32 & (r ^ ((r << np.uint64(7)) & tb))
         r = m32 & (r ^ ((r << np.uint64(15)) & tc))
         r ^= r >> np.uint64(18)
-        take = min(_MT_N, n - done)
-        out[done:done + take] = r[:take].astype(np.float64) * (1.0 / 4294967296.0)
-        done += take
+        return r.astype(np.float64) * (1.0 / 4294967296.0)
+
+    def _fill(self, n: int) -> None:
+        """At least n draws buffered from pos on."""
+        have = self.buf.size - self.pos
+        if have >= n:
+            return
+        blocks = [self.buf[self.pos:]]
+        for _ in range((n - have + _MT_N - 1) // _MT_N):
+            blocks.append(self._block())
+        self.buf = np.concatenate(blocks)
+        self.pos = 0
+
+    def real2(self, n: int) -> np.ndarray:
+        self._fill(n)
+        out = self.buf[self.pos:self.pos + n].copy()
+        self.pos += n
+        return out
+
+
+def mtprng_real2(seed: int, n: int) -> np.ndarray:
+    """The first n draws of the reference's stream after rng_init(seed) (``MtprngStream``)."""
+    return MtprngStream(seed).real2(n)
+
+
+def initmag_random(natom: int, stream: MtprngStream, chunk: int = 65536) -> np.ndarray:
+    """Initmag 1 (magninit, System/magnetizationinit.f90:141-170): per atom of the full list,
+    in order, three draws give x, y, z = 2 (r - 1/2); while outside the unit sphere, three
+    more give x, y, z = (r - 1/2) (the reference's factor 1 on a retry, so a retry always
+    lands inside); normalised.  Returns (natom, 3) unit vectors; the stream moves past the
+    draws used."""
+    out = np.empty((natom, 3))
+    for a0 in range(0, natom, chunk):
+        na = min(chunk, natom - a0)
+        stream._fill(6 * na)   # at most two tries per atom
+        buf = stream.buf[stream.pos:stream.pos + 6 * na].tolist()
+        k = 0
+        for i in range(a0, a0 + na):
+            x, y, z = 2.0 * (buf[k] - 0.50), 2.0 * (buf[k + 1] - 0.50), 2.0 * (buf[k + 2] - 0.50)
+            k += 3
+            while x * x + y * y + z * z > 1.0:
+                x, y, z = 1.0 * (buf[k] - 0.50), 1.0 * (buf[k + 1] - 0.50), 1.0 * (buf[k + 2] - 0.50)
+                k += 3
+            n = np.sqrt(x * x + y * y + z * z)
+            out[i, 0], out[i, 1], out[i, 2] = x / n, y / n, z / n
+        stream.pos += k
     return out
 
 
