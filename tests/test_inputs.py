@@ -134,6 +134,25 @@ def test_restart_start(tmp_path):
     assert par["initmag"] == 4 and lat.mensemble == 2
     assert np.allclose(emom, e, atol=1e-8) and np.allclose(lat.mmom, mm, atol=1e-8)
     _write(tmp_path, "inpsd.dat", "ncell 2 2 1\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\n"
-                                  "initmag 2\n")
+                                  "initmag 6\n")
     with pytest.raises(ValueError):
         inputs.load_system(str(tmp_path))
+
+
+def test_cone_start(tmp_path):
+    """Initmag 2: two draws per atom in the cone theta0 (radians) about z; mavg0 >= 0
+    replaces the cone by theta0 = 2 acos(mavg0), phi0 = 2 pi."""
+    _write(tmp_path, "p", "1 1 0 0 0\n")
+    _write(tmp_path, "m", "1 1 1.0 1 0 0\n")
+    _write(tmp_path, "j", "1 1 1 0 0 1.0\n")
+    base = "ncell 4 4 4\ncell 1 0 0 0 1 0 0 0 1\nposfile p\nmomfile m\nexchange j\ninitmag 2\ntseed 9\n"
+    _write(tmp_path, "inpsd.dat", base + "theta0 0.3\nphi0 6.283185307179586\n")
+    _, emom, _ = inputs.load_system(str(tmp_path))
+    r = lattice.mtprng_real2(9, 128).reshape(64, 2)
+    want = np.stack([np.sin(0.3 * r[:, 0]) * np.cos(2 * np.pi * r[:, 1]),
+                     np.sin(0.3 * r[:, 0]) * np.sin(2 * np.pi * r[:, 1]), np.cos(0.3 * r[:, 0])], axis=1)
+    assert np.array_equal(emom[0], want)
+    assert np.all(emom[0, :, 2] >= np.cos(0.3) - 1e-15)
+    _write(tmp_path, "inpsd.dat", base + "mavg0 0.9\n")
+    _, emom, _ = inputs.load_system(str(tmp_path))
+    assert np.all(emom[0, :, 2] >= np.cos(2 * np.arccos(0.9)) - 1e-15)

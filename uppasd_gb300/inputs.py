@@ -33,6 +33,7 @@ _VALUES = {
     "alat": (1, float), "do_dip": (1, int), "simid": (1, str), "gpu_rng_seed": (1, int),
     "ip_mode": (1, str), "ip_nphase": (1, int), "ip_mcanneal": (1, int), "avrg_step": (1, int),
     "cumu_step": (1, int), "cumu_buff": (1, int), "plotenergy": (1, int),
+    "theta0": (1, float), "phi0": (1, float), "mavg0": (1, float),
 }
 _FILES = ("posfile", "momfile", "exchange", "dm", "anisotropy", "restartfile")
 
@@ -103,8 +104,9 @@ def load_system(directory: str, inpsd: str = "inpsd.dat", mensemble: Optional[in
     with do_ralloy 1, their chemical types drawn from tseed as the reference draws them),
     with Mensemble copies and hfield as the external field of every spin.  emom follows
     Initmag (default 4): 1 the reference's random start on its stream after rng_init(tseed)
-    (after the alloy's chemical draws), 3 the momfile directions, 4 the restart file
-    (directions and moment lengths); other values are refused.  params holds the run keywords: mode,
+    (after the alloy's chemical draws), 2 random in the cone of theta0, phi0 (or mavg0) on
+    the same stream, 3 the momfile directions, 4 the restart file (directions and moment
+    lengths); other values are refused.  params holds the run keywords: mode,
     SDEalgh, Temp, timestep (the reference's REAL(4) default 1e-16 when absent), damping,
     Nstep, mcNstep, Initmag, tseed, ip phases, simid and the rest of ``read_inpsd``."""
     k = read_inpsd(os.path.join(directory, inpsd))
@@ -136,8 +138,8 @@ def load_system(directory: str, inpsd: str = "inpsd.dat", mensemble: Optional[in
         sites = [(p[s][1], p[s][2], p[s][3], p[s][4], *m[s][2:6]) for s in sorted(p)]
     tseed = int(k.get("tseed", 1))
     initmag = int(k.get("initmag", 4))
-    if initmag not in (1, 3, 4):
-        raise ValueError(f"Initmag {initmag} is not read (1, 3 and 4 are)")
+    if initmag not in (1, 2, 3, 4):
+        raise ValueError(f"Initmag {initmag} is not read (1 to 4 are)")
     # the main stream after rng_init(tseed): the alloy's chemical draws, then Initmag 1
     stream = _lattice.MtprngStream(tseed)
     ncells = int(np.prod(k["ncell"]))
@@ -156,8 +158,11 @@ def load_system(directory: str, inpsd: str = "inpsd.dat", mensemble: Optional[in
     if "hfield" in k:
         lat.extfield = np.ascontiguousarray(np.broadcast_to(np.asarray(k["hfield"], dtype=np.float64),
                                                             (M, lat.natom, 3)))
-    if initmag == 1:
-        u = _lattice.initmag_random(len(sites) * ncells, stream)
+    if initmag in (1, 2):
+        nfull = len(sites) * ncells
+        u = (_lattice.initmag_random(nfull, stream) if initmag == 1 else
+             _lattice.initmag_cone(nfull, stream, float(k.get("theta0", 0.0)), float(k.get("phi0", 0.0)),
+                                   float(k.get("mavg0", -1.0))))
         emom = u[achtype > 0] if ralloy else u
         emom = np.ascontiguousarray(np.broadcast_to(emom[None], (M, lat.natom, 3)))
     elif initmag == 4:

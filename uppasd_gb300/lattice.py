@@ -468,6 +468,19 @@ def initmag_random(natom: int, stream: MtprngStream, chunk: int = 65536) -> np.n
     return out
 
 
+def initmag_cone(natom: int, stream: MtprngStream, theta0: float, phi0: float,
+                 mavg0: float = -1.0) -> np.ndarray:
+    """Initmag 2 (magninit, System/magnetizationinit.f90:187-228): per atom of the full list,
+    in order, two draws r1, r2 give u = (sin(theta0 r1) cos(phi0 r2), sin(theta0 r1)
+    sin(phi0 r2), cos(theta0 r1)), angles in radians; mavg0 >= 0 sets phi0 = 2 pi and
+    theta0 = 2 acos(mavg0).  Returns (natom, 3) unit vectors."""
+    if mavg0 >= 0.0:
+        phi0, theta0 = 2.0 * np.pi, 2.0 * np.arccos(mavg0)
+    r = stream.real2(2 * natom).reshape(natom, 2)
+    th, ph = theta0 * r[:, 0], phi0 * r[:, 1]
+    return np.stack([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], axis=1)
+
+
 def _nint(x: float) -> int:
     """Fortran nint of a non-negative real: the nearest integer, halves away from zero."""
     q = int(x)
