@@ -617,11 +617,20 @@ def from_tables(cell, ncell, bc, sites, jfile, sym: int = 0, dmfile=None, kfile=
         achtype = np.asarray(achtype, dtype=np.int32).reshape(-1)
         if achtype.size != natom or achtype.min() < 0:
             raise ValueError(f"achtype needs {natom} non-negative entries")
-        mom_of = {(s, int(r[0])): r for s in rows_of for r in rows_of[s]}
-        for b, a in zip(b_of, achtype):
-            if a and (b + 1, int(a)) not in mom_of:
-                raise ValueError(f"chemical type {a} has no row on site {b + 1}")
-        rec = np.array([mom_of[(b + 1, int(a))] if a else (0.0,) * 6 for b, a in zip(b_of, achtype)])
+        # (site, type) -> its row (ichem, conc, mom, ex, ey, ez); type 0, a vacancy, all zero
+        nch = max(int(achtype.max()), max(int(r[0]) for rs in rows_of.values() for r in rs))
+        tab = np.zeros((na, nch + 1, 6))
+        known = np.zeros((na, nch + 1), dtype=bool)
+        known[:, 0] = True
+        for s, rs in rows_of.items():
+            for r in rs:
+                tab[s - 1, int(r[0])] = r
+                known[s - 1, int(r[0])] = True
+        miss = ~known[b_of, achtype]
+        if np.any(miss):
+            i = int(np.nonzero(miss)[0][0])
+            raise ValueError(f"chemical type {achtype[i]} has no row on site {b_of[i] + 1}")
+        rec = tab[b_of, achtype]
         m_of = rec[:, 2].copy()
 
     def coupled(rows, width):
