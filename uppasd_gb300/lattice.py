@@ -348,9 +348,18 @@ def _table_neighbours(cell, ncell, periodic, pos, types, shells):
     idx = np.arange(natom, dtype=np.int64)
     bb, cidx = idx % na, idx // na
     x, y, z = cidx % n1, (cidx // n1) % n2, cidx // (n1 * n2)
+    dims = (n1, n2, n3)
     for b in range(na):
         sel = np.nonzero(bb == b)[0]
+        earlier = []
         for dx, dy, dz, b2, k in stencil[b]:
+            # an earlier entry can give the same neighbour only with the same basis atom and
+            # offsets equal on open axes, congruent modulo the cells on periodic ones; without
+            # one the duplicate test below finds nothing and is skipped
+            clash = any(q[3] == b2 and all(((d - e) % n == 0) if per else d == e
+                                           for d, e, n, per in zip((dx, dy, dz), q[:3], dims, periodic))
+                        for q in earlier)
+            earlier.append((dx, dy, dz, b2))
             xx, yy, zz = x[sel] + dx, y[sel] + dy, z[sel] + dz
             ok = np.ones(sel.size, dtype=bool)
             for vv, nn, per in ((xx, n1, periodic[0]), (yy, n2, periodic[1]), (zz, n3, periodic[2])):
@@ -360,8 +369,9 @@ def _table_neighbours(cell, ncell, periodic, pos, types, shells):
                     ok &= (vv >= 0) & (vv < nn)
             j = _site_index(b2, xx, yy, zz, na, n1, n2) + 1
             rows, j = sel[ok], j[ok]
-            fresh = ~np.any(nlist[rows] == j[:, None].astype(np.int32), axis=1)
-            rows, j = rows[fresh], j[fresh]
+            if clash:
+                fresh = ~np.any(nlist[rows] == j[:, None].astype(np.int32), axis=1)
+                rows, j = rows[fresh], j[fresh]
             slot = nsize[rows]
             nlist[rows, slot] = j
             shell[rows, slot] = k
