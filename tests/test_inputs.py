@@ -156,3 +156,52 @@ def test_cone_start(tmp_path):
     _write(tmp_path, "inpsd.dat", base + "mavg0 0.9\n")
     _, emom, _ = inputs.load_system(str(tmp_path))
     assert np.all(emom[0, :, 2] >= np.cos(2 * np.arccos(0.9)) - 1e-15)
+
+
+def _fmt(v):
+    return repr(float(v)) if isinstance(v, float) else str(v)
+
+
+def _write_case(d, inp, extra=""):
+    """A pinned regression case's tables written back out as an input directory (the
+    tables stored in the golden fixture, in the reference's file layouts)."""
+    sites = inp["sites"]
+    _write(d, "posfile", "".join(f"{i + 1} {int(s[0])} {s[1]} {s[2]} {s[3]}\n" for i, s in enumerate(sites)))
+    _write(d, "momfile", "".join(f"{i + 1} 1 {s[4]} {s[5]} {s[6]} {s[7]}\n" for i, s in enumerate(sites)))
+    _write(d, "jfile", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in inp["jfile"]))
+    text = (f"ncell {' '.join(str(n) for n in inp['ncell'])}\nBC {' '.join(inp['bc'])}\n"
+            "cell " + "\n     ".join(" ".join(repr(float(v)) for v in row) for row in inp["cell"]) + "\n"
+            f"Sym {inp['sym']}\nmaptype {inp['maptype']}\nposfiletype {inp['posfiletype']}\n"
+            "posfile ./posfile\nmomfile ./momfile\nexchange ./jfile\n"
+            f"Initmag {inp['initmag']}\nSDEalgh {inp['sdealgh']}\nTemp {inp['temp']}\n"
+            f"timestep {inp['timestep']!r}\ndamping {inp['damping']}\nmode S\nNstep {inp['nstep']}\n")
+    if "kfile" in inp:
+        _write(d, "kfile", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in inp["kfile"]))
+        text += "anisotropy ./kfile\n"
+    _write(d, "inpsd.dat", text + extra)
+
+
+def test_pinned_case_through_the_reader(tmp_path):
+    """tests/HeisStripe end to end through the reader: its tables written as an input
+    directory, read by load_system (Initmag 1 drawn from the default tseed), run on the
+    oracle with the directory's solver, time step and damping: <m> after 1190 steps equals
+    the reference's printed value."""
+    import json
+    import os
+    from oracle import pyoracle as po
+    here = os.path.dirname(os.path.abspath(__file__))
+    pins = json.load(open(os.path.join(here, "golden", "reference_pins.json")))
+    _write_case(tmp_path, pins["inputs"]["heisstripe"])
+    lat, e0, par = inputs.load_system(str(tmp_path))
+    o = po.Oracle(lat, threads=1)
+    o.set_moments(e0)
+    o.setup_ziggurat(par["tseed"])
+    o.make_llg(par["sdealgh"], par["timestep"], par["damping"], par["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+    for _ in range(1190):
+        o.sd_step()
+    mv, ma = o.mavg()
+    got = np.array(list(mv[0] / lat.natom) + [ma[0]])
+    pin = pins["heisstripe_iter1190"]
+    exp = np.asarray(pin["expected"])
+    printed = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(exp) + 1e-300)) - 8)
+    assert np.all(np.abs(got - exp) <= 1e-8 + printed), (got, exp)
