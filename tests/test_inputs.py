@@ -175,33 +175,40 @@ def _write_case(d, inp, extra=""):
             "posfile ./posfile\nmomfile ./momfile\nexchange ./jfile\n"
             f"Initmag {inp['initmag']}\nSDEalgh {inp['sdealgh']}\nTemp {inp['temp']}\n"
             f"timestep {inp['timestep']!r}\ndamping {inp['damping']}\nmode S\nNstep {inp['nstep']}\n")
-    if "kfile" in inp:
-        _write(d, "kfile", "".join(" ".join(_fmt(v) for v in r) + "\n" for r in inp["kfile"]))
-        text += "anisotropy ./kfile\n"
+    for key, name, word in (("kfile", "kfile", "anisotropy"), ("dmfile", "dmfile", "dm")):
+        if key in inp:
+            _write(d, name, "".join(" ".join(_fmt(v) for v in r) + "\n" for r in inp[key]))
+            text += f"{word} ./{name}\n"
+    if inp.get("aunits"):
+        text += "aunits Y\n"
     _write(d, "inpsd.dat", text + extra)
 
 
-def test_pinned_case_through_the_reader(tmp_path):
-    """tests/HeisStripe end to end through the reader: its tables written as an input
-    directory, read by load_system (Initmag 1 drawn from the default tseed), run on the
-    oracle with the directory's solver, time step and damping: <m> after 1190 steps equals
-    the reference's printed value."""
+@pytest.mark.parametrize("case,steps,pin", [("heisstripe", 1190, "heisstripe_iter1190"),
+                                            ("scsurf", 800, "scsurf_iter800")])
+def test_pinned_case_through_the_reader(tmp_path, case, steps, pin):
+    """Pinned regression cases end to end through the reader: the tables of tests/HeisStripe
+    (vacuum edges, anisotropy) and tests/SCsurf (atomic units, maptype 2, DM and
+    anisotropy) written as input directories, read by load_system (Initmag 1 drawn from the
+    default tseed), run on the oracle with each directory's solver, time step and damping:
+    <m> equals the reference's printed value."""
     import json
     import os
     from oracle import pyoracle as po
     here = os.path.dirname(os.path.abspath(__file__))
     pins = json.load(open(os.path.join(here, "golden", "reference_pins.json")))
-    _write_case(tmp_path, pins["inputs"]["heisstripe"])
+    _write_case(tmp_path, pins["inputs"][case])
     lat, e0, par = inputs.load_system(str(tmp_path))
-    o = po.Oracle(lat, threads=1)
-    o.set_moments(e0)
-    o.setup_ziggurat(par["tseed"])
-    o.make_llg(par["sdealgh"], par["timestep"], par["damping"], par["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
-    for _ in range(1190):
-        o.sd_step()
-    mv, ma = o.mavg()
+    with po.units(po.ATOMIC_UNITS if str(par.get("aunits", "N")).upper() == "Y" else po.SI_UNITS):
+        o = po.Oracle(lat, threads=1)
+        o.set_moments(e0)
+        o.setup_ziggurat(par["tseed"])
+        o.make_llg(par["sdealgh"], par["timestep"], par["damping"], par["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
+        for _ in range(steps):
+            o.sd_step()
+        mv, ma = o.mavg()
     got = np.array(list(mv[0] / lat.natom) + [ma[0]])
-    pin = pins["heisstripe_iter1190"]
+    pin = pins[pin]
     exp = np.asarray(pin["expected"])
     printed = 0.5 * 10.0 ** (np.floor(np.log10(np.abs(exp) + 1e-300)) - 8)
     assert np.all(np.abs(got - exp) <= 1e-8 + printed), (got, exp)
