@@ -181,17 +181,27 @@ def _write_case(d, inp, extra=""):
             text += f"{word} ./{name}\n"
     if inp.get("aunits"):
         text += "aunits Y\n"
+    if "restart" in inp:   # rows |m|, m_x, m_y, m_z per atom, written in the standard layout
+        from uppasd_gb300 import output
+        r = np.asarray(inp["restart"], dtype=np.float64)
+        output.write_restart_std(str(d / "restart.in"), 0, r[None, :, 1:4], r[None, :, 0])
+        text += "restartfile ./restart.in\n"
+    if "ip_phases" in inp:
+        text += f"ip_mode S\nip_nphase {len(inp['ip_phases'])}\n" + "".join(
+            f"{int(n)} {t!r} {dt!r} {dmp!r}\n" for n, t, dt, dmp in inp["ip_phases"])
     _write(d, "inpsd.dat", text + extra)
 
 
 @pytest.mark.parametrize("case,steps,pin", [("heisstripe", 1190, "heisstripe_iter1190"),
-                                            ("scsurf", 800, "scsurf_iter800")])
+                                            ("scsurf", 800, "scsurf_iter800"),
+                                            ("heischain", 1000, "heischain_iter1000")])
 def test_pinned_case_through_the_reader(tmp_path, case, steps, pin):
     """Pinned regression cases end to end through the reader: the tables of tests/HeisStripe
-    (vacuum edges, anisotropy) and tests/SCsurf (atomic units, maptype 2, DM and
-    anisotropy) written as input directories, read by load_system (Initmag 1 drawn from the
-    default tseed), run on the oracle with each directory's solver, time step and damping:
-    <m> equals the reference's printed value."""
+    (vacuum edges, anisotropy), tests/SCsurf (atomic units, maptype 2, DM and anisotropy)
+    and tests/HeisChain (a restart-file start, Initmag 4, and an initial phase) written as
+    input directories, read by load_system (Initmag 1 drawn from the default tseed), run on
+    the oracle with each directory's phases, solver, time steps and damping: <m> equals the
+    reference's printed value."""
     import json
     import os
     from oracle import pyoracle as po
@@ -203,6 +213,11 @@ def test_pinned_case_through_the_reader(tmp_path, case, steps, pin):
         o = po.Oracle(lat, threads=1)
         o.set_moments(e0)
         o.setup_ziggurat(par["tseed"])
+        if str(par.get("ip_mode", "N")).upper() == "S":
+            for nstep, temp, dt, damping in par.get("ip_phases", []):
+                o.make_llg(par["sdealgh"], dt, damping, temp, 1.0, noise_mode=po.NOISE_ZIGGURAT)
+                for _ in range(int(nstep)):
+                    o.sd_step()
         o.make_llg(par["sdealgh"], par["timestep"], par["damping"], par["temp"], 1.0, noise_mode=po.NOISE_ZIGGURAT)
         for _ in range(steps):
             o.sd_step()
